@@ -1,0 +1,358 @@
+#!/usr/bin/env python
+"""Benchmark of the PBF substep: particle-substeps/s at 2^20 particles.
+
+Workload (default): the 1,048,576-particle sphere-drop scene — a jittered
+128x64x128 lattice (r = 0.0125, h = 4r) dropped onto a sphere (R = 0.4) in a
+3.3 x 2.6 x 3.3 box described by a 128^3 volume map; XSPH, vorticity
+confinement and Akinci surface tension on; 2 substeps of 1/120 s per step,
+4 solver iterations.  A "step" is one frame (2 substeps).
+
+  value  — device throughput, state resident in HBM, CUDA events on the
+           library's stream, max over ranks (N replicas for --gpus N).
+  e2e    — the same metric through the public C ABI as a host program uses
+           it: per step pbf_set_options (the 20-byte SimulationOptions from
+           host memory) + pbf_step + pbf_copy_field(POSITION) into a host
+           array (N * 16 bytes), wall clock.
+  roofline — the pass with the largest share of device time, its
+           algorithmic bytes per launch over its average launch duration.
+  cpu_baseline — the CPU restatement (oracle/) on a bounded sample.
+
+`--impl reference` times the reference method on the host cores (the CPU
+restatement: the reference itself is WGSL and has no CPU path) on the same
+workload, metric and unit.
+"""
+import argparse
+import ctypes
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+REPO = os.path.dirname(os.path.abspath(__file__))
+PKG = os.path.join(REPO, "webgpu-fluid-simulation_gb300")
+for _p in (REPO, PKG):
+    if _p not in sys.path:
+        sys.path.insert(0, _p)
+
+METRIC = "particle-substeps/s @1M PBF, learned vs plain at equal max density err ≤1%"
+UNIT = "particle-substeps/s"
+PEAKS_PATH = os.path.join(REPO, "MEASURED_PEAKS.json")
+FALLBACK_HBM_GBS = 6800.0
+
+# Algorithmic bytes per particle of each pass (SoA float4 = 16 B, u32 = 4 B),
+# each field read or written once; neighbour gathers are cache-served.
+ALG_BYTES = {
+    "predict": 68,            # read x, v, a; write x*, key (+ rank)
+    "sort": 32,               # key, rank, id -> perm_raw, id_raw; cell fix -> perm
+    "gather": 76,             # perm -> pos, x*, id in the new order
+    "nbr_count": 20,          # read x*, write count
+    "nbr_scan": 8,
+    "nbr_list": 20,           # read x*, offset (+ 4 B per neighbour written, counted separately)
+    "lambda": 20,             # read x*, write lambda
+    "deltap_apply": 36,       # read x*, lambda; write x*
+    "density_velocity": 64,   # read x*, x; write v, (x, rho)
+    "vorticity": 64,          # read x, v; write omega, n
+    "xsph": 80,               # read x, v, omega, n; write a
+    "export": 36,             # id, (x, rho) -> by-id buffer
+}
+
+
+def parse_args():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--workload", default="sphere_drop_1m", choices=["sphere_drop_1m", "dam_break_16k"])
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--graph", action="store_true", help="replay the frame as a CUDA graph")
+    return ap.parse_args()
+
+
+# ---- distributed plumbing (N independent replicas) ----------------------------------------
+class Dist:
+    def __init__(self, gpus):
+        self.world = int(os.environ.get("WORLD_SIZE", "1"))
+        self.rank = int(os.environ.get("RANK", "0"))
+        self.local = int(os.environ.get("LOCAL_RANK", "0"))
+        self.pg = None
+        if self.world > 1:
+            import torch
+            import torch.distributed as dist
+            backend = "nccl" if torch.cuda.is_available() else "gloo"
+            if backend == "nccl":
+                torch.cuda.set_device(self.local)
+            dist.init_process_group(backend=backend)
+            self.pg = dist
+
+    def barrier(self):
+        if self.pg:
+            self.pg.barrier()
+
+    def max(self, v):
+        if not self.pg:
+            return v
+        import torch
+        t = torch.tensor([float(v)], dtype=torch.float64,
+                         device="cuda" if torch.cuda.is_available() else "cpu")
+        self.pg.all_reduce(t, op=self.pg.ReduceOp.MAX)
+        return float(t.item())
+
+    def close(self):
+        if self.pg:
+            self.pg.destroy_process_group()
+
+
+# ---- clocks --------------------------------------------------------------------------------
+class ClockSampler:
+    QUERY = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+             "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+             "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index):
+        self.idx = gpu_index
+        self.proc = None
+        self.lines = []
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "--query-gpu=" + self.QUERY, "--format=csv,noheader,nounits",
+                                          "-i", str(self.idx), "-lms", "200"], stdout=subprocess.PIPE,
+                                         stderr=subprocess.DEVNULL, text=True)
+        except Exception:
+            self.proc = None
+            return
+        self.t = threading.Thread(target=self._read, daemon=True)
+        self.t.start()
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def stop(self):
+        if not self.proc:
+            return None
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except Exception:
+            self.proc.kill()
+        sm, smax, reasons = [], None, set()
+        for ln in self.lines:
+            f = [x.strip() for x in ln.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                sm.append(float(f[1]))
+                smax = float(f[2])
+            except ValueError:
+                continue
+            names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+            for nm, val in zip(names, f[5:9]):
+                if val.lower() == "active":
+                    reasons.add(nm)
+        if not sm:
+            return None
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": smax, "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+# ---- workload ------------------------------------------------------------------------------
+def build_workload(name, field_backend="gpu"):
+    from pbf_gb300 import scenes
+    if name == "sphere_drop_1m":
+        spec = scenes.sphere_drop_spec()
+        desc = ("sphere_drop_1m: 1,048,576 particles (128x64x128 lattice, r=0.0125, h=0.05, jitter 0.1r) "
+                "dropped on a R=0.4 sphere in a 3.3x2.6x3.3 box, 128^3 cubic volume map, 2 substeps x 1/120 s, "
+                "4 iterations, XSPH 0.01, vorticity 5e-4, surface tension 0.1")
+    else:
+        spec = scenes.dam_break_16k_spec()
+        desc = ("dam_break_16k: 16,384 particles (32x16x32 lattice, r=0.025, h=0.1) in a 3.2x1.0x1.6 box, "
+                "64^3 volume map, 2 substeps x 1/120 s, 4 iterations")
+    sc = scenes.build_scene(spec, quadrature=12, backend=field_backend, name=name)
+    return sc, desc
+
+
+def peaks():
+    try:
+        with open(PEAKS_PATH) as f:
+            d = json.load(f)
+        return float(d["hbm_gbs"]), "measured"
+    except Exception:
+        return FALLBACK_HBM_GBS, "fallback"
+
+
+# ---- CPU restatement timing ----------------------------------------------------------------
+def cpu_sample(sc, particles_max, substeps):
+    """Time the CPU restatement on the first `particles_max` lattice particles."""
+    from oracle import oracle as O
+    pts = sc.particles[:particles_max]
+    o = O.Oracle(sc.config, 32)
+    o.set_particles(pts)
+    f = sc.field
+    o.set_field(f["res"], f["origin"], f["extent"], f["sdf"], f["vol"])
+    t0 = time.perf_counter()
+    o.substep(substeps)
+    dt = time.perf_counter() - t0
+    o.close()
+    return len(pts) * substeps / dt, dt, len(pts), O.threads()
+
+
+def reference_arm(args, dist):
+    if dist.rank != 0:
+        return
+    sc, desc = build_workload(args.workload, field_backend=_cpu_field_backend())
+    sub = sc.config.substeps
+    sample = min(sc.n, 262144)
+    # warm-up (untimed) and timed steps, each one frame of the sample
+    from oracle import oracle as O
+    o = O.Oracle(sc.config, 32)
+    o.set_particles(sc.particles[:sample])
+    f = sc.field
+    o.set_field(f["res"], f["origin"], f["extent"], f["sdf"], f["vol"])
+    o.substep(sub * max(args.warmup, 0))
+    t0 = time.perf_counter()
+    o.substep(sub * args.steps)
+    dt = time.perf_counter() - t0
+    value = sample * sub * args.steps / dt
+    cores = O.threads()
+    line = {
+        "impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1000.0 * dt / args.steps,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+        "config": {"workload": desc, "sample": "first %d particles of the lattice" % sample},
+        "cpu_baseline": {"value": value, "unit": UNIT, "cores": cores, "kind": "port",
+                         "sample": "%d particles x %d substeps per step (CPU restatement, OpenMP)" % (sample, sub)},
+        "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+        "note": "the reference is TypeScript+WGSL with no CPU path and no WebGPU runtime here; "
+                "its method runs as the project's CPU restatement",
+    }
+    print(json.dumps(line), flush=True)
+
+
+def _cpu_field_backend():
+    from oracle import oracle as O
+    return O.generate_volume_map_backend()
+
+
+# ---- the GPU arm ---------------------------------------------------------------------------
+def gpu_arm(args, dist):
+    import torch
+    from pbf_gb300 import PBF
+    from pbf_gb300 import _lib as L
+
+    torch.cuda.set_device(dist.local if dist.world > 1 else 0)
+    sc, desc = build_workload(args.workload)
+    cfg = sc.config
+    sim = PBF(cfg)
+    sim.set_particles(sc.particles)
+    f = sc.field
+    sim.set_boundary_field(f["res"], f["origin"], f["extent"], f["sdf"], f["vol"])
+    if args.graph:
+        sim.enable_graph(True)
+    n = sc.n
+    sub = cfg.substeps
+    iters = cfg.options.iterations
+    for _ in range(max(args.warmup, 3)):
+        sim.step(1)
+    sim.synchronize()
+
+    stream = torch.cuda.ExternalStream(sim.stream)
+    ev0 = torch.cuda.Event(enable_timing=True)
+    ev1 = torch.cuda.Event(enable_timing=True)
+    sim.set_kernel_timing(not args.graph)
+    sim.kernel_timing()  # clear
+    clocks = ClockSampler(dist.local)
+    clocks.start()
+    dist.barrier()
+    torch.cuda.synchronize()
+    ev0.record(stream)
+    for _ in range(args.steps):
+        sim.step(1)
+    ev1.record(stream)
+    ev1.synchronize()
+    torch.cuda.synchronize()
+    dist.barrier()
+    clk = clocks.stop()
+    ms = ev0.elapsed_time(ev1)
+    kt = sim.kernel_timing() if not args.graph else {}
+    sim.set_kernel_timing(False)
+    m = sim.metrics()
+    ms_max = dist.max(ms)
+    value = dist.world * n * sub * args.steps / (ms_max / 1000.0)
+
+    # end to end through the C ABI with host buffers
+    host = np.zeros((n, 4), np.float32)
+    opts = L.Options()
+    lib = L.load()
+    lib.pbf_get_options(sim._h, ctypes.byref(opts))
+    sim.synchronize()
+    dist.barrier()
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        lib.pbf_set_options(sim._h, ctypes.byref(opts))
+        sim.step(1)
+        lib.pbf_copy_field(sim._h, L.FIELD_POSITION, host.ctypes.data_as(ctypes.c_void_p), host.nbytes)
+    e2e_s = time.perf_counter() - t0
+    e2e_s = dist.max(e2e_s)
+    e2e = {"value": dist.world * n * sub * args.steps / e2e_s, "unit": UNIT,
+           "h2d_bytes_per_step": ctypes.sizeof(L.Options), "d2h_bytes_per_step": int(host.nbytes)}
+
+    # roofline of the dominant pass
+    roof = None
+    peak, peak_kind = peaks()
+    if kt:
+        dom = max(kt.items(), key=lambda kv: kv[1][1])
+        name, (launches, tot_ms) = dom
+        per_launch_s = tot_ms / launches / 1000.0
+        bytes_launch = ALG_BYTES.get(name, 0) * n
+        achieved = bytes_launch / per_launch_s / 1e9
+        total_ms = sum(v[1] for v in kt.values())
+        roof = {"bound": "hbm", "kernel": name, "achieved": achieved, "peak": peak, "unit": "GB/s",
+                "frac": achieved / peak, "peak_kind": peak_kind, "traffic": None,
+                "alg_bytes_per_launch": bytes_launch, "avg_launch_ms": per_launch_s * 1000.0,
+                "share": tot_ms / total_ms if total_ms else None,
+                "passes": {k: {"launches": v[0], "ms": round(v[1], 4),
+                               "share": round(v[1] / total_ms, 4) if total_ms else None} for k, v in kt.items()}}
+    launches_per_frame = sub * (12 + 2 * iters) + 1
+    line = {
+        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": dist.world, "steps": args.steps,
+        "warmup": max(args.warmup, 3), "ms_per_step": ms_max / args.steps, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+        "config": {"workload": desc, "path": "plain 4-iteration solve",
+                   "graph": bool(args.graph), "parallelism": "replicas x%d" % dist.world,
+                   "l2": "state + neighbour lists ~0.4 GB per replica, larger than the 129 MB L2"},
+        "e2e": e2e, "gpu_launches": launches_per_frame * args.steps,
+        "roofline": roof, "clocks": clk,
+        "state_metrics": {"max_compression": m["max_compression"], "mean_abs_density_err": m["mean_abs_density_err"],
+                          "nonfinite": m["nonfinite"], "neighbors_per_particle": m["neighbor_total"] / max(n, 1)},
+    }
+    sim.close()
+    if dist.rank == 0 and dist.world == 1 and not args.no_cpu_baseline:
+        v, secs, cnt, cores = cpu_sample(sc, 262144, sub)
+        line["cpu_baseline"] = {"value": v, "unit": UNIT, "cores": cores, "kind": "port",
+                                "sample": "first %d lattice particles x %d substeps (%.1f s), CPU restatement"
+                                          % (cnt, sub, secs)}
+    if dist.rank == 0:
+        print(json.dumps(line), flush=True)
+
+
+def main():
+    args = parse_args()
+    dist = Dist(args.gpus)
+    try:
+        if args.impl == "reference":
+            reference_arm(args, dist)
+        else:
+            gpu_arm(args, dist)
+    finally:
+        dist.close()
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,291 @@
+/*
+ * pbf_gb300.h — C ABI of the GB300-native Position Based Fluids substep.
+ *
+ * This is the drop-in boundary for the simulator of WebGPU-Fluid-Simulation
+ * (TypeScript + WGSL).  Every entry point below names the reference member it
+ * replaces (paths are relative to the reference project root).  A TypeScript
+ * host binds these through the N-API addon in the package's napi/ folder; the
+ * Python tests bind them through ctypes.
+ *
+ * Conventions
+ *  - Every call returns a pbf_status (0 = ok).  The reference throws
+ *    synchronous JS errors for the same conditions
+ *    (src/simulator/PBF/PBFConfig.ts:50-55, src/simulator/boundary/volumeMap.ts:31-33,
+ *    src/simulator/neighbor/exclusiveScan.ts:38-41); here the call fails and
+ *    pbf_last_error() holds the message.
+ *  - One handle owns one CUDA stream and all device buffers.  Device pointers
+ *    handed out stay valid until pbf_reset / pbf_destroy.  Calls on one handle
+ *    are not thread-safe.  Step calls are asynchronous until a copy or
+ *    pbf_synchronize.
+ *  - Particle arrays crossing the boundary are float4 per particle
+ *    (x, y, z, w), indexed by particle id, exactly like the reference's
+ *    `position` GPU buffer (src/simulator/SPH.ts:39, w = density written by
+ *    src/simulator/PBF/shader/attributeUpdate.ts:56).
+ */
+#ifndef PBF_GB300_H
+#define PBF_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define PBF_ABI_VERSION 1
+
+typedef enum pbf_status {
+  PBF_OK = 0,
+  PBF_EINVAL = 1,     /* bad argument or length */
+  PBF_ECAPACITY = 2,  /* too many particles / neighbour list overflow */
+  PBF_EFORMAT = 3,    /* malformed .cdm boundary text */
+  PBF_ECUDA = 4,      /* CUDA runtime error */
+  PBF_ETIMEOUT = 5,   /* a bounded device wait gave up (scan look-back) */
+  PBF_EDIVERGED = 6,  /* NaN/Inf found in the particle state */
+  PBF_ESTATE = 7      /* call not valid in the current state */
+} pbf_status;
+
+typedef enum pbf_jitter_mode {
+  PBF_JITTER_HASH = 0, /* integer hash of the float bits: bit-identical on every platform */
+  PBF_JITTER_SIN = 1   /* fract(sin(dot(p, (12.9898, 78.233))) * 43758.5453), common.ts:51-59 */
+} pbf_jitter_mode;
+
+typedef enum pbf_fp_mode {
+  PBF_FP_FAST = 0,     /* FMA contraction allowed (production) */
+  PBF_FP_EXACT = 1     /* no contraction: bit-identical with the CPU restatement */
+} pbf_fp_mode;
+
+typedef enum pbf_boundary_interp {
+  PBF_INTERP_CUBIC = 0,     /* 32-node cubic serendipity cell, discreteFieldShader.ts:15-192 */
+  PBF_INTERP_TRILINEAR = 1  /* trilinear over the corner nodes only (fast mode) */
+} pbf_boundary_interp;
+
+/* Runtime options: SimulationOptions (src/common/shader.ts:50-58) plus the
+ * iteration count, set by PBFConfig.setConfig (src/simulator/PBF/PBFConfig.ts:31-46)
+ * with the GUI defaults of src/common/config.ts:22-28. */
+typedef struct pbf_options {
+  uint32_t iterations;      /* constrainIterationCount (default 5) */
+  float xsph;               /* XSPHCoef (0.01) */
+  float vorticity;          /* vorticityCoef (0.1) */
+  float surface_tension;    /* tensionCoef (0.5) */
+  float gravity;            /* g; the step applies (0, -g, 0) (9.8) */
+} pbf_options;
+
+/* Static configuration.  The reference bakes these into WGSL constants and
+ * pipeline override constants (src/simulator/SPH.ts:24-27,49-50,
+ * src/simulator/PBF/PBFConfig.ts:8,21, src/simulator/neighbor/neighborSearch.ts:9-14).
+ * pbf_config_default() fills the reference's values. */
+typedef struct pbf_config {
+  uint32_t struct_size;     /* sizeof(pbf_config) */
+  uint32_t max_particles;   /* capacity (reference: 1 << 18 - 1 == 131072) */
+  float particle_radius;    /* r (0.006) */
+  float kernel_radius;      /* h (0.025) */
+  float rest_density;       /* rho0 (1000) */
+  float time_step;          /* dt of one substep (1/300) */
+  uint32_t substeps;        /* stepCount: substeps per pbf_step frame (1) */
+  float domain_min[3];      /* simulation box (0,0,0) */
+  float domain_max[3];      /* (1,1,1) */
+  uint32_t grid_dim[3];     /* hash-grid cells per axis; 0 = ceil(extent / h) (40) */
+  float lambda_eps;         /* lambdaEPS (1e-6) */
+  float wall_jitter;        /* EPS of boundary_rand (1e-4) */
+  uint32_t jitter_mode;     /* pbf_jitter_mode */
+  uint32_t volume_quirk;    /* 1 = read the volume-map nodes exactly as the reference
+                               does (discreteFieldShader.ts:146-147,152-153) */
+  uint32_t fp_mode;         /* pbf_fp_mode */
+  uint32_t boundary_interp; /* pbf_boundary_interp */
+  uint32_t max_neighbors;   /* mean neighbour-list capacity per particle (60) */
+  pbf_options options;
+  void* stream;             /* cudaStream_t to run on, or NULL for a library-owned stream */
+} pbf_config;
+
+/* Per-particle fields readable with pbf_copy_field (all indexed by particle id). */
+typedef enum pbf_field {
+  PBF_FIELD_POSITION = 0,     /* float4 (x, rho)   — SPH.position */
+  PBF_FIELD_VELOCITY = 1,     /* float4 (v, 0)     — SPH.velocity */
+  PBF_FIELD_ACCELERATION = 2, /* float4 (a, 0)     — SPH.acceleration */
+  PBF_FIELD_PREDICTED = 3,    /* float4 (x*, 0)    — PBF.position2 before the non-pressure passes */
+  PBF_FIELD_LAMBDA = 4,       /* float             — PBF.lambda (last iteration) */
+  PBF_FIELD_BOUNDARY = 5,     /* float4 (x_b, V_b) — PBF.boundaryData (last iteration) */
+  PBF_FIELD_OMEGA = 6,        /* float4 (w, |w|)   — PBF.angularVelocity */
+  PBF_FIELD_NORMAL = 7,       /* float4 (n, 0)     — PBF.normal */
+  PBF_FIELD_DELTA_P = 8,      /* float4 (dp, 0)    — PBF.deltaPosition of the last iteration
+                                 (kept only when capture is enabled) */
+  PBF_FIELD_NEIGHBOR_COUNT = 9/* uint32 per particle — NeighborSearch.neighborCount */
+} pbf_field;
+
+typedef struct pbf_metrics {
+  uint32_t particles;
+  uint32_t nonfinite;        /* particles with a NaN/Inf in x or v */
+  uint32_t penetrations;     /* particles whose boundary SDF is < 0 */
+  uint32_t error_flags;      /* device error word (see PBF_DEVERR_*) */
+  float max_compression;     /* max_i max(0, rho_i/rho0 - 1) */
+  float mean_abs_density_err;/* mean_i |rho_i/rho0 - 1| */
+  float max_abs_density_err; /* max_i |rho_i/rho0 - 1| */
+  float kinetic_energy;      /* 0.5 m sum |v|^2 */
+  uint32_t neighbor_total;   /* neighbour-list entries of the last substep */
+  uint32_t fallback_steps;   /* learned-start substeps that fell back to the plain solve */
+} pbf_metrics;
+
+#define PBF_DEVERR_NEIGHBOR_OVERFLOW 0x1u
+#define PBF_DEVERR_SCAN_TIMEOUT 0x2u
+#define PBF_DEVERR_CELL_OVERFLOW 0x4u
+
+typedef struct pbf_handle pbf_handle;
+
+/* ---- life cycle: PBF constructor + initResource (src/simulator/PBF/PBF.ts:67-69,262-279) */
+int pbf_config_default(pbf_config* cfg);
+int pbf_create(const pbf_config* cfg, pbf_handle** out);
+int pbf_destroy(pbf_handle* h);
+/* PBF.reset (PBF.ts:71-89): clears all particle buffers, the particle array and the boundary. */
+int pbf_reset(pbf_handle* h);
+const char* pbf_last_error(const pbf_handle* h);
+int pbf_abi_version(void);
+
+/* ---- options: PBFConfig.setConfig / optionsChange (PBFConfig.ts:31-46,64-66) */
+int pbf_set_options(pbf_handle* h, const pbf_options* opt);
+int pbf_get_options(const pbf_handle* h, pbf_options* opt);
+
+/* ---- scene seeding: SPH.voxelizeCube / voxelizeSphere (src/simulator/SPH.ts:99-149).
+ * They append lattice points (spacing 2r) to the host particle array and
+ * return how many were added; pbf_set_particle_position uploads the array
+ * (PBFConfig.setParticlePosition, PBFConfig.ts:48-62). */
+int pbf_voxelize_cube(pbf_handle* h, const float mn[3], const float mx[3], uint32_t* added);
+int pbf_voxelize_sphere(pbf_handle* h, const float center[3], float radius, uint32_t* added);
+/* Seeded uniform jitter in [-amplitude, amplitude] on the host array (splitmix64). */
+int pbf_jitter_particles(pbf_handle* h, float amplitude, uint64_t seed);
+int pbf_host_particle_count(const pbf_handle* h, uint32_t* count);
+int pbf_copy_host_particles(const pbf_handle* h, float* xyzw, uint32_t n);
+int pbf_set_particle_position(pbf_handle* h);
+/* Direct upload of n float4 positions (w ignored); velocities/accelerations are zeroed. */
+int pbf_set_particles(pbf_handle* h, const float* xyzw, uint32_t n);
+/* Optional: overwrite velocities (float4 per particle, by id). */
+int pbf_set_velocities(pbf_handle* h, const float* xyzw, uint32_t n);
+
+/* ---- boundary: PBF.setBoundaryData -> BoundaryModel.setData (PBF.ts:91-94, volumeMap.ts:23-39).
+ * `text` is the .cdm file: "nx ny nz\n<len>\n<sdf floats>\n<len>\n<volume floats>".
+ * The field covers the simulation domain. */
+int pbf_set_boundary_data(pbf_handle* h, const char* text, size_t len);
+/* The same, from arrays in the .cdm node layout; origin/extent give the box the field covers. */
+int pbf_set_boundary_field(pbf_handle* h, const uint32_t res[3], const float origin[3],
+                           const float extent[3], const float* sdf, const float* volume,
+                           size_t nodes);
+int pbf_clear_boundary(pbf_handle* h);
+/* Number of floats per field for a resolution (BoundaryModel.FIELD_LENGTH, volumeMap.ts:7-11). */
+size_t pbf_field_length(const uint32_t res[3]);
+
+/* ---- volume-map generation (Bender et al. 2019 volume maps in the .cdm node layout).
+ * The reference ships precomputed maps (public/model/torus.cdm,
+ * domain_boundary.cdm); this builds maps for analytic shapes on the GPU in
+ * FP64.  The SDF is the minimum over the shapes (positive on the fluid side);
+ * the volume at a node x is
+ *   V(x) = 0.8 * integral over |y| <= h of gamma(x + y) dy,
+ *   gamma = 1 where SDF <= 0, C(SDF/h) for 0 < SDF < h (C = cubic spline,
+ *   C(0) = 1), 0 beyond,
+ * integrated with an n^3 Gauss-Legendre rule over [-h, h]^3. */
+typedef enum pbf_shape_kind {
+  PBF_SHAPE_BOX_CONTAINER = 0, /* fluid inside the box center +- size; solid outside */
+  PBF_SHAPE_SPHERE = 1,        /* solid sphere, radius size[0] */
+  PBF_SHAPE_CYLINDER = 2,      /* solid cylinder along y: radius size[0], half height size[1] */
+  PBF_SHAPE_TORUS = 3,         /* solid torus around the y axis: radii size[0] (major), size[1] (minor) */
+  PBF_SHAPE_BOX_SOLID = 4      /* solid box, half extents size */
+} pbf_shape_kind;
+typedef struct pbf_shape {
+  uint32_t kind;
+  float center[3];
+  float size[3];
+} pbf_shape;
+/* Treat points outside the field's box as empty when integrating the volume
+ * (the convention the reference's domain_boundary.cdm was built with). */
+#define PBF_VOLMAP_OUTSIDE_EMPTY 0x1u
+/* Evaluate gamma through the map's own cubic interpolation of the node SDF
+ * (instead of the analytic SDF), as the reference's assets were built. */
+#define PBF_VOLMAP_DISCRETE_SDF 0x2u
+/* sdf_out / vol_out are host arrays of pbf_field_length(res) floats. */
+int pbf_generate_volume_map(const pbf_shape* shapes, uint32_t count, const uint32_t res[3],
+                            const float origin[3], const float extent[3], float support_radius,
+                            uint32_t quadrature, uint32_t flags, float* sdf_out, float* vol_out);
+
+/* Volumes for a given node SDF (e.g. of a triangle mesh), integrated through
+ * the map's own cubic interpolation; vol_out has pbf_field_length(res) floats. */
+int pbf_volume_from_sdf(const uint32_t res[3], const float origin[3], const float extent[3],
+                        float support_radius, uint32_t quadrature, uint32_t flags, const float* sdf,
+                        float* vol_out);
+
+/* ---- stepping: PBF.run (PBF.ts:398-448) is one substep; the controller
+ * calls it stepCount times per frame (src/controller.ts:375-376). */
+int pbf_run(pbf_handle* h);
+int pbf_step(pbf_handle* h, uint32_t frames);
+/* PBF.runTimestamp (PBF.ts:450-510): one substep split into the four
+ * reference intervals [integrate | neighbour search | constraint loop | non-pressure],
+ * returned in milliseconds (CUDA events on the handle's stream). */
+int pbf_run_timestamp(pbf_handle* h, float ms[4]);
+int pbf_synchronize(pbf_handle* h);
+/* SPH.pause / switch / start / stop (SPH.ts:82-84): a paused handle's pbf_run is a no-op. */
+int pbf_set_paused(pbf_handle* h, int paused);
+int pbf_is_paused(const pbf_handle* h);
+
+/* Capture the whole frame (substeps x passes) in a CUDA graph and replay it. */
+int pbf_enable_graph(pbf_handle* h, int enable);
+
+/* Per-kernel device timing: when enabled, every launch of pbf_run / pbf_step
+ * is bracketed by CUDA events on the handle's stream (graphs are bypassed).
+ * pbf_get_kernel_timing synchronises, sums the durations per pass name and
+ * clears the record. */
+typedef struct pbf_kernel_time {
+  char name[32];
+  uint32_t launches;
+  float total_ms;
+} pbf_kernel_time;
+int pbf_set_kernel_timing(pbf_handle* h, int enable);
+int pbf_get_kernel_timing(pbf_handle* h, pbf_kernel_time* out, uint32_t max, uint32_t* count);
+
+/* ---- state access */
+uint32_t pbf_particle_count(const pbf_handle* h);
+/* Device float4 (x, rho) per particle id, valid after each run/step — the
+ * buffer the renderer binds (paricleRasterizer.ts:74-77). */
+const float* pbf_position_device(pbf_handle* h);
+const float* pbf_velocity_device(pbf_handle* h);
+int pbf_copy_field(pbf_handle* h, int field, void* host, size_t bytes);
+int pbf_get_metrics(pbf_handle* h, pbf_metrics* out);
+/* Keep per-iteration debug fields (PBF_FIELD_DELTA_P); off by default. */
+int pbf_set_capture(pbf_handle* h, int enable);
+void* pbf_stream(pbf_handle* h);
+
+/* ---- neighbour search alone: NeighborSearch.execute (src/simulator/neighbor/neighborSearch.ts:270-301).
+ * All pointers are device pointers.  Inputs: n float4 positions.  Outputs
+ * (each may be NULL to skip): per-particle cell key (ParticleInsert),
+ * per-cell count (cellParticleCount), per-cell exclusive offset
+ * (cellOffset, cells+1 entries), the sorted order slot -> particle id
+ * (particleSortIndexCopy), per-particle rank within its cell
+ * (particleSortIndex), stable by particle id. */
+typedef struct pbf_grid {
+  float origin[3];
+  float inv_cell[3];        /* cells per unit length per axis */
+  uint32_t dim[3];
+} pbf_grid;
+typedef struct pbf_ns pbf_ns;
+int pbf_ns_create(const pbf_grid* grid, uint32_t max_particles, void* stream, pbf_ns** out);
+int pbf_ns_destroy(pbf_ns* ns);
+int pbf_ns_run(pbf_ns* ns, const float* d_pos4, uint32_t n, uint32_t* d_keys,
+               uint32_t* d_cell_count, uint32_t* d_cell_offset, uint32_t* d_order,
+               uint32_t* d_rank);
+/* Neighbour lists in the reference layout (NeighborCount + particle scan +
+ * NeighborList, neighborShader.ts:101-246): d_nbr_offset has n+1 entries and
+ * d_nbr_list holds particle ids.  Call after pbf_ns_run with the same positions.
+ * Fails with PBF_ECAPACITY (writing nothing past capacity) if the lists need
+ * more than `capacity` entries; *total receives the needed size. */
+int pbf_ns_lists(pbf_ns* ns, const float* d_pos4, uint32_t n, float radius,
+                 uint32_t* d_nbr_offset, uint32_t* d_nbr_list, uint32_t capacity,
+                 uint32_t* total);
+int pbf_ns_sync(pbf_ns* ns);
+const char* pbf_ns_last_error(const pbf_ns* ns);
+
+/* ---- exclusive scan (ExclusiveScan.execute, exclusiveScan.ts:134-166):
+ * single-pass decoupled look-back over any length (no 512-multiple or
+ * 262144 limit).  Scratch is owned by the call's context. */
+int pbf_exclusive_scan_u32(const uint32_t* d_in, uint32_t* d_out, size_t n, void* stream);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* PBF_GB300_H */

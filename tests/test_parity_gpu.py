@@ -1,0 +1,320 @@
+"""GPU parity: the CUDA path (through the C ABI) against the CPU restatement.
+
+Bars:
+  - integer work (cell keys, counts, scan offsets, sorted order, ranks,
+    neighbour lists): bit-exact;
+  - float passes in PBF_FP_EXACT mode: bit-exact with the FP32 restatement,
+    every field, one and several substeps;
+  - float passes in PBF_FP_FAST mode (FMA contraction): per field, the
+    distance to the FP64 replica is at most 2x the FP32 restatement's own
+    distance to it plus 1e-5 of the field's scale, and the distance to the
+    FP32 restatement is within 1e-5 of the scale for the well-conditioned
+    fields (x, rho, n, a).
+"""
+import ctypes
+
+import numpy as np
+import pytest
+
+from oracle import oracle as O
+from pbf_gb300 import PBF, NeighborSearch, exclusive_scan, scenes
+from pbf_gb300 import _lib as L
+
+torch = pytest.importorskip("torch")
+pytestmark = pytest.mark.gpu
+
+FIELDS = [(L.FIELD_POSITION, "position"), (L.FIELD_VELOCITY, "velocity"), (L.FIELD_ACCELERATION, "acceleration"),
+          (L.FIELD_LAMBDA, "lambda"), (L.FIELD_BOUNDARY, "boundary"), (L.FIELD_OMEGA, "omega"),
+          (L.FIELD_NORMAL, "normal"), (L.FIELD_DELTA_P, "delta_p"), (L.FIELD_NEIGHBOR_COUNT, "nbr_count")]
+
+
+def dev(a):
+    return torch.from_numpy(np.ascontiguousarray(a)).cuda()
+
+
+# ---- scan -------------------------------------------------------------------------------
+@pytest.mark.parametrize("n", [1, 7, 2047, 2048, 2049, 262144, 262145, 2097153, 16777217])
+def test_exclusive_scan(n):
+    rng = np.random.default_rng(n)
+    x = rng.integers(0, 40, size=n, dtype=np.uint32)
+    d_in = dev(x.view(np.int32))
+    d_out = torch.empty_like(d_in)
+    exclusive_scan(d_in.data_ptr(), d_out.data_ptr(), n)
+    torch.cuda.synchronize()
+    got = d_out.cpu().numpy().view(np.uint32)
+    assert np.array_equal(got, O.exclusive_scan(x))
+
+
+# ---- neighbour search ---------------------------------------------------------------------
+def run_ns(cfg, pts, lists=False):
+    n = pts.shape[0]
+    dims, cells = O.grid_dims(cfg)
+    g = cfg
+    inv = [float(np.float32(float(dims[a]) / (g.domain_max[a] - g.domain_min[a]))) for a in range(3)]
+    ns = NeighborSearch(list(g.domain_min), inv, list(dims), max(n, 1))
+    d_pos = dev(pts)
+    keys = torch.empty(n, dtype=torch.int32, device="cuda")
+    cc = torch.empty(cells, dtype=torch.int32, device="cuda")
+    co = torch.empty(cells + 1, dtype=torch.int32, device="cuda")
+    order = torch.empty(n, dtype=torch.int32, device="cuda")
+    rank = torch.empty(n, dtype=torch.int32, device="cuda")
+    ns.run(d_pos.data_ptr(), n, keys.data_ptr(), cc.data_ptr(), co.data_ptr(), order.data_ptr(), rank.data_ptr())
+    ns.sync()
+    out = dict(keys=keys, cell_count=cc, cell_offset=co, order=order, rank=rank)
+    out = {k: v.cpu().numpy().view(np.uint32) for k, v in out.items()}
+    if lists:
+        off = torch.empty(n + 1, dtype=torch.int32, device="cuda")
+        cap = 80 * n
+        lst = torch.empty(cap, dtype=torch.int32, device="cuda")
+        rc, tot = ns.lists(d_pos.data_ptr(), n, g.kernel_radius, off.data_ptr(), lst.data_ptr(), cap)
+        assert rc == 0
+        ns.sync()
+        out["nbr_offset"] = off.cpu().numpy().view(np.uint32)
+        out["nbr_list"] = lst[:tot].cpu().numpy().view(np.uint32)
+    ns.close()
+    return out
+
+
+@pytest.mark.parametrize("dist,n", [("uniform", 200000), ("clumps", 200000), ("uniform", 1 << 20),
+                                    ("clumps", 1 << 20)])
+def test_neighbor_search_bitexact(dist, n):
+    cfg, pts = scenes.neighbor_case(n, dist, seed=11, dim=128)
+    ref = O.neighbor_search(cfg, pts)
+    got = run_ns(cfg, pts)
+    for k in ("keys", "cell_count", "cell_offset", "order", "rank"):
+        assert np.array_equal(got[k], ref[k]), k
+
+
+def test_neighbor_search_full_cells():
+    """Cells past the warp paths (33..1024 by counting, >1024 by block radix)."""
+    rng = np.random.default_rng(5)
+    blobs = [(0.5, 0.5, 0.5, 5000), (0.1, 0.2, 0.3, 700), (0.8, 0.8, 0.1, 33), (0.3, 0.9, 0.6, 31)]
+    parts = []
+    for x, y, z, m in blobs:
+        p = np.zeros((m, 4), np.float32)
+        p[:, :3] = np.array([x, y, z], np.float32) + rng.uniform(0, 0.9 / 128, size=(m, 3)).astype(np.float32)
+        parts.append(p)
+    pts = np.concatenate(parts)
+    pts = pts[rng.permutation(len(pts))]
+    cfg = scenes.base_config(kernel_radius=1.0 / 128, grid_dim=(128, 128, 128), max_particles=len(pts))
+    ref = O.neighbor_search(cfg, pts)
+    assert ref["cell_count"].max() >= 5000
+    got = run_ns(cfg, pts)
+    for k in ("keys", "cell_count", "cell_offset", "order", "rank"):
+        assert np.array_equal(got[k], ref[k]), k
+
+
+def test_neighbor_lists_bitexact():
+    sc = scenes.reference_scene("cube_drop")
+    pts = scenes.jitter(sc.particles, 0.002, seed=3)
+    ref = O.neighbor_search(sc.config, pts, lists=True)
+    got = run_ns(sc.config, pts, lists=True)
+    assert np.array_equal(got["nbr_offset"], ref["nbr_offset"])
+    assert np.array_equal(got["nbr_list"], ref["nbr_list"])
+
+
+# ---- the substep ---------------------------------------------------------------------------
+def make_pair(sc, fp_mode, pts=None, precision=32):
+    cfg = scenes.copy_config(sc.config)
+    cfg.fp_mode = fp_mode
+    sim = PBF(cfg)
+    sim.set_capture(True)
+    orc = O.Oracle(cfg, precision)
+    p = sc.particles if pts is None else pts
+    sim.set_particles(p)
+    orc.set_particles(p)
+    if sc.field is not None:
+        f = sc.field
+        sim.set_boundary_field(f["res"], f["origin"], f["extent"], f["sdf"], f["vol"])
+        orc.set_field(f["res"], f["origin"], f["extent"], f["sdf"], f["vol"])
+    return sim, orc
+
+
+def fields_of(sim):
+    return {name: sim.copy_field(f) for f, name in FIELDS}
+
+
+def oracle_fields(orc):
+    out = {}
+    for f, name in FIELDS:
+        v = orc.field(f)
+        out[name] = v.astype(np.uint32) if f == L.FIELD_NEIGHBOR_COUNT else v.astype(np.float32)
+    return out
+
+
+SCENES = ["cube_small", "boundary_small", "water_droplet"]
+
+
+@pytest.mark.parametrize("name", SCENES)
+@pytest.mark.parametrize("substeps", [1, 4])
+def test_step_exact_mode_bitexact(name, substeps):
+    sc = scenes.reference_scene(name)
+    pts = scenes.jitter(sc.particles, 0.001, seed=substeps)
+    sim, orc = make_pair(sc, L.FP_EXACT, pts)
+    for _ in range(substeps):
+        sim.run()
+    orc.substep(substeps)
+    a, b = fields_of(sim), oracle_fields(orc)
+    for k in a:
+        assert np.array_equal(a[k], b[k]), (name, k, np.abs(a[k].astype(np.float64) - b[k]).max())
+    if name == "boundary_small":
+        assert (b["boundary"][:, 3] > 0).sum() > 50  # the volume map was exercised
+    sim.close()
+
+
+@pytest.mark.parametrize("name", SCENES)
+def test_step_fast_mode_tolerance(name):
+    sc = scenes.reference_scene(name)
+    pts = scenes.jitter(sc.particles, 0.001, seed=9)
+    sim, o32 = make_pair(sc, L.FP_FAST, pts, 32)
+    o64 = O.Oracle(sc.config, 64)
+    o64.set_particles(pts)
+    if sc.field is not None:
+        f = sc.field
+        o64.set_field(f["res"], f["origin"], f["extent"], f["sdf"], f["vol"])
+    sim.run()
+    o32.substep(1)
+    o64.substep(1)
+    g = fields_of(sim)
+    a = oracle_fields(o32)
+    d = {name: o64.field(f) for f, name in FIELDS}
+    report = {}
+    for k in ("position", "velocity", "acceleration", "lambda", "omega", "normal", "delta_p"):
+        scale = max(np.abs(d[k]).max(), 1e-30)
+        e_gpu64 = np.abs(g[k] - d[k]).max()
+        e_ref64 = np.abs(a[k] - d[k]).max()
+        e_gpu32 = np.abs(g[k].astype(np.float64) - a[k]).max()
+        report[k] = (e_gpu32 / scale, e_gpu64 / scale, e_ref64 / scale)
+        assert e_gpu64 <= 2 * e_ref64 + 1e-5 * scale, (k, report[k])
+    for k in ("normal",):
+        assert report[k][0] <= 1e-5, (k, report[k])
+    rho_g, rho_a = g["position"][:, 3], a["position"][:, 3]
+    assert np.abs(rho_g - rho_a).max() <= 1e-5 * rho_a.max()
+    assert np.abs(g["position"][:, :3] - a["position"][:, :3]).max() <= 1e-5
+    sim.close()
+
+
+def test_sin_jitter_mode_close():
+    """The reference's sin-hash wall jitter: only clamped particles differ,
+    by at most the jitter amplitude."""
+    sc = scenes.reference_scene("water_droplet", jitter_mode=L.JITTER_SIN)
+    sim, orc = make_pair(sc, L.FP_EXACT)
+    sim.run()
+    orc.substep(1)
+    a = sim.copy_field(L.FIELD_POSITION)[:, :3]
+    b = orc.field(L.FIELD_POSITION)[:, :3]
+    assert np.abs(a - b).max() <= 2.0 * sc.config.wall_jitter
+    sim.close()
+
+
+def test_graph_replay_matches_eager():
+    sc = scenes.reference_scene("cube_small")
+    cfg = scenes.copy_config(sc.config)
+    cfg.substeps = 3
+    a, b = PBF(cfg), PBF(cfg)
+    for s in (a, b):
+        s.set_particles(sc.particles)
+    b.enable_graph(True)
+    a.step(5)
+    b.step(5)
+    assert np.array_equal(a.positions(), b.positions())
+    assert np.array_equal(a.velocities(), b.velocities())
+    a.close()
+    b.close()
+
+
+def test_seeding_matches_reference_lattice():
+    sim = PBF(scenes.base_config())
+    n1 = sim.voxelizeCube((0.15, 0.35, 0.15), (0.65, 0.85, 0.65))
+    n2 = sim.voxelizeSphere((0.5, 0.7, 0.5), 0.12)
+    sim.jitter(0.0006, 42)
+    host = sim.hostParticles()
+    ref = np.concatenate([scenes.lattice_cube(0.006, (0.15, 0.35, 0.15), (0.65, 0.85, 0.65)),
+                          scenes.lattice_sphere(0.006, (0.5, 0.7, 0.5), 0.12)])
+    ref = scenes.jitter(ref, 0.0006, 42)
+    assert n1 == 41 ** 3 and n1 + n2 == len(ref)
+    assert np.array_equal(host, ref)
+    sim.setParticlePosition()
+    assert sim.particleCount == len(ref)
+    assert np.array_equal(sim.positions()[:, :3], ref[:, :3])
+    sim.close()
+
+
+def test_volume_generator_gpu_matches_cpu():
+    shapes = [(L.SHAPE_BOX_CONTAINER, (0.8, 0.5, 0.6), (0.8, 0.5, 0.6)), (L.SHAPE_SPHERE, (0.8, 0.3, 0.6), (0.25, 0, 0)),
+              (L.SHAPE_CYLINDER, (0.3, 0.2, 0.3), (0.1, 0.2, 0)), (L.SHAPE_TORUS, (1.2, 0.4, 0.6), (0.2, 0.05, 0))]
+    for flags in (0, L.VOLMAP_OUTSIDE_EMPTY | L.VOLMAP_DISCRETE_SDF):
+        args = (shapes, (12, 8, 10), (0, 0, 0), (1.6, 1.0, 1.2), 0.1)
+        g = scenes.generate_field(*args, quadrature=8, flags=flags)
+        c = scenes.generate_field(*args, quadrature=8, flags=flags, backend=O.generate_volume_map_backend())
+        assert np.array_equal(g["sdf"], c["sdf"])
+        assert np.abs(g["vol"] - c["vol"]).max() <= 1e-6 * c["vol"].max()
+
+
+def test_cdm_text_roundtrip_and_errors():
+    sc = scenes.reference_scene("boundary_small")
+    sim, orc = make_pair(scenes.Scene("x", sc.config, sc.particles, None), L.FP_EXACT)
+    sim.setBoundaryData(scenes.cdm_text(sc.field))
+    f = sc.field
+    orc.set_field(f["res"], f["origin"], f["extent"], f["sdf"], f["vol"])
+    sim.run()
+    orc.substep(1)
+    assert np.array_equal(sim.copy_field(L.FIELD_BOUNDARY), orc.field(L.FIELD_BOUNDARY).astype(np.float32))
+    with pytest.raises(L.PBFError) as e:
+        sim.setBoundaryData("20 20 20\n3\n1 2 3 \n3\n1 2 3 \n")
+    assert e.value.code == L.PBF_EFORMAT
+    with pytest.raises(L.PBFError) as e:
+        sim.setBoundaryData("garbage")
+    assert e.value.code == L.PBF_EFORMAT
+    sim.close()
+
+
+def test_capacity_errors():
+    cfg = scenes.base_config(max_particles=100)
+    sim = PBF(cfg)
+    with pytest.raises(L.PBFError) as e:
+        sim.set_particles(np.zeros((101, 4), np.float32))
+    assert e.value.code == L.PBF_ECAPACITY
+    sim.close()
+    # neighbour-list overflow is reported at the next synchronisation, with no out-of-bounds write
+    sc = scenes.reference_scene("cube_small", max_neighbors=4)
+    sim = PBF(sc.config)
+    sim.set_particles(sc.particles)
+    sim.run()
+    with pytest.raises(L.PBFError) as e:
+        sim.synchronize()
+    assert e.value.code == L.PBF_ECAPACITY
+    sim.close()
+
+
+def test_reset_pause_and_timestamp():
+    sc = scenes.reference_scene("cube_small")
+    sim = PBF(sc.config)
+    sim.set_particles(sc.particles)
+    sim.stop()
+    sim.run()
+    assert np.array_equal(sim.positions()[:, :3], sc.particles[:, :3])
+    sim.start()
+    ms = sim.runTimestamp()
+    assert len(ms) == 4 and all(m >= 0 for m in ms)
+    m = sim.metrics()
+    assert m["nonfinite"] == 0 and m["particles"] == sc.n
+    sim.reset()
+    assert sim.particleCount == 0
+    sim.close()
+
+
+def test_dam_break_runs_stably():
+    cfg, pts, fa = scenes.dam_break_16k_spec()
+    field = scenes.generate_field(fa["shapes"], (32, 32, 32), fa["origin"], fa["extent"], fa["h"], quadrature=8)
+    sim = PBF(cfg)
+    sim.set_particles(pts)
+    sim.set_boundary_field(field["res"], field["origin"], field["extent"], field["sdf"], field["vol"])
+    sim.step(60)
+    sim.synchronize()
+    m = sim.metrics()
+    assert m["nonfinite"] == 0
+    assert m["max_compression"] < 0.5
+    x = sim.positions()[:, :3]
+    assert (x >= 0).all() and (x <= np.array([3.2, 1.0, 1.6], np.float32)).all()
+    sim.close()

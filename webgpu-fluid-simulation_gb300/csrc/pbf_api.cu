@@ -1,0 +1,1192 @@
+// pbf_api.cu — the C ABI (include/pbf_gb300.h): handle life cycle, scene
+// seeding, boundary upload, the substep driver and state access.
+//
+// One pbf_handle plays the role of the reference's PBF object
+// (src/simulator/PBF/PBF.ts:27-576) together with its NeighborSearch
+// (src/simulator/neighbor/neighborSearch.ts) and BoundaryModel
+// (src/simulator/boundary/volumeMap.ts).  Device state is kept in
+// cell-sorted slot order; the id-ordered `position` buffer the renderer reads
+// is refreshed at the end of every pbf_run / pbf_step.
+#include <cmath>
+#include <cstdarg>
+#include <cstdio>
+#include <cstdlib>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include <cuda_runtime.h>
+
+#include "../../include/pbf_gb300.h"
+#include "pbf_kernels.h"
+
+using namespace pbf;
+
+namespace {
+
+template <typename T>
+struct DBuf {
+  T* p = nullptr;
+  size_t n = 0;
+  cudaError_t alloc(size_t count) {
+    n = count;
+    if (count == 0) count = 1;
+    return cudaMalloc((void**)&p, count * sizeof(T));
+  }
+  void release() {
+    if (p) cudaFree(p);
+    p = nullptr;
+    n = 0;
+  }
+};
+
+}  // namespace
+
+struct pbf_handle {
+  pbf_config cfg;
+  SimParams sp;
+  GridParams gp;
+  FieldParams fp;
+  PassTable passes;
+  cudaStream_t stream = nullptr;
+  bool own_stream = false;
+  std::string err;
+  uint32_t n = 0;
+  bool paused = false;
+  bool capture = false;
+  int cur = 0;  // which of pos[]/ids[] holds the current state
+  std::vector<float> host_particles;  // SPH.particlePositionArray
+
+  DBuf<float4> pos[2], xs[2], vel, acc, bdata, omega, normal, dp, out_pos, out_tmp;
+  DBuf<uint32_t> ids[2], key, rank, perm_raw, id_raw, perm, tmp_a, tmp_b;
+  DBuf<uint32_t> cell_count, cell_start, big_list, big_count;
+  DBuf<uint32_t> nbr_count, nbr_offset, nbr_list;
+  DBuf<float> lambda, sdf, vol;
+  DBuf<uint32_t> err_word;
+  DBuf<float> m_f;
+  DBuf<double> m_d;
+  DBuf<uint32_t> m_u;
+  void* scan_scratch = nullptr;
+  uint32_t nbr_capacity = 0;
+  uint32_t id_bits = 1;
+
+  cudaGraphExec_t graph_exec = nullptr;
+  bool graph_enabled = false;
+  bool graph_valid = false;
+  cudaEvent_t ev[5] = {nullptr, nullptr, nullptr, nullptr, nullptr};
+  uint32_t last_nbr_total = 0;
+  // per-kernel timing (pbf_set_kernel_timing)
+  bool ktiming = false;
+  std::vector<cudaEvent_t> kt_events;
+  std::vector<std::pair<int, size_t>> kt_pairs;  // (pass id, index of the first event)
+};
+
+namespace {
+
+enum PassId {
+  K_PREDICT, K_SORT, K_GATHER, K_NBR_COUNT, K_NBR_SCAN, K_NBR_LIST, K_LAMBDA, K_DELTAP, K_DENSITY, K_VORTICITY,
+  K_XSPH, K_EXPORT, K_NUM
+};
+const char* kPassNames[K_NUM] = {"predict",   "sort",         "gather",   "nbr_count", "nbr_scan", "nbr_list",
+                                 "lambda",    "deltap_apply", "density_velocity", "vorticity", "xsph", "export"};
+
+// Brackets one launch (or one group of launches) with events when timing is on.
+struct KScope {
+  pbf_handle* h;
+  int id;
+  size_t ev;
+  KScope(pbf_handle* hh, int pass) : h(hh), id(pass), ev((size_t)-1) {
+    if (!h->ktiming) return;
+    ev = h->kt_pairs.size() * 2;
+    while (h->kt_events.size() < ev + 2) {
+      cudaEvent_t e;
+      if (cudaEventCreate(&e) != cudaSuccess) {
+        ev = (size_t)-1;
+        return;
+      }
+      h->kt_events.push_back(e);
+    }
+    cudaEventRecord(h->kt_events[ev], h->stream);
+  }
+  ~KScope() {
+    if (ev == (size_t)-1) return;
+    cudaEventRecord(h->kt_events[ev + 1], h->stream);
+    h->kt_pairs.emplace_back(id, ev);
+  }
+};
+
+int fail(pbf_handle* h, int code, const char* fmt, ...) {
+  if (h) {
+    char buf[512];
+    va_list ap;
+    va_start(ap, fmt);
+    vsnprintf(buf, sizeof(buf), fmt, ap);
+    va_end(ap);
+    h->err = buf;
+  }
+  return code;
+}
+
+#define CU(h, call)                                                                         \
+  do {                                                                                      \
+    cudaError_t e_ = (call);                                                                \
+    if (e_ != cudaSuccess) return fail((h), PBF_ECUDA, "%s: %s", #call, cudaGetErrorString(e_)); \
+  } while (0)
+
+void derive_params(pbf_handle* h) {
+  const pbf_config& c = h->cfg;
+  const double PI = 3.14159265358979323846;
+  SimParams& p = h->sp;
+  double hh = c.kernel_radius, r = c.particle_radius;
+  p.h = (float)hh;
+  p.h2 = (float)(hh * hh);
+  p.half_h = (float)(0.5 * hh);
+  p.poly6 = (float)(315.0 / (64.0 * PI * std::pow(hh, 9)));
+  p.spiky = (float)(-45.0 / (PI * std::pow(hh, 6)));
+  p.coh = (float)(32.0 / (PI * std::pow(hh, 9)));
+  p.coh_bias = (float)(-std::pow(hh, 6) / 64.0);
+  double diam = 2.0 * r;
+  double V = 0.9 * diam * diam * diam;
+  p.r = (float)r;
+  p.V = (float)V;
+  p.V2 = (float)(V * V);
+  p.m = (float)(V * (double)c.rest_density);
+  p.rho0 = c.rest_density;
+  p.two_rho0 = (float)(2.0 * (double)c.rest_density);
+  p.dt = c.time_step;
+  p.inv_dt = (float)(1.0 / (double)c.time_step);
+  p.lambda_eps = c.lambda_eps;
+  p.jitter = c.wall_jitter;
+  p.jitter_mode = (int)c.jitter_mode;
+  for (int a = 0; a < 3; ++a) {
+    p.dmin[a] = c.domain_min[a];
+    p.dmax[a] = c.domain_max[a];
+  }
+  p.gy = (float)(-(double)c.options.gravity);
+  p.xsph = c.options.xsph;
+  p.vorticity = c.options.vorticity;
+  p.tension = c.options.surface_tension;
+  p.n = h->n;
+
+  GridParams& g = h->gp;
+  uint64_t cells = 1;
+  for (int a = 0; a < 3; ++a) {
+    double ext = (double)c.domain_max[a] - (double)c.domain_min[a];
+    int d = (int)c.grid_dim[a];
+    if (d == 0) d = (int)std::ceil(ext / hh);
+    g.dim[a] = d;
+    g.origin[a] = c.domain_min[a];
+    g.inv_cell[a] = (float)((double)d / ext);
+    cells *= (uint64_t)d;
+  }
+  g.cells = (uint32_t)cells;
+}
+
+void set_field_params(pbf_handle* h, const uint32_t res[3], const float origin[3], const float extent[3]) {
+  FieldParams& f = h->fp;
+  for (int a = 0; a < 3; ++a) {
+    f.res[a] = (int)res[a];
+    f.origin[a] = origin[a];
+    f.scale[a] = (float)((double)res[a] / (double)extent[a]);
+    f.gscale[a] = (float)(2.0 * (double)res[a] / (double)extent[a]);
+  }
+  f.quirk = h->cfg.volume_quirk ? 1 : 0;
+  f.trilinear = h->cfg.boundary_interp == PBF_INTERP_TRILINEAR ? 1 : 0;
+}
+
+inline unsigned nblocks(uint32_t n, int t) { return (n + t - 1) / t; }
+
+void invalidate_graph(pbf_handle* h) {
+  if (h->graph_exec) cudaGraphExecDestroy(h->graph_exec);
+  h->graph_exec = nullptr;
+  h->graph_valid = false;
+}
+
+int check_device_errors(pbf_handle* h) {
+  uint32_t e = 0;
+  CU(h, cudaMemcpyAsync(&e, h->err_word.p, sizeof(uint32_t), cudaMemcpyDeviceToHost, h->stream));
+  CU(h, cudaStreamSynchronize(h->stream));
+  if (e) {
+    CU(h, cudaMemsetAsync(h->err_word.p, 0, sizeof(uint32_t), h->stream));
+    CU(h, cudaStreamSynchronize(h->stream));
+    if (e & PBF_DEVERR_NEIGHBOR_OVERFLOW)
+      return fail(h, PBF_ECAPACITY, "neighbour list overflow: more than %u entries needed (max_neighbors=%u)",
+                  h->nbr_capacity, h->cfg.max_neighbors);
+    if (e & PBF_DEVERR_SCAN_TIMEOUT) return fail(h, PBF_ETIMEOUT, "scan look-back wait gave up");
+    return fail(h, PBF_ECUDA, "device error word 0x%x", e);
+  }
+  return PBF_OK;
+}
+
+// One substep: the dispatch sequence of PBF.run (PBF.ts:398-448).  When
+// `ev` is given, events are recorded at the reference's four interval
+// boundaries (PBF.runTimestamp, PBF.ts:450-510).
+int substep(pbf_handle* h, cudaEvent_t* ev) {
+  const uint32_t n = h->n;
+  cudaStream_t st = h->stream;
+  SimParams p = h->sp;
+  p.n = n;
+  const GridParams g = h->gp;
+  const int c = h->cur, nx = 1 - c;
+  if (ev) CU(h, cudaEventRecord(ev[0], st));
+  // neighborSearch.clearBuffer + TimeIntegration (+ ParticleInsert counts)
+  CU(h, cudaMemsetAsync(h->cell_count.p, 0, ((size_t)g.cells + 1) * sizeof(uint32_t), st));
+  {
+  KScope ks(h, K_PREDICT);
+  h->passes.predict<<<nblocks(n, 256), 256, 0, st>>>(p, g, h->pos[c].p, h->vel.p, h->acc.p, h->xs[1].p, h->key.p,
+                                                      h->rank.p, h->cell_count.p);
+  }
+  CU(h, cudaGetLastError());
+  if (ev) CU(h, cudaEventRecord(ev[1], st));
+  // cell scan + counting sort (stable by id) + reorder of the state
+  SortBuffers sb{h->key.p,     h->rank.p,  h->cell_count.p, h->cell_start.p, h->perm_raw.p, h->id_raw.p,
+                 h->perm.p,    h->tmp_a.p, h->tmp_b.p,      h->big_list.p,   h->big_count.p, h->scan_scratch,
+                 h->err_word.p};
+  {
+    KScope ks(h, K_SORT);
+    CU(h, launch_sort_by_cell(g, n, h->ids[c].p, sb, h->id_bits, st));
+  }
+  {
+    KScope ks(h, K_GATHER);
+    CU(h, launch_gather_state(n, h->perm.p, h->pos[c].p, h->xs[1].p, h->ids[c].p, h->pos[nx].p, h->xs[0].p,
+                              h->ids[nx].p, st));
+  }
+  h->cur = nx;
+  const int cc = nx;
+  // NeighborCount + particle scan + NeighborList
+  {
+    KScope ks(h, K_NBR_COUNT);
+    h->passes.nbr_count<<<nblocks(n + 1, 256), 256, 0, st>>>(p, g, h->xs[0].p, h->cell_start.p, h->nbr_count.p);
+  }
+  CU(h, cudaGetLastError());
+  {
+    KScope ks(h, K_NBR_SCAN);
+    CU(h, launch_exclusive_scan(h->nbr_count.p, h->nbr_offset.p, (size_t)n + 1, h->scan_scratch, h->err_word.p, st));
+  }
+  {
+    KScope ks(h, K_NBR_LIST);
+    h->passes.nbr_list<<<nblocks(n, 256), 256, 0, st>>>(p, g, h->xs[0].p, h->cell_start.p, h->nbr_offset.p,
+                                                         h->nbr_list.p, h->nbr_capacity, h->err_word.p);
+  }
+  CU(h, cudaGetLastError());
+  if (ev) CU(h, cudaEventRecord(ev[2], st));
+  // constraint loop
+  int a = 0;
+  const FieldParams f = h->fp;
+  const uint32_t cap = h->nbr_capacity;
+  for (uint32_t it = 0; it < h->cfg.options.iterations; ++it) {
+    {
+      KScope ks(h, K_LAMBDA);
+      h->passes.lambda<<<nblocks(n, 256), 256, 0, st>>>(p, f, h->sdf.p, h->vol.p, h->xs[a].p, h->nbr_offset.p,
+                                                         h->nbr_list.p, cap, h->lambda.p, h->bdata.p);
+    }
+    CU(h, cudaGetLastError());
+    {
+      KScope ks(h, K_DELTAP);
+      h->passes.deltap<<<nblocks(n, 256), 256, 0, st>>>(p, f.loaded, h->xs[a].p, h->lambda.p, h->bdata.p,
+                                                         h->nbr_offset.p, h->nbr_list.p, cap, h->xs[1 - a].p,
+                                                         h->capture ? h->dp.p : nullptr);
+    }
+    CU(h, cudaGetLastError());
+    a = 1 - a;
+  }
+  if (ev) CU(h, cudaEventRecord(ev[3], st));
+  // non-pressure passes
+  {
+    KScope ks(h, K_DENSITY);
+    h->passes.density_velocity<<<nblocks(n, 256), 256, 0, st>>>(p, h->xs[a].p, h->nbr_offset.p, h->nbr_list.p,
+                                                                 cap, h->pos[cc].p, h->vel.p);
+  }
+  CU(h, cudaGetLastError());
+  if (a != 0) CU(h, cudaMemcpyAsync(h->xs[0].p, h->xs[1].p, (size_t)n * sizeof(float4), cudaMemcpyDeviceToDevice, st));
+  {
+    KScope ks(h, K_VORTICITY);
+    h->passes.vorticity<<<nblocks(n, 256), 256, 0, st>>>(p, h->pos[cc].p, h->vel.p, h->nbr_offset.p,
+                                                          h->nbr_list.p, cap, h->omega.p, h->normal.p);
+  }
+  CU(h, cudaGetLastError());
+  {
+    KScope ks(h, K_XSPH);
+    h->passes.xsph<<<nblocks(n, 256), 256, 0, st>>>(p, h->pos[cc].p, h->vel.p, h->omega.p, h->normal.p,
+                                                     h->nbr_offset.p, h->nbr_list.p, cap, h->acc.p);
+  }
+  CU(h, cudaGetLastError());
+  if (ev) CU(h, cudaEventRecord(ev[4], st));
+  return PBF_OK;
+}
+
+int export_positions(pbf_handle* h) {
+  KScope ks(h, K_EXPORT);
+  CU(h, launch_scatter_by_id(h->n, h->ids[h->cur].p, h->pos[h->cur].p, h->out_pos.p, h->stream));
+  return PBF_OK;
+}
+
+int frame(pbf_handle* h) {
+  for (uint32_t s = 0; s < h->cfg.substeps; ++s) {
+    int rc = substep(h, nullptr);
+    if (rc) return rc;
+  }
+  return export_positions(h);
+}
+
+int upload_particles(pbf_handle* h, const float* xyzw, uint32_t n) {
+  if (n > h->cfg.max_particles)
+    return fail(h, PBF_ECAPACITY, "To Many Particles! (%u > max_particles %u)", n, h->cfg.max_particles);
+  invalidate_graph(h);
+  h->n = n;
+  h->cur = 0;
+  h->sp.n = n;
+  uint32_t bits = 1;
+  while (bits < 32 && (1ull << bits) < (uint64_t)n) ++bits;
+  h->id_bits = bits;
+  std::vector<float> tmp((size_t)n * 4);
+  std::vector<uint32_t> iota(n);
+  for (uint32_t i = 0; i < n; ++i) {
+    tmp[4 * (size_t)i] = xyzw[4 * (size_t)i];
+    tmp[4 * (size_t)i + 1] = xyzw[4 * (size_t)i + 1];
+    tmp[4 * (size_t)i + 2] = xyzw[4 * (size_t)i + 2];
+    tmp[4 * (size_t)i + 3] = 0.0f;
+    iota[i] = i;
+  }
+  cudaStream_t st = h->stream;
+  if (n) {
+    CU(h, cudaMemcpyAsync(h->pos[0].p, tmp.data(), (size_t)n * sizeof(float4), cudaMemcpyHostToDevice, st));
+    CU(h, cudaMemcpyAsync(h->ids[0].p, iota.data(), (size_t)n * sizeof(uint32_t), cudaMemcpyHostToDevice, st));
+    CU(h, cudaMemsetAsync(h->vel.p, 0, (size_t)n * sizeof(float4), st));
+    CU(h, cudaMemsetAsync(h->acc.p, 0, (size_t)n * sizeof(float4), st));
+    CU(h, cudaMemsetAsync(h->lambda.p, 0, (size_t)n * sizeof(float), st));
+    CU(h, cudaMemsetAsync(h->bdata.p, 0, (size_t)n * sizeof(float4), st));
+  }
+  int rc = export_positions(h);
+  if (rc) return rc;
+  CU(h, cudaStreamSynchronize(st));
+  return PBF_OK;
+}
+
+void release_all(pbf_handle* h) {
+  invalidate_graph(h);
+  DBuf<float4>* f4s[] = {&h->pos[0], &h->pos[1], &h->xs[0], &h->xs[1], &h->vel, &h->acc, &h->bdata,
+                         &h->omega,  &h->normal, &h->dp,    &h->out_pos, &h->out_tmp};
+  for (auto* b : f4s) b->release();
+  DBuf<uint32_t>* u32s[] = {&h->ids[0],   &h->ids[1],      &h->key,      &h->rank,      &h->perm_raw,
+                            &h->id_raw,   &h->perm,        &h->tmp_a,    &h->tmp_b,     &h->cell_count,
+                            &h->cell_start, &h->big_list,  &h->big_count, &h->nbr_count, &h->nbr_offset,
+                            &h->nbr_list, &h->err_word,    &h->m_u};
+  for (auto* b : u32s) b->release();
+  h->lambda.release();
+  h->sdf.release();
+  h->vol.release();
+  h->m_f.release();
+  h->m_d.release();
+  if (h->scan_scratch) cudaFree(h->scan_scratch);
+  h->scan_scratch = nullptr;
+}
+
+bool finite_positive(float v) { return std::isfinite(v) && v > 0.0f; }
+
+}  // namespace
+
+extern "C" {
+
+int pbf_abi_version(void) { return PBF_ABI_VERSION; }
+
+int pbf_config_default(pbf_config* c) {
+  if (!c) return PBF_EINVAL;
+  std::memset(c, 0, sizeof(*c));
+  c->struct_size = sizeof(pbf_config);
+  c->max_particles = 1u << 17;  // SPH.MAX_PARTICLE_NUM = 1 << 18 - 1 == 1 << 17 (SPH.ts:24)
+  c->particle_radius = 0.006f;  // PBFConfig.ts:21
+  c->kernel_radius = 0.025f;    // SPH.ts:26
+  c->rest_density = 1000.0f;    // SPH.ts:33
+  c->time_step = (float)(1.0 / 300.0);  // SPH.ts:27
+  c->substeps = 1;              // PBFConfig.ts:21
+  c->domain_min[0] = c->domain_min[1] = c->domain_min[2] = 0.0f;
+  c->domain_max[0] = c->domain_max[1] = c->domain_max[2] = 1.0f;
+  c->lambda_eps = 1e-6f;        // PBFConfig.ts:8
+  c->wall_jitter = 1e-4f;       // common.ts:62
+  c->jitter_mode = PBF_JITTER_HASH;
+  c->volume_quirk = 1;
+  c->fp_mode = PBF_FP_FAST;
+  c->boundary_interp = PBF_INTERP_CUBIC;
+  c->max_neighbors = 60;        // SPH.MAX_NEIGHBOR_COUNT (SPH.ts:25)
+  c->options.iterations = 5;    // config.ts:22-28
+  c->options.xsph = 0.01f;
+  c->options.vorticity = 0.1f;
+  c->options.surface_tension = 0.5f;
+  c->options.gravity = 9.8f;
+  c->stream = nullptr;
+  return PBF_OK;
+}
+
+const char* pbf_last_error(const pbf_handle* h) { return h ? h->err.c_str() : "null handle"; }
+
+int pbf_create(const pbf_config* cfg, pbf_handle** out) {
+  if (!cfg || !out) return PBF_EINVAL;
+  *out = nullptr;
+  if (cfg->struct_size != sizeof(pbf_config)) return PBF_EINVAL;
+  if (!finite_positive(cfg->particle_radius) || !finite_positive(cfg->kernel_radius) ||
+      !finite_positive(cfg->rest_density) || !finite_positive(cfg->time_step) || cfg->max_particles == 0 ||
+      cfg->substeps == 0 || cfg->max_neighbors == 0)
+    return PBF_EINVAL;
+  for (int a = 0; a < 3; ++a)
+    if (!(cfg->domain_max[a] > cfg->domain_min[a])) return PBF_EINVAL;
+  pbf_handle* h = new pbf_handle();
+  h->cfg = *cfg;
+  derive_params(h);
+  if (h->gp.cells == 0 || (uint64_t)h->gp.dim[0] * h->gp.dim[1] * h->gp.dim[2] > 0xfffffffeull) {
+    delete h;
+    return PBF_EINVAL;
+  }
+  if (cfg->fp_mode == PBF_FP_EXACT)
+    exact::fill_pass_table(&h->passes);
+  else
+    fast::fill_pass_table(&h->passes);
+  h->fp = FieldParams{};
+  h->fp.loaded = 0;
+  cudaError_t e = cudaSuccess;
+  if (cfg->stream) {
+    h->stream = (cudaStream_t)cfg->stream;
+  } else {
+    e = cudaStreamCreateWithFlags(&h->stream, cudaStreamNonBlocking);
+    h->own_stream = true;
+  }
+  const size_t cap = cfg->max_particles, cells = h->gp.cells;
+  uint64_t ncap64 = (uint64_t)cap * cfg->max_neighbors;
+  if (ncap64 > 0xffffffffull) ncap64 = 0xffffffffull;
+  h->nbr_capacity = (uint32_t)ncap64;
+  auto A = [&](cudaError_t r) {
+    if (e == cudaSuccess) e = r;
+  };
+  for (int i = 0; i < 2; ++i) {
+    A(h->pos[i].alloc(cap));
+    A(h->xs[i].alloc(cap));
+    A(h->ids[i].alloc(cap));
+  }
+  A(h->vel.alloc(cap));
+  A(h->acc.alloc(cap));
+  A(h->bdata.alloc(cap));
+  A(h->omega.alloc(cap));
+  A(h->normal.alloc(cap));
+  A(h->out_pos.alloc(cap));
+  A(h->out_tmp.alloc(cap));
+  A(h->key.alloc(cap));
+  A(h->rank.alloc(cap));
+  A(h->perm_raw.alloc(cap));
+  A(h->id_raw.alloc(cap));
+  A(h->perm.alloc(cap));
+  A(h->tmp_a.alloc(cap));
+  A(h->tmp_b.alloc(cap));
+  A(h->cell_count.alloc(cells + 1));
+  A(h->cell_start.alloc(cells + 1));
+  A(h->big_list.alloc(cells));
+  A(h->big_count.alloc(1));
+  A(h->nbr_count.alloc(cap + 1));
+  A(h->nbr_offset.alloc(cap + 1));
+  A(h->nbr_list.alloc(h->nbr_capacity));
+  A(h->lambda.alloc(cap));
+  A(h->err_word.alloc(1));
+  A(h->m_f.alloc(2));
+  A(h->m_d.alloc(2));
+  A(h->m_u.alloc(2));
+  size_t sb = scan_scratch_bytes(cells + 1);
+  size_t sb2 = scan_scratch_bytes(cap + 1);
+  if (sb2 > sb) sb = sb2;
+  A(cudaMalloc(&h->scan_scratch, sb));
+  for (int i = 0; i < 5; ++i) A(cudaEventCreate(&h->ev[i]));
+  if (e == cudaSuccess) {
+    A(cudaMemsetAsync(h->err_word.p, 0, sizeof(uint32_t), h->stream));
+    A(cudaMemsetAsync(h->vel.p, 0, cap * sizeof(float4), h->stream));
+    A(cudaMemsetAsync(h->acc.p, 0, cap * sizeof(float4), h->stream));
+    A(cudaStreamSynchronize(h->stream));
+  }
+  if (e != cudaSuccess) {
+    release_all(h);
+    if (h->own_stream && h->stream) cudaStreamDestroy(h->stream);
+    for (int i = 0; i < 5; ++i)
+      if (h->ev[i]) cudaEventDestroy(h->ev[i]);
+    delete h;
+    return PBF_ECUDA;
+  }
+  *out = h;
+  return PBF_OK;
+}
+
+int pbf_destroy(pbf_handle* h) {
+  if (!h) return PBF_EINVAL;
+  cudaStreamSynchronize(h->stream);
+  release_all(h);
+  for (int i = 0; i < 5; ++i)
+    if (h->ev[i]) cudaEventDestroy(h->ev[i]);
+  for (auto e : h->kt_events) cudaEventDestroy(e);
+  if (h->own_stream && h->stream) cudaStreamDestroy(h->stream);
+  delete h;
+  return PBF_OK;
+}
+
+int pbf_reset(pbf_handle* h) {
+  if (!h) return PBF_EINVAL;
+  invalidate_graph(h);
+  h->host_particles.clear();
+  h->n = 0;
+  h->cur = 0;
+  h->fp.loaded = 0;
+  h->sdf.release();
+  h->vol.release();
+  const size_t cap = h->cfg.max_particles;
+  cudaStream_t st = h->stream;
+  for (int i = 0; i < 2; ++i) CU(h, cudaMemsetAsync(h->pos[i].p, 0, cap * sizeof(float4), st));
+  CU(h, cudaMemsetAsync(h->vel.p, 0, cap * sizeof(float4), st));
+  CU(h, cudaMemsetAsync(h->acc.p, 0, cap * sizeof(float4), st));
+  CU(h, cudaMemsetAsync(h->out_pos.p, 0, cap * sizeof(float4), st));
+  CU(h, cudaMemsetAsync(h->err_word.p, 0, sizeof(uint32_t), st));
+  CU(h, cudaStreamSynchronize(st));
+  return PBF_OK;
+}
+
+int pbf_set_options(pbf_handle* h, const pbf_options* o) {
+  if (!h || !o) return PBF_EINVAL;
+  if (!std::isfinite(o->xsph) || !std::isfinite(o->vorticity) || !std::isfinite(o->surface_tension) ||
+      !std::isfinite(o->gravity))
+    return fail(h, PBF_EINVAL, "non-finite option");
+  if (std::memcmp(&h->cfg.options, o, sizeof(pbf_options)) == 0) return PBF_OK;
+  h->cfg.options = *o;
+  h->sp.gy = (float)(-(double)o->gravity);
+  h->sp.xsph = o->xsph;
+  h->sp.vorticity = o->vorticity;
+  h->sp.tension = o->surface_tension;
+  invalidate_graph(h);
+  return PBF_OK;
+}
+
+int pbf_get_options(const pbf_handle* h, pbf_options* o) {
+  if (!h || !o) return PBF_EINVAL;
+  *o = h->cfg.options;
+  return PBF_OK;
+}
+
+int pbf_voxelize_cube(pbf_handle* h, const float mn[3], const float mx[3], uint32_t* added) {
+  if (!h || !mn || !mx) return PBF_EINVAL;
+  const double diam = 2.0 * (double)h->cfg.particle_radius;
+  long nx = (long)std::floor(((double)mx[0] - mn[0]) / diam);
+  long ny = (long)std::floor(((double)mx[1] - mn[1]) / diam);
+  long nz = (long)std::floor(((double)mx[2] - mn[2]) / diam);
+  uint32_t count = 0;
+  for (long i = 0; i < nx; ++i)
+    for (long j = 0; j < ny; ++j)
+      for (long k = 0; k < nz; ++k) {
+        h->host_particles.push_back((float)(i * diam + mn[0]));
+        h->host_particles.push_back((float)(j * diam + mn[1]));
+        h->host_particles.push_back((float)(k * diam + mn[2]));
+        h->host_particles.push_back(0.0f);
+        ++count;
+      }
+  if (added) *added = count;
+  return PBF_OK;
+}
+
+int pbf_voxelize_sphere(pbf_handle* h, const float c[3], float radius, uint32_t* added) {
+  if (!h || !c) return PBF_EINVAL;
+  const double diam = 2.0 * (double)h->cfg.particle_radius;
+  long vd = (long)std::floor((double)radius / (double)h->cfg.particle_radius / 2.0);
+  const double r2 = (double)radius * radius;
+  uint32_t count = 0;
+  for (long i = -vd; i <= vd; ++i)
+    for (long j = -vd; j <= vd; ++j)
+      for (long k = -vd; k <= vd; ++k) {
+        double x = i * diam, y = j * diam, z = k * diam;
+        if (x * x + y * y + z * z <= r2) {
+          h->host_particles.push_back((float)(x + c[0]));
+          h->host_particles.push_back((float)(y + c[1]));
+          h->host_particles.push_back((float)(z + c[2]));
+          h->host_particles.push_back(0.0f);
+          ++count;
+        }
+      }
+  if (added) *added = count;
+  return PBF_OK;
+}
+
+int pbf_jitter_particles(pbf_handle* h, float amplitude, uint64_t seed) {
+  if (!h) return PBF_EINVAL;
+  uint64_t s = seed;
+  auto next = [&]() {  // splitmix64
+    s += 0x9e3779b97f4a7c15ull;
+    uint64_t z = s;
+    z = (z ^ (z >> 30)) * 0xbf58476d1ce4e5b9ull;
+    z = (z ^ (z >> 27)) * 0x94d049bb133111ebull;
+    return z ^ (z >> 31);
+  };
+  size_t n = h->host_particles.size() / 4;
+  for (size_t i = 0; i < n; ++i)
+    for (int a = 0; a < 3; ++a) {
+      double u = (double)(next() >> 11) * (1.0 / 9007199254740992.0);
+      h->host_particles[4 * i + a] = (float)((double)h->host_particles[4 * i + a] + (double)amplitude * (2.0 * u - 1.0));
+    }
+  return PBF_OK;
+}
+
+int pbf_host_particle_count(const pbf_handle* h, uint32_t* count) {
+  if (!h || !count) return PBF_EINVAL;
+  *count = (uint32_t)(h->host_particles.size() / 4);
+  return PBF_OK;
+}
+
+int pbf_copy_host_particles(const pbf_handle* h, float* xyzw, uint32_t n) {
+  if (!h || !xyzw) return PBF_EINVAL;
+  if ((size_t)n * 4 != h->host_particles.size()) return PBF_EINVAL;
+  std::memcpy(xyzw, h->host_particles.data(), h->host_particles.size() * sizeof(float));
+  return PBF_OK;
+}
+
+int pbf_set_particle_position(pbf_handle* h) {
+  if (!h) return PBF_EINVAL;
+  if (h->host_particles.size() % 4 != 0) return fail(h, PBF_EINVAL, "Illegal length of Particle Position Buffer!");
+  uint32_t n = (uint32_t)(h->host_particles.size() / 4);
+  return upload_particles(h, h->host_particles.data(), n);
+}
+
+int pbf_set_particles(pbf_handle* h, const float* xyzw, uint32_t n) {
+  if (!h || (!xyzw && n)) return PBF_EINVAL;
+  for (size_t i = 0; i < (size_t)n * 4; ++i)
+    if ((i & 3) != 3 && !std::isfinite(xyzw[i])) return fail(h, PBF_EINVAL, "non-finite particle position");
+  h->host_particles.assign(xyzw, xyzw + (size_t)n * 4);
+  return upload_particles(h, xyzw, n);
+}
+
+int pbf_set_velocities(pbf_handle* h, const float* xyzw, uint32_t n) {
+  if (!h || !xyzw) return PBF_EINVAL;
+  if (n != h->n) return fail(h, PBF_EINVAL, "velocity count %u != particle count %u", n, h->n);
+  // velocities are stored in slot order: scatter through the current ids
+  // (slot -> id); upload by id into out_tmp then gather with a host-side inverse
+  std::vector<uint32_t> ids(n);
+  CU(h, cudaMemcpyAsync(ids.data(), h->ids[h->cur].p, (size_t)n * 4, cudaMemcpyDeviceToHost, h->stream));
+  CU(h, cudaStreamSynchronize(h->stream));
+  std::vector<float> v((size_t)n * 4);
+  for (uint32_t t = 0; t < n; ++t)
+    for (int a = 0; a < 4; ++a) v[4 * (size_t)t + a] = (a == 3) ? 0.0f : xyzw[4 * (size_t)ids[t] + a];
+  CU(h, cudaMemcpyAsync(h->vel.p, v.data(), (size_t)n * sizeof(float4), cudaMemcpyHostToDevice, h->stream));
+  CU(h, cudaStreamSynchronize(h->stream));
+  invalidate_graph(h);
+  return PBF_OK;
+}
+
+size_t pbf_field_length(const uint32_t res[3]) {
+  const size_t nx = res[0], ny = res[1], nz = res[2];
+  return (nx + 1) * (ny + 1) * (nz + 1) + 2 * nx * (ny + 1) * (nz + 1) + (nx + 1) * 2 * ny * (nz + 1) +
+         (nx + 1) * (ny + 1) * 2 * nz;
+}
+
+int pbf_set_boundary_field(pbf_handle* h, const uint32_t res[3], const float origin[3], const float extent[3],
+                           const float* sdf, const float* volume, size_t nodes) {
+  if (!h || !res || !origin || !extent || !sdf || !volume) return PBF_EINVAL;
+  for (int a = 0; a < 3; ++a) {
+    if (res[a] == 0 || res[a] > 4096) return fail(h, PBF_EINVAL, "bad field resolution");
+    if (!finite_positive(extent[a])) return fail(h, PBF_EINVAL, "bad field extent");
+  }
+  size_t len = pbf_field_length(res);
+  if (nodes != len) return fail(h, PBF_EFORMAT, "Invalid Boundary Model File! (%zu values, expected %zu)", nodes, len);
+  invalidate_graph(h);
+  h->sdf.release();
+  h->vol.release();
+  CU(h, h->sdf.alloc(len));
+  CU(h, h->vol.alloc(len));
+  CU(h, cudaMemcpyAsync(h->sdf.p, sdf, len * sizeof(float), cudaMemcpyHostToDevice, h->stream));
+  CU(h, cudaMemcpyAsync(h->vol.p, volume, len * sizeof(float), cudaMemcpyHostToDevice, h->stream));
+  CU(h, cudaMemsetAsync(h->bdata.p, 0, (size_t)h->cfg.max_particles * sizeof(float4), h->stream));
+  CU(h, cudaStreamSynchronize(h->stream));
+  set_field_params(h, res, origin, extent);
+  h->fp.loaded = 1;
+  return PBF_OK;
+}
+
+// BoundaryModel.setData (volumeMap.ts:23-39): line 0 resolution, line 2 the
+// SDF values, line 4 the volume values.  The field spans the simulation domain.
+int pbf_set_boundary_data(pbf_handle* h, const char* text, size_t len) {
+  if (!h || !text) return PBF_EINVAL;
+  std::vector<std::string> lines;
+  {
+    size_t s = 0;
+    for (size_t i = 0; i <= len; ++i) {
+      if (i == len || text[i] == '\n') {
+        lines.emplace_back(text + s, i - s);
+        s = i + 1;
+      }
+    }
+  }
+  if (lines.size() < 5) return fail(h, PBF_EFORMAT, "Invalid Boundary Model File! (%zu lines)", lines.size());
+  uint32_t res[3];
+  {
+    double r[3];
+    if (std::sscanf(lines[0].c_str(), "%lf %lf %lf", &r[0], &r[1], &r[2]) != 3)
+      return fail(h, PBF_EFORMAT, "Invalid Boundary Model File! (resolution line)");
+    for (int a = 0; a < 3; ++a) {
+      if (!(r[a] >= 1.0 && r[a] <= 4096.0) || r[a] != std::floor(r[a]))
+        return fail(h, PBF_EFORMAT, "Invalid Boundary Model File! (resolution)");
+      res[a] = (uint32_t)r[a];
+    }
+  }
+  const size_t expect = pbf_field_length(res);
+  auto parse = [&](const std::string& line, std::vector<float>& out) -> bool {
+    out.clear();
+    out.reserve(expect);
+    const char* p = line.c_str();
+    const char* end = p + line.size();
+    while (p < end) {
+      while (p < end && (*p == ' ' || *p == '\t' || *p == '\r')) ++p;
+      if (p >= end) break;
+      char* q = nullptr;
+      float v = std::strtof(p, &q);
+      if (q == p) return false;
+      if (!std::isfinite(v)) return false;
+      out.push_back(v);
+      p = q;
+    }
+    return true;
+  };
+  std::vector<float> sdf, vol;
+  if (!parse(lines[2], sdf) || !parse(lines[4], vol))
+    return fail(h, PBF_EFORMAT, "Invalid Boundary Model File! (non-numeric value)");
+  if (sdf.size() != expect || vol.size() != expect)
+    return fail(h, PBF_EFORMAT, "Invalid Boundary Model File! (%zu / %zu values, expected %zu)", sdf.size(),
+                vol.size(), expect);
+  float origin[3], extent[3];
+  for (int a = 0; a < 3; ++a) {
+    origin[a] = h->cfg.domain_min[a];
+    extent[a] = h->cfg.domain_max[a] - h->cfg.domain_min[a];
+  }
+  return pbf_set_boundary_field(h, res, origin, extent, sdf.data(), vol.data(), expect);
+}
+
+int pbf_clear_boundary(pbf_handle* h) {
+  if (!h) return PBF_EINVAL;
+  invalidate_graph(h);
+  h->fp.loaded = 0;
+  return PBF_OK;
+}
+
+int pbf_set_paused(pbf_handle* h, int paused) {
+  if (!h) return PBF_EINVAL;
+  h->paused = paused != 0;
+  return PBF_OK;
+}
+int pbf_is_paused(const pbf_handle* h) { return h ? (h->paused ? 1 : 0) : -1; }
+
+int pbf_set_capture(pbf_handle* h, int enable) {
+  if (!h) return PBF_EINVAL;
+  invalidate_graph(h);
+  if (enable && !h->dp.p) CU(h, h->dp.alloc(h->cfg.max_particles));
+  h->capture = enable != 0;
+  return PBF_OK;
+}
+
+int pbf_run(pbf_handle* h) {
+  if (!h) return PBF_EINVAL;
+  if (h->paused || h->n == 0) return PBF_OK;
+  int rc = substep(h, nullptr);
+  if (rc) return rc;
+  return export_positions(h);
+}
+
+int pbf_enable_graph(pbf_handle* h, int enable) {
+  if (!h) return PBF_EINVAL;
+  invalidate_graph(h);
+  h->graph_enabled = enable != 0;
+  return PBF_OK;
+}
+
+int pbf_step(pbf_handle* h, uint32_t frames) {
+  if (!h) return PBF_EINVAL;
+  if (h->paused || h->n == 0) return PBF_OK;
+  if (!h->graph_enabled || h->ktiming) {
+    for (uint32_t f = 0; f < frames; ++f) {
+      int rc = frame(h);
+      if (rc) return rc;
+    }
+    return PBF_OK;
+  }
+  // Each substep swaps the state buffers once, so a graph covers an even
+  // number of substeps (one frame, or two frames when substeps is odd) and
+  // every replay starts from the same buffers.
+  const uint32_t per_graph = (h->cfg.substeps % 2 == 0) ? 1u : 2u;
+  if (!h->graph_valid) {
+    const int start_cur = h->cur;
+    cudaGraph_t g = nullptr;
+    CU(h, cudaStreamBeginCapture(h->stream, cudaStreamCaptureModeThreadLocal));
+    int rc = PBF_OK;
+    for (uint32_t f = 0; f < per_graph && rc == PBF_OK; ++f) rc = frame(h);
+    cudaError_t ce = cudaStreamEndCapture(h->stream, &g);
+    h->cur = start_cur;  // capture only recorded the work
+    if (rc) {
+      if (g) cudaGraphDestroy(g);
+      return rc;
+    }
+    if (ce != cudaSuccess) return fail(h, PBF_ECUDA, "graph capture: %s", cudaGetErrorString(ce));
+    ce = cudaGraphInstantiate(&h->graph_exec, g, 0);
+    cudaGraphDestroy(g);
+    if (ce != cudaSuccess) return fail(h, PBF_ECUDA, "graph instantiate: %s", cudaGetErrorString(ce));
+    h->graph_valid = true;
+  }
+  uint32_t full = frames / per_graph, rest = frames % per_graph;
+  for (uint32_t f = 0; f < full; ++f) CU(h, cudaGraphLaunch(h->graph_exec, h->stream));
+  for (uint32_t f = 0; f < rest; ++f) {
+    // an odd remainder runs eagerly and leaves the buffers swapped: the graph
+    // no longer matches them
+    invalidate_graph(h);
+    int rc = frame(h);
+    if (rc) return rc;
+  }
+  return PBF_OK;
+}
+
+int pbf_run_timestamp(pbf_handle* h, float ms[4]) {
+  if (!h || !ms) return PBF_EINVAL;
+  for (int i = 0; i < 4; ++i) ms[i] = 0.0f;
+  if (h->n == 0) return PBF_OK;
+  int rc = substep(h, h->ev);
+  if (rc) return rc;
+  rc = export_positions(h);
+  if (rc) return rc;
+  CU(h, cudaEventSynchronize(h->ev[4]));
+  for (int i = 0; i < 4; ++i) CU(h, cudaEventElapsedTime(&ms[i], h->ev[i], h->ev[i + 1]));
+  return check_device_errors(h);
+}
+
+int pbf_synchronize(pbf_handle* h) {
+  if (!h) return PBF_EINVAL;
+  CU(h, cudaStreamSynchronize(h->stream));
+  return check_device_errors(h);
+}
+
+int pbf_set_kernel_timing(pbf_handle* h, int enable) {
+  if (!h) return PBF_EINVAL;
+  h->ktiming = enable != 0;
+  return PBF_OK;
+}
+
+int pbf_get_kernel_timing(pbf_handle* h, pbf_kernel_time* out, uint32_t max, uint32_t* count) {
+  if (!h || (!out && max)) return PBF_EINVAL;
+  CU(h, cudaStreamSynchronize(h->stream));
+  double total[K_NUM] = {0};
+  uint32_t launches[K_NUM] = {0};
+  for (auto& pr : h->kt_pairs) {
+    float ms = 0.0f;
+    CU(h, cudaEventElapsedTime(&ms, h->kt_events[pr.second], h->kt_events[pr.second + 1]));
+    total[pr.first] += ms;
+    launches[pr.first] += 1;
+  }
+  h->kt_pairs.clear();
+  uint32_t c = 0;
+  for (int k = 0; k < K_NUM; ++k) {
+    if (!launches[k]) continue;
+    if (c < max) {
+      std::memset(out[c].name, 0, sizeof(out[c].name));
+      std::strncpy(out[c].name, kPassNames[k], sizeof(out[c].name) - 1);
+      out[c].launches = launches[k];
+      out[c].total_ms = (float)total[k];
+    }
+    ++c;
+  }
+  if (count) *count = c;
+  return PBF_OK;
+}
+
+uint32_t pbf_particle_count(const pbf_handle* h) { return h ? h->n : 0; }
+const float* pbf_position_device(pbf_handle* h) { return h ? (const float*)h->out_pos.p : nullptr; }
+const float* pbf_velocity_device(pbf_handle* h) {
+  if (!h) return nullptr;
+  if (launch_scatter_by_id(h->n, h->ids[h->cur].p, h->vel.p, h->out_tmp.p, h->stream) != cudaSuccess) return nullptr;
+  return (const float*)h->out_tmp.p;
+}
+void* pbf_stream(pbf_handle* h) { return h ? (void*)h->stream : nullptr; }
+
+int pbf_copy_field(pbf_handle* h, int field, void* host, size_t bytes) {
+  if (!h || (!host && bytes)) return PBF_EINVAL;
+  const uint32_t n = h->n;
+  cudaStream_t st = h->stream;
+  const uint32_t* id = h->ids[h->cur].p;
+  size_t need4 = (size_t)n * sizeof(float4), need1 = (size_t)n * 4;
+  const float4* src4 = nullptr;
+  switch (field) {
+    case PBF_FIELD_POSITION: src4 = h->pos[h->cur].p; break;
+    case PBF_FIELD_VELOCITY: src4 = h->vel.p; break;
+    case PBF_FIELD_ACCELERATION: src4 = h->acc.p; break;
+    case PBF_FIELD_PREDICTED: src4 = h->xs[0].p; break;
+    case PBF_FIELD_BOUNDARY: src4 = h->bdata.p; break;
+    case PBF_FIELD_OMEGA: src4 = h->omega.p; break;
+    case PBF_FIELD_NORMAL: src4 = h->normal.p; break;
+    case PBF_FIELD_DELTA_P:
+      if (!h->capture || !h->dp.p) return fail(h, PBF_ESTATE, "delta_p needs pbf_set_capture(1) before the step");
+      src4 = h->dp.p;
+      break;
+    case PBF_FIELD_LAMBDA:
+    case PBF_FIELD_NEIGHBOR_COUNT: break;
+    default: return fail(h, PBF_EINVAL, "unknown field %d", field);
+  }
+  if (src4) {
+    if (bytes != need4) return fail(h, PBF_EINVAL, "field needs %zu bytes, got %zu", need4, bytes);
+    if (n) {
+      CU(h, launch_scatter_by_id(n, id, src4, h->out_tmp.p, st));
+      CU(h, cudaMemcpyAsync(host, h->out_tmp.p, need4, cudaMemcpyDeviceToHost, st));
+    }
+  } else {
+    if (bytes != need1) return fail(h, PBF_EINVAL, "field needs %zu bytes, got %zu", need1, bytes);
+    if (n) {
+      if (field == PBF_FIELD_LAMBDA)
+        CU(h, launch_scatter_by_id_f32(n, id, h->lambda.p, (float*)h->out_tmp.p, st));
+      else
+        CU(h, launch_scatter_by_id_u32(n, id, h->nbr_count.p, (uint32_t*)h->out_tmp.p, st));
+      CU(h, cudaMemcpyAsync(host, h->out_tmp.p, need1, cudaMemcpyDeviceToHost, st));
+    }
+  }
+  CU(h, cudaStreamSynchronize(st));
+  return check_device_errors(h);
+}
+
+int pbf_get_metrics(pbf_handle* h, pbf_metrics* out) {
+  if (!h || !out) return PBF_EINVAL;
+  std::memset(out, 0, sizeof(*out));
+  out->particles = h->n;
+  cudaStream_t st = h->stream;
+  CU(h, cudaMemsetAsync(h->m_f.p, 0, 2 * sizeof(float), st));
+  CU(h, cudaMemsetAsync(h->m_d.p, 0, 2 * sizeof(double), st));
+  CU(h, cudaMemsetAsync(h->m_u.p, 0, 2 * sizeof(uint32_t), st));
+  SimParams p = h->sp;
+  p.n = h->n;
+  CU(h, launch_metrics(p, h->fp, h->fp.loaded ? h->sdf.p : nullptr, h->pos[h->cur].p, h->vel.p, h->n, h->m_f.p,
+                       h->m_d.p, h->m_u.p, st));
+  float mf[2];
+  double md[2];
+  uint32_t mu[2], tot = 0, errw = 0;
+  CU(h, cudaMemcpyAsync(mf, h->m_f.p, sizeof(mf), cudaMemcpyDeviceToHost, st));
+  CU(h, cudaMemcpyAsync(md, h->m_d.p, sizeof(md), cudaMemcpyDeviceToHost, st));
+  CU(h, cudaMemcpyAsync(mu, h->m_u.p, sizeof(mu), cudaMemcpyDeviceToHost, st));
+  CU(h, cudaMemcpyAsync(&errw, h->err_word.p, sizeof(uint32_t), cudaMemcpyDeviceToHost, st));
+  if (h->n) CU(h, cudaMemcpyAsync(&tot, h->nbr_offset.p + h->n, sizeof(uint32_t), cudaMemcpyDeviceToHost, st));
+  CU(h, cudaStreamSynchronize(st));
+  out->max_compression = mf[0];
+  out->max_abs_density_err = mf[1];
+  out->mean_abs_density_err = h->n ? (float)(md[0] / h->n) : 0.0f;
+  out->kinetic_energy = (float)md[1];
+  out->nonfinite = mu[0];
+  out->penetrations = mu[1];
+  out->error_flags = errw;
+  out->neighbor_total = tot;
+  return PBF_OK;
+}
+
+// ---- neighbour search alone -------------------------------------------------------
+}  // extern "C"
+
+struct pbf_ns {
+  GridParams g;
+  uint32_t max_n;
+  cudaStream_t stream;
+  bool own_stream;
+  std::string err;
+  DBuf<uint32_t> key, rank, cell_count, cell_start, perm_raw, id_raw, perm, tmp_a, tmp_b, big_list, big_count, err_word;
+  DBuf<uint32_t> nbr_count;
+  void* scan_scratch = nullptr;
+};
+
+namespace {
+int nsfail(pbf_ns* s, int code, const char* msg) {
+  if (s) s->err = msg;
+  return code;
+}
+#define NSCU(s, call)                                                    \
+  do {                                                                   \
+    cudaError_t e_ = (call);                                             \
+    if (e_ != cudaSuccess) return nsfail((s), PBF_ECUDA, cudaGetErrorString(e_)); \
+  } while (0)
+
+// NeighborCount / NeighborList over positions in id order: reuse the fast
+// pass kernels with the stand-alone radius (distance test only, no float
+// arithmetic beyond d.d, identical in both variants).
+}  // namespace
+
+extern "C" {
+
+int pbf_ns_create(const pbf_grid* grid, uint32_t max_particles, void* stream, pbf_ns** out) {
+  if (!grid || !out || max_particles == 0) return PBF_EINVAL;
+  *out = nullptr;
+  uint64_t cells = 1;
+  for (int a = 0; a < 3; ++a) {
+    if (grid->dim[a] == 0 || !(grid->inv_cell[a] > 0.0f)) return PBF_EINVAL;
+    cells *= grid->dim[a];
+  }
+  if (cells > 0xfffffffeull) return PBF_EINVAL;
+  pbf_ns* s = new pbf_ns();
+  for (int a = 0; a < 3; ++a) {
+    s->g.origin[a] = grid->origin[a];
+    s->g.inv_cell[a] = grid->inv_cell[a];
+    s->g.dim[a] = (int)grid->dim[a];
+  }
+  s->g.cells = (uint32_t)cells;
+  s->max_n = max_particles;
+  cudaError_t e = cudaSuccess;
+  if (stream) {
+    s->stream = (cudaStream_t)stream;
+    s->own_stream = false;
+  } else {
+    e = cudaStreamCreateWithFlags(&s->stream, cudaStreamNonBlocking);
+    s->own_stream = true;
+  }
+  auto A = [&](cudaError_t r) {
+    if (e == cudaSuccess) e = r;
+  };
+  size_t n = max_particles;
+  A(s->key.alloc(n));
+  A(s->rank.alloc(n));
+  A(s->perm_raw.alloc(n));
+  A(s->id_raw.alloc(n));
+  A(s->perm.alloc(n));
+  A(s->tmp_a.alloc(n));
+  A(s->tmp_b.alloc(n));
+  A(s->cell_count.alloc(cells + 1));
+  A(s->cell_start.alloc(cells + 1));
+  A(s->big_list.alloc(cells));
+  A(s->big_count.alloc(1));
+  A(s->err_word.alloc(1));
+  A(s->nbr_count.alloc(n + 1));
+  size_t sb = scan_scratch_bytes(cells + 1), sb2 = scan_scratch_bytes(n + 1);
+  A(cudaMalloc(&s->scan_scratch, sb > sb2 ? sb : sb2));
+  if (e == cudaSuccess) {
+    A(cudaMemsetAsync(s->err_word.p, 0, 4, s->stream));
+    A(cudaStreamSynchronize(s->stream));
+  }
+  if (e != cudaSuccess) {
+    pbf_ns_destroy(s);
+    return PBF_ECUDA;
+  }
+  *out = s;
+  return PBF_OK;
+}
+
+int pbf_ns_destroy(pbf_ns* s) {
+  if (!s) return PBF_EINVAL;
+  if (s->stream) cudaStreamSynchronize(s->stream);
+  DBuf<uint32_t>* bufs[] = {&s->key,   &s->rank,  &s->cell_count, &s->cell_start, &s->perm_raw, &s->id_raw, &s->perm,
+                            &s->tmp_a, &s->tmp_b, &s->big_list,   &s->big_count,  &s->err_word, &s->nbr_count};
+  for (auto* b : bufs) b->release();
+  if (s->scan_scratch) cudaFree(s->scan_scratch);
+  if (s->own_stream && s->stream) cudaStreamDestroy(s->stream);
+  delete s;
+  return PBF_OK;
+}
+
+const char* pbf_ns_last_error(const pbf_ns* s) { return s ? s->err.c_str() : "null"; }
+
+int pbf_ns_run(pbf_ns* s, const float* d_pos4, uint32_t n, uint32_t* d_keys, uint32_t* d_cell_count,
+               uint32_t* d_cell_offset, uint32_t* d_order, uint32_t* d_rank) {
+  if (!s || (!d_pos4 && n)) return PBF_EINVAL;
+  if (n > s->max_n) return nsfail(s, PBF_ECAPACITY, "too many particles for this search context");
+  cudaStream_t st = s->stream;
+  const GridParams g = s->g;
+  NSCU(s, cudaMemsetAsync(s->cell_count.p, 0, ((size_t)g.cells + 1) * 4, st));
+  NSCU(s, launch_insert(g, (const float4*)d_pos4, n, s->key.p, s->rank.p, s->cell_count.p, st));
+  uint32_t bits = 1;
+  while (bits < 32 && (1ull << bits) < (uint64_t)n) ++bits;
+  SortBuffers sb{s->key.p,   s->rank.p,  s->cell_count.p, s->cell_start.p, s->perm_raw.p, s->id_raw.p,
+                 s->perm.p,  s->tmp_a.p, s->tmp_b.p,      s->big_list.p,   s->big_count.p, s->scan_scratch,
+                 s->err_word.p};
+  NSCU(s, launch_sort_by_cell(g, n, nullptr, sb, bits, st));
+  if (d_keys && n) NSCU(s, cudaMemcpyAsync(d_keys, s->key.p, (size_t)n * 4, cudaMemcpyDeviceToDevice, st));
+  if (d_cell_count)
+    NSCU(s, cudaMemcpyAsync(d_cell_count, s->cell_count.p, (size_t)g.cells * 4, cudaMemcpyDeviceToDevice, st));
+  if (d_cell_offset)
+    NSCU(s, cudaMemcpyAsync(d_cell_offset, s->cell_start.p, ((size_t)g.cells + 1) * 4, cudaMemcpyDeviceToDevice, st));
+  if (d_order && n) NSCU(s, cudaMemcpyAsync(d_order, s->perm.p, (size_t)n * 4, cudaMemcpyDeviceToDevice, st));
+  if (d_rank && n) NSCU(s, launch_rank_from_order(n, s->perm.p, s->key.p, s->cell_start.p, d_rank, st));
+  return PBF_OK;
+}
+
+int pbf_ns_lists(pbf_ns* s, const float* d_pos4, uint32_t n, float radius, uint32_t* d_nbr_offset,
+                 uint32_t* d_nbr_list, uint32_t capacity, uint32_t* total) {
+  if (!s || !d_nbr_offset || (!d_pos4 && n)) return PBF_EINVAL;
+  if (n > s->max_n) return nsfail(s, PBF_ECAPACITY, "too many particles for this search context");
+  cudaStream_t st = s->stream;
+  // The pass kernels traverse particles in cell-sorted order; gather the
+  // positions into that order (tmp buffers reinterpreted as float4 need 4x
+  // room, so use a temporary allocation).
+  float4* sorted = nullptr;
+  uint32_t* sorted_list = nullptr;
+  uint32_t* ids = nullptr;
+  NSCU(s, cudaMallocAsync((void**)&sorted, ((size_t)n + 1) * sizeof(float4), st));
+  NSCU(s, cudaMallocAsync((void**)&ids, ((size_t)n + 1) * 4, st));
+  SimParams p{};
+  p.h = radius;
+  p.h2 = (float)((double)radius * (double)radius);
+  p.n = n;
+  PassTable tbl;
+  exact::fill_pass_table(&tbl);
+  NSCU(s, launch_gather_state(n, s->perm.p, (const float4*)d_pos4, (const float4*)d_pos4, s->perm.p, sorted, sorted,
+                              ids, st));
+  tbl.nbr_count<<<nblocks(n + 1, 256), 256, 0, st>>>(p, s->g, sorted, s->cell_start.p, s->nbr_count.p);
+  NSCU(s, cudaGetLastError());
+  // counts are in slot order; the reference's offsets are by particle id
+  uint32_t* cnt_by_id = nullptr;
+  NSCU(s, cudaMallocAsync((void**)&cnt_by_id, ((size_t)n + 1) * 4, st));
+  NSCU(s, cudaMemsetAsync(cnt_by_id, 0, ((size_t)n + 1) * 4, st));
+  NSCU(s, launch_scatter_by_id_u32(n, ids, s->nbr_count.p, cnt_by_id, st));
+  NSCU(s, launch_exclusive_scan(cnt_by_id, d_nbr_offset, (size_t)n + 1, s->scan_scratch, s->err_word.p, st));
+  // slot-order offsets for the list kernel
+  uint32_t* slot_off = nullptr;
+  NSCU(s, cudaMallocAsync((void**)&slot_off, ((size_t)n + 1) * 4, st));
+  NSCU(s, launch_exclusive_scan(s->nbr_count.p, slot_off, (size_t)n + 1, s->scan_scratch, s->err_word.p, st));
+  uint32_t tot = 0;
+  NSCU(s, cudaMemcpyAsync(&tot, slot_off + n, 4, cudaMemcpyDeviceToHost, st));
+  NSCU(s, cudaStreamSynchronize(st));
+  if (total) *total = tot;
+  int rc = PBF_OK;
+  if (tot > capacity) {
+    rc = nsfail(s, PBF_ECAPACITY, "neighbour lists exceed capacity");
+  } else if (tot && d_nbr_list) {
+    NSCU(s, cudaMallocAsync((void**)&sorted_list, (size_t)tot * 4, st));
+    tbl.nbr_list<<<nblocks(n, 256), 256, 0, st>>>(p, s->g, sorted, s->cell_start.p, slot_off, sorted_list, tot,
+                                                   s->err_word.p);
+    NSCU(s, cudaGetLastError());
+    // translate slot ids to particle ids, then move each particle's run to its id-order offset
+    NSCU(s, launch_list_to_ids(tot, sorted_list, ids, sorted_list, st));
+    // move each particle's run from its slot-order offset to its id-order offset
+    NSCU(s, launch_copy_runs(n, slot_off, d_nbr_offset, ids, sorted_list, d_nbr_list, st));
+    NSCU(s, cudaFreeAsync(sorted_list, st));
+  }
+  NSCU(s, cudaFreeAsync(slot_off, st));
+  NSCU(s, cudaFreeAsync(cnt_by_id, st));
+  NSCU(s, cudaFreeAsync(sorted, st));
+  NSCU(s, cudaFreeAsync(ids, st));
+  NSCU(s, cudaStreamSynchronize(st));
+  return rc;
+}
+
+int pbf_ns_sync(pbf_ns* s) {
+  if (!s) return PBF_EINVAL;
+  NSCU(s, cudaStreamSynchronize(s->stream));
+  uint32_t e = 0;
+  NSCU(s, cudaMemcpy(&e, s->err_word.p, 4, cudaMemcpyDeviceToHost));
+  if (e & PBF_DEVERR_SCAN_TIMEOUT) {
+    cudaMemset(s->err_word.p, 0, 4);
+    return nsfail(s, PBF_ETIMEOUT, "scan look-back wait gave up");
+  }
+  return PBF_OK;
+}
+
+int pbf_exclusive_scan_u32(const uint32_t* d_in, uint32_t* d_out, size_t n, void* stream) {
+  if ((!d_in || !d_out) && n) return PBF_EINVAL;
+  if (n == 0) return PBF_OK;
+  cudaStream_t st = (cudaStream_t)stream;
+  void* scratch = nullptr;
+  uint32_t* err = nullptr;
+  size_t bytes = scan_scratch_bytes(n);
+  if (cudaMallocAsync(&scratch, bytes + 16, st) != cudaSuccess) return PBF_ECUDA;
+  err = (uint32_t*)((char*)scratch + bytes);
+  if (cudaMemsetAsync(err, 0, 4, st) != cudaSuccess) return PBF_ECUDA;
+  if (launch_exclusive_scan(d_in, d_out, n, scratch, err, st) != cudaSuccess) return PBF_ECUDA;
+  uint32_t e = 0;
+  if (cudaMemcpyAsync(&e, err, 4, cudaMemcpyDeviceToHost, st) != cudaSuccess) return PBF_ECUDA;
+  if (cudaFreeAsync(scratch, st) != cudaSuccess) return PBF_ECUDA;
+  if (cudaStreamSynchronize(st) != cudaSuccess) return PBF_ECUDA;
+  return e ? PBF_ETIMEOUT : PBF_OK;
+}
+
+}  // extern "C"

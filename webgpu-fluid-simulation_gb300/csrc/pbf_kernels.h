@@ -1,0 +1,96 @@
+// pbf_kernels.h — host-visible declarations of the device kernels and launch
+// helpers.  The float passes exist twice (exact / fast) and are reached
+// through a PassTable of kernel pointers.
+#pragma once
+#include <cstddef>
+#include <cstdint>
+#include <cuda_runtime.h>
+
+#include "pbf_params.h"
+
+namespace pbf {
+
+struct PassTable {
+  void (*predict)(SimParams, GridParams, const float4*, const float4*, const float4*, float4*, uint32_t*, uint32_t*,
+                  uint32_t*);
+  void (*nbr_count)(SimParams, GridParams, const float4*, const uint32_t*, uint32_t*);
+  void (*nbr_list)(SimParams, GridParams, const float4*, const uint32_t*, const uint32_t*, uint32_t*, uint32_t,
+                   uint32_t*);
+  void (*lambda)(SimParams, FieldParams, const float*, const float*, const float4*, const uint32_t*, const uint32_t*,
+                 uint32_t, float*, float4*);
+  void (*deltap)(SimParams, int, const float4*, const float*, const float4*, const uint32_t*, const uint32_t*, uint32_t,
+                 float4*, float4*);
+  void (*density_velocity)(SimParams, const float4*, const uint32_t*, const uint32_t*, uint32_t, float4*, float4*);
+  void (*vorticity)(SimParams, const float4*, const float4*, const uint32_t*, const uint32_t*, uint32_t, float4*,
+                    float4*);
+  void (*xsph)(SimParams, const float4*, const float4*, const float4*, const float4*, const uint32_t*,
+               const uint32_t*, uint32_t, float4*);
+};
+
+namespace exact {
+void fill_pass_table(PassTable* tbl);
+}
+namespace fast {
+void fill_pass_table(PassTable* tbl);
+}
+
+// ---- integer pipeline (pbf_sort.cu) ---------------------------------------------
+// Scratch of the single-pass scan for up to `n` elements, in bytes.
+size_t scan_scratch_bytes(size_t n);
+// Exclusive scan of n u32 (out may alias nothing in in).  `scratch` holds
+// scan_scratch_bytes(n) bytes; err receives PBF_DEVERR_SCAN_TIMEOUT when a
+// bounded look-back wait gives up.
+cudaError_t launch_exclusive_scan(const uint32_t* in, uint32_t* out, size_t n, void* scratch, uint32_t* err,
+                                  cudaStream_t st);
+
+// Counting-sort pipeline shared by the step and the stand-alone search.
+struct SortBuffers {
+  uint32_t* key;        // [n] cell key per input slot
+  uint32_t* rank;       // [n] warp-aggregated (unordered) rank per input slot
+  uint32_t* cell_count; // [cells + 1]
+  uint32_t* cell_start; // [cells + 1] exclusive scan of cell_count
+  uint32_t* perm_raw;   // [n] scattered slots (unordered within a cell)
+  uint32_t* id_raw;     // [n] particle id of perm_raw entries
+  uint32_t* perm;       // [n] output: sorted slot -> input slot, stable by id
+  uint32_t* tmp_a;      // [n] radix scratch for very full cells
+  uint32_t* tmp_b;      // [n]
+  uint32_t* big_list;   // [cells] cells sorted by the block radix path
+  uint32_t* big_count;  // [1]
+  void* scan_scratch;
+  uint32_t* err;
+};
+
+cudaError_t launch_insert(GridParams g, const float4* pos, uint32_t n, uint32_t* key, uint32_t* rank,
+                          uint32_t* cell_count, cudaStream_t st);
+// scatter + stable within-cell order + (optionally) gather of the particle state.
+cudaError_t launch_sort_by_cell(GridParams g, uint32_t n, const uint32_t* ids, SortBuffers& b, uint32_t id_bits,
+                                cudaStream_t st);
+cudaError_t launch_gather_state(uint32_t n, const uint32_t* perm, const float4* pos_in, const float4* xs_in,
+                                const uint32_t* id_in, float4* pos_out, float4* xs_out, uint32_t* id_out,
+                                cudaStream_t st);
+cudaError_t launch_rank_from_order(uint32_t n, const uint32_t* perm, const uint32_t* key, const uint32_t* cell_start,
+                                   uint32_t* rank_out, cudaStream_t st);
+cudaError_t launch_scatter_by_id(uint32_t n, const uint32_t* id, const float4* src, float4* dst, cudaStream_t st);
+cudaError_t launch_scatter_by_id_u32(uint32_t n, const uint32_t* id, const uint32_t* src, uint32_t* dst,
+                                     cudaStream_t st);
+cudaError_t launch_scatter_by_id_f32(uint32_t n, const uint32_t* id, const float* src, float* dst, cudaStream_t st);
+cudaError_t launch_list_to_ids(uint32_t total, const uint32_t* list, const uint32_t* id, uint32_t* out,
+                               cudaStream_t st);
+// dst[id_off[ids[t]] + q] = src[slot_off[t] + q] for each slot t's run.
+cudaError_t launch_copy_runs(uint32_t n, const uint32_t* slot_off, const uint32_t* id_off, const uint32_t* ids,
+                             const uint32_t* src, uint32_t* dst, cudaStream_t st);
+cudaError_t launch_nbr_count_sub(uint32_t n, const uint32_t* off, uint32_t* cnt, cudaStream_t st);
+
+// Metrics (max / mean density error, kinetic energy, non-finite and penetration counts).
+struct MetricsAccum {
+  float max_compression;
+  float max_abs_err;
+  double sum_abs_err;
+  double kinetic;
+  uint32_t nonfinite;
+  uint32_t penetrations;
+};
+cudaError_t launch_metrics(SimParams p, FieldParams f, const float* sdf, const float4* pos, const float4* vel,
+                           uint32_t n, float* accum_f, double* accum_d, uint32_t* accum_u, cudaStream_t st);
+
+}  // namespace pbf

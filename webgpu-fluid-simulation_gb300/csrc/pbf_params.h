@@ -1,0 +1,42 @@
+// pbf_params.h — plain-old-data parameter blocks passed by value to the kernels.
+// Host code (pbf_api.cu) fills them from pbf_config; every derived constant
+// is computed in double from the float configuration and rounded once.
+#pragma once
+#include <cstdint>
+
+namespace pbf {
+
+struct GridParams {
+  float origin[3];
+  float inv_cell[3];  // cells per unit length
+  int dim[3];
+  uint32_t cells;     // dim[0] * dim[1] * dim[2]
+};
+
+struct FieldParams {
+  int res[3];
+  float origin[3];
+  float scale[3];     // res / extent
+  float gscale[3];    // 2 * res / extent (gradient scale, discreteFieldShader.ts:174)
+  int quirk;          // reference volume-node quirk
+  int trilinear;      // 1 = trilinear corner interpolation
+  int loaded;
+};
+
+struct SimParams {
+  // kernels (common.ts:1-40)
+  float h, h2, half_h, poly6, spiky, coh, coh_bias;
+  // particle (SPH.ts:49-50, PBF.ts:328,390)
+  float r, V, V2, m, rho0, two_rho0;
+  // time integration
+  float dt, inv_dt;
+  float lambda_eps;
+  float jitter;
+  int jitter_mode;
+  float dmin[3], dmax[3];
+  // SimulationOptions (shader.ts:50-58)
+  float gy, xsph, vorticity, tension;
+  uint32_t n;
+};
+
+}  // namespace pbf

@@ -1,0 +1,324 @@
+// pbf_passes.cuh — the floating-point passes of one PBF substep.
+//
+// This header is compiled twice, into namespace pbf::exact (-fmad=false) and
+// pbf::fast, by pbf_passes_exact.cu / pbf_passes_fast.cu.  PBF_NS names the
+// namespace.  All particle arrays are in cell-sorted slot order (the layout
+// the counting-sort reorder writes); neighbour lists hold slot indices.
+//
+// Reference passes restated here (paths relative to the reference root):
+//   predict + key + count  TimeIntegration (src/simulator/PBF/shader/timeIntegration.ts:20-32)
+//                          + ParticleInsert (src/simulator/neighbor/neighborShader.ts:24-32)
+//   nbr_count / nbr_list   NeighborCount / NeighborList (neighborShader.ts:101-246)
+//   lambda                 BoundaryVolume (boundaryVolume.ts:26-57) + LambdaCalculation
+//                          (src/simulator/PBF/shader/pressureConstrain.ts:31-85)
+//   deltap                 ConstrainSolve + ConstrainApply (pressureConstrain.ts:109-179)
+//   density_velocity       AttributeUpdate (attributeUpdate.ts:25-59)
+//   vorticity              VorticityConfinement (vorticityConfinement.ts:25-66)
+//   xsph                   XSPH + vorticity force + surface tension (XSPH.ts:31-92)
+#pragma once
+
+#include "pbf_device.cuh"
+#include "pbf_kernels.h"
+
+namespace pbf {
+namespace PBF_NS {
+
+constexpr uint32_t kFull = 0xffffffffu;
+constexpr uint32_t kNoKey = 0xffffffffu;
+
+// Warp-aggregated count: lanes with equal keys elect one leader that does a
+// single atomicAdd for all of them; each lane's rank = leader's base + its
+// position among its peers.
+__device__ __forceinline__ uint32_t warp_aggregated_rank(uint32_t* cell_count, uint32_t key) {
+  const uint32_t lane = threadIdx.x & 31u;
+  uint32_t peers = __match_any_sync(kFull, key);
+  uint32_t leader = __ffs(peers) - 1;
+  uint32_t base = 0;
+  if (lane == leader && key != kNoKey) base = atomicAdd(cell_count + key, (uint32_t)__popc(peers));
+  base = __shfl_sync(kFull, base, leader);
+  uint32_t lt = (1u << lane) - 1u;
+  return base + (uint32_t)__popc(peers & lt);
+}
+
+__device__ __forceinline__ uint32_t key_of(const GridParams& g, f3 x) {
+  int cx = cell_axis(x.x, g.origin[0], g.inv_cell[0], g.dim[0]);
+  int cy = cell_axis(x.y, g.origin[1], g.inv_cell[1], g.dim[1]);
+  int cz = cell_axis(x.z, g.origin[2], g.inv_cell[2], g.dim[2]);
+  return cell_key(cx, cy, cz, g);
+}
+
+// predict x* (TimeIntegration), its cell key and within-cell rank (ParticleInsert).
+__global__ void __launch_bounds__(256) k_predict(SimParams p, GridParams g, const float4* __restrict__ pos,
+                                                 const float4* __restrict__ vel, const float4* __restrict__ acc,
+                                                 float4* __restrict__ xs_out, uint32_t* __restrict__ key_out,
+                                                 uint32_t* __restrict__ rank_out, uint32_t* cell_count) {
+  uint32_t s = blockIdx.x * blockDim.x + threadIdx.x;
+  uint32_t key = kNoKey;
+  if (s < p.n) {
+    f3 x = xyz(pos[s]);
+    f3 v = xyz(vel[s]);
+    f3 a = xyz(acc[s]);
+    f3 gv = mk(0.0f + a.x, p.gy + a.y, 0.0f + a.z);
+    f3 vp = v + p.dt * gv;
+    f3 xp = clamp_rand(p, x + p.dt * vp);
+    xs_out[s] = f4(xp, 0.0f);
+    key = key_of(g, xp);
+    key_out[s] = key;
+  }
+  uint32_t rank = warp_aggregated_rank(cell_count, key);
+  if (s < p.n) rank_out[s] = rank;
+}
+
+// Range of slots covering cells (cx+dx, cy+dy, cz-1 .. cz+1): the 27-cell
+// neighbourhood is 9 runs of consecutive keys because keys are z-fastest.
+struct Run {
+  uint32_t b, e;
+};
+__device__ __forceinline__ Run run_of(const GridParams& g, const uint32_t* __restrict__ cell_start, int cx, int cy,
+                                      int cz, int dx, int dy) {
+  int x = cx + dx, y = cy + dy;
+  if (x < 0 || y < 0 || x >= g.dim[0] || y >= g.dim[1]) return Run{0, 0};
+  int zlo = max(cz - 1, 0), zhi = min(cz + 1, g.dim[2] - 1);
+  uint32_t k0 = cell_key(x, y, zlo, g), k1 = cell_key(x, y, zhi, g) + 1u;
+  return Run{__ldg(cell_start + k0), __ldg(cell_start + k1)};
+}
+
+// NeighborCount: neighbours within h of x*, self included, 27 cells in key order.
+__global__ void __launch_bounds__(256) k_nbr_count(SimParams p, GridParams g, const float4* __restrict__ xs,
+                                                   const uint32_t* __restrict__ cell_start,
+                                                   uint32_t* __restrict__ nbr_count) {
+  uint32_t t = blockIdx.x * blockDim.x + threadIdx.x;
+  if (t > p.n) return;
+  if (t == p.n) {
+    nbr_count[t] = 0;
+    return;
+  }
+  f3 xi = xyz(xs[t]);
+  int cx = cell_axis(xi.x, g.origin[0], g.inv_cell[0], g.dim[0]);
+  int cy = cell_axis(xi.y, g.origin[1], g.inv_cell[1], g.dim[1]);
+  int cz = cell_axis(xi.z, g.origin[2], g.inv_cell[2], g.dim[2]);
+  uint32_t cnt = 0;
+  for (int dx = -1; dx <= 1; ++dx)
+    for (int dy = -1; dy <= 1; ++dy) {
+      Run r = run_of(g, cell_start, cx, cy, cz, dx, dy);
+      for (uint32_t u = r.b; u < r.e; ++u) {
+        f3 d = xyz(__ldg(xs + u)) - xi;
+        if (dot3(d, d) <= p.h2) ++cnt;
+      }
+    }
+  nbr_count[t] = cnt;
+}
+
+// NeighborList: the same traversal writing slot indices at nbr_offset[t].
+__global__ void __launch_bounds__(256) k_nbr_list(SimParams p, GridParams g, const float4* __restrict__ xs,
+                                                  const uint32_t* __restrict__ cell_start,
+                                                  const uint32_t* __restrict__ nbr_offset, uint32_t* __restrict__ nbr_list,
+                                                  uint32_t capacity, uint32_t* err) {
+  uint32_t t = blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= p.n) return;
+  if (t == 0 && nbr_offset[p.n] > capacity) atomicOr(err, 0x1u);
+  f3 xi = xyz(xs[t]);
+  int cx = cell_axis(xi.x, g.origin[0], g.inv_cell[0], g.dim[0]);
+  int cy = cell_axis(xi.y, g.origin[1], g.inv_cell[1], g.dim[1]);
+  int cz = cell_axis(xi.z, g.origin[2], g.inv_cell[2], g.dim[2]);
+  uint32_t o = nbr_offset[t];
+  for (int dx = -1; dx <= 1; ++dx)
+    for (int dy = -1; dy <= 1; ++dy) {
+      Run r = run_of(g, cell_start, cx, cy, cz, dx, dy);
+      for (uint32_t u = r.b; u < r.e; ++u) {
+        f3 d = xyz(__ldg(xs + u)) - xi;
+        if (dot3(d, d) <= p.h2) {
+          if (o < capacity) nbr_list[o] = u;
+          ++o;
+        }
+      }
+    }
+}
+
+// Clamp a neighbour-list range to the list capacity (an overflowed list has
+// been flagged; the step's results are then invalid but no access is out of bounds).
+__device__ __forceinline__ void list_range(const uint32_t* __restrict__ off, uint32_t t, uint32_t cap, uint32_t& b,
+                                           uint32_t& e) {
+  b = min(__ldg(off + t), cap);
+  e = min(__ldg(off + t + 1), cap);
+}
+
+// BoundaryVolume + LambdaCalculation.
+__global__ void __launch_bounds__(256) k_lambda(SimParams p, FieldParams f, const float* __restrict__ sdf,
+                                                const float* __restrict__ vol, const float4* __restrict__ xs,
+                                                const uint32_t* __restrict__ nbr_offset,
+                                                const uint32_t* __restrict__ nbr_list, uint32_t cap,
+                                                float* __restrict__ lambda, float4* __restrict__ bdata) {
+  uint32_t t = blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= p.n) return;
+  f3 xi = xyz(xs[t]);
+  uint32_t b, e;
+  list_range(nbr_offset, t, cap, b, e);
+  f3 grad = mk(0.f, 0.f, 0.f);
+  float sum2 = 0.0f, dens = 0.0f;
+  for (uint32_t q = b; q < e; ++q) {
+    uint32_t j = __ldg(nbr_list + q);
+    f3 d = xi - xyz(__ldg(xs + j));
+    float rl = len3(d);
+    f3 gk = spiky_grad(p, d, rl);
+    grad = grad + gk;
+    sum2 = sum2 + dot3(gk, gk);
+    dens = dens + poly6(p, rl);
+  }
+  dens = dens * p.V;
+  grad = p.V * grad;
+  sum2 = sum2 * p.V2;
+  float4 bd = make_float4(0.f, 0.f, 0.f, 0.f);
+  if (f.loaded) {
+    bd = boundary_sample(p, f, sdf, vol, xi);
+    if (bd.w != 0.0f) {
+      f3 d = xi - xyz(bd);
+      float rl = len3(d);
+      f3 gk = bd.w * spiky_grad(p, d, rl);
+      grad = grad + gk;
+      dens = dens + bd.w * poly6(p, rl);
+    }
+    bdata[t] = bd;
+  }
+  float c = fmaxf(0.0f, dens - 1.0f);
+  float s = dot3(grad, grad) + sum2;
+  lambda[t] = -c / (s + p.lambda_eps);
+}
+
+// ConstrainSolve + ConstrainApply: x*_new = clamp(x* + 0.5 * dp) into the other buffer.
+__global__ void __launch_bounds__(256) k_deltap(SimParams p, int have_field, const float4* __restrict__ xs,
+                                                const float* __restrict__ lambda, const float4* __restrict__ bdata,
+                                                const uint32_t* __restrict__ nbr_offset,
+                                                const uint32_t* __restrict__ nbr_list, uint32_t cap,
+                                                float4* __restrict__ xs_out, float4* __restrict__ dp_out) {
+  uint32_t t = blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= p.n) return;
+  f3 xi = xyz(xs[t]);
+  float li = lambda[t];
+  uint32_t b, e;
+  list_range(nbr_offset, t, cap, b, e);
+  f3 pu = mk(0.f, 0.f, 0.f);
+  for (uint32_t q = b; q < e; ++q) {
+    uint32_t j = __ldg(nbr_list + q);
+    f3 d = xi - xyz(__ldg(xs + j));
+    float rl = len3(d);
+    float lj = __ldg(lambda + j);
+    pu = pu + (li + lj) * spiky_grad(p, d, rl);
+  }
+  pu = p.V * pu;
+  if (have_field) {
+    float4 bd = bdata[t];
+    if (bd.w != 0.0f) {
+      f3 d = xi - xyz(bd);
+      float rl = len3(d);
+      pu = pu + (bd.w * li) * spiky_grad(p, d, rl);
+    }
+  }
+  f3 dp = 0.5f * pu;
+  if (dp_out) dp_out[t] = f4(dp, 0.0f);
+  xs_out[t] = f4(clamp_rand(p, xi + dp), 0.0f);
+}
+
+// AttributeUpdate: rho = m * sum W (fluid only), v = (x* - x) / dt, x <- (x*, rho).
+__global__ void __launch_bounds__(256) k_density_velocity(SimParams p, const float4* __restrict__ xs,
+                                                          const uint32_t* __restrict__ nbr_offset,
+                                                          const uint32_t* __restrict__ nbr_list, uint32_t cap,
+                                                          float4* __restrict__ pos, float4* __restrict__ vel) {
+  uint32_t t = blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= p.n) return;
+  f3 xi = xyz(xs[t]);
+  uint32_t b, e;
+  list_range(nbr_offset, t, cap, b, e);
+  float dens = 0.0f;
+  for (uint32_t q = b; q < e; ++q) {
+    uint32_t j = __ldg(nbr_list + q);
+    f3 d = xi - xyz(__ldg(xs + j));
+    dens = dens + poly6(p, len3(d));
+  }
+  dens = dens * p.m;
+  f3 xo = xyz(pos[t]);
+  vel[t] = f4(p.inv_dt * (xi - xo), 0.0f);
+  pos[t] = f4(xi, dens);
+}
+
+// VorticityConfinement: omega_i and the Akinci normal n_i.
+__global__ void __launch_bounds__(256) k_vorticity(SimParams p, const float4* __restrict__ pos,
+                                                   const float4* __restrict__ vel,
+                                                   const uint32_t* __restrict__ nbr_offset,
+                                                   const uint32_t* __restrict__ nbr_list, uint32_t cap,
+                                                   float4* __restrict__ omega, float4* __restrict__ normal) {
+  uint32_t t = blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= p.n) return;
+  f3 xi = xyz(pos[t]);
+  f3 vi = xyz(vel[t]);
+  uint32_t b, e;
+  list_range(nbr_offset, t, cap, b, e);
+  f3 om = mk(0.f, 0.f, 0.f), nm = mk(0.f, 0.f, 0.f);
+  for (uint32_t q = b; q < e; ++q) {
+    uint32_t j = __ldg(nbr_list + q);
+    float4 pj = __ldg(pos + j);
+    f3 d = xi - xyz(pj);
+    float rl = len3(d);
+    f3 vd = xyz(__ldg(vel + j)) - vi;
+    float volume = p.m / pj.w;
+    f3 gw = spiky_grad(p, d, rl);
+    om = om + volume * cross3(vd, gw);
+    nm = nm + volume * gw;
+  }
+  omega[t] = f4(om, len3(om));
+  normal[t] = f4(p.h * nm, 0.0f);
+}
+
+// XSPH viscosity + vorticity confinement force + Akinci surface tension -> a.
+__global__ void __launch_bounds__(256) k_xsph(SimParams p, const float4* __restrict__ pos,
+                                              const float4* __restrict__ vel, const float4* __restrict__ omega,
+                                              const float4* __restrict__ normal,
+                                              const uint32_t* __restrict__ nbr_offset,
+                                              const uint32_t* __restrict__ nbr_list, uint32_t cap,
+                                              float4* __restrict__ acc) {
+  uint32_t t = blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= p.n) return;
+  float4 pi = pos[t];
+  f3 xi = xyz(pi);
+  float ri = pi.w;
+  f3 vi = xyz(vel[t]);
+  f3 wi = xyz(omega[t]);
+  f3 ni = xyz(normal[t]);
+  uint32_t b, e;
+  list_range(nbr_offset, t, cap, b, e);
+  f3 vu = mk(0.f, 0.f, 0.f), eta = mk(0.f, 0.f, 0.f), ten = mk(0.f, 0.f, 0.f);
+  for (uint32_t q = b; q < e; ++q) {
+    uint32_t j = __ldg(nbr_list + q);
+    float4 pj = __ldg(pos + j);
+    float rj = pj.w;
+    f3 d = xi - xyz(pj);
+    float rl = len3(d);
+    f3 vd = xyz(__ldg(vel + j)) - vi;
+    float kij = p.two_rho0 / (ri + rj);
+    vu = vu + divs(poly6(p, rl) * vd, rj);
+    eta = eta + divs(__ldg(&omega[j].w) * spiky_grad(p, d, rl), rj);
+    f3 coh = p.m * cohesion(p, d, rl);
+    f3 curv = ni - xyz(__ldg(normal + j));
+    ten = ten - kij * (coh + curv);
+  }
+  float el = len3(eta);
+  f3 en = (el > 0.0f) ? divs(eta, el) : mk(0.f, 0.f, 0.f);
+  float sx = p.xsph * p.inv_dt * p.m;
+  f3 a = (sx * vu + p.vorticity * cross3(en, wi)) + p.tension * ten;
+  acc[t] = f4(a, 0.0f);
+}
+
+// Launch table for this precision variant.
+void fill_pass_table(PassTable* tbl) {
+  tbl->predict = k_predict;
+  tbl->nbr_count = k_nbr_count;
+  tbl->nbr_list = k_nbr_list;
+  tbl->lambda = k_lambda;
+  tbl->deltap = k_deltap;
+  tbl->density_velocity = k_density_velocity;
+  tbl->vorticity = k_vorticity;
+  tbl->xsph = k_xsph;
+}
+
+}  // namespace PBF_NS
+}  // namespace pbf

@@ -1,0 +1,540 @@
+// pbf_sort.cu — integer pipeline of the neighbour search: single-pass
+// decoupled look-back exclusive scan, counting-sort scatter, stable
+// within-cell order by particle id, state gather, id-order export and the
+// per-step metrics reduction.
+//
+// Reference counterparts (relative to the reference root):
+//   ExclusiveScan.execute + scanShader.ts  src/simulator/neighbor/exclusiveScan.ts:134-166,
+//                                          src/simulator/neighbor/scanShader.ts:16-107
+//   ParticleInsert / CountingSort          src/simulator/neighbor/neighborShader.ts:24-60
+// The reference's within-cell order is the order its atomicAdd calls happened
+// to return; here it is defined as particle-id order (the sequential
+// semantics), which the sort below reproduces exactly whatever order the
+// warp-aggregated atomics ran in.
+#include <cstdint>
+#include <cuda_runtime.h>
+
+#include "../../include/pbf_gb300.h"
+#include "pbf_device.cuh"
+#include "pbf_kernels.h"
+
+namespace pbf {
+
+namespace {
+constexpr uint32_t kFull = 0xffffffffu;
+constexpr int kScanThreads = 256;
+constexpr int kScanItems = 8;
+constexpr int kScanTile = kScanThreads * kScanItems;  // 2048 elements per tile
+constexpr uint32_t kFlagAggregate = 1u, kFlagPrefix = 2u;
+constexpr uint32_t kSpinLimit = 1u << 22;             // ~ tens of ms at worst, then give up
+
+__device__ __forceinline__ unsigned long long ld_acquire_u64(const unsigned long long* p) {
+  unsigned long long v;
+  asm volatile("ld.acquire.gpu.global.u64 %0, [%1];" : "=l"(v) : "l"(p) : "memory");
+  return v;
+}
+__device__ __forceinline__ void st_release_u64(unsigned long long* p, unsigned long long v) {
+  asm volatile("st.release.gpu.global.u64 [%0], %1;" ::"l"(p), "l"(v) : "memory");
+}
+__device__ __forceinline__ unsigned long long pack(uint32_t flag, uint32_t value) {
+  return ((unsigned long long)flag << 32) | value;
+}
+
+// Block-wide exclusive scan of one value per thread; returns the block total in *total.
+__device__ __forceinline__ uint32_t block_exclusive(uint32_t v, uint32_t* total, uint32_t* warp_sums) {
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  uint32_t x = v;
+#pragma unroll
+  for (int o = 1; o < 32; o <<= 1) {
+    uint32_t y = __shfl_up_sync(kFull, x, o);
+    if (lane >= o) x += y;
+  }
+  if (lane == 31) warp_sums[warp] = x;
+  __syncthreads();
+  if (warp == 0) {
+    const int nw = blockDim.x >> 5;
+    uint32_t w = (lane < nw) ? warp_sums[lane] : 0u;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      uint32_t y = __shfl_up_sync(kFull, w, o);
+      if (lane >= o) w += y;
+    }
+    if (lane < nw) warp_sums[lane] = w;  // inclusive warp prefix
+  }
+  __syncthreads();
+  uint32_t warp_excl = (warp == 0) ? 0u : warp_sums[warp - 1];
+  *total = warp_sums[(blockDim.x >> 5) - 1];
+  return warp_excl + x - v;
+}
+
+// Single-pass scan: tiles take ids from a counter in launch order, publish
+// their aggregate, look back over predecessors (bounded waits) and publish
+// the inclusive prefix.  Status words pack (flag << 32 | value).
+__global__ void __launch_bounds__(kScanThreads) k_scan(const uint32_t* __restrict__ in, uint32_t* __restrict__ out,
+                                                       size_t n, unsigned long long* status, uint32_t* counter,
+                                                       uint32_t* err) {
+  __shared__ uint32_t s_items[kScanTile + kScanTile / 32];
+  __shared__ uint32_t s_warp[32];
+  __shared__ uint32_t s_tile;
+  __shared__ uint32_t s_prefix;
+  if (threadIdx.x == 0) s_tile = atomicAdd(counter, 1u);
+  __syncthreads();
+  const uint32_t tile = s_tile;
+  const size_t base = (size_t)tile * kScanTile;
+  // striped coalesced load, padded transpose to blocked order
+#pragma unroll
+  for (int k = 0; k < kScanItems; ++k) {
+    int li = k * kScanThreads + threadIdx.x;
+    size_t gi = base + li;
+    s_items[li + (li >> 5)] = (gi < n) ? __ldg(in + gi) : 0u;
+  }
+  __syncthreads();
+  uint32_t items[kScanItems];
+  uint32_t sum = 0;
+#pragma unroll
+  for (int k = 0; k < kScanItems; ++k) {
+    int li = threadIdx.x * kScanItems + k;
+    items[k] = s_items[li + (li >> 5)];
+    sum += items[k];
+  }
+  uint32_t total;
+  uint32_t texcl = block_exclusive(sum, &total, s_warp);
+  // look-back
+  if (threadIdx.x < 32) {
+    const int lane = threadIdx.x;
+    uint32_t prefix = 0;
+    if (tile == 0) {
+      if (lane == 0) st_release_u64(status + 0, pack(kFlagPrefix, total));
+    } else {
+      if (lane == 0) st_release_u64(status + tile, pack(kFlagAggregate, total));
+      long pred = (long)tile - 1;
+      bool done = false;
+      while (!done) {
+        long idx = pred - lane;
+        unsigned long long w = pack(kFlagPrefix, 0);  // lanes past tile 0 read as an empty prefix
+        uint32_t spins = 0;
+        if (idx >= 0) {
+          w = ld_acquire_u64(status + idx);
+          while ((uint32_t)(w >> 32) == 0u) {
+            if (++spins > kSpinLimit) {
+              atomicOr(err, (uint32_t)PBF_DEVERR_SCAN_TIMEOUT);
+              w = pack(kFlagPrefix, 0);
+              break;
+            }
+            __nanosleep(32);
+            w = ld_acquire_u64(status + idx);
+          }
+        }
+        uint32_t flag = (uint32_t)(w >> 32), val = (uint32_t)w;
+        uint32_t pmask = __ballot_sync(kFull, flag == kFlagPrefix);
+        // lanes up to (and including) the nearest prefix contribute
+        int stop = pmask ? (__ffs(pmask) - 1) : 31;
+        uint32_t contrib = (lane <= stop) ? val : 0u;
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) contrib += __shfl_xor_sync(kFull, contrib, o);
+        prefix += contrib;
+        if (pmask) done = true;
+        pred -= 32;
+      }
+      if (lane == 0) st_release_u64(status + tile, pack(kFlagPrefix, prefix + total));
+    }
+    if (lane == 0) s_prefix = prefix;
+  }
+  __syncthreads();
+  uint32_t run = s_prefix + texcl;
+#pragma unroll
+  for (int k = 0; k < kScanItems; ++k) {
+    int li = threadIdx.x * kScanItems + k;
+    s_items[li + (li >> 5)] = run;
+    run += items[k];
+  }
+  __syncthreads();
+#pragma unroll
+  for (int k = 0; k < kScanItems; ++k) {
+    int li = k * kScanThreads + threadIdx.x;
+    size_t gi = base + li;
+    if (gi < n) out[gi] = s_items[li + (li >> 5)];
+  }
+}
+
+// ---- insert (ParticleInsert on given positions; the step fuses this into predict) ----
+__global__ void __launch_bounds__(256) k_insert(GridParams g, const float4* __restrict__ pos, uint32_t n,
+                                                uint32_t* __restrict__ key, uint32_t* __restrict__ rank,
+                                                uint32_t* cell_count) {
+  uint32_t s = blockIdx.x * blockDim.x + threadIdx.x;
+  uint32_t k = 0xffffffffu;
+  if (s < n) {
+    float4 x = __ldg(pos + s);
+    int cx = cell_axis(x.x, g.origin[0], g.inv_cell[0], g.dim[0]);
+    int cy = cell_axis(x.y, g.origin[1], g.inv_cell[1], g.dim[1]);
+    int cz = cell_axis(x.z, g.origin[2], g.inv_cell[2], g.dim[2]);
+    k = cell_key(cx, cy, cz, g);
+    key[s] = k;
+  }
+  const uint32_t lane = threadIdx.x & 31u;
+  uint32_t peers = __match_any_sync(kFull, k);
+  uint32_t leader = __ffs(peers) - 1;
+  uint32_t b = 0;
+  if (lane == leader && k != 0xffffffffu) b = atomicAdd(cell_count + k, (uint32_t)__popc(peers));
+  b = __shfl_sync(kFull, b, leader);
+  if (s < n) rank[s] = b + (uint32_t)__popc(peers & ((1u << lane) - 1u));
+}
+
+// ---- counting-sort scatter (CountingSort, neighborShader.ts:49-60) -----------------
+__global__ void __launch_bounds__(256) k_scatter(uint32_t n, const uint32_t* __restrict__ key,
+                                                 const uint32_t* __restrict__ rank, const uint32_t* __restrict__ cell_start,
+                                                 const uint32_t* __restrict__ ids, uint32_t* __restrict__ perm_raw,
+                                                 uint32_t* __restrict__ id_raw) {
+  uint32_t s = blockIdx.x * blockDim.x + threadIdx.x;
+  if (s >= n) return;
+  uint32_t k = key[s];
+  uint32_t dst = __ldg(cell_start + k) + rank[s];
+  perm_raw[dst] = s;
+  id_raw[dst] = ids ? __ldg(ids + s) : s;
+}
+
+// ---- stable within-cell order ------------------------------------------------------
+// One warp per cell.  Cells with <= 32 entries rank in registers; up to
+// kWarpMax by warp-wide counting; larger cells go to the block radix path.
+constexpr uint32_t kWarpMax = 1024;
+
+__global__ void __launch_bounds__(256) k_cellfix(uint32_t cells, const uint32_t* __restrict__ cell_count,
+                                                 const uint32_t* __restrict__ cell_start,
+                                                 const uint32_t* __restrict__ perm_raw,
+                                                 const uint32_t* __restrict__ id_raw, uint32_t* __restrict__ perm,
+                                                 uint32_t* big_list, uint32_t* big_count) {
+  const uint32_t lane = threadIdx.x & 31u;
+  const uint32_t warp_global = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const uint32_t nwarps = (gridDim.x * blockDim.x) >> 5;
+  for (uint32_t c = warp_global; c < cells; c += nwarps) {
+    uint32_t cnt = __ldg(cell_count + c);
+    if (cnt == 0) continue;
+    uint32_t st = __ldg(cell_start + c);
+    if (cnt == 1) {
+      if (lane == 0) perm[st] = perm_raw[st];
+      continue;
+    }
+    if (cnt <= 32) {
+      uint32_t my_id = 0xffffffffu, my_slot = 0;
+      if (lane < cnt) {
+        my_id = id_raw[st + lane];
+        my_slot = perm_raw[st + lane];
+      }
+      uint32_t r = 0;
+      for (uint32_t m = 0; m < cnt; ++m) {
+        uint32_t other = __shfl_sync(kFull, my_id, m);
+        r += (other < my_id) ? 1u : 0u;
+      }
+      if (lane < cnt) perm[st + r] = my_slot;
+    } else if (cnt <= kWarpMax) {
+      for (uint32_t e = lane; e < cnt; e += 32) {
+        uint32_t my_id = id_raw[st + e];
+        uint32_t r = 0;
+        for (uint32_t m = 0; m < cnt; ++m) r += (__ldg(id_raw + st + m) < my_id) ? 1u : 0u;
+        perm[st + r] = perm_raw[st + e];
+      }
+    } else {
+      if (lane == 0) {
+        uint32_t q = atomicAdd(big_count, 1u);
+        big_list[q] = c;
+      }
+    }
+  }
+}
+
+// Block LSD radix sort (8-bit digits) of one very full cell by particle id;
+// stable because tiles are processed in order and ranks within a tile follow
+// thread order.
+constexpr int kRadixThreads = 256;
+__global__ void __launch_bounds__(kRadixThreads) k_bigcell(const uint32_t* __restrict__ big_list,
+                                                           const uint32_t* __restrict__ big_count,
+                                                           const uint32_t* __restrict__ cell_count,
+                                                           const uint32_t* __restrict__ cell_start,
+                                                           uint32_t* __restrict__ perm_raw, uint32_t* __restrict__ id_raw,
+                                                           uint32_t* __restrict__ perm, uint32_t* __restrict__ tmp_slot,
+                                                           uint32_t* __restrict__ tmp_id, int passes) {
+  __shared__ uint32_t s_base[256];
+  __shared__ uint32_t s_wcount[kRadixThreads / 32][256];
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  const uint32_t nb = *big_count;
+  for (uint32_t bi = blockIdx.x; bi < nb; bi += gridDim.x) {
+    const uint32_t c = big_list[bi];
+    const uint32_t cnt = cell_count[c], st = cell_start[c];
+    // ping-pong between the cell's own segments of (perm_raw, id_raw) and (tmp_slot, tmp_id);
+    // the last pass writes the slots straight into perm.
+    uint32_t* src_slot = perm_raw + st;
+    uint32_t* src_id = id_raw + st;
+    for (int pass = 0; pass < passes; ++pass) {
+      const int shift = 8 * pass;
+      const bool even = (pass & 1) == 0;
+      uint32_t* dst_slot = (even ? tmp_slot : perm_raw) + st;
+      uint32_t* dst_id = (even ? tmp_id : id_raw) + st;
+      if (pass == passes - 1) dst_slot = perm + st;
+      // histogram
+      for (int d = tid; d < 256; d += kRadixThreads) s_base[d] = 0;
+      __syncthreads();
+      for (uint32_t e = tid; e < cnt; e += kRadixThreads) atomicAdd(&s_base[(src_id[e] >> shift) & 255u], 1u);
+      __syncthreads();
+      if (tid == 0) {
+        uint32_t run = 0;
+        for (int d = 0; d < 256; ++d) {
+          uint32_t v = s_base[d];
+          s_base[d] = run;
+          run += v;
+        }
+      }
+      __syncthreads();
+      for (uint32_t t0 = 0; t0 < cnt; t0 += kRadixThreads) {
+        for (int q = tid; q < (kRadixThreads / 32) * 256; q += kRadixThreads) (&s_wcount[0][0])[q] = 0;
+        __syncthreads();
+        uint32_t e = t0 + tid;
+        bool valid = e < cnt;
+        uint32_t d = valid ? ((src_id[e] >> shift) & 255u) : 256u;
+        uint32_t peers = __match_any_sync(kFull, d);
+        uint32_t lrank = __popc(peers & ((1u << lane) - 1u));
+        if (valid && lrank == 0) s_wcount[warp][d] = __popc(peers);
+        __syncthreads();
+        if (valid) {
+          uint32_t r = s_base[d] + lrank;
+          for (int w = 0; w < warp; ++w) r += s_wcount[w][d];
+          dst_slot[r] = src_slot[e];
+          dst_id[r] = src_id[e];
+        }
+        __syncthreads();
+        for (int dd = tid; dd < 256; dd += kRadixThreads) {
+          uint32_t add = 0;
+          for (int w = 0; w < kRadixThreads / 32; ++w) add += s_wcount[w][dd];
+          s_base[dd] += add;
+        }
+        __syncthreads();
+      }
+      src_slot = dst_slot;
+      src_id = dst_id;
+      __syncthreads();
+    }
+  }
+}
+
+// ---- gather of the particle state into the new order -------------------------------
+__global__ void __launch_bounds__(256) k_gather(uint32_t n, const uint32_t* __restrict__ perm,
+                                                const float4* __restrict__ pos_in, const float4* __restrict__ xs_in,
+                                                const uint32_t* __restrict__ id_in, float4* __restrict__ pos_out,
+                                                float4* __restrict__ xs_out, uint32_t* __restrict__ id_out) {
+  uint32_t t = blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= n) return;
+  uint32_t o = perm[t];
+  pos_out[t] = __ldg(pos_in + o);
+  xs_out[t] = __ldg(xs_in + o);
+  id_out[t] = __ldg(id_in + o);
+}
+
+__global__ void k_rank_from_order(uint32_t n, const uint32_t* __restrict__ perm, const uint32_t* __restrict__ key,
+                                  const uint32_t* __restrict__ cell_start, uint32_t* __restrict__ rank_out) {
+  uint32_t t = blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= n) return;
+  uint32_t s = perm[t];
+  rank_out[s] = t - cell_start[key[s]];
+}
+
+__global__ void k_scatter_f4(uint32_t n, const uint32_t* __restrict__ id, const float4* __restrict__ src,
+                             float4* __restrict__ dst) {
+  uint32_t t = blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= n) return;
+  dst[id[t]] = src[t];
+}
+__global__ void k_scatter_u32(uint32_t n, const uint32_t* __restrict__ id, const uint32_t* __restrict__ src,
+                              uint32_t* __restrict__ dst) {
+  uint32_t t = blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= n) return;
+  dst[id[t]] = src[t];
+}
+__global__ void k_scatter_f32(uint32_t n, const uint32_t* __restrict__ id, const float* __restrict__ src,
+                              float* __restrict__ dst) {
+  uint32_t t = blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= n) return;
+  dst[id[t]] = src[t];
+}
+__global__ void k_list_to_ids(uint32_t total, const uint32_t* __restrict__ list, const uint32_t* __restrict__ id,
+                              uint32_t* __restrict__ out) {
+  uint32_t q = blockIdx.x * blockDim.x + threadIdx.x;
+  if (q >= total) return;
+  out[q] = id[list[q]];
+}
+__global__ void k_copy_runs(uint32_t n, const uint32_t* __restrict__ slot_off, const uint32_t* __restrict__ id_off,
+                            const uint32_t* __restrict__ ids, const uint32_t* __restrict__ src, uint32_t* __restrict__ dst) {
+  uint32_t t = blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= n) return;
+  uint32_t b = slot_off[t], e = slot_off[t + 1], o = id_off[ids[t]];
+  for (uint32_t q = b; q < e; ++q) dst[o + (q - b)] = src[q];
+}
+__global__ void k_count_from_offsets(uint32_t n, const uint32_t* __restrict__ off, uint32_t* __restrict__ cnt) {
+  uint32_t t = blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= n) return;
+  cnt[t] = off[t + 1] - off[t];
+}
+
+// ---- metrics --------------------------------------------------------------------------
+__device__ __forceinline__ void atomic_max_pos_float(float* addr, float v) {
+  // v >= 0: the int ordering of non-negative floats matches their value ordering
+  atomicMax(reinterpret_cast<int*>(addr), __float_as_int(v));
+}
+__global__ void __launch_bounds__(256) k_metrics(SimParams p, FieldParams f, const float* __restrict__ sdf,
+                                                 const float4* __restrict__ pos, const float4* __restrict__ vel,
+                                                 uint32_t n, float* accum_f, double* accum_d, uint32_t* accum_u) {
+  uint32_t t = blockIdx.x * blockDim.x + threadIdx.x;
+  float comp = 0.f, aerr = 0.f;
+  double ke = 0.0, serr = 0.0;
+  uint32_t bad = 0, pen = 0;
+  if (t < n) {
+    float4 x = pos[t];
+    float4 v = vel[t];
+    bool fin = isfinite(x.x) && isfinite(x.y) && isfinite(x.z) && isfinite(v.x) && isfinite(v.y) && isfinite(v.z);
+    if (!fin) {
+      bad = 1;
+    } else {
+      float e = x.w / p.rho0 - 1.0f;
+      comp = fmaxf(0.0f, e);
+      aerr = fabsf(e);
+      serr = aerr;
+      ke = 0.5 * (double)p.m * ((double)v.x * v.x + (double)v.y * v.y + (double)v.z * v.z);
+      if (f.loaded && sdf) {
+        CellLoc L = field_locate(f, mk(x.x, x.y, x.z));
+        uint32_t idx[32];
+        cell_nodes(f, L.i, L.j, L.k, false, idx);
+        float N[32];
+        f3 dN[32];
+        float val[32];
+        shape32(L.s, N, dN);
+        for (int q = 0; q < 32; ++q) val[q] = sdf[idx[q]];
+        if (sum32(N, val) < 0.0f) pen = 1;
+      }
+    }
+  }
+  // warp reduce then one atomic per warp
+  for (int o = 16; o > 0; o >>= 1) {
+    comp = fmaxf(comp, __shfl_xor_sync(kFull, comp, o));
+    aerr = fmaxf(aerr, __shfl_xor_sync(kFull, aerr, o));
+    ke += __shfl_xor_sync(kFull, ke, o);
+    serr += __shfl_xor_sync(kFull, serr, o);
+    bad += __shfl_xor_sync(kFull, bad, o);
+    pen += __shfl_xor_sync(kFull, pen, o);
+  }
+  if ((threadIdx.x & 31) == 0) {
+    atomic_max_pos_float(accum_f + 0, comp);
+    atomic_max_pos_float(accum_f + 1, aerr);
+    atomicAdd(accum_d + 0, serr);
+    atomicAdd(accum_d + 1, ke);
+    atomicAdd(accum_u + 0, bad);
+    atomicAdd(accum_u + 1, pen);
+  }
+}
+
+inline unsigned blocks_for(size_t n, int threads) { return (unsigned)((n + threads - 1) / threads); }
+
+}  // namespace
+
+size_t scan_scratch_bytes(size_t n) {
+  size_t tiles = (n + kScanTile - 1) / kScanTile;
+  if (tiles == 0) tiles = 1;
+  return 256 + tiles * sizeof(unsigned long long);
+}
+
+cudaError_t launch_exclusive_scan(const uint32_t* in, uint32_t* out, size_t n, void* scratch, uint32_t* err,
+                                  cudaStream_t st) {
+  if (n == 0) return cudaSuccess;
+  size_t tiles = (n + kScanTile - 1) / kScanTile;
+  cudaError_t e = cudaMemsetAsync(scratch, 0, scan_scratch_bytes(n), st);
+  if (e != cudaSuccess) return e;
+  uint32_t* counter = reinterpret_cast<uint32_t*>(scratch);
+  unsigned long long* status = reinterpret_cast<unsigned long long*>(reinterpret_cast<char*>(scratch) + 256);
+  k_scan<<<(unsigned)tiles, kScanThreads, 0, st>>>(in, out, n, status, counter, err);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_insert(GridParams g, const float4* pos, uint32_t n, uint32_t* key, uint32_t* rank,
+                          uint32_t* cell_count, cudaStream_t st) {
+  if (n == 0) return cudaSuccess;
+  k_insert<<<blocks_for(n, 256), 256, 0, st>>>(g, pos, n, key, rank, cell_count);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_sort_by_cell(GridParams g, uint32_t n, const uint32_t* ids, SortBuffers& b, uint32_t id_bits,
+                                cudaStream_t st) {
+  cudaError_t e = launch_exclusive_scan(b.cell_count, b.cell_start, (size_t)g.cells + 1, b.scan_scratch, b.err, st);
+  if (e != cudaSuccess) return e;
+  if (n == 0) return cudaSuccess;
+  k_scatter<<<blocks_for(n, 256), 256, 0, st>>>(n, b.key, b.rank, b.cell_start, ids, b.perm_raw, b.id_raw);
+  e = cudaMemsetAsync(b.big_count, 0, sizeof(uint32_t), st);
+  if (e != cudaSuccess) return e;
+  {
+    unsigned warps_needed = g.cells;
+    unsigned blocks = (unsigned)((warps_needed + 7) / 8);
+    if (blocks > 152u * 16u) blocks = 152u * 16u;
+    if (blocks == 0) blocks = 1;
+    k_cellfix<<<blocks, 256, 0, st>>>(g.cells, b.cell_count, b.cell_start, b.perm_raw, b.id_raw, b.perm, b.big_list,
+                                      b.big_count);
+  }
+  int passes = (int)((id_bits + 7) / 8);
+  if (passes < 1) passes = 1;
+  k_bigcell<<<152, kRadixThreads, 0, st>>>(b.big_list, b.big_count, b.cell_count, b.cell_start, b.perm_raw, b.id_raw,
+                                           b.perm, b.tmp_a, b.tmp_b, passes);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_gather_state(uint32_t n, const uint32_t* perm, const float4* pos_in, const float4* xs_in,
+                                const uint32_t* id_in, float4* pos_out, float4* xs_out, uint32_t* id_out,
+                                cudaStream_t st) {
+  if (n == 0) return cudaSuccess;
+  k_gather<<<blocks_for(n, 256), 256, 0, st>>>(n, perm, pos_in, xs_in, id_in, pos_out, xs_out, id_out);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_rank_from_order(uint32_t n, const uint32_t* perm, const uint32_t* key, const uint32_t* cell_start,
+                                   uint32_t* rank_out, cudaStream_t st) {
+  if (n == 0) return cudaSuccess;
+  k_rank_from_order<<<blocks_for(n, 256), 256, 0, st>>>(n, perm, key, cell_start, rank_out);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_scatter_by_id(uint32_t n, const uint32_t* id, const float4* src, float4* dst, cudaStream_t st) {
+  if (n == 0) return cudaSuccess;
+  k_scatter_f4<<<blocks_for(n, 256), 256, 0, st>>>(n, id, src, dst);
+  return cudaGetLastError();
+}
+cudaError_t launch_scatter_by_id_u32(uint32_t n, const uint32_t* id, const uint32_t* src, uint32_t* dst,
+                                     cudaStream_t st) {
+  if (n == 0) return cudaSuccess;
+  k_scatter_u32<<<blocks_for(n, 256), 256, 0, st>>>(n, id, src, dst);
+  return cudaGetLastError();
+}
+cudaError_t launch_scatter_by_id_f32(uint32_t n, const uint32_t* id, const float* src, float* dst, cudaStream_t st) {
+  if (n == 0) return cudaSuccess;
+  k_scatter_f32<<<blocks_for(n, 256), 256, 0, st>>>(n, id, src, dst);
+  return cudaGetLastError();
+}
+cudaError_t launch_list_to_ids(uint32_t total, const uint32_t* list, const uint32_t* id, uint32_t* out,
+                               cudaStream_t st) {
+  if (total == 0) return cudaSuccess;
+  k_list_to_ids<<<blocks_for(total, 256), 256, 0, st>>>(total, list, id, out);
+  return cudaGetLastError();
+}
+cudaError_t launch_copy_runs(uint32_t n, const uint32_t* slot_off, const uint32_t* id_off, const uint32_t* ids,
+                             const uint32_t* src, uint32_t* dst, cudaStream_t st) {
+  if (n == 0) return cudaSuccess;
+  k_copy_runs<<<blocks_for(n, 256), 256, 0, st>>>(n, slot_off, id_off, ids, src, dst);
+  return cudaGetLastError();
+}
+cudaError_t launch_nbr_count_sub(uint32_t n, const uint32_t* off, uint32_t* cnt, cudaStream_t st) {
+  if (n == 0) return cudaSuccess;
+  k_count_from_offsets<<<blocks_for(n, 256), 256, 0, st>>>(n, off, cnt);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_metrics(SimParams p, FieldParams f, const float* sdf, const float4* pos, const float4* vel,
+                           uint32_t n, float* accum_f, double* accum_d, uint32_t* accum_u, cudaStream_t st) {
+  if (n == 0) return cudaSuccess;
+  k_metrics<<<blocks_for(n, 256), 256, 0, st>>>(p, f, sdf, pos, vel, n, accum_f, accum_d, accum_u);
+  return cudaGetLastError();
+}
+
+}  // namespace pbf

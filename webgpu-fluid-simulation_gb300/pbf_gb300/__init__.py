@@ -1,0 +1,11 @@
+"""GB300-native Position Based Fluids substep (Python side of the C ABI).
+
+`PBF` mirrors the reference simulator's interface; `scenes` builds the
+reference presets and the benchmark workloads.  All compute runs in
+libpbf_gb300.so (CUDA, sm_103a).
+"""
+from . import _lib
+from .simulator import PBF, NeighborSearch, exclusive_scan
+from . import scenes
+
+__all__ = ["PBF", "NeighborSearch", "exclusive_scan", "scenes", "_lib"]

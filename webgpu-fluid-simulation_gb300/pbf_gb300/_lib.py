@@ -1,0 +1,147 @@
+"""ctypes binding of libpbf_gb300.so (include/pbf_gb300.h).
+
+The structures below mirror the C declarations field by field.  Loading
+fails loudly when the library has not been built: there is no CPU fallback.
+"""
+import ctypes
+import os
+
+_HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(os.path.dirname(_HERE), "_build", "libpbf_gb300.so")
+
+PBF_OK, PBF_EINVAL, PBF_ECAPACITY, PBF_EFORMAT, PBF_ECUDA, PBF_ETIMEOUT, PBF_EDIVERGED, PBF_ESTATE = range(8)
+STATUS_NAMES = {0: "PBF_OK", 1: "PBF_EINVAL", 2: "PBF_ECAPACITY", 3: "PBF_EFORMAT", 4: "PBF_ECUDA",
+                5: "PBF_ETIMEOUT", 6: "PBF_EDIVERGED", 7: "PBF_ESTATE"}
+JITTER_HASH, JITTER_SIN = 0, 1
+FP_FAST, FP_EXACT = 0, 1
+INTERP_CUBIC, INTERP_TRILINEAR = 0, 1
+(FIELD_POSITION, FIELD_VELOCITY, FIELD_ACCELERATION, FIELD_PREDICTED, FIELD_LAMBDA, FIELD_BOUNDARY,
+ FIELD_OMEGA, FIELD_NORMAL, FIELD_DELTA_P, FIELD_NEIGHBOR_COUNT) = range(10)
+SCALAR_FIELDS = {FIELD_LAMBDA: "f4", FIELD_NEIGHBOR_COUNT: "u4"}
+
+u32, f32 = ctypes.c_uint32, ctypes.c_float
+
+
+class Options(ctypes.Structure):
+    _fields_ = [("iterations", u32), ("xsph", f32), ("vorticity", f32), ("surface_tension", f32),
+                ("gravity", f32)]
+
+
+class Config(ctypes.Structure):
+    _fields_ = [("struct_size", u32), ("max_particles", u32), ("particle_radius", f32),
+                ("kernel_radius", f32), ("rest_density", f32), ("time_step", f32), ("substeps", u32),
+                ("domain_min", f32 * 3), ("domain_max", f32 * 3), ("grid_dim", u32 * 3),
+                ("lambda_eps", f32), ("wall_jitter", f32), ("jitter_mode", u32), ("volume_quirk", u32),
+                ("fp_mode", u32), ("boundary_interp", u32), ("max_neighbors", u32), ("options", Options),
+                ("stream", ctypes.c_void_p)]
+
+
+class Metrics(ctypes.Structure):
+    _fields_ = [("particles", u32), ("nonfinite", u32), ("penetrations", u32), ("error_flags", u32),
+                ("max_compression", f32), ("mean_abs_density_err", f32), ("max_abs_density_err", f32),
+                ("kinetic_energy", f32), ("neighbor_total", u32), ("fallback_steps", u32)]
+
+
+SHAPE_BOX_CONTAINER, SHAPE_SPHERE, SHAPE_CYLINDER, SHAPE_TORUS, SHAPE_BOX_SOLID = range(5)
+VOLMAP_OUTSIDE_EMPTY = 0x1
+VOLMAP_DISCRETE_SDF = 0x2
+
+
+class Shape(ctypes.Structure):
+    _fields_ = [("kind", u32), ("center", f32 * 3), ("size", f32 * 3)]
+
+
+class KernelTime(ctypes.Structure):
+    _fields_ = [("name", ctypes.c_char * 32), ("launches", u32), ("total_ms", f32)]
+
+
+class Grid(ctypes.Structure):
+    _fields_ = [("origin", f32 * 3), ("inv_cell", f32 * 3), ("dim", u32 * 3)]
+
+
+# Every symbol the header declares, with (restype, argtypes).
+_P = ctypes.c_void_p
+_FP = ctypes.POINTER(ctypes.c_float)
+_UP = ctypes.POINTER(ctypes.c_uint32)
+SIGNATURES = {
+    "pbf_abi_version": (ctypes.c_int, []),
+    "pbf_config_default": (ctypes.c_int, [ctypes.POINTER(Config)]),
+    "pbf_create": (ctypes.c_int, [ctypes.POINTER(Config), ctypes.POINTER(_P)]),
+    "pbf_destroy": (ctypes.c_int, [_P]),
+    "pbf_reset": (ctypes.c_int, [_P]),
+    "pbf_last_error": (ctypes.c_char_p, [_P]),
+    "pbf_set_options": (ctypes.c_int, [_P, ctypes.POINTER(Options)]),
+    "pbf_get_options": (ctypes.c_int, [_P, ctypes.POINTER(Options)]),
+    "pbf_voxelize_cube": (ctypes.c_int, [_P, _FP, _FP, _UP]),
+    "pbf_voxelize_sphere": (ctypes.c_int, [_P, _FP, ctypes.c_float, _UP]),
+    "pbf_jitter_particles": (ctypes.c_int, [_P, ctypes.c_float, ctypes.c_uint64]),
+    "pbf_host_particle_count": (ctypes.c_int, [_P, _UP]),
+    "pbf_copy_host_particles": (ctypes.c_int, [_P, _FP, u32]),
+    "pbf_set_particle_position": (ctypes.c_int, [_P]),
+    "pbf_set_particles": (ctypes.c_int, [_P, _FP, u32]),
+    "pbf_set_velocities": (ctypes.c_int, [_P, _FP, u32]),
+    "pbf_set_boundary_data": (ctypes.c_int, [_P, ctypes.c_char_p, ctypes.c_size_t]),
+    "pbf_set_boundary_field": (ctypes.c_int, [_P, _UP, _FP, _FP, _FP, _FP, ctypes.c_size_t]),
+    "pbf_clear_boundary": (ctypes.c_int, [_P]),
+    "pbf_field_length": (ctypes.c_size_t, [_UP]),
+    "pbf_run": (ctypes.c_int, [_P]),
+    "pbf_step": (ctypes.c_int, [_P, u32]),
+    "pbf_run_timestamp": (ctypes.c_int, [_P, _FP]),
+    "pbf_synchronize": (ctypes.c_int, [_P]),
+    "pbf_set_paused": (ctypes.c_int, [_P, ctypes.c_int]),
+    "pbf_is_paused": (ctypes.c_int, [_P]),
+    "pbf_enable_graph": (ctypes.c_int, [_P, ctypes.c_int]),
+    "pbf_particle_count": (u32, [_P]),
+    "pbf_position_device": (_P, [_P]),
+    "pbf_velocity_device": (_P, [_P]),
+    "pbf_copy_field": (ctypes.c_int, [_P, ctypes.c_int, _P, ctypes.c_size_t]),
+    "pbf_get_metrics": (ctypes.c_int, [_P, ctypes.POINTER(Metrics)]),
+    "pbf_set_capture": (ctypes.c_int, [_P, ctypes.c_int]),
+    "pbf_stream": (_P, [_P]),
+    "pbf_set_kernel_timing": (ctypes.c_int, [_P, ctypes.c_int]),
+    "pbf_get_kernel_timing": (ctypes.c_int, [_P, ctypes.POINTER(KernelTime), u32, _UP]),
+    "pbf_ns_create": (ctypes.c_int, [ctypes.POINTER(Grid), u32, _P, ctypes.POINTER(_P)]),
+    "pbf_ns_destroy": (ctypes.c_int, [_P]),
+    "pbf_ns_run": (ctypes.c_int, [_P, _P, u32, _P, _P, _P, _P, _P]),
+    "pbf_ns_lists": (ctypes.c_int, [_P, _P, u32, ctypes.c_float, _P, _P, u32, _UP]),
+    "pbf_ns_sync": (ctypes.c_int, [_P]),
+    "pbf_ns_last_error": (ctypes.c_char_p, [_P]),
+    "pbf_exclusive_scan_u32": (ctypes.c_int, [_P, _P, ctypes.c_size_t, _P]),
+    "pbf_generate_volume_map": (ctypes.c_int, [ctypes.POINTER(Shape), u32, _UP, _FP, _FP, ctypes.c_float, u32, u32,
+                                               _FP, _FP]),
+    "pbf_volume_from_sdf": (ctypes.c_int, [_UP, _FP, _FP, ctypes.c_float, u32, u32, _FP, _FP]),
+}
+
+_lib = None
+
+
+def load(path=None):
+    """Load the library (once) and attach the signatures."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    p = path or LIB_PATH
+    if not os.path.exists(p):
+        raise OSError("libpbf_gb300.so not built (%s); run webgpu-fluid-simulation_gb300/build_lib.py" % p)
+    lib = ctypes.CDLL(p)
+    for name, (res, args) in SIGNATURES.items():
+        fn = getattr(lib, name)
+        fn.restype = res
+        fn.argtypes = args
+    _lib = lib
+    return lib
+
+
+class PBFError(RuntimeError):
+    def __init__(self, code, msg):
+        super().__init__("%s: %s" % (STATUS_NAMES.get(code, code), msg))
+        self.code = code
+
+
+def default_config():
+    lib = load()
+    c = Config()
+    rc = lib.pbf_config_default(ctypes.byref(c))
+    if rc:
+        raise PBFError(rc, "pbf_config_default")
+    return c

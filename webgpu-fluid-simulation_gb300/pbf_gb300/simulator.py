@@ -1,0 +1,306 @@
+"""Python mirror of the reference simulator interface over the C ABI.
+
+The class `PBF` keeps the member names of the reference's TypeScript
+classes so that host code and tests read alike:
+  SPH        src/simulator/SPH.ts:7-208      (seeding, pause/start/stop, position buffer)
+  PBFConfig  src/simulator/PBF/PBFConfig.ts  (setConfig, setParticlePosition)
+  PBF        src/simulator/PBF/PBF.ts        (reset, setBoundaryData, run, runTimestamp, debug)
+All work runs in libpbf_gb300.so on the GPU; this file only marshals arguments.
+"""
+import ctypes
+
+import numpy as np
+
+from . import _lib as L
+
+
+def _f3(v):
+    return (ctypes.c_float * 3)(*[float(x) for x in v])
+
+
+class PBF:
+    """One simulator instance (one CUDA stream, device-resident state)."""
+
+    MAX_NEIGHBOR_COUNT = 60       # SPH.ts:25
+    KERNEL_RADIUS = 0.025         # SPH.ts:26
+    TIME_STEP = 1.0 / 300.0       # SPH.ts:27
+    MAX_PARTICLE_NUM = 1 << 17    # SPH.ts:24 (1 << 18 - 1 evaluates to 1 << 17)
+
+    def __init__(self, config=None, **overrides):
+        self._lib = L.load()
+        cfg = config if config is not None else L.default_config()
+        for k, v in overrides.items():
+            if k in ("domain_min", "domain_max"):
+                getattr(cfg, k)[:] = [float(x) for x in v]
+            elif k == "grid_dim":
+                cfg.grid_dim[:] = [int(x) for x in v]
+            elif k == "options":
+                for ok, ov in v.items():
+                    setattr(cfg.options, ok, ov)
+            else:
+                setattr(cfg, k, v)
+        cfg.struct_size = ctypes.sizeof(L.Config)
+        self.config = cfg
+        h = ctypes.c_void_p()
+        rc = self._lib.pbf_create(ctypes.byref(cfg), ctypes.byref(h))
+        if rc:
+            raise L.PBFError(rc, "pbf_create failed")
+        self._h = h
+
+    # ---- life cycle -------------------------------------------------------
+    def close(self):
+        if getattr(self, "_h", None):
+            self._lib.pbf_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+    def _check(self, rc, what):
+        if rc:
+            raise L.PBFError(rc, "%s: %s" % (what, self._lib.pbf_last_error(self._h).decode()))
+
+    def initResource(self):
+        """Buffers are allocated at construction (PBF.initResource, PBF.ts:262-279)."""
+        return None
+
+    def reset(self):
+        self._check(self._lib.pbf_reset(self._h), "reset")
+
+    # ---- config -----------------------------------------------------------
+    def setConfig(self, conf):
+        """PBFConfig.setConfig: {iteration, XSPH, vorticity, surfaceTension, gravity}."""
+        o = L.Options()
+        self._check(self._lib.pbf_get_options(self._h, ctypes.byref(o)), "get_options")
+        if "iteration" in conf:
+            o.iterations = int(conf["iteration"])
+        if "XSPH" in conf:
+            o.xsph = float(conf["XSPH"])
+        if "vorticity" in conf:
+            o.vorticity = float(conf["vorticity"])
+        if "surfaceTension" in conf:
+            o.surface_tension = float(conf["surfaceTension"])
+        if "gravity" in conf:
+            o.gravity = float(conf["gravity"])
+        self._check(self._lib.pbf_set_options(self._h, ctypes.byref(o)), "setConfig")
+
+    def optionsChange(self, e):
+        self.setConfig(e["object"] if isinstance(e, dict) and "object" in e else e)
+
+    # ---- seeding ------------------------------------------------------------
+    def voxelizeCube(self, mn, mx):
+        c = ctypes.c_uint32()
+        self._check(self._lib.pbf_voxelize_cube(self._h, _f3(mn), _f3(mx), ctypes.byref(c)), "voxelizeCube")
+        return c.value
+
+    def voxelizeSphere(self, center, radius):
+        c = ctypes.c_uint32()
+        self._check(self._lib.pbf_voxelize_sphere(self._h, _f3(center), float(radius), ctypes.byref(c)),
+                    "voxelizeSphere")
+        return c.value
+
+    def jitter(self, amplitude, seed):
+        self._check(self._lib.pbf_jitter_particles(self._h, float(amplitude), int(seed)), "jitter")
+
+    def hostParticles(self):
+        c = ctypes.c_uint32()
+        self._check(self._lib.pbf_host_particle_count(self._h, ctypes.byref(c)), "host count")
+        out = np.zeros((c.value, 4), dtype=np.float32)
+        self._check(self._lib.pbf_copy_host_particles(
+            self._h, out.ctypes.data_as(ctypes.POINTER(ctypes.c_float)), c.value), "host particles")
+        return out
+
+    def setParticlePosition(self):
+        self._check(self._lib.pbf_set_particle_position(self._h), "setParticlePosition")
+
+    def set_particles(self, xyzw):
+        a = np.ascontiguousarray(xyzw, dtype=np.float32)
+        if a.ndim != 2 or a.shape[1] != 4:
+            raise ValueError("positions must be (n, 4) float32")
+        self._check(self._lib.pbf_set_particles(
+            self._h, a.ctypes.data_as(ctypes.POINTER(ctypes.c_float)), a.shape[0]), "set_particles")
+
+    def set_velocities(self, xyzw):
+        a = np.ascontiguousarray(xyzw, dtype=np.float32)
+        self._check(self._lib.pbf_set_velocities(
+            self._h, a.ctypes.data_as(ctypes.POINTER(ctypes.c_float)), a.shape[0]), "set_velocities")
+
+    # ---- boundary -----------------------------------------------------------
+    def setBoundaryData(self, text):
+        b = text.encode() if isinstance(text, str) else bytes(text)
+        self._check(self._lib.pbf_set_boundary_data(self._h, b, len(b)), "setBoundaryData")
+
+    def set_boundary_field(self, res, origin, extent, sdf, vol):
+        r = (ctypes.c_uint32 * 3)(*[int(x) for x in res])
+        s = np.ascontiguousarray(sdf, dtype=np.float32)
+        v = np.ascontiguousarray(vol, dtype=np.float32)
+        fp = ctypes.POINTER(ctypes.c_float)
+        self._check(self._lib.pbf_set_boundary_field(self._h, r, _f3(origin), _f3(extent), s.ctypes.data_as(fp),
+                                                      v.ctypes.data_as(fp), s.size), "set_boundary_field")
+
+    def clear_boundary(self):
+        self._check(self._lib.pbf_clear_boundary(self._h), "clear_boundary")
+
+    # ---- stepping -----------------------------------------------------------
+    def run(self):
+        """One substep (PBF.run)."""
+        self._check(self._lib.pbf_run(self._h), "run")
+
+    def step(self, frames=1):
+        """`frames` x stepCount substeps (the controller loop, controller.ts:375-376)."""
+        self._check(self._lib.pbf_step(self._h, int(frames)), "step")
+
+    def runTimestamp(self):
+        ms = (ctypes.c_float * 4)()
+        self._check(self._lib.pbf_run_timestamp(self._h, ms), "runTimestamp")
+        return list(ms)
+
+    def synchronize(self):
+        self._check(self._lib.pbf_synchronize(self._h), "synchronize")
+
+    def enable_graph(self, on=True):
+        self._check(self._lib.pbf_enable_graph(self._h, 1 if on else 0), "enable_graph")
+
+    def set_capture(self, on=True):
+        self._check(self._lib.pbf_set_capture(self._h, 1 if on else 0), "set_capture")
+
+    def set_kernel_timing(self, on=True):
+        self._check(self._lib.pbf_set_kernel_timing(self._h, 1 if on else 0), "set_kernel_timing")
+
+    def kernel_timing(self):
+        """{pass name: (launches, total ms)} since the last call (synchronises)."""
+        buf = (L.KernelTime * 32)()
+        c = ctypes.c_uint32()
+        self._check(self._lib.pbf_get_kernel_timing(self._h, buf, 32, ctypes.byref(c)), "kernel_timing")
+        return {buf[i].name.decode(): (int(buf[i].launches), float(buf[i].total_ms)) for i in range(c.value)}
+
+    def update(self):
+        return None
+
+    # ---- pause (SPH.ts:82-84) ---------------------------------------------
+    @property
+    def pause(self):
+        return self._lib.pbf_is_paused(self._h) == 1
+
+    @pause.setter
+    def pause(self, v):
+        self._lib.pbf_set_paused(self._h, 1 if v else 0)
+
+    def switch(self):
+        self.pause = not self.pause
+
+    def stop(self):
+        self.pause = True
+
+    def start(self):
+        self.pause = False
+
+    # ---- state --------------------------------------------------------------
+    @property
+    def particleCount(self):
+        return int(self._lib.pbf_particle_count(self._h))
+
+    @property
+    def stepCount(self):
+        return int(self.config.substeps)
+
+    @property
+    def position(self):
+        """Device address of the float4 (x, rho) buffer, by particle id."""
+        return int(self._lib.pbf_position_device(self._h) or 0)
+
+    @property
+    def stream(self):
+        return int(self._lib.pbf_stream(self._h) or 0)
+
+    def copy_field(self, field):
+        n = self.particleCount
+        if field in L.SCALAR_FIELDS:
+            out = np.zeros(n, dtype=np.dtype(L.SCALAR_FIELDS[field]))
+        else:
+            out = np.zeros((n, 4), dtype=np.float32)
+        self._check(self._lib.pbf_copy_field(self._h, int(field), out.ctypes.data_as(ctypes.c_void_p),
+                                             out.nbytes), "copy_field")
+        return out
+
+    def positions(self):
+        return self.copy_field(L.FIELD_POSITION)
+
+    def velocities(self):
+        return self.copy_field(L.FIELD_VELOCITY)
+
+    def metrics(self):
+        m = L.Metrics()
+        self._check(self._lib.pbf_get_metrics(self._h, ctypes.byref(m)), "metrics")
+        return {k: getattr(m, k) for k, _ in L.Metrics._fields_}
+
+    def debug(self):
+        """PBF.debug (PBF.ts:514-573) read back the acceleration buffer; here
+        the same read-back plus the step metrics."""
+        return {"acceleration": self.copy_field(L.FIELD_ACCELERATION), "metrics": self.metrics()}
+
+
+class NeighborSearch:
+    """Stand-alone hash-grid search (NeighborSearch.execute, neighborSearch.ts:270-301)
+    on device pointers; see pbf_ns_run in include/pbf_gb300.h."""
+
+    def __init__(self, origin, inv_cell, dim, max_particles, stream=0):
+        self._lib = L.load()
+        g = L.Grid()
+        g.origin[:] = [float(x) for x in origin]
+        g.inv_cell[:] = [float(x) for x in inv_cell]
+        g.dim[:] = [int(x) for x in dim]
+        self.cells = int(dim[0]) * int(dim[1]) * int(dim[2])
+        h = ctypes.c_void_p()
+        rc = self._lib.pbf_ns_create(ctypes.byref(g), int(max_particles), ctypes.c_void_p(stream or None),
+                                     ctypes.byref(h))
+        if rc:
+            raise L.PBFError(rc, "pbf_ns_create")
+        self._h = h
+
+    def _check(self, rc, what):
+        if rc:
+            raise L.PBFError(rc, "%s: %s" % (what, self._lib.pbf_ns_last_error(self._h).decode()))
+
+    def run(self, d_pos4, n, d_keys=0, d_cell_count=0, d_cell_offset=0, d_order=0, d_rank=0):
+        v = lambda p: ctypes.c_void_p(p or None)
+        self._check(self._lib.pbf_ns_run(self._h, v(d_pos4), int(n), v(d_keys), v(d_cell_count),
+                                         v(d_cell_offset), v(d_order), v(d_rank)), "pbf_ns_run")
+
+    def lists(self, d_pos4, n, radius, d_offset, d_list, capacity):
+        tot = ctypes.c_uint32()
+        v = lambda p: ctypes.c_void_p(p or None)
+        rc = self._lib.pbf_ns_lists(self._h, v(d_pos4), int(n), float(radius), v(d_offset), v(d_list),
+                                    int(capacity), ctypes.byref(tot))
+        return rc, tot.value
+
+    def sync(self):
+        self._check(self._lib.pbf_ns_sync(self._h), "pbf_ns_sync")
+
+    def close(self):
+        if getattr(self, "_h", None):
+            self._lib.pbf_ns_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+def exclusive_scan(d_in, d_out, n, stream=0):
+    lib = L.load()
+    rc = lib.pbf_exclusive_scan_u32(ctypes.c_void_p(d_in), ctypes.c_void_p(d_out), int(n),
+                                    ctypes.c_void_p(stream or None))
+    if rc:
+        raise L.PBFError(rc, "pbf_exclusive_scan_u32")

@@ -53,6 +53,7 @@ ALG_BYTES = {
     "nbr_count": 20,          # read x*, write count
     "nbr_scan": 8,
     "nbr_list": 20,           # read x*, offset (+ 4 B per neighbour written, counted separately)
+    "boundary": 32,           # read x*, write (x_b, V_b)
     "lambda": 20,             # read x*, write lambda
     "deltap_apply": 36,       # read x*, lambda; write x*
     "density_velocity": 64,   # read x*, x; write v, (x, rho)
@@ -110,56 +111,87 @@ class Dist:
 
 # ---- clocks --------------------------------------------------------------------------------
 class ClockSampler:
-    QUERY = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
-             "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
-             "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+    """Samples SM clock and clock-event reasons during the timed region
+    (read-only NVML queries every 2 ms; falls back to nvidia-smi -lms 200)."""
+    REASONS = {0x4: "sw_power_cap", 0x8: "hw_slowdown", 0x20: "sw_thermal_slowdown", 0x40: "hw_thermal_slowdown",
+               0x80: "hw_power_brake_slowdown"}
 
     def __init__(self, gpu_index):
         self.idx = gpu_index
+        self.samples = []
+        self.max_mhz = None
+        self.stop_flag = threading.Event()
+        self.nvml = None
         self.proc = None
         self.lines = []
 
-    def start(self):
+    def _nvml_init(self):
         try:
-            self.proc = subprocess.Popen(["nvidia-smi", "--query-gpu=" + self.QUERY, "--format=csv,noheader,nounits",
-                                          "-i", str(self.idx), "-lms", "200"], stdout=subprocess.PIPE,
+            nv = ctypes.CDLL("libnvidia-ml.so.1")
+            if nv.nvmlInit_v2() != 0:
+                return False
+            h = ctypes.c_void_p()
+            if nv.nvmlDeviceGetHandleByIndex_v2(ctypes.c_uint(self.idx), ctypes.byref(h)) != 0:
+                return False
+            mx = ctypes.c_uint()
+            if nv.nvmlDeviceGetMaxClockInfo(h, ctypes.c_int(1), ctypes.byref(mx)) == 0:
+                self.max_mhz = float(mx.value)
+            self.nvml, self.handle = nv, h
+            fn = getattr(nv, "nvmlDeviceGetCurrentClocksEventReasons", None)
+            self.reason_fn = fn or nv.nvmlDeviceGetCurrentClocksThrottleReasons
+            return True
+        except Exception:
+            return False
+
+    def _poll(self):
+        c = ctypes.c_uint()
+        r = ctypes.c_ulonglong()
+        while not self.stop_flag.is_set():
+            if self.nvml.nvmlDeviceGetClockInfo(self.handle, ctypes.c_int(1), ctypes.byref(c)) == 0:
+                rr = r.value if self.reason_fn(self.handle, ctypes.byref(r)) == 0 else 0
+                self.samples.append((float(c.value), int(rr)))
+            time.sleep(0.002)
+
+    def start(self):
+        if self._nvml_init():
+            self.t = threading.Thread(target=self._poll, daemon=True)
+            self.t.start()
+            return
+        try:
+            q = "clocks.sm,clocks.max.sm,clocks_event_reasons.active"
+            self.proc = subprocess.Popen(["nvidia-smi", "--query-gpu=" + q, "--format=csv,noheader,nounits", "-i",
+                                          str(self.idx), "-lms", "200"], stdout=subprocess.PIPE,
                                          stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=lambda: [self.lines.append(x) for x in self.proc.stdout], daemon=True)
+            self.t.start()
         except Exception:
             self.proc = None
-            return
-        self.t = threading.Thread(target=self._read, daemon=True)
-        self.t.start()
-
-    def _read(self):
-        for line in self.proc.stdout:
-            self.lines.append(line.strip())
 
     def stop(self):
-        if not self.proc:
-            return None
-        self.proc.terminate()
-        try:
-            self.proc.wait(timeout=5)
-        except Exception:
-            self.proc.kill()
-        sm, smax, reasons = [], None, set()
-        for ln in self.lines:
-            f = [x.strip() for x in ln.split(",")]
-            if len(f) < 9:
-                continue
+        if self.nvml:
+            self.stop_flag.set()
+            self.t.join(timeout=2)
+        elif self.proc:
+            self.proc.terminate()
             try:
-                sm.append(float(f[1]))
-                smax = float(f[2])
-            except ValueError:
-                continue
-            names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
-            for nm, val in zip(names, f[5:9]):
-                if val.lower() == "active":
-                    reasons.add(nm)
-        if not sm:
+                self.proc.wait(timeout=5)
+            except Exception:
+                self.proc.kill()
+            for ln in self.lines:
+                f = [x.strip() for x in ln.split(",")]
+                try:
+                    self.samples.append((float(f[0]), int(f[2], 16)))
+                    self.max_mhz = float(f[1])
+                except (ValueError, IndexError):
+                    continue
+        if not self.samples:
             return None
-        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": smax, "reasons": sorted(reasons),
-                "samples": len(sm)}
+        seen = 0
+        for _, rr in self.samples:
+            seen |= rr
+        reasons = sorted(name for bit, name in self.REASONS.items() if seen & bit)
+        return {"sm_mhz": statistics.median(c for c, _ in self.samples), "sm_max_mhz": self.max_mhz,
+                "reasons": reasons, "samples": len(self.samples)}
 
 
 # ---- workload ------------------------------------------------------------------------------
@@ -188,19 +220,25 @@ def peaks():
 
 
 # ---- CPU restatement timing ----------------------------------------------------------------
-def cpu_sample(sc, particles_max, substeps):
-    """Time the CPU restatement on the first `particles_max` lattice particles."""
+def cpu_sample(sc, particles_max, substeps, min_seconds=10.0):
+    """Time the CPU restatement on the first `particles_max` lattice particles,
+    repeating frames until at least `min_seconds` of CPU work."""
     from oracle import oracle as O
     pts = sc.particles[:particles_max]
     o = O.Oracle(sc.config, 32)
     o.set_particles(pts)
     f = sc.field
     o.set_field(f["res"], f["origin"], f["extent"], f["sdf"], f["vol"])
+    done = 0
     t0 = time.perf_counter()
-    o.substep(substeps)
-    dt = time.perf_counter() - t0
+    while True:
+        o.substep(substeps)
+        done += substeps
+        dt = time.perf_counter() - t0
+        if dt >= min_seconds:
+            break
     o.close()
-    return len(pts) * substeps / dt, dt, len(pts), O.threads()
+    return len(pts) * done / dt, dt, len(pts), O.threads(), done
 
 
 def reference_arm(args, dist):
@@ -319,7 +357,7 @@ def gpu_arm(args, dist):
                 "share": tot_ms / total_ms if total_ms else None,
                 "passes": {k: {"launches": v[0], "ms": round(v[1], 4),
                                "share": round(v[1] / total_ms, 4) if total_ms else None} for k, v in kt.items()}}
-    launches_per_frame = sub * (12 + 2 * iters) + 1
+    launches_per_frame = sub * (12 + 3 * iters) + 1
     line = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": dist.world, "steps": args.steps,
         "warmup": max(args.warmup, 3), "ms_per_step": ms_max / args.steps, "higher_is_better": True,
@@ -334,10 +372,10 @@ def gpu_arm(args, dist):
     }
     sim.close()
     if dist.rank == 0 and dist.world == 1 and not args.no_cpu_baseline:
-        v, secs, cnt, cores = cpu_sample(sc, 262144, sub)
+        v, secs, cnt, cores, done = cpu_sample(sc, sc.n, sub)
         line["cpu_baseline"] = {"value": v, "unit": UNIT, "cores": cores, "kind": "port",
-                                "sample": "first %d lattice particles x %d substeps (%.1f s), CPU restatement"
-                                          % (cnt, sub, secs)}
+                                "sample": "%d particles x %d substeps (%.1f s) of the same scene from its initial "
+                                          "state, CPU restatement with OpenMP" % (cnt, done, secs)}
     if dist.rank == 0:
         print(json.dumps(line), flush=True)
 

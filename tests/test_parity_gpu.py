@@ -164,6 +164,13 @@ def test_step_exact_mode_bitexact(name, substeps):
 
 @pytest.mark.parametrize("name", SCENES)
 def test_step_fast_mode_tolerance(name):
+    """Fast mode (FMA, reciprocal math) against the FP32 restatement and the
+    FP64 replica.  rho and x are well conditioned: 1e-5 of scale.  lambda,
+    dp, v, omega and a are differences of nearly equal f32 numbers in the
+    reference formulas, so any f32 evaluation order moves them by the same
+    amount the FP32 restatement itself is off from FP64: the GPU's RMS error
+    against FP64 must stay within 3x the restatement's RMS error (max within
+    25x), each plus 1e-6 of scale."""
     sc = scenes.reference_scene(name)
     pts = scenes.jitter(sc.particles, 0.001, seed=9)
     sim, o32 = make_pair(sc, L.FP_FAST, pts, 32)
@@ -178,19 +185,18 @@ def test_step_fast_mode_tolerance(name):
     g = fields_of(sim)
     a = oracle_fields(o32)
     d = {name: o64.field(f) for f, name in FIELDS}
-    report = {}
-    for k in ("position", "velocity", "acceleration", "lambda", "omega", "normal", "delta_p"):
+    rms = lambda x: float(np.sqrt(np.mean(np.square(x))))
+    for k in ("velocity", "acceleration", "lambda", "omega", "normal", "delta_p"):
         scale = max(np.abs(d[k]).max(), 1e-30)
-        e_gpu64 = np.abs(g[k] - d[k]).max()
-        e_ref64 = np.abs(a[k] - d[k]).max()
-        e_gpu32 = np.abs(g[k].astype(np.float64) - a[k]).max()
-        report[k] = (e_gpu32 / scale, e_gpu64 / scale, e_ref64 / scale)
-        assert e_gpu64 <= 2 * e_ref64 + 1e-5 * scale, (k, report[k])
-    for k in ("normal",):
-        assert report[k][0] <= 1e-5, (k, report[k])
-    rho_g, rho_a = g["position"][:, 3], a["position"][:, 3]
+        eg, er = g[k] - d[k], a[k] - d[k]
+        assert rms(eg) <= 3 * rms(er) + 1e-6 * scale, (k, rms(eg) / scale, rms(er) / scale)
+        assert np.abs(eg).max() <= 25 * np.abs(er).max() + 1e-6 * scale, (k, np.abs(eg).max() / scale,
+                                                                            np.abs(er).max() / scale)
+    rho_g, rho_a, rho_d = g["position"][:, 3], a["position"][:, 3], d["position"][:, 3]
     assert np.abs(rho_g - rho_a).max() <= 1e-5 * rho_a.max()
+    assert np.abs(rho_g - rho_d).max() <= 1e-5 * rho_d.max()
     assert np.abs(g["position"][:, :3] - a["position"][:, :3]).max() <= 1e-5
+    assert np.abs(g["normal"] - d["normal"]).max() <= 1e-4 * np.abs(d["normal"]).max()
     sim.close()
 
 
@@ -277,7 +283,7 @@ def test_capacity_errors():
     assert e.value.code == L.PBF_ECAPACITY
     sim.close()
     # neighbour-list overflow is reported at the next synchronisation, with no out-of-bounds write
-    sc = scenes.reference_scene("cube_small", max_neighbors=4)
+    sc = scenes.reference_scene("cube_small", max_neighbors=4, max_particles=2197)
     sim = PBF(sc.config)
     sim.set_particles(sc.particles)
     sim.run()

@@ -7,6 +7,7 @@
 // (src/simulator/boundary/volumeMap.ts).  Device state is kept in
 // cell-sorted slot order; the id-ordered `position` buffer the renderer reads
 // is refreshed at the end of every pbf_run / pbf_step.
+#include <algorithm>
 #include <cmath>
 #include <cstdarg>
 #include <cstdio>
@@ -62,6 +63,7 @@ struct pbf_handle {
   DBuf<uint32_t> cell_count, cell_start, big_list, big_count;
   DBuf<uint32_t> nbr_count, nbr_offset, nbr_list;
   DBuf<float> lambda, sdf, vol;
+  DBuf<uint8_t> bflag;  // per field cell: 1 when the boundary sample can be non-zero
   DBuf<uint32_t> err_word;
   DBuf<float> m_f;
   DBuf<double> m_d;
@@ -84,11 +86,12 @@ struct pbf_handle {
 namespace {
 
 enum PassId {
-  K_PREDICT, K_SORT, K_GATHER, K_NBR_COUNT, K_NBR_SCAN, K_NBR_LIST, K_LAMBDA, K_DELTAP, K_DENSITY, K_VORTICITY,
-  K_XSPH, K_EXPORT, K_NUM
+  K_PREDICT, K_SORT, K_GATHER, K_NBR_COUNT, K_NBR_SCAN, K_NBR_LIST, K_BOUNDARY, K_LAMBDA, K_DELTAP, K_DENSITY,
+  K_VORTICITY, K_XSPH, K_EXPORT, K_NUM
 };
-const char* kPassNames[K_NUM] = {"predict",   "sort",         "gather",   "nbr_count", "nbr_scan", "nbr_list",
-                                 "lambda",    "deltap_apply", "density_velocity", "vorticity", "xsph", "export"};
+const char* kPassNames[K_NUM] = {"predict",  "sort",   "gather",       "nbr_count",        "nbr_scan",
+                                 "nbr_list", "boundary", "lambda",     "deltap_apply",     "density_velocity",
+                                 "vorticity", "xsph",   "export"};
 
 // Brackets one launch (or one group of launches) with events when timing is on.
 struct KScope {
@@ -275,10 +278,16 @@ int substep(pbf_handle* h, cudaEvent_t* ev) {
   const FieldParams f = h->fp;
   const uint32_t cap = h->nbr_capacity;
   for (uint32_t it = 0; it < h->cfg.options.iterations; ++it) {
+    if (f.loaded) {
+      KScope ks(h, K_BOUNDARY);
+      h->passes.boundary<<<nblocks(n, 256), 256, 0, st>>>(p, f, h->sdf.p, h->vol.p, h->bflag.p, h->xs[a].p,
+                                                           h->bdata.p);
+    }
+    CU(h, cudaGetLastError());
     {
       KScope ks(h, K_LAMBDA);
-      h->passes.lambda<<<nblocks(n, 256), 256, 0, st>>>(p, f, h->sdf.p, h->vol.p, h->xs[a].p, h->nbr_offset.p,
-                                                         h->nbr_list.p, cap, h->lambda.p, h->bdata.p);
+      h->passes.lambda<<<nblocks(n, 256), 256, 0, st>>>(p, f.loaded, h->bdata.p, h->xs[a].p, h->nbr_offset.p,
+                                                         h->nbr_list.p, cap, h->lambda.p);
     }
     CU(h, cudaGetLastError());
     {
@@ -376,6 +385,7 @@ void release_all(pbf_handle* h) {
   h->lambda.release();
   h->sdf.release();
   h->vol.release();
+  h->bflag.release();
   h->m_f.release();
   h->m_d.release();
   if (h->scan_scratch) cudaFree(h->scan_scratch);
@@ -383,6 +393,47 @@ void release_all(pbf_handle* h) {
 }
 
 bool finite_positive(float v) { return std::isfinite(v) && v > 0.0f; }
+
+// Per field cell, whether BoundaryVolume can return a non-zero bData there.
+// It cannot when all 32 volume nodes are zero (the interpolated volume is
+// exactly 0 and `volume > 0` fails) or when the interpolated SDF provably
+// stays >= h (or <= 0) over the cell: the cubic serendipity weights sum to 1
+// with at most 2.375 of negative weight, so the value lies within
+// [m - 2.375 (M - m), M + 2.375 (M - m)] of the node range [m, M]; a margin
+// covers the float rounding of the 32-term sum.
+void boundary_flags(const uint32_t res[3], const float* sdf, const float* vol, float h, std::vector<uint8_t>& flag) {
+  const size_t nx = res[0], ny = res[1], nz = res[2];
+  const size_t nc = (nx + 1) * (ny + 1) * (nz + 1);
+  const size_t nex = 2 * nx * (ny + 1) * (nz + 1);
+  const size_t ney = (nx + 1) * 2 * ny * (nz + 1);
+  flag.assign(nx * ny * nz, 1);
+  for (size_t k = 0; k < nz; ++k)
+    for (size_t j = 0; j < ny; ++j)
+      for (size_t i = 0; i < nx; ++i) {
+        size_t idx[32];
+        int q = 0;
+        for (int c = 0; c < 8; ++c)
+          idx[q++] = ((k + (c >> 2 & 1)) * (ny + 1) + (j + (c >> 1 & 1))) * (nx + 1) + (i + (c & 1));
+        for (int c = 0; c < 8; ++c)
+          idx[q++] = nc + ((k + (c >> 1 & 1)) * (ny + 1) + (j + (c >> 2 & 1))) * (2 * nx) + 2 * i + (c & 1);
+        for (int c = 0; c < 8; ++c)
+          idx[q++] = nc + nex + ((i + (c >> 1 & 1)) * (nz + 1) + (k + (c >> 2 & 1))) * (2 * ny) + 2 * j + (c & 1);
+        for (int c = 0; c < 8; ++c)
+          idx[q++] = nc + nex + ney + ((j + (c >> 1 & 1)) * (nx + 1) + (i + (c >> 2 & 1))) * (2 * nz) + 2 * k + (c & 1);
+        bool vzero = true;
+        double m = 1e300, M = -1e300, amax = 0.0;
+        for (int t = 0; t < 32; ++t) {
+          if (vol[idx[t]] != 0.0f) vzero = false;
+          double v = sdf[idx[t]];
+          m = std::min(m, v);
+          M = std::max(M, v);
+          amax = std::max(amax, std::fabs(v));
+        }
+        double spread = 2.375 * (M - m) + 2e-5 * amax + 1e-30;
+        bool far = (m - spread >= (double)h) || (M + spread <= 0.0);
+        if (vzero || far) flag[(k * ny + j) * nx + i] = 0;
+      }
+}
 
 }  // namespace
 
@@ -693,6 +744,14 @@ int pbf_set_boundary_field(pbf_handle* h, const uint32_t res[3], const float ori
   CU(h, cudaMemcpyAsync(h->sdf.p, sdf, len * sizeof(float), cudaMemcpyHostToDevice, h->stream));
   CU(h, cudaMemcpyAsync(h->vol.p, volume, len * sizeof(float), cudaMemcpyHostToDevice, h->stream));
   CU(h, cudaMemsetAsync(h->bdata.p, 0, (size_t)h->cfg.max_particles * sizeof(float4), h->stream));
+  {
+    std::vector<uint8_t> flag;
+    boundary_flags(res, sdf, volume, h->cfg.kernel_radius, flag);
+    h->bflag.release();
+    CU(h, h->bflag.alloc(flag.size()));
+    CU(h, cudaMemcpyAsync(h->bflag.p, flag.data(), flag.size(), cudaMemcpyHostToDevice, h->stream));
+    CU(h, cudaStreamSynchronize(h->stream));
+  }
   CU(h, cudaStreamSynchronize(h->stream));
   set_field_params(h, res, origin, extent);
   h->fp.loaded = 1;
@@ -1119,7 +1178,7 @@ int pbf_ns_lists(pbf_ns* s, const float* d_pos4, uint32_t n, float radius, uint3
   p.n = n;
   PassTable tbl;
   exact::fill_pass_table(&tbl);
-  NSCU(s, launch_gather_state(n, s->perm.p, (const float4*)d_pos4, (const float4*)d_pos4, s->perm.p, sorted, sorted,
+  NSCU(s, launch_gather_state(n, s->perm.p, (const float4*)d_pos4, (const float4*)d_pos4, nullptr, sorted, sorted,
                               ids, st));
   tbl.nbr_count<<<nblocks(n + 1, 256), 256, 0, st>>>(p, s->g, sorted, s->cell_start.p, s->nbr_count.p);
   NSCU(s, cudaGetLastError());

@@ -15,6 +15,12 @@
 
 namespace pbf {
 
+#ifdef PBF_FAST_MATH
+constexpr bool kFast = true;
+#else
+constexpr bool kFast = false;
+#endif
+
 struct f3 {
   float x, y, z;
 };
@@ -55,6 +61,61 @@ __device__ __forceinline__ f3 cohesion(const SimParams& p, f3 d, float rl) {
   res = (rl <= p.h) ? res : 0.0f;
   f3 n = (rl > 0.0f) ? divs(d, rl) : mk(0.f, 0.f, 0.f);
   return (p.coh * res) * n;
+}
+
+// One particle pair: offset d, |d|^2, |d| and 1/|d| (0 at d = 0).  Exact mode
+// evaluates |d| = sqrt(d.d) and divides like the reference; fast mode uses
+// rsqrt and multiplies by the reciprocal.
+struct Pair {
+  f3 d;
+  float r2, rl, ir;
+};
+__device__ __forceinline__ Pair make_pair_of(f3 d) {
+  Pair q;
+  q.d = d;
+  q.r2 = dot3(d, d);
+  if (kFast) {
+    q.ir = (q.r2 > 0.0f) ? rsqrtf(q.r2) : 0.0f;
+    q.rl = q.r2 * q.ir;
+  } else {
+    q.rl = sqrtf(q.r2);
+    q.ir = 0.0f;
+  }
+  return q;
+}
+__device__ __forceinline__ float poly6_p(const SimParams& p, const Pair& q) {
+  if (kFast) {
+    float t = p.h2 - q.r2;
+    return (q.r2 <= p.h2) ? p.poly6 * (t * t * t) : 0.0f;
+  }
+  return poly6(p, q.rl);
+}
+__device__ __forceinline__ f3 spiky_p(const SimParams& p, const Pair& q) {
+  if (kFast) {
+    float t = p.h - q.rl;
+    float x = (q.rl <= p.h) ? (t * t) : 0.0f;
+    return (p.spiky * x * q.ir) * q.d;
+  }
+  return spiky_grad(p, q.d, q.rl);
+}
+__device__ __forceinline__ f3 cohesion_p(const SimParams& p, const Pair& q) {
+  if (kFast) {
+    float a = p.h - q.rl;
+    float t = (a * a * a) * (q.rl * q.rl * q.rl);
+    float res = (q.rl > p.half_h) ? t : fmaf(2.0f, t, p.coh_bias);
+    res = (q.rl <= p.h) ? res : 0.0f;
+    return (p.coh * res * q.ir) * q.d;
+  }
+  return cohesion(p, q.d, q.rl);
+}
+// a / b: IEEE division in exact mode, reciprocal-multiply in fast mode.
+__device__ __forceinline__ float fdiv(float a, float b) { return kFast ? a * __frcp_rn(b) : a / b; }
+__device__ __forceinline__ f3 fdiv3(f3 a, float b) {
+  if (kFast) {
+    float r = __frcp_rn(b);
+    return r * a;
+  }
+  return divs(a, b);
 }
 
 // ---- wall clamp with jitter (common.ts:43-67) ------------------------------------

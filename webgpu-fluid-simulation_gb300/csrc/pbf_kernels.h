@@ -16,8 +16,8 @@ struct PassTable {
   void (*nbr_count)(SimParams, GridParams, const float4*, const uint32_t*, uint32_t*);
   void (*nbr_list)(SimParams, GridParams, const float4*, const uint32_t*, const uint32_t*, uint32_t*, uint32_t,
                    uint32_t*);
-  void (*lambda)(SimParams, FieldParams, const float*, const float*, const float4*, const uint32_t*, const uint32_t*,
-                 uint32_t, float*, float4*);
+  void (*boundary)(SimParams, FieldParams, const float*, const float*, const uint8_t*, const float4*, float4*);
+  void (*lambda)(SimParams, int, const float4*, const float4*, const uint32_t*, const uint32_t*, uint32_t, float*);
   void (*deltap)(SimParams, int, const float4*, const float*, const float4*, const uint32_t*, const uint32_t*, uint32_t,
                  float4*, float4*);
   void (*density_velocity)(SimParams, const float4*, const uint32_t*, const uint32_t*, uint32_t, float4*, float4*);

@@ -135,6 +135,43 @@ __global__ void __launch_bounds__(256) k_nbr_list(SimParams p, GridParams g, con
     }
 }
 
+// Visit list entries b..e-1 in order; indices and the neighbour's float4 are
+// loaded four at a time so the gathers overlap.  fn(j, xj) keeps the
+// sequential accumulation order of the reference loop.
+template <class Fn>
+__device__ __forceinline__ void for_each_neighbor(const uint32_t* __restrict__ list, uint32_t b, uint32_t e,
+                                                  const float4* __restrict__ xs, Fn&& fn) {
+  uint32_t q = b;
+  for (; q + 4 <= e; q += 4) {
+    uint32_t j0 = __ldg(list + q), j1 = __ldg(list + q + 1), j2 = __ldg(list + q + 2), j3 = __ldg(list + q + 3);
+    float4 x0 = __ldg(xs + j0), x1 = __ldg(xs + j1), x2 = __ldg(xs + j2), x3 = __ldg(xs + j3);
+    fn(j0, x0);
+    fn(j1, x1);
+    fn(j2, x2);
+    fn(j3, x3);
+  }
+  for (; q < e; ++q) {
+    uint32_t j = __ldg(list + q);
+    fn(j, __ldg(xs + j));
+  }
+}
+
+// Whether the boundary sample of a particle can be non-zero: per field cell,
+// 0 when all 32 volume nodes are zero (the interpolated volume is then zero)
+// or the SDF provably stays >= h over the cell; then bData = 0 exactly.
+__device__ __forceinline__ bool boundary_possible(const FieldParams& f, const uint8_t* __restrict__ flag, f3 x) {
+  if (!flag) return true;
+  int c[3];
+  float q[3] = {x.x, x.y, x.z};
+#pragma unroll
+  for (int a = 0; a < 3; ++a) {
+    float u = (q[a] - f.origin[a]) * f.scale[a];
+    int ci = (int)floorf(u);
+    c[a] = min(max(ci, 0), f.res[a] - 1);
+  }
+  return __ldg(flag + ((size_t)c[2] * f.res[1] + c[1]) * f.res[0] + c[0]) != 0;
+}
+
 // Clamp a neighbour-list range to the list capacity (an overflowed list has
 // been flagged; the step's results are then invalid but no access is out of bounds).
 __device__ __forceinline__ void list_range(const uint32_t* __restrict__ off, uint32_t t, uint32_t cap, uint32_t& b,
@@ -143,12 +180,24 @@ __device__ __forceinline__ void list_range(const uint32_t* __restrict__ off, uin
   e = min(__ldg(off + t + 1), cap);
 }
 
-// BoundaryVolume + LambdaCalculation.
-__global__ void __launch_bounds__(256) k_lambda(SimParams p, FieldParams f, const float* __restrict__ sdf,
-                                                const float* __restrict__ vol, const float4* __restrict__ xs,
-                                                const uint32_t* __restrict__ nbr_offset,
+// BoundaryVolume (boundaryVolume.ts:26-57): (x_b, V_b) per particle, skipping
+// the 64-node interpolation where the field cell cannot produce a sample.
+__global__ void __launch_bounds__(256) k_boundary(SimParams p, FieldParams f, const float* __restrict__ sdf,
+                                                  const float* __restrict__ vol, const uint8_t* __restrict__ bflag,
+                                                  const float4* __restrict__ xs, float4* __restrict__ bdata) {
+  uint32_t t = blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= p.n) return;
+  f3 xi = xyz(xs[t]);
+  float4 bd = make_float4(0.f, 0.f, 0.f, 0.f);
+  if (boundary_possible(f, bflag, xi)) bd = boundary_sample(p, f, sdf, vol, xi);
+  bdata[t] = bd;
+}
+
+// LambdaCalculation (pressureConstrain.ts:31-85).
+__global__ void __launch_bounds__(256) k_lambda(SimParams p, int have_field, const float4* __restrict__ bdata,
+                                                const float4* __restrict__ xs, const uint32_t* __restrict__ nbr_offset,
                                                 const uint32_t* __restrict__ nbr_list, uint32_t cap,
-                                                float* __restrict__ lambda, float4* __restrict__ bdata) {
+                                                float* __restrict__ lambda) {
   uint32_t t = blockIdx.x * blockDim.x + threadIdx.x;
   if (t >= p.n) return;
   f3 xi = xyz(xs[t]);
@@ -156,33 +205,28 @@ __global__ void __launch_bounds__(256) k_lambda(SimParams p, FieldParams f, cons
   list_range(nbr_offset, t, cap, b, e);
   f3 grad = mk(0.f, 0.f, 0.f);
   float sum2 = 0.0f, dens = 0.0f;
-  for (uint32_t q = b; q < e; ++q) {
-    uint32_t j = __ldg(nbr_list + q);
-    f3 d = xi - xyz(__ldg(xs + j));
-    float rl = len3(d);
-    f3 gk = spiky_grad(p, d, rl);
+  for_each_neighbor(nbr_list, b, e, xs, [&](uint32_t, float4 xj) {
+    Pair q = make_pair_of(xi - xyz(xj));
+    f3 gk = spiky_p(p, q);
     grad = grad + gk;
     sum2 = sum2 + dot3(gk, gk);
-    dens = dens + poly6(p, rl);
-  }
+    dens = dens + poly6_p(p, q);
+  });
   dens = dens * p.V;
   grad = p.V * grad;
   sum2 = sum2 * p.V2;
-  float4 bd = make_float4(0.f, 0.f, 0.f, 0.f);
-  if (f.loaded) {
-    bd = boundary_sample(p, f, sdf, vol, xi);
+  if (have_field) {
+    float4 bd = bdata[t];
     if (bd.w != 0.0f) {
-      f3 d = xi - xyz(bd);
-      float rl = len3(d);
-      f3 gk = bd.w * spiky_grad(p, d, rl);
+      Pair q = make_pair_of(xi - xyz(bd));
+      f3 gk = bd.w * spiky_p(p, q);
       grad = grad + gk;
-      dens = dens + bd.w * poly6(p, rl);
+      dens = dens + bd.w * poly6_p(p, q);
     }
-    bdata[t] = bd;
   }
   float c = fmaxf(0.0f, dens - 1.0f);
   float s = dot3(grad, grad) + sum2;
-  lambda[t] = -c / (s + p.lambda_eps);
+  lambda[t] = fdiv(-c, s + p.lambda_eps);
 }
 
 // ConstrainSolve + ConstrainApply: x*_new = clamp(x* + 0.5 * dp) into the other buffer.
@@ -198,20 +242,17 @@ __global__ void __launch_bounds__(256) k_deltap(SimParams p, int have_field, con
   uint32_t b, e;
   list_range(nbr_offset, t, cap, b, e);
   f3 pu = mk(0.f, 0.f, 0.f);
-  for (uint32_t q = b; q < e; ++q) {
-    uint32_t j = __ldg(nbr_list + q);
-    f3 d = xi - xyz(__ldg(xs + j));
-    float rl = len3(d);
+  for_each_neighbor(nbr_list, b, e, xs, [&](uint32_t j, float4 xj) {
+    Pair q = make_pair_of(xi - xyz(xj));
     float lj = __ldg(lambda + j);
-    pu = pu + (li + lj) * spiky_grad(p, d, rl);
-  }
+    pu = pu + (li + lj) * spiky_p(p, q);
+  });
   pu = p.V * pu;
   if (have_field) {
     float4 bd = bdata[t];
     if (bd.w != 0.0f) {
-      f3 d = xi - xyz(bd);
-      float rl = len3(d);
-      pu = pu + (bd.w * li) * spiky_grad(p, d, rl);
+      Pair q = make_pair_of(xi - xyz(bd));
+      pu = pu + (bd.w * li) * spiky_p(p, q);
     }
   }
   f3 dp = 0.5f * pu;
@@ -230,11 +271,10 @@ __global__ void __launch_bounds__(256) k_density_velocity(SimParams p, const flo
   uint32_t b, e;
   list_range(nbr_offset, t, cap, b, e);
   float dens = 0.0f;
-  for (uint32_t q = b; q < e; ++q) {
-    uint32_t j = __ldg(nbr_list + q);
-    f3 d = xi - xyz(__ldg(xs + j));
-    dens = dens + poly6(p, len3(d));
-  }
+  for_each_neighbor(nbr_list, b, e, xs, [&](uint32_t, float4 xj) {
+    Pair q = make_pair_of(xi - xyz(xj));
+    dens = dens + poly6_p(p, q);
+  });
   dens = dens * p.m;
   f3 xo = xyz(pos[t]);
   vel[t] = f4(p.inv_dt * (xi - xo), 0.0f);
@@ -254,17 +294,14 @@ __global__ void __launch_bounds__(256) k_vorticity(SimParams p, const float4* __
   uint32_t b, e;
   list_range(nbr_offset, t, cap, b, e);
   f3 om = mk(0.f, 0.f, 0.f), nm = mk(0.f, 0.f, 0.f);
-  for (uint32_t q = b; q < e; ++q) {
-    uint32_t j = __ldg(nbr_list + q);
-    float4 pj = __ldg(pos + j);
-    f3 d = xi - xyz(pj);
-    float rl = len3(d);
+  for_each_neighbor(nbr_list, b, e, pos, [&](uint32_t j, float4 pj) {
+    Pair q = make_pair_of(xi - xyz(pj));
     f3 vd = xyz(__ldg(vel + j)) - vi;
-    float volume = p.m / pj.w;
-    f3 gw = spiky_grad(p, d, rl);
+    float volume = fdiv(p.m, pj.w);
+    f3 gw = spiky_p(p, q);
     om = om + volume * cross3(vd, gw);
     nm = nm + volume * gw;
-  }
+  });
   omega[t] = f4(om, len3(om));
   normal[t] = f4(p.h * nm, 0.0f);
 }
@@ -287,20 +324,17 @@ __global__ void __launch_bounds__(256) k_xsph(SimParams p, const float4* __restr
   uint32_t b, e;
   list_range(nbr_offset, t, cap, b, e);
   f3 vu = mk(0.f, 0.f, 0.f), eta = mk(0.f, 0.f, 0.f), ten = mk(0.f, 0.f, 0.f);
-  for (uint32_t q = b; q < e; ++q) {
-    uint32_t j = __ldg(nbr_list + q);
-    float4 pj = __ldg(pos + j);
+  for_each_neighbor(nbr_list, b, e, pos, [&](uint32_t j, float4 pj) {
     float rj = pj.w;
-    f3 d = xi - xyz(pj);
-    float rl = len3(d);
+    Pair q = make_pair_of(xi - xyz(pj));
     f3 vd = xyz(__ldg(vel + j)) - vi;
-    float kij = p.two_rho0 / (ri + rj);
-    vu = vu + divs(poly6(p, rl) * vd, rj);
-    eta = eta + divs(__ldg(&omega[j].w) * spiky_grad(p, d, rl), rj);
-    f3 coh = p.m * cohesion(p, d, rl);
+    float kij = fdiv(p.two_rho0, ri + rj);
+    vu = vu + fdiv3(poly6_p(p, q) * vd, rj);
+    eta = eta + fdiv3(__ldg(&omega[j].w) * spiky_p(p, q), rj);
+    f3 coh = p.m * cohesion_p(p, q);
     f3 curv = ni - xyz(__ldg(normal + j));
     ten = ten - kij * (coh + curv);
-  }
+  });
   float el = len3(eta);
   f3 en = (el > 0.0f) ? divs(eta, el) : mk(0.f, 0.f, 0.f);
   float sx = p.xsph * p.inv_dt * p.m;
@@ -313,6 +347,7 @@ void fill_pass_table(PassTable* tbl) {
   tbl->predict = k_predict;
   tbl->nbr_count = k_nbr_count;
   tbl->nbr_list = k_nbr_list;
+  tbl->boundary = k_boundary;
   tbl->lambda = k_lambda;
   tbl->deltap = k_deltap;
   tbl->density_velocity = k_density_velocity;

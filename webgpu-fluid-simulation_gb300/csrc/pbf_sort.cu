@@ -325,7 +325,7 @@ __global__ void __launch_bounds__(256) k_gather(uint32_t n, const uint32_t* __re
   uint32_t o = perm[t];
   pos_out[t] = __ldg(pos_in + o);
   xs_out[t] = __ldg(xs_in + o);
-  id_out[t] = __ldg(id_in + o);
+  id_out[t] = id_in ? __ldg(id_in + o) : o;  // no id array: the input order is the id order
 }
 
 __global__ void k_rank_from_order(uint32_t n, const uint32_t* __restrict__ perm, const uint32_t* __restrict__ key,

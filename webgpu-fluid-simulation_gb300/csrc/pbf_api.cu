@@ -61,7 +61,7 @@ struct pbf_handle {
   DBuf<float4> pos[2], xs[2], vel, acc, bdata, omega, normal, dp, out_pos, out_tmp;
   DBuf<uint32_t> ids[2], key, rank, perm_raw, id_raw, perm, tmp_a, tmp_b;
   DBuf<uint32_t> cell_count, cell_start, big_list, big_count;
-  DBuf<uint32_t> nbr_count, nbr_offset, nbr_list;
+  DBuf<uint32_t> nbr_count, warp_len, warp_off, nbr_list;
   DBuf<float> lambda, sdf, vol;
   DBuf<uint8_t> bflag;  // per field cell: 1 when the boundary sample can be non-zero
   DBuf<uint32_t> err_word;
@@ -205,6 +205,9 @@ void invalidate_graph(pbf_handle* h) {
   h->graph_valid = false;
 }
 
+// Reads and clears the device error word.  A neighbour-list overflow grows
+// the list to 1.25x the size the last substep needed (the results of that
+// substep are invalid: its lists were truncated) and is reported once.
 int check_device_errors(pbf_handle* h) {
   uint32_t e = 0;
   CU(h, cudaMemcpyAsync(&e, h->err_word.p, sizeof(uint32_t), cudaMemcpyDeviceToHost, h->stream));
@@ -212,9 +215,24 @@ int check_device_errors(pbf_handle* h) {
   if (e) {
     CU(h, cudaMemsetAsync(h->err_word.p, 0, sizeof(uint32_t), h->stream));
     CU(h, cudaStreamSynchronize(h->stream));
-    if (e & PBF_DEVERR_NEIGHBOR_OVERFLOW)
-      return fail(h, PBF_ECAPACITY, "neighbour list overflow: more than %u entries needed (max_neighbors=%u)",
-                  h->nbr_capacity, h->cfg.max_neighbors);
+    if (e & PBF_DEVERR_NEIGHBOR_OVERFLOW) {
+      uint32_t need = 0;
+      const uint32_t nw = (h->n + 31) / 32;
+      CU(h, cudaMemcpy(&need, h->warp_off.p + nw, sizeof(uint32_t), cudaMemcpyDeviceToHost));
+      uint64_t grow = (uint64_t)need + need / 4 + 1024;
+      if (grow > 0xffffffffull) grow = 0xffffffffull;
+      uint32_t old = h->nbr_capacity;
+      if (grow > old) {
+        invalidate_graph(h);
+        h->nbr_list.release();
+        CU(h, h->nbr_list.alloc(grow));
+        h->nbr_capacity = (uint32_t)grow;
+      }
+      return fail(h, PBF_ECAPACITY,
+                  "neighbour list overflow: %u entries needed, capacity was %u; grown to %u, the last substep's "
+                  "results are invalid",
+                  need, old, h->nbr_capacity);
+    }
     if (e & PBF_DEVERR_SCAN_TIMEOUT) return fail(h, PBF_ETIMEOUT, "scan look-back wait gave up");
     return fail(h, PBF_ECUDA, "device error word 0x%x", e);
   }
@@ -257,19 +275,23 @@ int substep(pbf_handle* h, cudaEvent_t* ev) {
   h->cur = nx;
   const int cc = nx;
   // NeighborCount + particle scan + NeighborList
+  const uint32_t nw = (n + 31) / 32;
   {
     KScope ks(h, K_NBR_COUNT);
-    h->passes.nbr_count<<<nblocks(n + 1, 256), 256, 0, st>>>(p, g, h->xs[0].p, h->cell_start.p, h->nbr_count.p);
+    // n + 33 threads: the lane-0 thread of warp ceil(n/32), which writes the
+    // terminating zero of the slice lengths, is always in the grid
+    h->passes.nbr_count<<<nblocks(n + 33, 256), 256, 0, st>>>(p, g, h->xs[0].p, h->cell_start.p, h->nbr_count.p,
+                                                               h->warp_len.p);
   }
   CU(h, cudaGetLastError());
   {
     KScope ks(h, K_NBR_SCAN);
-    CU(h, launch_exclusive_scan(h->nbr_count.p, h->nbr_offset.p, (size_t)n + 1, h->scan_scratch, h->err_word.p, st));
+    CU(h, launch_exclusive_scan(h->warp_len.p, h->warp_off.p, (size_t)nw + 1, h->scan_scratch, h->err_word.p, st));
   }
   {
     KScope ks(h, K_NBR_LIST);
-    h->passes.nbr_list<<<nblocks(n, 256), 256, 0, st>>>(p, g, h->xs[0].p, h->cell_start.p, h->nbr_offset.p,
-                                                         h->nbr_list.p, h->nbr_capacity, h->err_word.p);
+    h->passes.nbr_list_sliced<<<nblocks(n, 256), 256, 0, st>>>(p, g, h->xs[0].p, h->cell_start.p, h->warp_off.p,
+                                                                h->nbr_list.p, h->nbr_capacity, h->err_word.p);
   }
   CU(h, cudaGetLastError());
   if (ev) CU(h, cudaEventRecord(ev[2], st));
@@ -286,14 +308,15 @@ int substep(pbf_handle* h, cudaEvent_t* ev) {
     CU(h, cudaGetLastError());
     {
       KScope ks(h, K_LAMBDA);
-      h->passes.lambda<<<nblocks(n, 256), 256, 0, st>>>(p, f.loaded, h->bdata.p, h->xs[a].p, h->nbr_offset.p,
-                                                         h->nbr_list.p, cap, h->lambda.p);
+      h->passes.lambda<<<nblocks(n, 256), 256, 0, st>>>(p, f.loaded, h->bdata.p, h->xs[a].p, h->warp_off.p,
+                                                         h->nbr_count.p, h->nbr_list.p, cap, h->lambda.p);
     }
     CU(h, cudaGetLastError());
     {
       KScope ks(h, K_DELTAP);
       h->passes.deltap<<<nblocks(n, 256), 256, 0, st>>>(p, f.loaded, h->xs[a].p, h->lambda.p, h->bdata.p,
-                                                         h->nbr_offset.p, h->nbr_list.p, cap, h->xs[1 - a].p,
+                                                         h->warp_off.p, h->nbr_count.p, h->nbr_list.p, cap,
+                                                         h->xs[1 - a].p,
                                                          h->capture ? h->dp.p : nullptr);
     }
     CU(h, cudaGetLastError());
@@ -303,21 +326,22 @@ int substep(pbf_handle* h, cudaEvent_t* ev) {
   // non-pressure passes
   {
     KScope ks(h, K_DENSITY);
-    h->passes.density_velocity<<<nblocks(n, 256), 256, 0, st>>>(p, h->xs[a].p, h->nbr_offset.p, h->nbr_list.p,
-                                                                 cap, h->pos[cc].p, h->vel.p);
+    h->passes.density_velocity<<<nblocks(n, 256), 256, 0, st>>>(p, h->xs[a].p, h->warp_off.p, h->nbr_count.p,
+                                                                 h->nbr_list.p, cap, h->pos[cc].p, h->vel.p);
   }
   CU(h, cudaGetLastError());
   if (a != 0) CU(h, cudaMemcpyAsync(h->xs[0].p, h->xs[1].p, (size_t)n * sizeof(float4), cudaMemcpyDeviceToDevice, st));
   {
     KScope ks(h, K_VORTICITY);
-    h->passes.vorticity<<<nblocks(n, 256), 256, 0, st>>>(p, h->pos[cc].p, h->vel.p, h->nbr_offset.p,
-                                                          h->nbr_list.p, cap, h->omega.p, h->normal.p);
+    h->passes.vorticity<<<nblocks(n, 256), 256, 0, st>>>(p, h->pos[cc].p, h->vel.p, h->warp_off.p,
+                                                          h->nbr_count.p, h->nbr_list.p, cap, h->omega.p,
+                                                          h->normal.p);
   }
   CU(h, cudaGetLastError());
   {
     KScope ks(h, K_XSPH);
     h->passes.xsph<<<nblocks(n, 256), 256, 0, st>>>(p, h->pos[cc].p, h->vel.p, h->omega.p, h->normal.p,
-                                                     h->nbr_offset.p, h->nbr_list.p, cap, h->acc.p);
+                                                     h->warp_off.p, h->nbr_count.p, h->nbr_list.p, cap, h->acc.p);
   }
   CU(h, cudaGetLastError());
   if (ev) CU(h, cudaEventRecord(ev[4], st));
@@ -379,7 +403,7 @@ void release_all(pbf_handle* h) {
   for (auto* b : f4s) b->release();
   DBuf<uint32_t>* u32s[] = {&h->ids[0],   &h->ids[1],      &h->key,      &h->rank,      &h->perm_raw,
                             &h->id_raw,   &h->perm,        &h->tmp_a,    &h->tmp_b,     &h->cell_count,
-                            &h->cell_start, &h->big_list,  &h->big_count, &h->nbr_count, &h->nbr_offset,
+                            &h->cell_start, &h->big_list,  &h->big_count, &h->nbr_count, &h->warp_len, &h->warp_off,
                             &h->nbr_list, &h->err_word,    &h->m_u};
   for (auto* b : u32s) b->release();
   h->lambda.release();
@@ -532,13 +556,14 @@ int pbf_create(const pbf_config* cfg, pbf_handle** out) {
   A(h->big_list.alloc(cells));
   A(h->big_count.alloc(1));
   A(h->nbr_count.alloc(cap + 1));
-  A(h->nbr_offset.alloc(cap + 1));
+  A(h->warp_len.alloc(cap / 32 + 3));
+  A(h->warp_off.alloc(cap / 32 + 3));
   A(h->nbr_list.alloc(h->nbr_capacity));
   A(h->lambda.alloc(cap));
   A(h->err_word.alloc(1));
   A(h->m_f.alloc(2));
   A(h->m_d.alloc(2));
-  A(h->m_u.alloc(2));
+  A(h->m_u.alloc(3));
   size_t sb = scan_scratch_bytes(cells + 1);
   size_t sb2 = scan_scratch_bytes(cap + 1);
   if (sb2 > sb) sb = sb2;
@@ -1008,19 +1033,18 @@ int pbf_get_metrics(pbf_handle* h, pbf_metrics* out) {
   cudaStream_t st = h->stream;
   CU(h, cudaMemsetAsync(h->m_f.p, 0, 2 * sizeof(float), st));
   CU(h, cudaMemsetAsync(h->m_d.p, 0, 2 * sizeof(double), st));
-  CU(h, cudaMemsetAsync(h->m_u.p, 0, 2 * sizeof(uint32_t), st));
+  CU(h, cudaMemsetAsync(h->m_u.p, 0, 3 * sizeof(uint32_t), st));
   SimParams p = h->sp;
   p.n = h->n;
-  CU(h, launch_metrics(p, h->fp, h->fp.loaded ? h->sdf.p : nullptr, h->pos[h->cur].p, h->vel.p, h->n, h->m_f.p,
-                       h->m_d.p, h->m_u.p, st));
+  CU(h, launch_metrics(p, h->fp, h->fp.loaded ? h->sdf.p : nullptr, h->pos[h->cur].p, h->vel.p, h->nbr_count.p,
+                       h->n, h->m_f.p, h->m_d.p, h->m_u.p, st));
   float mf[2];
   double md[2];
-  uint32_t mu[2], tot = 0, errw = 0;
+  uint32_t mu[3], errw = 0;
   CU(h, cudaMemcpyAsync(mf, h->m_f.p, sizeof(mf), cudaMemcpyDeviceToHost, st));
   CU(h, cudaMemcpyAsync(md, h->m_d.p, sizeof(md), cudaMemcpyDeviceToHost, st));
   CU(h, cudaMemcpyAsync(mu, h->m_u.p, sizeof(mu), cudaMemcpyDeviceToHost, st));
   CU(h, cudaMemcpyAsync(&errw, h->err_word.p, sizeof(uint32_t), cudaMemcpyDeviceToHost, st));
-  if (h->n) CU(h, cudaMemcpyAsync(&tot, h->nbr_offset.p + h->n, sizeof(uint32_t), cudaMemcpyDeviceToHost, st));
   CU(h, cudaStreamSynchronize(st));
   out->max_compression = mf[0];
   out->max_abs_density_err = mf[1];
@@ -1029,7 +1053,7 @@ int pbf_get_metrics(pbf_handle* h, pbf_metrics* out) {
   out->nonfinite = mu[0];
   out->penetrations = mu[1];
   out->error_flags = errw;
-  out->neighbor_total = tot;
+  out->neighbor_total = mu[2];
   return PBF_OK;
 }
 
@@ -1180,7 +1204,7 @@ int pbf_ns_lists(pbf_ns* s, const float* d_pos4, uint32_t n, float radius, uint3
   exact::fill_pass_table(&tbl);
   NSCU(s, launch_gather_state(n, s->perm.p, (const float4*)d_pos4, (const float4*)d_pos4, nullptr, sorted, sorted,
                               ids, st));
-  tbl.nbr_count<<<nblocks(n + 1, 256), 256, 0, st>>>(p, s->g, sorted, s->cell_start.p, s->nbr_count.p);
+  tbl.nbr_count<<<nblocks(n + 1, 256), 256, 0, st>>>(p, s->g, sorted, s->cell_start.p, s->nbr_count.p, nullptr);
   NSCU(s, cudaGetLastError());
   // counts are in slot order; the reference's offsets are by particle id
   uint32_t* cnt_by_id = nullptr;

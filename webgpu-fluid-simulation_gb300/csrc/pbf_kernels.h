@@ -13,18 +13,22 @@ namespace pbf {
 struct PassTable {
   void (*predict)(SimParams, GridParams, const float4*, const float4*, const float4*, float4*, uint32_t*, uint32_t*,
                   uint32_t*);
-  void (*nbr_count)(SimParams, GridParams, const float4*, const uint32_t*, uint32_t*);
+  void (*nbr_count)(SimParams, GridParams, const float4*, const uint32_t*, uint32_t*, uint32_t*);
   void (*nbr_list)(SimParams, GridParams, const float4*, const uint32_t*, const uint32_t*, uint32_t*, uint32_t,
                    uint32_t*);
+  void (*nbr_list_sliced)(SimParams, GridParams, const float4*, const uint32_t*, const uint32_t*, uint32_t*, uint32_t,
+                          uint32_t*);
   void (*boundary)(SimParams, FieldParams, const float*, const float*, const uint8_t*, const float4*, float4*);
-  void (*lambda)(SimParams, int, const float4*, const float4*, const uint32_t*, const uint32_t*, uint32_t, float*);
-  void (*deltap)(SimParams, int, const float4*, const float*, const float4*, const uint32_t*, const uint32_t*, uint32_t,
-                 float4*, float4*);
-  void (*density_velocity)(SimParams, const float4*, const uint32_t*, const uint32_t*, uint32_t, float4*, float4*);
-  void (*vorticity)(SimParams, const float4*, const float4*, const uint32_t*, const uint32_t*, uint32_t, float4*,
-                    float4*);
+  void (*lambda)(SimParams, int, const float4*, const float4*, const uint32_t*, const uint32_t*, const uint32_t*,
+                 uint32_t, float*);
+  void (*deltap)(SimParams, int, const float4*, const float*, const float4*, const uint32_t*, const uint32_t*,
+                 const uint32_t*, uint32_t, float4*, float4*);
+  void (*density_velocity)(SimParams, const float4*, const uint32_t*, const uint32_t*, const uint32_t*, uint32_t,
+                           float4*, float4*);
+  void (*vorticity)(SimParams, const float4*, const float4*, const uint32_t*, const uint32_t*, const uint32_t*,
+                    uint32_t, float4*, float4*);
   void (*xsph)(SimParams, const float4*, const float4*, const float4*, const float4*, const uint32_t*,
-               const uint32_t*, uint32_t, float4*);
+               const uint32_t*, const uint32_t*, uint32_t, float4*);
 };
 
 namespace exact {
@@ -91,6 +95,7 @@ struct MetricsAccum {
   uint32_t penetrations;
 };
 cudaError_t launch_metrics(SimParams p, FieldParams f, const float* sdf, const float4* pos, const float4* vel,
-                           uint32_t n, float* accum_f, double* accum_d, uint32_t* accum_u, cudaStream_t st);
+                           const uint32_t* nbr_count, uint32_t n, float* accum_f, double* accum_d, uint32_t* accum_u,
+                           cudaStream_t st);
 
 }  // namespace pbf

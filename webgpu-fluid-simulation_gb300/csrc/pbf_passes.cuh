@@ -83,30 +83,64 @@ __device__ __forceinline__ Run run_of(const GridParams& g, const uint32_t* __res
   return Run{__ldg(cell_start + k0), __ldg(cell_start + k1)};
 }
 
-// NeighborCount: neighbours within h of x*, self included, 27 cells in key order.
+// NeighborCount: neighbours within h of x*, self included, 27 cells in key
+// order.  Also writes, per warp of 32 consecutive slots, 32 x the warp's
+// largest count: the slice length of the interleaved list layout.
 __global__ void __launch_bounds__(256) k_nbr_count(SimParams p, GridParams g, const float4* __restrict__ xs,
                                                    const uint32_t* __restrict__ cell_start,
-                                                   uint32_t* __restrict__ nbr_count) {
+                                                   uint32_t* __restrict__ nbr_count, uint32_t* __restrict__ warp_len) {
   uint32_t t = blockIdx.x * blockDim.x + threadIdx.x;
-  if (t > p.n) return;
-  if (t == p.n) {
-    nbr_count[t] = 0;
-    return;
+  uint32_t cnt = 0;
+  if (t < p.n) {
+    f3 xi = xyz(xs[t]);
+    int cx = cell_axis(xi.x, g.origin[0], g.inv_cell[0], g.dim[0]);
+    int cy = cell_axis(xi.y, g.origin[1], g.inv_cell[1], g.dim[1]);
+    int cz = cell_axis(xi.z, g.origin[2], g.inv_cell[2], g.dim[2]);
+    for (int dx = -1; dx <= 1; ++dx)
+      for (int dy = -1; dy <= 1; ++dy) {
+        Run r = run_of(g, cell_start, cx, cy, cz, dx, dy);
+        for (uint32_t u = r.b; u < r.e; ++u) {
+          f3 d = xyz(__ldg(xs + u)) - xi;
+          if (dot3(d, d) <= p.h2) ++cnt;
+        }
+      }
   }
+  if (t <= p.n) nbr_count[t] = cnt;
+  if (warp_len) {
+    uint32_t wmax = __reduce_max_sync(kFull, cnt);
+    uint32_t w = t >> 5;
+    if ((t & 31u) == 0 && w <= ((p.n + 31u) >> 5)) warp_len[w] = (t < p.n) ? 32u * wmax : 0u;
+  }
+}
+
+// Interleaved ("sliced") neighbour list of the step: the q-th neighbour of
+// slot t is at warp_off[t / 32] + 32 q + t % 32, so the q-th entries of a
+// warp's 32 particles are one contiguous 128-byte segment.  Same traversal
+// and order as NeighborList.
+__global__ void __launch_bounds__(256) k_nbr_list_sliced(SimParams p, GridParams g, const float4* __restrict__ xs,
+                                                         const uint32_t* __restrict__ cell_start,
+                                                         const uint32_t* __restrict__ warp_off,
+                                                         uint32_t* __restrict__ nbr_list, uint32_t capacity,
+                                                         uint32_t* err) {
+  uint32_t t = blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= p.n) return;
+  if (t == 0 && warp_off[(p.n + 31) >> 5] > capacity) atomicOr(err, 0x1u);
   f3 xi = xyz(xs[t]);
   int cx = cell_axis(xi.x, g.origin[0], g.inv_cell[0], g.dim[0]);
   int cy = cell_axis(xi.y, g.origin[1], g.inv_cell[1], g.dim[1]);
   int cz = cell_axis(xi.z, g.origin[2], g.inv_cell[2], g.dim[2]);
-  uint32_t cnt = 0;
+  uint32_t o = warp_off[t >> 5] + (t & 31u);
   for (int dx = -1; dx <= 1; ++dx)
     for (int dy = -1; dy <= 1; ++dy) {
       Run r = run_of(g, cell_start, cx, cy, cz, dx, dy);
       for (uint32_t u = r.b; u < r.e; ++u) {
         f3 d = xyz(__ldg(xs + u)) - xi;
-        if (dot3(d, d) <= p.h2) ++cnt;
+        if (dot3(d, d) <= p.h2) {
+          if (o < capacity) nbr_list[o] = u;
+          o += 32;
+        }
       }
     }
-  nbr_count[t] = cnt;
 }
 
 // NeighborList: the same traversal writing slot indices at nbr_offset[t].
@@ -135,23 +169,26 @@ __global__ void __launch_bounds__(256) k_nbr_list(SimParams p, GridParams g, con
     }
 }
 
-// Visit list entries b..e-1 in order; indices and the neighbour's float4 are
-// loaded four at a time so the gathers overlap.  fn(j, xj) keeps the
-// sequential accumulation order of the reference loop.
+// Visit the cnt neighbours of a slot in list order (interleaved layout:
+// entry q at base + 32 q).  Indices and the neighbour's float4 are loaded
+// four at a time so the gathers overlap; fn(j, xj) keeps the sequential
+// accumulation order of the reference loop.
 template <class Fn>
-__device__ __forceinline__ void for_each_neighbor(const uint32_t* __restrict__ list, uint32_t b, uint32_t e,
+__device__ __forceinline__ void for_each_neighbor(const uint32_t* __restrict__ list, uint32_t base, uint32_t cnt,
                                                   const float4* __restrict__ xs, Fn&& fn) {
-  uint32_t q = b;
-  for (; q + 4 <= e; q += 4) {
-    uint32_t j0 = __ldg(list + q), j1 = __ldg(list + q + 1), j2 = __ldg(list + q + 2), j3 = __ldg(list + q + 3);
+  const uint32_t* l = list + base;
+  uint32_t q = 0;
+  for (; q + 4 <= cnt; q += 4) {
+    uint32_t j0 = __ldg(l + 32 * q), j1 = __ldg(l + 32 * q + 32), j2 = __ldg(l + 32 * q + 64),
+             j3 = __ldg(l + 32 * q + 96);
     float4 x0 = __ldg(xs + j0), x1 = __ldg(xs + j1), x2 = __ldg(xs + j2), x3 = __ldg(xs + j3);
     fn(j0, x0);
     fn(j1, x1);
     fn(j2, x2);
     fn(j3, x3);
   }
-  for (; q < e; ++q) {
-    uint32_t j = __ldg(list + q);
+  for (; q < cnt; ++q) {
+    uint32_t j = __ldg(l + 32 * q);
     fn(j, __ldg(xs + j));
   }
 }
@@ -172,12 +209,17 @@ __device__ __forceinline__ bool boundary_possible(const FieldParams& f, const ui
   return __ldg(flag + ((size_t)c[2] * f.res[1] + c[1]) * f.res[0] + c[0]) != 0;
 }
 
-// Clamp a neighbour-list range to the list capacity (an overflowed list has
-// been flagged; the step's results are then invalid but no access is out of bounds).
-__device__ __forceinline__ void list_range(const uint32_t* __restrict__ off, uint32_t t, uint32_t cap, uint32_t& b,
-                                           uint32_t& e) {
-  b = min(__ldg(off + t), cap);
-  e = min(__ldg(off + t + 1), cap);
+// Slice of slot t in the interleaved list, clamped to the list capacity (an
+// overflowed list has been flagged; the step's results are then invalid but
+// no access is out of bounds).
+__device__ __forceinline__ void list_slice(const uint32_t* __restrict__ warp_off, const uint32_t* __restrict__ cnt_of,
+                                           uint32_t t, uint32_t cap, uint32_t& base, uint32_t& cnt) {
+  base = __ldg(warp_off + (t >> 5)) + (t & 31u);
+  cnt = __ldg(cnt_of + t);
+  if (base >= cap)
+    cnt = 0;
+  else
+    cnt = min(cnt, (cap - base + 31u) >> 5);
 }
 
 // BoundaryVolume (boundaryVolume.ts:26-57): (x_b, V_b) per particle, skipping
@@ -195,14 +237,14 @@ __global__ void __launch_bounds__(256) k_boundary(SimParams p, FieldParams f, co
 
 // LambdaCalculation (pressureConstrain.ts:31-85).
 __global__ void __launch_bounds__(256) k_lambda(SimParams p, int have_field, const float4* __restrict__ bdata,
-                                                const float4* __restrict__ xs, const uint32_t* __restrict__ nbr_offset,
+                                                const float4* __restrict__ xs, const uint32_t* __restrict__ warp_off, const uint32_t* __restrict__ nbr_cnt,
                                                 const uint32_t* __restrict__ nbr_list, uint32_t cap,
                                                 float* __restrict__ lambda) {
   uint32_t t = blockIdx.x * blockDim.x + threadIdx.x;
   if (t >= p.n) return;
   f3 xi = xyz(xs[t]);
   uint32_t b, e;
-  list_range(nbr_offset, t, cap, b, e);
+  list_slice(warp_off, nbr_cnt, t, cap, b, e);
   f3 grad = mk(0.f, 0.f, 0.f);
   float sum2 = 0.0f, dens = 0.0f;
   for_each_neighbor(nbr_list, b, e, xs, [&](uint32_t, float4 xj) {
@@ -232,7 +274,7 @@ __global__ void __launch_bounds__(256) k_lambda(SimParams p, int have_field, con
 // ConstrainSolve + ConstrainApply: x*_new = clamp(x* + 0.5 * dp) into the other buffer.
 __global__ void __launch_bounds__(256) k_deltap(SimParams p, int have_field, const float4* __restrict__ xs,
                                                 const float* __restrict__ lambda, const float4* __restrict__ bdata,
-                                                const uint32_t* __restrict__ nbr_offset,
+                                                const uint32_t* __restrict__ warp_off, const uint32_t* __restrict__ nbr_cnt,
                                                 const uint32_t* __restrict__ nbr_list, uint32_t cap,
                                                 float4* __restrict__ xs_out, float4* __restrict__ dp_out) {
   uint32_t t = blockIdx.x * blockDim.x + threadIdx.x;
@@ -240,7 +282,7 @@ __global__ void __launch_bounds__(256) k_deltap(SimParams p, int have_field, con
   f3 xi = xyz(xs[t]);
   float li = lambda[t];
   uint32_t b, e;
-  list_range(nbr_offset, t, cap, b, e);
+  list_slice(warp_off, nbr_cnt, t, cap, b, e);
   f3 pu = mk(0.f, 0.f, 0.f);
   for_each_neighbor(nbr_list, b, e, xs, [&](uint32_t j, float4 xj) {
     Pair q = make_pair_of(xi - xyz(xj));
@@ -262,14 +304,15 @@ __global__ void __launch_bounds__(256) k_deltap(SimParams p, int have_field, con
 
 // AttributeUpdate: rho = m * sum W (fluid only), v = (x* - x) / dt, x <- (x*, rho).
 __global__ void __launch_bounds__(256) k_density_velocity(SimParams p, const float4* __restrict__ xs,
-                                                          const uint32_t* __restrict__ nbr_offset,
+                                                          const uint32_t* __restrict__ warp_off,
+                                                          const uint32_t* __restrict__ nbr_cnt,
                                                           const uint32_t* __restrict__ nbr_list, uint32_t cap,
                                                           float4* __restrict__ pos, float4* __restrict__ vel) {
   uint32_t t = blockIdx.x * blockDim.x + threadIdx.x;
   if (t >= p.n) return;
   f3 xi = xyz(xs[t]);
   uint32_t b, e;
-  list_range(nbr_offset, t, cap, b, e);
+  list_slice(warp_off, nbr_cnt, t, cap, b, e);
   float dens = 0.0f;
   for_each_neighbor(nbr_list, b, e, xs, [&](uint32_t, float4 xj) {
     Pair q = make_pair_of(xi - xyz(xj));
@@ -284,7 +327,8 @@ __global__ void __launch_bounds__(256) k_density_velocity(SimParams p, const flo
 // VorticityConfinement: omega_i and the Akinci normal n_i.
 __global__ void __launch_bounds__(256) k_vorticity(SimParams p, const float4* __restrict__ pos,
                                                    const float4* __restrict__ vel,
-                                                   const uint32_t* __restrict__ nbr_offset,
+                                                   const uint32_t* __restrict__ warp_off,
+                                                   const uint32_t* __restrict__ nbr_cnt,
                                                    const uint32_t* __restrict__ nbr_list, uint32_t cap,
                                                    float4* __restrict__ omega, float4* __restrict__ normal) {
   uint32_t t = blockIdx.x * blockDim.x + threadIdx.x;
@@ -292,7 +336,7 @@ __global__ void __launch_bounds__(256) k_vorticity(SimParams p, const float4* __
   f3 xi = xyz(pos[t]);
   f3 vi = xyz(vel[t]);
   uint32_t b, e;
-  list_range(nbr_offset, t, cap, b, e);
+  list_slice(warp_off, nbr_cnt, t, cap, b, e);
   f3 om = mk(0.f, 0.f, 0.f), nm = mk(0.f, 0.f, 0.f);
   for_each_neighbor(nbr_list, b, e, pos, [&](uint32_t j, float4 pj) {
     Pair q = make_pair_of(xi - xyz(pj));
@@ -310,7 +354,8 @@ __global__ void __launch_bounds__(256) k_vorticity(SimParams p, const float4* __
 __global__ void __launch_bounds__(256) k_xsph(SimParams p, const float4* __restrict__ pos,
                                               const float4* __restrict__ vel, const float4* __restrict__ omega,
                                               const float4* __restrict__ normal,
-                                              const uint32_t* __restrict__ nbr_offset,
+                                              const uint32_t* __restrict__ warp_off,
+                                              const uint32_t* __restrict__ nbr_cnt,
                                               const uint32_t* __restrict__ nbr_list, uint32_t cap,
                                               float4* __restrict__ acc) {
   uint32_t t = blockIdx.x * blockDim.x + threadIdx.x;
@@ -322,7 +367,7 @@ __global__ void __launch_bounds__(256) k_xsph(SimParams p, const float4* __restr
   f3 wi = xyz(omega[t]);
   f3 ni = xyz(normal[t]);
   uint32_t b, e;
-  list_range(nbr_offset, t, cap, b, e);
+  list_slice(warp_off, nbr_cnt, t, cap, b, e);
   f3 vu = mk(0.f, 0.f, 0.f), eta = mk(0.f, 0.f, 0.f), ten = mk(0.f, 0.f, 0.f);
   for_each_neighbor(nbr_list, b, e, pos, [&](uint32_t j, float4 pj) {
     float rj = pj.w;
@@ -347,6 +392,7 @@ void fill_pass_table(PassTable* tbl) {
   tbl->predict = k_predict;
   tbl->nbr_count = k_nbr_count;
   tbl->nbr_list = k_nbr_list;
+  tbl->nbr_list_sliced = k_nbr_list_sliced;
   tbl->boundary = k_boundary;
   tbl->lambda = k_lambda;
   tbl->deltap = k_deltap;

@@ -380,12 +380,14 @@ __device__ __forceinline__ void atomic_max_pos_float(float* addr, float v) {
 }
 __global__ void __launch_bounds__(256) k_metrics(SimParams p, FieldParams f, const float* __restrict__ sdf,
                                                  const float4* __restrict__ pos, const float4* __restrict__ vel,
-                                                 uint32_t n, float* accum_f, double* accum_d, uint32_t* accum_u) {
+                                                 const uint32_t* __restrict__ nbr_count, uint32_t n, float* accum_f,
+                                                 double* accum_d, uint32_t* accum_u) {
   uint32_t t = blockIdx.x * blockDim.x + threadIdx.x;
   float comp = 0.f, aerr = 0.f;
   double ke = 0.0, serr = 0.0;
-  uint32_t bad = 0, pen = 0;
+  uint32_t bad = 0, pen = 0, nb = 0;
   if (t < n) {
+    if (nbr_count) nb = nbr_count[t];
     float4 x = pos[t];
     float4 v = vel[t];
     bool fin = isfinite(x.x) && isfinite(x.y) && isfinite(x.z) && isfinite(v.x) && isfinite(v.y) && isfinite(v.z);
@@ -418,6 +420,7 @@ __global__ void __launch_bounds__(256) k_metrics(SimParams p, FieldParams f, con
     serr += __shfl_xor_sync(kFull, serr, o);
     bad += __shfl_xor_sync(kFull, bad, o);
     pen += __shfl_xor_sync(kFull, pen, o);
+    nb += __shfl_xor_sync(kFull, nb, o);
   }
   if ((threadIdx.x & 31) == 0) {
     atomic_max_pos_float(accum_f + 0, comp);
@@ -426,6 +429,7 @@ __global__ void __launch_bounds__(256) k_metrics(SimParams p, FieldParams f, con
     atomicAdd(accum_d + 1, ke);
     atomicAdd(accum_u + 0, bad);
     atomicAdd(accum_u + 1, pen);
+    atomicAdd(accum_u + 2, nb);
   }
 }
 
@@ -531,9 +535,10 @@ cudaError_t launch_nbr_count_sub(uint32_t n, const uint32_t* off, uint32_t* cnt,
 }
 
 cudaError_t launch_metrics(SimParams p, FieldParams f, const float* sdf, const float4* pos, const float4* vel,
-                           uint32_t n, float* accum_f, double* accum_d, uint32_t* accum_u, cudaStream_t st) {
+                           const uint32_t* nbr_count, uint32_t n, float* accum_f, double* accum_d, uint32_t* accum_u,
+                           cudaStream_t st) {
   if (n == 0) return cudaSuccess;
-  k_metrics<<<blocks_for(n, 256), 256, 0, st>>>(p, f, sdf, pos, vel, n, accum_f, accum_d, accum_u);
+  k_metrics<<<blocks_for(n, 256), 256, 0, st>>>(p, f, sdf, pos, vel, nbr_count, n, accum_f, accum_d, accum_u);
   return cudaGetLastError();
 }
 

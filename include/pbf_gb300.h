@@ -285,6 +285,22 @@ const char* pbf_ns_last_error(const pbf_ns* ns);
  * 262144 limit).  Scratch is owned by the call's context. */
 int pbf_exclusive_scan_u32(const uint32_t* d_in, uint32_t* d_out, size_t n, void* stream);
 
+/* ---- allocation-free exclusive scan.  No counterpart in the reference: an
+ * addition for callers that cannot allocate device memory when they scan —
+ * hosts whose own pool owns all device memory, real-time loops that must not
+ * enter the allocator, code running during stream capture.  Same result as
+ * pbf_exclusive_scan_u32, but the look-back scratch is a fixed static device
+ * array of about 256 KB that every GPU loading this library keeps until
+ * exit, and the call allocates nothing (no cudaMalloc / cudaMallocAsync /
+ * cudaFree).  Sizes above PBF_SCAN_NOALLOC_MAX elements return
+ * PBF_ECAPACITY without launching anything.  The first call on a device
+ * looks up the array's device address; make that first call before any
+ * stream capture on that device.  All calls on a device share the array:
+ * calls that overlap on the GPU (e.g. on unordered streams) race and give
+ * wrong results; serialise them.  Synchronises `stream` before returning. */
+#define PBF_SCAN_NOALLOC_MAX (1u << 26)
+int pbf_exclusive_scan_u32_noalloc(const uint32_t* d_in, uint32_t* d_out, size_t n, void* stream);
+
 #ifdef __cplusplus
 }
 #endif

@@ -21,6 +21,7 @@ UNITS = [
     ("pbf_passes_fast.cu", []),
     ("pbf_passes_exact.cu", ["-fmad=false"]),
     ("pbf_volume.cu", ["-fmad=false"]),
+    ("pbf_scan_static.cu", []),
 ]
 
 

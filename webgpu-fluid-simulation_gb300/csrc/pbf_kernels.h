@@ -39,7 +39,10 @@ void fill_pass_table(PassTable* tbl);
 }
 
 // ---- integer pipeline (pbf_sort.cu) ---------------------------------------------
-// Scratch of the single-pass scan for up to `n` elements, in bytes.
+// Elements per tile of the single-pass scan.
+constexpr size_t kScanTileElements = 2048;
+// Scratch of the single-pass scan for up to `n` elements, in bytes:
+// 256 bytes (tile counter) + one 8-byte status word per tile.
 size_t scan_scratch_bytes(size_t n);
 // Exclusive scan of n u32 (out may alias nothing in in).  `scratch` holds
 // scan_scratch_bytes(n) bytes; err receives PBF_DEVERR_SCAN_TIMEOUT when a

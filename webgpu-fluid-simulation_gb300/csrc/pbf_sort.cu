@@ -25,6 +25,7 @@ constexpr uint32_t kFull = 0xffffffffu;
 constexpr int kScanThreads = 256;
 constexpr int kScanItems = 8;
 constexpr int kScanTile = kScanThreads * kScanItems;  // 2048 elements per tile
+static_assert(kScanTile == (int)kScanTileElements, "scan tile size");
 constexpr uint32_t kFlagAggregate = 1u, kFlagPrefix = 2u;
 constexpr uint32_t kSpinLimit = 1u << 22;             // ~ tens of ms at worst, then give up
 

@@ -17,6 +17,7 @@ FP_FAST, FP_EXACT = 0, 1
 INTERP_CUBIC, INTERP_TRILINEAR = 0, 1
 (FIELD_POSITION, FIELD_VELOCITY, FIELD_ACCELERATION, FIELD_PREDICTED, FIELD_LAMBDA, FIELD_BOUNDARY,
  FIELD_OMEGA, FIELD_NORMAL, FIELD_DELTA_P, FIELD_NEIGHBOR_COUNT) = range(10)
+SCAN_NOALLOC_MAX = 1 << 26
 SCALAR_FIELDS = {FIELD_LAMBDA: "f4", FIELD_NEIGHBOR_COUNT: "u4"}
 
 u32, f32 = ctypes.c_uint32, ctypes.c_float
@@ -110,6 +111,7 @@ SIGNATURES = {
     "pbf_generate_volume_map": (ctypes.c_int, [ctypes.POINTER(Shape), u32, _UP, _FP, _FP, ctypes.c_float, u32, u32,
                                                _FP, _FP]),
     "pbf_volume_from_sdf": (ctypes.c_int, [_UP, _FP, _FP, ctypes.c_float, u32, u32, _FP, _FP]),
+    "pbf_exclusive_scan_u32_noalloc": (ctypes.c_int, [_P, _P, ctypes.c_size_t, _P]),
 }
 
 _lib = None

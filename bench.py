@@ -63,6 +63,15 @@ ALG_BYTES = {
 }
 
 
+# DRAM bytes (read + write) per launch from one `ncu --set full` capture of
+# the same workload (profiles/neighbor_passes_sphere_drop_1m_ncu.md); the
+# neighbour list (~185 MB) is the difference to the algorithmic bytes.
+NCU_TRAFFIC_BYTES = {
+    "lambda": 208.0e6, "deltap_apply": 218.9e6, "xsph": 250.5e6, "nbr_list": 310.4e6, "nbr_count": 17.7e6,
+    "vorticity": 226.0e6, "boundary": 46.0e6,
+}
+
+
 def parse_args():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -358,7 +367,8 @@ def gpu_arm(args, dist):
         achieved = bytes_launch / per_launch_s / 1e9
         total_ms = sum(v[1] for v in kt.values())
         roof = {"bound": "hbm", "kernel": name, "achieved": achieved, "peak": peak, "unit": "GB/s",
-                "frac": achieved / peak, "peak_kind": peak_kind, "traffic": None,
+                "frac": achieved / peak, "peak_kind": peak_kind,
+                "traffic": NCU_TRAFFIC_BYTES.get(name) if args.workload == "sphere_drop_1m" else None,
                 "alg_bytes_per_launch": bytes_launch, "avg_launch_ms": per_launch_s * 1000.0,
                 "share": tot_ms / total_ms if total_ms else None,
                 "passes": {k: {"launches": v[0], "ms": round(v[1], 4),

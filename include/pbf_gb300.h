@@ -122,6 +122,7 @@ typedef struct pbf_metrics {
   float mean_abs_density_err;/* mean_i |rho_i/rho0 - 1| */
   float max_abs_density_err; /* max_i |rho_i/rho0 - 1| */
   float kinetic_energy;      /* 0.5 m sum |v|^2 */
+  float mean_compression;    /* mean_i max(0, rho_i/rho0 - 1) */
   uint32_t neighbor_total;   /* neighbour-list entries of the last substep */
   uint32_t fallback_steps;   /* learned-start substeps that fell back to the plain solve */
 } pbf_metrics;

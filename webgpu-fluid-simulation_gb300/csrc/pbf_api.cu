@@ -562,7 +562,7 @@ int pbf_create(const pbf_config* cfg, pbf_handle** out) {
   A(h->lambda.alloc(cap));
   A(h->err_word.alloc(1));
   A(h->m_f.alloc(2));
-  A(h->m_d.alloc(2));
+  A(h->m_d.alloc(3));
   A(h->m_u.alloc(3));
   size_t sb = scan_scratch_bytes(cells + 1);
   size_t sb2 = scan_scratch_bytes(cap + 1);
@@ -1032,14 +1032,14 @@ int pbf_get_metrics(pbf_handle* h, pbf_metrics* out) {
   out->particles = h->n;
   cudaStream_t st = h->stream;
   CU(h, cudaMemsetAsync(h->m_f.p, 0, 2 * sizeof(float), st));
-  CU(h, cudaMemsetAsync(h->m_d.p, 0, 2 * sizeof(double), st));
+  CU(h, cudaMemsetAsync(h->m_d.p, 0, 3 * sizeof(double), st));
   CU(h, cudaMemsetAsync(h->m_u.p, 0, 3 * sizeof(uint32_t), st));
   SimParams p = h->sp;
   p.n = h->n;
   CU(h, launch_metrics(p, h->fp, h->fp.loaded ? h->sdf.p : nullptr, h->pos[h->cur].p, h->vel.p, h->nbr_count.p,
                        h->n, h->m_f.p, h->m_d.p, h->m_u.p, st));
   float mf[2];
-  double md[2];
+  double md[3];
   uint32_t mu[3], errw = 0;
   CU(h, cudaMemcpyAsync(mf, h->m_f.p, sizeof(mf), cudaMemcpyDeviceToHost, st));
   CU(h, cudaMemcpyAsync(md, h->m_d.p, sizeof(md), cudaMemcpyDeviceToHost, st));
@@ -1050,6 +1050,7 @@ int pbf_get_metrics(pbf_handle* h, pbf_metrics* out) {
   out->max_abs_density_err = mf[1];
   out->mean_abs_density_err = h->n ? (float)(md[0] / h->n) : 0.0f;
   out->kinetic_energy = (float)md[1];
+  out->mean_compression = h->n ? (float)(md[2] / h->n) : 0.0f;
   out->nonfinite = mu[0];
   out->penetrations = mu[1];
   out->error_flags = errw;

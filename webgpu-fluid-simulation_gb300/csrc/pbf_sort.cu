@@ -385,7 +385,7 @@ __global__ void __launch_bounds__(256) k_metrics(SimParams p, FieldParams f, con
                                                  double* accum_d, uint32_t* accum_u) {
   uint32_t t = blockIdx.x * blockDim.x + threadIdx.x;
   float comp = 0.f, aerr = 0.f;
-  double ke = 0.0, serr = 0.0;
+  double ke = 0.0, serr = 0.0, scomp = 0.0;
   uint32_t bad = 0, pen = 0, nb = 0;
   if (t < n) {
     if (nbr_count) nb = nbr_count[t];
@@ -399,6 +399,7 @@ __global__ void __launch_bounds__(256) k_metrics(SimParams p, FieldParams f, con
       comp = fmaxf(0.0f, e);
       aerr = fabsf(e);
       serr = aerr;
+      scomp = comp;
       ke = 0.5 * (double)p.m * ((double)v.x * v.x + (double)v.y * v.y + (double)v.z * v.z);
       if (f.loaded && sdf) {
         CellLoc L = field_locate(f, mk(x.x, x.y, x.z));
@@ -419,6 +420,7 @@ __global__ void __launch_bounds__(256) k_metrics(SimParams p, FieldParams f, con
     aerr = fmaxf(aerr, __shfl_xor_sync(kFull, aerr, o));
     ke += __shfl_xor_sync(kFull, ke, o);
     serr += __shfl_xor_sync(kFull, serr, o);
+    scomp += __shfl_xor_sync(kFull, scomp, o);
     bad += __shfl_xor_sync(kFull, bad, o);
     pen += __shfl_xor_sync(kFull, pen, o);
     nb += __shfl_xor_sync(kFull, nb, o);
@@ -428,6 +430,7 @@ __global__ void __launch_bounds__(256) k_metrics(SimParams p, FieldParams f, con
     atomic_max_pos_float(accum_f + 1, aerr);
     atomicAdd(accum_d + 0, serr);
     atomicAdd(accum_d + 1, ke);
+    atomicAdd(accum_d + 2, scomp);
     atomicAdd(accum_u + 0, bad);
     atomicAdd(accum_u + 1, pen);
     atomicAdd(accum_u + 2, nb);

@@ -40,7 +40,8 @@ class Config(ctypes.Structure):
 class Metrics(ctypes.Structure):
     _fields_ = [("particles", u32), ("nonfinite", u32), ("penetrations", u32), ("error_flags", u32),
                 ("max_compression", f32), ("mean_abs_density_err", f32), ("max_abs_density_err", f32),
-                ("kinetic_energy", f32), ("neighbor_total", u32), ("fallback_steps", u32)]
+                ("kinetic_energy", f32), ("mean_compression", f32), ("neighbor_total", u32),
+                ("fallback_steps", u32)]
 
 
 SHAPE_BOX_CONTAINER, SHAPE_SPHERE, SHAPE_CYLINDER, SHAPE_TORUS, SHAPE_BOX_SOLID = range(5)

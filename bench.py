@@ -83,6 +83,9 @@ def parse_args():
     ap.add_argument("--graph", action="store_true", help="replay the frame as a CUDA graph")
     ap.add_argument("--settle", type=int, default=150,
                     help="frames advanced from the initial lattice to build the input state (untimed set-up)")
+    ap.add_argument("--no-learned", action="store_true", help="skip the learned warm-start measurement")
+    ap.add_argument("--bound", type=float, default=0.01,
+                    help="learned start: fall back to the plain solve when the mean compression exceeds this")
     return ap.parse_args()
 
 
@@ -307,9 +310,27 @@ def gpu_arm(args, dist):
     n = sc.n
     sub = cfg.substeps
     iters = cfg.options.iterations
-    # input state: the scene after `settle` frames (past the impact), resident on the device
-    sim.step(args.settle)
+    # input state: the scene after `settle` frames (past the impact), resident on
+    # the device; the last third of the settling run is traced for training
+    trace_from = (2 * args.settle) // 3
+    sim.step(trace_from)
+    if not args.no_learned:
+        sim.set_trace(2_000_000, stride=max(1, n // 20000), salt=12345)
+    sim.step(args.settle - trace_from)
     sim.synchronize()
+    model = None
+    train_info = None
+    if not args.no_learned:
+        from pbf_gb300 import mlp_init, mlp_fit_normalization, mlp_train
+        feat, tgt = sim.trace()
+        sim.set_trace(0)
+        model = mlp_init(7)
+        mlp_fit_normalization(model, feat, tgt)
+        t0 = time.perf_counter()
+        loss = mlp_train(model, feat, tgt, epochs=10, batch=8192, lr=3e-3, seed=7)
+        train_info = {"rows": int(len(tgt)), "epochs": 10, "batch": 8192, "final_mse_normalised": loss,
+                      "seconds": time.perf_counter() - t0}
+    snap = (sim.positions(), sim.velocities())
     for _ in range(max(args.warmup, 3)):
         sim.step(1)
     sim.synchronize()
@@ -389,6 +410,8 @@ def gpu_arm(args, dist):
                           "nonfinite": m["nonfinite"], "neighbors_per_particle": m["neighbor_total"] / max(n, 1)},
     }
     sim.close()
+    if model is not None:
+        line["learned"] = learned_arm(args, sc, snap, model, train_info, dist)
     if dist.rank == 0 and dist.world == 1 and not args.no_cpu_baseline:
         v, secs, cnt, cores, done = cpu_sample(sc, sc.n, sub)
         line["cpu_baseline"] = {"value": v, "unit": UNIT, "cores": cores, "kind": "port",
@@ -396,6 +419,67 @@ def gpu_arm(args, dist):
                                           "state, CPU restatement with OpenMP" % (cnt, done, secs)}
     if dist.rank == 0:
         print(json.dumps(line), flush=True)
+
+
+def _handle_from(sc, snap, iterations=None):
+    from pbf_gb300 import PBF, scenes
+    c = scenes.copy_config(sc.config)
+    if iterations is not None:
+        c.options.iterations = iterations
+    sim = PBF(c)
+    sim.set_particles(snap[0])
+    sim.set_velocities(snap[1])
+    f = sc.field
+    sim.set_boundary_field(f["res"], f["origin"], f["extent"], f["sdf"], f["vol"])
+    return sim
+
+
+def learned_arm(args, sc, snap, model, train_info, dist):
+    """Learned start (+2 iterations, plain-4 fallback above the bound) against
+    the plain 4-iteration solve, both from the same input state: throughput
+    over the timed region and mean compression per step afterwards."""
+    import torch
+    n, sub = sc.n, sc.config.substeps
+    out = {"training": train_info, "iterations": 2, "fallback_bound_mean_compression": args.bound}
+    sim = _handle_from(sc, snap)
+    sim.set_learned(model, iterations=2, fallback_bound=args.bound)
+    for _ in range(max(args.warmup, 3)):
+        sim.step(1)
+    sim.synchronize()
+    fb0 = sim.metrics()["fallback_steps"]
+    stream = torch.cuda.ExternalStream(sim.stream)
+    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    sim.set_kernel_timing(True)
+    sim.kernel_timing()
+    dist.barrier()
+    torch.cuda.synchronize()
+    ev0.record(stream)
+    for _ in range(args.steps):
+        sim.step(1)
+    ev1.record(stream)
+    ev1.synchronize()
+    ms = dist.max(ev0.elapsed_time(ev1))
+    kt = sim.kernel_timing()
+    sim.set_kernel_timing(False)
+    fb = sim.metrics()["fallback_steps"] - fb0
+    out.update({"value": dist.world * n * sub * args.steps / (ms / 1000.0), "ms_per_step": ms / args.steps,
+                "fallback_substeps": int(fb), "timed_substeps": sub * args.steps,
+                "passes_ms": {k: round(v[1], 4) for k, v in kt.items()}})
+    sim.close()
+    # density error from the same state, per step, outside any timed region
+    errs = {}
+    for name, mdl, iters in (("plain4", None, None), ("plain2", None, 2), ("learned2", model, None)):
+        h = _handle_from(sc, snap, iterations=iters)
+        if mdl is not None:
+            h.set_learned(mdl, iterations=2, fallback_bound=1e9)  # the network alone, no fallback
+        e = []
+        for _ in range(max(args.steps, 10)):
+            h.step(1)
+            e.append(h.metrics()["mean_compression"])
+        errs[name] = {"mean_compression": float(np.mean(e)), "max_step_mean_compression": float(np.max(e))}
+        h.close()
+    out["density_error_same_state"] = errs
+    return out
 
 
 def main():

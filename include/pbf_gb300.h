@@ -286,6 +286,51 @@ const char* pbf_ns_last_error(const pbf_ns* ns);
  * 262144 limit).  Scratch is owned by the call's context. */
 int pbf_exclusive_scan_u32(const uint32_t* d_in, uint32_t* d_out, size_t n, void* stream);
 
+/* ---- learned lambda warm start.  No counterpart in the reference (its solve
+ * is a fixed number of plain iterations, PBF.ts:417-431): an MLP
+ * 8 -> 64 -> 64 -> 1 (SiLU, BF16 weights/activations, FP32 accumulate)
+ * predicts an effective multiplier per particle from features at the
+ * predicted positions: density error, previous substep's multiplier,
+ * neighbour count, |v'| dt/h, div(v') dt, boundary SDF/h, boundary volume/V,
+ * substep index.  One projection with it (ConstrainSolve with lambda_hat)
+ * is followed by `iterations` plain iterations; when the mean compression
+ * max(0, rho/rho0 - 1) measured in the last iteration exceeds
+ * `fallback_bound`, the substep is re-solved from its predicted positions
+ * with the plain solve (options.iterations), on the device, without a host
+ * round trip.  Training targets are the sums of the plain solver's
+ * per-iteration multipliers, captured by the trace below. */
+#define PBF_MLP_PARAMS 4801  /* W1 8x64, b1 64, W2 64x64, b2 64, w3 64, b3 */
+typedef struct pbf_mlp {
+  float params[PBF_MLP_PARAMS];
+  float feat_mean[8];
+  float feat_inv_std[8];
+  float lam_scale;          /* target scale: the network predicts lambda / lam_scale */
+} pbf_mlp;
+typedef struct pbf_train_config {
+  uint32_t epochs;
+  uint32_t batch;
+  float learning_rate;      /* Adam, cosine-decayed over the epochs */
+  uint32_t reserved;
+  uint64_t seed;
+} pbf_train_config;
+int pbf_mlp_init(pbf_mlp* m, uint64_t seed);
+int pbf_mlp_fit_normalization(pbf_mlp* m, const float* feat, const float* target, uint32_t rows);
+/* Host arrays: feat rows x 8 (raw features), out rows (lambda_hat). */
+int pbf_mlp_forward(const pbf_mlp* m, const float* feat, uint32_t rows, float* out);
+/* Gradient of mean((y - target/lam_scale)^2) w.r.t. params (PBF_MLP_PARAMS floats), one GPU pass. */
+int pbf_mlp_gradient(const pbf_mlp* m, const float* feat, const float* target, uint32_t rows, float* grad,
+                     float* loss);
+int pbf_mlp_train(pbf_mlp* m, const float* feat, const float* target, uint32_t rows,
+                  const pbf_train_config* cfg, float* final_loss);
+/* Trace capture during plain substeps: every `stride`-th particle (hashed
+ * with `salt`) appends (features, target) rows until `capacity`; 0 = off. */
+int pbf_set_trace(pbf_handle* h, uint32_t capacity, uint32_t stride, uint64_t salt);
+int pbf_trace_rows(pbf_handle* h, uint32_t* rows);
+int pbf_copy_trace(pbf_handle* h, float* feat, float* target, uint32_t rows);
+/* model = NULL switches the learned start off.  A negative bound makes every
+ * substep fall back (the result is then the plain solve's). */
+int pbf_set_learned(pbf_handle* h, const pbf_mlp* model, uint32_t iterations, float fallback_bound);
+
 /* ---- allocation-free exclusive scan.  No counterpart in the reference: an
  * addition for callers that cannot allocate device memory when they scan —
  * hosts whose own pool owns all device memory, real-time loops that must not

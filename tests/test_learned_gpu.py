@@ -1,0 +1,166 @@
+"""The learned lambda warm start: BF16 mma MLP kernels against an FP64 CPU
+reference, training, the device-side fallback, and the gain over the method
+without the network."""
+import ctypes
+
+import numpy as np
+import pytest
+
+from oracle import mlp_ref
+from pbf_gb300 import PBF, scenes
+from pbf_gb300 import _lib as L
+from pbf_gb300 import mlp_fit_normalization, mlp_forward, mlp_gradient, mlp_init, mlp_params, mlp_train
+
+pytestmark = pytest.mark.gpu
+
+
+def random_model(seed, rows=1024):
+    rng = np.random.default_rng(seed)
+    m = mlp_init(seed)
+    feat = rng.normal(size=(rows, 8)).astype(np.float32) * np.array([0.02, 1e-5, 30, 0.2, 0.01, 1.5, 0.3, 1],
+                                                                     np.float32)
+    feat += np.array([0.0, -2e-5, 35, 0.1, 0.0, 1.0, 0.1, 0.5], np.float32)
+    target = (feat[:, 0] * -3e-4 + feat[:, 1] * 0.7).astype(np.float32)
+    mlp_fit_normalization(m, feat, target)
+    # non-trivial biases
+    p = np.ctypeslib.as_array(m.params)
+    p[mlp_ref.OFF_B1:mlp_ref.OFF_W2] = rng.normal(size=64).astype(np.float32) * 0.1
+    p[mlp_ref.OFF_B2:mlp_ref.OFF_W3] = rng.normal(size=64).astype(np.float32) * 0.1
+    p[mlp_ref.OFF_B3] = 0.05
+    return m, feat, target
+
+
+def norm_of(m):
+    return (np.ctypeslib.as_array(m.feat_mean).copy(), np.ctypeslib.as_array(m.feat_inv_std).copy(),
+            float(m.lam_scale))
+
+
+def test_mlp_forward_matches_fp64_reference():
+    m, feat, _ = random_model(1, rows=1000)  # not a multiple of 16: ragged last tile
+    got = mlp_forward(m, feat)
+    mean, istd, scale = norm_of(m)
+    ref = mlp_ref.forward(mlp_params(m), mean, istd, scale, feat, emulate=True)["lam"]
+    exact = mlp_ref.forward(mlp_params(m), mean, istd, scale, feat, emulate=False)["lam"]
+    scl = np.abs(ref).max()
+    assert np.abs(got - ref).max() <= 2e-3 * scl          # same bf16 rounding points, FP32 accumulation
+    assert np.abs(got - exact).max() <= 3e-2 * scl        # against full FP64 (bf16 quantisation)
+
+
+def test_mlp_gradient_matches_fp64_reference():
+    m, feat, target = random_model(2, rows=777)
+    g, loss = mlp_gradient(m, feat, target)
+    mean, istd, scale = norm_of(m)
+    ge, le = mlp_ref.gradient(mlp_params(m), mean, istd, scale, feat, target, emulate=True)
+    gx, _ = mlp_ref.gradient(mlp_params(m), mean, istd, scale, feat, target, emulate=False)
+    assert abs(loss - le) <= 1e-3 * max(le, 1e-12)
+    blocks = [(mlp_ref.OFF_W1, mlp_ref.OFF_B1), (mlp_ref.OFF_B1, mlp_ref.OFF_W2), (mlp_ref.OFF_W2, mlp_ref.OFF_B2),
+              (mlp_ref.OFF_B2, mlp_ref.OFF_W3), (mlp_ref.OFF_W3, mlp_ref.OFF_B3), (mlp_ref.OFF_B3, 4801)]
+    for a, b in blocks:
+        ref = ge[a:b]
+        err = np.linalg.norm(g[a:b] - ref) / max(np.linalg.norm(ref), 1e-30)
+        assert err <= 2e-2, (a, b, err)
+        cos = float(np.dot(g[a:b], gx[a:b]) / max(np.linalg.norm(g[a:b]) * np.linalg.norm(gx[a:b]), 1e-30))
+        assert cos >= 0.99, (a, b, cos)
+
+
+def test_training_reduces_loss():
+    rng = np.random.default_rng(3)
+    feat = rng.normal(size=(50000, 8)).astype(np.float32)
+    target = (np.tanh(feat[:, 0]) - 0.5 * feat[:, 1] * feat[:, 2] + 0.1 * feat[:, 3]).astype(np.float32) * 1e-5
+    m = mlp_init(3)
+    mlp_fit_normalization(m, feat, target)
+    _, l0 = mlp_gradient(m, feat, target)
+    loss = mlp_train(m, feat, target, epochs=30, batch=2048, lr=3e-3, seed=3)
+    _, l1 = mlp_gradient(m, feat, target)
+    assert l1 < 0.05 * l0 and loss < 0.05 * l0, (l0, l1, loss)
+
+
+def test_trace_target_is_sum_of_iteration_multipliers():
+    sc = scenes.reference_scene("cube_small", options=dict(iterations=1))
+    sim = PBF(sc.config)
+    sim.set_particles(scenes.jitter(sc.particles, 0.001, seed=4))
+    sim.set_trace(10 * sc.n, stride=1)
+    sim.run()
+    feat, tgt = sim.trace()
+    lam = sim.copy_field(L.FIELD_LAMBDA)
+    assert len(tgt) == sc.n
+    assert np.array_equal(np.sort(tgt), np.sort(lam))  # one iteration: target == its lambda
+    nb = sim.copy_field(L.FIELD_NEIGHBOR_COUNT)
+    assert np.array_equal(np.sort(feat[:, 2].astype(np.uint32)), np.sort(nb))
+    sim.close()
+
+
+def test_always_fallback_equals_plain_solve_bitexact():
+    """With a negative bound every substep falls back to the plain solve from
+    its predicted positions: the learned path then reproduces the plain path
+    bit for bit (exact mode), including the network and feature passes that
+    ran before the fallback."""
+    sc = scenes.reference_scene("boundary_small", fp_mode=L.FP_EXACT)
+    pts = scenes.jitter(sc.particles, 0.001, seed=6)
+    f = sc.field
+    a, b = PBF(sc.config), PBF(sc.config)
+    for s in (a, b):
+        s.set_particles(pts)
+        s.set_boundary_field(f["res"], f["origin"], f["extent"], f["sdf"], f["vol"])
+    m, _, _ = random_model(7)
+    b.set_learned(m, iterations=2, fallback_bound=-1.0)
+    for _ in range(3):
+        a.run()
+        b.run()
+    assert np.array_equal(a.positions(), b.positions())
+    assert np.array_equal(a.velocities(), b.velocities())
+    assert b.metrics()["fallback_steps"] == 3
+    a.close()
+    b.close()
+
+
+def _state(sim):
+    return sim.positions(), sim.velocities()
+
+
+def _run_mean_compression(cfg, field, state, frames, model=None, iters=None, learned_iters=2):
+    c = scenes.copy_config(cfg)
+    if iters is not None:
+        c.options.iterations = iters
+    sim = PBF(c)
+    x, v = state
+    sim.set_particles(x)
+    sim.set_velocities(v)
+    sim.set_boundary_field(field["res"], field["origin"], field["extent"], field["sdf"], field["vol"])
+    if model is not None:
+        sim.set_learned(model, iterations=learned_iters, fallback_bound=1e9)
+    errs = []
+    for _ in range(frames):
+        sim.step(1)
+        errs.append(sim.metrics()["mean_compression"])
+    m = sim.metrics()
+    sim.close()
+    return float(np.mean(errs)), m
+
+
+def test_learned_start_gain_over_plain_two_iterations():
+    """Train on plain 4-iteration traces of a dam break, then compare from the
+    same state: learned start + 2 iterations against plain 2 and plain 4."""
+    cfg, pts, fa = scenes.dam_break_16k_spec()
+    field = scenes.generate_field(fa["shapes"], (32, 32, 32), fa["origin"], fa["extent"], fa["h"], quadrature=8)
+    sim = PBF(cfg)
+    sim.set_particles(pts)
+    sim.set_boundary_field(field["res"], field["origin"], field["extent"], field["sdf"], field["vol"])
+    sim.step(40)  # the column collapses and hits the far wall
+    sim.set_trace(400000, stride=2, salt=11)
+    sim.step(40)
+    feat, tgt = sim.trace()
+    state = _state(sim)
+    sim.close()
+    assert len(tgt) > 100000
+    m = mlp_init(5)
+    mlp_fit_normalization(m, feat, tgt)
+    loss = mlp_train(m, feat, tgt, epochs=20, batch=4096, lr=3e-3, seed=5)
+    assert loss < 0.5  # normalised MSE well below the target variance (1.0)
+    e2, _ = _run_mean_compression(cfg, field, state, 20, iters=2)
+    e4, _ = _run_mean_compression(cfg, field, state, 20, iters=4)
+    el, ml = _run_mean_compression(cfg, field, state, 20, model=m)
+    print("mean compression: plain-2 %.5f  plain-4 %.5f  learned+2 %.5f" % (e2, e4, el))
+    assert ml["nonfinite"] == 0
+    assert e4 < e2
+    assert el < e2  # the network's start beats the method without it at equal iterations

@@ -22,6 +22,7 @@ UNITS = [
     ("pbf_passes_exact.cu", ["-fmad=false"]),
     ("pbf_volume.cu", ["-fmad=false"]),
     ("pbf_scan_static.cu", []),
+    ("pbf_learned.cu", []),
 ]
 
 

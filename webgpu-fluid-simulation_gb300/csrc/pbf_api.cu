@@ -77,6 +77,21 @@ struct pbf_handle {
   bool graph_valid = false;
   cudaEvent_t ev[5] = {nullptr, nullptr, nullptr, nullptr, nullptr};
   uint32_t last_nbr_total = 0;
+  // learned start and trace capture
+  bool learned = false;
+  uint32_t learned_iters = 2;
+  float fallback_bound = 0.01f;
+  pbf_mlp model;
+  DBuf<float> mlp_params, lam_sum, lam_prev, bsdf, fb_mean;
+  DBuf<float4> feat, xs_save;
+  DBuf<SolveStats> stats;
+  DBuf<int> fb_flag;
+  DBuf<uint32_t> fb_count;
+  uint32_t trace_cap = 0, trace_stride = 1;
+  uint64_t trace_salt = 0;
+  uint32_t substep_counter = 0;
+  DBuf<float> trace_feat, trace_tgt;
+  DBuf<uint32_t> trace_count;
   // per-kernel timing (pbf_set_kernel_timing)
   bool ktiming = false;
   std::vector<cudaEvent_t> kt_events;
@@ -87,11 +102,11 @@ namespace {
 
 enum PassId {
   K_PREDICT, K_SORT, K_GATHER, K_NBR_COUNT, K_NBR_SCAN, K_NBR_LIST, K_BOUNDARY, K_LAMBDA, K_DELTAP, K_DENSITY,
-  K_VORTICITY, K_XSPH, K_EXPORT, K_NUM
+  K_VORTICITY, K_XSPH, K_EXPORT, K_FEATURES, K_MLP, K_NUM
 };
 const char* kPassNames[K_NUM] = {"predict",  "sort",   "gather",       "nbr_count",        "nbr_scan",
                                  "nbr_list", "boundary", "lambda",     "deltap_apply",     "density_velocity",
-                                 "vorticity", "xsph",   "export"};
+                                 "vorticity", "xsph",   "export",       "features",         "mlp"};
 
 // Brackets one launch (or one group of launches) with events when timing is on.
 struct KScope {
@@ -272,6 +287,8 @@ int substep(pbf_handle* h, cudaEvent_t* ev) {
     CU(h, launch_gather_state(n, h->perm.p, h->pos[c].p, h->xs[1].p, h->ids[c].p, h->pos[nx].p, h->xs[0].p,
                               h->ids[nx].p, st));
   }
+  const bool need_feat = h->learned || h->trace_cap > 0;
+  if (need_feat) CU(h, launch_gather_f32(n, h->perm.p, h->lam_sum.p, h->lam_prev.p, st));
   h->cur = nx;
   const int cc = nx;
   // NeighborCount + particle scan + NeighborList
@@ -296,32 +313,116 @@ int substep(pbf_handle* h, cudaEvent_t* ev) {
   CU(h, cudaGetLastError());
   if (ev) CU(h, cudaEventRecord(ev[2], st));
   // constraint loop
-  int a = 0;
   const FieldParams f = h->fp;
   const uint32_t cap = h->nbr_capacity;
-  for (uint32_t it = 0; it < h->cfg.options.iterations; ++it) {
+  const float sub_index = (float)(h->substep_counter % h->cfg.substeps);
+  // `iters` plain iterations starting from xs[a]; returns the buffer holding
+  // the result.  aux0 is used by the first iteration's lambda pass (features
+  // and/or starting lam_sum), stats by the last one; guard makes every
+  // launch conditional on the device flag (fallback path).
+  auto iterate = [&](int a, uint32_t iters, bool feat_first, bool lam_sum_on, bool first_starts_sum,
+                     SolveStats* stats, const int* guard, int* rc) -> int {
+    for (uint32_t it = 0; it < iters; ++it) {
+      SolverAux ab{};
+      ab.guard = guard;
+      if (need_feat && feat_first && it == 0) ab.bsdf = h->bsdf.p;
+      if (f.loaded) {
+        KScope ks(h, K_BOUNDARY);
+        h->passes.boundary<<<nblocks(n, 256), 256, 0, st>>>(p, f, h->sdf.p, h->vol.p, h->bflag.p, h->xs[a].p,
+                                                             h->bdata.p, ab);
+      }
+      if (cudaGetLastError() != cudaSuccess) { *rc = PBF_ECUDA; return a; }
+      SolverAux al{};
+      al.guard = guard;
+      if (lam_sum_on) {
+        al.lam_sum = h->lam_sum.p;
+        al.lam_first = (first_starts_sum && it == 0) ? 1 : 0;
+      }
+      if (stats && it + 1 == iters) al.stats = stats;
+      const bool fe = feat_first && it == 0;
+      if (fe) {
+        al.feat = h->feat.p;
+        al.pos = h->pos[cc].p;
+        al.lam_prev = h->lam_prev.p;
+        al.bsdf = f.loaded ? h->bsdf.p : nullptr;
+        al.substep_index = sub_index;
+      }
+      {
+        KScope ks(h, K_LAMBDA);
+        auto kl = fe ? h->passes.lambda_feat : h->passes.lambda;
+        kl<<<nblocks(n, 256), 256, 0, st>>>(p, f.loaded, h->bdata.p, h->xs[a].p, h->warp_off.p, h->nbr_count.p,
+                                             h->nbr_list.p, cap, h->lambda.p, al);
+      }
+      if (cudaGetLastError() != cudaSuccess) { *rc = PBF_ECUDA; return a; }
+      SolverAux ad{};
+      ad.guard = guard;
+      {
+        KScope ks(h, K_DELTAP);
+        h->passes.deltap<<<nblocks(n, 256), 256, 0, st>>>(p, ad, f.loaded, h->xs[a].p, h->lambda.p, h->bdata.p,
+                                                           h->warp_off.p, h->nbr_count.p, h->nbr_list.p, cap,
+                                                           h->xs[1 - a].p, h->capture ? h->dp.p : nullptr);
+      }
+      if (cudaGetLastError() != cudaSuccess) { *rc = PBF_ECUDA; return a; }
+      a = 1 - a;
+    }
+    *rc = PBF_OK;
+    return a;
+  };
+  int a = 0, rc = PBF_OK;
+  if (h->learned) {
+    // learned start: features at x*_0 -> lambda_hat -> one projection ->
+    // learned_iters plain iterations -> device-side fallback test
+    CU(h, cudaMemcpyAsync(h->xs_save.p, h->xs[0].p, (size_t)n * sizeof(float4), cudaMemcpyDeviceToDevice, st));
+    SolverAux ab{};
+    ab.bsdf = h->bsdf.p;
     if (f.loaded) {
       KScope ks(h, K_BOUNDARY);
-      h->passes.boundary<<<nblocks(n, 256), 256, 0, st>>>(p, f, h->sdf.p, h->vol.p, h->bflag.p, h->xs[a].p,
-                                                           h->bdata.p);
+      h->passes.boundary<<<nblocks(n, 256), 256, 0, st>>>(p, f, h->sdf.p, h->vol.p, h->bflag.p, h->xs[0].p,
+                                                           h->bdata.p, ab);
+    }
+    CU(h, cudaGetLastError());
+    SolverAux al{};
+    al.feat = h->feat.p;
+    al.pos = h->pos[cc].p;
+    al.lam_prev = h->lam_prev.p;
+    al.bsdf = f.loaded ? h->bsdf.p : nullptr;
+    al.substep_index = sub_index;
+    {
+      KScope ks(h, K_FEATURES);
+      h->passes.lambda_feat<<<nblocks(n, 256), 256, 0, st>>>(p, f.loaded, h->bdata.p, h->xs[0].p, h->warp_off.p,
+                                                              h->nbr_count.p, h->nbr_list.p, cap, h->lambda.p, al);
     }
     CU(h, cudaGetLastError());
     {
-      KScope ks(h, K_LAMBDA);
-      h->passes.lambda<<<nblocks(n, 256), 256, 0, st>>>(p, f.loaded, h->bdata.p, h->xs[a].p, h->warp_off.p,
-                                                         h->nbr_count.p, h->nbr_list.p, cap, h->lambda.p);
+      KScope ks(h, K_MLP);
+      CU(h, launch_mlp_infer(h->mlp_params.p, h->model, (const float*)h->feat.p, n, h->lambda.p, h->lam_sum.p, st));
     }
-    CU(h, cudaGetLastError());
     {
       KScope ks(h, K_DELTAP);
-      h->passes.deltap<<<nblocks(n, 256), 256, 0, st>>>(p, f.loaded, h->xs[a].p, h->lambda.p, h->bdata.p,
+      SolverAux ad{};
+      h->passes.deltap<<<nblocks(n, 256), 256, 0, st>>>(p, ad, f.loaded, h->xs[0].p, h->lambda.p, h->bdata.p,
                                                          h->warp_off.p, h->nbr_count.p, h->nbr_list.p, cap,
-                                                         h->xs[1 - a].p,
-                                                         h->capture ? h->dp.p : nullptr);
+                                                         h->xs[1].p, nullptr);
     }
     CU(h, cudaGetLastError());
-    a = 1 - a;
+    a = iterate(1, h->learned_iters, false, true, false, h->stats.p, nullptr, &rc);
+    if (rc) return fail(h, rc, "learned solve launch failed");
+    CU(h, launch_fallback_decide(h->stats.p, h->fallback_bound, h->fb_flag.p, h->fb_count.p, h->fb_mean.p, st));
+    // guarded plain solve from x*_0 (a no-op unless the flag is set)
+    CU(h, launch_copy_guarded(n, h->fb_flag.p, h->xs_save.p, h->xs[0].p, st));
+    int b = iterate(0, h->cfg.options.iterations, false, true, true, nullptr, h->fb_flag.p, &rc);
+    if (rc) return fail(h, rc, "fallback solve launch failed");
+    if (b != a) CU(h, launch_copy_guarded(n, h->fb_flag.p, h->xs[b].p, h->xs[a].p, st));
+  } else {
+    a = iterate(0, h->cfg.options.iterations, need_feat, need_feat, true, nullptr, nullptr, &rc);
+    if (rc) return fail(h, rc, "solve launch failed");
+    if (h->trace_cap > 0) {
+      CU(h, launch_trace_append(n, h->ids[cc].p, h->feat.p, h->lam_sum.p, h->trace_stride,
+                                (uint32_t)(h->trace_salt ^ (uint64_t)h->substep_counter * 0x9e3779b9ull),
+                                h->trace_feat.p, h->trace_tgt.p, h->trace_count.p, h->trace_cap, st));
+    }
   }
+  h->substep_counter++;
   if (ev) CU(h, cudaEventRecord(ev[3], st));
   // non-pressure passes
   {
@@ -410,6 +511,19 @@ void release_all(pbf_handle* h) {
   h->sdf.release();
   h->vol.release();
   h->bflag.release();
+  h->mlp_params.release();
+  h->lam_sum.release();
+  h->lam_prev.release();
+  h->bsdf.release();
+  h->fb_mean.release();
+  h->feat.release();
+  h->xs_save.release();
+  h->stats.release();
+  h->fb_flag.release();
+  h->fb_count.release();
+  h->trace_feat.release();
+  h->trace_tgt.release();
+  h->trace_count.release();
   h->m_f.release();
   h->m_d.release();
   if (h->scan_scratch) cudaFree(h->scan_scratch);
@@ -974,6 +1088,98 @@ int pbf_get_kernel_timing(pbf_handle* h, pbf_kernel_time* out, uint32_t max, uin
   return PBF_OK;
 }
 
+// Buffers shared by trace capture and the learned start (allocated on first use).
+static int ensure_feature_buffers(pbf_handle* h) {
+  const size_t cap = h->cfg.max_particles;
+  if (!h->feat.p) {
+    CU(h, h->feat.alloc(2 * cap));
+    CU(h, h->lam_sum.alloc(cap));
+    CU(h, h->lam_prev.alloc(cap));
+    CU(h, h->bsdf.alloc(cap));
+    CU(h, cudaMemsetAsync(h->lam_sum.p, 0, cap * sizeof(float), h->stream));
+    CU(h, cudaMemsetAsync(h->lam_prev.p, 0, cap * sizeof(float), h->stream));
+    CU(h, cudaMemsetAsync(h->bsdf.p, 0, cap * sizeof(float), h->stream));
+  }
+  return PBF_OK;
+}
+
+int pbf_set_trace(pbf_handle* h, uint32_t capacity, uint32_t stride, uint64_t salt) {
+  if (!h || stride == 0) return PBF_EINVAL;
+  invalidate_graph(h);
+  h->trace_feat.release();
+  h->trace_tgt.release();
+  h->trace_cap = 0;
+  if (capacity == 0) return PBF_OK;
+  int rc = ensure_feature_buffers(h);
+  if (rc) return rc;
+  CU(h, h->trace_feat.alloc((size_t)capacity * 8));
+  CU(h, h->trace_tgt.alloc(capacity));
+  if (!h->trace_count.p) CU(h, h->trace_count.alloc(1));
+  CU(h, cudaMemsetAsync(h->trace_count.p, 0, sizeof(uint32_t), h->stream));
+  CU(h, cudaStreamSynchronize(h->stream));
+  h->trace_cap = capacity;
+  h->trace_stride = stride;
+  h->trace_salt = salt;
+  return PBF_OK;
+}
+
+int pbf_trace_rows(pbf_handle* h, uint32_t* rows) {
+  if (!h || !rows) return PBF_EINVAL;
+  *rows = 0;
+  if (!h->trace_count.p) return PBF_OK;
+  uint32_t c = 0;
+  CU(h, cudaMemcpyAsync(&c, h->trace_count.p, sizeof(uint32_t), cudaMemcpyDeviceToHost, h->stream));
+  CU(h, cudaStreamSynchronize(h->stream));
+  *rows = c < h->trace_cap ? c : h->trace_cap;
+  return PBF_OK;
+}
+
+int pbf_copy_trace(pbf_handle* h, float* feat, float* target, uint32_t rows) {
+  if (!h || !feat || !target) return PBF_EINVAL;
+  uint32_t have = 0;
+  int rc = pbf_trace_rows(h, &have);
+  if (rc) return rc;
+  if (rows > have) return fail(h, PBF_EINVAL, "trace holds %u rows, %u requested", have, rows);
+  if (rows == 0) return PBF_OK;
+  CU(h, cudaMemcpyAsync(feat, h->trace_feat.p, (size_t)rows * 8 * sizeof(float), cudaMemcpyDeviceToHost, h->stream));
+  CU(h, cudaMemcpyAsync(target, h->trace_tgt.p, (size_t)rows * sizeof(float), cudaMemcpyDeviceToHost, h->stream));
+  CU(h, cudaStreamSynchronize(h->stream));
+  return PBF_OK;
+}
+
+int pbf_set_learned(pbf_handle* h, const pbf_mlp* model, uint32_t iterations, float fallback_bound) {
+  if (!h) return PBF_EINVAL;
+  invalidate_graph(h);
+  if (!model) {
+    h->learned = false;
+    return PBF_OK;
+  }
+  if (iterations == 0 || !std::isfinite(fallback_bound) || !(model->lam_scale > 0.0f))
+    return fail(h, PBF_EINVAL, "learned start needs iterations >= 1, a finite bound and lam_scale > 0");
+  int rc = ensure_feature_buffers(h);
+  if (rc) return rc;
+  const size_t cap = h->cfg.max_particles;
+  if (!h->mlp_params.p) {
+    CU(h, h->mlp_params.alloc(PBF_MLP_PARAMS));
+    CU(h, h->xs_save.alloc(cap));
+    CU(h, h->stats.alloc(1));
+    CU(h, h->fb_flag.alloc(1));
+    CU(h, h->fb_count.alloc(1));
+    CU(h, h->fb_mean.alloc(1));
+    CU(h, cudaMemsetAsync(h->stats.p, 0, sizeof(SolveStats), h->stream));
+    CU(h, cudaMemsetAsync(h->fb_flag.p, 0, sizeof(int), h->stream));
+    CU(h, cudaMemsetAsync(h->fb_count.p, 0, sizeof(uint32_t), h->stream));
+    CU(h, cudaMemsetAsync(h->fb_mean.p, 0, sizeof(float), h->stream));
+  }
+  h->model = *model;
+  CU(h, cudaMemcpyAsync(h->mlp_params.p, model->params, sizeof(model->params), cudaMemcpyHostToDevice, h->stream));
+  CU(h, cudaStreamSynchronize(h->stream));
+  h->learned_iters = iterations;
+  h->fallback_bound = fallback_bound;
+  h->learned = true;
+  return PBF_OK;
+}
+
 uint32_t pbf_particle_count(const pbf_handle* h) { return h ? h->n : 0; }
 const float* pbf_position_device(pbf_handle* h) { return h ? (const float*)h->out_pos.p : nullptr; }
 const float* pbf_velocity_device(pbf_handle* h) {
@@ -1055,6 +1261,11 @@ int pbf_get_metrics(pbf_handle* h, pbf_metrics* out) {
   out->penetrations = mu[1];
   out->error_flags = errw;
   out->neighbor_total = mu[2];
+  if (h->fb_count.p) {
+    uint32_t fb = 0;
+    CU(h, cudaMemcpy(&fb, h->fb_count.p, sizeof(uint32_t), cudaMemcpyDeviceToHost));
+    out->fallback_steps = fb;
+  }
   return PBF_OK;
 }
 

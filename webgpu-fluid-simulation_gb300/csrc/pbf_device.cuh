@@ -303,6 +303,31 @@ __device__ __forceinline__ f3 sum32v(const f3* w, const float* v) {
   return lo + hi;
 }
 
+// Interpolated SDF value only (the learned start's boundary feature).
+__device__ __forceinline__ float boundary_distance(const FieldParams& f, const float* __restrict__ sdf, f3 x) {
+  CellLoc L = field_locate(f, x);
+  uint32_t idx[32];
+  cell_nodes(f, L.i, L.j, L.k, false, idx);
+  if (f.trilinear) {
+    float tx = (L.s.x + 1.0f) * 0.5f, ty = (L.s.y + 1.0f) * 0.5f, tz = (L.s.z + 1.0f) * 0.5f;
+    float d = 0.0f;
+#pragma unroll
+    for (int q = 0; q < 8; ++q) {
+      int a = q & 1, b = (q >> 1) & 1, e = (q >> 2) & 1;
+      float wx = a ? tx : 1.0f - tx, wy = b ? ty : 1.0f - ty, wz = e ? tz : 1.0f - tz;
+      d = d + wx * wy * wz * __ldg(sdf + idx[q]);
+    }
+    return d;
+  }
+  float N[32];
+  f3 dN[32];
+  float val[32];
+  shape32(L.s, N, dN);
+#pragma unroll
+  for (int q = 0; q < 32; ++q) val[q] = __ldg(sdf + idx[q]);
+  return sum32(N, val);
+}
+
 // BoundaryVolume pass for one particle (src/simulator/PBF/shader/boundaryVolume.ts:31-55):
 // returns (x_b, V_b) or zero when the particle is outside the band 0 < d < h.
 __device__ __forceinline__ float4 boundary_sample(const SimParams& p, const FieldParams& f, const float* __restrict__ sdf,

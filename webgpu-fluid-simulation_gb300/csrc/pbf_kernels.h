@@ -18,11 +18,14 @@ struct PassTable {
                    uint32_t*);
   void (*nbr_list_sliced)(SimParams, GridParams, const float4*, const uint32_t*, const uint32_t*, uint32_t*, uint32_t,
                           uint32_t*);
-  void (*boundary)(SimParams, FieldParams, const float*, const float*, const uint8_t*, const float4*, float4*);
+  void (*boundary)(SimParams, FieldParams, const float*, const float*, const uint8_t*, const float4*, float4*,
+                   SolverAux);
   void (*lambda)(SimParams, int, const float4*, const float4*, const uint32_t*, const uint32_t*, const uint32_t*,
-                 uint32_t, float*);
-  void (*deltap)(SimParams, int, const float4*, const float*, const float4*, const uint32_t*, const uint32_t*,
-                 const uint32_t*, uint32_t, float4*, float4*);
+                 uint32_t, float*, SolverAux);
+  void (*lambda_feat)(SimParams, int, const float4*, const float4*, const uint32_t*, const uint32_t*,
+                      const uint32_t*, uint32_t, float*, SolverAux);
+  void (*deltap)(SimParams, SolverAux, int, const float4*, const float*, const float4*, const uint32_t*,
+                 const uint32_t*, const uint32_t*, uint32_t, float4*, float4*);
   void (*density_velocity)(SimParams, const float4*, const uint32_t*, const uint32_t*, const uint32_t*, uint32_t,
                            float4*, float4*);
   void (*vorticity)(SimParams, const float4*, const float4*, const uint32_t*, const uint32_t*, const uint32_t*,
@@ -101,4 +104,19 @@ cudaError_t launch_metrics(SimParams p, FieldParams f, const float* sdf, const f
                            const uint32_t* nbr_count, uint32_t n, float* accum_f, double* accum_d, uint32_t* accum_u,
                            cudaStream_t st);
 
+// Learned start (pbf_learned.cu).
+}  // namespace pbf
+#include "../../include/pbf_gb300.h"
+namespace pbf {
+cudaError_t launch_mlp_infer(const float* d_params, const pbf_mlp& model, const float* d_feat, uint32_t rows,
+                             float* d_lambda, float* d_lam_sum, cudaStream_t st);
+cudaError_t launch_mlp_grad(const float* d_params, const pbf_mlp& model, const float* d_feat, const float* d_target,
+                            uint32_t rows, float* d_grad, float* d_loss, cudaStream_t st);
+cudaError_t launch_gather_f32(uint32_t n, const uint32_t* perm, const float* src, float* dst, cudaStream_t st);
+cudaError_t launch_copy_guarded(uint32_t n, const int* guard, const float4* src, float4* dst, cudaStream_t st);
+cudaError_t launch_fallback_decide(SolveStats* stats, float bound, int* flag, uint32_t* fallbacks, float* last_mean,
+                                   cudaStream_t st);
+cudaError_t launch_trace_append(uint32_t n, const uint32_t* ids, const float4* feat, const float* lam_sum,
+                                uint32_t stride, uint32_t salt, float* tf, float* tt, uint32_t* count, uint32_t cap,
+                                cudaStream_t st);
 }  // namespace pbf

@@ -1,0 +1,710 @@
+// pbf_learned.cu — the learned lambda warm start: a per-particle MLP
+// 8 -> 64 -> 64 -> 1 (SiLU) with BF16 weights and activations and FP32
+// accumulation, run and trained with hand-written mma.sync.m16n8k16 kernels.
+//
+// The reference solves with a fixed number of plain PBF iterations
+// (src/simulator/PBF/PBF.ts:417-431) and recomputes lambda from scratch in
+// each (pressureConstrain.ts:80-83), so there is no lambda to warm-start in
+// the reference itself.  Here the network predicts an effective multiplier
+// lambda_hat_i; one projection with it (the ConstrainSolve formula with
+// lambda_hat in place of lambda) replaces the first iterations.  Its training
+// target is the sum of the multipliers of the plain solver's iterations in
+// the same substep: dp is linear in lambda for fixed positions, so one
+// projection with the sum reproduces the plain iterations' cumulative
+// correction to first order.
+//
+// Tiles: a warp owns 16 particles (rows).  The D fragment of one layer is the
+// A fragment of the next (no shared-memory round trip); weights are staged
+// in shared memory, transposed so every B-fragment register is one 32-bit
+// load.  Weight gradients (H1^T dZ2, X^T dZ1) are mma.sync products over the
+// rows of a 64-row block chunk, read through shared-memory transposes.
+#include <cmath>
+#include <cstdint>
+#include <cstring>
+#include <vector>
+
+#include <cuda_bf16.h>
+#include <cuda_runtime.h>
+
+#include "../../include/pbf_gb300.h"
+#include "pbf_kernels.h"
+
+namespace pbf {
+namespace {
+
+constexpr int kIn = 8, kH = 64;
+constexpr int OFF_W1 = 0, OFF_B1 = OFF_W1 + kIn * kH, OFF_W2 = OFF_B1 + kH, OFF_B2 = OFF_W2 + kH * kH,
+              OFF_W3 = OFF_B2 + kH, OFF_B3 = OFF_W3 + kH, kParams = OFF_B3 + 1;
+static_assert(kParams == PBF_MLP_PARAMS, "flat parameter layout");
+
+constexpr int kW1S = 24;  // bf16 row stride of W1^T in smem (16 + 8 pad)
+constexpr int kW2S = 72;  // bf16 row stride of 64-wide tiles (64 + 8 pad)
+
+struct Norm {
+  float mean[kIn];
+  float inv_std[kIn];
+  float lam_scale;
+};
+
+__device__ __forceinline__ uint32_t pack_bf16(float lo, float hi) {
+  __nv_bfloat162 v = __floats2bfloat162_rn(lo, hi);
+  return *reinterpret_cast<uint32_t*>(&v);
+}
+__device__ __forceinline__ uint32_t pack_raw(uint16_t lo, uint16_t hi) { return (uint32_t)lo | ((uint32_t)hi << 16); }
+__device__ __forceinline__ float bf16_round(float x) { return __bfloat162float(__float2bfloat16_rn(x)); }
+
+__device__ __forceinline__ void mma16816(float (&d)[4], const uint32_t (&a)[4], uint32_t b0, uint32_t b1) {
+  asm volatile(
+      "mma.sync.aligned.m16n8k16.row.col.f32.bf16.bf16.f32 {%0,%1,%2,%3}, {%4,%5,%6,%7}, {%8,%9}, "
+      "{%0,%1,%2,%3};\n"
+      : "+f"(d[0]), "+f"(d[1]), "+f"(d[2]), "+f"(d[3])
+      : "r"(a[0]), "r"(a[1]), "r"(a[2]), "r"(a[3]), "r"(b0), "r"(b1));
+}
+
+__device__ __forceinline__ float sigmoid_f(float z) { return 1.0f / (1.0f + __expf(-z)); }
+__device__ __forceinline__ float silu_f(float z) { return z * sigmoid_f(z); }
+__device__ __forceinline__ float dsilu_f(float z) {
+  float s = sigmoid_f(z);
+  return s * (1.0f + z * (1.0f - s));
+}
+
+// Stage W1^T (bf16, k padded to 16), W2^T and optionally W2 into shared memory.
+__device__ void stage_weights(const float* __restrict__ P, uint16_t* sW1t, uint16_t* sW2t, uint16_t* sW2) {
+  for (int q = threadIdx.x; q < kH * 16; q += blockDim.x) {
+    int n = q / 16, k = q % 16;
+    float w = (k < kIn) ? P[OFF_W1 + k * kH + n] : 0.0f;
+    __nv_bfloat16 b = __float2bfloat16_rn(w);
+    sW1t[n * kW1S + k] = *reinterpret_cast<uint16_t*>(&b);
+  }
+  for (int q = threadIdx.x; q < kH * kH; q += blockDim.x) {
+    int k = q / kH, n = q % kH;  // W2[k][n]
+    __nv_bfloat16 b = __float2bfloat16_rn(P[OFF_W2 + q]);
+    uint16_t u = *reinterpret_cast<uint16_t*>(&b);
+    sW2t[n * kW2S + k] = u;
+    if (sW2) sW2[k * kW2S + n] = u;
+  }
+}
+
+// Forward pass of one 16-row tile held by a warp.  x: normalised inputs of
+// rows g and g+8, features 2t and 2t+1 (the A fragment columns this lane
+// holds).  Returns z1/z2 pre-activations (for the backward pass), the bf16
+// A fragments of h1, and y for rows g and g+8 in every lane of the group.
+struct Fwd {
+  float z1[8][4];
+  float z2[8][4];
+  uint32_t a2[4][4];  // h1 as A fragments (k-steps of layer 2)
+  float h2[8][4];     // bf16-rounded h2
+  float y0, y8;
+};
+
+__device__ __forceinline__ void forward_tile(const float (&xg)[2], const float (&x8)[2], const uint16_t* sW1t,
+                                             const uint16_t* sW2t, const float* sB1, const float* sB2,
+                                             const float* sW3, float b3, Fwd& F) {
+  const int lane = threadIdx.x & 31, g = lane >> 2, t = lane & 3;
+  uint32_t a1[4] = {pack_bf16(xg[0], xg[1]), pack_bf16(x8[0], x8[1]), 0u, 0u};
+#pragma unroll
+  for (int j = 0; j < 8; ++j) {
+    int n = 8 * j + g;
+    uint32_t b0 = *reinterpret_cast<const uint32_t*>(sW1t + n * kW1S + 2 * t);
+    uint32_t b1 = *reinterpret_cast<const uint32_t*>(sW1t + n * kW1S + 8 + 2 * t);
+    float c0 = sB1[8 * j + 2 * t], c1 = sB1[8 * j + 2 * t + 1];
+    float d[4] = {c0, c1, c0, c1};
+    mma16816(d, a1, b0, b1);
+#pragma unroll
+    for (int q = 0; q < 4; ++q) F.z1[j][q] = d[q];
+  }
+#pragma unroll
+  for (int s = 0; s < 4; ++s) {
+    F.a2[s][0] = pack_bf16(silu_f(F.z1[2 * s][0]), silu_f(F.z1[2 * s][1]));
+    F.a2[s][1] = pack_bf16(silu_f(F.z1[2 * s][2]), silu_f(F.z1[2 * s][3]));
+    F.a2[s][2] = pack_bf16(silu_f(F.z1[2 * s + 1][0]), silu_f(F.z1[2 * s + 1][1]));
+    F.a2[s][3] = pack_bf16(silu_f(F.z1[2 * s + 1][2]), silu_f(F.z1[2 * s + 1][3]));
+  }
+  float yg = 0.0f, y8 = 0.0f;
+#pragma unroll
+  for (int j = 0; j < 8; ++j) {
+    int n = 8 * j + g;
+    float c0 = sB2[8 * j + 2 * t], c1 = sB2[8 * j + 2 * t + 1];
+    float d[4] = {c0, c1, c0, c1};
+#pragma unroll
+    for (int s = 0; s < 4; ++s) {
+      uint32_t b0 = *reinterpret_cast<const uint32_t*>(sW2t + n * kW2S + 16 * s + 2 * t);
+      uint32_t b1 = *reinterpret_cast<const uint32_t*>(sW2t + n * kW2S + 16 * s + 8 + 2 * t);
+      mma16816(d, F.a2[s], b0, b1);
+    }
+#pragma unroll
+    for (int q = 0; q < 4; ++q) {
+      F.z2[j][q] = d[q];
+      F.h2[j][q] = bf16_round(silu_f(d[q]));
+    }
+    float w0 = sW3[8 * j + 2 * t], w1 = sW3[8 * j + 2 * t + 1];
+    yg += F.h2[j][0] * w0 + F.h2[j][1] * w1;
+    y8 += F.h2[j][2] * w0 + F.h2[j][3] * w1;
+  }
+  yg += __shfl_xor_sync(0xffffffffu, yg, 1);
+  yg += __shfl_xor_sync(0xffffffffu, yg, 2);
+  y8 += __shfl_xor_sync(0xffffffffu, y8, 1);
+  y8 += __shfl_xor_sync(0xffffffffu, y8, 2);
+  F.y0 = yg + b3;
+  F.y8 = y8 + b3;
+}
+
+__device__ __forceinline__ void load_inputs(const float* __restrict__ feat, const Norm& nm, uint32_t rows,
+                                            uint32_t r0, float (&xg)[2], float (&x8)[2]) {
+  const int lane = threadIdx.x & 31, g = lane >> 2, t = lane & 3;
+  uint32_t ra = r0 + g, rb = r0 + g + 8;
+  float2 fa = (ra < rows) ? *reinterpret_cast<const float2*>(feat + 8 * (size_t)ra + 2 * t) : make_float2(0.f, 0.f);
+  float2 fb = (rb < rows) ? *reinterpret_cast<const float2*>(feat + 8 * (size_t)rb + 2 * t) : make_float2(0.f, 0.f);
+  int k0 = 2 * t, k1 = 2 * t + 1;
+  xg[0] = (ra < rows) ? (fa.x - nm.mean[k0]) * nm.inv_std[k0] : 0.0f;
+  xg[1] = (ra < rows) ? (fa.y - nm.mean[k1]) * nm.inv_std[k1] : 0.0f;
+  x8[0] = (rb < rows) ? (fb.x - nm.mean[k0]) * nm.inv_std[k0] : 0.0f;
+  x8[1] = (rb < rows) ? (fb.y - nm.mean[k1]) * nm.inv_std[k1] : 0.0f;
+}
+
+constexpr int kInferThreads = 128;
+
+// Inference: lambda_hat for each row (particle) of feat; also starts lam_sum.
+__global__ void __launch_bounds__(kInferThreads) k_mlp_infer(const float* __restrict__ P, Norm nm,
+                                                            const float* __restrict__ feat, uint32_t rows,
+                                                            float* __restrict__ lambda, float* __restrict__ lam_sum) {
+  __shared__ __align__(16) uint16_t sW1t[kH * kW1S];
+  __shared__ __align__(16) uint16_t sW2t[kH * kW2S];
+  __shared__ float sB1[kH], sB2[kH], sW3[kH];
+  stage_weights(P, sW1t, sW2t, nullptr);
+  for (int q = threadIdx.x; q < kH; q += blockDim.x) {
+    sB1[q] = P[OFF_B1 + q];
+    sB2[q] = P[OFF_B2 + q];
+    sW3[q] = P[OFF_W3 + q];
+  }
+  __syncthreads();
+  const float b3 = P[OFF_B3];
+  const int lane = threadIdx.x & 31, g = lane >> 2, t = lane & 3;
+  const uint32_t warps = gridDim.x * (blockDim.x >> 5);
+  for (uint32_t tile = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5); tile * 16 < rows; tile += warps) {
+    uint32_t r0 = tile * 16;
+    float xg[2], x8[2];
+    load_inputs(feat, nm, rows, r0, xg, x8);
+    Fwd F;
+    forward_tile(xg, x8, sW1t, sW2t, sB1, sB2, sW3, b3, F);
+    if (t == 0) {
+      uint32_t ra = r0 + g, rb = r0 + g + 8;
+      if (ra < rows) {
+        float l = F.y0 * nm.lam_scale;
+        lambda[ra] = l;
+        if (lam_sum) lam_sum[ra] = l;
+      }
+      if (rb < rows) {
+        float l = F.y8 * nm.lam_scale;
+        lambda[rb] = l;
+        if (lam_sum) lam_sum[rb] = l;
+      }
+    }
+  }
+}
+
+constexpr int kTrainWarps = 4;
+constexpr int kTrainRows = 16 * kTrainWarps;  // rows per block chunk
+constexpr int kTrainSmem = 2 * (kH * kW1S + 3 * kH * kW2S + kTrainRows * kW1S + 3 * kTrainRows * kW2S) +
+                           4 * (3 * kH);
+
+// One forward + backward over `rows` training rows: accumulates the loss
+// (sum of squared errors) and the gradient of mean((y - t/lam_scale)^2) into
+// G (flat layout, FP32, atomically across blocks).
+__global__ void __launch_bounds__(32 * kTrainWarps) k_mlp_grad(const float* __restrict__ P, Norm nm,
+                                                               const float* __restrict__ feat,
+                                                               const float* __restrict__ target, uint32_t rows,
+                                                               float inv_batch, float* __restrict__ G,
+                                                               float* __restrict__ loss) {
+  extern __shared__ __align__(16) unsigned char smem[];
+  uint16_t* sW1t = reinterpret_cast<uint16_t*>(smem);
+  uint16_t* sW2t = sW1t + kH * kW1S;
+  uint16_t* sW2 = sW2t + kH * kW2S;
+  uint16_t* sX = sW2 + kH * kW2S;         // [rows][kW1S] normalised inputs (bf16), k 8..15 zero
+  uint16_t* sH1 = sX + kTrainRows * kW1S;  // [rows][kW2S]
+  uint16_t* sDZ2 = sH1 + kTrainRows * kW2S;
+  uint16_t* sDZ1 = sDZ2 + kTrainRows * kW2S;
+  float* sB1 = reinterpret_cast<float*>(sDZ1 + kTrainRows * kW2S);
+  float* sB2 = sB1 + kH;
+  float* sW3 = sB2 + kH;
+  stage_weights(P, sW1t, sW2t, sW2);
+  for (int q = threadIdx.x; q < kH; q += blockDim.x) {
+    sB1[q] = P[OFF_B1 + q];
+    sB2[q] = P[OFF_B2 + q];
+    sW3[q] = P[OFF_W3 + q];
+  }
+  for (int q = threadIdx.x; q < kTrainRows * kW1S; q += blockDim.x) sX[q] = 0;
+  __syncthreads();
+  const float b3 = P[OFF_B3];
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, g = lane >> 2, t = lane & 3;
+
+  // gradient accumulators kept in registers across the block's chunks
+  float gW2[8][4];  // output tiles (mt, nt) with (mt*8+nt) % 4 == warp
+  float gW1[2][4];  // dW1 n-tiles 2*warp, 2*warp+1
+  float gB1[8][2], gB2[8][2], gW3[8][2], gB3 = 0.0f, lsum = 0.0f;
+#pragma unroll
+  for (int i = 0; i < 8; ++i)
+#pragma unroll
+    for (int q = 0; q < 4; ++q) gW2[i][q] = 0.0f;
+#pragma unroll
+  for (int i = 0; i < 2; ++i)
+#pragma unroll
+    for (int q = 0; q < 4; ++q) gW1[i][q] = 0.0f;
+#pragma unroll
+  for (int j = 0; j < 8; ++j) gB1[j][0] = gB1[j][1] = gB2[j][0] = gB2[j][1] = gW3[j][0] = gW3[j][1] = 0.0f;
+
+  for (uint32_t chunk = blockIdx.x; chunk * kTrainRows < rows; chunk += gridDim.x) {
+    const uint32_t r0 = chunk * kTrainRows + 16 * warp;
+    float xg[2], x8[2];
+    load_inputs(feat, nm, rows, r0, xg, x8);
+    Fwd F;
+    forward_tile(xg, x8, sW1t, sW2t, sB1, sB2, sW3, b3, F);
+    const uint32_t ra = r0 + g, rb = r0 + g + 8;
+    float tg = (ra < rows) ? target[ra] / nm.lam_scale : 0.0f;
+    float t8 = (rb < rows) ? target[rb] / nm.lam_scale : 0.0f;
+    float eg = (ra < rows) ? F.y0 - tg : 0.0f;
+    float e8 = (rb < rows) ? F.y8 - t8 : 0.0f;
+    if (t == 0) lsum += eg * eg + e8 * e8;
+    float dyg = 2.0f * eg * inv_batch, dy8 = 2.0f * e8 * inv_batch;
+    if (t == 0) gB3 += dyg + dy8;
+    // dZ2 = dy w3^T * silu'(z2); dw3 += h2^T dy; db2 += sum dZ2
+    float dz2[8][4];
+#pragma unroll
+    for (int j = 0; j < 8; ++j) {
+      float w0 = sW3[8 * j + 2 * t], w1 = sW3[8 * j + 2 * t + 1];
+      dz2[j][0] = dyg * w0 * dsilu_f(F.z2[j][0]);
+      dz2[j][1] = dyg * w1 * dsilu_f(F.z2[j][1]);
+      dz2[j][2] = dy8 * w0 * dsilu_f(F.z2[j][2]);
+      dz2[j][3] = dy8 * w1 * dsilu_f(F.z2[j][3]);
+      gW3[j][0] += F.h2[j][0] * dyg + F.h2[j][2] * dy8;
+      gW3[j][1] += F.h2[j][1] * dyg + F.h2[j][3] * dy8;
+      gB2[j][0] += dz2[j][0] + dz2[j][2];
+      gB2[j][1] += dz2[j][1] + dz2[j][3];
+    }
+    // dH1 = dZ2 W2^T (mma; A = dZ2 from the D layout, B from W2 rows)
+    uint32_t ad[4][4];
+#pragma unroll
+    for (int s = 0; s < 4; ++s) {
+      ad[s][0] = pack_bf16(dz2[2 * s][0], dz2[2 * s][1]);
+      ad[s][1] = pack_bf16(dz2[2 * s][2], dz2[2 * s][3]);
+      ad[s][2] = pack_bf16(dz2[2 * s + 1][0], dz2[2 * s + 1][1]);
+      ad[s][3] = pack_bf16(dz2[2 * s + 1][2], dz2[2 * s + 1][3]);
+    }
+    float dz1[8][4];
+#pragma unroll
+    for (int j = 0; j < 8; ++j) {
+      int n = 8 * j + g;
+      float d[4] = {0.f, 0.f, 0.f, 0.f};
+#pragma unroll
+      for (int s = 0; s < 4; ++s) {
+        uint32_t b0 = *reinterpret_cast<const uint32_t*>(sW2 + n * kW2S + 16 * s + 2 * t);
+        uint32_t b1 = *reinterpret_cast<const uint32_t*>(sW2 + n * kW2S + 16 * s + 8 + 2 * t);
+        mma16816(d, ad[s], b0, b1);
+      }
+#pragma unroll
+      for (int q = 0; q < 4; ++q) dz1[j][q] = d[q] * dsilu_f(F.z1[j][q]);
+      gB1[j][0] += dz1[j][0] + dz1[j][2];
+      gB1[j][1] += dz1[j][1] + dz1[j][3];
+    }
+    // stage X, H1, dZ2, dZ1 of this warp's 16 rows for the weight-gradient products
+    __syncthreads();  // previous chunk's readers are done
+    {
+      const int rl = 16 * warp + g;
+      uint16_t* xr = sX + rl * kW1S;
+      *reinterpret_cast<uint32_t*>(xr + 2 * t) = pack_bf16(xg[0], xg[1]);
+      *reinterpret_cast<uint32_t*>(xr + 8 * kW1S + 2 * t) = pack_bf16(x8[0], x8[1]);
+#pragma unroll
+      for (int s = 0; s < 4; ++s) {
+        *reinterpret_cast<uint32_t*>(sH1 + rl * kW2S + 16 * s + 2 * t) = F.a2[s][0];
+        *reinterpret_cast<uint32_t*>(sH1 + (rl + 8) * kW2S + 16 * s + 2 * t) = F.a2[s][1];
+        *reinterpret_cast<uint32_t*>(sH1 + rl * kW2S + 16 * s + 8 + 2 * t) = F.a2[s][2];
+        *reinterpret_cast<uint32_t*>(sH1 + (rl + 8) * kW2S + 16 * s + 8 + 2 * t) = F.a2[s][3];
+        *reinterpret_cast<uint32_t*>(sDZ2 + rl * kW2S + 16 * s + 2 * t) = ad[s][0];
+        *reinterpret_cast<uint32_t*>(sDZ2 + (rl + 8) * kW2S + 16 * s + 2 * t) = ad[s][1];
+        *reinterpret_cast<uint32_t*>(sDZ2 + rl * kW2S + 16 * s + 8 + 2 * t) = ad[s][2];
+        *reinterpret_cast<uint32_t*>(sDZ2 + (rl + 8) * kW2S + 16 * s + 8 + 2 * t) = ad[s][3];
+      }
+#pragma unroll
+      for (int j = 0; j < 8; ++j) {
+        *reinterpret_cast<uint32_t*>(sDZ1 + rl * kW2S + 8 * j + 2 * t) = pack_bf16(dz1[j][0], dz1[j][1]);
+        *reinterpret_cast<uint32_t*>(sDZ1 + (rl + 8) * kW2S + 8 * j + 2 * t) = pack_bf16(dz1[j][2], dz1[j][3]);
+      }
+    }
+    __syncthreads();
+    // dW2 = H1^T dZ2 over the chunk's 64 rows: M = hidden1, N = hidden2, K = rows
+#pragma unroll
+    for (int i = 0; i < 8; ++i) {
+      const int tile = warp + 4 * i, mt = tile >> 3, nt = tile & 7;
+#pragma unroll
+      for (int kk = 0; kk < kTrainRows / 16; ++kk) {
+        const int rk = 16 * kk + 2 * t, m0 = 16 * mt + g, nn = 8 * nt + g;
+        uint32_t a[4];
+        a[0] = pack_raw(sH1[rk * kW2S + m0], sH1[(rk + 1) * kW2S + m0]);
+        a[1] = pack_raw(sH1[rk * kW2S + m0 + 8], sH1[(rk + 1) * kW2S + m0 + 8]);
+        a[2] = pack_raw(sH1[(rk + 8) * kW2S + m0], sH1[(rk + 9) * kW2S + m0]);
+        a[3] = pack_raw(sH1[(rk + 8) * kW2S + m0 + 8], sH1[(rk + 9) * kW2S + m0 + 8]);
+        uint32_t b0 = pack_raw(sDZ2[rk * kW2S + nn], sDZ2[(rk + 1) * kW2S + nn]);
+        uint32_t b1 = pack_raw(sDZ2[(rk + 8) * kW2S + nn], sDZ2[(rk + 9) * kW2S + nn]);
+        mma16816(gW2[i], a, b0, b1);
+      }
+    }
+    // dW1 = X^T dZ1: M = inputs (16, rows 8..15 padding), N = hidden1, K = rows
+#pragma unroll
+    for (int i = 0; i < 2; ++i) {
+      const int nt = 2 * warp + i;
+#pragma unroll
+      for (int kk = 0; kk < kTrainRows / 16; ++kk) {
+        const int rk = 16 * kk + 2 * t, nn = 8 * nt + g;
+        uint32_t a[4];
+        a[0] = pack_raw(sX[rk * kW1S + g], sX[(rk + 1) * kW1S + g]);
+        a[1] = pack_raw(sX[rk * kW1S + g + 8], sX[(rk + 1) * kW1S + g + 8]);
+        a[2] = pack_raw(sX[(rk + 8) * kW1S + g], sX[(rk + 9) * kW1S + g]);
+        a[3] = pack_raw(sX[(rk + 8) * kW1S + g + 8], sX[(rk + 9) * kW1S + g + 8]);
+        uint32_t b0 = pack_raw(sDZ1[rk * kW2S + nn], sDZ1[(rk + 1) * kW2S + nn]);
+        uint32_t b1 = pack_raw(sDZ1[(rk + 8) * kW2S + nn], sDZ1[(rk + 9) * kW2S + nn]);
+        mma16816(gW1[i], a, b0, b1);
+      }
+    }
+  }
+  // flush: weight-gradient tiles (one owner per element), then the
+  // per-column sums reduced over the 8 row groups of the warp
+#pragma unroll
+  for (int i = 0; i < 8; ++i) {
+    const int tile = warp + 4 * i, mt = tile >> 3, nt = tile & 7;
+    const int m0 = 16 * mt + g, n0 = 8 * nt + 2 * t;
+    atomicAdd(G + OFF_W2 + m0 * kH + n0, gW2[i][0]);
+    atomicAdd(G + OFF_W2 + m0 * kH + n0 + 1, gW2[i][1]);
+    atomicAdd(G + OFF_W2 + (m0 + 8) * kH + n0, gW2[i][2]);
+    atomicAdd(G + OFF_W2 + (m0 + 8) * kH + n0 + 1, gW2[i][3]);
+  }
+#pragma unroll
+  for (int i = 0; i < 2; ++i) {
+    const int n0 = 8 * (2 * warp + i) + 2 * t;
+    if (g < kIn) {
+      atomicAdd(G + OFF_W1 + g * kH + n0, gW1[i][0]);
+      atomicAdd(G + OFF_W1 + g * kH + n0 + 1, gW1[i][1]);
+    }
+  }
+#pragma unroll
+  for (int j = 0; j < 8; ++j)
+#pragma unroll
+    for (int c = 0; c < 2; ++c) {
+      float v1 = gB1[j][c], v2 = gB2[j][c], v3 = gW3[j][c];
+#pragma unroll
+      for (int o = 4; o < 32; o <<= 1) {
+        v1 += __shfl_xor_sync(0xffffffffu, v1, o);
+        v2 += __shfl_xor_sync(0xffffffffu, v2, o);
+        v3 += __shfl_xor_sync(0xffffffffu, v3, o);
+      }
+      if (g == 0) {
+        atomicAdd(G + OFF_B1 + 8 * j + 2 * t + c, v1);
+        atomicAdd(G + OFF_B2 + 8 * j + 2 * t + c, v2);
+        atomicAdd(G + OFF_W3 + 8 * j + 2 * t + c, v3);
+      }
+    }
+#pragma unroll
+  for (int o = 1; o < 32; o <<= 1) {
+    gB3 += __shfl_xor_sync(0xffffffffu, gB3, o);
+    lsum += __shfl_xor_sync(0xffffffffu, lsum, o);
+  }
+  if (lane == 0) {
+    atomicAdd(G + OFF_B3, gB3);
+    atomicAdd(loss, lsum);
+  }
+}
+
+// Adam (Kingma & Ba 2015) on the flat FP32 parameters.
+__global__ void k_adam(float* __restrict__ P, const float* __restrict__ G, float* __restrict__ M, float* __restrict__ V,
+                       int n, float lr, float b1, float b2, float eps, float c1, float c2) {
+  int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  float gr = G[i];
+  float m = b1 * M[i] + (1.0f - b1) * gr;
+  float v = b2 * V[i] + (1.0f - b2) * gr * gr;
+  M[i] = m;
+  V[i] = v;
+  P[i] -= lr * (m / c1) / (sqrtf(v / c2) + eps);
+}
+
+Norm norm_of(const pbf_mlp& m) {
+  Norm n;
+  for (int k = 0; k < kIn; ++k) {
+    n.mean[k] = m.feat_mean[k];
+    n.inv_std[k] = m.feat_inv_std[k];
+  }
+  n.lam_scale = m.lam_scale;
+  return n;
+}
+
+bool grad_kernel_ready = false;
+cudaError_t ensure_grad_kernel() {
+  if (grad_kernel_ready) return cudaSuccess;
+  cudaError_t e = cudaFuncSetAttribute(k_mlp_grad, cudaFuncAttributeMaxDynamicSharedMemorySize, kTrainSmem);
+  if (e == cudaSuccess) grad_kernel_ready = true;
+  return e;
+}
+
+}  // namespace
+
+__global__ void k_gather_f32(uint32_t n, const uint32_t* __restrict__ perm, const float* __restrict__ src,
+                             float* __restrict__ dst) {
+  uint32_t t = blockIdx.x * blockDim.x + threadIdx.x;
+  if (t < n) dst[t] = src[perm[t]];
+}
+
+__global__ void k_copy_guarded(uint32_t n, const int* __restrict__ guard, const float4* __restrict__ src,
+                               float4* __restrict__ dst) {
+  if (guard && *guard == 0) return;
+  uint32_t t = blockIdx.x * blockDim.x + threadIdx.x;
+  if (t < n) dst[t] = src[t];
+}
+
+// Fallback decision from the last learned iteration's statistics; resets
+// them for the next substep.
+__global__ void k_fallback_decide(SolveStats* stats, float bound, int* flag, uint32_t* fallbacks, float* last_mean) {
+  unsigned cnt = stats->count;
+  double mean = cnt ? (double)stats->sum_fx / 1048576.0 / (double)cnt : 0.0;
+  int f = mean > (double)bound ? 1 : 0;
+  *flag = f;
+  if (f) atomicAdd(fallbacks, 1u);
+  *last_mean = (float)mean;
+  stats->max_bits = 0u;
+  stats->count = 0u;
+  stats->sum_fx = 0ull;
+}
+
+__device__ __forceinline__ uint32_t mix_id(uint32_t x) {
+  x ^= x >> 16;
+  x *= 0x7feb352dU;
+  x ^= x >> 15;
+  x *= 0x846ca68bU;
+  x ^= x >> 16;
+  return x;
+}
+
+__global__ void k_trace_append(uint32_t n, const uint32_t* __restrict__ ids, const float4* __restrict__ feat,
+                               const float* __restrict__ lam_sum, uint32_t stride, uint32_t salt,
+                               float* __restrict__ tf, float* __restrict__ tt, uint32_t* count, uint32_t cap) {
+  uint32_t t = blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= n) return;
+  if (mix_id(ids[t] ^ salt) % stride != 0) return;
+  uint32_t r = atomicAdd(count, 1u);
+  if (r >= cap) return;
+  float4 a = feat[2 * t], b = feat[2 * t + 1];
+  float* o = tf + 8 * (size_t)r;
+  o[0] = a.x; o[1] = a.y; o[2] = a.z; o[3] = a.w;
+  o[4] = b.x; o[5] = b.y; o[6] = b.z; o[7] = b.w;
+  tt[r] = lam_sum[t];
+}
+
+// ---- launch helpers used by the step driver -------------------------------------------
+cudaError_t launch_gather_f32(uint32_t n, const uint32_t* perm, const float* src, float* dst, cudaStream_t st) {
+  if (n == 0) return cudaSuccess;
+  k_gather_f32<<<(n + 255) / 256, 256, 0, st>>>(n, perm, src, dst);
+  return cudaGetLastError();
+}
+cudaError_t launch_copy_guarded(uint32_t n, const int* guard, const float4* src, float4* dst, cudaStream_t st) {
+  if (n == 0) return cudaSuccess;
+  k_copy_guarded<<<(n + 255) / 256, 256, 0, st>>>(n, guard, src, dst);
+  return cudaGetLastError();
+}
+cudaError_t launch_fallback_decide(SolveStats* stats, float bound, int* flag, uint32_t* fallbacks, float* last_mean,
+                                   cudaStream_t st) {
+  k_fallback_decide<<<1, 1, 0, st>>>(stats, bound, flag, fallbacks, last_mean);
+  return cudaGetLastError();
+}
+cudaError_t launch_trace_append(uint32_t n, const uint32_t* ids, const float4* feat, const float* lam_sum,
+                                uint32_t stride, uint32_t salt, float* tf, float* tt, uint32_t* count, uint32_t cap,
+                                cudaStream_t st) {
+  if (n == 0) return cudaSuccess;
+  k_trace_append<<<(n + 255) / 256, 256, 0, st>>>(n, ids, feat, lam_sum, stride, salt, tf, tt, count, cap);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_mlp_infer(const float* d_params, const pbf_mlp& model, const float* d_feat, uint32_t rows,
+                             float* d_lambda, float* d_lam_sum, cudaStream_t st) {
+  if (rows == 0) return cudaSuccess;
+  uint32_t tiles = (rows + 15) / 16;
+  uint32_t blocks = (tiles + 3) / 4;
+  if (blocks > 152u * 8u) blocks = 152u * 8u;
+  k_mlp_infer<<<blocks, kInferThreads, 0, st>>>(d_params, norm_of(model), d_feat, rows, d_lambda, d_lam_sum);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_mlp_grad(const float* d_params, const pbf_mlp& model, const float* d_feat, const float* d_target,
+                            uint32_t rows, float* d_grad, float* d_loss, cudaStream_t st) {
+  if (rows == 0) return cudaSuccess;
+  cudaError_t e = ensure_grad_kernel();
+  if (e != cudaSuccess) return e;
+  uint32_t chunks = (rows + kTrainRows - 1) / kTrainRows;
+  uint32_t blocks = chunks < 152u * 4u ? chunks : 152u * 4u;
+  k_mlp_grad<<<blocks, 32 * kTrainWarps, kTrainSmem, st>>>(d_params, norm_of(model), d_feat, d_target, rows,
+                                                           1.0f / (float)rows, d_grad, d_loss);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_adam(float* P, const float* G, float* M, float* V, int step, float lr, cudaStream_t st) {
+  const float b1 = 0.9f, b2 = 0.999f;
+  float c1 = 1.0f - std::pow(b1, (float)step), c2 = 1.0f - std::pow(b2, (float)step);
+  k_adam<<<(PBF_MLP_PARAMS + 255) / 256, 256, 0, st>>>(P, G, M, V, PBF_MLP_PARAMS, lr, b1, b2, 1e-8f, c1, c2);
+  return cudaGetLastError();
+}
+
+}  // namespace pbf
+
+using namespace pbf;
+
+namespace {
+uint64_t splitmix(uint64_t& s) {
+  s += 0x9e3779b97f4a7c15ull;
+  uint64_t z = s;
+  z = (z ^ (z >> 30)) * 0xbf58476d1ce4e5b9ull;
+  z = (z ^ (z >> 27)) * 0x94d049bb133111ebull;
+  return z ^ (z >> 31);
+}
+double unif(uint64_t& s) { return (double)(splitmix(s) >> 11) * (1.0 / 9007199254740992.0); }
+}  // namespace
+
+extern "C" {
+
+int pbf_mlp_init(pbf_mlp* m, uint64_t seed) {
+  if (!m) return PBF_EINVAL;
+  std::memset(m, 0, sizeof(*m));
+  uint64_t s = seed;
+  // Glorot-uniform weights, zero biases, identity normalisation
+  double l1 = std::sqrt(6.0 / (kIn + kH)), l2 = std::sqrt(6.0 / (kH + kH)), l3 = std::sqrt(6.0 / (kH + 1));
+  for (int i = 0; i < kIn * kH; ++i) m->params[OFF_W1 + i] = (float)((2.0 * unif(s) - 1.0) * l1);
+  for (int i = 0; i < kH * kH; ++i) m->params[OFF_W2 + i] = (float)((2.0 * unif(s) - 1.0) * l2);
+  for (int i = 0; i < kH; ++i) m->params[OFF_W3 + i] = (float)((2.0 * unif(s) - 1.0) * l3);
+  for (int k = 0; k < kIn; ++k) m->feat_inv_std[k] = 1.0f;
+  m->lam_scale = 1.0f;
+  return PBF_OK;
+}
+
+int pbf_mlp_fit_normalization(pbf_mlp* m, const float* feat, const float* target, uint32_t rows) {
+  if (!m || !feat || !target || rows == 0) return PBF_EINVAL;
+  double mean[kIn] = {0}, sq[kIn] = {0}, tsq = 0;
+  for (uint32_t r = 0; r < rows; ++r) {
+    for (int k = 0; k < kIn; ++k) {
+      double v = feat[8 * (size_t)r + k];
+      mean[k] += v;
+      sq[k] += v * v;
+    }
+    tsq += (double)target[r] * target[r];
+  }
+  for (int k = 0; k < kIn; ++k) {
+    double mu = mean[k] / rows, var = sq[k] / rows - mu * mu;
+    m->feat_mean[k] = (float)mu;
+    m->feat_inv_std[k] = (float)(var > 1e-20 ? 1.0 / std::sqrt(var) : 1.0);
+  }
+  double rms = std::sqrt(tsq / rows);
+  m->lam_scale = (float)(rms > 0 ? rms : 1.0);
+  return PBF_OK;
+}
+
+int pbf_mlp_forward(const pbf_mlp* m, const float* feat, uint32_t rows, float* out) {
+  if (!m || (!feat && rows) || (!out && rows)) return PBF_EINVAL;
+  if (rows == 0) return PBF_OK;
+  float *dP = nullptr, *dF = nullptr, *dO = nullptr;
+  cudaError_t e = cudaMalloc(&dP, sizeof(m->params));
+  if (e == cudaSuccess) e = cudaMalloc(&dF, (size_t)rows * 8 * sizeof(float));
+  if (e == cudaSuccess) e = cudaMalloc(&dO, (size_t)rows * sizeof(float));
+  if (e == cudaSuccess) e = cudaMemcpy(dP, m->params, sizeof(m->params), cudaMemcpyHostToDevice);
+  if (e == cudaSuccess) e = cudaMemcpy(dF, feat, (size_t)rows * 8 * sizeof(float), cudaMemcpyHostToDevice);
+  if (e == cudaSuccess) e = launch_mlp_infer(dP, *m, dF, rows, dO, nullptr, 0);
+  if (e == cudaSuccess) e = cudaMemcpy(out, dO, (size_t)rows * sizeof(float), cudaMemcpyDeviceToHost);
+  cudaFree(dP);
+  cudaFree(dF);
+  cudaFree(dO);
+  return e == cudaSuccess ? PBF_OK : PBF_ECUDA;
+}
+
+int pbf_mlp_gradient(const pbf_mlp* m, const float* feat, const float* target, uint32_t rows, float* grad,
+                     float* loss) {
+  if (!m || !feat || !target || !grad || rows == 0) return PBF_EINVAL;
+  float *dP = nullptr, *dF = nullptr, *dT = nullptr, *dG = nullptr;
+  cudaError_t e = cudaMalloc(&dP, sizeof(m->params));
+  if (e == cudaSuccess) e = cudaMalloc(&dF, (size_t)rows * 8 * sizeof(float));
+  if (e == cudaSuccess) e = cudaMalloc(&dT, (size_t)rows * sizeof(float));
+  if (e == cudaSuccess) e = cudaMalloc(&dG, (PBF_MLP_PARAMS + 1) * sizeof(float));
+  if (e == cudaSuccess) e = cudaMemcpy(dP, m->params, sizeof(m->params), cudaMemcpyHostToDevice);
+  if (e == cudaSuccess) e = cudaMemcpy(dF, feat, (size_t)rows * 8 * sizeof(float), cudaMemcpyHostToDevice);
+  if (e == cudaSuccess) e = cudaMemcpy(dT, target, (size_t)rows * sizeof(float), cudaMemcpyHostToDevice);
+  if (e == cudaSuccess) e = cudaMemset(dG, 0, (PBF_MLP_PARAMS + 1) * sizeof(float));
+  if (e == cudaSuccess) e = launch_mlp_grad(dP, *m, dF, dT, rows, dG, dG + PBF_MLP_PARAMS, 0);
+  float l = 0.0f;
+  if (e == cudaSuccess) e = cudaMemcpy(grad, dG, PBF_MLP_PARAMS * sizeof(float), cudaMemcpyDeviceToHost);
+  if (e == cudaSuccess) e = cudaMemcpy(&l, dG + PBF_MLP_PARAMS, sizeof(float), cudaMemcpyDeviceToHost);
+  if (loss) *loss = l / (float)rows;
+  cudaFree(dP);
+  cudaFree(dF);
+  cudaFree(dT);
+  cudaFree(dG);
+  return e == cudaSuccess ? PBF_OK : PBF_ECUDA;
+}
+
+// Mini-batch Adam on rows (feat, target) held on the host; shuffled once by
+// a seeded permutation.  Returns the mean loss of the last epoch.
+int pbf_mlp_train(pbf_mlp* m, const float* feat, const float* target, uint32_t rows, const pbf_train_config* tc,
+                  float* final_loss) {
+  if (!m || !feat || !target || !tc || rows == 0 || tc->batch == 0) return PBF_EINVAL;
+  std::vector<uint32_t> perm(rows);
+  for (uint32_t i = 0; i < rows; ++i) perm[i] = i;
+  uint64_t s = tc->seed ^ 0x5eedull;
+  for (uint32_t i = rows - 1; i > 0; --i) {
+    uint32_t j = (uint32_t)(splitmix(s) % (uint64_t)(i + 1));
+    std::swap(perm[i], perm[j]);
+  }
+  std::vector<float> f((size_t)rows * 8), tg(rows);
+  for (uint32_t i = 0; i < rows; ++i) {
+    std::memcpy(&f[8 * (size_t)i], feat + 8 * (size_t)perm[i], 8 * sizeof(float));
+    tg[i] = target[perm[i]];
+  }
+  float *dP = nullptr, *dF = nullptr, *dT = nullptr, *dG = nullptr, *dM = nullptr, *dV = nullptr;
+  cudaError_t e = cudaMalloc(&dP, sizeof(m->params));
+  if (e == cudaSuccess) e = cudaMalloc(&dF, f.size() * sizeof(float));
+  if (e == cudaSuccess) e = cudaMalloc(&dT, tg.size() * sizeof(float));
+  if (e == cudaSuccess) e = cudaMalloc(&dG, (PBF_MLP_PARAMS + 1) * sizeof(float));
+  if (e == cudaSuccess) e = cudaMalloc(&dM, PBF_MLP_PARAMS * sizeof(float));
+  if (e == cudaSuccess) e = cudaMalloc(&dV, PBF_MLP_PARAMS * sizeof(float));
+  if (e == cudaSuccess) e = cudaMemcpy(dP, m->params, sizeof(m->params), cudaMemcpyHostToDevice);
+  if (e == cudaSuccess) e = cudaMemcpy(dF, f.data(), f.size() * sizeof(float), cudaMemcpyHostToDevice);
+  if (e == cudaSuccess) e = cudaMemcpy(dT, tg.data(), tg.size() * sizeof(float), cudaMemcpyHostToDevice);
+  if (e == cudaSuccess) e = cudaMemset(dM, 0, PBF_MLP_PARAMS * sizeof(float));
+  if (e == cudaSuccess) e = cudaMemset(dV, 0, PBF_MLP_PARAMS * sizeof(float));
+  const uint32_t batch = tc->batch < rows ? tc->batch : rows;
+  const uint32_t per_epoch = rows / batch;
+  double epoch_loss = 0.0;
+  int step = 0;
+  std::vector<float> lossbuf;
+  for (uint32_t ep = 0; ep < tc->epochs && e == cudaSuccess; ++ep) {
+    float* dLoss = dG + PBF_MLP_PARAMS;
+    double acc = 0.0;
+    for (uint32_t b = 0; b < per_epoch && e == cudaSuccess; ++b) {
+      e = cudaMemsetAsync(dG, 0, (PBF_MLP_PARAMS + 1) * sizeof(float), 0);
+      if (e == cudaSuccess)
+        e = launch_mlp_grad(dP, *m, dF + 8 * (size_t)b * batch, dT + (size_t)b * batch, batch, dG, dLoss, 0);
+      ++step;
+      float lr = tc->learning_rate;
+      if (tc->epochs > 1) lr *= (float)(0.5 * (1.0 + std::cos(3.14159265358979 * ep / tc->epochs)));
+      if (e == cudaSuccess) e = launch_adam(dP, dG, dM, dV, step, lr, 0);
+      if (e == cudaSuccess && b + 1 == per_epoch) {
+        float l = 0.0f;
+        e = cudaMemcpy(&l, dLoss, sizeof(float), cudaMemcpyDeviceToHost);
+        acc = l / batch;
+      }
+    }
+    epoch_loss = acc;
+  }
+  if (e == cudaSuccess) e = cudaMemcpy(m->params, dP, sizeof(m->params), cudaMemcpyDeviceToHost);
+  cudaFree(dP);
+  cudaFree(dF);
+  cudaFree(dT);
+  cudaFree(dG);
+  cudaFree(dM);
+  cudaFree(dV);
+  if (final_loss) *final_loss = (float)epoch_loss;
+  return e == cudaSuccess ? PBF_OK : PBF_ECUDA;
+}
+
+}  // extern "C"

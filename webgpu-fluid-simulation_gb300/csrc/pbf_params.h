@@ -39,4 +39,25 @@ struct SimParams {
   uint32_t n;
 };
 
+// Compression statistics of a solver iteration (learned-start fallback test).
+struct SolveStats {
+  unsigned int max_bits;     // max_i max(0, rho_i - 1) as float bits (non-negative)
+  unsigned int count;        // particles accumulated
+  unsigned long long sum_fx; // sum_i min(max(0, rho_i - 1), 1) in 2^-20 fixed point
+};
+
+// Optional inputs/outputs of the constraint passes used by the learned
+// start and by trace capture.  All null/zero in the plain solve.
+struct SolverAux {
+  const int* guard;          // non-null: the kernel returns unless *guard != 0 (fallback path)
+  float* bsdf;               // boundary pass: SDF at x* (features)
+  float* lam_sum;            // lambda pass: multiplier accumulated over this substep
+  int lam_first;             // lambda pass: 1 = this iteration starts lam_sum
+  float4* feat;              // lambda pass: 8 raw features per particle (2 x float4)
+  const float4* pos;         // lambda pass (features): x before the predict step
+  const float* lam_prev;     // lambda pass (features): previous substep's multiplier
+  SolveStats* stats;         // lambda pass: compression statistics
+  float substep_index;       // lambda pass (features)
+};
+
 }  // namespace pbf

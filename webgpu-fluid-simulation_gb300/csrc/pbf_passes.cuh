@@ -226,39 +226,62 @@ __device__ __forceinline__ void list_slice(const uint32_t* __restrict__ warp_off
 // the 64-node interpolation where the field cell cannot produce a sample.
 __global__ void __launch_bounds__(256) k_boundary(SimParams p, FieldParams f, const float* __restrict__ sdf,
                                                   const float* __restrict__ vol, const uint8_t* __restrict__ bflag,
-                                                  const float4* __restrict__ xs, float4* __restrict__ bdata) {
+                                                  const float4* __restrict__ xs, float4* __restrict__ bdata,
+                                                  SolverAux a) {
+  if (a.guard && *a.guard == 0) return;
   uint32_t t = blockIdx.x * blockDim.x + threadIdx.x;
   if (t >= p.n) return;
   f3 xi = xyz(xs[t]);
   float4 bd = make_float4(0.f, 0.f, 0.f, 0.f);
-  if (boundary_possible(f, bflag, xi)) bd = boundary_sample(p, f, sdf, vol, xi);
+  float dist = 2.0f * p.h;  // "far" for the feature when the cell cannot contribute
+  if (boundary_possible(f, bflag, xi)) {
+    if (a.bsdf) {
+      dist = boundary_distance(f, sdf, xi);
+    }
+    bd = boundary_sample(p, f, sdf, vol, xi);
+  }
   bdata[t] = bd;
+  if (a.bsdf) a.bsdf[t] = dist;
 }
 
-// LambdaCalculation (pressureConstrain.ts:31-85).
+// LambdaCalculation (pressureConstrain.ts:31-85).  kFeat additionally
+// computes the learned start's features at x*_0 (density error, previous
+// multiplier, neighbour count, |v'|, div v', boundary SDF and volume,
+// substep index; v' = (x* - x)/dt).
+template <bool kFeat>
 __global__ void __launch_bounds__(256) k_lambda(SimParams p, int have_field, const float4* __restrict__ bdata,
-                                                const float4* __restrict__ xs, const uint32_t* __restrict__ warp_off, const uint32_t* __restrict__ nbr_cnt,
+                                                const float4* __restrict__ xs, const uint32_t* __restrict__ warp_off,
+                                                const uint32_t* __restrict__ nbr_cnt,
                                                 const uint32_t* __restrict__ nbr_list, uint32_t cap,
-                                                float* __restrict__ lambda) {
+                                                float* __restrict__ lambda, SolverAux a) {
+  if (a.guard && *a.guard == 0) return;
   uint32_t t = blockIdx.x * blockDim.x + threadIdx.x;
   if (t >= p.n) return;
   f3 xi = xyz(xs[t]);
   uint32_t b, e;
   list_slice(warp_off, nbr_cnt, t, cap, b, e);
   f3 grad = mk(0.f, 0.f, 0.f);
-  float sum2 = 0.0f, dens = 0.0f;
-  for_each_neighbor(nbr_list, b, e, xs, [&](uint32_t, float4 xj) {
+  float sum2 = 0.0f, dens = 0.0f, div = 0.0f;
+  f3 vi = mk(0.f, 0.f, 0.f);
+  if (kFeat) vi = p.inv_dt * (xi - xyz(a.pos[t]));
+  for_each_neighbor(nbr_list, b, e, xs, [&](uint32_t j, float4 xj) {
     Pair q = make_pair_of(xi - xyz(xj));
     f3 gk = spiky_p(p, q);
     grad = grad + gk;
     sum2 = sum2 + dot3(gk, gk);
     dens = dens + poly6_p(p, q);
+    if (kFeat) {
+      f3 vj = p.inv_dt * (xyz(xj) - xyz(__ldg(a.pos + j)));
+      div = div + dot3(vj - vi, gk);
+    }
   });
   dens = dens * p.V;
   grad = p.V * grad;
   sum2 = sum2 * p.V2;
+  float vb = 0.0f;
   if (have_field) {
     float4 bd = bdata[t];
+    vb = bd.w;
     if (bd.w != 0.0f) {
       Pair q = make_pair_of(xi - xyz(bd));
       f3 gk = bd.w * spiky_p(p, q);
@@ -268,15 +291,38 @@ __global__ void __launch_bounds__(256) k_lambda(SimParams p, int have_field, con
   }
   float c = fmaxf(0.0f, dens - 1.0f);
   float s = dot3(grad, grad) + sum2;
-  lambda[t] = fdiv(-c, s + p.lambda_eps);
+  float lam = fdiv(-c, s + p.lambda_eps);
+  lambda[t] = lam;
+  if (a.lam_sum) a.lam_sum[t] = a.lam_first ? lam : a.lam_sum[t] + lam;
+  if (kFeat) {
+    float sd = a.bsdf ? fminf(a.bsdf[t], 2.0f * p.h) : 2.0f * p.h;
+    a.feat[2 * t] = make_float4(dens - 1.0f, a.lam_prev ? a.lam_prev[t] : 0.0f, (float)e,
+                                len3(vi) * p.dt / p.h);
+    a.feat[2 * t + 1] = make_float4(p.V * div * p.dt, sd / p.h, vb / p.V, a.substep_index);
+  }
+  if (a.stats) {
+    // warp-aggregated compression statistics (lanes past n have returned)
+    const unsigned m = __activemask();
+    unsigned bits = __float_as_uint(c);
+    unsigned fx = (unsigned)(fminf(c, 1.0f) * 1048576.0f);
+    unsigned wmax = __reduce_max_sync(m, bits);
+    unsigned wsum = __reduce_add_sync(m, fx);
+    unsigned wcnt = __popc(m);
+    if ((threadIdx.x & 31u) == (unsigned)(__ffs(m) - 1)) {
+      atomicMax(&a.stats->max_bits, wmax);
+      atomicAdd(&a.stats->count, wcnt);
+      atomicAdd(&a.stats->sum_fx, (unsigned long long)wsum);
+    }
+  }
 }
 
 // ConstrainSolve + ConstrainApply: x*_new = clamp(x* + 0.5 * dp) into the other buffer.
-__global__ void __launch_bounds__(256) k_deltap(SimParams p, int have_field, const float4* __restrict__ xs,
+__global__ void __launch_bounds__(256) k_deltap(SimParams p, SolverAux a, int have_field, const float4* __restrict__ xs,
                                                 const float* __restrict__ lambda, const float4* __restrict__ bdata,
                                                 const uint32_t* __restrict__ warp_off, const uint32_t* __restrict__ nbr_cnt,
                                                 const uint32_t* __restrict__ nbr_list, uint32_t cap,
                                                 float4* __restrict__ xs_out, float4* __restrict__ dp_out) {
+  if (a.guard && *a.guard == 0) return;
   uint32_t t = blockIdx.x * blockDim.x + threadIdx.x;
   if (t >= p.n) return;
   f3 xi = xyz(xs[t]);
@@ -394,7 +440,8 @@ void fill_pass_table(PassTable* tbl) {
   tbl->nbr_list = k_nbr_list;
   tbl->nbr_list_sliced = k_nbr_list_sliced;
   tbl->boundary = k_boundary;
-  tbl->lambda = k_lambda;
+  tbl->lambda = k_lambda<false>;
+  tbl->lambda_feat = k_lambda<true>;
   tbl->deltap = k_deltap;
   tbl->density_velocity = k_density_velocity;
   tbl->vorticity = k_vorticity;

@@ -6,6 +6,7 @@ libpbf_gb300.so (CUDA, sm_103a).
 """
 from . import _lib
 from .simulator import PBF, NeighborSearch, exclusive_scan
+from .simulator import mlp_init, mlp_params, mlp_fit_normalization, mlp_forward, mlp_gradient, mlp_train
 from . import scenes
 
 __all__ = ["PBF", "NeighborSearch", "exclusive_scan", "scenes", "_lib"]

@@ -57,6 +57,19 @@ class KernelTime(ctypes.Structure):
     _fields_ = [("name", ctypes.c_char * 32), ("launches", u32), ("total_ms", f32)]
 
 
+MLP_PARAMS = 4801
+
+
+class MLP(ctypes.Structure):
+    _fields_ = [("params", f32 * MLP_PARAMS), ("feat_mean", f32 * 8), ("feat_inv_std", f32 * 8),
+                ("lam_scale", f32)]
+
+
+class TrainConfig(ctypes.Structure):
+    _fields_ = [("epochs", u32), ("batch", u32), ("learning_rate", f32), ("reserved", u32),
+                ("seed", ctypes.c_uint64)]
+
+
 class Grid(ctypes.Structure):
     _fields_ = [("origin", f32 * 3), ("inv_cell", f32 * 3), ("dim", u32 * 3)]
 
@@ -113,6 +126,15 @@ SIGNATURES = {
                                                _FP, _FP]),
     "pbf_volume_from_sdf": (ctypes.c_int, [_UP, _FP, _FP, ctypes.c_float, u32, u32, _FP, _FP]),
     "pbf_exclusive_scan_u32_noalloc": (ctypes.c_int, [_P, _P, ctypes.c_size_t, _P]),
+    "pbf_mlp_init": (ctypes.c_int, [ctypes.POINTER(MLP), ctypes.c_uint64]),
+    "pbf_mlp_fit_normalization": (ctypes.c_int, [ctypes.POINTER(MLP), _FP, _FP, u32]),
+    "pbf_mlp_forward": (ctypes.c_int, [ctypes.POINTER(MLP), _FP, u32, _FP]),
+    "pbf_mlp_gradient": (ctypes.c_int, [ctypes.POINTER(MLP), _FP, _FP, u32, _FP, _FP]),
+    "pbf_mlp_train": (ctypes.c_int, [ctypes.POINTER(MLP), _FP, _FP, u32, ctypes.POINTER(TrainConfig), _FP]),
+    "pbf_set_trace": (ctypes.c_int, [_P, u32, u32, ctypes.c_uint64]),
+    "pbf_trace_rows": (ctypes.c_int, [_P, _UP]),
+    "pbf_copy_trace": (ctypes.c_int, [_P, _FP, _FP, u32]),
+    "pbf_set_learned": (ctypes.c_int, [_P, ctypes.POINTER(MLP), u32, ctypes.c_float]),
 }
 
 _lib = None

@@ -183,6 +183,25 @@ class PBF:
         self._check(self._lib.pbf_get_kernel_timing(self._h, buf, 32, ctypes.byref(c)), "kernel_timing")
         return {buf[i].name.decode(): (int(buf[i].launches), float(buf[i].total_ms)) for i in range(c.value)}
 
+    # ---- learned start ------------------------------------------------------
+    def set_trace(self, capacity, stride=1, salt=0):
+        self._check(self._lib.pbf_set_trace(self._h, int(capacity), int(stride), int(salt)), "set_trace")
+
+    def trace(self):
+        """(features (rows, 8), targets (rows,)) captured so far."""
+        c = ctypes.c_uint32()
+        self._check(self._lib.pbf_trace_rows(self._h, ctypes.byref(c)), "trace_rows")
+        f = np.zeros((c.value, 8), np.float32)
+        t = np.zeros(c.value, np.float32)
+        fp = ctypes.POINTER(ctypes.c_float)
+        self._check(self._lib.pbf_copy_trace(self._h, f.ctypes.data_as(fp), t.ctypes.data_as(fp), c.value),
+                    "copy_trace")
+        return f, t
+
+    def set_learned(self, model, iterations=2, fallback_bound=0.01):
+        m = None if model is None else ctypes.byref(model)
+        self._check(self._lib.pbf_set_learned(self._h, m, int(iterations), float(fallback_bound)), "set_learned")
+
     def update(self):
         return None
 
@@ -304,3 +323,57 @@ def exclusive_scan(d_in, d_out, n, stream=0):
                                     ctypes.c_void_p(stream or None))
     if rc:
         raise L.PBFError(rc, "pbf_exclusive_scan_u32")
+
+
+# ---- MLP helpers (the learned start's network) ------------------------------------------
+def _fp(a):
+    return a.ctypes.data_as(ctypes.POINTER(ctypes.c_float))
+
+
+def mlp_init(seed=0):
+    m = L.MLP()
+    L.load().pbf_mlp_init(ctypes.byref(m), int(seed))
+    return m
+
+
+def mlp_params(m):
+    return np.ctypeslib.as_array(m.params).copy()
+
+
+def mlp_fit_normalization(m, feat, target):
+    f = np.ascontiguousarray(feat, np.float32)
+    t = np.ascontiguousarray(target, np.float32)
+    rc = L.load().pbf_mlp_fit_normalization(ctypes.byref(m), _fp(f), _fp(t), f.shape[0])
+    if rc:
+        raise L.PBFError(rc, "mlp_fit_normalization")
+
+
+def mlp_forward(m, feat):
+    f = np.ascontiguousarray(feat, np.float32)
+    out = np.zeros(f.shape[0], np.float32)
+    rc = L.load().pbf_mlp_forward(ctypes.byref(m), _fp(f), f.shape[0], _fp(out))
+    if rc:
+        raise L.PBFError(rc, "mlp_forward")
+    return out
+
+
+def mlp_gradient(m, feat, target):
+    f = np.ascontiguousarray(feat, np.float32)
+    t = np.ascontiguousarray(target, np.float32)
+    g = np.zeros(L.MLP_PARAMS, np.float32)
+    loss = ctypes.c_float()
+    rc = L.load().pbf_mlp_gradient(ctypes.byref(m), _fp(f), _fp(t), f.shape[0], _fp(g), ctypes.byref(loss))
+    if rc:
+        raise L.PBFError(rc, "mlp_gradient")
+    return g, loss.value
+
+
+def mlp_train(m, feat, target, epochs=20, batch=8192, lr=2e-3, seed=0):
+    f = np.ascontiguousarray(feat, np.float32)
+    t = np.ascontiguousarray(target, np.float32)
+    tc = L.TrainConfig(epochs=int(epochs), batch=int(batch), learning_rate=float(lr), reserved=0, seed=int(seed))
+    loss = ctypes.c_float()
+    rc = L.load().pbf_mlp_train(ctypes.byref(m), _fp(f), _fp(t), f.shape[0], ctypes.byref(tc), ctypes.byref(loss))
+    if rc:
+        raise L.PBFError(rc, "mlp_train")
+    return loss.value

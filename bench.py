@@ -84,8 +84,10 @@ def parse_args():
     ap.add_argument("--settle", type=int, default=150,
                     help="frames advanced from the initial lattice to build the input state (untimed set-up)")
     ap.add_argument("--no-learned", action="store_true", help="skip the learned warm-start measurement")
-    ap.add_argument("--bound", type=float, default=0.01,
-                    help="learned start: fall back to the plain solve when the mean compression exceeds this")
+    ap.add_argument("--bound", type=float, default=None,
+                    help="learned start: fall back to the plain solve when the in-solve mean compression exceeds "
+                         "this (default: the largest per-substep value the plain 4-iteration solve showed while "
+                         "the training traces were recorded)")
     return ap.parse_args()
 
 
@@ -323,13 +325,15 @@ def gpu_arm(args, dist):
     if not args.no_learned:
         from pbf_gb300 import mlp_init, mlp_fit_normalization, mlp_train
         feat, tgt = sim.trace()
+        plain_err_max, plain_err_avg = sim.trace_error()
         sim.set_trace(0)
         model = mlp_init(7)
         mlp_fit_normalization(model, feat, tgt)
         t0 = time.perf_counter()
         loss = mlp_train(model, feat, tgt, epochs=10, batch=8192, lr=3e-3, seed=7)
         train_info = {"rows": int(len(tgt)), "epochs": 10, "batch": 8192, "final_mse_normalised": loss,
-                      "seconds": time.perf_counter() - t0}
+                      "seconds": time.perf_counter() - t0, "traced_frames": args.settle - trace_from,
+                      "plain_mean_compression_while_tracing": {"max": plain_err_max, "avg": plain_err_avg}}
     snap = (sim.positions(), sim.velocities())
     for _ in range(max(args.warmup, 3)):
         sim.step(1)
@@ -411,7 +415,7 @@ def gpu_arm(args, dist):
     }
     sim.close()
     if model is not None:
-        line["learned"] = learned_arm(args, sc, snap, model, train_info, dist)
+        line["learned"] = learned_arm(args, sc, snap, model, train_info, dist, value)
     if dist.rank == 0 and dist.world == 1 and not args.no_cpu_baseline:
         v, secs, cnt, cores, done = cpu_sample(sc, sc.n, sub)
         line["cpu_baseline"] = {"value": v, "unit": UNIT, "cores": cores, "kind": "port",
@@ -434,15 +438,25 @@ def _handle_from(sc, snap, iterations=None):
     return sim
 
 
-def learned_arm(args, sc, snap, model, train_info, dist):
-    """Learned start (+2 iterations, plain-4 fallback above the bound) against
-    the plain 4-iteration solve, both from the same input state: throughput
-    over the timed region and mean compression per step afterwards."""
+def _errors_from(sc, snap, frames, model=None, iterations=None, learned_iters=2, bound=1e9):
+    """Per-step mean compression (the metrics' density error) from a snapshot."""
+    h = _handle_from(sc, snap, iterations=iterations)
+    if model is not None:
+        h.set_learned(model, iterations=learned_iters, fallback_bound=bound)
+    e = []
+    for _ in range(frames):
+        h.step(1)
+        e.append(h.metrics()["mean_compression"])
+    fb = h.metrics()["fallback_steps"]
+    h.close()
+    return np.array(e), fb
+
+
+def _timed_learned(args, sc, snap, model, learned_iters, bound, dist):
     import torch
     n, sub = sc.n, sc.config.substeps
-    out = {"training": train_info, "iterations": 2, "fallback_bound_mean_compression": args.bound}
     sim = _handle_from(sc, snap)
-    sim.set_learned(model, iterations=2, fallback_bound=args.bound)
+    sim.set_learned(model, iterations=learned_iters, fallback_bound=bound)
     for _ in range(max(args.warmup, 3)):
         sim.step(1)
     sim.synchronize()
@@ -460,25 +474,40 @@ def learned_arm(args, sc, snap, model, train_info, dist):
     ev1.synchronize()
     ms = dist.max(ev0.elapsed_time(ev1))
     kt = sim.kernel_timing()
-    sim.set_kernel_timing(False)
     fb = sim.metrics()["fallback_steps"] - fb0
-    out.update({"value": dist.world * n * sub * args.steps / (ms / 1000.0), "ms_per_step": ms / args.steps,
-                "fallback_substeps": int(fb), "timed_substeps": sub * args.steps,
-                "passes_ms": {k: round(v[1], 4) for k, v in kt.items()}})
     sim.close()
-    # density error from the same state, per step, outside any timed region
-    errs = {}
-    for name, mdl, iters in (("plain4", None, None), ("plain2", None, 2), ("learned2", model, None)):
-        h = _handle_from(sc, snap, iterations=iters)
-        if mdl is not None:
-            h.set_learned(mdl, iterations=2, fallback_bound=1e9)  # the network alone, no fallback
-        e = []
-        for _ in range(max(args.steps, 10)):
-            h.step(1)
-            e.append(h.metrics()["mean_compression"])
-        errs[name] = {"mean_compression": float(np.mean(e)), "max_step_mean_compression": float(np.max(e))}
-        h.close()
-    out["density_error_same_state"] = errs
+    return {"value": dist.world * n * sub * args.steps / (ms / 1000.0), "ms_per_step": ms / args.steps,
+            "fallback_substeps": int(fb), "timed_substeps": sub * args.steps,
+            "passes_ms": {k: round(v[1], 4) for k, v in kt.items()}}
+
+
+def learned_arm(args, sc, snap, model, train_info, dist, plain_value):
+    """Learned start against the plain 4-iteration solve at equal max density
+    error: from the same input state, the plain solve's largest per-step mean
+    compression over the window is the learned start's fallback bound; the
+    learned start then runs the same window (timed), falling back to the
+    plain solve on the device in any substep that exceeds it."""
+    frames = max(args.warmup, 3) + args.steps
+    e_plain, _ = _errors_from(sc, snap, frames)
+    e_plain2, _ = _errors_from(sc, snap, frames, iterations=2)
+    window = slice(max(args.warmup, 3), frames)
+    bound = float(e_plain[window].max()) if args.bound is None else float(args.bound)
+    out = {"training": train_info, "iterations": 2, "fallback": "plain 4-iteration solve",
+           "bound_mean_compression": bound,
+           "bound_source": "max per-step mean compression of the plain 4-iteration solve over the timed window "
+                           "from the same input state" if args.bound is None else "--bound"}
+    out.update(_timed_learned(args, sc, snap, model, 2, bound, dist))
+    out["speedup_vs_plain"] = out["value"] / plain_value
+    one = _timed_learned(args, sc, snap, model, 1, bound, dist)
+    out["one_iteration"] = {"value": one["value"], "speedup_vs_plain": one["value"] / plain_value,
+                            "fallback_substeps": one["fallback_substeps"]}
+    e_l2, fb2 = _errors_from(sc, snap, frames, model=model, learned_iters=2, bound=bound)
+    e_l1, fb1 = _errors_from(sc, snap, frames, model=model, learned_iters=1, bound=bound)
+    e_n2, _ = _errors_from(sc, snap, frames, model=model, learned_iters=2)
+    w = lambda e: {"mean": float(e[window].mean()), "max_step": float(e[window].max())}
+    out["density_error_same_window"] = {"plain4": w(e_plain), "plain2": w(e_plain2),
+                                        "learned2_with_fallback": w(e_l2), "learned1_with_fallback": w(e_l1),
+                                        "learned2_network_only": w(e_n2)}
     return out
 
 

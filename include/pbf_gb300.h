@@ -293,11 +293,11 @@ int pbf_exclusive_scan_u32(const uint32_t* d_in, uint32_t* d_out, size_t n, void
  * predicted positions: density error, previous substep's multiplier,
  * neighbour count, |v'| dt/h, div(v') dt, boundary SDF/h, boundary volume/V,
  * substep index.  One projection with it (ConstrainSolve with lambda_hat)
- * is followed by `iterations` plain iterations; when the mean compression
- * max(0, rho/rho0 - 1) measured in the last iteration exceeds
- * `fallback_bound`, the substep is re-solved from its predicted positions
- * with the plain solve (options.iterations), on the device, without a host
- * round trip.  Training targets are the sums of the plain solver's
+ * is followed by `iterations` plain iterations; when the substep's density
+ * error — the mean over particles of max(0, rho/rho0 - 1) after the solve,
+ * the mean_compression of pbf_get_metrics — exceeds `fallback_bound`, the
+ * substep is re-solved from its predicted positions with the plain solve
+ * (options.iterations), on the device, without a host round trip.  Training targets are the sums of the plain solver's
  * per-iteration multipliers, captured by the trace below. */
 #define PBF_MLP_PARAMS 4801  /* W1 8x64, b1 64, W2 64x64, b2 64, w3 64, b3 */
 typedef struct pbf_mlp {
@@ -327,6 +327,11 @@ int pbf_mlp_train(pbf_mlp* m, const float* feat, const float* target, uint32_t r
 int pbf_set_trace(pbf_handle* h, uint32_t capacity, uint32_t stride, uint64_t salt);
 int pbf_trace_rows(pbf_handle* h, uint32_t* rows);
 int pbf_copy_trace(pbf_handle* h, float* feat, float* target, uint32_t rows);
+/* The plain solve's own density error over the traced substeps: the largest
+ * and the average per-substep mean compression after the solve (the measure
+ * the learned start's fallback test uses; its largest value is the bound at
+ * which the learned start matches the plain solve's worst error). */
+int pbf_trace_error(pbf_handle* h, float* max_mean, float* avg_mean);
 /* model = NULL switches the learned start off.  A negative bound makes every
  * substep fall back (the result is then the plain solve's). */
 int pbf_set_learned(pbf_handle* h, const pbf_mlp* model, uint32_t iterations, float fallback_bound);

@@ -83,14 +83,14 @@ struct pbf_handle {
   float fallback_bound = 0.01f;
   pbf_mlp model;
   DBuf<float> mlp_params, lam_sum, lam_prev, bsdf, fb_mean;
-  DBuf<float4> feat, xs_save;
+  DBuf<float4> feat, xs_save, pos_save;
   DBuf<SolveStats> stats;
   DBuf<int> fb_flag;
   DBuf<uint32_t> fb_count;
   uint32_t trace_cap = 0, trace_stride = 1;
   uint64_t trace_salt = 0;
   uint32_t substep_counter = 0;
-  DBuf<float> trace_feat, trace_tgt;
+  DBuf<float> trace_feat, trace_tgt, trace_err;  // trace_err: [max, sum, count] of the plain solve's error
   DBuf<uint32_t> trace_count;
   // per-kernel timing (pbf_set_kernel_timing)
   bool ktiming = false;
@@ -106,7 +106,7 @@ enum PassId {
 };
 const char* kPassNames[K_NUM] = {"predict",  "sort",   "gather",       "nbr_count",        "nbr_scan",
                                  "nbr_list", "boundary", "lambda",     "deltap_apply",     "density_velocity",
-                                 "vorticity", "xsph",   "export",       "features",         "mlp"};
+                                 "vorticity", "xsph",   "export",       "features_mlp",     "mlp"};
 
 // Brackets one launch (or one group of launches) with events when timing is on.
 struct KScope {
@@ -382,21 +382,24 @@ int substep(pbf_handle* h, cudaEvent_t* ev) {
     }
     CU(h, cudaGetLastError());
     SolverAux al{};
-    al.feat = h->feat.p;
     al.pos = h->pos[cc].p;
     al.lam_prev = h->lam_prev.p;
     al.bsdf = f.loaded ? h->bsdf.p : nullptr;
     al.substep_index = sub_index;
+    al.lam_sum = h->lam_sum.p;
+    al.mlp = h->mlp_params.p;
+    for (int k = 0; k < 8; ++k) {
+      al.norm.mean[k] = h->model.feat_mean[k];
+      al.norm.inv_std[k] = h->model.feat_inv_std[k];
+    }
+    al.norm.lam_scale = h->model.lam_scale;
     {
       KScope ks(h, K_FEATURES);
-      h->passes.lambda_feat<<<nblocks(n, 256), 256, 0, st>>>(p, f.loaded, h->bdata.p, h->xs[0].p, h->warp_off.p,
-                                                              h->nbr_count.p, h->nbr_list.p, cap, h->lambda.p, al);
+      h->passes.lambda_learned<<<nblocks(n, 256), 256, 0, st>>>(p, f.loaded, h->bdata.p, h->xs[0].p,
+                                                                 h->warp_off.p, h->nbr_count.p, h->nbr_list.p, cap,
+                                                                 h->lambda.p, al);
     }
     CU(h, cudaGetLastError());
-    {
-      KScope ks(h, K_MLP);
-      CU(h, launch_mlp_infer(h->mlp_params.p, h->model, (const float*)h->feat.p, n, h->lambda.p, h->lam_sum.p, st));
-    }
     {
       KScope ks(h, K_DELTAP);
       SolverAux ad{};
@@ -405,14 +408,8 @@ int substep(pbf_handle* h, cudaEvent_t* ev) {
                                                          h->xs[1].p, nullptr);
     }
     CU(h, cudaGetLastError());
-    a = iterate(1, h->learned_iters, false, true, false, h->stats.p, nullptr, &rc);
+    a = iterate(1, h->learned_iters, false, true, false, nullptr, nullptr, &rc);
     if (rc) return fail(h, rc, "learned solve launch failed");
-    CU(h, launch_fallback_decide(h->stats.p, h->fallback_bound, h->fb_flag.p, h->fb_count.p, h->fb_mean.p, st));
-    // guarded plain solve from x*_0 (a no-op unless the flag is set)
-    CU(h, launch_copy_guarded(n, h->fb_flag.p, h->xs_save.p, h->xs[0].p, st));
-    int b = iterate(0, h->cfg.options.iterations, false, true, true, nullptr, h->fb_flag.p, &rc);
-    if (rc) return fail(h, rc, "fallback solve launch failed");
-    if (b != a) CU(h, launch_copy_guarded(n, h->fb_flag.p, h->xs[b].p, h->xs[a].p, st));
   } else {
     a = iterate(0, h->cfg.options.iterations, need_feat, need_feat, true, nullptr, nullptr, &rc);
     if (rc) return fail(h, rc, "solve launch failed");
@@ -425,12 +422,35 @@ int substep(pbf_handle* h, cudaEvent_t* ev) {
   h->substep_counter++;
   if (ev) CU(h, cudaEventRecord(ev[3], st));
   // non-pressure passes
+  // AttributeUpdate.  Its density error (mean compression) is the learned
+  // start's fallback test; while tracing it records the plain solve's error.
+  const bool rec = !h->learned && h->trace_cap > 0 && h->stats.p && h->trace_err.p;
+  if (h->learned) CU(h, cudaMemcpyAsync(h->pos_save.p, h->pos[cc].p, (size_t)n * sizeof(float4),
+                                        cudaMemcpyDeviceToDevice, st));
   {
     KScope ks(h, K_DENSITY);
-    h->passes.density_velocity<<<nblocks(n, 256), 256, 0, st>>>(p, h->xs[a].p, h->warp_off.p, h->nbr_count.p,
+    SolverAux ad{};
+    if (h->learned || rec) ad.stats = h->stats.p;
+    h->passes.density_velocity<<<nblocks(n, 256), 256, 0, st>>>(p, ad, h->xs[a].p, h->warp_off.p, h->nbr_count.p,
                                                                  h->nbr_list.p, cap, h->pos[cc].p, h->vel.p);
   }
   CU(h, cudaGetLastError());
+  if (rec) CU(h, launch_stats_record(h->stats.p, h->trace_err.p, st));
+  if (h->learned) {
+    CU(h, launch_fallback_decide(h->stats.p, h->fallback_bound, h->fb_flag.p, h->fb_count.p, h->fb_mean.p, st));
+    // guarded plain re-solve from x*_0 (every launch is a no-op unless the flag is set)
+    const int* fl = h->fb_flag.p;
+    CU(h, launch_copy_guarded(n, fl, h->pos_save.p, h->pos[cc].p, st));
+    CU(h, launch_copy_guarded(n, fl, h->xs_save.p, h->xs[0].p, st));
+    int b = iterate(0, h->cfg.options.iterations, false, true, true, nullptr, fl, &rc);
+    if (rc) return fail(h, rc, "fallback solve launch failed");
+    if (b != a) CU(h, launch_copy_guarded(n, fl, h->xs[b].p, h->xs[a].p, st));
+    SolverAux ag{};
+    ag.guard = fl;
+    h->passes.density_velocity<<<nblocks(n, 256), 256, 0, st>>>(p, ag, h->xs[a].p, h->warp_off.p, h->nbr_count.p,
+                                                                 h->nbr_list.p, cap, h->pos[cc].p, h->vel.p);
+    CU(h, cudaGetLastError());
+  }
   if (a != 0) CU(h, cudaMemcpyAsync(h->xs[0].p, h->xs[1].p, (size_t)n * sizeof(float4), cudaMemcpyDeviceToDevice, st));
   {
     KScope ks(h, K_VORTICITY);
@@ -518,11 +538,13 @@ void release_all(pbf_handle* h) {
   h->fb_mean.release();
   h->feat.release();
   h->xs_save.release();
+  h->pos_save.release();
   h->stats.release();
   h->fb_flag.release();
   h->fb_count.release();
   h->trace_feat.release();
   h->trace_tgt.release();
+  h->trace_err.release();
   h->trace_count.release();
   h->m_f.release();
   h->m_d.release();
@@ -1114,6 +1136,12 @@ int pbf_set_trace(pbf_handle* h, uint32_t capacity, uint32_t stride, uint64_t sa
   if (rc) return rc;
   CU(h, h->trace_feat.alloc((size_t)capacity * 8));
   CU(h, h->trace_tgt.alloc(capacity));
+  if (!h->stats.p) {
+    CU(h, h->stats.alloc(1));
+    CU(h, cudaMemsetAsync(h->stats.p, 0, sizeof(SolveStats), h->stream));
+  }
+  if (!h->trace_err.p) CU(h, h->trace_err.alloc(3));
+  CU(h, cudaMemsetAsync(h->trace_err.p, 0, 3 * sizeof(float), h->stream));
   if (!h->trace_count.p) CU(h, h->trace_count.alloc(1));
   CU(h, cudaMemsetAsync(h->trace_count.p, 0, sizeof(uint32_t), h->stream));
   CU(h, cudaStreamSynchronize(h->stream));
@@ -1147,6 +1175,18 @@ int pbf_copy_trace(pbf_handle* h, float* feat, float* target, uint32_t rows) {
   return PBF_OK;
 }
 
+int pbf_trace_error(pbf_handle* h, float* max_mean, float* avg_mean) {
+  if (!h || !max_mean || !avg_mean) return PBF_EINVAL;
+  *max_mean = *avg_mean = 0.0f;
+  if (!h->trace_err.p) return PBF_OK;
+  float r[3];
+  CU(h, cudaMemcpyAsync(r, h->trace_err.p, sizeof(r), cudaMemcpyDeviceToHost, h->stream));
+  CU(h, cudaStreamSynchronize(h->stream));
+  *max_mean = r[0];
+  *avg_mean = r[2] > 0 ? r[1] / r[2] : 0.0f;
+  return PBF_OK;
+}
+
 int pbf_set_learned(pbf_handle* h, const pbf_mlp* model, uint32_t iterations, float fallback_bound) {
   if (!h) return PBF_EINVAL;
   invalidate_graph(h);
@@ -1162,7 +1202,8 @@ int pbf_set_learned(pbf_handle* h, const pbf_mlp* model, uint32_t iterations, fl
   if (!h->mlp_params.p) {
     CU(h, h->mlp_params.alloc(PBF_MLP_PARAMS));
     CU(h, h->xs_save.alloc(cap));
-    CU(h, h->stats.alloc(1));
+    CU(h, h->pos_save.alloc(cap));
+    if (!h->stats.p) CU(h, h->stats.alloc(1));
     CU(h, h->fb_flag.alloc(1));
     CU(h, h->fb_count.alloc(1));
     CU(h, h->fb_mean.alloc(1));

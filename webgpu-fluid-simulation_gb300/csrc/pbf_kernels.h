@@ -24,10 +24,12 @@ struct PassTable {
                  uint32_t, float*, SolverAux);
   void (*lambda_feat)(SimParams, int, const float4*, const float4*, const uint32_t*, const uint32_t*,
                       const uint32_t*, uint32_t, float*, SolverAux);
+  void (*lambda_learned)(SimParams, int, const float4*, const float4*, const uint32_t*, const uint32_t*,
+                         const uint32_t*, uint32_t, float*, SolverAux);
   void (*deltap)(SimParams, SolverAux, int, const float4*, const float*, const float4*, const uint32_t*,
                  const uint32_t*, const uint32_t*, uint32_t, float4*, float4*);
-  void (*density_velocity)(SimParams, const float4*, const uint32_t*, const uint32_t*, const uint32_t*, uint32_t,
-                           float4*, float4*);
+  void (*density_velocity)(SimParams, SolverAux, const float4*, const uint32_t*, const uint32_t*, const uint32_t*,
+                           uint32_t, float4*, float4*);
   void (*vorticity)(SimParams, const float4*, const float4*, const uint32_t*, const uint32_t*, const uint32_t*,
                     uint32_t, float4*, float4*);
   void (*xsph)(SimParams, const float4*, const float4*, const float4*, const float4*, const uint32_t*,
@@ -116,6 +118,7 @@ cudaError_t launch_gather_f32(uint32_t n, const uint32_t* perm, const float* src
 cudaError_t launch_copy_guarded(uint32_t n, const int* guard, const float4* src, float4* dst, cudaStream_t st);
 cudaError_t launch_fallback_decide(SolveStats* stats, float bound, int* flag, uint32_t* fallbacks, float* last_mean,
                                    cudaStream_t st);
+cudaError_t launch_stats_record(SolveStats* stats, float* rec, cudaStream_t st);
 cudaError_t launch_trace_append(uint32_t n, const uint32_t* ids, const float4* feat, const float* lam_sum,
                                 uint32_t stride, uint32_t salt, float* tf, float* tt, uint32_t* count, uint32_t cap,
                                 cudaStream_t st);

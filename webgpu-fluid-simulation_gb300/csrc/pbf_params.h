@@ -46,6 +46,13 @@ struct SolveStats {
   unsigned long long sum_fx; // sum_i min(max(0, rho_i - 1), 1) in 2^-20 fixed point
 };
 
+// Input normalisation of the learned start's network.
+struct MLPNorm {
+  float mean[8];
+  float inv_std[8];
+  float lam_scale;
+};
+
 // Optional inputs/outputs of the constraint passes used by the learned
 // start and by trace capture.  All null/zero in the plain solve.
 struct SolverAux {
@@ -58,6 +65,8 @@ struct SolverAux {
   const float* lam_prev;     // lambda pass (features): previous substep's multiplier
   SolveStats* stats;         // lambda pass: compression statistics
   float substep_index;       // lambda pass (features)
+  const float* mlp;          // lambda pass (network): flat FP32 parameters
+  MLPNorm norm;              // lambda pass (network)
 };
 
 }  // namespace pbf

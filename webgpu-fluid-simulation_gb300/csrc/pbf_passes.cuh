@@ -19,6 +19,7 @@
 
 #include "pbf_device.cuh"
 #include "pbf_kernels.h"
+#include "pbf_mlp.cuh"
 
 namespace pbf {
 namespace PBF_NS {
@@ -244,74 +245,136 @@ __global__ void __launch_bounds__(256) k_boundary(SimParams p, FieldParams f, co
   if (a.bsdf) a.bsdf[t] = dist;
 }
 
-// LambdaCalculation (pressureConstrain.ts:31-85).  kFeat additionally
-// computes the learned start's features at x*_0 (density error, previous
-// multiplier, neighbour count, |v'|, div v', boundary SDF and volume,
-// substep index; v' = (x* - x)/dt).
-template <bool kFeat>
+// LambdaCalculation (pressureConstrain.ts:31-85).
+//   kMode 0: the reference pass.
+//   kMode 1: also writes the learned start's 8 features at x*_0 (density
+//            error, previous multiplier, neighbour count, |v'| dt/h, div(v') dt,
+//            boundary SDF/h, boundary volume/V, substep index; v' = (x* - x)/dt)
+//            for trace capture.
+//   kMode 2: the learned start: the features go through the MLP in-warp
+//            (32 particles = two 16-row mma tiles) and lambda_hat replaces lambda.
+template <int kMode>
 __global__ void __launch_bounds__(256) k_lambda(SimParams p, int have_field, const float4* __restrict__ bdata,
                                                 const float4* __restrict__ xs, const uint32_t* __restrict__ warp_off,
                                                 const uint32_t* __restrict__ nbr_cnt,
                                                 const uint32_t* __restrict__ nbr_list, uint32_t cap,
                                                 float* __restrict__ lambda, SolverAux a) {
+  constexpr bool kFeat = kMode >= 1;
   if (a.guard && *a.guard == 0) return;
   uint32_t t = blockIdx.x * blockDim.x + threadIdx.x;
-  if (t >= p.n) return;
-  f3 xi = xyz(xs[t]);
-  uint32_t b, e;
-  list_slice(warp_off, nbr_cnt, t, cap, b, e);
-  f3 grad = mk(0.f, 0.f, 0.f);
-  float sum2 = 0.0f, dens = 0.0f, div = 0.0f;
-  f3 vi = mk(0.f, 0.f, 0.f);
-  if (kFeat) vi = p.inv_dt * (xi - xyz(a.pos[t]));
-  for_each_neighbor(nbr_list, b, e, xs, [&](uint32_t j, float4 xj) {
-    Pair q = make_pair_of(xi - xyz(xj));
-    f3 gk = spiky_p(p, q);
-    grad = grad + gk;
-    sum2 = sum2 + dot3(gk, gk);
-    dens = dens + poly6_p(p, q);
-    if (kFeat) {
-      f3 vj = p.inv_dt * (xyz(xj) - xyz(__ldg(a.pos + j)));
-      div = div + dot3(vj - vi, gk);
+  if constexpr (kMode == 2) {
+    __shared__ __align__(16) uint16_t sW1t[mlp::kH * mlp::kW1S];
+    __shared__ __align__(16) uint16_t sW2t[mlp::kH * mlp::kW2S];
+    __shared__ float sB1[mlp::kH], sB2[mlp::kH], sW3[mlp::kH];
+    __shared__ float sF[256 / 32][32][9];
+    mlp::stage_weights(a.mlp, sW1t, sW2t, nullptr);
+    for (int q = threadIdx.x; q < mlp::kH; q += blockDim.x) {
+      sB1[q] = a.mlp[mlp::OFF_B1 + q];
+      sB2[q] = a.mlp[mlp::OFF_B2 + q];
+      sW3[q] = a.mlp[mlp::OFF_W3 + q];
     }
-  });
-  dens = dens * p.V;
-  grad = p.V * grad;
-  sum2 = sum2 * p.V2;
-  float vb = 0.0f;
-  if (have_field) {
-    float4 bd = bdata[t];
-    vb = bd.w;
-    if (bd.w != 0.0f) {
-      Pair q = make_pair_of(xi - xyz(bd));
-      f3 gk = bd.w * spiky_p(p, q);
+    __syncthreads();
+    const bool valid = t < p.n;
+    float fv[8] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
+    if (valid) {
+      f3 xi = xyz(xs[t]);
+      uint32_t b, e;
+      list_slice(warp_off, nbr_cnt, t, cap, b, e);
+      float dens = 0.0f, div = 0.0f;
+      f3 vi = p.inv_dt * (xi - xyz(a.pos[t]));
+      for_each_neighbor(nbr_list, b, e, xs, [&](uint32_t j, float4 xj) {
+        Pair q = make_pair_of(xi - xyz(xj));
+        dens = dens + poly6_p(p, q);
+        f3 vj = p.inv_dt * (xyz(xj) - xyz(__ldg(a.pos + j)));
+        div = div + dot3(vj - vi, spiky_p(p, q));
+      });
+      dens = dens * p.V;
+      float vb = 0.0f;
+      if (have_field) {
+        float4 bd = bdata[t];
+        vb = bd.w;
+        if (bd.w != 0.0f) dens = dens + bd.w * poly6_p(p, make_pair_of(xi - xyz(bd)));
+      }
+      float sd = a.bsdf ? fminf(a.bsdf[t], 2.0f * p.h) : 2.0f * p.h;
+      fv[0] = dens - 1.0f;
+      fv[1] = a.lam_prev ? a.lam_prev[t] : 0.0f;
+      fv[2] = (float)e;
+      fv[3] = len3(vi) * p.dt / p.h;
+      fv[4] = p.V * div * p.dt;
+      fv[5] = sd / p.h;
+      fv[6] = vb / p.V;
+      fv[7] = a.substep_index;
+    }
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, g = lane >> 2, t4 = lane & 3;
+#pragma unroll
+    for (int k = 0; k < 8; ++k) sF[warp][lane][k] = valid ? (fv[k] - a.norm.mean[k]) * a.norm.inv_std[k] : 0.0f;
+    __syncwarp();
+    const uint32_t base = t - lane;
+#pragma unroll
+    for (int tile = 0; tile < 2; ++tile) {
+      const int r = 16 * tile + g;
+      float xg[2] = {sF[warp][r][2 * t4], sF[warp][r][2 * t4 + 1]};
+      float x8[2] = {sF[warp][r + 8][2 * t4], sF[warp][r + 8][2 * t4 + 1]};
+      mlp::Fwd F;
+      mlp::forward_tile(xg, x8, sW1t, sW2t, sB1, sB2, sW3, a.mlp[mlp::OFF_B3], F);
+      if (t4 == 0) {
+        uint32_t ra = base + r, rb = base + r + 8;
+        if (ra < p.n) {
+          float l = F.y0 * a.norm.lam_scale;
+          lambda[ra] = l;
+          a.lam_sum[ra] = l;
+        }
+        if (rb < p.n) {
+          float l = F.y8 * a.norm.lam_scale;
+          lambda[rb] = l;
+          a.lam_sum[rb] = l;
+        }
+      }
+    }
+    return;
+  } else {
+    if (t >= p.n) return;
+    f3 xi = xyz(xs[t]);
+    uint32_t b, e;
+    list_slice(warp_off, nbr_cnt, t, cap, b, e);
+    f3 grad = mk(0.f, 0.f, 0.f);
+    float sum2 = 0.0f, dens = 0.0f, div = 0.0f;
+    f3 vi = mk(0.f, 0.f, 0.f);
+    if (kFeat) vi = p.inv_dt * (xi - xyz(a.pos[t]));
+    for_each_neighbor(nbr_list, b, e, xs, [&](uint32_t j, float4 xj) {
+      Pair q = make_pair_of(xi - xyz(xj));
+      f3 gk = spiky_p(p, q);
       grad = grad + gk;
-      dens = dens + bd.w * poly6_p(p, q);
+      sum2 = sum2 + dot3(gk, gk);
+      dens = dens + poly6_p(p, q);
+      if (kFeat) {
+        f3 vj = p.inv_dt * (xyz(xj) - xyz(__ldg(a.pos + j)));
+        div = div + dot3(vj - vi, gk);
+      }
+    });
+    dens = dens * p.V;
+    grad = p.V * grad;
+    sum2 = sum2 * p.V2;
+    float vb = 0.0f;
+    if (have_field) {
+      float4 bd = bdata[t];
+      vb = bd.w;
+      if (bd.w != 0.0f) {
+        Pair q = make_pair_of(xi - xyz(bd));
+        f3 gk = bd.w * spiky_p(p, q);
+        grad = grad + gk;
+        dens = dens + bd.w * poly6_p(p, q);
+      }
     }
-  }
-  float c = fmaxf(0.0f, dens - 1.0f);
-  float s = dot3(grad, grad) + sum2;
-  float lam = fdiv(-c, s + p.lambda_eps);
-  lambda[t] = lam;
-  if (a.lam_sum) a.lam_sum[t] = a.lam_first ? lam : a.lam_sum[t] + lam;
-  if (kFeat) {
-    float sd = a.bsdf ? fminf(a.bsdf[t], 2.0f * p.h) : 2.0f * p.h;
-    a.feat[2 * t] = make_float4(dens - 1.0f, a.lam_prev ? a.lam_prev[t] : 0.0f, (float)e,
-                                len3(vi) * p.dt / p.h);
-    a.feat[2 * t + 1] = make_float4(p.V * div * p.dt, sd / p.h, vb / p.V, a.substep_index);
-  }
-  if (a.stats) {
-    // warp-aggregated compression statistics (lanes past n have returned)
-    const unsigned m = __activemask();
-    unsigned bits = __float_as_uint(c);
-    unsigned fx = (unsigned)(fminf(c, 1.0f) * 1048576.0f);
-    unsigned wmax = __reduce_max_sync(m, bits);
-    unsigned wsum = __reduce_add_sync(m, fx);
-    unsigned wcnt = __popc(m);
-    if ((threadIdx.x & 31u) == (unsigned)(__ffs(m) - 1)) {
-      atomicMax(&a.stats->max_bits, wmax);
-      atomicAdd(&a.stats->count, wcnt);
-      atomicAdd(&a.stats->sum_fx, (unsigned long long)wsum);
+    float c = fmaxf(0.0f, dens - 1.0f);
+    float s = dot3(grad, grad) + sum2;
+    float lam = fdiv(-c, s + p.lambda_eps);
+    lambda[t] = lam;
+    if (a.lam_sum) a.lam_sum[t] = a.lam_first ? lam : a.lam_sum[t] + lam;
+    if (kFeat) {
+      float sd = a.bsdf ? fminf(a.bsdf[t], 2.0f * p.h) : 2.0f * p.h;
+      a.feat[2 * t] = make_float4(dens - 1.0f, a.lam_prev ? a.lam_prev[t] : 0.0f, (float)e, len3(vi) * p.dt / p.h);
+      a.feat[2 * t + 1] = make_float4(p.V * div * p.dt, sd / p.h, vb / p.V, a.substep_index);
     }
   }
 }
@@ -349,11 +412,12 @@ __global__ void __launch_bounds__(256) k_deltap(SimParams p, SolverAux a, int ha
 }
 
 // AttributeUpdate: rho = m * sum W (fluid only), v = (x* - x) / dt, x <- (x*, rho).
-__global__ void __launch_bounds__(256) k_density_velocity(SimParams p, const float4* __restrict__ xs,
+__global__ void __launch_bounds__(256) k_density_velocity(SimParams p, SolverAux a, const float4* __restrict__ xs,
                                                           const uint32_t* __restrict__ warp_off,
                                                           const uint32_t* __restrict__ nbr_cnt,
                                                           const uint32_t* __restrict__ nbr_list, uint32_t cap,
                                                           float4* __restrict__ pos, float4* __restrict__ vel) {
+  if (a.guard && *a.guard == 0) return;
   uint32_t t = blockIdx.x * blockDim.x + threadIdx.x;
   if (t >= p.n) return;
   f3 xi = xyz(xs[t]);
@@ -364,10 +428,25 @@ __global__ void __launch_bounds__(256) k_density_velocity(SimParams p, const flo
     Pair q = make_pair_of(xi - xyz(xj));
     dens = dens + poly6_p(p, q);
   });
+  float vsum = dens;
   dens = dens * p.m;
   f3 xo = xyz(pos[t]);
   vel[t] = f4(p.inv_dt * (xi - xo), 0.0f);
   pos[t] = f4(xi, dens);
+  if (a.stats) {
+    // per-step density error: compression max(0, rho/rho0 - 1) = max(0, V sum W - 1),
+    // warp-aggregated (lanes past n have returned)
+    float c = fmaxf(0.0f, vsum * p.V - 1.0f);
+    const unsigned m = __activemask();
+    unsigned fx = (unsigned)(fminf(c, 1.0f) * 1048576.0f);
+    unsigned wmax = __reduce_max_sync(m, __float_as_uint(c));
+    unsigned wsum = __reduce_add_sync(m, fx);
+    if ((threadIdx.x & 31u) == (unsigned)(__ffs(m) - 1)) {
+      atomicMax(&a.stats->max_bits, wmax);
+      atomicAdd(&a.stats->count, (unsigned)__popc(m));
+      atomicAdd(&a.stats->sum_fx, (unsigned long long)wsum);
+    }
+  }
 }
 
 // VorticityConfinement: omega_i and the Akinci normal n_i.
@@ -440,8 +519,9 @@ void fill_pass_table(PassTable* tbl) {
   tbl->nbr_list = k_nbr_list;
   tbl->nbr_list_sliced = k_nbr_list_sliced;
   tbl->boundary = k_boundary;
-  tbl->lambda = k_lambda<false>;
-  tbl->lambda_feat = k_lambda<true>;
+  tbl->lambda = k_lambda<0>;
+  tbl->lambda_feat = k_lambda<1>;
+  tbl->lambda_learned = k_lambda<2>;
   tbl->deltap = k_deltap;
   tbl->density_velocity = k_density_velocity;
   tbl->vorticity = k_vorticity;

@@ -134,6 +134,7 @@ SIGNATURES = {
     "pbf_set_trace": (ctypes.c_int, [_P, u32, u32, ctypes.c_uint64]),
     "pbf_trace_rows": (ctypes.c_int, [_P, _UP]),
     "pbf_copy_trace": (ctypes.c_int, [_P, _FP, _FP, u32]),
+    "pbf_trace_error": (ctypes.c_int, [_P, _FP, _FP]),
     "pbf_set_learned": (ctypes.c_int, [_P, ctypes.POINTER(MLP), u32, ctypes.c_float]),
 }
 

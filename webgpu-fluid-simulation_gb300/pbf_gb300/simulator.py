@@ -198,6 +198,12 @@ class PBF:
                     "copy_trace")
         return f, t
 
+    def trace_error(self):
+        """(max, average) per-substep mean compression of the traced plain solve."""
+        a, b = ctypes.c_float(), ctypes.c_float()
+        self._check(self._lib.pbf_trace_error(self._h, ctypes.byref(a), ctypes.byref(b)), "trace_error")
+        return a.value, b.value
+
     def set_learned(self, model, iterations=2, fallback_bound=0.01):
         m = None if model is None else ctypes.byref(model)
         self._check(self._lib.pbf_set_learned(self._h, m, int(iterations), float(fallback_bound)), "set_learned")

@@ -50,12 +50,10 @@ ALG_BYTES = {
     "predict": 68,            # read x, v, a; write x*, key (+ rank)
     "sort": 32,               # key, rank, id -> perm_raw, id_raw; cell fix -> perm
     "gather": 76,             # perm -> pos, x*, id in the new order
-    "nbr_count": 20,          # read x*, write count
-    "nbr_scan": 8,
-    "nbr_list": 20,           # read x*, offset (+ 4 B per neighbour written, counted separately)
+    "nbr_build": 20,          # read x*, write count (+ 4 B per neighbour written, counted separately)
     "boundary": 32,           # read x*, write (x_b, V_b)
-    "lambda": 20,             # read x*, write lambda
-    "deltap_apply": 36,       # read x*, lambda; write x*
+    "lambda": 32,             # read x*, write (x*, lambda)
+    "deltap_apply": 32,       # read (x*, lambda); write x*
     "density_velocity": 64,   # read x*, x; write v, (x, rho)
     "vorticity": 64,          # read x, v; write omega, n
     "xsph": 80,               # read x, v, omega, n; write a
@@ -67,8 +65,8 @@ ALG_BYTES = {
 # the same workload (profiles/neighbor_passes_sphere_drop_1m_ncu.md); the
 # neighbour list (~185 MB) is the difference to the algorithmic bytes.
 NCU_TRAFFIC_BYTES = {
-    "lambda": 208.0e6, "deltap_apply": 218.9e6, "xsph": 250.5e6, "nbr_list": 310.4e6, "nbr_count": 17.7e6,
-    "vorticity": 226.0e6, "boundary": 46.0e6,
+    "lambda": 214.0e6, "deltap_apply": 214.1e6, "xsph": 250.5e6, "nbr_build": 286.8e6, "vorticity": 225.5e6,
+    "boundary": 48.9e6, "density_velocity": 222.5e6,
 }
 
 
@@ -398,7 +396,9 @@ def gpu_arm(args, dist):
                 "share": tot_ms / total_ms if total_ms else None,
                 "passes": {k: {"launches": v[0], "ms": round(v[1], 4),
                                "share": round(v[1] / total_ms, 4) if total_ms else None} for k, v in kt.items()}}
-    launches_per_frame = sub * (12 + 3 * iters) + 1
+    # per substep: predict, scan + scatter + cell fix + big cells, gather, neighbour
+    # build, 3 per iteration, density/velocity, vorticity, XSPH; + 1 export
+    launches_per_frame = sub * (10 + 3 * iters) + 1
     line = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": dist.world, "steps": args.steps,
         "warmup": max(args.warmup, 3), "ms_per_step": ms_max / args.steps, "higher_is_better": True,

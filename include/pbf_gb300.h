@@ -93,7 +93,11 @@ typedef struct pbf_config {
                                does (discreteFieldShader.ts:146-147,152-153) */
   uint32_t fp_mode;         /* pbf_fp_mode */
   uint32_t boundary_interp; /* pbf_boundary_interp */
-  uint32_t max_neighbors;   /* mean neighbour-list capacity per particle (60) */
+  uint32_t max_neighbors;   /* neighbour-list capacity per particle (60; the reference
+                               sizes its list as SPH.MAX_NEIGHBOR_COUNT x particles,
+                               neighborSearch.ts:81).  Each particle has a fixed slice
+                               of this many entries; a particle with more neighbours
+                               fails its substep with PBF_ECAPACITY and grows the slice */
   pbf_options options;
   void* stream;             /* cudaStream_t to run on, or NULL for a library-owned stream */
 } pbf_config;

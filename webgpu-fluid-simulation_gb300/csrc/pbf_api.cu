@@ -58,18 +58,18 @@ struct pbf_handle {
   int cur = 0;  // which of pos[]/ids[] holds the current state
   std::vector<float> host_particles;  // SPH.particlePositionArray
 
-  DBuf<float4> pos[2], xs[2], vel, acc, bdata, omega, normal, dp, out_pos, out_tmp;
+  DBuf<float4> pos[2], xs[2], xl, vel, acc, bdata, omega, normal, dp, out_pos, out_tmp;
   DBuf<uint32_t> ids[2], key, rank, perm_raw, id_raw, perm, tmp_a, tmp_b;
   DBuf<uint32_t> cell_count, cell_start, big_list, big_count;
-  DBuf<uint32_t> nbr_count, warp_len, warp_off, nbr_list;
-  DBuf<float> lambda, sdf, vol;
+  DBuf<uint32_t> nbr_count, nbr_max, nbr_list;
+  DBuf<float> sdf, vol;
   DBuf<uint8_t> bflag;  // per field cell: 1 when the boundary sample can be non-zero
   DBuf<uint32_t> err_word;
   DBuf<float> m_f;
   DBuf<double> m_d;
   DBuf<uint32_t> m_u;
   void* scan_scratch = nullptr;
-  uint32_t nbr_capacity = 0;
+  uint32_t nbr_slice = 0;  // list entries per particle (fixed slice)
   uint32_t id_bits = 1;
 
   cudaGraphExec_t graph_exec = nullptr;
@@ -101,12 +101,11 @@ struct pbf_handle {
 namespace {
 
 enum PassId {
-  K_PREDICT, K_SORT, K_GATHER, K_NBR_COUNT, K_NBR_SCAN, K_NBR_LIST, K_BOUNDARY, K_LAMBDA, K_DELTAP, K_DENSITY,
-  K_VORTICITY, K_XSPH, K_EXPORT, K_FEATURES, K_MLP, K_NUM
+  K_PREDICT, K_SORT, K_GATHER, K_NBR_BUILD, K_BOUNDARY, K_LAMBDA, K_DELTAP, K_DENSITY, K_VORTICITY, K_XSPH,
+  K_EXPORT, K_FEATURES, K_MLP, K_NUM
 };
-const char* kPassNames[K_NUM] = {"predict",  "sort",   "gather",       "nbr_count",        "nbr_scan",
-                                 "nbr_list", "boundary", "lambda",     "deltap_apply",     "density_velocity",
-                                 "vorticity", "xsph",   "export",       "features_mlp",     "mlp"};
+const char* kPassNames[K_NUM] = {"predict",   "sort", "gather", "nbr_build", "boundary",     "lambda", "deltap_apply",
+                                 "density_velocity", "vorticity", "xsph", "export", "features_mlp", "mlp"};
 
 // Brackets one launch (or one group of launches) with events when timing is on.
 struct KScope {
@@ -220,9 +219,10 @@ void invalidate_graph(pbf_handle* h) {
   h->graph_valid = false;
 }
 
-// Reads and clears the device error word.  A neighbour-list overflow grows
-// the list to 1.25x the size the last substep needed (the results of that
-// substep are invalid: its lists were truncated) and is reported once.
+// Reads and clears the device error word.  A neighbour-list overflow (a
+// particle with more neighbours than the per-particle slice) grows the slice
+// to 1.25x the largest count seen; the results of that substep are invalid
+// (its lists were truncated) and the overflow is reported once.
 int check_device_errors(pbf_handle* h) {
   uint32_t e = 0;
   CU(h, cudaMemcpyAsync(&e, h->err_word.p, sizeof(uint32_t), cudaMemcpyDeviceToHost, h->stream));
@@ -232,21 +232,22 @@ int check_device_errors(pbf_handle* h) {
     CU(h, cudaStreamSynchronize(h->stream));
     if (e & PBF_DEVERR_NEIGHBOR_OVERFLOW) {
       uint32_t need = 0;
-      const uint32_t nw = (h->n + 31) / 32;
-      CU(h, cudaMemcpy(&need, h->warp_off.p + nw, sizeof(uint32_t), cudaMemcpyDeviceToHost));
-      uint64_t grow = (uint64_t)need + need / 4 + 1024;
-      if (grow > 0xffffffffull) grow = 0xffffffffull;
-      uint32_t old = h->nbr_capacity;
+      CU(h, cudaMemcpy(&need, h->nbr_max.p, sizeof(uint32_t), cudaMemcpyDeviceToHost));
+      CU(h, cudaMemset(h->nbr_max.p, 0, sizeof(uint32_t)));
+      const uint64_t rows = ((uint64_t)h->cfg.max_particles + 31) / 32 * 32;
+      uint64_t grow = (uint64_t)need + need / 4 + 4;
+      if (grow * rows > 0xffffffffull) grow = 0xffffffffull / rows;
+      const uint32_t old = h->nbr_slice;
       if (grow > old) {
         invalidate_graph(h);
         h->nbr_list.release();
-        CU(h, h->nbr_list.alloc(grow));
-        h->nbr_capacity = (uint32_t)grow;
+        CU(h, h->nbr_list.alloc(rows * grow));
+        h->nbr_slice = (uint32_t)grow;
       }
       return fail(h, PBF_ECAPACITY,
-                  "neighbour list overflow: %u entries needed, capacity was %u; grown to %u, the last substep's "
-                  "results are invalid",
-                  need, old, h->nbr_capacity);
+                  "neighbour list overflow: a particle has %u neighbours, the per-particle capacity was %u; grown "
+                  "to %u, the last substep's results are invalid",
+                  need, old, h->nbr_slice);
     }
     if (e & PBF_DEVERR_SCAN_TIMEOUT) return fail(h, PBF_ETIMEOUT, "scan look-back wait gave up");
     return fail(h, PBF_ECUDA, "device error word 0x%x", e);
@@ -291,30 +292,17 @@ int substep(pbf_handle* h, cudaEvent_t* ev) {
   if (need_feat) CU(h, launch_gather_f32(n, h->perm.p, h->lam_sum.p, h->lam_prev.p, st));
   h->cur = nx;
   const int cc = nx;
-  // NeighborCount + particle scan + NeighborList
-  const uint32_t nw = (n + 31) / 32;
+  // NeighborCount + NeighborList in one pass (fixed per-particle slices: no scan)
   {
-    KScope ks(h, K_NBR_COUNT);
-    // n + 33 threads: the lane-0 thread of warp ceil(n/32), which writes the
-    // terminating zero of the slice lengths, is always in the grid
-    h->passes.nbr_count<<<nblocks(n + 33, 256), 256, 0, st>>>(p, g, h->xs[0].p, h->cell_start.p, h->nbr_count.p,
-                                                               h->warp_len.p);
-  }
-  CU(h, cudaGetLastError());
-  {
-    KScope ks(h, K_NBR_SCAN);
-    CU(h, launch_exclusive_scan(h->warp_len.p, h->warp_off.p, (size_t)nw + 1, h->scan_scratch, h->err_word.p, st));
-  }
-  {
-    KScope ks(h, K_NBR_LIST);
-    h->passes.nbr_list_sliced<<<nblocks(n, 256), 256, 0, st>>>(p, g, h->xs[0].p, h->cell_start.p, h->warp_off.p,
-                                                                h->nbr_list.p, h->nbr_capacity, h->err_word.p);
+    KScope ks(h, K_NBR_BUILD);
+    h->passes.nbr_build<<<nblocks(n, 256), 256, 0, st>>>(p, g, h->xs[0].p, h->cell_start.p, h->nbr_slice,
+                                                          h->nbr_list.p, h->nbr_count.p, h->nbr_max.p, h->err_word.p);
   }
   CU(h, cudaGetLastError());
   if (ev) CU(h, cudaEventRecord(ev[2], st));
   // constraint loop
   const FieldParams f = h->fp;
-  const uint32_t cap = h->nbr_capacity;
+  const uint32_t ms = h->nbr_slice;
   const float sub_index = (float)(h->substep_counter % h->cfg.substeps);
   // `iters` plain iterations starting from xs[a]; returns the buffer holding
   // the result.  aux0 is used by the first iteration's lambda pass (features
@@ -350,16 +338,16 @@ int substep(pbf_handle* h, cudaEvent_t* ev) {
       {
         KScope ks(h, K_LAMBDA);
         auto kl = fe ? h->passes.lambda_feat : h->passes.lambda;
-        kl<<<nblocks(n, 256), 256, 0, st>>>(p, f.loaded, h->bdata.p, h->xs[a].p, h->warp_off.p, h->nbr_count.p,
-                                             h->nbr_list.p, cap, h->lambda.p, al);
+        kl<<<nblocks(n, 256), 256, 0, st>>>(p, f.loaded, h->bdata.p, h->xs[a].p, ms, h->nbr_count.p,
+                                             h->nbr_list.p, h->xl.p, al);
       }
       if (cudaGetLastError() != cudaSuccess) { *rc = PBF_ECUDA; return a; }
       SolverAux ad{};
       ad.guard = guard;
       {
         KScope ks(h, K_DELTAP);
-        h->passes.deltap<<<nblocks(n, 256), 256, 0, st>>>(p, ad, f.loaded, h->xs[a].p, h->lambda.p, h->bdata.p,
-                                                           h->warp_off.p, h->nbr_count.p, h->nbr_list.p, cap,
+        h->passes.deltap<<<nblocks(n, 256), 256, 0, st>>>(p, ad, f.loaded, h->xl.p, h->bdata.p,
+                                                           ms, h->nbr_count.p, h->nbr_list.p,
                                                            h->xs[1 - a].p, h->capture ? h->dp.p : nullptr);
       }
       if (cudaGetLastError() != cudaSuccess) { *rc = PBF_ECUDA; return a; }
@@ -396,15 +384,15 @@ int substep(pbf_handle* h, cudaEvent_t* ev) {
     {
       KScope ks(h, K_FEATURES);
       h->passes.lambda_learned<<<nblocks(n, 256), 256, 0, st>>>(p, f.loaded, h->bdata.p, h->xs[0].p,
-                                                                 h->warp_off.p, h->nbr_count.p, h->nbr_list.p, cap,
-                                                                 h->lambda.p, al);
+                                                                 ms, h->nbr_count.p, h->nbr_list.p,
+                                                                 h->xl.p, al);
     }
     CU(h, cudaGetLastError());
     {
       KScope ks(h, K_DELTAP);
       SolverAux ad{};
-      h->passes.deltap<<<nblocks(n, 256), 256, 0, st>>>(p, ad, f.loaded, h->xs[0].p, h->lambda.p, h->bdata.p,
-                                                         h->warp_off.p, h->nbr_count.p, h->nbr_list.p, cap,
+      h->passes.deltap<<<nblocks(n, 256), 256, 0, st>>>(p, ad, f.loaded, h->xl.p, h->bdata.p,
+                                                         ms, h->nbr_count.p, h->nbr_list.p,
                                                          h->xs[1].p, nullptr);
     }
     CU(h, cudaGetLastError());
@@ -431,8 +419,8 @@ int substep(pbf_handle* h, cudaEvent_t* ev) {
     KScope ks(h, K_DENSITY);
     SolverAux ad{};
     if (h->learned || rec) ad.stats = h->stats.p;
-    h->passes.density_velocity<<<nblocks(n, 256), 256, 0, st>>>(p, ad, h->xs[a].p, h->warp_off.p, h->nbr_count.p,
-                                                                 h->nbr_list.p, cap, h->pos[cc].p, h->vel.p);
+    h->passes.density_velocity<<<nblocks(n, 256), 256, 0, st>>>(p, ad, h->xs[a].p, ms, h->nbr_count.p,
+                                                                 h->nbr_list.p, h->pos[cc].p, h->vel.p);
   }
   CU(h, cudaGetLastError());
   if (rec) CU(h, launch_stats_record(h->stats.p, h->trace_err.p, st));
@@ -447,22 +435,21 @@ int substep(pbf_handle* h, cudaEvent_t* ev) {
     if (b != a) CU(h, launch_copy_guarded(n, fl, h->xs[b].p, h->xs[a].p, st));
     SolverAux ag{};
     ag.guard = fl;
-    h->passes.density_velocity<<<nblocks(n, 256), 256, 0, st>>>(p, ag, h->xs[a].p, h->warp_off.p, h->nbr_count.p,
-                                                                 h->nbr_list.p, cap, h->pos[cc].p, h->vel.p);
+    h->passes.density_velocity<<<nblocks(n, 256), 256, 0, st>>>(p, ag, h->xs[a].p, ms, h->nbr_count.p,
+                                                                 h->nbr_list.p, h->pos[cc].p, h->vel.p);
     CU(h, cudaGetLastError());
   }
   if (a != 0) CU(h, cudaMemcpyAsync(h->xs[0].p, h->xs[1].p, (size_t)n * sizeof(float4), cudaMemcpyDeviceToDevice, st));
   {
     KScope ks(h, K_VORTICITY);
-    h->passes.vorticity<<<nblocks(n, 256), 256, 0, st>>>(p, h->pos[cc].p, h->vel.p, h->warp_off.p,
-                                                          h->nbr_count.p, h->nbr_list.p, cap, h->omega.p,
+    h->passes.vorticity<<<nblocks(n, 256), 256, 0, st>>>(p, h->pos[cc].p, h->vel.p, ms, h->nbr_count.p, h->nbr_list.p, h->omega.p,
                                                           h->normal.p);
   }
   CU(h, cudaGetLastError());
   {
     KScope ks(h, K_XSPH);
     h->passes.xsph<<<nblocks(n, 256), 256, 0, st>>>(p, h->pos[cc].p, h->vel.p, h->omega.p, h->normal.p,
-                                                     h->warp_off.p, h->nbr_count.p, h->nbr_list.p, cap, h->acc.p);
+                                                     ms, h->nbr_count.p, h->nbr_list.p, h->acc.p);
   }
   CU(h, cudaGetLastError());
   if (ev) CU(h, cudaEventRecord(ev[4], st));
@@ -508,7 +495,7 @@ int upload_particles(pbf_handle* h, const float* xyzw, uint32_t n) {
     CU(h, cudaMemcpyAsync(h->ids[0].p, iota.data(), (size_t)n * sizeof(uint32_t), cudaMemcpyHostToDevice, st));
     CU(h, cudaMemsetAsync(h->vel.p, 0, (size_t)n * sizeof(float4), st));
     CU(h, cudaMemsetAsync(h->acc.p, 0, (size_t)n * sizeof(float4), st));
-    CU(h, cudaMemsetAsync(h->lambda.p, 0, (size_t)n * sizeof(float), st));
+    CU(h, cudaMemsetAsync(h->xl.p, 0, (size_t)n * sizeof(float4), st));
     CU(h, cudaMemsetAsync(h->bdata.p, 0, (size_t)n * sizeof(float4), st));
   }
   int rc = export_positions(h);
@@ -519,15 +506,14 @@ int upload_particles(pbf_handle* h, const float* xyzw, uint32_t n) {
 
 void release_all(pbf_handle* h) {
   invalidate_graph(h);
-  DBuf<float4>* f4s[] = {&h->pos[0], &h->pos[1], &h->xs[0], &h->xs[1], &h->vel, &h->acc, &h->bdata,
+  DBuf<float4>* f4s[] = {&h->pos[0], &h->pos[1], &h->xs[0], &h->xs[1], &h->xl, &h->vel, &h->acc, &h->bdata,
                          &h->omega,  &h->normal, &h->dp,    &h->out_pos, &h->out_tmp};
   for (auto* b : f4s) b->release();
   DBuf<uint32_t>* u32s[] = {&h->ids[0],   &h->ids[1],      &h->key,      &h->rank,      &h->perm_raw,
                             &h->id_raw,   &h->perm,        &h->tmp_a,    &h->tmp_b,     &h->cell_count,
-                            &h->cell_start, &h->big_list,  &h->big_count, &h->nbr_count, &h->warp_len, &h->warp_off,
+                            &h->cell_start, &h->big_list,  &h->big_count, &h->nbr_count, &h->nbr_max,
                             &h->nbr_list, &h->err_word,    &h->m_u};
   for (auto* b : u32s) b->release();
-  h->lambda.release();
   h->sdf.release();
   h->vol.release();
   h->bflag.release();
@@ -662,9 +648,10 @@ int pbf_create(const pbf_config* cfg, pbf_handle** out) {
     h->own_stream = true;
   }
   const size_t cap = cfg->max_particles, cells = h->gp.cells;
-  uint64_t ncap64 = (uint64_t)cap * cfg->max_neighbors;
-  if (ncap64 > 0xffffffffull) ncap64 = 0xffffffffull;
-  h->nbr_capacity = (uint32_t)ncap64;
+  const uint64_t rows = (uint64_t)(cap + 31) / 32 * 32;
+  uint64_t slice = cfg->max_neighbors;
+  if (slice * rows > 0xffffffffull) slice = 0xffffffffull / rows;
+  h->nbr_slice = (uint32_t)slice;
   auto A = [&](cudaError_t r) {
     if (e == cudaSuccess) e = r;
   };
@@ -692,10 +679,9 @@ int pbf_create(const pbf_config* cfg, pbf_handle** out) {
   A(h->big_list.alloc(cells));
   A(h->big_count.alloc(1));
   A(h->nbr_count.alloc(cap + 1));
-  A(h->warp_len.alloc(cap / 32 + 3));
-  A(h->warp_off.alloc(cap / 32 + 3));
-  A(h->nbr_list.alloc(h->nbr_capacity));
-  A(h->lambda.alloc(cap));
+  A(h->nbr_max.alloc(1));
+  A(h->nbr_list.alloc(rows * h->nbr_slice));
+  A(h->xl.alloc(cap));
   A(h->err_word.alloc(1));
   A(h->m_f.alloc(2));
   A(h->m_d.alloc(3));
@@ -706,6 +692,7 @@ int pbf_create(const pbf_config* cfg, pbf_handle** out) {
   A(cudaMalloc(&h->scan_scratch, sb));
   for (int i = 0; i < 5; ++i) A(cudaEventCreate(&h->ev[i]));
   if (e == cudaSuccess) {
+    A(cudaMemsetAsync(h->nbr_max.p, 0, sizeof(uint32_t), h->stream));
     A(cudaMemsetAsync(h->err_word.p, 0, sizeof(uint32_t), h->stream));
     A(cudaMemsetAsync(h->vel.p, 0, cap * sizeof(float4), h->stream));
     A(cudaMemsetAsync(h->acc.p, 0, cap * sizeof(float4), h->stream));
@@ -1244,7 +1231,7 @@ int pbf_copy_field(pbf_handle* h, int field, void* host, size_t bytes) {
     case PBF_FIELD_PREDICTED: src4 = h->xs[0].p; break;
     case PBF_FIELD_BOUNDARY: src4 = h->bdata.p; break;
     case PBF_FIELD_OMEGA: src4 = h->omega.p; break;
-    case PBF_FIELD_NORMAL: src4 = h->normal.p; break;
+    case PBF_FIELD_NORMAL: src4 = h->normal.p; break;  // w (|omega|, internal) is cleared below
     case PBF_FIELD_DELTA_P:
       if (!h->capture || !h->dp.p) return fail(h, PBF_ESTATE, "delta_p needs pbf_set_capture(1) before the step");
       src4 = h->dp.p;
@@ -1257,13 +1244,14 @@ int pbf_copy_field(pbf_handle* h, int field, void* host, size_t bytes) {
     if (bytes != need4) return fail(h, PBF_EINVAL, "field needs %zu bytes, got %zu", need4, bytes);
     if (n) {
       CU(h, launch_scatter_by_id(n, id, src4, h->out_tmp.p, st));
+      if (field == PBF_FIELD_NORMAL) CU(h, cudaMemset2DAsync((char*)h->out_tmp.p + 12, 16, 0, 4, n, st));
       CU(h, cudaMemcpyAsync(host, h->out_tmp.p, need4, cudaMemcpyDeviceToHost, st));
     }
   } else {
     if (bytes != need1) return fail(h, PBF_EINVAL, "field needs %zu bytes, got %zu", need1, bytes);
     if (n) {
       if (field == PBF_FIELD_LAMBDA)
-        CU(h, launch_scatter_by_id_f32(n, id, h->lambda.p, (float*)h->out_tmp.p, st));
+        CU(h, launch_scatter_w_by_id(n, id, h->xl.p, (float*)h->out_tmp.p, st));
       else
         CU(h, launch_scatter_by_id_u32(n, id, h->nbr_count.p, (uint32_t*)h->out_tmp.p, st));
       CU(h, cudaMemcpyAsync(host, h->out_tmp.p, need1, cudaMemcpyDeviceToHost, st));
@@ -1457,7 +1445,7 @@ int pbf_ns_lists(pbf_ns* s, const float* d_pos4, uint32_t n, float radius, uint3
   exact::fill_pass_table(&tbl);
   NSCU(s, launch_gather_state(n, s->perm.p, (const float4*)d_pos4, (const float4*)d_pos4, nullptr, sorted, sorted,
                               ids, st));
-  tbl.nbr_count<<<nblocks(n + 1, 256), 256, 0, st>>>(p, s->g, sorted, s->cell_start.p, s->nbr_count.p, nullptr);
+  tbl.nbr_count<<<nblocks(n + 1, 256), 256, 0, st>>>(p, s->g, sorted, s->cell_start.p, s->nbr_count.p);
   NSCU(s, cudaGetLastError());
   // counts are in slot order; the reference's offsets are by particle id
   uint32_t* cnt_by_id = nullptr;

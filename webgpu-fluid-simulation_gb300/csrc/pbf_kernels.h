@@ -13,27 +13,27 @@ namespace pbf {
 struct PassTable {
   void (*predict)(SimParams, GridParams, const float4*, const float4*, const float4*, float4*, uint32_t*, uint32_t*,
                   uint32_t*);
-  void (*nbr_count)(SimParams, GridParams, const float4*, const uint32_t*, uint32_t*, uint32_t*);
+  void (*nbr_count)(SimParams, GridParams, const float4*, const uint32_t*, uint32_t*);
   void (*nbr_list)(SimParams, GridParams, const float4*, const uint32_t*, const uint32_t*, uint32_t*, uint32_t,
                    uint32_t*);
-  void (*nbr_list_sliced)(SimParams, GridParams, const float4*, const uint32_t*, const uint32_t*, uint32_t*, uint32_t,
-                          uint32_t*);
+  void (*nbr_build)(SimParams, GridParams, const float4*, const uint32_t*, uint32_t, uint32_t*, uint32_t*,
+                    uint32_t*, uint32_t*);
   void (*boundary)(SimParams, FieldParams, const float*, const float*, const uint8_t*, const float4*, float4*,
                    SolverAux);
-  void (*lambda)(SimParams, int, const float4*, const float4*, const uint32_t*, const uint32_t*, const uint32_t*,
-                 uint32_t, float*, SolverAux);
-  void (*lambda_feat)(SimParams, int, const float4*, const float4*, const uint32_t*, const uint32_t*,
-                      const uint32_t*, uint32_t, float*, SolverAux);
-  void (*lambda_learned)(SimParams, int, const float4*, const float4*, const uint32_t*, const uint32_t*,
-                         const uint32_t*, uint32_t, float*, SolverAux);
-  void (*deltap)(SimParams, SolverAux, int, const float4*, const float*, const float4*, const uint32_t*,
-                 const uint32_t*, const uint32_t*, uint32_t, float4*, float4*);
-  void (*density_velocity)(SimParams, SolverAux, const float4*, const uint32_t*, const uint32_t*, const uint32_t*,
-                           uint32_t, float4*, float4*);
-  void (*vorticity)(SimParams, const float4*, const float4*, const uint32_t*, const uint32_t*, const uint32_t*,
-                    uint32_t, float4*, float4*);
-  void (*xsph)(SimParams, const float4*, const float4*, const float4*, const float4*, const uint32_t*,
-               const uint32_t*, const uint32_t*, uint32_t, float4*);
+  void (*lambda)(SimParams, int, const float4*, const float4*, uint32_t, const uint32_t*, const uint32_t*, float4*,
+                 SolverAux);
+  void (*lambda_feat)(SimParams, int, const float4*, const float4*, uint32_t, const uint32_t*, const uint32_t*,
+                      float4*, SolverAux);
+  void (*lambda_learned)(SimParams, int, const float4*, const float4*, uint32_t, const uint32_t*, const uint32_t*,
+                         float4*, SolverAux);
+  void (*deltap)(SimParams, SolverAux, int, const float4*, const float4*, uint32_t, const uint32_t*, const uint32_t*,
+                 float4*, float4*);
+  void (*density_velocity)(SimParams, SolverAux, const float4*, uint32_t, const uint32_t*, const uint32_t*, float4*,
+                           float4*);
+  void (*vorticity)(SimParams, const float4*, const float4*, uint32_t, const uint32_t*, const uint32_t*, float4*,
+                    float4*);
+  void (*xsph)(SimParams, const float4*, const float4*, const float4*, const float4*, uint32_t, const uint32_t*,
+               const uint32_t*, float4*);
 };
 
 namespace exact {
@@ -83,6 +83,8 @@ cudaError_t launch_gather_state(uint32_t n, const uint32_t* perm, const float4* 
 cudaError_t launch_rank_from_order(uint32_t n, const uint32_t* perm, const uint32_t* key, const uint32_t* cell_start,
                                    uint32_t* rank_out, cudaStream_t st);
 cudaError_t launch_scatter_by_id(uint32_t n, const uint32_t* id, const float4* src, float4* dst, cudaStream_t st);
+// dst[id[t]] = src[t].w (a scalar kept in the w lane of a packed float4 array)
+cudaError_t launch_scatter_w_by_id(uint32_t n, const uint32_t* id, const float4* src, float* dst, cudaStream_t st);
 cudaError_t launch_scatter_by_id_u32(uint32_t n, const uint32_t* id, const uint32_t* src, uint32_t* dst,
                                      cudaStream_t st);
 cudaError_t launch_scatter_by_id_f32(uint32_t n, const uint32_t* id, const float* src, float* dst, cudaStream_t st);

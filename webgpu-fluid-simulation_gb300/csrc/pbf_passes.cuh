@@ -85,11 +85,11 @@ __device__ __forceinline__ Run run_of(const GridParams& g, const uint32_t* __res
 }
 
 // NeighborCount: neighbours within h of x*, self included, 27 cells in key
-// order.  Also writes, per warp of 32 consecutive slots, 32 x the warp's
-// largest count: the slice length of the interleaved list layout.
+// order (stand-alone search; slot n receives 0 so a scan of n + 1 counts
+// ends in the total).
 __global__ void __launch_bounds__(256) k_nbr_count(SimParams p, GridParams g, const float4* __restrict__ xs,
                                                    const uint32_t* __restrict__ cell_start,
-                                                   uint32_t* __restrict__ nbr_count, uint32_t* __restrict__ warp_len) {
+                                                   uint32_t* __restrict__ nbr_count) {
   uint32_t t = blockIdx.x * blockDim.x + threadIdx.x;
   uint32_t cnt = 0;
   if (t < p.n) {
@@ -107,41 +107,47 @@ __global__ void __launch_bounds__(256) k_nbr_count(SimParams p, GridParams g, co
       }
   }
   if (t <= p.n) nbr_count[t] = cnt;
-  if (warp_len) {
-    uint32_t wmax = __reduce_max_sync(kFull, cnt);
-    uint32_t w = t >> 5;
-    if ((t & 31u) == 0 && w <= ((p.n + 31u) >> 5)) warp_len[w] = (t < p.n) ? 32u * wmax : 0u;
-  }
 }
 
-// Interleaved ("sliced") neighbour list of the step: the q-th neighbour of
-// slot t is at warp_off[t / 32] + 32 q + t % 32, so the q-th entries of a
-// warp's 32 particles are one contiguous 128-byte segment.  Same traversal
-// and order as NeighborList.
-__global__ void __launch_bounds__(256) k_nbr_list_sliced(SimParams p, GridParams g, const float4* __restrict__ xs,
-                                                         const uint32_t* __restrict__ cell_start,
-                                                         const uint32_t* __restrict__ warp_off,
-                                                         uint32_t* __restrict__ nbr_list, uint32_t capacity,
-                                                         uint32_t* err) {
+// NeighborCount + NeighborList of the step in one traversal.  The list is
+// interleaved by warp with a fixed slice of max_nbr entries per particle:
+// neighbour q of slot t is at (t / 32) * 32 * max_nbr + 32 q + t % 32, so the
+// q-th entries of a warp's 32 particles are one contiguous 128-byte segment,
+// and no count pass or scan is needed to place them.  nbr_count[t] receives
+// the true count; a count above max_nbr flags an overflow (the entries past
+// the slice are dropped and max_seen records the largest count for growing).
+__global__ void __launch_bounds__(256) k_nbr_build(SimParams p, GridParams g, const float4* __restrict__ xs,
+                                                   const uint32_t* __restrict__ cell_start, uint32_t max_nbr,
+                                                   uint32_t* __restrict__ nbr_list, uint32_t* __restrict__ nbr_count,
+                                                   uint32_t* max_seen, uint32_t* err) {
   uint32_t t = blockIdx.x * blockDim.x + threadIdx.x;
   if (t >= p.n) return;
-  if (t == 0 && warp_off[(p.n + 31) >> 5] > capacity) atomicOr(err, 0x1u);
   f3 xi = xyz(xs[t]);
   int cx = cell_axis(xi.x, g.origin[0], g.inv_cell[0], g.dim[0]);
   int cy = cell_axis(xi.y, g.origin[1], g.inv_cell[1], g.dim[1]);
   int cz = cell_axis(xi.z, g.origin[2], g.inv_cell[2], g.dim[2]);
-  uint32_t o = warp_off[t >> 5] + (t & 31u);
+  uint32_t* out = nbr_list + (size_t)(t >> 5) * 32u * max_nbr + (t & 31u);
+  uint32_t q = 0;
   for (int dx = -1; dx <= 1; ++dx)
     for (int dy = -1; dy <= 1; ++dy) {
       Run r = run_of(g, cell_start, cx, cy, cz, dx, dy);
       for (uint32_t u = r.b; u < r.e; ++u) {
         f3 d = xyz(__ldg(xs + u)) - xi;
         if (dot3(d, d) <= p.h2) {
-          if (o < capacity) nbr_list[o] = u;
-          o += 32;
+          if (q < max_nbr) out[32u * q] = u;
+          ++q;
         }
       }
     }
+  nbr_count[t] = q;
+  const unsigned m = __activemask();
+  if (__any_sync(m, q > max_nbr)) {
+    unsigned wmax = __reduce_max_sync(m, q);
+    if ((threadIdx.x & 31u) == (unsigned)(__ffs(m) - 1)) {
+      atomicMax(max_seen, wmax);
+      atomicOr(err, 0x1u);
+    }
+  }
 }
 
 // NeighborList: the same traversal writing slot indices at nbr_offset[t].
@@ -210,22 +216,17 @@ __device__ __forceinline__ bool boundary_possible(const FieldParams& f, const ui
   return __ldg(flag + ((size_t)c[2] * f.res[1] + c[1]) * f.res[0] + c[0]) != 0;
 }
 
-// Slice of slot t in the interleaved list, clamped to the list capacity (an
-// overflowed list has been flagged; the step's results are then invalid but
-// no access is out of bounds).
-__device__ __forceinline__ void list_slice(const uint32_t* __restrict__ warp_off, const uint32_t* __restrict__ cnt_of,
-                                           uint32_t t, uint32_t cap, uint32_t& base, uint32_t& cnt) {
-  base = __ldg(warp_off + (t >> 5)) + (t & 31u);
-  cnt = __ldg(cnt_of + t);
-  if (base >= cap)
-    cnt = 0;
-  else
-    cnt = min(cnt, (cap - base + 31u) >> 5);
+// Slice of slot t in the interleaved list (see k_nbr_build); a count past the
+// slice (an overflowed substep, already flagged) is clamped to it.
+__device__ __forceinline__ void list_slice(uint32_t max_nbr, const uint32_t* __restrict__ cnt_of, uint32_t t,
+                                           uint32_t& base, uint32_t& cnt) {
+  base = (t >> 5) * 32u * max_nbr + (t & 31u);
+  cnt = min(__ldg(cnt_of + t), max_nbr);
 }
 
 // BoundaryVolume (boundaryVolume.ts:26-57): (x_b, V_b) per particle, skipping
 // the 64-node interpolation where the field cell cannot produce a sample.
-__global__ void __launch_bounds__(256) k_boundary(SimParams p, FieldParams f, const float* __restrict__ sdf,
+__global__ void __launch_bounds__(256, 3) k_boundary(SimParams p, FieldParams f, const float* __restrict__ sdf,
                                                   const float* __restrict__ vol, const uint8_t* __restrict__ bflag,
                                                   const float4* __restrict__ xs, float4* __restrict__ bdata,
                                                   SolverAux a) {
@@ -245,7 +246,8 @@ __global__ void __launch_bounds__(256) k_boundary(SimParams p, FieldParams f, co
   if (a.bsdf) a.bsdf[t] = dist;
 }
 
-// LambdaCalculation (pressureConstrain.ts:31-85).
+// LambdaCalculation (pressureConstrain.ts:31-85).  Writes xl[t] = (x*, lambda):
+// the next pass gathers a neighbour's position and multiplier in one load.
 //   kMode 0: the reference pass.
 //   kMode 1: also writes the learned start's 8 features at x*_0 (density
 //            error, previous multiplier, neighbour count, |v'| dt/h, div(v') dt,
@@ -255,10 +257,10 @@ __global__ void __launch_bounds__(256) k_boundary(SimParams p, FieldParams f, co
 //            (32 particles = two 16-row mma tiles) and lambda_hat replaces lambda.
 template <int kMode>
 __global__ void __launch_bounds__(256) k_lambda(SimParams p, int have_field, const float4* __restrict__ bdata,
-                                                const float4* __restrict__ xs, const uint32_t* __restrict__ warp_off,
+                                                const float4* __restrict__ xs, uint32_t max_nbr,
                                                 const uint32_t* __restrict__ nbr_cnt,
-                                                const uint32_t* __restrict__ nbr_list, uint32_t cap,
-                                                float* __restrict__ lambda, SolverAux a) {
+                                                const uint32_t* __restrict__ nbr_list,
+                                                float4* __restrict__ xl, SolverAux a) {
   constexpr bool kFeat = kMode >= 1;
   if (a.guard && *a.guard == 0) return;
   uint32_t t = blockIdx.x * blockDim.x + threadIdx.x;
@@ -276,10 +278,11 @@ __global__ void __launch_bounds__(256) k_lambda(SimParams p, int have_field, con
     __syncthreads();
     const bool valid = t < p.n;
     float fv[8] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
+    f3 xi = mk(0.f, 0.f, 0.f);
     if (valid) {
-      f3 xi = xyz(xs[t]);
+      xi = xyz(xs[t]);
       uint32_t b, e;
-      list_slice(warp_off, nbr_cnt, t, cap, b, e);
+      list_slice(max_nbr, nbr_cnt, t, b, e);
       float dens = 0.0f, div = 0.0f;
       f3 vi = p.inv_dt * (xi - xyz(a.pos[t]));
       for_each_neighbor(nbr_list, b, e, xs, [&](uint32_t j, float4 xj) {
@@ -309,7 +312,6 @@ __global__ void __launch_bounds__(256) k_lambda(SimParams p, int have_field, con
 #pragma unroll
     for (int k = 0; k < 8; ++k) sF[warp][lane][k] = valid ? (fv[k] - a.norm.mean[k]) * a.norm.inv_std[k] : 0.0f;
     __syncwarp();
-    const uint32_t base = t - lane;
 #pragma unroll
     for (int tile = 0; tile < 2; ++tile) {
       const int r = 16 * tile + g;
@@ -317,26 +319,23 @@ __global__ void __launch_bounds__(256) k_lambda(SimParams p, int have_field, con
       float x8[2] = {sF[warp][r + 8][2 * t4], sF[warp][r + 8][2 * t4 + 1]};
       mlp::Fwd F;
       mlp::forward_tile(xg, x8, sW1t, sW2t, sB1, sB2, sW3, a.mlp[mlp::OFF_B3], F);
-      if (t4 == 0) {
-        uint32_t ra = base + r, rb = base + r + 8;
-        if (ra < p.n) {
-          float l = F.y0 * a.norm.lam_scale;
-          lambda[ra] = l;
-          a.lam_sum[ra] = l;
-        }
-        if (rb < p.n) {
-          float l = F.y8 * a.norm.lam_scale;
-          lambda[rb] = l;
-          a.lam_sum[rb] = l;
-        }
+      if (t4 == 0) {  // rows r and r + 8 of this warp: column 8 of sF is free
+        sF[warp][r][8] = F.y0 * a.norm.lam_scale;
+        sF[warp][r + 8][8] = F.y8 * a.norm.lam_scale;
       }
+    }
+    __syncwarp();
+    if (valid) {
+      float l = sF[warp][lane][8];
+      xl[t] = f4(xi, l);
+      a.lam_sum[t] = l;
     }
     return;
   } else {
     if (t >= p.n) return;
     f3 xi = xyz(xs[t]);
     uint32_t b, e;
-    list_slice(warp_off, nbr_cnt, t, cap, b, e);
+    list_slice(max_nbr, nbr_cnt, t, b, e);
     f3 grad = mk(0.f, 0.f, 0.f);
     float sum2 = 0.0f, dens = 0.0f, div = 0.0f;
     f3 vi = mk(0.f, 0.f, 0.f);
@@ -369,7 +368,7 @@ __global__ void __launch_bounds__(256) k_lambda(SimParams p, int have_field, con
     float c = fmaxf(0.0f, dens - 1.0f);
     float s = dot3(grad, grad) + sum2;
     float lam = fdiv(-c, s + p.lambda_eps);
-    lambda[t] = lam;
+    xl[t] = f4(xi, lam);
     if (a.lam_sum) a.lam_sum[t] = a.lam_first ? lam : a.lam_sum[t] + lam;
     if (kFeat) {
       float sd = a.bsdf ? fminf(a.bsdf[t], 2.0f * p.h) : 2.0f * p.h;
@@ -379,24 +378,25 @@ __global__ void __launch_bounds__(256) k_lambda(SimParams p, int have_field, con
   }
 }
 
-// ConstrainSolve + ConstrainApply: x*_new = clamp(x* + 0.5 * dp) into the other buffer.
-__global__ void __launch_bounds__(256) k_deltap(SimParams p, SolverAux a, int have_field, const float4* __restrict__ xs,
-                                                const float* __restrict__ lambda, const float4* __restrict__ bdata,
-                                                const uint32_t* __restrict__ warp_off, const uint32_t* __restrict__ nbr_cnt,
-                                                const uint32_t* __restrict__ nbr_list, uint32_t cap,
+// ConstrainSolve + ConstrainApply: x*_new = clamp(x* + 0.5 * dp) into the other
+// buffer; (x*_j, lambda_j) come packed from the lambda pass.
+__global__ void __launch_bounds__(256) k_deltap(SimParams p, SolverAux a, int have_field, const float4* __restrict__ xl,
+                                                const float4* __restrict__ bdata,
+                                                uint32_t max_nbr, const uint32_t* __restrict__ nbr_cnt,
+                                                const uint32_t* __restrict__ nbr_list,
                                                 float4* __restrict__ xs_out, float4* __restrict__ dp_out) {
   if (a.guard && *a.guard == 0) return;
   uint32_t t = blockIdx.x * blockDim.x + threadIdx.x;
   if (t >= p.n) return;
-  f3 xi = xyz(xs[t]);
-  float li = lambda[t];
+  const float4 xli = xl[t];
+  f3 xi = xyz(xli);
+  float li = xli.w;
   uint32_t b, e;
-  list_slice(warp_off, nbr_cnt, t, cap, b, e);
+  list_slice(max_nbr, nbr_cnt, t, b, e);
   f3 pu = mk(0.f, 0.f, 0.f);
-  for_each_neighbor(nbr_list, b, e, xs, [&](uint32_t j, float4 xj) {
+  for_each_neighbor(nbr_list, b, e, xl, [&](uint32_t, float4 xj) {
     Pair q = make_pair_of(xi - xyz(xj));
-    float lj = __ldg(lambda + j);
-    pu = pu + (li + lj) * spiky_p(p, q);
+    pu = pu + (li + xj.w) * spiky_p(p, q);
   });
   pu = p.V * pu;
   if (have_field) {
@@ -413,16 +413,16 @@ __global__ void __launch_bounds__(256) k_deltap(SimParams p, SolverAux a, int ha
 
 // AttributeUpdate: rho = m * sum W (fluid only), v = (x* - x) / dt, x <- (x*, rho).
 __global__ void __launch_bounds__(256) k_density_velocity(SimParams p, SolverAux a, const float4* __restrict__ xs,
-                                                          const uint32_t* __restrict__ warp_off,
+                                                          uint32_t max_nbr,
                                                           const uint32_t* __restrict__ nbr_cnt,
-                                                          const uint32_t* __restrict__ nbr_list, uint32_t cap,
+                                                          const uint32_t* __restrict__ nbr_list,
                                                           float4* __restrict__ pos, float4* __restrict__ vel) {
   if (a.guard && *a.guard == 0) return;
   uint32_t t = blockIdx.x * blockDim.x + threadIdx.x;
   if (t >= p.n) return;
   f3 xi = xyz(xs[t]);
   uint32_t b, e;
-  list_slice(warp_off, nbr_cnt, t, cap, b, e);
+  list_slice(max_nbr, nbr_cnt, t, b, e);
   float dens = 0.0f;
   for_each_neighbor(nbr_list, b, e, xs, [&](uint32_t, float4 xj) {
     Pair q = make_pair_of(xi - xyz(xj));
@@ -452,16 +452,16 @@ __global__ void __launch_bounds__(256) k_density_velocity(SimParams p, SolverAux
 // VorticityConfinement: omega_i and the Akinci normal n_i.
 __global__ void __launch_bounds__(256) k_vorticity(SimParams p, const float4* __restrict__ pos,
                                                    const float4* __restrict__ vel,
-                                                   const uint32_t* __restrict__ warp_off,
+                                                   uint32_t max_nbr,
                                                    const uint32_t* __restrict__ nbr_cnt,
-                                                   const uint32_t* __restrict__ nbr_list, uint32_t cap,
+                                                   const uint32_t* __restrict__ nbr_list,
                                                    float4* __restrict__ omega, float4* __restrict__ normal) {
   uint32_t t = blockIdx.x * blockDim.x + threadIdx.x;
   if (t >= p.n) return;
   f3 xi = xyz(pos[t]);
   f3 vi = xyz(vel[t]);
   uint32_t b, e;
-  list_slice(warp_off, nbr_cnt, t, cap, b, e);
+  list_slice(max_nbr, nbr_cnt, t, b, e);
   f3 om = mk(0.f, 0.f, 0.f), nm = mk(0.f, 0.f, 0.f);
   for_each_neighbor(nbr_list, b, e, pos, [&](uint32_t j, float4 pj) {
     Pair q = make_pair_of(xi - xyz(pj));
@@ -471,17 +471,18 @@ __global__ void __launch_bounds__(256) k_vorticity(SimParams p, const float4* __
     om = om + volume * cross3(vd, gw);
     nm = nm + volume * gw;
   });
-  omega[t] = f4(om, len3(om));
-  normal[t] = f4(p.h * nm, 0.0f);
+  const float wl = len3(om);
+  omega[t] = f4(om, wl);
+  normal[t] = f4(p.h * nm, wl);  // w: |omega| again, so XSPH gathers one float4 per neighbour fewer
 }
 
 // XSPH viscosity + vorticity confinement force + Akinci surface tension -> a.
-__global__ void __launch_bounds__(256) k_xsph(SimParams p, const float4* __restrict__ pos,
+__global__ void __launch_bounds__(256, 4) k_xsph(SimParams p, const float4* __restrict__ pos,
                                               const float4* __restrict__ vel, const float4* __restrict__ omega,
                                               const float4* __restrict__ normal,
-                                              const uint32_t* __restrict__ warp_off,
+                                              uint32_t max_nbr,
                                               const uint32_t* __restrict__ nbr_cnt,
-                                              const uint32_t* __restrict__ nbr_list, uint32_t cap,
+                                              const uint32_t* __restrict__ nbr_list,
                                               float4* __restrict__ acc) {
   uint32_t t = blockIdx.x * blockDim.x + threadIdx.x;
   if (t >= p.n) return;
@@ -492,7 +493,7 @@ __global__ void __launch_bounds__(256) k_xsph(SimParams p, const float4* __restr
   f3 wi = xyz(omega[t]);
   f3 ni = xyz(normal[t]);
   uint32_t b, e;
-  list_slice(warp_off, nbr_cnt, t, cap, b, e);
+  list_slice(max_nbr, nbr_cnt, t, b, e);
   f3 vu = mk(0.f, 0.f, 0.f), eta = mk(0.f, 0.f, 0.f), ten = mk(0.f, 0.f, 0.f);
   for_each_neighbor(nbr_list, b, e, pos, [&](uint32_t j, float4 pj) {
     float rj = pj.w;
@@ -500,9 +501,10 @@ __global__ void __launch_bounds__(256) k_xsph(SimParams p, const float4* __restr
     f3 vd = xyz(__ldg(vel + j)) - vi;
     float kij = fdiv(p.two_rho0, ri + rj);
     vu = vu + fdiv3(poly6_p(p, q) * vd, rj);
-    eta = eta + fdiv3(__ldg(&omega[j].w) * spiky_p(p, q), rj);
+    const float4 nj = __ldg(normal + j);  // (normal_j, |omega_j|)
+    eta = eta + fdiv3(nj.w * spiky_p(p, q), rj);
     f3 coh = p.m * cohesion_p(p, q);
-    f3 curv = ni - xyz(__ldg(normal + j));
+    f3 curv = ni - xyz(nj);
     ten = ten - kij * (coh + curv);
   });
   float el = len3(eta);
@@ -517,7 +519,7 @@ void fill_pass_table(PassTable* tbl) {
   tbl->predict = k_predict;
   tbl->nbr_count = k_nbr_count;
   tbl->nbr_list = k_nbr_list;
-  tbl->nbr_list_sliced = k_nbr_list_sliced;
+  tbl->nbr_build = k_nbr_build;
   tbl->boundary = k_boundary;
   tbl->lambda = k_lambda<0>;
   tbl->lambda_feat = k_lambda<1>;

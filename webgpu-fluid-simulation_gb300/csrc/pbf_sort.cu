@@ -343,6 +343,12 @@ __global__ void k_scatter_f4(uint32_t n, const uint32_t* __restrict__ id, const 
   if (t >= n) return;
   dst[id[t]] = src[t];
 }
+__global__ void k_scatter_w(uint32_t n, const uint32_t* __restrict__ id, const float4* __restrict__ src,
+                            float* __restrict__ dst) {
+  uint32_t t = blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= n) return;
+  dst[id[t]] = src[t].w;
+}
 __global__ void k_scatter_u32(uint32_t n, const uint32_t* __restrict__ id, const uint32_t* __restrict__ src,
                               uint32_t* __restrict__ dst) {
   uint32_t t = blockIdx.x * blockDim.x + threadIdx.x;
@@ -507,6 +513,11 @@ cudaError_t launch_rank_from_order(uint32_t n, const uint32_t* perm, const uint3
 cudaError_t launch_scatter_by_id(uint32_t n, const uint32_t* id, const float4* src, float4* dst, cudaStream_t st) {
   if (n == 0) return cudaSuccess;
   k_scatter_f4<<<blocks_for(n, 256), 256, 0, st>>>(n, id, src, dst);
+  return cudaGetLastError();
+}
+cudaError_t launch_scatter_w_by_id(uint32_t n, const uint32_t* id, const float4* src, float* dst, cudaStream_t st) {
+  if (n == 0) return cudaSuccess;
+  k_scatter_w<<<blocks_for(n, 256), 256, 0, st>>>(n, id, src, dst);
   return cudaGetLastError();
 }
 cudaError_t launch_scatter_by_id_u32(uint32_t n, const uint32_t* id, const uint32_t* src, uint32_t* dst,

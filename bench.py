@@ -76,12 +76,16 @@ def parse_args():
     ap.add_argument("--steps", type=int, default=20)
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
-    ap.add_argument("--workload", default="sphere_drop_1m", choices=["sphere_drop_1m", "dam_break_16k"])
+    ap.add_argument("--workload", default="sphere_drop_1m", choices=["sphere_drop_1m", "dam_break_16k", "batch64"],
+                    help="batch64: 64 independent scenes in one batch handle (its own JSON line; the scenes are "
+                         "split over the ranks)")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--graph", action="store_true", help="replay the frame as a CUDA graph")
     ap.add_argument("--settle", type=int, default=150,
                     help="frames advanced from the initial lattice to build the input state (untimed set-up)")
     ap.add_argument("--no-learned", action="store_true", help="skip the learned warm-start measurement")
+    ap.add_argument("--no-tune", action="store_true",
+                    help="keep the default launch shape instead of the autotuner's choice")
     ap.add_argument("--bound", type=float, default=None,
                     help="learned start: fall back to the plain solve when the in-solve mean compression exceeds "
                          "this (default: the largest per-substep value the plain 4-iteration solve showed while "
@@ -255,10 +259,31 @@ def cpu_sample(sc, particles_max, substeps, min_seconds=10.0):
     return len(pts) * done / dt, dt, len(pts), O.threads(), done
 
 
+def _batch_reference_scene():
+    """The smallest scene of the batch64 workload as a single Scene (the CPU
+    restatement's sample for that workload)."""
+    from pbf_gb300 import scenes
+    cfg, sc_all, fa_all = scenes.batch_scenes_spec()
+    i = min(range(len(sc_all)), key=lambda k: sc_all[k]["positions"].shape[0])
+    c = scenes.copy_config(cfg)
+    c.max_particles = sc_all[i]["positions"].shape[0]
+    c.domain_min[:] = list(sc_all[i]["domain_min"])
+    c.domain_max[:] = list(sc_all[i]["domain_max"])
+    c.options.iterations = sc_all[i]["iterations"]
+    fa = fa_all[i]
+    field = scenes.generate_field(fa["shapes"], fa["res"], fa["origin"], fa["extent"], fa["h"], quadrature=8,
+                                  backend=_cpu_field_backend())
+    desc = "batch64 (CPU sample: its smallest scene, %d particles)" % c.max_particles
+    return scenes.Scene("batch64_smallest", c, sc_all[i]["positions"], field, frames=1), desc
+
+
 def reference_arm(args, dist):
     if dist.rank != 0:
         return
-    sc, desc = build_workload(args.workload, field_backend=_cpu_field_backend())
+    if args.workload == "batch64":
+        sc, desc = _batch_reference_scene()
+    else:
+        sc, desc = build_workload(args.workload, field_backend=_cpu_field_backend())
     sub = sc.config.substeps
     sample = min(sc.n, 262144)
     # warm-up (untimed) and timed steps, each one frame of the sample
@@ -274,7 +299,7 @@ def reference_arm(args, dist):
     value = sample * sub * args.steps / dt
     cores = O.threads()
     line = {
-        "impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus,
+        "impl": "reference", "metric": BATCH_METRIC if args.workload == "batch64" else METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1000.0 * dt / args.steps,
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
         "config": {"workload": desc, "sample": "first %d particles of the lattice" % sample},
@@ -332,6 +357,12 @@ def gpu_arm(args, dist):
         train_info = {"rows": int(len(tgt)), "epochs": 10, "batch": 8192, "final_mse_normalised": loss,
                       "seconds": time.perf_counter() - t0, "traced_frames": args.settle - trace_from,
                       "plain_mean_compression_while_tracing": {"max": plain_err_max, "avg": plain_err_avg}}
+    global _LAUNCH
+    tune = None
+    if not args.no_tune:
+        best, trials = sim.autotune(substeps=4, cell_ratio=True)
+        _LAUNCH = best
+        tune = {"launch": best, "trials": trials}
     snap = (sim.positions(), sim.velocities())
     for _ in range(max(args.warmup, 3)):
         sim.step(1)
@@ -404,12 +435,13 @@ def gpu_arm(args, dist):
         "warmup": max(args.warmup, 3), "ms_per_step": ms_max / args.steps, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
         "config": {"workload": desc, "path": "plain 4-iteration solve",
+                   "launch": _LAUNCH if _LAUNCH else "default (256 threads, one tile per CTA, cell = h)",
                    "input_state": "frame %d of the run (after the impact); %d warm-up frames" % (args.settle,
                                                                                              max(args.warmup, 3)),
                    "graph": bool(args.graph), "parallelism": "replicas x%d" % dist.world,
                    "l2": "state + neighbour lists ~0.4 GB per replica, larger than the 129 MB L2"},
         "e2e": e2e, "gpu_launches": launches_per_frame * args.steps,
-        "roofline": roof, "clocks": clk,
+        "roofline": roof, "clocks": clk, "tuner": tune,
         "state_metrics": {"max_compression": m["max_compression"], "mean_abs_density_err": m["mean_abs_density_err"],
                           "nonfinite": m["nonfinite"], "neighbors_per_particle": m["neighbor_total"] / max(n, 1)},
     }
@@ -425,12 +457,17 @@ def gpu_arm(args, dist):
         print(json.dumps(line), flush=True)
 
 
+_LAUNCH = None  # the autotuner's launch shape, applied to every handle of the run
+
+
 def _handle_from(sc, snap, iterations=None):
     from pbf_gb300 import PBF, scenes
     c = scenes.copy_config(sc.config)
     if iterations is not None:
         c.options.iterations = iterations
     sim = PBF(c)
+    if _LAUNCH:
+        sim.set_launch(**_LAUNCH)
     sim.set_particles(snap[0])
     sim.set_velocities(snap[1])
     f = sc.field
@@ -511,12 +548,120 @@ def learned_arm(args, sc, snap, model, train_info, dist, plain_value):
     return out
 
 
+BATCH_METRIC = "particle-substeps/s, 64 batched PBF scenes (4,096-262,144 particles each)"
+
+
+def batch_arm(args, dist):
+    """64 independent scenes (particle counts log-uniform in [4096, 262144],
+    box / box+sphere / box+cylinder maps at 64^3, 3 or 4 iterations): each
+    rank steps its share of the scenes (greedy partition by particle count)
+    in one batch handle, one launch per pass, launch shape from the
+    autotuner, each frame replayed as a CUDA graph."""
+    import torch
+    from pbf_gb300 import PBFBatch, scenes
+    from pbf_gb300.batch import gather_scene_results, imbalance, partition_scenes
+    from pbf_gb300 import _lib as L
+
+    torch.cuda.set_device(dist.local if dist.world > 1 else 0)
+    cfg, sc_all, fa_all = scenes.batch_scenes_spec()
+    counts = [s["positions"].shape[0] for s in sc_all]
+    parts = partition_scenes(counts, dist.world)
+    mine = parts[dist.rank]
+    cfg, sc = scenes.build_batch((cfg, [sc_all[i] for i in mine], [fa_all[i] for i in mine]), quadrature=8)
+    b = PBFBatch(cfg, sc)
+    n = sum(counts[i] for i in mine)
+    sub = cfg.substeps
+    b.step(args.settle // 3)  # the columns collapse (untimed)
+    best, trials = b.autotune(substeps=4, cell_ratio=True)
+    # eager frames with per-pass events: pass shares
+    b.set_kernel_timing(True)
+    b.kernel_timing()
+    b.step(max(args.warmup, 3))
+    kt = b.kernel_timing()
+    b.set_kernel_timing(False)
+    b.enable_graph(True)
+    for _ in range(max(args.warmup, 3)):
+        b.step(1)
+    b.synchronize()
+    stream = torch.cuda.ExternalStream(b.stream)
+    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    clocks = ClockSampler(dist.local)
+    clocks.start()
+    dist.barrier()
+    torch.cuda.synchronize()
+    ev0.record(stream)
+    for _ in range(args.steps):
+        b.step(1)
+    ev1.record(stream)
+    ev1.synchronize()
+    torch.cuda.synchronize()
+    dist.barrier()
+    clk = clocks.stop()
+    ms_max = dist.max(ev0.elapsed_time(ev1))
+    total = sum(counts)
+    value = total * sub * args.steps / (ms_max / 1000.0)
+    # end to end: options in, every scene's positions out each frame (pinned)
+    host_t = torch.empty((n, 4), dtype=torch.float32, pin_memory=True)
+    host = host_t.numpy()
+    lib = L.load()
+    opts = L.Options()
+    lib.pbf_get_options(b._h, ctypes.byref(opts))
+    b.synchronize()
+    dist.barrier()
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        lib.pbf_set_options(b._h, ctypes.byref(opts))
+        b.step(1)
+        lib.pbf_copy_field(b._h, L.FIELD_POSITION, host.ctypes.data_as(ctypes.c_void_p), host.nbytes)
+    e2e_s = dist.max(time.perf_counter() - t0)
+    per_scene = {mine[s]: b.scene_metrics(s) for s in range(len(mine))}
+    merged = gather_scene_results(per_scene, dist.pg)
+    b.close()
+    peak, peak_kind = peaks()
+    roof = None
+    if kt:
+        name, (launches, tot_ms) = max(kt.items(), key=lambda kv: kv[1][1])
+        per_launch_s = tot_ms / launches / 1000.0
+        achieved = ALG_BYTES.get(name, 0) * n / per_launch_s / 1e9
+        total_ms = sum(v[1] for v in kt.values())
+        roof = {"bound": "hbm", "kernel": name, "achieved": achieved, "peak": peak, "unit": "GB/s",
+                "frac": achieved / peak, "peak_kind": peak_kind, "traffic": None,
+                "alg_bytes_per_launch": ALG_BYTES.get(name, 0) * n, "avg_launch_ms": per_launch_s * 1000.0,
+                "share": tot_ms / total_ms if total_ms else None,
+                "passes": {k: {"launches": v[0], "ms": round(v[1], 4)} for k, v in kt.items()}}
+    iters_max = max(s["iterations"] for s in sc_all)
+    line = {
+        "metric": BATCH_METRIC, "value": value, "unit": UNIT, "n_gpus": dist.world, "steps": args.steps,
+        "warmup": max(args.warmup, 3), "ms_per_step": ms_max / args.steps, "higher_is_better": True,
+        "scaling": "strong", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+        "config": {"workload": "batch64: 64 scenes, %d particles in total, log-uniform 4,096-262,144 per scene, "
+                               "box / box+sphere / box+cylinder 64^3 volume maps, 3 or 4 iterations, 2 substeps "
+                               "x 1/300 s, r=0.0125, h=0.05" % total,
+                   "parallelism": "scenes split over %d rank(s), load imbalance %.3f" % (
+                       dist.world, imbalance(counts, parts)),
+                   "launch": best, "graph": True, "input_state": "frame %d of the run" % (args.settle // 3),
+                   "l2": "state + lists of 3.7M particles ~1.4 GB, larger than the 129 MB L2"},
+        "tuner_trials": trials,
+        "e2e": {"value": total * sub * args.steps / e2e_s, "unit": UNIT,
+                "h2d_bytes_per_step": ctypes.sizeof(L.Options), "d2h_bytes_per_step": int(host.nbytes)},
+        "gpu_launches": (sub * (10 + 3 * iters_max) + 1) * args.steps,
+        "roofline": roof, "clocks": clk,
+        "scene_metrics": {"scenes": len(merged), "nonfinite": sum(m["nonfinite"] for m in merged.values()),
+                          "penetrations": sum(m["penetrations"] for m in merged.values()),
+                          "max_compression": max(m["max_compression"] for m in merged.values())},
+    }
+    if dist.rank == 0:
+        print(json.dumps(line), flush=True)
+
+
 def main():
     args = parse_args()
     dist = Dist(args.gpus)
     try:
         if args.impl == "reference":
             reference_arm(args, dist)
+        elif args.workload == "batch64":
+            batch_arm(args, dist)
         else:
             gpu_arm(args, dist)
     finally:

@@ -356,6 +356,76 @@ int pbf_set_learned(pbf_handle* h, const pbf_mlp* model, uint32_t iterations, fl
 #define PBF_SCAN_NOALLOC_MAX (1u << 26)
 int pbf_exclusive_scan_u32_noalloc(const uint32_t* d_in, uint32_t* d_out, size_t n, void* stream);
 
+/* ---- launch shape and autotuner.  No counterpart in the reference (its
+ * passes use a fixed workgroup size of 256).  The step's passes are
+ * grid-stride loops over tiles of `block` slots: ctas_per_sm = 0 launches one
+ * tile per CTA; k > 0 launches at most k CTAs per SM that loop over the
+ * tiles.  cell_ratio is the hash-grid cell edge over the kernel radius: 1 is
+ * the reference's grid (27-cell search, neighbour order and results as the
+ * reference); 0.5 uses h/2 cells and a 125-cell search (the same neighbour
+ * sets, summed in a different order, so results differ in rounding). */
+typedef struct pbf_launch {
+  uint32_t block;        /* threads per CTA: 128 or 256 (default 256) */
+  uint32_t ctas_per_sm;  /* 0 (default) or 1..16 */
+  float cell_ratio;      /* 1 (default) or 0.5 */
+} pbf_launch;
+int pbf_set_launch(pbf_handle* h, const pbf_launch* launch);
+int pbf_get_launch(const pbf_handle* h, pbf_launch* launch);
+
+typedef struct pbf_tune_trial {
+  pbf_launch launch;
+  float ms_per_substep;
+} pbf_tune_trial;
+#define PBF_TUNE_CELL_RATIO 0x1u /* also try cell_ratio 0.5 */
+/* Times `substeps` substeps (after 2 warm-up substeps) for every candidate
+ * launch shape — block {128, 256} x ctas_per_sm {0, 1024/block, 2048/block}
+ * (x cell_ratio {1, 0.5} with PBF_TUNE_CELL_RATIO) — on the current state,
+ * restores the state (positions, velocities, accelerations, ids), keeps the fastest
+ * shape (also returned in *best).  trials (up to max_trials) receive every
+ * candidate's time.  PBF_ESTATE while trace capture is on. */
+int pbf_autotune(pbf_handle* h, uint32_t substeps, uint32_t flags, pbf_tune_trial* trials, uint32_t max_trials,
+                 uint32_t* count, pbf_launch* best);
+
+/* ---- batched scenes.  The reference runs one scene per simulator; a batch
+ * runs many independent scenes of uneven sizes, each with its own domain,
+ * volume map and iteration count, in ONE launch per pass: the scenes share
+ * the particle arrays (scene s holds ids and slots [first_id, first_id + n))
+ * and one cell-key space (scene s's grid keys follow scene s-1's), so one
+ * counting sort orders them all, and the passes look up each slot's scene in
+ * a device table.  The shared pbf_config gives the particle/kernel radius,
+ * density, time step, substeps, options (the default iteration count),
+ * jitter, fp mode, interpolation and list slice; its domain, grid_dim and
+ * max_particles are ignored.  Each scene's grid has floor(extent / (ratio h))
+ * cells per axis (cells no smaller than ratio x h).  The returned handle
+ * works with pbf_step / pbf_run / pbf_enable_graph (one graph per substep
+ * group) / pbf_set_launch / pbf_autotune / pbf_copy_field (all scenes, by
+ * global id) / pbf_get_metrics (all scenes); the single-scene setup calls
+ * (particles, boundary, reset, learned start, trace) return PBF_ESTATE.  In
+ * PBF_FP_EXACT mode a scene's results are bit-identical to the same scene
+ * run alone with the same grid. */
+typedef struct pbf_scene {
+  uint32_t struct_size;    /* sizeof(pbf_scene) */
+  uint32_t particles;
+  const float* positions;  /* host float4 [particles]: x, y, z, (ignored) */
+  float domain_min[3], domain_max[3];
+  uint32_t iterations;     /* solver iterations; 0 = the shared options' count */
+  uint32_t field_res[3];   /* volume-map cells per axis; 0,0,0 = no map */
+  float field_origin[3], field_extent[3];
+  const float* sdf;        /* pbf_field_length(field_res) nodes each, .cdm layout */
+  const float* volume;
+} pbf_scene;
+typedef struct pbf_scene_info {
+  uint32_t first_id;
+  uint32_t particles;
+  uint32_t iterations;
+  uint32_t grid_dim[3];
+  uint32_t cells;
+} pbf_scene_info;
+int pbf_batch_create(const pbf_config* shared, const pbf_scene* scenes, uint32_t count, pbf_handle** out);
+uint32_t pbf_scene_count(const pbf_handle* h); /* 1 for a single-scene handle */
+int pbf_get_scene_info(const pbf_handle* h, uint32_t scene, pbf_scene_info* out);
+int pbf_get_scene_metrics(pbf_handle* h, uint32_t scene, pbf_metrics* out);
+
 #ifdef __cplusplus
 }
 #endif

@@ -92,6 +92,19 @@ struct pbf_handle {
   uint32_t substep_counter = 0;
   DBuf<float> trace_feat, trace_tgt, trace_err;  // trace_err: [max, sum, count] of the plain solve's error
   DBuf<uint32_t> trace_count;
+  // launch shape of the step's passes (pbf_set_launch / pbf_autotune)
+  int blk = 256;            // threads per CTA
+  uint32_t grid_cap = 0;    // CTAs per launch at most (0: one tile of blk slots per CTA)
+  uint32_t per_sm = 0;      // grid_cap / SM count as set by the caller
+  float cell_ratio = 1.0f;  // grid cell edge / h
+  int sms = 152;            // SM count of the device
+  // batched scenes (pbf_batch_create)
+  bool batch = false;
+  std::vector<pbf_scene_info> scene_info;
+  std::vector<SceneDesc> scenes;
+  DBuf<SceneDesc> scenes_dev;
+  DBuf<uint16_t> slot_scene;
+  SceneTab tab{nullptr, nullptr};
   // per-kernel timing (pbf_set_kernel_timing)
   bool ktiming = false;
   std::vector<cudaEvent_t> kt_events;
@@ -150,6 +163,38 @@ int fail(pbf_handle* h, int code, const char* fmt, ...) {
     if (e_ != cudaSuccess) return fail((h), PBF_ECUDA, "%s: %s", #call, cudaGetErrorString(e_)); \
   } while (0)
 
+// Hash grid over [dmin, dmax].  Cell ratio 1 keeps the reference's grid: the
+// given dims, else ceil(extent / h) cells per axis, searched over 27 cells.
+// Other ratios (and every batched scene: floor_dims) use floor(extent /
+// (ratio h)) cells, so no cell is smaller than ratio h and a search of
+// +-ceil(1/ratio) cells covers the kernel radius.
+GridParams make_grid(const float dmin[3], const float dmax[3], float hk, float ratio, const uint32_t fixed_dim[3],
+                     bool floor_dims) {
+  GridParams g{};
+  uint64_t cells = 1;
+  const bool ref = ratio == 1.0f && !floor_dims;
+  for (int a = 0; a < 3; ++a) {
+    double ext = (double)dmax[a] - (double)dmin[a];
+    int d = fixed_dim ? (int)fixed_dim[a] : 0;
+    if (d == 0) {
+      if (ref) {
+        d = (int)std::ceil(ext / (double)hk);
+      } else {
+        d = (int)std::floor(ext / ((double)ratio * (double)hk));
+        if (d < 1) d = 1;
+      }
+    }
+    g.dim[a] = d;
+    g.origin[a] = dmin[a];
+    g.inv_cell[a] = (float)((double)d / ext);
+    cells *= (uint64_t)d;
+  }
+  g.cells = cells > 0xfffffffeull ? 0u : (uint32_t)cells;
+  g.key_base = 0;
+  g.reach = ratio == 1.0f ? 1 : (int)std::ceil(1.0 / (double)ratio - 1e-9);
+  return g;
+}
+
 void derive_params(pbf_handle* h) {
   const pbf_config& c = h->cfg;
   const double PI = 3.14159265358979323846;
@@ -185,18 +230,21 @@ void derive_params(pbf_handle* h) {
   p.tension = c.options.surface_tension;
   p.n = h->n;
 
-  GridParams& g = h->gp;
-  uint64_t cells = 1;
+  h->gp = make_grid(c.domain_min, c.domain_max, c.kernel_radius, h->cell_ratio, c.grid_dim, false);
+}
+
+FieldParams make_field(const pbf_config& c, const uint32_t res[3], const float origin[3], const float extent[3]) {
+  FieldParams f{};
   for (int a = 0; a < 3; ++a) {
-    double ext = (double)c.domain_max[a] - (double)c.domain_min[a];
-    int d = (int)c.grid_dim[a];
-    if (d == 0) d = (int)std::ceil(ext / hh);
-    g.dim[a] = d;
-    g.origin[a] = c.domain_min[a];
-    g.inv_cell[a] = (float)((double)d / ext);
-    cells *= (uint64_t)d;
+    f.res[a] = (int)res[a];
+    f.origin[a] = origin[a];
+    f.scale[a] = (float)((double)res[a] / (double)extent[a]);
+    f.gscale[a] = (float)(2.0 * (double)res[a] / (double)extent[a]);
   }
-  g.cells = (uint32_t)cells;
+  f.quirk = c.volume_quirk ? 1 : 0;
+  f.trilinear = c.boundary_interp == PBF_INTERP_TRILINEAR ? 1 : 0;
+  f.loaded = 1;
+  return f;
 }
 
 void set_field_params(pbf_handle* h, const uint32_t res[3], const float origin[3], const float extent[3]) {
@@ -212,6 +260,14 @@ void set_field_params(pbf_handle* h, const uint32_t res[3], const float origin[3
 }
 
 inline unsigned nblocks(uint32_t n, int t) { return (n + t - 1) / t; }
+
+// Grid of a step pass over n slots: one tile of blk slots per CTA, capped
+// at grid_cap CTAs (the kernels loop over the remaining tiles).
+inline unsigned grid_of(const pbf_handle* h, uint32_t n) {
+  unsigned g = nblocks(n, h->blk);
+  if (h->grid_cap && g > h->grid_cap) g = h->grid_cap;
+  return g ? g : 1u;
+}
 
 void invalidate_graph(pbf_handle* h) {
   if (h->graph_exec) cudaGraphExecDestroy(h->graph_exec);
@@ -265,13 +321,14 @@ int substep(pbf_handle* h, cudaEvent_t* ev) {
   p.n = n;
   const GridParams g = h->gp;
   const int c = h->cur, nx = 1 - c;
+  const PassSet& ps = h->passes.set[h->batch ? 1 : 0][h->grid_cap ? 1 : 0];
   if (ev) CU(h, cudaEventRecord(ev[0], st));
   // neighborSearch.clearBuffer + TimeIntegration (+ ParticleInsert counts)
   CU(h, cudaMemsetAsync(h->cell_count.p, 0, ((size_t)g.cells + 1) * sizeof(uint32_t), st));
   {
   KScope ks(h, K_PREDICT);
-  h->passes.predict<<<nblocks(n, 256), 256, 0, st>>>(p, g, h->pos[c].p, h->vel.p, h->acc.p, h->xs[1].p, h->key.p,
-                                                      h->rank.p, h->cell_count.p);
+  ps.predict<<<grid_of(h, n), h->blk, 0, st>>>(p, g, h->tab, h->pos[c].p, h->vel.p, h->acc.p, h->xs[1].p,
+                                                       h->key.p, h->rank.p, h->cell_count.p);
   }
   CU(h, cudaGetLastError());
   if (ev) CU(h, cudaEventRecord(ev[1], st));
@@ -295,8 +352,8 @@ int substep(pbf_handle* h, cudaEvent_t* ev) {
   // NeighborCount + NeighborList in one pass (fixed per-particle slices: no scan)
   {
     KScope ks(h, K_NBR_BUILD);
-    h->passes.nbr_build<<<nblocks(n, 256), 256, 0, st>>>(p, g, h->xs[0].p, h->cell_start.p, h->nbr_slice,
-                                                          h->nbr_list.p, h->nbr_count.p, h->nbr_max.p, h->err_word.p);
+    ps.nbr_build<<<grid_of(h, n), h->blk, 0, st>>>(p, g, h->tab, h->xs[0].p, h->cell_start.p, h->nbr_slice,
+                                                           h->nbr_list.p, h->nbr_count.p, h->nbr_max.p, h->err_word.p);
   }
   CU(h, cudaGetLastError());
   if (ev) CU(h, cudaEventRecord(ev[2], st));
@@ -313,15 +370,20 @@ int substep(pbf_handle* h, cudaEvent_t* ev) {
     for (uint32_t it = 0; it < iters; ++it) {
       SolverAux ab{};
       ab.guard = guard;
+      ab.tab = h->tab;
+      ab.iter = (int)it;
       if (need_feat && feat_first && it == 0) ab.bsdf = h->bsdf.p;
       if (f.loaded) {
         KScope ks(h, K_BOUNDARY);
-        h->passes.boundary<<<nblocks(n, 256), 256, 0, st>>>(p, f, h->sdf.p, h->vol.p, h->bflag.p, h->xs[a].p,
+        ps.boundary<<<grid_of(h, n), h->blk, 0, st>>>(
+            p, f, h->sdf.p, h->vol.p, h->bflag.p, h->xs[a].p,
                                                              h->bdata.p, ab);
       }
       if (cudaGetLastError() != cudaSuccess) { *rc = PBF_ECUDA; return a; }
       SolverAux al{};
       al.guard = guard;
+      al.tab = h->tab;
+      al.iter = (int)it;
       if (lam_sum_on) {
         al.lam_sum = h->lam_sum.p;
         al.lam_first = (first_starts_sum && it == 0) ? 1 : 0;
@@ -337,16 +399,20 @@ int substep(pbf_handle* h, cudaEvent_t* ev) {
       }
       {
         KScope ks(h, K_LAMBDA);
-        auto kl = fe ? h->passes.lambda_feat : h->passes.lambda;
-        kl<<<nblocks(n, 256), 256, 0, st>>>(p, f.loaded, h->bdata.p, h->xs[a].p, ms, h->nbr_count.p,
+        auto kl = fe ? ps.lambda_feat : ps.lambda;
+        kl<<<grid_of(h, n), h->blk, 0, st>>>(p, f.loaded, h->bdata.p, h->xs[a].p, ms, h->nbr_count.p,
                                              h->nbr_list.p, h->xl.p, al);
       }
       if (cudaGetLastError() != cudaSuccess) { *rc = PBF_ECUDA; return a; }
       SolverAux ad{};
       ad.guard = guard;
+      ad.tab = h->tab;
+      ad.iter = (int)it;
+      ad.xs_in = h->xs[a].p;
       {
         KScope ks(h, K_DELTAP);
-        h->passes.deltap<<<nblocks(n, 256), 256, 0, st>>>(p, ad, f.loaded, h->xl.p, h->bdata.p,
+        ps.deltap<<<grid_of(h, n), h->blk, 0, st>>>(
+            p, ad, f.loaded, h->xl.p, h->bdata.p,
                                                            ms, h->nbr_count.p, h->nbr_list.p,
                                                            h->xs[1 - a].p, h->capture ? h->dp.p : nullptr);
       }
@@ -365,7 +431,7 @@ int substep(pbf_handle* h, cudaEvent_t* ev) {
     ab.bsdf = h->bsdf.p;
     if (f.loaded) {
       KScope ks(h, K_BOUNDARY);
-      h->passes.boundary<<<nblocks(n, 256), 256, 0, st>>>(p, f, h->sdf.p, h->vol.p, h->bflag.p, h->xs[0].p,
+      ps.boundary<<<grid_of(h, n), h->blk, 0, st>>>(p, f, h->sdf.p, h->vol.p, h->bflag.p, h->xs[0].p,
                                                            h->bdata.p, ab);
     }
     CU(h, cudaGetLastError());
@@ -383,7 +449,7 @@ int substep(pbf_handle* h, cudaEvent_t* ev) {
     al.norm.lam_scale = h->model.lam_scale;
     {
       KScope ks(h, K_FEATURES);
-      h->passes.lambda_learned<<<nblocks(n, 256), 256, 0, st>>>(p, f.loaded, h->bdata.p, h->xs[0].p,
+      ps.lambda_learned<<<grid_of(h, n), h->blk, 0, st>>>(p, f.loaded, h->bdata.p, h->xs[0].p,
                                                                  ms, h->nbr_count.p, h->nbr_list.p,
                                                                  h->xl.p, al);
     }
@@ -391,7 +457,7 @@ int substep(pbf_handle* h, cudaEvent_t* ev) {
     {
       KScope ks(h, K_DELTAP);
       SolverAux ad{};
-      h->passes.deltap<<<nblocks(n, 256), 256, 0, st>>>(p, ad, f.loaded, h->xl.p, h->bdata.p,
+      ps.deltap<<<grid_of(h, n), h->blk, 0, st>>>(p, ad, f.loaded, h->xl.p, h->bdata.p,
                                                          ms, h->nbr_count.p, h->nbr_list.p,
                                                          h->xs[1].p, nullptr);
     }
@@ -419,7 +485,7 @@ int substep(pbf_handle* h, cudaEvent_t* ev) {
     KScope ks(h, K_DENSITY);
     SolverAux ad{};
     if (h->learned || rec) ad.stats = h->stats.p;
-    h->passes.density_velocity<<<nblocks(n, 256), 256, 0, st>>>(p, ad, h->xs[a].p, ms, h->nbr_count.p,
+    ps.density_velocity<<<grid_of(h, n), h->blk, 0, st>>>(p, ad, h->xs[a].p, ms, h->nbr_count.p,
                                                                  h->nbr_list.p, h->pos[cc].p, h->vel.p);
   }
   CU(h, cudaGetLastError());
@@ -435,20 +501,20 @@ int substep(pbf_handle* h, cudaEvent_t* ev) {
     if (b != a) CU(h, launch_copy_guarded(n, fl, h->xs[b].p, h->xs[a].p, st));
     SolverAux ag{};
     ag.guard = fl;
-    h->passes.density_velocity<<<nblocks(n, 256), 256, 0, st>>>(p, ag, h->xs[a].p, ms, h->nbr_count.p,
+    ps.density_velocity<<<grid_of(h, n), h->blk, 0, st>>>(p, ag, h->xs[a].p, ms, h->nbr_count.p,
                                                                  h->nbr_list.p, h->pos[cc].p, h->vel.p);
     CU(h, cudaGetLastError());
   }
   if (a != 0) CU(h, cudaMemcpyAsync(h->xs[0].p, h->xs[1].p, (size_t)n * sizeof(float4), cudaMemcpyDeviceToDevice, st));
   {
     KScope ks(h, K_VORTICITY);
-    h->passes.vorticity<<<nblocks(n, 256), 256, 0, st>>>(p, h->pos[cc].p, h->vel.p, ms, h->nbr_count.p, h->nbr_list.p, h->omega.p,
+    ps.vorticity<<<grid_of(h, n), h->blk, 0, st>>>(p, h->pos[cc].p, h->vel.p, ms, h->nbr_count.p, h->nbr_list.p, h->omega.p,
                                                           h->normal.p);
   }
   CU(h, cudaGetLastError());
   {
     KScope ks(h, K_XSPH);
-    h->passes.xsph<<<nblocks(n, 256), 256, 0, st>>>(p, h->pos[cc].p, h->vel.p, h->omega.p, h->normal.p,
+    ps.xsph<<<grid_of(h, n), h->blk, 0, st>>>(p, h->pos[cc].p, h->vel.p, h->omega.p, h->normal.p,
                                                      ms, h->nbr_count.p, h->nbr_list.p, h->acc.p);
   }
   CU(h, cudaGetLastError());
@@ -517,6 +583,8 @@ void release_all(pbf_handle* h) {
   h->sdf.release();
   h->vol.release();
   h->bflag.release();
+  h->scenes_dev.release();
+  h->slot_scene.release();
   h->mlp_params.release();
   h->lam_sum.release();
   h->lam_prev.release();
@@ -579,6 +647,120 @@ void boundary_flags(const uint32_t res[3], const float* sdf, const float* vol, f
         bool far = (m - spread >= (double)h) || (M + spread <= 0.0);
         if (vzero || far) flag[(k * ny + j) * nx + i] = 0;
       }
+}
+
+
+// (Re)allocates the cell arrays for h->gp.cells cells.
+cudaError_t alloc_cells(pbf_handle* h) {
+  const size_t cells = h->gp.cells;
+  if (h->cell_count.p && h->cell_count.n == cells + 1) return cudaSuccess;
+  h->cell_count.release();
+  h->cell_start.release();
+  h->big_list.release();
+  cudaError_t e = h->cell_count.alloc(cells + 1);
+  if (e == cudaSuccess) e = h->cell_start.alloc(cells + 1);
+  if (e == cudaSuccess) e = h->big_list.alloc(cells);
+  if (h->scan_scratch) {
+    cudaFree(h->scan_scratch);
+    h->scan_scratch = nullptr;
+  }
+  if (e == cudaSuccess) e = cudaMalloc(&h->scan_scratch, scan_scratch_bytes(std::max(cells + 1, (size_t)h->cfg.max_particles + 1)));
+  return e;
+}
+
+// Grids of the scenes of a batch at the handle's cell ratio, with consecutive
+// key ranges; uploads the scene table.  Returns the total cell count (0 on
+// overflow of the 32-bit key space).
+uint64_t layout_scenes(pbf_handle* h) {
+  uint64_t base = 0;
+  for (auto& sd : h->scenes) {
+    GridParams g = make_grid(sd.dmin, sd.dmax, h->cfg.kernel_radius, h->cell_ratio, nullptr, true);
+    if (g.cells == 0) return 0;
+    g.key_base = (uint32_t)base;
+    sd.grid = g;
+    base += g.cells;
+    if (base > 0xfffffffeull) return 0;
+  }
+  return base;
+}
+
+// Applies a cell ratio: new grid(s), cell arrays, scene table.
+int apply_cell_ratio(pbf_handle* h, float ratio) {
+  if (ratio == h->cell_ratio) return PBF_OK;
+  const float old = h->cell_ratio;
+  h->cell_ratio = ratio;
+  if (h->batch) {
+    uint64_t cells = layout_scenes(h);
+    if (cells == 0) {
+      h->cell_ratio = old;
+      layout_scenes(h);
+      return fail(h, PBF_EINVAL, "cell ratio %g: too many cells", (double)ratio);
+    }
+    h->gp.cells = (uint32_t)cells;
+    CU(h, cudaMemcpy(h->scenes_dev.p, h->scenes.data(), h->scenes.size() * sizeof(SceneDesc), cudaMemcpyHostToDevice));
+  } else {
+    GridParams g = make_grid(h->cfg.domain_min, h->cfg.domain_max, h->cfg.kernel_radius, ratio,
+                             ratio == 1.0f ? h->cfg.grid_dim : nullptr, false);
+    if (g.cells == 0) {
+      h->cell_ratio = old;
+      return fail(h, PBF_EINVAL, "cell ratio %g: too many cells", (double)ratio);
+    }
+    h->gp = g;
+  }
+  invalidate_graph(h);
+  CU(h, alloc_cells(h));
+  return PBF_OK;
+}
+
+int apply_launch(pbf_handle* h, const pbf_launch& l) {
+  if (l.block != 128 && l.block != 256) return fail(h, PBF_EINVAL, "block must be 128 or 256");
+  if (l.ctas_per_sm > 16) return fail(h, PBF_EINVAL, "ctas_per_sm must be 0..16");
+  if (l.cell_ratio != 1.0f && l.cell_ratio != 0.5f) return fail(h, PBF_EINVAL, "cell_ratio must be 1 or 0.5");
+  int rc = apply_cell_ratio(h, l.cell_ratio);
+  if (rc) return rc;
+  if ((int)l.block != h->blk || l.ctas_per_sm != h->per_sm) invalidate_graph(h);
+  h->blk = (int)l.block;
+  h->per_sm = l.ctas_per_sm;
+  h->grid_cap = l.ctas_per_sm * (uint32_t)h->sms;
+  return PBF_OK;
+}
+
+// Metrics of slots [first, first + n) with the given volume map.
+int metrics_range(pbf_handle* h, uint32_t first, uint32_t n, const FieldParams& f, const float* sdf,
+                  pbf_metrics* out) {
+  std::memset(out, 0, sizeof(*out));
+  out->particles = n;
+  cudaStream_t st = h->stream;
+  CU(h, cudaMemsetAsync(h->m_f.p, 0, 2 * sizeof(float), st));
+  CU(h, cudaMemsetAsync(h->m_d.p, 0, 3 * sizeof(double), st));
+  CU(h, cudaMemsetAsync(h->m_u.p, 0, 3 * sizeof(uint32_t), st));
+  SimParams p = h->sp;
+  p.n = n;
+  if (n)
+    CU(h, launch_metrics(p, f, f.loaded ? sdf : nullptr, h->pos[h->cur].p + first, h->vel.p + first,
+                         h->nbr_count.p + first, n, h->m_f.p, h->m_d.p, h->m_u.p, st));
+  float mf[2];
+  double md[3];
+  uint32_t mu[3], errw = 0;
+  CU(h, cudaMemcpyAsync(mf, h->m_f.p, sizeof(mf), cudaMemcpyDeviceToHost, st));
+  CU(h, cudaMemcpyAsync(md, h->m_d.p, sizeof(md), cudaMemcpyDeviceToHost, st));
+  CU(h, cudaMemcpyAsync(mu, h->m_u.p, sizeof(mu), cudaMemcpyDeviceToHost, st));
+  CU(h, cudaMemcpyAsync(&errw, h->err_word.p, sizeof(uint32_t), cudaMemcpyDeviceToHost, st));
+  CU(h, cudaStreamSynchronize(st));
+  out->max_compression = mf[0];
+  out->max_abs_density_err = mf[1];
+  out->mean_abs_density_err = n ? (float)(md[0] / n) : 0.0f;
+  out->kinetic_energy = (float)md[1];
+  out->mean_compression = n ? (float)(md[2] / n) : 0.0f;
+  out->nonfinite = mu[0];
+  out->penetrations = mu[1];
+  out->error_flags = errw;
+  out->neighbor_total = mu[2];
+  return PBF_OK;
+}
+
+int not_for_batch(pbf_handle* h, const char* what) {
+  return fail(h, PBF_ESTATE, "%s is not available on a batch handle", what);
 }
 
 }  // namespace
@@ -646,6 +828,12 @@ int pbf_create(const pbf_config* cfg, pbf_handle** out) {
   } else {
     e = cudaStreamCreateWithFlags(&h->stream, cudaStreamNonBlocking);
     h->own_stream = true;
+  }
+  {
+    int dev = 0, sms = 0;
+    if (cudaGetDevice(&dev) == cudaSuccess && cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) == cudaSuccess &&
+        sms > 0)
+      h->sms = sms;
   }
   const size_t cap = cfg->max_particles, cells = h->gp.cells;
   const uint64_t rows = (uint64_t)(cap + 31) / 32 * 32;
@@ -724,6 +912,7 @@ int pbf_destroy(pbf_handle* h) {
 
 int pbf_reset(pbf_handle* h) {
   if (!h) return PBF_EINVAL;
+  if (h->batch) return not_for_batch(h, "pbf_reset");
   invalidate_graph(h);
   h->host_particles.clear();
   h->n = 0;
@@ -839,6 +1028,7 @@ int pbf_copy_host_particles(const pbf_handle* h, float* xyzw, uint32_t n) {
 
 int pbf_set_particle_position(pbf_handle* h) {
   if (!h) return PBF_EINVAL;
+  if (h->batch) return not_for_batch(h, "pbf_set_particle_position");
   if (h->host_particles.size() % 4 != 0) return fail(h, PBF_EINVAL, "Illegal length of Particle Position Buffer!");
   uint32_t n = (uint32_t)(h->host_particles.size() / 4);
   return upload_particles(h, h->host_particles.data(), n);
@@ -846,6 +1036,7 @@ int pbf_set_particle_position(pbf_handle* h) {
 
 int pbf_set_particles(pbf_handle* h, const float* xyzw, uint32_t n) {
   if (!h || (!xyzw && n)) return PBF_EINVAL;
+  if (h->batch) return not_for_batch(h, "pbf_set_particles");
   for (size_t i = 0; i < (size_t)n * 4; ++i)
     if ((i & 3) != 3 && !std::isfinite(xyzw[i])) return fail(h, PBF_EINVAL, "non-finite particle position");
   h->host_particles.assign(xyzw, xyzw + (size_t)n * 4);
@@ -878,6 +1069,7 @@ size_t pbf_field_length(const uint32_t res[3]) {
 int pbf_set_boundary_field(pbf_handle* h, const uint32_t res[3], const float origin[3], const float extent[3],
                            const float* sdf, const float* volume, size_t nodes) {
   if (!h || !res || !origin || !extent || !sdf || !volume) return PBF_EINVAL;
+  if (h->batch) return not_for_batch(h, "pbf_set_boundary_field");
   for (int a = 0; a < 3; ++a) {
     if (res[a] == 0 || res[a] > 4096) return fail(h, PBF_EINVAL, "bad field resolution");
     if (!finite_positive(extent[a])) return fail(h, PBF_EINVAL, "bad field extent");
@@ -966,6 +1158,7 @@ int pbf_set_boundary_data(pbf_handle* h, const char* text, size_t len) {
 
 int pbf_clear_boundary(pbf_handle* h) {
   if (!h) return PBF_EINVAL;
+  if (h->batch) return not_for_batch(h, "pbf_clear_boundary");
   invalidate_graph(h);
   h->fp.loaded = 0;
   return PBF_OK;
@@ -1113,6 +1306,7 @@ static int ensure_feature_buffers(pbf_handle* h) {
 }
 
 int pbf_set_trace(pbf_handle* h, uint32_t capacity, uint32_t stride, uint64_t salt) {
+  if (h && h->batch) return not_for_batch(h, "pbf_set_trace");
   if (!h || stride == 0) return PBF_EINVAL;
   invalidate_graph(h);
   h->trace_feat.release();
@@ -1175,6 +1369,7 @@ int pbf_trace_error(pbf_handle* h, float* max_mean, float* avg_mean) {
 }
 
 int pbf_set_learned(pbf_handle* h, const pbf_mlp* model, uint32_t iterations, float fallback_bound) {
+  if (h && h->batch) return not_for_batch(h, "pbf_set_learned");
   if (!h) return PBF_EINVAL;
   invalidate_graph(h);
   if (!model) {
@@ -1263,39 +1458,321 @@ int pbf_copy_field(pbf_handle* h, int field, void* host, size_t bytes) {
 
 int pbf_get_metrics(pbf_handle* h, pbf_metrics* out) {
   if (!h || !out) return PBF_EINVAL;
-  std::memset(out, 0, sizeof(*out));
-  out->particles = h->n;
-  cudaStream_t st = h->stream;
-  CU(h, cudaMemsetAsync(h->m_f.p, 0, 2 * sizeof(float), st));
-  CU(h, cudaMemsetAsync(h->m_d.p, 0, 3 * sizeof(double), st));
-  CU(h, cudaMemsetAsync(h->m_u.p, 0, 3 * sizeof(uint32_t), st));
-  SimParams p = h->sp;
-  p.n = h->n;
-  CU(h, launch_metrics(p, h->fp, h->fp.loaded ? h->sdf.p : nullptr, h->pos[h->cur].p, h->vel.p, h->nbr_count.p,
-                       h->n, h->m_f.p, h->m_d.p, h->m_u.p, st));
-  float mf[2];
-  double md[3];
-  uint32_t mu[3], errw = 0;
-  CU(h, cudaMemcpyAsync(mf, h->m_f.p, sizeof(mf), cudaMemcpyDeviceToHost, st));
-  CU(h, cudaMemcpyAsync(md, h->m_d.p, sizeof(md), cudaMemcpyDeviceToHost, st));
-  CU(h, cudaMemcpyAsync(mu, h->m_u.p, sizeof(mu), cudaMemcpyDeviceToHost, st));
-  CU(h, cudaMemcpyAsync(&errw, h->err_word.p, sizeof(uint32_t), cudaMemcpyDeviceToHost, st));
-  CU(h, cudaStreamSynchronize(st));
-  out->max_compression = mf[0];
-  out->max_abs_density_err = mf[1];
-  out->mean_abs_density_err = h->n ? (float)(md[0] / h->n) : 0.0f;
-  out->kinetic_energy = (float)md[1];
-  out->mean_compression = h->n ? (float)(md[2] / h->n) : 0.0f;
-  out->nonfinite = mu[0];
-  out->penetrations = mu[1];
-  out->error_flags = errw;
-  out->neighbor_total = mu[2];
+  if (!h->batch) {
+    int rc = metrics_range(h, 0, h->n, h->fp, h->sdf.p, out);
+    if (rc) return rc;
+  } else {
+    // all scenes: sums, maxima, particle-weighted means
+    pbf_metrics acc;
+    std::memset(&acc, 0, sizeof(acc));
+    double mean_abs = 0.0, mean_c = 0.0;
+    for (size_t s = 0; s < h->scenes.size(); ++s) {
+      const SceneDesc& sd = h->scenes[s];
+      pbf_metrics m;
+      int rc = metrics_range(h, sd.first, sd.n, sd.field, h->sdf.p ? h->sdf.p + sd.field.node_off : nullptr, &m);
+      if (rc) return rc;
+      acc.particles += m.particles;
+      acc.nonfinite += m.nonfinite;
+      acc.penetrations += m.penetrations;
+      acc.error_flags |= m.error_flags;
+      acc.max_compression = std::max(acc.max_compression, m.max_compression);
+      acc.max_abs_density_err = std::max(acc.max_abs_density_err, m.max_abs_density_err);
+      acc.kinetic_energy += m.kinetic_energy;
+      acc.neighbor_total += m.neighbor_total;
+      mean_abs += (double)m.mean_abs_density_err * m.particles;
+      mean_c += (double)m.mean_compression * m.particles;
+    }
+    if (acc.particles) {
+      acc.mean_abs_density_err = (float)(mean_abs / acc.particles);
+      acc.mean_compression = (float)(mean_c / acc.particles);
+    }
+    *out = acc;
+  }
   if (h->fb_count.p) {
     uint32_t fb = 0;
     CU(h, cudaMemcpy(&fb, h->fb_count.p, sizeof(uint32_t), cudaMemcpyDeviceToHost));
     out->fallback_steps = fb;
   }
   return PBF_OK;
+}
+
+int pbf_set_launch(pbf_handle* h, const pbf_launch* l) {
+  if (!h || !l) return PBF_EINVAL;
+  return apply_launch(h, *l);
+}
+
+int pbf_get_launch(const pbf_handle* h, pbf_launch* l) {
+  if (!h || !l) return PBF_EINVAL;
+  l->block = (uint32_t)h->blk;
+  l->ctas_per_sm = h->per_sm;
+  l->cell_ratio = h->cell_ratio;
+  return PBF_OK;
+}
+
+int pbf_autotune(pbf_handle* h, uint32_t substeps, uint32_t flags, pbf_tune_trial* trials, uint32_t max_trials,
+                 uint32_t* count, pbf_launch* best) {
+  if (!h || (!trials && max_trials)) return PBF_EINVAL;
+  if (h->trace_cap > 0) return fail(h, PBF_ESTATE, "pbf_autotune while trace capture is on");
+  if (h->n == 0) return fail(h, PBF_ESTATE, "pbf_autotune needs particles");
+  if (substeps == 0) substeps = 4;
+  const uint32_t n = h->n;
+  cudaStream_t st = h->stream;
+  CU(h, cudaStreamSynchronize(st));
+  int rc = check_device_errors(h);
+  if (rc) return rc;
+  // the state the trials start from and that is restored afterwards
+  const int cur0 = h->cur;
+  const uint32_t ctr0 = h->substep_counter;
+  DBuf<float4> s_pos, s_vel, s_acc;
+  DBuf<uint32_t> s_ids;
+  DBuf<float> s_lam;
+  uint32_t fb0 = 0;
+  struct Free {
+    DBuf<float4>*a, *b, *c;
+    DBuf<uint32_t>* d;
+    DBuf<float>* e;
+    ~Free() {
+      a->release();
+      b->release();
+      c->release();
+      d->release();
+      e->release();
+    }
+  } fr{&s_pos, &s_vel, &s_acc, &s_ids, &s_lam};
+  CU(h, s_pos.alloc(n));
+  CU(h, s_vel.alloc(n));
+  CU(h, s_acc.alloc(n));
+  CU(h, s_ids.alloc(n));
+  const size_t b4 = (size_t)n * sizeof(float4), b1 = (size_t)n * sizeof(uint32_t);
+  CU(h, cudaMemcpyAsync(s_pos.p, h->pos[cur0].p, b4, cudaMemcpyDeviceToDevice, st));
+  CU(h, cudaMemcpyAsync(s_vel.p, h->vel.p, b4, cudaMemcpyDeviceToDevice, st));
+  CU(h, cudaMemcpyAsync(s_acc.p, h->acc.p, b4, cudaMemcpyDeviceToDevice, st));
+  CU(h, cudaMemcpyAsync(s_ids.p, h->ids[cur0].p, b1, cudaMemcpyDeviceToDevice, st));
+  if (h->lam_sum.p) {
+    CU(h, s_lam.alloc(n));
+    CU(h, cudaMemcpyAsync(s_lam.p, h->lam_sum.p, b1, cudaMemcpyDeviceToDevice, st));
+  }
+  if (h->fb_count.p) CU(h, cudaMemcpy(&fb0, h->fb_count.p, sizeof(uint32_t), cudaMemcpyDeviceToHost));
+  auto restore = [&]() -> int {
+    h->cur = cur0;
+    h->substep_counter = ctr0;
+    CU(h, cudaMemcpyAsync(h->pos[cur0].p, s_pos.p, b4, cudaMemcpyDeviceToDevice, st));
+    CU(h, cudaMemcpyAsync(h->vel.p, s_vel.p, b4, cudaMemcpyDeviceToDevice, st));
+    CU(h, cudaMemcpyAsync(h->acc.p, s_acc.p, b4, cudaMemcpyDeviceToDevice, st));
+    CU(h, cudaMemcpyAsync(h->ids[cur0].p, s_ids.p, b1, cudaMemcpyDeviceToDevice, st));
+    if (s_lam.p) CU(h, cudaMemcpyAsync(h->lam_sum.p, s_lam.p, b1, cudaMemcpyDeviceToDevice, st));
+    if (h->fb_count.p) CU(h, cudaMemcpyAsync(h->fb_count.p, &fb0, sizeof(uint32_t), cudaMemcpyHostToDevice, st));
+    CU(h, cudaStreamSynchronize(st));
+    return PBF_OK;
+  };
+  std::vector<pbf_launch> cand;
+  const float ratios[2] = {1.0f, 0.5f};
+  // one tile per CTA, or persistent grids holding half or all of an SM's
+  // 2048 threads
+  const uint32_t blocks[2] = {128, 256};
+  for (int r = 0; r < ((flags & PBF_TUNE_CELL_RATIO) ? 2 : 1); ++r)
+    for (uint32_t b : blocks)
+      for (uint32_t k : {0u, 1024u / b, 2048u / b}) cand.push_back(pbf_launch{b, k, ratios[r]});
+  const pbf_launch orig{(uint32_t)h->blk, h->per_sm, h->cell_ratio};
+  const bool kt = h->ktiming;
+  h->ktiming = false;
+  cudaEvent_t e0 = nullptr, e1 = nullptr;
+  CU(h, cudaEventCreate(&e0));
+  CU(h, cudaEventCreate(&e1));
+  float best_ms = 3.4e38f;
+  pbf_launch best_l = orig;
+  uint32_t c = 0;
+  for (const pbf_launch& l : cand) {
+    rc = apply_launch(h, l);
+    for (int attempt = 0; rc == PBF_OK && attempt < 2; ++attempt) {
+      rc = restore();
+      for (int w = 0; rc == PBF_OK && w < 2; ++w) rc = substep(h, nullptr);
+      if (rc == PBF_OK && cudaEventRecord(e0, st) != cudaSuccess) rc = PBF_ECUDA;
+      for (uint32_t k = 0; rc == PBF_OK && k < substeps; ++k) rc = substep(h, nullptr);
+      if (rc == PBF_OK && cudaEventRecord(e1, st) != cudaSuccess) rc = PBF_ECUDA;
+      if (rc == PBF_OK && cudaEventSynchronize(e1) != cudaSuccess) rc = PBF_ECUDA;
+      if (rc == PBF_OK) rc = check_device_errors(h);
+      if (rc != PBF_ECAPACITY) break;  // a grown neighbour list: time the candidate again
+      rc = PBF_OK;
+    }
+    if (rc) break;
+    float ms = 0.0f;
+    cudaEventElapsedTime(&ms, e0, e1);
+    ms /= (float)substeps;
+    if (c < max_trials) trials[c] = pbf_tune_trial{l, ms};
+    ++c;
+    if (ms < best_ms) {
+      best_ms = ms;
+      best_l = l;
+    }
+  }
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  h->ktiming = kt;
+  const std::string err = h->err;
+  int rc2 = apply_launch(h, rc ? orig : best_l);
+  if (rc2 == PBF_OK) rc2 = restore();
+  if (rc2 == PBF_OK) rc2 = export_positions(h);
+  invalidate_graph(h);
+  if (count) *count = c;
+  if (best) *best = rc ? orig : best_l;
+  if (rc) {
+    h->err = err;
+    return rc;
+  }
+  return rc2;
+}
+
+int pbf_batch_create(const pbf_config* shared, const pbf_scene* scenes, uint32_t count, pbf_handle** out) {
+  if (!shared || !scenes || !out || count == 0 || count > 65535) return PBF_EINVAL;
+  *out = nullptr;
+  uint64_t total = 0;
+  uint32_t max_it = 0;
+  for (uint32_t s = 0; s < count; ++s) {
+    const pbf_scene& sc = scenes[s];
+    if (sc.struct_size != sizeof(pbf_scene) || sc.particles == 0 || !sc.positions) return PBF_EINVAL;
+    for (int a = 0; a < 3; ++a)
+      if (!(sc.domain_max[a] > sc.domain_min[a])) return PBF_EINVAL;
+    const bool fld = sc.field_res[0] || sc.field_res[1] || sc.field_res[2];
+    if (fld) {
+      if (!sc.sdf || !sc.volume) return PBF_EINVAL;
+      for (int a = 0; a < 3; ++a)
+        if (sc.field_res[a] == 0 || sc.field_res[a] > 4096 || !finite_positive(sc.field_extent[a])) return PBF_EINVAL;
+    }
+    for (size_t i = 0; i < (size_t)sc.particles * 4; ++i)
+      if ((i & 3) != 3 && !std::isfinite(sc.positions[i])) return PBF_EINVAL;
+    total += sc.particles;
+    uint32_t it = sc.iterations ? sc.iterations : shared->options.iterations;
+    max_it = std::max(max_it, it);
+  }
+  if (total > 0x7fffffffull) return PBF_ECAPACITY;
+  pbf_config c = *shared;
+  c.max_particles = (uint32_t)total;
+  for (int a = 0; a < 3; ++a) {
+    c.domain_min[a] = scenes[0].domain_min[a];
+    c.domain_max[a] = scenes[0].domain_max[a];
+    c.grid_dim[a] = 0;
+  }
+  c.options.iterations = max_it;
+  pbf_handle* h = nullptr;
+  int rc = pbf_create(&c, &h);
+  if (rc) return rc;
+  auto bail = [&](int code, const char* msg) {
+    pbf_destroy(h);
+    (void)msg;
+    return code;
+  };
+  h->batch = true;
+  h->scenes.resize(count);
+  h->scene_info.resize(count);
+  uint64_t nodes = 0, flags = 0;
+  bool any_field = false;
+  uint32_t first = 0;
+  for (uint32_t s = 0; s < count; ++s) {
+    const pbf_scene& sc = scenes[s];
+    SceneDesc sd{};
+    for (int a = 0; a < 3; ++a) {
+      sd.dmin[a] = sc.domain_min[a];
+      sd.dmax[a] = sc.domain_max[a];
+    }
+    sd.iterations = sc.iterations ? sc.iterations : shared->options.iterations;
+    sd.first = first;
+    sd.n = sc.particles;
+    first += sc.particles;
+    if (sc.field_res[0] || sc.field_res[1] || sc.field_res[2]) {
+      sd.field = make_field(c, sc.field_res, sc.field_origin, sc.field_extent);
+      sd.field.node_off = (uint32_t)nodes;
+      sd.field.flag_off = (uint32_t)flags;
+      nodes += pbf_field_length(sc.field_res);
+      flags += (uint64_t)sc.field_res[0] * sc.field_res[1] * sc.field_res[2];
+      if (nodes > 0xffffffffull || flags > 0xffffffffull) return bail(PBF_ECAPACITY, "fields");
+      any_field = true;
+    } else {
+      sd.field.loaded = 0;
+    }
+    h->scenes[s] = sd;
+  }
+  const uint64_t cells = layout_scenes(h);
+  if (cells == 0) return bail(PBF_EINVAL, "cells");
+  h->gp.cells = (uint32_t)cells;
+  if (alloc_cells(h) != cudaSuccess) return bail(PBF_ECUDA, "cells");
+  if (any_field) {
+    std::vector<float> sdf(nodes), vol(nodes);
+    std::vector<uint8_t> flag(flags), f1;
+    for (uint32_t s = 0; s < count; ++s) {
+      const pbf_scene& sc = scenes[s];
+      const SceneDesc& sd = h->scenes[s];
+      if (!sd.field.loaded) continue;
+      const size_t len = pbf_field_length(sc.field_res);
+      std::memcpy(sdf.data() + sd.field.node_off, sc.sdf, len * sizeof(float));
+      std::memcpy(vol.data() + sd.field.node_off, sc.volume, len * sizeof(float));
+      boundary_flags(sc.field_res, sc.sdf, sc.volume, c.kernel_radius, f1);
+      std::memcpy(flag.data() + sd.field.flag_off, f1.data(), f1.size());
+    }
+    if (h->sdf.alloc(nodes) != cudaSuccess || h->vol.alloc(nodes) != cudaSuccess || h->bflag.alloc(flags) != cudaSuccess)
+      return bail(PBF_ECUDA, "fields");
+    if (cudaMemcpy(h->sdf.p, sdf.data(), nodes * sizeof(float), cudaMemcpyHostToDevice) != cudaSuccess ||
+        cudaMemcpy(h->vol.p, vol.data(), nodes * sizeof(float), cudaMemcpyHostToDevice) != cudaSuccess ||
+        cudaMemcpy(h->bflag.p, flag.data(), flags, cudaMemcpyHostToDevice) != cudaSuccess)
+      return bail(PBF_ECUDA, "fields");
+    h->fp = FieldParams{};
+    h->fp.loaded = 1;
+  }
+  std::vector<uint16_t> slot_scene((size_t)total);
+  std::vector<float> xyzw((size_t)total * 4);
+  for (uint32_t s = 0; s < count; ++s) {
+    const SceneDesc& sd = h->scenes[s];
+    std::fill(slot_scene.begin() + sd.first, slot_scene.begin() + sd.first + sd.n, (uint16_t)s);
+    std::memcpy(xyzw.data() + (size_t)sd.first * 4, scenes[s].positions, (size_t)sd.n * 4 * sizeof(float));
+  }
+  if (h->scenes_dev.alloc(count) != cudaSuccess || h->slot_scene.alloc(total) != cudaSuccess)
+    return bail(PBF_ECUDA, "table");
+  if (cudaMemcpy(h->scenes_dev.p, h->scenes.data(), count * sizeof(SceneDesc), cudaMemcpyHostToDevice) != cudaSuccess ||
+      cudaMemcpy(h->slot_scene.p, slot_scene.data(), total * sizeof(uint16_t), cudaMemcpyHostToDevice) != cudaSuccess)
+    return bail(PBF_ECUDA, "table");
+  h->tab = SceneTab{h->scenes_dev.p, h->slot_scene.p};
+  rc = upload_particles(h, xyzw.data(), (uint32_t)total);
+  if (rc) {
+    pbf_destroy(h);
+    return rc;
+  }
+  for (uint32_t s = 0; s < count; ++s) {
+    const SceneDesc& sd = h->scenes[s];
+    pbf_scene_info& in = h->scene_info[s];
+    in.first_id = sd.first;
+    in.particles = sd.n;
+    in.iterations = sd.iterations;
+  }
+  *out = h;
+  return PBF_OK;
+}
+
+uint32_t pbf_scene_count(const pbf_handle* h) {
+  if (!h) return 0;
+  return h->batch ? (uint32_t)h->scenes.size() : 1u;
+}
+
+int pbf_get_scene_info(const pbf_handle* h, uint32_t scene, pbf_scene_info* out) {
+  if (!h || !out || scene >= pbf_scene_count(h)) return PBF_EINVAL;
+  std::memset(out, 0, sizeof(*out));
+  const GridParams& g = h->batch ? h->scenes[scene].grid : h->gp;
+  if (h->batch) {
+    *out = h->scene_info[scene];
+  } else {
+    out->first_id = 0;
+    out->particles = h->n;
+    out->iterations = h->cfg.options.iterations;
+  }
+  for (int a = 0; a < 3; ++a) out->grid_dim[a] = (uint32_t)g.dim[a];
+  out->cells = g.cells;
+  return PBF_OK;
+}
+
+int pbf_get_scene_metrics(pbf_handle* h, uint32_t scene, pbf_metrics* out) {
+  if (!h || !out || scene >= pbf_scene_count(h)) return PBF_EINVAL;
+  if (!h->batch) return pbf_get_metrics(h, out);
+  const SceneDesc& sd = h->scenes[scene];
+  return metrics_range(h, sd.first, sd.n, sd.field, h->sdf.p ? h->sdf.p + sd.field.node_off : nullptr, out);
 }
 
 // ---- neighbour search alone -------------------------------------------------------
@@ -1346,6 +1823,8 @@ int pbf_ns_create(const pbf_grid* grid, uint32_t max_particles, void* stream, pb
     s->g.dim[a] = (int)grid->dim[a];
   }
   s->g.cells = (uint32_t)cells;
+  s->g.key_base = 0;
+  s->g.reach = 1;
   s->max_n = max_particles;
   cudaError_t e = cudaSuccess;
   if (stream) {

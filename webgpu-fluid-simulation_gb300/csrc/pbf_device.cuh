@@ -165,7 +165,8 @@ __device__ __forceinline__ int cell_axis(float x, float o, float inv, int d) {
   return min(max(c, 0), d - 1);
 }
 __device__ __forceinline__ uint32_t cell_key(int cx, int cy, int cz, const GridParams& g) {
-  return (uint32_t)cx * (uint32_t)(g.dim[1] * g.dim[2]) + (uint32_t)cy * (uint32_t)g.dim[2] + (uint32_t)cz;
+  return g.key_base + (uint32_t)cx * (uint32_t)(g.dim[1] * g.dim[2]) + (uint32_t)cy * (uint32_t)g.dim[2] +
+         (uint32_t)cz;
 }
 
 // ---- volume map (src/simulator/boundary/discreteFieldShader.ts:1-192) ---------------

@@ -10,22 +10,21 @@
 
 namespace pbf {
 
-struct PassTable {
-  void (*predict)(SimParams, GridParams, const float4*, const float4*, const float4*, float4*, uint32_t*, uint32_t*,
-                  uint32_t*);
-  void (*nbr_count)(SimParams, GridParams, const float4*, const uint32_t*, uint32_t*);
-  void (*nbr_list)(SimParams, GridParams, const float4*, const uint32_t*, const uint32_t*, uint32_t*, uint32_t,
-                   uint32_t*);
-  void (*nbr_build)(SimParams, GridParams, const float4*, const uint32_t*, uint32_t, uint32_t*, uint32_t*,
+// The step's passes of one variant: single scene or batch (scene table),
+// one tile per CTA or persistent (grid-stride).
+struct PassSet {
+  void (*predict)(SimParams, GridParams, SceneTab, const float4*, const float4*, const float4*, float4*, uint32_t*,
+                  uint32_t*, uint32_t*);
+  void (*nbr_build)(SimParams, GridParams, SceneTab, const float4*, const uint32_t*, uint32_t, uint32_t*, uint32_t*,
                     uint32_t*, uint32_t*);
   void (*boundary)(SimParams, FieldParams, const float*, const float*, const uint8_t*, const float4*, float4*,
                    SolverAux);
   void (*lambda)(SimParams, int, const float4*, const float4*, uint32_t, const uint32_t*, const uint32_t*, float4*,
                  SolverAux);
   void (*lambda_feat)(SimParams, int, const float4*, const float4*, uint32_t, const uint32_t*, const uint32_t*,
-                      float4*, SolverAux);
+                      float4*, SolverAux);     // null in batch sets
   void (*lambda_learned)(SimParams, int, const float4*, const float4*, uint32_t, const uint32_t*, const uint32_t*,
-                         float4*, SolverAux);
+                         float4*, SolverAux);  // null in batch sets
   void (*deltap)(SimParams, SolverAux, int, const float4*, const float4*, uint32_t, const uint32_t*, const uint32_t*,
                  float4*, float4*);
   void (*density_velocity)(SimParams, SolverAux, const float4*, uint32_t, const uint32_t*, const uint32_t*, float4*,
@@ -34,6 +33,14 @@ struct PassTable {
                     float4*);
   void (*xsph)(SimParams, const float4*, const float4*, const float4*, const float4*, uint32_t, const uint32_t*,
                const uint32_t*, float4*);
+};
+
+struct PassTable {
+  // the stand-alone neighbour search (reference list layout)
+  void (*nbr_count)(SimParams, GridParams, const float4*, const uint32_t*, uint32_t*);
+  void (*nbr_list)(SimParams, GridParams, const float4*, const uint32_t*, const uint32_t*, uint32_t*, uint32_t,
+                   uint32_t*);
+  PassSet set[2][2];  // [batch][persistent]
 };
 
 namespace exact {

@@ -11,6 +11,8 @@ struct GridParams {
   float inv_cell[3];  // cells per unit length
   int dim[3];
   uint32_t cells;     // dim[0] * dim[1] * dim[2]
+  uint32_t key_base;  // first key of this grid in a shared key space (batched scenes; 0 otherwise)
+  int reach;          // neighbourhood half-width in cells (1: the 27-cell search; 2 when cells are h/2)
 };
 
 struct FieldParams {
@@ -21,6 +23,8 @@ struct FieldParams {
   int quirk;          // reference volume-node quirk
   int trilinear;      // 1 = trilinear corner interpolation
   int loaded;
+  uint32_t node_off;  // first node of this map in the concatenated SDF/volume arrays (batched scenes)
+  uint32_t flag_off;  // first cell flag of this map in the concatenated flag array
 };
 
 struct SimParams {
@@ -46,6 +50,24 @@ struct SolveStats {
   unsigned long long sum_fx; // sum_i min(max(0, rho_i - 1), 1) in 2^-20 fixed point
 };
 
+// One scene of a batch: its grid (with its key range), volume map, domain and
+// solver iterations.  Its particles occupy slots (and ids) [first, first + n)
+// for the whole run: its keys sort after every earlier scene's keys.
+struct SceneDesc {
+  GridParams grid;
+  FieldParams field;
+  float dmin[3], dmax[3];
+  uint32_t iterations;
+  uint32_t first, n;
+};
+
+// Per-slot scene lookup of a batch; scene == nullptr for a single scene
+// (every parameter then comes by value).
+struct SceneTab {
+  const SceneDesc* scene;
+  const uint16_t* slot_scene;
+};
+
 // Input normalisation of the learned start's network.
 struct MLPNorm {
   float mean[8];
@@ -67,6 +89,9 @@ struct SolverAux {
   float substep_index;       // lambda pass (features)
   const float* mlp;          // lambda pass (network): flat FP32 parameters
   MLPNorm norm;              // lambda pass (network)
+  SceneTab tab;              // batched scenes: per-scene iteration counts, domains, maps
+  int iter;                  // solver iteration of this launch (scenes with fewer iterations skip it)
+  const float4* xs_in;       // delta-p pass: x* of a scene that skips the iteration is copied through
 };
 
 }  // namespace pbf

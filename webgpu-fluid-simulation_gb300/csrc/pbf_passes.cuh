@@ -48,30 +48,71 @@ __device__ __forceinline__ uint32_t key_of(const GridParams& g, f3 x) {
   return cell_key(cx, cy, cz, g);
 }
 
-// predict x* (TimeIntegration), its cell key and within-cell rank (ParticleInsert).
-__global__ void __launch_bounds__(256) k_predict(SimParams p, GridParams g, const float4* __restrict__ pos,
-                                                 const float4* __restrict__ vel, const float4* __restrict__ acc,
-                                                 float4* __restrict__ xs_out, uint32_t* __restrict__ key_out,
-                                                 uint32_t* __restrict__ rank_out, uint32_t* cell_count) {
-  uint32_t s = blockIdx.x * blockDim.x + threadIdx.x;
-  uint32_t key = kNoKey;
-  if (s < p.n) {
-    f3 x = xyz(pos[s]);
-    f3 v = xyz(vel[s]);
-    f3 a = xyz(acc[s]);
-    f3 gv = mk(0.0f + a.x, p.gy + a.y, 0.0f + a.z);
-    f3 vp = v + p.dt * gv;
-    f3 xp = clamp_rand(p, x + p.dt * vp);
-    xs_out[s] = f4(xp, 0.0f);
-    key = key_of(g, xp);
-    key_out[s] = key;
+// Every step pass exists as a one-tile-per-CTA kernel (kLoop = false: the
+// loop below runs once and compiles away) and as a persistent kernel
+// (kLoop = true: a grid of a few CTAs per SM walks the tiles blockIdx.x,
+// blockIdx.x + gridDim.x, ...).  PBF_TILES keeps the bound uniform across a
+// CTA, so warp collectives stay converged; PBF_SLOTS is per thread.  A
+// `continue` ends the one-tile form too (the step sets the index to n).
+#define PBF_TILES(n) \
+  for (uint32_t tile0 = blockIdx.x * blockDim.x; tile0 < (n); tile0 = kLoop ? tile0 + gridDim.x * blockDim.x : (n))
+#define PBF_SLOTS(t, n)                                                                     \
+  for (uint32_t t = blockIdx.x * blockDim.x + threadIdx.x; t < (n); \
+       t = kLoop ? t + gridDim.x * blockDim.x : (n))
+
+// Per-slot scene of a batch: overrides the by-value grid / domain.  The
+// kernels that consult it are instantiated twice; with kBatch = false the
+// lookup folds away and the single-scene code is what it was without batches.
+template <bool kBatch>
+__device__ __forceinline__ const SceneDesc* scene_of(const SceneTab& tab, uint32_t t) {
+  if constexpr (!kBatch) return nullptr;
+  return tab.scene + __ldg(tab.slot_scene + t);
+}
+__device__ __forceinline__ void scene_domain(SimParams& p, const SceneDesc* sd) {
+  if (!sd) return;
+#pragma unroll
+  for (int a = 0; a < 3; ++a) {
+    p.dmin[a] = sd->dmin[a];
+    p.dmax[a] = sd->dmax[a];
   }
-  uint32_t rank = warp_aggregated_rank(cell_count, key);
-  if (s < p.n) rank_out[s] = rank;
 }
 
-// Range of slots covering cells (cx+dx, cy+dy, cz-1 .. cz+1): the 27-cell
-// neighbourhood is 9 runs of consecutive keys because keys are z-fastest.
+// predict x* (TimeIntegration), its cell key and within-cell rank (ParticleInsert).
+template <bool kBatch, bool kLoop>
+__global__ void __launch_bounds__(256) k_predict(SimParams p0, GridParams g0, SceneTab tab,
+                                                 const float4* __restrict__ pos, const float4* __restrict__ vel,
+                                                 const float4* __restrict__ acc, float4* __restrict__ xs_out,
+                                                 uint32_t* __restrict__ key_out, uint32_t* __restrict__ rank_out,
+                                                 uint32_t* cell_count) {
+  PBF_TILES(p0.n) {
+    const uint32_t s = tile0 + threadIdx.x;
+    uint32_t key = kNoKey;
+    if (s < p0.n) {
+      SimParams p = p0;
+      GridParams g = g0;
+      const SceneDesc* sd = scene_of<kBatch>(tab, s);
+      if (sd) {
+        scene_domain(p, sd);
+        g = sd->grid;
+      }
+      f3 x = xyz(pos[s]);
+      f3 v = xyz(vel[s]);
+      f3 a = xyz(acc[s]);
+      f3 gv = mk(0.0f + a.x, p.gy + a.y, 0.0f + a.z);
+      f3 vp = v + p.dt * gv;
+      f3 xp = clamp_rand(p, x + p.dt * vp);
+      xs_out[s] = f4(xp, 0.0f);
+      key = key_of(g, xp);
+      key_out[s] = key;
+    }
+    uint32_t rank = warp_aggregated_rank(cell_count, key);
+    if (s < p0.n) rank_out[s] = rank;
+  }
+}
+
+// Range of slots covering cells (cx+dx, cy+dy, cz-R .. cz+R), R = g.reach:
+// the (2R+1)^3-cell neighbourhood is (2R+1)^2 runs of consecutive keys
+// because keys are z-fastest (R = 1: the reference's 27 cells as 9 runs).
 struct Run {
   uint32_t b, e;
 };
@@ -79,7 +120,7 @@ __device__ __forceinline__ Run run_of(const GridParams& g, const uint32_t* __res
                                       int cz, int dx, int dy) {
   int x = cx + dx, y = cy + dy;
   if (x < 0 || y < 0 || x >= g.dim[0] || y >= g.dim[1]) return Run{0, 0};
-  int zlo = max(cz - 1, 0), zhi = min(cz + 1, g.dim[2] - 1);
+  int zlo = max(cz - g.reach, 0), zhi = min(cz + g.reach, g.dim[2] - 1);
   uint32_t k0 = cell_key(x, y, zlo, g), k1 = cell_key(x, y, zhi, g) + 1u;
   return Run{__ldg(cell_start + k0), __ldg(cell_start + k1)};
 }
@@ -116,36 +157,44 @@ __global__ void __launch_bounds__(256) k_nbr_count(SimParams p, GridParams g, co
 // and no count pass or scan is needed to place them.  nbr_count[t] receives
 // the true count; a count above max_nbr flags an overflow (the entries past
 // the slice are dropped and max_seen records the largest count for growing).
-__global__ void __launch_bounds__(256) k_nbr_build(SimParams p, GridParams g, const float4* __restrict__ xs,
+// Runs are visited in key order, so entries come in increasing slot order.
+template <bool kBatch, bool kLoop>
+__global__ void __launch_bounds__(256) k_nbr_build(SimParams p, GridParams g0, SceneTab tab,
+                                                   const float4* __restrict__ xs,
                                                    const uint32_t* __restrict__ cell_start, uint32_t max_nbr,
                                                    uint32_t* __restrict__ nbr_list, uint32_t* __restrict__ nbr_count,
                                                    uint32_t* max_seen, uint32_t* err) {
-  uint32_t t = blockIdx.x * blockDim.x + threadIdx.x;
-  if (t >= p.n) return;
-  f3 xi = xyz(xs[t]);
-  int cx = cell_axis(xi.x, g.origin[0], g.inv_cell[0], g.dim[0]);
-  int cy = cell_axis(xi.y, g.origin[1], g.inv_cell[1], g.dim[1]);
-  int cz = cell_axis(xi.z, g.origin[2], g.inv_cell[2], g.dim[2]);
-  uint32_t* out = nbr_list + (size_t)(t >> 5) * 32u * max_nbr + (t & 31u);
-  uint32_t q = 0;
-  for (int dx = -1; dx <= 1; ++dx)
-    for (int dy = -1; dy <= 1; ++dy) {
-      Run r = run_of(g, cell_start, cx, cy, cz, dx, dy);
-      for (uint32_t u = r.b; u < r.e; ++u) {
-        f3 d = xyz(__ldg(xs + u)) - xi;
-        if (dot3(d, d) <= p.h2) {
-          if (q < max_nbr) out[32u * q] = u;
-          ++q;
+  PBF_TILES(p.n) {
+    const uint32_t t = tile0 + threadIdx.x;
+    if (t < p.n) {
+      const SceneDesc* sd = scene_of<kBatch>(tab, t);
+      const GridParams g = sd ? sd->grid : g0;
+      f3 xi = xyz(xs[t]);
+      int cx = cell_axis(xi.x, g.origin[0], g.inv_cell[0], g.dim[0]);
+      int cy = cell_axis(xi.y, g.origin[1], g.inv_cell[1], g.dim[1]);
+      int cz = cell_axis(xi.z, g.origin[2], g.inv_cell[2], g.dim[2]);
+      uint32_t* out = nbr_list + (size_t)(t >> 5) * 32u * max_nbr + (t & 31u);
+      uint32_t q = 0;
+      for (int dx = -g.reach; dx <= g.reach; ++dx)
+        for (int dy = -g.reach; dy <= g.reach; ++dy) {
+          Run r = run_of(g, cell_start, cx, cy, cz, dx, dy);
+          for (uint32_t u = r.b; u < r.e; ++u) {
+            f3 d = xyz(__ldg(xs + u)) - xi;
+            if (dot3(d, d) <= p.h2) {
+              if (q < max_nbr) out[32u * q] = u;
+              ++q;
+            }
+          }
+        }
+      nbr_count[t] = q;
+      const unsigned m = __activemask();
+      if (__any_sync(m, q > max_nbr)) {
+        unsigned wmax = __reduce_max_sync(m, q);
+        if ((threadIdx.x & 31u) == (unsigned)(__ffs(m) - 1)) {
+          atomicMax(max_seen, wmax);
+          atomicOr(err, 0x1u);
         }
       }
-    }
-  nbr_count[t] = q;
-  const unsigned m = __activemask();
-  if (__any_sync(m, q > max_nbr)) {
-    unsigned wmax = __reduce_max_sync(m, q);
-    if ((threadIdx.x & 31u) == (unsigned)(__ffs(m) - 1)) {
-      atomicMax(max_seen, wmax);
-      atomicOr(err, 0x1u);
     }
   }
 }
@@ -224,26 +273,43 @@ __device__ __forceinline__ void list_slice(uint32_t max_nbr, const uint32_t* __r
   cnt = min(__ldg(cnt_of + t), max_nbr);
 }
 
+// Whether a scene (of a batch) runs solver iteration `iter`.
+__device__ __forceinline__ bool iter_active(const SceneDesc* sd, int iter) {
+  return !sd || (uint32_t)iter < sd->iterations;
+}
+
 // BoundaryVolume (boundaryVolume.ts:26-57): (x_b, V_b) per particle, skipping
-// the 64-node interpolation where the field cell cannot produce a sample.
-__global__ void __launch_bounds__(256, 3) k_boundary(SimParams p, FieldParams f, const float* __restrict__ sdf,
-                                                  const float* __restrict__ vol, const uint8_t* __restrict__ bflag,
-                                                  const float4* __restrict__ xs, float4* __restrict__ bdata,
-                                                  SolverAux a) {
+// the 64-node interpolation where the field cell cannot produce a sample.  In
+// a batch each scene samples its own map (offsets into the concatenated
+// arrays); a scene without a map gets (0, 0).
+template <bool kBatch, bool kLoop>
+__global__ void __launch_bounds__(256, 3) k_boundary(SimParams p, FieldParams f0, const float* __restrict__ sdf0,
+                                                     const float* __restrict__ vol0,
+                                                     const uint8_t* __restrict__ bflag0,
+                                                     const float4* __restrict__ xs, float4* __restrict__ bdata,
+                                                     SolverAux a) {
   if (a.guard && *a.guard == 0) return;
-  uint32_t t = blockIdx.x * blockDim.x + threadIdx.x;
-  if (t >= p.n) return;
-  f3 xi = xyz(xs[t]);
-  float4 bd = make_float4(0.f, 0.f, 0.f, 0.f);
-  float dist = 2.0f * p.h;  // "far" for the feature when the cell cannot contribute
-  if (boundary_possible(f, bflag, xi)) {
-    if (a.bsdf) {
-      dist = boundary_distance(f, sdf, xi);
+  PBF_SLOTS(t, p.n) {
+    const SceneDesc* sd = scene_of<kBatch>(a.tab, t);
+    if (!iter_active(sd, a.iter)) continue;
+    const FieldParams f = sd ? sd->field : f0;
+    f3 xi = xyz(xs[t]);
+    float4 bd = make_float4(0.f, 0.f, 0.f, 0.f);
+    float dist = 2.0f * p.h;  // "far" for the feature when the cell cannot contribute
+    if (f.loaded) {
+      const float* sdf = sdf0 + f.node_off;
+      const float* vol = vol0 + f.node_off;
+      const uint8_t* bflag = bflag0 ? bflag0 + f.flag_off : nullptr;
+      if (boundary_possible(f, bflag, xi)) {
+        if (a.bsdf) {
+          dist = boundary_distance(f, sdf, xi);
+        }
+        bd = boundary_sample(p, f, sdf, vol, xi);
+      }
     }
-    bd = boundary_sample(p, f, sdf, vol, xi);
+    bdata[t] = bd;
+    if (a.bsdf) a.bsdf[t] = dist;
   }
-  bdata[t] = bd;
-  if (a.bsdf) a.bsdf[t] = dist;
 }
 
 // LambdaCalculation (pressureConstrain.ts:31-85).  Writes xl[t] = (x*, lambda):
@@ -255,7 +321,7 @@ __global__ void __launch_bounds__(256, 3) k_boundary(SimParams p, FieldParams f,
 //            for trace capture.
 //   kMode 2: the learned start: the features go through the MLP in-warp
 //            (32 particles = two 16-row mma tiles) and lambda_hat replaces lambda.
-template <int kMode>
+template <int kMode, bool kBatch, bool kLoop>
 __global__ void __launch_bounds__(256) k_lambda(SimParams p, int have_field, const float4* __restrict__ bdata,
                                                 const float4* __restrict__ xs, uint32_t max_nbr,
                                                 const uint32_t* __restrict__ nbr_cnt,
@@ -263,8 +329,8 @@ __global__ void __launch_bounds__(256) k_lambda(SimParams p, int have_field, con
                                                 float4* __restrict__ xl, SolverAux a) {
   constexpr bool kFeat = kMode >= 1;
   if (a.guard && *a.guard == 0) return;
-  uint32_t t = blockIdx.x * blockDim.x + threadIdx.x;
   if constexpr (kMode == 2) {
+    // weights are staged once per CTA; the CTA then loops over its tiles
     __shared__ __align__(16) uint16_t sW1t[mlp::kH * mlp::kW1S];
     __shared__ __align__(16) uint16_t sW2t[mlp::kH * mlp::kW2S];
     __shared__ float sB1[mlp::kH], sB2[mlp::kH], sW3[mlp::kH];
@@ -276,258 +342,287 @@ __global__ void __launch_bounds__(256) k_lambda(SimParams p, int have_field, con
       sW3[q] = a.mlp[mlp::OFF_W3 + q];
     }
     __syncthreads();
-    const bool valid = t < p.n;
-    float fv[8] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
-    f3 xi = mk(0.f, 0.f, 0.f);
-    if (valid) {
-      xi = xyz(xs[t]);
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, g = lane >> 2, t4 = lane & 3;
+    PBF_TILES(p.n) {
+      const uint32_t t = tile0 + threadIdx.x;
+      const bool valid = t < p.n;
+      float fv[8] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
+      f3 xi = mk(0.f, 0.f, 0.f);
+      if (valid) {
+        xi = xyz(xs[t]);
+        uint32_t b, e;
+        list_slice(max_nbr, nbr_cnt, t, b, e);
+        float dens = 0.0f, div = 0.0f;
+        f3 vi = p.inv_dt * (xi - xyz(a.pos[t]));
+        for_each_neighbor(nbr_list, b, e, xs, [&](uint32_t j, float4 xj) {
+          Pair q = make_pair_of(xi - xyz(xj));
+          dens = dens + poly6_p(p, q);
+          f3 vj = p.inv_dt * (xyz(xj) - xyz(__ldg(a.pos + j)));
+          div = div + dot3(vj - vi, spiky_p(p, q));
+        });
+        dens = dens * p.V;
+        float vb = 0.0f;
+        if (have_field) {
+          float4 bd = bdata[t];
+          vb = bd.w;
+          if (bd.w != 0.0f) dens = dens + bd.w * poly6_p(p, make_pair_of(xi - xyz(bd)));
+        }
+        float sd = a.bsdf ? fminf(a.bsdf[t], 2.0f * p.h) : 2.0f * p.h;
+        fv[0] = dens - 1.0f;
+        fv[1] = a.lam_prev ? a.lam_prev[t] : 0.0f;
+        fv[2] = (float)e;
+        fv[3] = len3(vi) * p.dt / p.h;
+        fv[4] = p.V * div * p.dt;
+        fv[5] = sd / p.h;
+        fv[6] = vb / p.V;
+        fv[7] = a.substep_index;
+      }
+#pragma unroll
+      for (int k = 0; k < 8; ++k) sF[warp][lane][k] = valid ? (fv[k] - a.norm.mean[k]) * a.norm.inv_std[k] : 0.0f;
+      __syncwarp();
+#pragma unroll
+      for (int tile = 0; tile < 2; ++tile) {
+        const int r = 16 * tile + g;
+        float xg[2] = {sF[warp][r][2 * t4], sF[warp][r][2 * t4 + 1]};
+        float x8[2] = {sF[warp][r + 8][2 * t4], sF[warp][r + 8][2 * t4 + 1]};
+        mlp::Fwd F;
+        mlp::forward_tile(xg, x8, sW1t, sW2t, sB1, sB2, sW3, a.mlp[mlp::OFF_B3], F);
+        if (t4 == 0) {  // rows r and r + 8 of this warp: column 8 of sF is free
+          sF[warp][r][8] = F.y0 * a.norm.lam_scale;
+          sF[warp][r + 8][8] = F.y8 * a.norm.lam_scale;
+        }
+      }
+      __syncwarp();
+      if (valid) {
+        float l = sF[warp][lane][8];
+        xl[t] = f4(xi, l);
+        a.lam_sum[t] = l;
+      }
+      __syncwarp();  // sF is rewritten by the next tile
+    }
+  } else {
+    PBF_SLOTS(t, p.n) {
+      if (!iter_active(scene_of<kBatch>(a.tab, t), a.iter)) continue;
+      f3 xi = xyz(xs[t]);
       uint32_t b, e;
       list_slice(max_nbr, nbr_cnt, t, b, e);
-      float dens = 0.0f, div = 0.0f;
-      f3 vi = p.inv_dt * (xi - xyz(a.pos[t]));
+      f3 grad = mk(0.f, 0.f, 0.f);
+      float sum2 = 0.0f, dens = 0.0f, div = 0.0f;
+      f3 vi = mk(0.f, 0.f, 0.f);
+      if (kFeat) vi = p.inv_dt * (xi - xyz(a.pos[t]));
       for_each_neighbor(nbr_list, b, e, xs, [&](uint32_t j, float4 xj) {
         Pair q = make_pair_of(xi - xyz(xj));
+        f3 gk = spiky_p(p, q);
+        grad = grad + gk;
+        sum2 = sum2 + dot3(gk, gk);
         dens = dens + poly6_p(p, q);
-        f3 vj = p.inv_dt * (xyz(xj) - xyz(__ldg(a.pos + j)));
-        div = div + dot3(vj - vi, spiky_p(p, q));
+        if (kFeat) {
+          f3 vj = p.inv_dt * (xyz(xj) - xyz(__ldg(a.pos + j)));
+          div = div + dot3(vj - vi, gk);
+        }
       });
       dens = dens * p.V;
+      grad = p.V * grad;
+      sum2 = sum2 * p.V2;
       float vb = 0.0f;
       if (have_field) {
         float4 bd = bdata[t];
         vb = bd.w;
-        if (bd.w != 0.0f) dens = dens + bd.w * poly6_p(p, make_pair_of(xi - xyz(bd)));
+        if (bd.w != 0.0f) {
+          Pair q = make_pair_of(xi - xyz(bd));
+          f3 gk = bd.w * spiky_p(p, q);
+          grad = grad + gk;
+          dens = dens + bd.w * poly6_p(p, q);
+        }
       }
-      float sd = a.bsdf ? fminf(a.bsdf[t], 2.0f * p.h) : 2.0f * p.h;
-      fv[0] = dens - 1.0f;
-      fv[1] = a.lam_prev ? a.lam_prev[t] : 0.0f;
-      fv[2] = (float)e;
-      fv[3] = len3(vi) * p.dt / p.h;
-      fv[4] = p.V * div * p.dt;
-      fv[5] = sd / p.h;
-      fv[6] = vb / p.V;
-      fv[7] = a.substep_index;
-    }
-    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, g = lane >> 2, t4 = lane & 3;
-#pragma unroll
-    for (int k = 0; k < 8; ++k) sF[warp][lane][k] = valid ? (fv[k] - a.norm.mean[k]) * a.norm.inv_std[k] : 0.0f;
-    __syncwarp();
-#pragma unroll
-    for (int tile = 0; tile < 2; ++tile) {
-      const int r = 16 * tile + g;
-      float xg[2] = {sF[warp][r][2 * t4], sF[warp][r][2 * t4 + 1]};
-      float x8[2] = {sF[warp][r + 8][2 * t4], sF[warp][r + 8][2 * t4 + 1]};
-      mlp::Fwd F;
-      mlp::forward_tile(xg, x8, sW1t, sW2t, sB1, sB2, sW3, a.mlp[mlp::OFF_B3], F);
-      if (t4 == 0) {  // rows r and r + 8 of this warp: column 8 of sF is free
-        sF[warp][r][8] = F.y0 * a.norm.lam_scale;
-        sF[warp][r + 8][8] = F.y8 * a.norm.lam_scale;
-      }
-    }
-    __syncwarp();
-    if (valid) {
-      float l = sF[warp][lane][8];
-      xl[t] = f4(xi, l);
-      a.lam_sum[t] = l;
-    }
-    return;
-  } else {
-    if (t >= p.n) return;
-    f3 xi = xyz(xs[t]);
-    uint32_t b, e;
-    list_slice(max_nbr, nbr_cnt, t, b, e);
-    f3 grad = mk(0.f, 0.f, 0.f);
-    float sum2 = 0.0f, dens = 0.0f, div = 0.0f;
-    f3 vi = mk(0.f, 0.f, 0.f);
-    if (kFeat) vi = p.inv_dt * (xi - xyz(a.pos[t]));
-    for_each_neighbor(nbr_list, b, e, xs, [&](uint32_t j, float4 xj) {
-      Pair q = make_pair_of(xi - xyz(xj));
-      f3 gk = spiky_p(p, q);
-      grad = grad + gk;
-      sum2 = sum2 + dot3(gk, gk);
-      dens = dens + poly6_p(p, q);
+      float c = fmaxf(0.0f, dens - 1.0f);
+      float s = dot3(grad, grad) + sum2;
+      float lam = fdiv(-c, s + p.lambda_eps);
+      xl[t] = f4(xi, lam);
+      if (a.lam_sum) a.lam_sum[t] = a.lam_first ? lam : a.lam_sum[t] + lam;
       if (kFeat) {
-        f3 vj = p.inv_dt * (xyz(xj) - xyz(__ldg(a.pos + j)));
-        div = div + dot3(vj - vi, gk);
+        float sd = a.bsdf ? fminf(a.bsdf[t], 2.0f * p.h) : 2.0f * p.h;
+        a.feat[2 * t] = make_float4(dens - 1.0f, a.lam_prev ? a.lam_prev[t] : 0.0f, (float)e, len3(vi) * p.dt / p.h);
+        a.feat[2 * t + 1] = make_float4(p.V * div * p.dt, sd / p.h, vb / p.V, a.substep_index);
       }
-    });
-    dens = dens * p.V;
-    grad = p.V * grad;
-    sum2 = sum2 * p.V2;
-    float vb = 0.0f;
-    if (have_field) {
-      float4 bd = bdata[t];
-      vb = bd.w;
-      if (bd.w != 0.0f) {
-        Pair q = make_pair_of(xi - xyz(bd));
-        f3 gk = bd.w * spiky_p(p, q);
-        grad = grad + gk;
-        dens = dens + bd.w * poly6_p(p, q);
-      }
-    }
-    float c = fmaxf(0.0f, dens - 1.0f);
-    float s = dot3(grad, grad) + sum2;
-    float lam = fdiv(-c, s + p.lambda_eps);
-    xl[t] = f4(xi, lam);
-    if (a.lam_sum) a.lam_sum[t] = a.lam_first ? lam : a.lam_sum[t] + lam;
-    if (kFeat) {
-      float sd = a.bsdf ? fminf(a.bsdf[t], 2.0f * p.h) : 2.0f * p.h;
-      a.feat[2 * t] = make_float4(dens - 1.0f, a.lam_prev ? a.lam_prev[t] : 0.0f, (float)e, len3(vi) * p.dt / p.h);
-      a.feat[2 * t + 1] = make_float4(p.V * div * p.dt, sd / p.h, vb / p.V, a.substep_index);
     }
   }
 }
 
 // ConstrainSolve + ConstrainApply: x*_new = clamp(x* + 0.5 * dp) into the other
-// buffer; (x*_j, lambda_j) come packed from the lambda pass.
-__global__ void __launch_bounds__(256) k_deltap(SimParams p, SolverAux a, int have_field, const float4* __restrict__ xl,
-                                                const float4* __restrict__ bdata,
+// buffer; (x*_j, lambda_j) come packed from the lambda pass.  A scene of a
+// batch that has finished its iterations copies its x* through (a.xs_in), so
+// every scene ends in the same buffer.
+template <bool kBatch, bool kLoop>
+__global__ void __launch_bounds__(256) k_deltap(SimParams p, SolverAux a, int have_field,
+                                                const float4* __restrict__ xl, const float4* __restrict__ bdata,
                                                 uint32_t max_nbr, const uint32_t* __restrict__ nbr_cnt,
                                                 const uint32_t* __restrict__ nbr_list,
                                                 float4* __restrict__ xs_out, float4* __restrict__ dp_out) {
   if (a.guard && *a.guard == 0) return;
-  uint32_t t = blockIdx.x * blockDim.x + threadIdx.x;
-  if (t >= p.n) return;
-  const float4 xli = xl[t];
-  f3 xi = xyz(xli);
-  float li = xli.w;
-  uint32_t b, e;
-  list_slice(max_nbr, nbr_cnt, t, b, e);
-  f3 pu = mk(0.f, 0.f, 0.f);
-  for_each_neighbor(nbr_list, b, e, xl, [&](uint32_t, float4 xj) {
-    Pair q = make_pair_of(xi - xyz(xj));
-    pu = pu + (li + xj.w) * spiky_p(p, q);
-  });
-  pu = p.V * pu;
-  if (have_field) {
-    float4 bd = bdata[t];
-    if (bd.w != 0.0f) {
-      Pair q = make_pair_of(xi - xyz(bd));
-      pu = pu + (bd.w * li) * spiky_p(p, q);
+  PBF_SLOTS(t, p.n) {
+    if (!iter_active(scene_of<kBatch>(a.tab, t), a.iter)) {
+      xs_out[t] = a.xs_in[t];
+      continue;
+    }
+    const float4 xli = xl[t];
+    f3 xi = xyz(xli);
+    float li = xli.w;
+    uint32_t b, e;
+    list_slice(max_nbr, nbr_cnt, t, b, e);
+    f3 pu = mk(0.f, 0.f, 0.f);
+    for_each_neighbor(nbr_list, b, e, xl, [&](uint32_t, float4 xj) {
+      Pair q = make_pair_of(xi - xyz(xj));
+      pu = pu + (li + xj.w) * spiky_p(p, q);
+    });
+    pu = p.V * pu;
+    if (have_field) {
+      float4 bd = bdata[t];
+      if (bd.w != 0.0f) {
+        Pair q = make_pair_of(xi - xyz(bd));
+        pu = pu + (bd.w * li) * spiky_p(p, q);
+      }
+    }
+    f3 dp = 0.5f * pu;
+    if (dp_out) dp_out[t] = f4(dp, 0.0f);
+    if constexpr (kBatch) {  // the scene's own domain (looked up after the loop: no registers held across it)
+      SimParams ps = p;
+      scene_domain(ps, scene_of<kBatch>(a.tab, t));
+      xs_out[t] = f4(clamp_rand(ps, xi + dp), 0.0f);
+    } else {
+      xs_out[t] = f4(clamp_rand(p, xi + dp), 0.0f);
     }
   }
-  f3 dp = 0.5f * pu;
-  if (dp_out) dp_out[t] = f4(dp, 0.0f);
-  xs_out[t] = f4(clamp_rand(p, xi + dp), 0.0f);
 }
 
 // AttributeUpdate: rho = m * sum W (fluid only), v = (x* - x) / dt, x <- (x*, rho).
+template <bool kLoop>
 __global__ void __launch_bounds__(256) k_density_velocity(SimParams p, SolverAux a, const float4* __restrict__ xs,
                                                           uint32_t max_nbr,
                                                           const uint32_t* __restrict__ nbr_cnt,
                                                           const uint32_t* __restrict__ nbr_list,
                                                           float4* __restrict__ pos, float4* __restrict__ vel) {
   if (a.guard && *a.guard == 0) return;
-  uint32_t t = blockIdx.x * blockDim.x + threadIdx.x;
-  if (t >= p.n) return;
-  f3 xi = xyz(xs[t]);
-  uint32_t b, e;
-  list_slice(max_nbr, nbr_cnt, t, b, e);
-  float dens = 0.0f;
-  for_each_neighbor(nbr_list, b, e, xs, [&](uint32_t, float4 xj) {
-    Pair q = make_pair_of(xi - xyz(xj));
-    dens = dens + poly6_p(p, q);
-  });
-  float vsum = dens;
-  dens = dens * p.m;
-  f3 xo = xyz(pos[t]);
-  vel[t] = f4(p.inv_dt * (xi - xo), 0.0f);
-  pos[t] = f4(xi, dens);
-  if (a.stats) {
-    // per-step density error: compression max(0, rho/rho0 - 1) = max(0, V sum W - 1),
-    // warp-aggregated (lanes past n have returned)
-    float c = fmaxf(0.0f, vsum * p.V - 1.0f);
-    const unsigned m = __activemask();
-    unsigned fx = (unsigned)(fminf(c, 1.0f) * 1048576.0f);
-    unsigned wmax = __reduce_max_sync(m, __float_as_uint(c));
-    unsigned wsum = __reduce_add_sync(m, fx);
-    if ((threadIdx.x & 31u) == (unsigned)(__ffs(m) - 1)) {
-      atomicMax(&a.stats->max_bits, wmax);
-      atomicAdd(&a.stats->count, (unsigned)__popc(m));
-      atomicAdd(&a.stats->sum_fx, (unsigned long long)wsum);
+  PBF_SLOTS(t, p.n) {
+    f3 xi = xyz(xs[t]);
+    uint32_t b, e;
+    list_slice(max_nbr, nbr_cnt, t, b, e);
+    float dens = 0.0f;
+    for_each_neighbor(nbr_list, b, e, xs, [&](uint32_t, float4 xj) {
+      Pair q = make_pair_of(xi - xyz(xj));
+      dens = dens + poly6_p(p, q);
+    });
+    float vsum = dens;
+    dens = dens * p.m;
+    f3 xo = xyz(pos[t]);
+    vel[t] = f4(p.inv_dt * (xi - xo), 0.0f);
+    pos[t] = f4(xi, dens);
+    if (a.stats) {
+      // per-step density error: compression max(0, rho/rho0 - 1) = max(0, V sum W - 1),
+      // warp-aggregated over the lanes still in the loop
+      float c = fmaxf(0.0f, vsum * p.V - 1.0f);
+      const unsigned m = __activemask();
+      unsigned fx = (unsigned)(fminf(c, 1.0f) * 1048576.0f);
+      unsigned wmax = __reduce_max_sync(m, __float_as_uint(c));
+      unsigned wsum = __reduce_add_sync(m, fx);
+      if ((threadIdx.x & 31u) == (unsigned)(__ffs(m) - 1)) {
+        atomicMax(&a.stats->max_bits, wmax);
+        atomicAdd(&a.stats->count, (unsigned)__popc(m));
+        atomicAdd(&a.stats->sum_fx, (unsigned long long)wsum);
+      }
     }
   }
 }
 
 // VorticityConfinement: omega_i and the Akinci normal n_i.
+template <bool kLoop>
 __global__ void __launch_bounds__(256) k_vorticity(SimParams p, const float4* __restrict__ pos,
                                                    const float4* __restrict__ vel,
                                                    uint32_t max_nbr,
                                                    const uint32_t* __restrict__ nbr_cnt,
                                                    const uint32_t* __restrict__ nbr_list,
                                                    float4* __restrict__ omega, float4* __restrict__ normal) {
-  uint32_t t = blockIdx.x * blockDim.x + threadIdx.x;
-  if (t >= p.n) return;
-  f3 xi = xyz(pos[t]);
-  f3 vi = xyz(vel[t]);
-  uint32_t b, e;
-  list_slice(max_nbr, nbr_cnt, t, b, e);
-  f3 om = mk(0.f, 0.f, 0.f), nm = mk(0.f, 0.f, 0.f);
-  for_each_neighbor(nbr_list, b, e, pos, [&](uint32_t j, float4 pj) {
-    Pair q = make_pair_of(xi - xyz(pj));
-    f3 vd = xyz(__ldg(vel + j)) - vi;
-    float volume = fdiv(p.m, pj.w);
-    f3 gw = spiky_p(p, q);
-    om = om + volume * cross3(vd, gw);
-    nm = nm + volume * gw;
-  });
-  const float wl = len3(om);
-  omega[t] = f4(om, wl);
-  normal[t] = f4(p.h * nm, wl);  // w: |omega| again, so XSPH gathers one float4 per neighbour fewer
+  PBF_SLOTS(t, p.n) {
+    f3 xi = xyz(pos[t]);
+    f3 vi = xyz(vel[t]);
+    uint32_t b, e;
+    list_slice(max_nbr, nbr_cnt, t, b, e);
+    f3 om = mk(0.f, 0.f, 0.f), nm = mk(0.f, 0.f, 0.f);
+    for_each_neighbor(nbr_list, b, e, pos, [&](uint32_t j, float4 pj) {
+      Pair q = make_pair_of(xi - xyz(pj));
+      f3 vd = xyz(__ldg(vel + j)) - vi;
+      float volume = fdiv(p.m, pj.w);
+      f3 gw = spiky_p(p, q);
+      om = om + volume * cross3(vd, gw);
+      nm = nm + volume * gw;
+    });
+    const float wl = len3(om);
+    omega[t] = f4(om, wl);
+    normal[t] = f4(p.h * nm, wl);  // w: |omega| again, so XSPH gathers one float4 per neighbour fewer
+  }
 }
 
 // XSPH viscosity + vorticity confinement force + Akinci surface tension -> a.
+template <bool kLoop>
 __global__ void __launch_bounds__(256, 4) k_xsph(SimParams p, const float4* __restrict__ pos,
-                                              const float4* __restrict__ vel, const float4* __restrict__ omega,
-                                              const float4* __restrict__ normal,
-                                              uint32_t max_nbr,
-                                              const uint32_t* __restrict__ nbr_cnt,
-                                              const uint32_t* __restrict__ nbr_list,
-                                              float4* __restrict__ acc) {
-  uint32_t t = blockIdx.x * blockDim.x + threadIdx.x;
-  if (t >= p.n) return;
-  float4 pi = pos[t];
-  f3 xi = xyz(pi);
-  float ri = pi.w;
-  f3 vi = xyz(vel[t]);
-  f3 wi = xyz(omega[t]);
-  f3 ni = xyz(normal[t]);
-  uint32_t b, e;
-  list_slice(max_nbr, nbr_cnt, t, b, e);
-  f3 vu = mk(0.f, 0.f, 0.f), eta = mk(0.f, 0.f, 0.f), ten = mk(0.f, 0.f, 0.f);
-  for_each_neighbor(nbr_list, b, e, pos, [&](uint32_t j, float4 pj) {
-    float rj = pj.w;
-    Pair q = make_pair_of(xi - xyz(pj));
-    f3 vd = xyz(__ldg(vel + j)) - vi;
-    float kij = fdiv(p.two_rho0, ri + rj);
-    vu = vu + fdiv3(poly6_p(p, q) * vd, rj);
-    const float4 nj = __ldg(normal + j);  // (normal_j, |omega_j|)
-    eta = eta + fdiv3(nj.w * spiky_p(p, q), rj);
-    f3 coh = p.m * cohesion_p(p, q);
-    f3 curv = ni - xyz(nj);
-    ten = ten - kij * (coh + curv);
-  });
-  float el = len3(eta);
-  f3 en = (el > 0.0f) ? divs(eta, el) : mk(0.f, 0.f, 0.f);
-  float sx = p.xsph * p.inv_dt * p.m;
-  f3 a = (sx * vu + p.vorticity * cross3(en, wi)) + p.tension * ten;
-  acc[t] = f4(a, 0.0f);
+                                                 const float4* __restrict__ vel, const float4* __restrict__ omega,
+                                                 const float4* __restrict__ normal,
+                                                 uint32_t max_nbr,
+                                                 const uint32_t* __restrict__ nbr_cnt,
+                                                 const uint32_t* __restrict__ nbr_list,
+                                                 float4* __restrict__ acc) {
+  PBF_SLOTS(t, p.n) {
+    float4 pi = pos[t];
+    f3 xi = xyz(pi);
+    float ri = pi.w;
+    f3 vi = xyz(vel[t]);
+    f3 wi = xyz(omega[t]);
+    f3 ni = xyz(normal[t]);
+    uint32_t b, e;
+    list_slice(max_nbr, nbr_cnt, t, b, e);
+    f3 vu = mk(0.f, 0.f, 0.f), eta = mk(0.f, 0.f, 0.f), ten = mk(0.f, 0.f, 0.f);
+    for_each_neighbor(nbr_list, b, e, pos, [&](uint32_t j, float4 pj) {
+      float rj = pj.w;
+      Pair q = make_pair_of(xi - xyz(pj));
+      f3 vd = xyz(__ldg(vel + j)) - vi;
+      float kij = fdiv(p.two_rho0, ri + rj);
+      vu = vu + fdiv3(poly6_p(p, q) * vd, rj);
+      const float4 nj = __ldg(normal + j);  // (normal_j, |omega_j|)
+      eta = eta + fdiv3(nj.w * spiky_p(p, q), rj);
+      f3 coh = p.m * cohesion_p(p, q);
+      f3 curv = ni - xyz(nj);
+      ten = ten - kij * (coh + curv);
+    });
+    float el = len3(eta);
+    f3 en = (el > 0.0f) ? divs(eta, el) : mk(0.f, 0.f, 0.f);
+    float sx = p.xsph * p.inv_dt * p.m;
+    f3 av = (sx * vu + p.vorticity * cross3(en, wi)) + p.tension * ten;
+    acc[t] = f4(av, 0.0f);
+  }
 }
 
-// Launch table for this precision variant.
+// Launch table for this precision variant: [batch][persistent] pass sets.
+template <bool B, bool P>
+void fill_set(PassSet* ps) {
+  ps->predict = k_predict<B, P>;
+  ps->nbr_build = k_nbr_build<B, P>;
+  ps->boundary = k_boundary<B, P>;
+  ps->lambda = k_lambda<0, B, P>;
+  ps->lambda_feat = B ? nullptr : k_lambda<1, false, P>;
+  ps->lambda_learned = B ? nullptr : k_lambda<2, false, P>;
+  ps->deltap = k_deltap<B, P>;
+  ps->density_velocity = k_density_velocity<P>;
+  ps->vorticity = k_vorticity<P>;
+  ps->xsph = k_xsph<P>;
+}
+
 void fill_pass_table(PassTable* tbl) {
-  tbl->predict = k_predict;
   tbl->nbr_count = k_nbr_count;
   tbl->nbr_list = k_nbr_list;
-  tbl->nbr_build = k_nbr_build;
-  tbl->boundary = k_boundary;
-  tbl->lambda = k_lambda<0>;
-  tbl->lambda_feat = k_lambda<1>;
-  tbl->lambda_learned = k_lambda<2>;
-  tbl->deltap = k_deltap;
-  tbl->density_velocity = k_density_velocity;
-  tbl->vorticity = k_vorticity;
-  tbl->xsph = k_xsph;
+  fill_set<false, false>(&tbl->set[0][0]);
+  fill_set<false, true>(&tbl->set[0][1]);
+  fill_set<true, false>(&tbl->set[1][0]);
+  fill_set<true, true>(&tbl->set[1][1]);
 }
 
 }  // namespace PBF_NS

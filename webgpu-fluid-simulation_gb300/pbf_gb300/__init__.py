@@ -5,8 +5,8 @@ reference presets and the benchmark workloads.  All compute runs in
 libpbf_gb300.so (CUDA, sm_103a).
 """
 from . import _lib
-from .simulator import PBF, NeighborSearch, exclusive_scan
+from .simulator import PBF, PBFBatch, NeighborSearch, exclusive_scan
 from .simulator import mlp_init, mlp_params, mlp_fit_normalization, mlp_forward, mlp_gradient, mlp_train
 from . import scenes
 
-__all__ = ["PBF", "NeighborSearch", "exclusive_scan", "scenes", "_lib"]
+__all__ = ["PBF", "PBFBatch", "NeighborSearch", "exclusive_scan", "scenes", "_lib"]

@@ -74,6 +74,28 @@ class Grid(ctypes.Structure):
     _fields_ = [("origin", f32 * 3), ("inv_cell", f32 * 3), ("dim", u32 * 3)]
 
 
+class Launch(ctypes.Structure):
+    _fields_ = [("block", u32), ("ctas_per_sm", u32), ("cell_ratio", f32)]
+
+
+class TuneTrial(ctypes.Structure):
+    _fields_ = [("launch", Launch), ("ms_per_substep", f32)]
+
+
+TUNE_CELL_RATIO = 0x1
+
+
+class Scene(ctypes.Structure):
+    _fields_ = [("struct_size", u32), ("particles", u32), ("positions", ctypes.POINTER(f32)),
+                ("domain_min", f32 * 3), ("domain_max", f32 * 3), ("iterations", u32), ("field_res", u32 * 3),
+                ("field_origin", f32 * 3), ("field_extent", f32 * 3), ("sdf", ctypes.POINTER(f32)),
+                ("volume", ctypes.POINTER(f32))]
+
+
+class SceneInfo(ctypes.Structure):
+    _fields_ = [("first_id", u32), ("particles", u32), ("iterations", u32), ("grid_dim", u32 * 3), ("cells", u32)]
+
+
 # Every symbol the header declares, with (restype, argtypes).
 _P = ctypes.c_void_p
 _FP = ctypes.POINTER(ctypes.c_float)
@@ -136,6 +158,13 @@ SIGNATURES = {
     "pbf_copy_trace": (ctypes.c_int, [_P, _FP, _FP, u32]),
     "pbf_trace_error": (ctypes.c_int, [_P, _FP, _FP]),
     "pbf_set_learned": (ctypes.c_int, [_P, ctypes.POINTER(MLP), u32, ctypes.c_float]),
+    "pbf_set_launch": (ctypes.c_int, [_P, ctypes.POINTER(Launch)]),
+    "pbf_get_launch": (ctypes.c_int, [_P, ctypes.POINTER(Launch)]),
+    "pbf_autotune": (ctypes.c_int, [_P, u32, u32, ctypes.POINTER(TuneTrial), u32, _UP, ctypes.POINTER(Launch)]),
+    "pbf_batch_create": (ctypes.c_int, [ctypes.POINTER(Config), ctypes.POINTER(Scene), u32, ctypes.POINTER(_P)]),
+    "pbf_scene_count": (u32, [_P]),
+    "pbf_get_scene_info": (ctypes.c_int, [_P, u32, ctypes.POINTER(SceneInfo)]),
+    "pbf_get_scene_metrics": (ctypes.c_int, [_P, u32, ctypes.POINTER(Metrics)]),
 }
 
 _lib = None

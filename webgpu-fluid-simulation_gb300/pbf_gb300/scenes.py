@@ -256,6 +256,67 @@ def sphere_drop_spec(nx=128, ny=64, nz=128, field_res=(128, 128, 128)):
     return cfg, pts, field_args
 
 
+BATCH_BOUNDARIES = ("box", "box+sphere", "box+cylinder")
+
+
+def batch_scenes_spec(count=64, n_min=4096, n_max=262144, seed=3, field_res=(64, 64, 64)):
+    """Independent scenes for one batch: particle counts log-uniform in
+    [n_min, n_max] (seeded), each a jittered block (spacing 2r, r = 0.0125,
+    h = 4r) in the corner of its own box (a dam break), the box with nothing
+    inside, a sphere resting on the floor, or a vertical cylinder (pillar),
+    each boundary a volume map of `field_res` cells over the box, and 3 or 4
+    solver iterations.  Returns (shared config, scene dicts without fields,
+    field arguments per scene)."""
+    rng = np.random.default_rng(seed)
+    r = 0.0125
+    d = 2 * r
+    cfg = base_config(particle_radius=r, kernel_radius=4 * r, time_step=np.float32(1.0 / 300.0), substeps=2,
+                      max_particles=1,
+                      options=dict(iterations=4, xsph=0.01, vorticity=5e-4, surface_tension=0.1, gravity=9.8))
+    cfg.max_neighbors = 96
+    counts = np.rint(np.exp(rng.uniform(np.log(n_min), np.log(n_max), size=count))).astype(np.int64)
+    kinds = rng.integers(0, len(BATCH_BOUNDARIES), size=count)
+    iters = rng.integers(3, 5, size=count)
+    scenes, fields = [], []
+    for i in range(count):
+        n = int(counts[i])
+        m = int(np.ceil(n ** (1.0 / 3.0)))
+        ny = int(np.ceil(n / (m * m)))
+        # block [d/2 + d/4, ...) so that the lattice keeps off the walls
+        ext = np.array([2.0 * m * d + 4 * d, 1.6 * ny * d + 4 * d, 1.25 * m * d + 4 * d])
+        ext = np.maximum(ext, 8 * 4 * r)
+        idx = np.arange(m * m * ny)[:n]
+        # x fastest within a layer, layers bottom-up, so a partial top layer stays on top
+        ix, iz, iy = idx % m, (idx // m) % m, idx // (m * m)
+        pts = np.stack([r + d * ix + d, r + d * iy + d, r + d * iz + d], axis=1).astype(np.float32)
+        pts = jitter(np.concatenate([pts, np.zeros((n, 1), np.float32)], axis=1), 0.1 * r, seed=seed * 1000 + i)
+        box = (L.SHAPE_BOX_CONTAINER, tuple(ext / 2), tuple(ext / 2))
+        shapes = [box]
+        kind = BATCH_BOUNDARIES[int(kinds[i])]
+        if kind == "box+sphere":
+            rad = 0.2 * min(ext[0], ext[2])
+            shapes.append((L.SHAPE_SPHERE, (0.75 * ext[0], 0.0, 0.5 * ext[2]), (rad, 0.0, 0.0)))
+        elif kind == "box+cylinder":
+            rad = 0.1 * min(ext[0], ext[2])
+            shapes.append((L.SHAPE_CYLINDER, (0.75 * ext[0], 0.5 * ext[1], 0.5 * ext[2]), (rad, ext[1], 0.0)))
+        scenes.append(dict(positions=pts, domain_min=(0.0, 0.0, 0.0), domain_max=tuple(float(v) for v in ext),
+                           iterations=int(iters[i]), boundary=kind))
+        fields.append(dict(shapes=shapes, res=field_res, origin=(0.0, 0.0, 0.0), extent=tuple(float(v) for v in ext),
+                           h=4 * r))
+    return cfg, scenes, fields
+
+
+def build_batch(spec, quadrature=8, backend="gpu"):
+    """Scene dicts of a batch spec with their volume maps generated."""
+    cfg, scenes, fields = spec
+    out = []
+    for sc, fa in zip(scenes, fields):
+        f = generate_field(fa["shapes"], fa["res"], fa["origin"], fa["extent"], fa["h"], quadrature=quadrature,
+                           backend=backend)
+        out.append(dict(sc, field=f))
+    return cfg, out
+
+
 def build_scene(spec, quadrature=12, backend="gpu", name="scene", frames=1):
     cfg, pts, fa = spec
     field = generate_field(fa["shapes"], fa["res"], fa["origin"], fa["extent"], fa["h"], quadrature=quadrature,

@@ -273,6 +273,93 @@ class PBF:
         the same read-back plus the step metrics."""
         return {"acceleration": self.copy_field(L.FIELD_ACCELERATION), "metrics": self.metrics()}
 
+    # ---- launch shape and autotuner (no reference counterpart) -------------
+    def set_launch(self, block=256, ctas_per_sm=0, cell_ratio=1.0):
+        lc = L.Launch(int(block), int(ctas_per_sm), float(cell_ratio))
+        self._check(self._lib.pbf_set_launch(self._h, ctypes.byref(lc)), "set_launch")
+
+    def launch(self):
+        lc = L.Launch()
+        self._check(self._lib.pbf_get_launch(self._h, ctypes.byref(lc)), "get_launch")
+        return {"block": lc.block, "ctas_per_sm": lc.ctas_per_sm, "cell_ratio": lc.cell_ratio}
+
+    def autotune(self, substeps=4, cell_ratio=False):
+        """Times every candidate launch shape on the current state (restored
+        afterwards) and keeps the fastest; returns (best, trials)."""
+        trials = (L.TuneTrial * 32)()
+        cnt = ctypes.c_uint32()
+        best = L.Launch()
+        flags = L.TUNE_CELL_RATIO if cell_ratio else 0
+        self._check(self._lib.pbf_autotune(self._h, int(substeps), flags, trials, 32, ctypes.byref(cnt),
+                                           ctypes.byref(best)), "autotune")
+        as_dict = lambda lc: {"block": lc.block, "ctas_per_sm": lc.ctas_per_sm, "cell_ratio": lc.cell_ratio}
+        return as_dict(best), [dict(as_dict(t.launch), ms_per_substep=t.ms_per_substep)
+                               for t in trials[:min(cnt.value, 32)]]
+
+    # ---- scenes (a batch handle holds many; a single handle holds one) ---------
+    def scene_count(self):
+        return int(self._lib.pbf_scene_count(self._h))
+
+    def scene_info(self, s):
+        si = L.SceneInfo()
+        self._check(self._lib.pbf_get_scene_info(self._h, int(s), ctypes.byref(si)), "scene_info")
+        return {"first_id": si.first_id, "particles": si.particles, "iterations": si.iterations,
+                "grid_dim": tuple(si.grid_dim), "cells": si.cells}
+
+    def scene_metrics(self, s):
+        m = L.Metrics()
+        self._check(self._lib.pbf_get_scene_metrics(self._h, int(s), ctypes.byref(m)), "scene_metrics")
+        return {k: getattr(m, k) for k, _ in L.Metrics._fields_}
+
+
+class PBFBatch(PBF):
+    """Many independent scenes stepped together, one launch per pass
+    (pbf_batch_create).  `scenes` is a list of dicts with keys
+    positions ((n, 3|4) float32), domain_min, domain_max, and optionally
+    iterations and field (dict with res, origin, extent, sdf, vol)."""
+
+    def __init__(self, config, scenes):
+        self._lib = L.load()
+        cfg = config
+        cfg.struct_size = ctypes.sizeof(L.Config)
+        self.config = cfg
+        arr = (L.Scene * len(scenes))()
+        self._keep = []
+        for i, sc in enumerate(scenes):
+            x = np.asarray(sc["positions"], dtype=np.float32)
+            if x.shape[1] == 3:
+                x = np.concatenate([x, np.zeros((x.shape[0], 1), np.float32)], axis=1)
+            x = np.ascontiguousarray(x)
+            self._keep.append(x)
+            d = arr[i]
+            d.struct_size = ctypes.sizeof(L.Scene)
+            d.particles = x.shape[0]
+            d.positions = x.ctypes.data_as(ctypes.POINTER(ctypes.c_float))
+            d.domain_min[:] = [float(v) for v in sc["domain_min"]]
+            d.domain_max[:] = [float(v) for v in sc["domain_max"]]
+            d.iterations = int(sc.get("iterations", 0))
+            f = sc.get("field")
+            if f is not None:
+                sdf = np.ascontiguousarray(f["sdf"], dtype=np.float32)
+                vol = np.ascontiguousarray(f["vol"], dtype=np.float32)
+                self._keep += [sdf, vol]
+                d.field_res[:] = [int(v) for v in f["res"]]
+                d.field_origin[:] = [float(v) for v in f["origin"]]
+                d.field_extent[:] = [float(v) for v in f["extent"]]
+                d.sdf = sdf.ctypes.data_as(ctypes.POINTER(ctypes.c_float))
+                d.volume = vol.ctypes.data_as(ctypes.POINTER(ctypes.c_float))
+        h = ctypes.c_void_p()
+        rc = self._lib.pbf_batch_create(ctypes.byref(cfg), arr, len(scenes), ctypes.byref(h))
+        self._keep = None
+        if rc:
+            raise L.PBFError(rc, "pbf_batch_create failed")
+        self._h = h
+
+    def scene_positions(self, s):
+        info = self.scene_info(s)
+        x = self.positions()
+        return x[info["first_id"]:info["first_id"] + info["particles"]]
+
 
 class NeighborSearch:
     """Stand-alone hash-grid search (NeighborSearch.execute, neighborSearch.ts:270-301)

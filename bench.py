@@ -535,16 +535,21 @@ def learned_arm(args, sc, snap, model, train_info, dist, plain_value):
                            "from the same input state" if args.bound is None else "--bound"}
     out.update(_timed_learned(args, sc, snap, model, 2, bound, dist))
     out["speedup_vs_plain"] = out["value"] / plain_value
-    one = _timed_learned(args, sc, snap, model, 1, bound, dist)
-    out["one_iteration"] = {"value": one["value"], "speedup_vs_plain": one["value"] / plain_value,
-                            "fallback_substeps": one["fallback_substeps"]}
+    for name, li in (("one_iteration", 1), ("zero_iterations", 0)):
+        r = _timed_learned(args, sc, snap, model, li, bound, dist)
+        out[name] = {"value": r["value"], "speedup_vs_plain": r["value"] / plain_value,
+                     "fallback_substeps": r["fallback_substeps"], "timed_substeps": r["timed_substeps"],
+                     "passes_ms": r["passes_ms"]}
     e_l2, fb2 = _errors_from(sc, snap, frames, model=model, learned_iters=2, bound=bound)
     e_l1, fb1 = _errors_from(sc, snap, frames, model=model, learned_iters=1, bound=bound)
+    e_l0, fb0 = _errors_from(sc, snap, frames, model=model, learned_iters=0, bound=bound)
     e_n2, _ = _errors_from(sc, snap, frames, model=model, learned_iters=2)
+    e_n0, _ = _errors_from(sc, snap, frames, model=model, learned_iters=0)
     w = lambda e: {"mean": float(e[window].mean()), "max_step": float(e[window].max())}
     out["density_error_same_window"] = {"plain4": w(e_plain), "plain2": w(e_plain2),
                                         "learned2_with_fallback": w(e_l2), "learned1_with_fallback": w(e_l1),
-                                        "learned2_network_only": w(e_n2)}
+                                        "learned0_with_fallback": w(e_l0), "learned2_network_only": w(e_n2),
+                                        "learned0_network_only": w(e_n0)}
     return out
 
 

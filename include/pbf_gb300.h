@@ -336,7 +336,11 @@ int pbf_copy_trace(pbf_handle* h, float* feat, float* target, uint32_t rows);
  * the learned start's fallback test uses; its largest value is the bound at
  * which the learned start matches the plain solve's worst error). */
 int pbf_trace_error(pbf_handle* h, float* max_mean, float* avg_mean);
-/* model = NULL switches the learned start off.  A negative bound makes every
+/* Learned start: each substep projects once with the network's multipliers,
+ * then runs `iterations` plain iterations (0 allowed); a substep whose mean
+ * compression after the solve exceeds fallback_bound is re-solved on the
+ * device with the plain solve from the same predicted positions.
+ * model = NULL switches the learned start off.  A negative bound makes every
  * substep fall back (the result is then the plain solve's). */
 int pbf_set_learned(pbf_handle* h, const pbf_mlp* model, uint32_t iterations, float fallback_bound);
 

@@ -164,3 +164,26 @@ def test_learned_start_gain_over_plain_two_iterations():
     assert ml["nonfinite"] == 0
     assert e4 < e2
     assert el < e2  # the network's start beats the method without it at equal iterations
+
+
+@pytest.mark.parametrize("bound", [-1.0, 1e9])
+def test_learned_graph_replay_matches_eager(bound):
+    """The learned substep (network pass, projection, iterations, the
+    cooperative fallback kernel) replayed from a CUDA graph gives the eager
+    results bit for bit, with the fallback taken every substep and never."""
+    sc = scenes.reference_scene("boundary_small", fp_mode=L.FP_EXACT)
+    pts = scenes.jitter(sc.particles, 0.001, seed=12)
+    f = sc.field
+    m, _, _ = random_model(9)
+    out = []
+    for graph in (False, True):
+        s = PBF(sc.config)
+        s.set_particles(pts)
+        s.set_boundary_field(f["res"], f["origin"], f["extent"], f["sdf"], f["vol"])
+        s.set_learned(m, iterations=1, fallback_bound=bound)
+        s.enable_graph(graph)
+        s.step(4)
+        out.append((s.positions(), s.velocities(), s.metrics()["fallback_steps"]))
+        s.close()
+    assert np.array_equal(out[0][0], out[1][0]) and np.array_equal(out[0][1], out[1][1])
+    assert out[0][2] == out[1][2] == (4 * sc.config.substeps if bound < 0 else 0)

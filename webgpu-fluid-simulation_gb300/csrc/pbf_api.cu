@@ -98,6 +98,7 @@ struct pbf_handle {
   uint32_t per_sm = 0;      // grid_cap / SM count as set by the caller
   float cell_ratio = 1.0f;  // grid cell edge / h
   int sms = 152;            // SM count of the device
+  unsigned fb_grid = 0;     // CTAs of the cooperative fallback kernel (resident wave)
   // batched scenes (pbf_batch_create)
   bool batch = false;
   std::vector<pbf_scene_info> scene_info;
@@ -115,10 +116,11 @@ namespace {
 
 enum PassId {
   K_PREDICT, K_SORT, K_GATHER, K_NBR_BUILD, K_BOUNDARY, K_LAMBDA, K_DELTAP, K_DENSITY, K_VORTICITY, K_XSPH,
-  K_EXPORT, K_FEATURES, K_MLP, K_NUM
+  K_EXPORT, K_FEATURES, K_MLP, K_FALLBACK, K_NUM
 };
 const char* kPassNames[K_NUM] = {"predict",   "sort", "gather", "nbr_build", "boundary",     "lambda", "deltap_apply",
-                                 "density_velocity", "vorticity", "xsph", "export", "features_mlp", "mlp"};
+                                 "density_velocity", "vorticity", "xsph", "export", "features", "mlp",
+                                 "fallback_guarded"};
 
 // Brackets one launch (or one group of launches) with events when timing is on.
 struct KScope {
@@ -350,23 +352,30 @@ int substep(pbf_handle* h, cudaEvent_t* ev) {
   h->cur = nx;
   const int cc = nx;
   // NeighborCount + NeighborList in one pass (fixed per-particle slices: no scan)
+  const FieldParams f = h->fp;
+  const uint32_t ms = h->nbr_slice;
+  const float sub_index = (float)(h->substep_counter % h->cfg.substeps);
   {
     KScope ks(h, K_NBR_BUILD);
-    ps.nbr_build<<<grid_of(h, n), h->blk, 0, st>>>(p, g, h->tab, h->xs[0].p, h->cell_start.p, h->nbr_slice,
-                                                           h->nbr_list.p, h->nbr_count.p, h->nbr_max.p, h->err_word.p);
+    ps.nbr_build<<<grid_of(h, n), h->blk, 0, st>>>(p, g, h->tab, h->xs[0].p, h->cell_start.p, ms, h->nbr_list.p,
+                                                    h->nbr_count.p, h->nbr_max.p, h->err_word.p);
   }
   CU(h, cudaGetLastError());
   if (ev) CU(h, cudaEventRecord(ev[2], st));
   // constraint loop
-  const FieldParams f = h->fp;
-  const uint32_t ms = h->nbr_slice;
-  const float sub_index = (float)(h->substep_counter % h->cfg.substeps);
   // `iters` plain iterations starting from xs[a]; returns the buffer holding
   // the result.  aux0 is used by the first iteration's lambda pass (features
   // and/or starting lam_sum), stats by the last one; guard makes every
   // launch conditional on the device flag (fallback path).
+  // Guarded launches (the learned start's fallback re-solve, normally a
+  // no-op) use the persistent variants with one wave of CTAs, so that an
+  // unset flag costs one short wave instead of a full grid.
+  const PassSet& pg = h->passes.set[h->batch ? 1 : 0][1];
+  const unsigned guard_grid = std::min(nblocks(n, h->blk), (unsigned)h->sms * (2048u / (unsigned)h->blk));
   auto iterate = [&](int a, uint32_t iters, bool feat_first, bool lam_sum_on, bool first_starts_sum,
                      SolveStats* stats, const int* guard, int* rc) -> int {
+    const PassSet& pi = guard ? pg : ps;
+    const unsigned gi = guard ? guard_grid : grid_of(h, n);
     for (uint32_t it = 0; it < iters; ++it) {
       SolverAux ab{};
       ab.guard = guard;
@@ -374,10 +383,8 @@ int substep(pbf_handle* h, cudaEvent_t* ev) {
       ab.iter = (int)it;
       if (need_feat && feat_first && it == 0) ab.bsdf = h->bsdf.p;
       if (f.loaded) {
-        KScope ks(h, K_BOUNDARY);
-        ps.boundary<<<grid_of(h, n), h->blk, 0, st>>>(
-            p, f, h->sdf.p, h->vol.p, h->bflag.p, h->xs[a].p,
-                                                             h->bdata.p, ab);
+        KScope ks(h, guard ? K_FALLBACK : K_BOUNDARY);
+        pi.boundary<<<gi, h->blk, 0, st>>>(p, f, h->sdf.p, h->vol.p, h->bflag.p, h->xs[a].p, h->bdata.p, ab);
       }
       if (cudaGetLastError() != cudaSuccess) { *rc = PBF_ECUDA; return a; }
       SolverAux al{};
@@ -398,10 +405,10 @@ int substep(pbf_handle* h, cudaEvent_t* ev) {
         al.substep_index = sub_index;
       }
       {
-        KScope ks(h, K_LAMBDA);
-        auto kl = fe ? ps.lambda_feat : ps.lambda;
-        kl<<<grid_of(h, n), h->blk, 0, st>>>(p, f.loaded, h->bdata.p, h->xs[a].p, ms, h->nbr_count.p,
-                                             h->nbr_list.p, h->xl.p, al);
+        KScope ks(h, guard ? K_FALLBACK : K_LAMBDA);
+        auto kl = fe ? pi.lambda_feat : pi.lambda;
+        kl<<<gi, h->blk, 0, st>>>(p, f.loaded, h->bdata.p, h->xs[a].p, ms, h->nbr_count.p, h->nbr_list.p, h->xl.p,
+                                  al);
       }
       if (cudaGetLastError() != cudaSuccess) { *rc = PBF_ECUDA; return a; }
       SolverAux ad{};
@@ -410,11 +417,9 @@ int substep(pbf_handle* h, cudaEvent_t* ev) {
       ad.iter = (int)it;
       ad.xs_in = h->xs[a].p;
       {
-        KScope ks(h, K_DELTAP);
-        ps.deltap<<<grid_of(h, n), h->blk, 0, st>>>(
-            p, ad, f.loaded, h->xl.p, h->bdata.p,
-                                                           ms, h->nbr_count.p, h->nbr_list.p,
-                                                           h->xs[1 - a].p, h->capture ? h->dp.p : nullptr);
+        KScope ks(h, guard ? K_FALLBACK : K_DELTAP);
+        pi.deltap<<<gi, h->blk, 0, st>>>(p, ad, f.loaded, h->xl.p, h->bdata.p, ms, h->nbr_count.p, h->nbr_list.p,
+                                         h->xs[1 - a].p, h->capture ? h->dp.p : nullptr);
       }
       if (cudaGetLastError() != cudaSuccess) { *rc = PBF_ECUDA; return a; }
       a = 1 - a;
@@ -424,15 +429,16 @@ int substep(pbf_handle* h, cudaEvent_t* ev) {
   };
   int a = 0, rc = PBF_OK;
   if (h->learned) {
-    // learned start: features at x*_0 -> lambda_hat -> one projection ->
-    // learned_iters plain iterations -> device-side fallback test
+    // learned start: boundary and features at x*_0 -> network -> (x*_0,
+    // lambda_hat) -> one projection -> learned_iters plain iterations ->
+    // device-side fallback test
     CU(h, cudaMemcpyAsync(h->xs_save.p, h->xs[0].p, (size_t)n * sizeof(float4), cudaMemcpyDeviceToDevice, st));
     SolverAux ab{};
     ab.bsdf = h->bsdf.p;
     if (f.loaded) {
       KScope ks(h, K_BOUNDARY);
-      ps.boundary<<<grid_of(h, n), h->blk, 0, st>>>(p, f, h->sdf.p, h->vol.p, h->bflag.p, h->xs[0].p,
-                                                           h->bdata.p, ab);
+      ps.boundary<<<grid_of(h, n), h->blk, 0, st>>>(p, f, h->sdf.p, h->vol.p, h->bflag.p, h->xs[0].p, h->bdata.p,
+                                                     ab);
     }
     CU(h, cudaGetLastError());
     SolverAux al{};
@@ -440,20 +446,18 @@ int substep(pbf_handle* h, cudaEvent_t* ev) {
     al.lam_prev = h->lam_prev.p;
     al.bsdf = f.loaded ? h->bsdf.p : nullptr;
     al.substep_index = sub_index;
-    al.lam_sum = h->lam_sum.p;
-    al.mlp = h->mlp_params.p;
-    for (int k = 0; k < 8; ++k) {
-      al.norm.mean[k] = h->model.feat_mean[k];
-      al.norm.inv_std[k] = h->model.feat_inv_std[k];
-    }
-    al.norm.lam_scale = h->model.lam_scale;
+    al.feat = h->feat.p;
     {
       KScope ks(h, K_FEATURES);
-      ps.lambda_learned<<<grid_of(h, n), h->blk, 0, st>>>(p, f.loaded, h->bdata.p, h->xs[0].p,
-                                                                 ms, h->nbr_count.p, h->nbr_list.p,
-                                                                 h->xl.p, al);
+      ps.features<<<grid_of(h, n), h->blk, 0, st>>>(p, f.loaded, h->bdata.p, h->xs[0].p, ms, h->nbr_count.p,
+                                                     h->nbr_list.p, al);
     }
     CU(h, cudaGetLastError());
+    {
+      KScope ks(h, K_MLP);
+      CU(h, launch_mlp_infer(h->mlp_params.p, h->model, (const float*)h->feat.p, n, nullptr, h->lam_sum.p, st,
+                             h->xs[0].p, h->xl.p));
+    }
     {
       KScope ks(h, K_DELTAP);
       SolverAux ad{};
@@ -492,18 +496,39 @@ int substep(pbf_handle* h, cudaEvent_t* ev) {
   if (rec) CU(h, launch_stats_record(h->stats.p, h->trace_err.p, st));
   if (h->learned) {
     CU(h, launch_fallback_decide(h->stats.p, h->fallback_bound, h->fb_flag.p, h->fb_count.p, h->fb_mean.p, st));
-    // guarded plain re-solve from x*_0 (every launch is a no-op unless the flag is set)
-    const int* fl = h->fb_flag.p;
-    CU(h, launch_copy_guarded(n, fl, h->pos_save.p, h->pos[cc].p, st));
-    CU(h, launch_copy_guarded(n, fl, h->xs_save.p, h->xs[0].p, st));
-    int b = iterate(0, h->cfg.options.iterations, false, true, true, nullptr, fl, &rc);
-    if (rc) return fail(h, rc, "fallback solve launch failed");
-    if (b != a) CU(h, launch_copy_guarded(n, fl, h->xs[b].p, h->xs[a].p, st));
-    SolverAux ag{};
-    ag.guard = fl;
-    ps.density_velocity<<<grid_of(h, n), h->blk, 0, st>>>(p, ag, h->xs[a].p, ms, h->nbr_count.p,
-                                                                 h->nbr_list.p, h->pos[cc].p, h->vel.p);
-    CU(h, cudaGetLastError());
+    // plain re-solve from x*_0 when the flag is set: one cooperative kernel
+    // (returns at once otherwise)
+    KScope ks(h, K_FALLBACK);
+    FallbackArgs fa{};
+    fa.p = p;
+    fa.f = f;
+    fa.guard = h->fb_flag.p;
+    fa.sdf = h->sdf.p;
+    fa.vol = h->vol.p;
+    fa.bflag = h->bflag.p;
+    fa.pos_save = h->pos_save.p;
+    fa.xs_save = h->xs_save.p;
+    fa.pos = h->pos[cc].p;
+    fa.vel = h->vel.p;
+    fa.xs0 = h->xs[0].p;
+    fa.xs1 = h->xs[1].p;
+    fa.xl = h->xl.p;
+    fa.bdata = h->bdata.p;
+    fa.lam_sum = h->lam_sum.p;
+    fa.nbr_cnt = h->nbr_count.p;
+    fa.nbr_list = h->nbr_list.p;
+    fa.max_nbr = ms;
+    fa.iters = (int)h->cfg.options.iterations;
+    fa.final_buf = a;
+    if (h->fb_grid == 0) {
+      int per_sm = 0;
+      CU(h, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, h->passes.fallback, 256, 0));
+      if (per_sm < 1) return fail(h, PBF_ECUDA, "fallback kernel does not fit on an SM");
+      h->fb_grid = (unsigned)per_sm * (unsigned)h->sms;
+    }
+    void* args[] = {&fa};
+    CU(h, cudaLaunchCooperativeKernel((const void*)h->passes.fallback, dim3(std::min(h->fb_grid, nblocks(n, 256))),
+                                      dim3(256), args, 0, st));
   }
   if (a != 0) CU(h, cudaMemcpyAsync(h->xs[0].p, h->xs[1].p, (size_t)n * sizeof(float4), cudaMemcpyDeviceToDevice, st));
   {
@@ -1376,8 +1401,8 @@ int pbf_set_learned(pbf_handle* h, const pbf_mlp* model, uint32_t iterations, fl
     h->learned = false;
     return PBF_OK;
   }
-  if (iterations == 0 || !std::isfinite(fallback_bound) || !(model->lam_scale > 0.0f))
-    return fail(h, PBF_EINVAL, "learned start needs iterations >= 1, a finite bound and lam_scale > 0");
+  if (!std::isfinite(fallback_bound) || !(model->lam_scale > 0.0f))
+    return fail(h, PBF_EINVAL, "learned start needs a finite bound and lam_scale > 0");
   int rc = ensure_feature_buffers(h);
   if (rc) return rc;
   const size_t cap = h->cfg.max_particles;

@@ -23,8 +23,8 @@ struct PassSet {
                  SolverAux);
   void (*lambda_feat)(SimParams, int, const float4*, const float4*, uint32_t, const uint32_t*, const uint32_t*,
                       float4*, SolverAux);     // null in batch sets
-  void (*lambda_learned)(SimParams, int, const float4*, const float4*, uint32_t, const uint32_t*, const uint32_t*,
-                         float4*, SolverAux);  // null in batch sets
+  void (*features)(SimParams, int, const float4*, const float4*, uint32_t, const uint32_t*, const uint32_t*,
+                   SolverAux);  // null in batch sets
   void (*deltap)(SimParams, SolverAux, int, const float4*, const float4*, uint32_t, const uint32_t*, const uint32_t*,
                  float4*, float4*);
   void (*density_velocity)(SimParams, SolverAux, const float4*, uint32_t, const uint32_t*, const uint32_t*, float4*,
@@ -41,6 +41,7 @@ struct PassTable {
   void (*nbr_list)(SimParams, GridParams, const float4*, const uint32_t*, const uint32_t*, uint32_t*, uint32_t,
                    uint32_t*);
   PassSet set[2][2];  // [batch][persistent]
+  void (*fallback)(FallbackArgs);  // cooperative launch only
 };
 
 namespace exact {
@@ -119,8 +120,11 @@ cudaError_t launch_metrics(SimParams p, FieldParams f, const float* sdf, const f
 }  // namespace pbf
 #include "../../include/pbf_gb300.h"
 namespace pbf {
+// lambda_hat per feature row into d_lambda, or, with d_xl, packed as
+// d_xl[r] = (d_xs[r].xyz, lambda_hat); d_lam_sum (optional) starts the sum.
 cudaError_t launch_mlp_infer(const float* d_params, const pbf_mlp& model, const float* d_feat, uint32_t rows,
-                             float* d_lambda, float* d_lam_sum, cudaStream_t st);
+                             float* d_lambda, float* d_lam_sum, cudaStream_t st, const float4* d_xs = nullptr,
+                             float4* d_xl = nullptr);
 cudaError_t launch_mlp_grad(const float* d_params, const pbf_mlp& model, const float* d_feat, const float* d_target,
                             uint32_t rows, float* d_grad, float* d_loss, cudaStream_t st);
 cudaError_t launch_gather_f32(uint32_t n, const uint32_t* perm, const float* src, float* dst, cudaStream_t st);

@@ -19,6 +19,7 @@
 // load.  Weight gradients (H1^T dZ2, X^T dZ1) are mma.sync products over the
 // rows of a 64-row block chunk, read through shared-memory transposes.
 #include <cmath>
+#include <algorithm>
 #include <cstdint>
 #include <cstring>
 #include <vector>
@@ -38,9 +39,13 @@ using namespace mlp;
 constexpr int kInferThreads = 128;
 
 // Inference: lambda_hat for each row (particle) of feat; also starts lam_sum.
+// Persistent: the weights are staged once per CTA, each warp then walks
+// 16-row tiles.  With xl given, writes xl[r] = (xs[r].xyz, lambda_hat) (the
+// packed record the step's delta-p pass gathers) instead of lambda[r].
 __global__ void __launch_bounds__(kInferThreads) k_mlp_infer(const float* __restrict__ P, Norm nm,
                                                             const float* __restrict__ feat, uint32_t rows,
-                                                            float* __restrict__ lambda, float* __restrict__ lam_sum) {
+                                                            float* __restrict__ lambda, float* __restrict__ lam_sum,
+                                                            const float4* __restrict__ xs, float4* __restrict__ xl) {
   __shared__ __align__(16) uint16_t sW1t[kH * kW1S];
   __shared__ __align__(16) uint16_t sW2t[kH * kW2S];
   __shared__ float sB1[kH], sB2[kH], sW3[kH];
@@ -64,12 +69,22 @@ __global__ void __launch_bounds__(kInferThreads) k_mlp_infer(const float* __rest
       uint32_t ra = r0 + g, rb = r0 + g + 8;
       if (ra < rows) {
         float l = F.y0 * nm.lam_scale;
-        lambda[ra] = l;
+        if (xl) {
+          float4 x = xs[ra];
+          xl[ra] = make_float4(x.x, x.y, x.z, l);
+        } else {
+          lambda[ra] = l;
+        }
         if (lam_sum) lam_sum[ra] = l;
       }
       if (rb < rows) {
         float l = F.y8 * nm.lam_scale;
-        lambda[rb] = l;
+        if (xl) {
+          float4 x = xs[rb];
+          xl[rb] = make_float4(x.x, x.y, x.z, l);
+        } else {
+          lambda[rb] = l;
+        }
         if (lam_sum) lam_sum[rb] = l;
       }
     }
@@ -328,8 +343,7 @@ __global__ void k_gather_f32(uint32_t n, const uint32_t* __restrict__ perm, cons
 __global__ void k_copy_guarded(uint32_t n, const int* __restrict__ guard, const float4* __restrict__ src,
                                float4* __restrict__ dst) {
   if (guard && *guard == 0) return;
-  uint32_t t = blockIdx.x * blockDim.x + threadIdx.x;
-  if (t < n) dst[t] = src[t];
+  for (uint32_t t = blockIdx.x * blockDim.x + threadIdx.x; t < n; t += gridDim.x * blockDim.x) dst[t] = src[t];
 }
 
 // Fallback decision from the last learned iteration's statistics; resets
@@ -391,7 +405,8 @@ cudaError_t launch_gather_f32(uint32_t n, const uint32_t* perm, const float* src
 }
 cudaError_t launch_copy_guarded(uint32_t n, const int* guard, const float4* src, float4* dst, cudaStream_t st) {
   if (n == 0) return cudaSuccess;
-  k_copy_guarded<<<(n + 255) / 256, 256, 0, st>>>(n, guard, src, dst);
+  // one wave of CTAs (grid-stride): an unset guard costs one short wave
+  k_copy_guarded<<<std::min((n + 255) / 256, 1216u), 256, 0, st>>>(n, guard, src, dst);
   return cudaGetLastError();
 }
 cudaError_t launch_fallback_decide(SolveStats* stats, float bound, int* flag, uint32_t* fallbacks, float* last_mean,
@@ -412,12 +427,13 @@ cudaError_t launch_trace_append(uint32_t n, const uint32_t* ids, const float4* f
 }
 
 cudaError_t launch_mlp_infer(const float* d_params, const pbf_mlp& model, const float* d_feat, uint32_t rows,
-                             float* d_lambda, float* d_lam_sum, cudaStream_t st) {
+                             float* d_lambda, float* d_lam_sum, cudaStream_t st, const float4* d_xs, float4* d_xl) {
   if (rows == 0) return cudaSuccess;
   uint32_t tiles = (rows + 15) / 16;
   uint32_t blocks = (tiles + 3) / 4;
   if (blocks > 152u * 8u) blocks = 152u * 8u;
-  k_mlp_infer<<<blocks, kInferThreads, 0, st>>>(d_params, norm_of(model), d_feat, rows, d_lambda, d_lam_sum);
+  k_mlp_infer<<<blocks, kInferThreads, 0, st>>>(d_params, norm_of(model), d_feat, rows, d_lambda, d_lam_sum, d_xs,
+                                                d_xl);
   return cudaGetLastError();
 }
 

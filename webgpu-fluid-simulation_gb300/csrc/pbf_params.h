@@ -94,4 +94,30 @@ struct SolverAux {
   const float4* xs_in;       // delta-p pass: x* of a scene that skips the iteration is copied through
 };
 
+// The learned start's fallback: the plain solve of one substep from the saved
+// predicted positions, run as one cooperative kernel when the device flag is
+// set (a no-op launch otherwise).
+struct FallbackArgs {
+  SimParams p;
+  FieldParams f;
+  const int* guard;
+  const float* sdf;
+  const float* vol;
+  const uint8_t* bflag;
+  const float4* pos_save;   // x at the start of the substep
+  const float4* xs_save;    // x*_0
+  float4* pos;
+  float4* vel;
+  float4* xs0;
+  float4* xs1;
+  float4* xl;
+  float4* bdata;
+  float* lam_sum;
+  const uint32_t* nbr_cnt;
+  const uint32_t* nbr_list;
+  uint32_t max_nbr;
+  int iters;
+  int final_buf;            // xs buffer (0/1) the learned solve ended in: the result goes there
+};
+
 }  // namespace pbf

@@ -17,9 +17,10 @@
 //   xsph                   XSPH + vorticity force + surface tension (XSPH.ts:31-92)
 #pragma once
 
+#include <cooperative_groups.h>
+
 #include "pbf_device.cuh"
 #include "pbf_kernels.h"
-#include "pbf_mlp.cuh"
 
 namespace pbf {
 namespace PBF_NS {
@@ -225,19 +226,34 @@ __global__ void __launch_bounds__(256) k_nbr_list(SimParams p, GridParams g, con
     }
 }
 
+// Loads of per-particle records.  kC = false: the read-only path (the record
+// is not written during the kernel).  kC = true: L2-coherent loads, for the
+// fallback solve, which rewrites positions and multipliers between its
+// grid-wide barriers within one kernel.
+template <bool kC>
+__device__ __forceinline__ float4 ldr(const float4* p) {
+  if constexpr (kC) return __ldcg(p);
+  return __ldg(p);
+}
+template <bool kC>
+__device__ __forceinline__ float4 ldo(const float4* p) {  // the slot's own record
+  if constexpr (kC) return __ldcg(p);
+  return *p;
+}
+
 // Visit the cnt neighbours of a slot in list order (interleaved layout:
 // entry q at base + 32 q).  Indices and the neighbour's float4 are loaded
 // four at a time so the gathers overlap; fn(j, xj) keeps the sequential
 // accumulation order of the reference loop.
-template <class Fn>
+template <bool kC = false, class Fn>
 __device__ __forceinline__ void for_each_neighbor(const uint32_t* __restrict__ list, uint32_t base, uint32_t cnt,
-                                                  const float4* __restrict__ xs, Fn&& fn) {
+                                                  const float4* xs, Fn&& fn) {
   const uint32_t* l = list + base;
   uint32_t q = 0;
   for (; q + 4 <= cnt; q += 4) {
     uint32_t j0 = __ldg(l + 32 * q), j1 = __ldg(l + 32 * q + 32), j2 = __ldg(l + 32 * q + 64),
              j3 = __ldg(l + 32 * q + 96);
-    float4 x0 = __ldg(xs + j0), x1 = __ldg(xs + j1), x2 = __ldg(xs + j2), x3 = __ldg(xs + j3);
+    float4 x0 = ldr<kC>(xs + j0), x1 = ldr<kC>(xs + j1), x2 = ldr<kC>(xs + j2), x3 = ldr<kC>(xs + j3);
     fn(j0, x0);
     fn(j1, x1);
     fn(j2, x2);
@@ -245,7 +261,7 @@ __device__ __forceinline__ void for_each_neighbor(const uint32_t* __restrict__ l
   }
   for (; q < cnt; ++q) {
     uint32_t j = __ldg(l + 32 * q);
-    fn(j, __ldg(xs + j));
+    fn(j, ldr<kC>(xs + j));
   }
 }
 
@@ -282,6 +298,28 @@ __device__ __forceinline__ bool iter_active(const SceneDesc* sd, int iter) {
 // the 64-node interpolation where the field cell cannot produce a sample.  In
 // a batch each scene samples its own map (offsets into the concatenated
 // arrays); a scene without a map gets (0, 0).
+template <bool kC>
+__device__ __forceinline__ void boundary_slot(const SimParams& p, const FieldParams& f, const float* __restrict__ sdf0,
+                                              const float* __restrict__ vol0, const uint8_t* __restrict__ bflag0,
+                                              const float4* xs, float4* bdata, float* bsdf, uint32_t t) {
+  f3 xi = xyz(ldo<kC>(xs + t));
+  float4 bd = make_float4(0.f, 0.f, 0.f, 0.f);
+  float dist = 2.0f * p.h;  // "far" for the feature when the cell cannot contribute
+  if (f.loaded) {
+    const float* sdf = sdf0 + f.node_off;
+    const float* vol = vol0 + f.node_off;
+    const uint8_t* bflag = bflag0 ? bflag0 + f.flag_off : nullptr;
+    if (boundary_possible(f, bflag, xi)) {
+      if (bsdf) {
+        dist = boundary_distance(f, sdf, xi);
+      }
+      bd = boundary_sample(p, f, sdf, vol, xi);
+    }
+  }
+  bdata[t] = bd;
+  if (bsdf) bsdf[t] = dist;
+}
+
 template <bool kBatch, bool kLoop>
 __global__ void __launch_bounds__(256, 3) k_boundary(SimParams p, FieldParams f0, const float* __restrict__ sdf0,
                                                      const float* __restrict__ vol0,
@@ -292,23 +330,7 @@ __global__ void __launch_bounds__(256, 3) k_boundary(SimParams p, FieldParams f0
   PBF_SLOTS(t, p.n) {
     const SceneDesc* sd = scene_of<kBatch>(a.tab, t);
     if (!iter_active(sd, a.iter)) continue;
-    const FieldParams f = sd ? sd->field : f0;
-    f3 xi = xyz(xs[t]);
-    float4 bd = make_float4(0.f, 0.f, 0.f, 0.f);
-    float dist = 2.0f * p.h;  // "far" for the feature when the cell cannot contribute
-    if (f.loaded) {
-      const float* sdf = sdf0 + f.node_off;
-      const float* vol = vol0 + f.node_off;
-      const uint8_t* bflag = bflag0 ? bflag0 + f.flag_off : nullptr;
-      if (boundary_possible(f, bflag, xi)) {
-        if (a.bsdf) {
-          dist = boundary_distance(f, sdf, xi);
-        }
-        bd = boundary_sample(p, f, sdf, vol, xi);
-      }
-    }
-    bdata[t] = bd;
-    if (a.bsdf) a.bsdf[t] = dist;
+    boundary_slot<false>(p, sd ? sd->field : f0, sdf0, vol0, bflag0, xs, bdata, a.bsdf, t);
   }
 }
 
@@ -319,133 +341,102 @@ __global__ void __launch_bounds__(256, 3) k_boundary(SimParams p, FieldParams f0
 //            error, previous multiplier, neighbour count, |v'| dt/h, div(v') dt,
 //            boundary SDF/h, boundary volume/V, substep index; v' = (x* - x)/dt)
 //            for trace capture.
-//   kMode 2: the learned start: the features go through the MLP in-warp
-//            (32 particles = two 16-row mma tiles) and lambda_hat replaces lambda.
+template <int kMode, bool kC>
+__device__ __forceinline__ void lambda_slot(const SimParams& p, int have_field, const float4* bdata, const float4* xs,
+                                            uint32_t max_nbr, const uint32_t* __restrict__ nbr_cnt,
+                                            const uint32_t* __restrict__ nbr_list, float4* xl, const SolverAux& a,
+                                            uint32_t t) {
+  constexpr bool kFeat = kMode >= 1;
+  f3 xi = xyz(ldo<kC>(xs + t));
+  uint32_t b, e;
+  list_slice(max_nbr, nbr_cnt, t, b, e);
+  f3 grad = mk(0.f, 0.f, 0.f);
+  float sum2 = 0.0f, dens = 0.0f, div = 0.0f;
+  f3 vi = mk(0.f, 0.f, 0.f);
+  if (kFeat) vi = p.inv_dt * (xi - xyz(a.pos[t]));
+  for_each_neighbor<kC>(nbr_list, b, e, xs, [&](uint32_t j, float4 xj) {
+    Pair q = make_pair_of(xi - xyz(xj));
+    f3 gk = spiky_p(p, q);
+    grad = grad + gk;
+    sum2 = sum2 + dot3(gk, gk);
+    dens = dens + poly6_p(p, q);
+    if (kFeat) {
+      f3 vj = p.inv_dt * (xyz(xj) - xyz(__ldg(a.pos + j)));
+      div = div + dot3(vj - vi, gk);
+    }
+  });
+  dens = dens * p.V;
+  grad = p.V * grad;
+  sum2 = sum2 * p.V2;
+  float vb = 0.0f;
+  if (have_field) {
+    float4 bd = ldo<kC>(bdata + t);
+    vb = bd.w;
+    if (bd.w != 0.0f) {
+      Pair q = make_pair_of(xi - xyz(bd));
+      f3 gk = bd.w * spiky_p(p, q);
+      grad = grad + gk;
+      dens = dens + bd.w * poly6_p(p, q);
+    }
+  }
+  float c = fmaxf(0.0f, dens - 1.0f);
+  float s = dot3(grad, grad) + sum2;
+  float lam = fdiv(-c, s + p.lambda_eps);
+  xl[t] = f4(xi, lam);
+  if (a.lam_sum) a.lam_sum[t] = a.lam_first ? lam : a.lam_sum[t] + lam;
+  if (kFeat) {
+    float sd = a.bsdf ? fminf(a.bsdf[t], 2.0f * p.h) : 2.0f * p.h;
+    a.feat[2 * t] = make_float4(dens - 1.0f, a.lam_prev ? a.lam_prev[t] : 0.0f, (float)e, len3(vi) * p.dt / p.h);
+    a.feat[2 * t + 1] = make_float4(p.V * div * p.dt, sd / p.h, vb / p.V, a.substep_index);
+  }
+}
+
 template <int kMode, bool kBatch, bool kLoop>
 __global__ void __launch_bounds__(256) k_lambda(SimParams p, int have_field, const float4* __restrict__ bdata,
                                                 const float4* __restrict__ xs, uint32_t max_nbr,
                                                 const uint32_t* __restrict__ nbr_cnt,
                                                 const uint32_t* __restrict__ nbr_list,
                                                 float4* __restrict__ xl, SolverAux a) {
-  constexpr bool kFeat = kMode >= 1;
   if (a.guard && *a.guard == 0) return;
-  if constexpr (kMode == 2) {
-    // weights are staged once per CTA; the CTA then loops over its tiles
-    __shared__ __align__(16) uint16_t sW1t[mlp::kH * mlp::kW1S];
-    __shared__ __align__(16) uint16_t sW2t[mlp::kH * mlp::kW2S];
-    __shared__ float sB1[mlp::kH], sB2[mlp::kH], sW3[mlp::kH];
-    __shared__ float sF[256 / 32][32][9];
-    mlp::stage_weights(a.mlp, sW1t, sW2t, nullptr);
-    for (int q = threadIdx.x; q < mlp::kH; q += blockDim.x) {
-      sB1[q] = a.mlp[mlp::OFF_B1 + q];
-      sB2[q] = a.mlp[mlp::OFF_B2 + q];
-      sW3[q] = a.mlp[mlp::OFF_W3 + q];
+  PBF_SLOTS(t, p.n) {
+    if (!iter_active(scene_of<kBatch>(a.tab, t), a.iter)) continue;
+    lambda_slot<kMode, false>(p, have_field, bdata, xs, max_nbr, nbr_cnt, nbr_list, xl, a, t);
+  }
+}
+
+// The learned start's features at x*_0, over the neighbour list: two float4
+// per particle (a.feat) with the layout and values the lambda pass records
+// for training (density error, previous multiplier, neighbour count,
+// |v'| dt/h, div(v') dt, boundary SDF/h, boundary volume/V, substep index;
+// v' = (x* - x)/dt).  Needs the boundary pass at x*_0 (bdata, a.bsdf).  The
+// network then runs over the rows as a separate dense pass.
+template <bool kLoop>
+__global__ void __launch_bounds__(256) k_features(SimParams p, int have_field, const float4* __restrict__ bdata,
+                                                  const float4* __restrict__ xs, uint32_t max_nbr,
+                                                  const uint32_t* __restrict__ nbr_cnt,
+                                                  const uint32_t* __restrict__ nbr_list, SolverAux a) {
+  PBF_SLOTS(t, p.n) {
+    const f3 xi = xyz(xs[t]);
+    uint32_t b, e;
+    list_slice(max_nbr, nbr_cnt, t, b, e);
+    float dens = 0.0f, div = 0.0f;
+    const f3 vi = p.inv_dt * (xi - xyz(a.pos[t]));
+    for_each_neighbor(nbr_list, b, e, xs, [&](uint32_t j, float4 xj) {
+      Pair q = make_pair_of(xi - xyz(xj));
+      dens = dens + poly6_p(p, q);
+      f3 vj = p.inv_dt * (xyz(xj) - xyz(__ldg(a.pos + j)));
+      div = div + dot3(vj - vi, spiky_p(p, q));
+    });
+    dens = dens * p.V;
+    float vb = 0.0f;
+    if (have_field) {
+      float4 bd = bdata[t];
+      vb = bd.w;
+      if (bd.w != 0.0f) dens = dens + bd.w * poly6_p(p, make_pair_of(xi - xyz(bd)));
     }
-    __syncthreads();
-    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, g = lane >> 2, t4 = lane & 3;
-    PBF_TILES(p.n) {
-      const uint32_t t = tile0 + threadIdx.x;
-      const bool valid = t < p.n;
-      float fv[8] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
-      f3 xi = mk(0.f, 0.f, 0.f);
-      if (valid) {
-        xi = xyz(xs[t]);
-        uint32_t b, e;
-        list_slice(max_nbr, nbr_cnt, t, b, e);
-        float dens = 0.0f, div = 0.0f;
-        f3 vi = p.inv_dt * (xi - xyz(a.pos[t]));
-        for_each_neighbor(nbr_list, b, e, xs, [&](uint32_t j, float4 xj) {
-          Pair q = make_pair_of(xi - xyz(xj));
-          dens = dens + poly6_p(p, q);
-          f3 vj = p.inv_dt * (xyz(xj) - xyz(__ldg(a.pos + j)));
-          div = div + dot3(vj - vi, spiky_p(p, q));
-        });
-        dens = dens * p.V;
-        float vb = 0.0f;
-        if (have_field) {
-          float4 bd = bdata[t];
-          vb = bd.w;
-          if (bd.w != 0.0f) dens = dens + bd.w * poly6_p(p, make_pair_of(xi - xyz(bd)));
-        }
-        float sd = a.bsdf ? fminf(a.bsdf[t], 2.0f * p.h) : 2.0f * p.h;
-        fv[0] = dens - 1.0f;
-        fv[1] = a.lam_prev ? a.lam_prev[t] : 0.0f;
-        fv[2] = (float)e;
-        fv[3] = len3(vi) * p.dt / p.h;
-        fv[4] = p.V * div * p.dt;
-        fv[5] = sd / p.h;
-        fv[6] = vb / p.V;
-        fv[7] = a.substep_index;
-      }
-#pragma unroll
-      for (int k = 0; k < 8; ++k) sF[warp][lane][k] = valid ? (fv[k] - a.norm.mean[k]) * a.norm.inv_std[k] : 0.0f;
-      __syncwarp();
-#pragma unroll
-      for (int tile = 0; tile < 2; ++tile) {
-        const int r = 16 * tile + g;
-        float xg[2] = {sF[warp][r][2 * t4], sF[warp][r][2 * t4 + 1]};
-        float x8[2] = {sF[warp][r + 8][2 * t4], sF[warp][r + 8][2 * t4 + 1]};
-        mlp::Fwd F;
-        mlp::forward_tile(xg, x8, sW1t, sW2t, sB1, sB2, sW3, a.mlp[mlp::OFF_B3], F);
-        if (t4 == 0) {  // rows r and r + 8 of this warp: column 8 of sF is free
-          sF[warp][r][8] = F.y0 * a.norm.lam_scale;
-          sF[warp][r + 8][8] = F.y8 * a.norm.lam_scale;
-        }
-      }
-      __syncwarp();
-      if (valid) {
-        float l = sF[warp][lane][8];
-        xl[t] = f4(xi, l);
-        a.lam_sum[t] = l;
-      }
-      __syncwarp();  // sF is rewritten by the next tile
-    }
-  } else {
-    PBF_SLOTS(t, p.n) {
-      if (!iter_active(scene_of<kBatch>(a.tab, t), a.iter)) continue;
-      f3 xi = xyz(xs[t]);
-      uint32_t b, e;
-      list_slice(max_nbr, nbr_cnt, t, b, e);
-      f3 grad = mk(0.f, 0.f, 0.f);
-      float sum2 = 0.0f, dens = 0.0f, div = 0.0f;
-      f3 vi = mk(0.f, 0.f, 0.f);
-      if (kFeat) vi = p.inv_dt * (xi - xyz(a.pos[t]));
-      for_each_neighbor(nbr_list, b, e, xs, [&](uint32_t j, float4 xj) {
-        Pair q = make_pair_of(xi - xyz(xj));
-        f3 gk = spiky_p(p, q);
-        grad = grad + gk;
-        sum2 = sum2 + dot3(gk, gk);
-        dens = dens + poly6_p(p, q);
-        if (kFeat) {
-          f3 vj = p.inv_dt * (xyz(xj) - xyz(__ldg(a.pos + j)));
-          div = div + dot3(vj - vi, gk);
-        }
-      });
-      dens = dens * p.V;
-      grad = p.V * grad;
-      sum2 = sum2 * p.V2;
-      float vb = 0.0f;
-      if (have_field) {
-        float4 bd = bdata[t];
-        vb = bd.w;
-        if (bd.w != 0.0f) {
-          Pair q = make_pair_of(xi - xyz(bd));
-          f3 gk = bd.w * spiky_p(p, q);
-          grad = grad + gk;
-          dens = dens + bd.w * poly6_p(p, q);
-        }
-      }
-      float c = fmaxf(0.0f, dens - 1.0f);
-      float s = dot3(grad, grad) + sum2;
-      float lam = fdiv(-c, s + p.lambda_eps);
-      xl[t] = f4(xi, lam);
-      if (a.lam_sum) a.lam_sum[t] = a.lam_first ? lam : a.lam_sum[t] + lam;
-      if (kFeat) {
-        float sd = a.bsdf ? fminf(a.bsdf[t], 2.0f * p.h) : 2.0f * p.h;
-        a.feat[2 * t] = make_float4(dens - 1.0f, a.lam_prev ? a.lam_prev[t] : 0.0f, (float)e, len3(vi) * p.dt / p.h);
-        a.feat[2 * t + 1] = make_float4(p.V * div * p.dt, sd / p.h, vb / p.V, a.substep_index);
-      }
-    }
+    float sd = a.bsdf ? fminf(a.bsdf[t], 2.0f * p.h) : 2.0f * p.h;
+    a.feat[2 * t] = make_float4(dens - 1.0f, a.lam_prev ? a.lam_prev[t] : 0.0f, (float)e, len3(vi) * p.dt / p.h);
+    a.feat[2 * t + 1] = make_float4(p.V * div * p.dt, sd / p.h, vb / p.V, a.substep_index);
   }
 }
 
@@ -453,6 +444,33 @@ __global__ void __launch_bounds__(256) k_lambda(SimParams p, int have_field, con
 // buffer; (x*_j, lambda_j) come packed from the lambda pass.  A scene of a
 // batch that has finished its iterations copies its x* through (a.xs_in), so
 // every scene ends in the same buffer.
+// Position correction of slot t from the packed (x*, lambda) records; xi
+// receives the slot's own x*.
+template <bool kC>
+__device__ __forceinline__ f3 deltap_slot(const SimParams& p, int have_field, const float4* xl, const float4* bdata,
+                                          uint32_t max_nbr, const uint32_t* __restrict__ nbr_cnt,
+                                          const uint32_t* __restrict__ nbr_list, uint32_t t, f3& xi) {
+  const float4 xli = ldo<kC>(xl + t);
+  xi = xyz(xli);
+  float li = xli.w;
+  uint32_t b, e;
+  list_slice(max_nbr, nbr_cnt, t, b, e);
+  f3 pu = mk(0.f, 0.f, 0.f);
+  for_each_neighbor<kC>(nbr_list, b, e, xl, [&](uint32_t, float4 xj) {
+    Pair q = make_pair_of(xi - xyz(xj));
+    pu = pu + (li + xj.w) * spiky_p(p, q);
+  });
+  pu = p.V * pu;
+  if (have_field) {
+    float4 bd = ldo<kC>(bdata + t);
+    if (bd.w != 0.0f) {
+      Pair q = make_pair_of(xi - xyz(bd));
+      pu = pu + (bd.w * li) * spiky_p(p, q);
+    }
+  }
+  return 0.5f * pu;
+}
+
 template <bool kBatch, bool kLoop>
 __global__ void __launch_bounds__(256) k_deltap(SimParams p, SolverAux a, int have_field,
                                                 const float4* __restrict__ xl, const float4* __restrict__ bdata,
@@ -465,25 +483,8 @@ __global__ void __launch_bounds__(256) k_deltap(SimParams p, SolverAux a, int ha
       xs_out[t] = a.xs_in[t];
       continue;
     }
-    const float4 xli = xl[t];
-    f3 xi = xyz(xli);
-    float li = xli.w;
-    uint32_t b, e;
-    list_slice(max_nbr, nbr_cnt, t, b, e);
-    f3 pu = mk(0.f, 0.f, 0.f);
-    for_each_neighbor(nbr_list, b, e, xl, [&](uint32_t, float4 xj) {
-      Pair q = make_pair_of(xi - xyz(xj));
-      pu = pu + (li + xj.w) * spiky_p(p, q);
-    });
-    pu = p.V * pu;
-    if (have_field) {
-      float4 bd = bdata[t];
-      if (bd.w != 0.0f) {
-        Pair q = make_pair_of(xi - xyz(bd));
-        pu = pu + (bd.w * li) * spiky_p(p, q);
-      }
-    }
-    f3 dp = 0.5f * pu;
+    f3 xi;
+    const f3 dp = deltap_slot<false>(p, have_field, xl, bdata, max_nbr, nbr_cnt, nbr_list, t, xi);
     if (dp_out) dp_out[t] = f4(dp, 0.0f);
     if constexpr (kBatch) {  // the scene's own domain (looked up after the loop: no registers held across it)
       SimParams ps = p;
@@ -495,7 +496,32 @@ __global__ void __launch_bounds__(256) k_deltap(SimParams p, SolverAux a, int ha
   }
 }
 
+// AttributeUpdate of slot t; returns sum W (fluid only).
+template <bool kC>
+__device__ __forceinline__ float density_slot(const SimParams& p, const float4* xs, uint32_t max_nbr,
+                                              const uint32_t* __restrict__ nbr_cnt,
+                                              const uint32_t* __restrict__ nbr_list, float4* pos, float4* vel,
+                                              uint32_t t) {
+  f3 xi = xyz(ldo<kC>(xs + t));
+  uint32_t b, e;
+  list_slice(max_nbr, nbr_cnt, t, b, e);
+  float dens = 0.0f;
+  for_each_neighbor<kC>(nbr_list, b, e, xs, [&](uint32_t, float4 xj) {
+    Pair q = make_pair_of(xi - xyz(xj));
+    dens = dens + poly6_p(p, q);
+  });
+  const float vsum = dens;
+  dens = dens * p.m;
+  f3 xo = xyz(ldo<kC>(pos + t));
+  vel[t] = f4(p.inv_dt * (xi - xo), 0.0f);
+  pos[t] = f4(xi, dens);
+  return vsum;
+}
+
 // AttributeUpdate: rho = m * sum W (fluid only), v = (x* - x) / dt, x <- (x*, rho).
+// With a.stats, also the per-step density error (compression
+// max(0, rho/rho0 - 1) = max(0, V sum W - 1)): reduced over the CTA in shared
+// memory, one set of atomics per CTA.
 template <bool kLoop>
 __global__ void __launch_bounds__(256) k_density_velocity(SimParams p, SolverAux a, const float4* __restrict__ xs,
                                                           uint32_t max_nbr,
@@ -503,35 +529,90 @@ __global__ void __launch_bounds__(256) k_density_velocity(SimParams p, SolverAux
                                                           const uint32_t* __restrict__ nbr_list,
                                                           float4* __restrict__ pos, float4* __restrict__ vel) {
   if (a.guard && *a.guard == 0) return;
+  unsigned cmax = 0u, csum = 0u, ccnt = 0u;
   PBF_SLOTS(t, p.n) {
-    f3 xi = xyz(xs[t]);
-    uint32_t b, e;
-    list_slice(max_nbr, nbr_cnt, t, b, e);
-    float dens = 0.0f;
-    for_each_neighbor(nbr_list, b, e, xs, [&](uint32_t, float4 xj) {
-      Pair q = make_pair_of(xi - xyz(xj));
-      dens = dens + poly6_p(p, q);
-    });
-    float vsum = dens;
-    dens = dens * p.m;
-    f3 xo = xyz(pos[t]);
-    vel[t] = f4(p.inv_dt * (xi - xo), 0.0f);
-    pos[t] = f4(xi, dens);
+    const float vsum = density_slot<false>(p, xs, max_nbr, nbr_cnt, nbr_list, pos, vel, t);
     if (a.stats) {
-      // per-step density error: compression max(0, rho/rho0 - 1) = max(0, V sum W - 1),
-      // warp-aggregated over the lanes still in the loop
       float c = fmaxf(0.0f, vsum * p.V - 1.0f);
-      const unsigned m = __activemask();
-      unsigned fx = (unsigned)(fminf(c, 1.0f) * 1048576.0f);
-      unsigned wmax = __reduce_max_sync(m, __float_as_uint(c));
-      unsigned wsum = __reduce_add_sync(m, fx);
-      if ((threadIdx.x & 31u) == (unsigned)(__ffs(m) - 1)) {
-        atomicMax(&a.stats->max_bits, wmax);
-        atomicAdd(&a.stats->count, (unsigned)__popc(m));
-        atomicAdd(&a.stats->sum_fx, (unsigned long long)wsum);
-      }
+      cmax = max(cmax, __float_as_uint(c));  // non-negative floats order as their bits
+      csum += (unsigned)(fminf(c, 1.0f) * 1048576.0f);
+      ++ccnt;
     }
   }
+  if (a.stats) {
+    __shared__ unsigned s_max, s_cnt;
+    __shared__ unsigned long long s_sum;
+    if (threadIdx.x == 0) {
+      s_max = 0u;
+      s_cnt = 0u;
+      s_sum = 0ull;
+    }
+    __syncthreads();
+    cmax = __reduce_max_sync(0xffffffffu, cmax);
+    csum = __reduce_add_sync(0xffffffffu, csum);
+    ccnt = __reduce_add_sync(0xffffffffu, ccnt);
+    if ((threadIdx.x & 31u) == 0) {
+      atomicMax(&s_max, cmax);
+      atomicAdd(&s_cnt, ccnt);
+      atomicAdd(&s_sum, (unsigned long long)csum);
+    }
+    __syncthreads();
+    if (threadIdx.x == 0 && s_cnt) {
+      atomicMax(&a.stats->max_bits, s_max);
+      atomicAdd(&a.stats->count, s_cnt);
+      atomicAdd(&a.stats->sum_fx, s_sum);
+    }
+  }
+}
+
+// The learned start's fallback: when *guard is set, restores x and x*_0 and
+// runs the plain solve (boundary, lambda, delta-p per iteration, the
+// multiplier sum restarted) and AttributeUpdate, with grid-wide barriers
+// between the phases; otherwise returns at once, so an unneeded fallback
+// costs one launch.  Launched cooperatively with at most one resident wave of
+// CTAs.  Positions and multipliers change between phases inside the kernel,
+// so their loads are L2-coherent (kC = true); the arithmetic is the pass
+// kernels' own (the same slot bodies).
+__global__ void __launch_bounds__(256) k_fallback_solve(FallbackArgs A) {
+  if (*A.guard == 0) return;
+  cooperative_groups::grid_group grid = cooperative_groups::this_grid();
+  const uint32_t n = A.p.n, stride = gridDim.x * blockDim.x, t0 = blockIdx.x * blockDim.x + threadIdx.x;
+  for (uint32_t t = t0; t < n; t += stride) {
+    A.pos[t] = __ldcg(A.pos_save + t);
+    A.xs0[t] = __ldcg(A.xs_save + t);
+  }
+  grid.sync();
+  int a = 0;
+  for (int it = 0; it < A.iters; ++it) {
+    float4* cur = a ? A.xs1 : A.xs0;
+    float4* nxt = a ? A.xs0 : A.xs1;
+    if (A.f.loaded) {
+      for (uint32_t t = t0; t < n; t += stride)
+        boundary_slot<true>(A.p, A.f, A.sdf, A.vol, A.bflag, cur, A.bdata, nullptr, t);
+      grid.sync();
+    }
+    SolverAux al{};
+    al.lam_sum = A.lam_sum;
+    al.lam_first = it == 0 ? 1 : 0;
+    for (uint32_t t = t0; t < n; t += stride)
+      lambda_slot<0, true>(A.p, A.f.loaded, A.bdata, cur, A.max_nbr, A.nbr_cnt, A.nbr_list, A.xl, al, t);
+    grid.sync();
+    for (uint32_t t = t0; t < n; t += stride) {
+      f3 xi;
+      const f3 dp = deltap_slot<true>(A.p, A.f.loaded, A.xl, A.bdata, A.max_nbr, A.nbr_cnt, A.nbr_list, t, xi);
+      nxt[t] = f4(clamp_rand(A.p, xi + dp), 0.0f);
+    }
+    grid.sync();
+    a = 1 - a;
+  }
+  float4* fin = A.final_buf ? A.xs1 : A.xs0;
+  if (a != A.final_buf) {
+    const float4* src = a ? A.xs1 : A.xs0;
+    for (uint32_t t = t0; t < n; t += stride) fin[t] = __ldcg(src + t);
+    grid.sync();
+  }
+  for (uint32_t t = t0; t < n; t += stride)
+    density_slot<true>(A.p, fin, A.max_nbr, A.nbr_cnt, A.nbr_list, A.pos, A.vel, t);
 }
 
 // VorticityConfinement: omega_i and the Akinci normal n_i.
@@ -609,7 +690,7 @@ void fill_set(PassSet* ps) {
   ps->boundary = k_boundary<B, P>;
   ps->lambda = k_lambda<0, B, P>;
   ps->lambda_feat = B ? nullptr : k_lambda<1, false, P>;
-  ps->lambda_learned = B ? nullptr : k_lambda<2, false, P>;
+  ps->features = B ? nullptr : k_features<P>;
   ps->deltap = k_deltap<B, P>;
   ps->density_velocity = k_density_velocity<P>;
   ps->vorticity = k_vorticity<P>;
@@ -617,6 +698,7 @@ void fill_set(PassSet* ps) {
 }
 
 void fill_pass_table(PassTable* tbl) {
+  tbl->fallback = k_fallback_solve;
   tbl->nbr_count = k_nbr_count;
   tbl->nbr_list = k_nbr_list;
   fill_set<false, false>(&tbl->set[0][0]);

@@ -295,7 +295,9 @@ int pbf_exclusive_scan_u32(const uint32_t* d_in, uint32_t* d_out, size_t n, void
  * 8 -> 64 -> 64 -> 1 (SiLU, BF16 weights/activations, FP32 accumulate)
  * predicts an effective multiplier per particle from features at the
  * predicted positions: density error, previous substep's multiplier,
- * neighbour count, |v'| dt/h, div(v') dt, boundary SDF/h, boundary volume/V,
+ * neighbour count, |v'| dt/h, velocity divergence -div(v') dt (by the
+ * continuity equation: (rho_prev - rho*) / rho*, rho_prev the particle's
+ * density after the previous substep), boundary SDF/h, boundary volume/V,
  * substep index.  One projection with it (ConstrainSolve with lambda_hat)
  * is followed by `iterations` plain iterations; when the substep's density
  * error — the mean over particles of max(0, rho/rho0 - 1) after the solve,

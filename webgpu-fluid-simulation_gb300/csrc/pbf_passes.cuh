@@ -338,9 +338,18 @@ __global__ void __launch_bounds__(256, 3) k_boundary(SimParams p, FieldParams f0
 // the next pass gathers a neighbour's position and multiplier in one load.
 //   kMode 0: the reference pass.
 //   kMode 1: also writes the learned start's 8 features at x*_0 (density
-//            error, previous multiplier, neighbour count, |v'| dt/h, div(v') dt,
-//            boundary SDF/h, boundary volume/V, substep index; v' = (x* - x)/dt)
-//            for trace capture.
+//            error, previous multiplier, neighbour count, |v'| dt/h, -div(v') dt
+//            by continuity, boundary SDF/h, boundary volume/V, substep index;
+//            v' = (x* - x)/dt) for trace capture.
+// Velocity divergence feature of the learned start, -div(v') dt, by the
+// continuity equation: (rho_prev - rho*) / rho* with rho* the fluid density
+// at x* (V sum W) and rho_prev the particle's density after the previous
+// substep (x.w / rho0); 0 before the first density pass.
+__device__ __forceinline__ float divergence_feature(const SimParams& p, float4 x_prev, float dens_fluid) {
+  const float prev = x_prev.w / p.rho0;
+  return (prev > 0.0f && dens_fluid > 0.0f) ? (prev - dens_fluid) / dens_fluid : 0.0f;
+}
+
 template <int kMode, bool kC>
 __device__ __forceinline__ void lambda_slot(const SimParams& p, int have_field, const float4* bdata, const float4* xs,
                                             uint32_t max_nbr, const uint32_t* __restrict__ nbr_cnt,
@@ -351,21 +360,16 @@ __device__ __forceinline__ void lambda_slot(const SimParams& p, int have_field, 
   uint32_t b, e;
   list_slice(max_nbr, nbr_cnt, t, b, e);
   f3 grad = mk(0.f, 0.f, 0.f);
-  float sum2 = 0.0f, dens = 0.0f, div = 0.0f;
-  f3 vi = mk(0.f, 0.f, 0.f);
-  if (kFeat) vi = p.inv_dt * (xi - xyz(a.pos[t]));
-  for_each_neighbor<kC>(nbr_list, b, e, xs, [&](uint32_t j, float4 xj) {
+  float sum2 = 0.0f, dens = 0.0f;
+  for_each_neighbor<kC>(nbr_list, b, e, xs, [&](uint32_t, float4 xj) {
     Pair q = make_pair_of(xi - xyz(xj));
     f3 gk = spiky_p(p, q);
     grad = grad + gk;
     sum2 = sum2 + dot3(gk, gk);
     dens = dens + poly6_p(p, q);
-    if (kFeat) {
-      f3 vj = p.inv_dt * (xyz(xj) - xyz(__ldg(a.pos + j)));
-      div = div + dot3(vj - vi, gk);
-    }
   });
   dens = dens * p.V;
+  const float dens_fluid = dens;
   grad = p.V * grad;
   sum2 = sum2 * p.V2;
   float vb = 0.0f;
@@ -385,9 +389,11 @@ __device__ __forceinline__ void lambda_slot(const SimParams& p, int have_field, 
   xl[t] = f4(xi, lam);
   if (a.lam_sum) a.lam_sum[t] = a.lam_first ? lam : a.lam_sum[t] + lam;
   if (kFeat) {
+    const float4 xo = a.pos[t];
+    const f3 vi = p.inv_dt * (xi - xyz(xo));
     float sd = a.bsdf ? fminf(a.bsdf[t], 2.0f * p.h) : 2.0f * p.h;
     a.feat[2 * t] = make_float4(dens - 1.0f, a.lam_prev ? a.lam_prev[t] : 0.0f, (float)e, len3(vi) * p.dt / p.h);
-    a.feat[2 * t + 1] = make_float4(p.V * div * p.dt, sd / p.h, vb / p.V, a.substep_index);
+    a.feat[2 * t + 1] = make_float4(divergence_feature(p, xo, dens_fluid), sd / p.h, vb / p.V, a.substep_index);
   }
 }
 
@@ -407,9 +413,9 @@ __global__ void __launch_bounds__(256) k_lambda(SimParams p, int have_field, con
 // The learned start's features at x*_0, over the neighbour list: two float4
 // per particle (a.feat) with the layout and values the lambda pass records
 // for training (density error, previous multiplier, neighbour count,
-// |v'| dt/h, div(v') dt, boundary SDF/h, boundary volume/V, substep index;
-// v' = (x* - x)/dt).  Needs the boundary pass at x*_0 (bdata, a.bsdf).  The
-// network then runs over the rows as a separate dense pass.
+// |v'| dt/h, -div(v') dt by continuity, boundary SDF/h, boundary volume/V,
+// substep index; v' = (x* - x)/dt).  Needs the boundary pass at x*_0 (bdata,
+// a.bsdf).  The network then runs over the rows as a separate dense pass.
 template <bool kLoop>
 __global__ void __launch_bounds__(256) k_features(SimParams p, int have_field, const float4* __restrict__ bdata,
                                                   const float4* __restrict__ xs, uint32_t max_nbr,
@@ -419,24 +425,23 @@ __global__ void __launch_bounds__(256) k_features(SimParams p, int have_field, c
     const f3 xi = xyz(xs[t]);
     uint32_t b, e;
     list_slice(max_nbr, nbr_cnt, t, b, e);
-    float dens = 0.0f, div = 0.0f;
-    const f3 vi = p.inv_dt * (xi - xyz(a.pos[t]));
-    for_each_neighbor(nbr_list, b, e, xs, [&](uint32_t j, float4 xj) {
-      Pair q = make_pair_of(xi - xyz(xj));
-      dens = dens + poly6_p(p, q);
-      f3 vj = p.inv_dt * (xyz(xj) - xyz(__ldg(a.pos + j)));
-      div = div + dot3(vj - vi, spiky_p(p, q));
+    float dens = 0.0f;
+    for_each_neighbor(nbr_list, b, e, xs, [&](uint32_t, float4 xj) {
+      dens = dens + poly6_p(p, make_pair_of(xi - xyz(xj)));
     });
     dens = dens * p.V;
+    const float dens_fluid = dens;
     float vb = 0.0f;
     if (have_field) {
       float4 bd = bdata[t];
       vb = bd.w;
       if (bd.w != 0.0f) dens = dens + bd.w * poly6_p(p, make_pair_of(xi - xyz(bd)));
     }
+    const float4 xo = a.pos[t];
+    const f3 vi = p.inv_dt * (xi - xyz(xo));
     float sd = a.bsdf ? fminf(a.bsdf[t], 2.0f * p.h) : 2.0f * p.h;
     a.feat[2 * t] = make_float4(dens - 1.0f, a.lam_prev ? a.lam_prev[t] : 0.0f, (float)e, len3(vi) * p.dt / p.h);
-    a.feat[2 * t + 1] = make_float4(p.V * div * p.dt, sd / p.h, vb / p.V, a.substep_index);
+    a.feat[2 * t + 1] = make_float4(divergence_feature(p, xo, dens_fluid), sd / p.h, vb / p.V, a.substep_index);
   }
 }
 

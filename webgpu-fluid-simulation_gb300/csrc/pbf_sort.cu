@@ -195,52 +195,37 @@ __global__ void __launch_bounds__(256) k_scatter(uint32_t n, const uint32_t* __r
 }
 
 // ---- stable within-cell order ------------------------------------------------------
-// One warp per cell.  Cells with <= 32 entries rank in registers; up to
-// kWarpMax by warp-wide counting; larger cells go to the block radix path.
-constexpr uint32_t kWarpMax = 1024;
+// One thread per sorted position q: the entry scattered there ranks itself
+// by particle id among its cell's entries and moves to cell_start + rank.
+// The work follows the particles (sum over cells of count^2), not the cell
+// count, so empty cells cost nothing.  Cells above kRankMax entries go to
+// the block radix path (the thread at the cell's first position lists it).
+constexpr uint32_t kRankMax = 1024;
 
-__global__ void __launch_bounds__(256) k_cellfix(uint32_t cells, const uint32_t* __restrict__ cell_count,
+__global__ void __launch_bounds__(256) k_cellfix(uint32_t n, const uint32_t* __restrict__ key,
+                                                 const uint32_t* __restrict__ cell_count,
                                                  const uint32_t* __restrict__ cell_start,
                                                  const uint32_t* __restrict__ perm_raw,
                                                  const uint32_t* __restrict__ id_raw, uint32_t* __restrict__ perm,
                                                  uint32_t* big_list, uint32_t* big_count) {
-  const uint32_t lane = threadIdx.x & 31u;
-  const uint32_t warp_global = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-  const uint32_t nwarps = (gridDim.x * blockDim.x) >> 5;
-  for (uint32_t c = warp_global; c < cells; c += nwarps) {
-    uint32_t cnt = __ldg(cell_count + c);
-    if (cnt == 0) continue;
-    uint32_t st = __ldg(cell_start + c);
-    if (cnt == 1) {
-      if (lane == 0) perm[st] = perm_raw[st];
-      continue;
-    }
-    if (cnt <= 32) {
-      uint32_t my_id = 0xffffffffu, my_slot = 0;
-      if (lane < cnt) {
-        my_id = id_raw[st + lane];
-        my_slot = perm_raw[st + lane];
-      }
-      uint32_t r = 0;
-      for (uint32_t m = 0; m < cnt; ++m) {
-        uint32_t other = __shfl_sync(kFull, my_id, m);
-        r += (other < my_id) ? 1u : 0u;
-      }
-      if (lane < cnt) perm[st + r] = my_slot;
-    } else if (cnt <= kWarpMax) {
-      for (uint32_t e = lane; e < cnt; e += 32) {
-        uint32_t my_id = id_raw[st + e];
-        uint32_t r = 0;
-        for (uint32_t m = 0; m < cnt; ++m) r += (__ldg(id_raw + st + m) < my_id) ? 1u : 0u;
-        perm[st + r] = perm_raw[st + e];
-      }
-    } else {
-      if (lane == 0) {
-        uint32_t q = atomicAdd(big_count, 1u);
-        big_list[q] = c;
-      }
-    }
+  const uint32_t q = blockIdx.x * blockDim.x + threadIdx.x;
+  if (q >= n) return;
+  const uint32_t s = perm_raw[q];
+  const uint32_t c = __ldg(key + s);
+  const uint32_t cnt = __ldg(cell_count + c);
+  if (cnt == 1) {
+    perm[q] = s;
+    return;
   }
+  const uint32_t st = __ldg(cell_start + c);
+  if (cnt > kRankMax) {
+    if (q == st) big_list[atomicAdd(big_count, 1u)] = c;
+    return;
+  }
+  const uint32_t my = id_raw[q];
+  uint32_t r = 0;
+  for (uint32_t m = 0; m < cnt; ++m) r += (__ldg(id_raw + st + m) < my) ? 1u : 0u;
+  perm[st + r] = s;
 }
 
 // Block LSD radix sort (8-bit digits) of one very full cell by particle id;
@@ -480,14 +465,8 @@ cudaError_t launch_sort_by_cell(GridParams g, uint32_t n, const uint32_t* ids, S
   k_scatter<<<blocks_for(n, 256), 256, 0, st>>>(n, b.key, b.rank, b.cell_start, ids, b.perm_raw, b.id_raw);
   e = cudaMemsetAsync(b.big_count, 0, sizeof(uint32_t), st);
   if (e != cudaSuccess) return e;
-  {
-    unsigned warps_needed = g.cells;
-    unsigned blocks = (unsigned)((warps_needed + 7) / 8);
-    if (blocks > 152u * 16u) blocks = 152u * 16u;
-    if (blocks == 0) blocks = 1;
-    k_cellfix<<<blocks, 256, 0, st>>>(g.cells, b.cell_count, b.cell_start, b.perm_raw, b.id_raw, b.perm, b.big_list,
-                                      b.big_count);
-  }
+  k_cellfix<<<blocks_for(n, 256), 256, 0, st>>>(n, b.key, b.cell_count, b.cell_start, b.perm_raw, b.id_raw, b.perm,
+                                                 b.big_list, b.big_count);
   int passes = (int)((id_bits + 7) / 8);
   if (passes < 1) passes = 1;
   k_bigcell<<<152, kRadixThreads, 0, st>>>(b.big_list, b.big_count, b.cell_count, b.cell_start, b.perm_raw, b.id_raw,

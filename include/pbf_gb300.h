@@ -374,7 +374,14 @@ typedef struct pbf_launch {
   uint32_t block;        /* threads per CTA: 128 or 256 (default 256) */
   uint32_t ctas_per_sm;  /* 0 (default) or 1..16 */
   float cell_ratio;      /* 1 (default) or 0.5 */
+  uint32_t build;        /* neighbour-build variant: PBF_BUILD_THREAD (default, one slot
+                            per thread), PBF_BUILD_PAIR (two slots of one cell per thread,
+                            sharing candidate loads), PBF_BUILD_WARP (warp-cooperative
+                            per cell: coalesced candidate chunks, ballot-collected hits) */
 } pbf_launch;
+#define PBF_BUILD_THREAD 0u
+#define PBF_BUILD_PAIR 1u
+#define PBF_BUILD_WARP 2u
 int pbf_set_launch(pbf_handle* h, const pbf_launch* launch);
 int pbf_get_launch(const pbf_handle* h, pbf_launch* launch);
 
@@ -384,9 +391,10 @@ typedef struct pbf_tune_trial {
 } pbf_tune_trial;
 #define PBF_TUNE_CELL_RATIO 0x1u /* also try cell_ratio 0.5 */
 /* Times `substeps` substeps (after 2 warm-up substeps) for every candidate
- * launch shape — block {128, 256} x ctas_per_sm {0, 1024/block, 2048/block}
- * (x cell_ratio {1, 0.5} with PBF_TUNE_CELL_RATIO) — on the current state,
- * restores the state (positions, velocities, accelerations, ids), keeps the fastest
+ * launch shape — block {128, 256} x ctas_per_sm {0, 2048/block} x
+ * build {THREAD, PAIR, WARP} (x cell_ratio {1, 0.5} with PBF_TUNE_CELL_RATIO) — on
+ * the current state, restores the state (positions, velocities,
+ * accelerations, ids), keeps the fastest
  * shape (also returned in *best).  trials (up to max_trials) receive every
  * candidate's time.  PBF_ESTATE while trace capture is on. */
 int pbf_autotune(pbf_handle* h, uint32_t substeps, uint32_t flags, pbf_tune_trial* trials, uint32_t max_trials,

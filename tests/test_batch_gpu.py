@@ -76,7 +76,7 @@ def test_batch_rejects_single_scene_setup():
     b.close()
 
 
-@pytest.mark.parametrize("shape", [(128, 0), (256, 2), (128, 16), (256, 8)])
+@pytest.mark.parametrize("shape", [(128, 0, 0), (256, 2, 1), (128, 16, 2), (256, 0, 2), (256, 8, 1)])
 def test_launch_shape_does_not_change_results(shape):
     sc = scenes.reference_scene("boundary_small", fp_mode=L.FP_EXACT)
     pts = scenes.jitter(sc.particles, 0.001, seed=9)
@@ -87,7 +87,7 @@ def test_launch_shape_does_not_change_results(shape):
         sim.set_particles(pts)
         sim.set_boundary_field(f["res"], f["origin"], f["extent"], f["sdf"], f["vol"])
         if launch:
-            sim.set_launch(block=launch[0], ctas_per_sm=launch[1])
+            sim.set_launch(block=launch[0], ctas_per_sm=launch[1], build=launch[2])
         sim.enable_graph(graph)
         sim.step(4)
         out = sim.positions(), sim.velocities()
@@ -105,7 +105,7 @@ def test_batch_graph_and_persistent_launch_bitexact():
     a = PBFBatch(cfg, sc)
     a.step(2)
     b = PBFBatch(cfg, sc)
-    b.set_launch(block=128, ctas_per_sm=2)
+    b.set_launch(block=128, ctas_per_sm=2, build=2)
     b.enable_graph(True)
     b.step(2)
     assert np.array_equal(a.positions(), b.positions())
@@ -144,7 +144,7 @@ def test_autotune_restores_state_and_keeps_results():
         s.step(2)
     before = b.positions().copy(), b.velocities().copy()
     best, trials = b.autotune(substeps=2)
-    assert len(trials) == 6 and best["block"] in (128, 256) and best["cell_ratio"] == 1.0
+    assert len(trials) == 12 and best["block"] in (128, 256) and best["cell_ratio"] == 1.0
     assert all(t["ms_per_substep"] > 0 for t in trials)
     assert b.launch() == best
     assert np.array_equal(b.positions(), before[0]) and np.array_equal(b.velocities(), before[1])

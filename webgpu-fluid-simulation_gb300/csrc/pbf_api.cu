@@ -97,6 +97,7 @@ struct pbf_handle {
   uint32_t grid_cap = 0;    // CTAs per launch at most (0: one tile of blk slots per CTA)
   uint32_t per_sm = 0;      // grid_cap / SM count as set by the caller
   float cell_ratio = 1.0f;  // grid cell edge / h
+  uint32_t build = PBF_BUILD_THREAD;  // neighbour-build variant
   int sms = 152;            // SM count of the device
   unsigned fb_grid = 0;     // CTAs of the cooperative fallback kernel (resident wave)
   // batched scenes (pbf_batch_create)
@@ -357,8 +358,17 @@ int substep(pbf_handle* h, cudaEvent_t* ev) {
   const float sub_index = (float)(h->substep_counter % h->cfg.substeps);
   {
     KScope ks(h, K_NBR_BUILD);
-    ps.nbr_build<<<grid_of(h, n), h->blk, 0, st>>>(p, g, h->tab, h->xs[0].p, h->cell_start.p, ms, h->nbr_list.p,
-                                                    h->nbr_count.p, h->nbr_max.p, h->err_word.p);
+    if (h->build == PBF_BUILD_PAIR)
+      ps.nbr_build2<<<grid_of(h, (n + 1) / 2), h->blk, 0, st>>>(p, g, h->tab, h->xs[0].p, h->cell_start.p, ms,
+                                                                  h->nbr_list.p, h->nbr_count.p, h->nbr_max.p,
+                                                                  h->err_word.p);
+    else if (h->build == PBF_BUILD_WARP)
+      ps.nbr_build_warp<<<grid_of(h, n), h->blk, 0, st>>>(p, g, h->tab, h->xs[0].p, h->cell_start.p, ms,
+                                                           h->nbr_list.p, h->nbr_count.p, h->nbr_max.p,
+                                                           h->err_word.p);
+    else
+      ps.nbr_build<<<grid_of(h, n), h->blk, 0, st>>>(p, g, h->tab, h->xs[0].p, h->cell_start.p, ms, h->nbr_list.p,
+                                                      h->nbr_count.p, h->nbr_max.p, h->err_word.p);
   }
   CU(h, cudaGetLastError());
   if (ev) CU(h, cudaEventRecord(ev[2], st));
@@ -741,9 +751,11 @@ int apply_launch(pbf_handle* h, const pbf_launch& l) {
   if (l.block != 128 && l.block != 256) return fail(h, PBF_EINVAL, "block must be 128 or 256");
   if (l.ctas_per_sm > 16) return fail(h, PBF_EINVAL, "ctas_per_sm must be 0..16");
   if (l.cell_ratio != 1.0f && l.cell_ratio != 0.5f) return fail(h, PBF_EINVAL, "cell_ratio must be 1 or 0.5");
+  if (l.build > PBF_BUILD_WARP) return fail(h, PBF_EINVAL, "unknown neighbour-build variant %u", l.build);
   int rc = apply_cell_ratio(h, l.cell_ratio);
   if (rc) return rc;
-  if ((int)l.block != h->blk || l.ctas_per_sm != h->per_sm) invalidate_graph(h);
+  if ((int)l.block != h->blk || l.ctas_per_sm != h->per_sm || l.build != h->build) invalidate_graph(h);
+  h->build = l.build;
   h->blk = (int)l.block;
   h->per_sm = l.ctas_per_sm;
   h->grid_cap = l.ctas_per_sm * (uint32_t)h->sms;
@@ -1531,6 +1543,7 @@ int pbf_get_launch(const pbf_handle* h, pbf_launch* l) {
   l->block = (uint32_t)h->blk;
   l->ctas_per_sm = h->per_sm;
   l->cell_ratio = h->cell_ratio;
+  l->build = h->build;
   return PBF_OK;
 }
 
@@ -1592,13 +1605,15 @@ int pbf_autotune(pbf_handle* h, uint32_t substeps, uint32_t flags, pbf_tune_tria
   };
   std::vector<pbf_launch> cand;
   const float ratios[2] = {1.0f, 0.5f};
-  // one tile per CTA, or persistent grids holding half or all of an SM's
-  // 2048 threads
+  // one tile per CTA or a persistent grid holding all of an SM's 2048
+  // threads; the three neighbour-build variants
   const uint32_t blocks[2] = {128, 256};
   for (int r = 0; r < ((flags & PBF_TUNE_CELL_RATIO) ? 2 : 1); ++r)
     for (uint32_t b : blocks)
-      for (uint32_t k : {0u, 1024u / b, 2048u / b}) cand.push_back(pbf_launch{b, k, ratios[r]});
-  const pbf_launch orig{(uint32_t)h->blk, h->per_sm, h->cell_ratio};
+      for (uint32_t k : {0u, 2048u / b})
+        for (uint32_t bv : {PBF_BUILD_THREAD, PBF_BUILD_PAIR, PBF_BUILD_WARP})
+          cand.push_back(pbf_launch{b, k, ratios[r], bv});
+  const pbf_launch orig{(uint32_t)h->blk, h->per_sm, h->cell_ratio, h->build};
   const bool kt = h->ktiming;
   h->ktiming = false;
   cudaEvent_t e0 = nullptr, e1 = nullptr;

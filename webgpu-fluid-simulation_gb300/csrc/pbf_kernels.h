@@ -17,6 +17,10 @@ struct PassSet {
                   uint32_t*, uint32_t*);
   void (*nbr_build)(SimParams, GridParams, SceneTab, const float4*, const uint32_t*, uint32_t, uint32_t*, uint32_t*,
                     uint32_t*, uint32_t*);
+  void (*nbr_build2)(SimParams, GridParams, SceneTab, const float4*, const uint32_t*, uint32_t, uint32_t*,
+                     uint32_t*, uint32_t*, uint32_t*);  // two slots per thread
+  void (*nbr_build_warp)(SimParams, GridParams, SceneTab, const float4*, const uint32_t*, uint32_t, uint32_t*,
+                         uint32_t*, uint32_t*, uint32_t*);  // warp-cooperative per cell
   void (*boundary)(SimParams, FieldParams, const float*, const float*, const uint8_t*, const float4*, float4*,
                    SolverAux);
   void (*lambda)(SimParams, int, const float4*, const float4*, uint32_t, const uint32_t*, const uint32_t*, float4*,

@@ -200,6 +200,191 @@ __global__ void __launch_bounds__(256) k_nbr_build(SimParams p, GridParams g0, S
   }
 }
 
+// The same build with two consecutive slots per thread.  Slots are sorted by
+// cell, so slots 2k and 2k+1 usually share a cell and therefore every
+// candidate run: each candidate is loaded once and tested against both
+// particles (half the loads and loop overhead per test).  A pair that spans
+// two cells (or scenes) walks its two neighbourhoods one after the other.
+// Lists, counts and their order are those of k_nbr_build.
+template <bool kBatch, bool kLoop>
+__global__ void __launch_bounds__(256) k_nbr_build2(SimParams p, GridParams g0, SceneTab tab,
+                                                    const float4* __restrict__ xs,
+                                                    const uint32_t* __restrict__ cell_start, uint32_t max_nbr,
+                                                    uint32_t* __restrict__ nbr_list, uint32_t* __restrict__ nbr_count,
+                                                    uint32_t* max_seen, uint32_t* err) {
+  const uint32_t npair = (p.n + 1u) >> 1;
+  PBF_TILES(npair) {
+    const uint32_t k = tile0 + threadIdx.x;
+    if (k < npair) {
+      const uint32_t ta = 2u * k, tb = ta + 1u;
+      const bool hb = tb < p.n;
+      const SceneDesc* sa = scene_of<kBatch>(tab, ta);
+      const GridParams ga = sa ? sa->grid : g0;
+      const f3 xa = xyz(xs[ta]);
+      const int ax = cell_axis(xa.x, ga.origin[0], ga.inv_cell[0], ga.dim[0]);
+      const int ay = cell_axis(xa.y, ga.origin[1], ga.inv_cell[1], ga.dim[1]);
+      const int az = cell_axis(xa.z, ga.origin[2], ga.inv_cell[2], ga.dim[2]);
+      uint32_t* outa = nbr_list + (size_t)(ta >> 5) * 32u * max_nbr + (ta & 31u);
+      uint32_t* outb = nbr_list + (size_t)(tb >> 5) * 32u * max_nbr + (tb & 31u);
+      uint32_t qa = 0, qb = 0;
+      f3 xb = xa;
+      bool joint = false;
+      GridParams gb = ga;
+      int bx = ax, by = ay, bz = az;
+      if (hb) {
+        const SceneDesc* sb = scene_of<kBatch>(tab, tb);
+        if (sb) gb = sb->grid;
+        xb = xyz(xs[tb]);
+        bx = cell_axis(xb.x, gb.origin[0], gb.inv_cell[0], gb.dim[0]);
+        by = cell_axis(xb.y, gb.origin[1], gb.inv_cell[1], gb.dim[1]);
+        bz = cell_axis(xb.z, gb.origin[2], gb.inv_cell[2], gb.dim[2]);
+        joint = cell_key(ax, ay, az, ga) == cell_key(bx, by, bz, gb);
+      }
+      if (joint) {
+        for (int dx = -ga.reach; dx <= ga.reach; ++dx)
+          for (int dy = -ga.reach; dy <= ga.reach; ++dy) {
+            Run r = run_of(ga, cell_start, ax, ay, az, dx, dy);
+            for (uint32_t u = r.b; u < r.e; ++u) {
+              const f3 xj = xyz(__ldg(xs + u));
+              const f3 da = xj - xa, db = xj - xb;
+              if (dot3(da, da) <= p.h2) {
+                if (qa < max_nbr) outa[32u * qa] = u;
+                ++qa;
+              }
+              if (dot3(db, db) <= p.h2) {
+                if (qb < max_nbr) outb[32u * qb] = u;
+                ++qb;
+              }
+            }
+          }
+      } else {
+        for (int dx = -ga.reach; dx <= ga.reach; ++dx)
+          for (int dy = -ga.reach; dy <= ga.reach; ++dy) {
+            Run r = run_of(ga, cell_start, ax, ay, az, dx, dy);
+            for (uint32_t u = r.b; u < r.e; ++u) {
+              const f3 d = xyz(__ldg(xs + u)) - xa;
+              if (dot3(d, d) <= p.h2) {
+                if (qa < max_nbr) outa[32u * qa] = u;
+                ++qa;
+              }
+            }
+          }
+        if (hb) {
+          for (int dx = -gb.reach; dx <= gb.reach; ++dx)
+            for (int dy = -gb.reach; dy <= gb.reach; ++dy) {
+              Run r = run_of(gb, cell_start, bx, by, bz, dx, dy);
+              for (uint32_t u = r.b; u < r.e; ++u) {
+                const f3 d = xyz(__ldg(xs + u)) - xb;
+                if (dot3(d, d) <= p.h2) {
+                  if (qb < max_nbr) outb[32u * qb] = u;
+                  ++qb;
+                }
+              }
+            }
+        }
+      }
+      nbr_count[ta] = qa;
+      if (hb) nbr_count[tb] = qb;
+      const uint32_t q = max(qa, qb);
+      const unsigned m = __activemask();
+      if (__any_sync(m, q > max_nbr)) {
+        unsigned wmax = __reduce_max_sync(m, q);
+        if ((threadIdx.x & 31u) == (unsigned)(__ffs(m) - 1)) {
+          atomicMax(max_seen, wmax);
+          atomicOr(err, 0x1u);
+        }
+      }
+    }
+  }
+}
+
+// The same build, warp-cooperative per cell.  The 32 sorted slots of a warp
+// fall into a few cells; for each cell group the warp walks the group's
+// candidate runs once, 32 candidates at a time (lane = candidate, coalesced
+// loads), tests each chunk against every particle of the group (its position
+// broadcast by shuffle, the hits collected by ballot into the owner lane's
+// mask), and each owner then appends its hits in slot order.  Lists, counts
+// and their order are those of k_nbr_build.
+template <bool kBatch, bool kLoop>
+__global__ void __launch_bounds__(256) k_nbr_build_warp(SimParams p, GridParams g0, SceneTab tab,
+                                                        const float4* __restrict__ xs,
+                                                        const uint32_t* __restrict__ cell_start, uint32_t max_nbr,
+                                                        uint32_t* __restrict__ nbr_list,
+                                                        uint32_t* __restrict__ nbr_count, uint32_t* max_seen,
+                                                        uint32_t* err) {
+  const uint32_t lane = threadIdx.x & 31u;
+  PBF_TILES(p.n) {
+    const uint32_t t = tile0 + threadIdx.x;
+    const bool valid = t < p.n;
+    GridParams g = g0;
+    f3 xi = mk(0.f, 0.f, 0.f);
+    int cx = 0, cy = 0, cz = 0;
+    uint32_t key = kNoKey;
+    if (valid) {
+      const SceneDesc* sd = scene_of<kBatch>(tab, t);
+      if (sd) g = sd->grid;
+      xi = xyz(xs[t]);
+      cx = cell_axis(xi.x, g.origin[0], g.inv_cell[0], g.dim[0]);
+      cy = cell_axis(xi.y, g.origin[1], g.inv_cell[1], g.dim[1]);
+      cz = cell_axis(xi.z, g.origin[2], g.inv_cell[2], g.dim[2]);
+      key = cell_key(cx, cy, cz, g);
+    }
+    const unsigned peers = __match_any_sync(kFull, key);
+    unsigned todo = __ballot_sync(kFull, valid);
+    uint32_t* out = nbr_list + (size_t)(t >> 5) * 32u * max_nbr + lane;
+    uint32_t q = 0;
+    while (todo) {
+      const int leader = __ffs(todo) - 1;
+      const unsigned gm = __shfl_sync(kFull, peers, leader);
+      todo &= ~gm;
+      const int lx = __shfl_sync(kFull, cx, leader), ly = __shfl_sync(kFull, cy, leader),
+                lz = __shfl_sync(kFull, cz, leader);
+      GridParams gl = g0;
+      if constexpr (kBatch) {  // the group's scene grid (run bounds and keys only)
+        gl.dim[0] = __shfl_sync(kFull, g.dim[0], leader);
+        gl.dim[1] = __shfl_sync(kFull, g.dim[1], leader);
+        gl.dim[2] = __shfl_sync(kFull, g.dim[2], leader);
+        gl.key_base = __shfl_sync(kFull, g.key_base, leader);
+        gl.reach = __shfl_sync(kFull, g.reach, leader);
+      }
+      for (int dx = -gl.reach; dx <= gl.reach; ++dx)
+        for (int dy = -gl.reach; dy <= gl.reach; ++dy) {
+          const Run r = run_of(gl, cell_start, lx, ly, lz, dx, dy);
+          for (uint32_t u0 = r.b; u0 < r.e; u0 += 32u) {
+            const uint32_t u = u0 + lane;
+            const bool in = u < r.e;
+            const f3 c = xyz(__ldg(xs + (in ? u : u0)));
+            unsigned mine = 0u;
+            unsigned pm = gm;
+            while (pm) {
+              const int pl = __ffs(pm) - 1;
+              pm &= pm - 1u;
+              const f3 xp = mk(__shfl_sync(kFull, xi.x, pl), __shfl_sync(kFull, xi.y, pl),
+                               __shfl_sync(kFull, xi.z, pl));
+              const f3 d = c - xp;
+              const unsigned hits = __ballot_sync(kFull, in && dot3(d, d) <= p.h2);
+              if ((int)lane == pl) mine = hits;
+            }
+            while (mine) {
+              const int b = __ffs(mine) - 1;
+              mine &= mine - 1u;
+              if (q < max_nbr) out[32u * q] = u0 + (uint32_t)b;
+              ++q;
+            }
+          }
+        }
+    }
+    if (valid) nbr_count[t] = q;
+    if (__any_sync(kFull, q > max_nbr)) {
+      const unsigned wmax = __reduce_max_sync(kFull, q);
+      if (lane == 0) {
+        atomicMax(max_seen, wmax);
+        atomicOr(err, 0x1u);
+      }
+    }
+  }
+}
+
 // NeighborList: the same traversal writing slot indices at nbr_offset[t].
 __global__ void __launch_bounds__(256) k_nbr_list(SimParams p, GridParams g, const float4* __restrict__ xs,
                                                   const uint32_t* __restrict__ cell_start,
@@ -692,6 +877,8 @@ template <bool B, bool P>
 void fill_set(PassSet* ps) {
   ps->predict = k_predict<B, P>;
   ps->nbr_build = k_nbr_build<B, P>;
+  ps->nbr_build2 = k_nbr_build2<B, P>;
+  ps->nbr_build_warp = k_nbr_build_warp<B, P>;
   ps->boundary = k_boundary<B, P>;
   ps->lambda = k_lambda<0, B, P>;
   ps->lambda_feat = B ? nullptr : k_lambda<1, false, P>;

@@ -75,7 +75,9 @@ class Grid(ctypes.Structure):
 
 
 class Launch(ctypes.Structure):
-    _fields_ = [("block", u32), ("ctas_per_sm", u32), ("cell_ratio", f32)]
+    _fields_ = [("block", u32), ("ctas_per_sm", u32), ("cell_ratio", f32), ("build", u32)]
+
+BUILD_THREAD, BUILD_PAIR, BUILD_WARP = 0, 1, 2
 
 
 class TuneTrial(ctypes.Structure):

@@ -274,14 +274,15 @@ class PBF:
         return {"acceleration": self.copy_field(L.FIELD_ACCELERATION), "metrics": self.metrics()}
 
     # ---- launch shape and autotuner (no reference counterpart) -------------
-    def set_launch(self, block=256, ctas_per_sm=0, cell_ratio=1.0):
-        lc = L.Launch(int(block), int(ctas_per_sm), float(cell_ratio))
+    def set_launch(self, block=256, ctas_per_sm=0, cell_ratio=1.0, build=0):
+        lc = L.Launch(int(block), int(ctas_per_sm), float(cell_ratio), int(build))
         self._check(self._lib.pbf_set_launch(self._h, ctypes.byref(lc)), "set_launch")
 
     def launch(self):
         lc = L.Launch()
         self._check(self._lib.pbf_get_launch(self._h, ctypes.byref(lc)), "get_launch")
-        return {"block": lc.block, "ctas_per_sm": lc.ctas_per_sm, "cell_ratio": lc.cell_ratio}
+        return {"block": lc.block, "ctas_per_sm": lc.ctas_per_sm, "cell_ratio": lc.cell_ratio,
+                "build": lc.build}
 
     def autotune(self, substeps=4, cell_ratio=False):
         """Times every candidate launch shape on the current state (restored
@@ -292,7 +293,8 @@ class PBF:
         flags = L.TUNE_CELL_RATIO if cell_ratio else 0
         self._check(self._lib.pbf_autotune(self._h, int(substeps), flags, trials, 32, ctypes.byref(cnt),
                                            ctypes.byref(best)), "autotune")
-        as_dict = lambda lc: {"block": lc.block, "ctas_per_sm": lc.ctas_per_sm, "cell_ratio": lc.cell_ratio}
+        as_dict = lambda lc: {"block": lc.block, "ctas_per_sm": lc.ctas_per_sm, "cell_ratio": lc.cell_ratio,
+                              "build": lc.build}
         return as_dict(best), [dict(as_dict(t.launch), ms_per_substep=t.ms_per_substep)
                                for t in trials[:min(cnt.value, 32)]]
 

@@ -76,13 +76,43 @@ def run_ns(cfg, pts, lists=False):
 
 
 @pytest.mark.parametrize("dist,n", [("uniform", 200000), ("clumps", 200000), ("uniform", 1 << 20),
-                                    ("clumps", 1 << 20)])
+                                    ("clumps", 1 << 20), ("uniform", 1 << 22), ("clumps", 1 << 22)])
 def test_neighbor_search_bitexact(dist, n):
     cfg, pts = scenes.neighbor_case(n, dist, seed=11, dim=128)
     ref = O.neighbor_search(cfg, pts)
     got = run_ns(cfg, pts)
     for k in ("keys", "cell_count", "cell_offset", "order", "rank"):
         assert np.array_equal(got[k], ref[k]), k
+
+
+@pytest.mark.parametrize("dist", ["uniform", "clumps"])
+def test_neighbor_search_16m_properties(dist):
+    """2^24 particles (the largest neighbour-search size): checked through
+    size-independent properties instead of the oracle — keys from the cell
+    formula, counts = histogram of keys, offsets = exclusive scan of counts,
+    order a permutation sorted by key and, within a cell, by particle id,
+    ranks placing every particle at its sorted position."""
+    n = 1 << 24
+    cfg, pts = scenes.neighbor_case(n, dist, seed=13, dim=128)
+    got = run_ns(cfg, pts)
+    dims = np.array([128, 128, 128])
+    inv = np.float32(128.0)  # unit cube, 128 cells per axis
+    c = np.floor(pts[:, :3] * inv).astype(np.int64)
+    c = np.clip(c, 0, dims - 1)
+    keys = (c[:, 0] * 128 + c[:, 1]) * 128 + c[:, 2]  # x-major keys
+    assert np.array_equal(got["keys"].astype(np.int64), keys)
+    cnt = np.bincount(keys, minlength=128 ** 3)
+    assert np.array_equal(got["cell_count"].astype(np.int64), cnt)
+    off = np.concatenate([[0], np.cumsum(cnt)])
+    assert np.array_equal(got["cell_offset"].astype(np.int64), off)
+    order = got["order"].astype(np.int64)
+    assert np.array_equal(np.sort(order), np.arange(n))
+    k_sorted = keys[order]
+    assert np.all(np.diff(k_sorted) >= 0)
+    same = np.diff(k_sorted) == 0
+    assert np.all(np.diff(order)[same] > 0)  # stable by id within a cell
+    pos = off[keys] + got["rank"].astype(np.int64)
+    assert np.array_equal(order[pos], np.arange(n))
 
 
 def test_neighbor_search_full_cells():

@@ -62,6 +62,7 @@ struct pbf_handle {
   DBuf<uint32_t> ids[2], key, rank, perm_raw, id_raw, perm, tmp_a, tmp_b;
   DBuf<uint32_t> cell_count, cell_start, big_list, big_count;
   DBuf<uint32_t> nbr_count, nbr_max, nbr_list;
+  DBuf<uint32_t> band_list[2], band_count;  // boundary band lists (ping-pong) and their lengths
   DBuf<float> sdf, vol;
   DBuf<uint8_t> bflag;  // per field cell: 1 when the boundary sample can be non-zero
   DBuf<uint32_t> err_word;
@@ -372,33 +373,49 @@ int substep(pbf_handle* h, cudaEvent_t* ev) {
   }
   CU(h, cudaGetLastError());
   if (ev) CU(h, cudaEventRecord(ev[2], st));
-  // constraint loop
+  // constraint loop.  Boundary sampling works on a band list (BandArgs): the
+  // band pass builds it at x*_0, each delta-p pass marks the band of the next
+  // iteration at the positions it writes, and the sampling kernel interpolates
+  // the volume map for the listed slots only.
+  CU(h, cudaMemsetAsync(h->band_count.p, 0, 2 * sizeof(uint32_t), st));
+  int band = -1;  // band list holding the current iteration's band (-1: not built)
+  const unsigned band_grid = std::min(nblocks(n, 256), (unsigned)h->sms * 2u);  // one resident wave
+  auto band_args = [&](int list, float* bsdf) {
+    BandArgs B{};
+    B.f = f;
+    B.flag = h->bflag.p;
+    B.bdata = h->bdata.p;
+    B.bsdf = bsdf;
+    B.list = h->band_list[list].p;
+    B.count = h->band_count.p + list;
+    return B;
+  };
+  // Boundary sampling at x*_a (bsdf: also the SDF feature).
+  auto sample_boundary = [&](int a, float* bsdf) -> cudaError_t {
+    KScope ks(h, K_BOUNDARY);
+    if (band < 0) {
+      ps.band<<<grid_of(h, n), h->blk, 0, st>>>(p, h->tab, h->xs[a].p, band_args(0, bsdf));
+      band = 0;
+    }
+    ps.boundary_band<<<band_grid, 256, 0, st>>>(p, f, h->sdf.p, h->vol.p, h->tab, h->xs[a].p, h->bdata.p, bsdf,
+                                                 h->band_list[band].p, h->band_count.p + band,
+                                                 h->band_count.p + (1 - band));
+    return cudaGetLastError();
+  };
   // `iters` plain iterations starting from xs[a]; returns the buffer holding
-  // the result.  aux0 is used by the first iteration's lambda pass (features
-  // and/or starting lam_sum), stats by the last one; guard makes every
-  // launch conditional on the device flag (fallback path).
-  // Guarded launches (the learned start's fallback re-solve, normally a
-  // no-op) use the persistent variants with one wave of CTAs, so that an
-  // unset flag costs one short wave instead of a full grid.
-  const PassSet& pg = h->passes.set[h->batch ? 1 : 0][1];
-  const unsigned guard_grid = std::min(nblocks(n, h->blk), (unsigned)h->sms * (2048u / (unsigned)h->blk));
+  // the result.  The first iteration's lambda pass records the features
+  // (feat_first) and/or starts lam_sum; stats go with the last one.
+  // mark_last: the last delta-p also marks the band for a boundary sampling
+  // that follows.
   auto iterate = [&](int a, uint32_t iters, bool feat_first, bool lam_sum_on, bool first_starts_sum,
-                     SolveStats* stats, const int* guard, int* rc) -> int {
-    const PassSet& pi = guard ? pg : ps;
-    const unsigned gi = guard ? guard_grid : grid_of(h, n);
+                     SolveStats* stats, int* rc) -> int {
     for (uint32_t it = 0; it < iters; ++it) {
-      SolverAux ab{};
-      ab.guard = guard;
-      ab.tab = h->tab;
-      ab.iter = (int)it;
-      if (need_feat && feat_first && it == 0) ab.bsdf = h->bsdf.p;
-      if (f.loaded) {
-        KScope ks(h, guard ? K_FALLBACK : K_BOUNDARY);
-        pi.boundary<<<gi, h->blk, 0, st>>>(p, f, h->sdf.p, h->vol.p, h->bflag.p, h->xs[a].p, h->bdata.p, ab);
+      if (f.loaded && sample_boundary(a, (need_feat && feat_first && it == 0) ? h->bsdf.p : nullptr) !=
+                          cudaSuccess) {
+        *rc = PBF_ECUDA;
+        return a;
       }
-      if (cudaGetLastError() != cudaSuccess) { *rc = PBF_ECUDA; return a; }
       SolverAux al{};
-      al.guard = guard;
       al.tab = h->tab;
       al.iter = (int)it;
       if (lam_sum_on) {
@@ -415,21 +432,24 @@ int substep(pbf_handle* h, cudaEvent_t* ev) {
         al.substep_index = sub_index;
       }
       {
-        KScope ks(h, guard ? K_FALLBACK : K_LAMBDA);
-        auto kl = fe ? pi.lambda_feat : pi.lambda;
-        kl<<<gi, h->blk, 0, st>>>(p, f.loaded, h->bdata.p, h->xs[a].p, ms, h->nbr_count.p, h->nbr_list.p, h->xl.p,
-                                  al);
+        KScope ks(h, K_LAMBDA);
+        auto kl = fe ? ps.lambda_feat : ps.lambda;
+        kl<<<grid_of(h, n), h->blk, 0, st>>>(p, f.loaded, h->bdata.p, h->xs[a].p, ms, h->nbr_count.p,
+                                             h->nbr_list.p, h->xl.p, al);
       }
       if (cudaGetLastError() != cudaSuccess) { *rc = PBF_ECUDA; return a; }
       SolverAux ad{};
-      ad.guard = guard;
       ad.tab = h->tab;
       ad.iter = (int)it;
       ad.xs_in = h->xs[a].p;
+      if (f.loaded && it + 1 < iters) {  // the next iteration's band, at the positions written now
+        ad.band = band_args(1 - band, nullptr);
+        band = 1 - band;
+      }
       {
-        KScope ks(h, guard ? K_FALLBACK : K_DELTAP);
-        pi.deltap<<<gi, h->blk, 0, st>>>(p, ad, f.loaded, h->xl.p, h->bdata.p, ms, h->nbr_count.p, h->nbr_list.p,
-                                         h->xs[1 - a].p, h->capture ? h->dp.p : nullptr);
+        KScope ks(h, K_DELTAP);
+        ps.deltap<<<grid_of(h, n), h->blk, 0, st>>>(p, ad, f.loaded, h->xl.p, h->bdata.p, ms, h->nbr_count.p,
+                                                     h->nbr_list.p, h->xs[1 - a].p, h->capture ? h->dp.p : nullptr);
       }
       if (cudaGetLastError() != cudaSuccess) { *rc = PBF_ECUDA; return a; }
       a = 1 - a;
@@ -443,14 +463,7 @@ int substep(pbf_handle* h, cudaEvent_t* ev) {
     // lambda_hat) -> one projection -> learned_iters plain iterations ->
     // device-side fallback test
     CU(h, cudaMemcpyAsync(h->xs_save.p, h->xs[0].p, (size_t)n * sizeof(float4), cudaMemcpyDeviceToDevice, st));
-    SolverAux ab{};
-    ab.bsdf = h->bsdf.p;
-    if (f.loaded) {
-      KScope ks(h, K_BOUNDARY);
-      ps.boundary<<<grid_of(h, n), h->blk, 0, st>>>(p, f, h->sdf.p, h->vol.p, h->bflag.p, h->xs[0].p, h->bdata.p,
-                                                     ab);
-    }
-    CU(h, cudaGetLastError());
+    if (f.loaded) CU(h, sample_boundary(0, h->bsdf.p));
     SolverAux al{};
     al.pos = h->pos[cc].p;
     al.lam_prev = h->lam_prev.p;
@@ -471,15 +484,18 @@ int substep(pbf_handle* h, cudaEvent_t* ev) {
     {
       KScope ks(h, K_DELTAP);
       SolverAux ad{};
-      ps.deltap<<<grid_of(h, n), h->blk, 0, st>>>(p, ad, f.loaded, h->xl.p, h->bdata.p,
-                                                         ms, h->nbr_count.p, h->nbr_list.p,
-                                                         h->xs[1].p, nullptr);
+      if (f.loaded && h->learned_iters > 0) {
+        ad.band = band_args(1 - band, nullptr);
+        band = 1 - band;
+      }
+      ps.deltap<<<grid_of(h, n), h->blk, 0, st>>>(p, ad, f.loaded, h->xl.p, h->bdata.p, ms, h->nbr_count.p,
+                                                   h->nbr_list.p, h->xs[1].p, nullptr);
     }
     CU(h, cudaGetLastError());
-    a = iterate(1, h->learned_iters, false, true, false, nullptr, nullptr, &rc);
+    a = iterate(1, h->learned_iters, false, true, false, nullptr, &rc);
     if (rc) return fail(h, rc, "learned solve launch failed");
   } else {
-    a = iterate(0, h->cfg.options.iterations, need_feat, need_feat, true, nullptr, nullptr, &rc);
+    a = iterate(0, h->cfg.options.iterations, need_feat, need_feat, true, nullptr, &rc);
     if (rc) return fail(h, rc, "solve launch failed");
     if (h->trace_cap > 0) {
       CU(h, launch_trace_append(n, h->ids[cc].p, h->feat.p, h->lam_sum.p, h->trace_stride,
@@ -620,6 +636,9 @@ void release_all(pbf_handle* h) {
   h->bflag.release();
   h->scenes_dev.release();
   h->slot_scene.release();
+  h->band_list[0].release();
+  h->band_list[1].release();
+  h->band_count.release();
   h->mlp_params.release();
   h->lam_sum.release();
   h->lam_prev.release();
@@ -905,6 +924,9 @@ int pbf_create(const pbf_config* cfg, pbf_handle** out) {
   A(h->big_count.alloc(1));
   A(h->nbr_count.alloc(cap + 1));
   A(h->nbr_max.alloc(1));
+  A(h->band_list[0].alloc(cap));
+  A(h->band_list[1].alloc(cap));
+  A(h->band_count.alloc(2));
   A(h->nbr_list.alloc(rows * h->nbr_slice));
   A(h->xl.alloc(cap));
   A(h->err_word.alloc(1));

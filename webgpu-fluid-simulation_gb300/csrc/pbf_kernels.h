@@ -21,8 +21,9 @@ struct PassSet {
                      uint32_t*, uint32_t*, uint32_t*);  // two slots per thread
   void (*nbr_build_warp)(SimParams, GridParams, SceneTab, const float4*, const uint32_t*, uint32_t, uint32_t*,
                          uint32_t*, uint32_t*, uint32_t*);  // warp-cooperative per cell
-  void (*boundary)(SimParams, FieldParams, const float*, const float*, const uint8_t*, const float4*, float4*,
-                   SolverAux);
+  void (*band)(SimParams, SceneTab, const float4*, BandArgs);
+  void (*boundary_band)(SimParams, FieldParams, const float*, const float*, SceneTab, const float4*, float4*, float*,
+                        const uint32_t*, const uint32_t*, uint32_t*);
   void (*lambda)(SimParams, int, const float4*, const float4*, uint32_t, const uint32_t*, const uint32_t*, float4*,
                  SolverAux);
   void (*lambda_feat)(SimParams, int, const float4*, const float4*, uint32_t, const uint32_t*, const uint32_t*,

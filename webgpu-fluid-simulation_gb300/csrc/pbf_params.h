@@ -61,6 +61,20 @@ struct SceneDesc {
   uint32_t first, n;
 };
 
+// Boundary band of the next boundary sampling: the particles whose field
+// cell can produce a sample.  Whoever computes a new x* (the band pass, or
+// delta-p for the next iteration) tests the cell flag: outside the band it
+// writes bData = 0 (and SDF feature = 2h) at once, inside it appends the slot
+// to the list that the sampling kernel then works through.
+struct BandArgs {
+  FieldParams f;        // the map (a batch uses each scene's own)
+  const uint8_t* flag;  // per field cell, concatenated for batches
+  float4* bdata;
+  float* bsdf;          // optional: the learned start's SDF feature
+  uint32_t* list;       // null: no band is built
+  uint32_t* count;
+};
+
 // Per-slot scene lookup of a batch; scene == nullptr for a single scene
 // (every parameter then comes by value).
 struct SceneTab {
@@ -92,6 +106,7 @@ struct SolverAux {
   SceneTab tab;              // batched scenes: per-scene iteration counts, domains, maps
   int iter;                  // solver iteration of this launch (scenes with fewer iterations skip it)
   const float4* xs_in;       // delta-p pass: x* of a scene that skips the iteration is copied through
+  BandArgs band;             // delta-p pass: the band of the next iteration's boundary sampling
 };
 
 // The learned start's fallback: the plain solve of one substep from the saved

@@ -479,10 +479,9 @@ __device__ __forceinline__ bool iter_active(const SceneDesc* sd, int iter) {
   return !sd || (uint32_t)iter < sd->iterations;
 }
 
-// BoundaryVolume (boundaryVolume.ts:26-57): (x_b, V_b) per particle, skipping
-// the 64-node interpolation where the field cell cannot produce a sample.  In
-// a batch each scene samples its own map (offsets into the concatenated
-// arrays); a scene without a map gets (0, 0).
+// BoundaryVolume (boundaryVolume.ts:26-57) of slot t: (x_b, V_b), skipping
+// the 64-node interpolation where the field cell cannot produce a sample (the
+// fallback solve's boundary phase; the step samples through the band list).
 template <bool kC>
 __device__ __forceinline__ void boundary_slot(const SimParams& p, const FieldParams& f, const float* __restrict__ sdf0,
                                               const float* __restrict__ vol0, const uint8_t* __restrict__ bflag0,
@@ -505,17 +504,57 @@ __device__ __forceinline__ void boundary_slot(const SimParams& p, const FieldPar
   if (bsdf) bsdf[t] = dist;
 }
 
+// Band test of slot t at x (see BandArgs): outside the band bData = 0 (and
+// the SDF feature 2h) at once; inside, the slot joins the list (one atomic
+// per warp).  Lanes that call this together must be the active ones.
+template <bool kBatch>
+__device__ __forceinline__ void band_mark(const SimParams& p, const BandArgs& B, const SceneTab& tab, uint32_t t,
+                                          f3 x) {
+  const SceneDesc* sd = scene_of<kBatch>(tab, t);
+  const FieldParams& f = sd ? sd->field : B.f;
+  const bool in = f.loaded && boundary_possible(f, B.flag ? B.flag + f.flag_off : nullptr, x);
+  if (!in) {
+    B.bdata[t] = make_float4(0.f, 0.f, 0.f, 0.f);
+    if (B.bsdf) B.bsdf[t] = 2.0f * p.h;
+  }
+  const unsigned m = __activemask();
+  const unsigned b = __ballot_sync(m, in);
+  if (b) {
+    const int leader = __ffs(m) - 1;
+    uint32_t base = 0;
+    if ((int)(threadIdx.x & 31u) == leader) base = atomicAdd(B.count, (uint32_t)__popc(b));
+    base = __shfl_sync(m, base, leader);
+    if (in) B.list[base + __popc(b & ((1u << (threadIdx.x & 31u)) - 1u))] = t;
+  }
+}
+
+// The band at the predicted positions x*_0 (the first boundary sampling of a
+// substep; later ones are marked by delta-p).
 template <bool kBatch, bool kLoop>
-__global__ void __launch_bounds__(256, 3) k_boundary(SimParams p, FieldParams f0, const float* __restrict__ sdf0,
-                                                     const float* __restrict__ vol0,
-                                                     const uint8_t* __restrict__ bflag0,
-                                                     const float4* __restrict__ xs, float4* __restrict__ bdata,
-                                                     SolverAux a) {
-  if (a.guard && *a.guard == 0) return;
-  PBF_SLOTS(t, p.n) {
-    const SceneDesc* sd = scene_of<kBatch>(a.tab, t);
-    if (!iter_active(sd, a.iter)) continue;
-    boundary_slot<false>(p, sd ? sd->field : f0, sdf0, vol0, bflag0, xs, bdata, a.bsdf, t);
+__global__ void __launch_bounds__(256) k_band(SimParams p, SceneTab tab, const float4* __restrict__ xs, BandArgs B) {
+  PBF_SLOTS(t, p.n) band_mark<kBatch>(p, B, tab, t, xyz(xs[t]));
+}
+
+// BoundaryVolume for the band's slots only: a grid of resident CTAs walks the
+// list (its length is known on the device only).  Also clears the count of
+// the other band list, which delta-p fills next.
+template <bool kBatch>
+__global__ void __launch_bounds__(256, 2) k_boundary_band(SimParams p, FieldParams f0, const float* __restrict__ sdf0,
+                                                          const float* __restrict__ vol0, SceneTab tab,
+                                                          const float4* __restrict__ xs, float4* __restrict__ bdata,
+                                                          float* __restrict__ bsdf, const uint32_t* __restrict__ list,
+                                                          const uint32_t* count, uint32_t* other_count) {
+  if (other_count && blockIdx.x == 0 && threadIdx.x == 0) *other_count = 0u;
+  const uint32_t nb = *count;
+  for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < nb; i += gridDim.x * blockDim.x) {
+    const uint32_t t = list[i];
+    const SceneDesc* sd = scene_of<kBatch>(tab, t);
+    const FieldParams f = sd ? sd->field : f0;
+    const float* sdf = sdf0 + f.node_off;
+    const float* vol = vol0 + f.node_off;
+    const f3 xi = xyz(xs[t]);
+    if (bsdf) bsdf[t] = boundary_distance(f, sdf, xi);
+    bdata[t] = boundary_sample(p, f, sdf, vol, xi);
   }
 }
 
@@ -676,13 +715,16 @@ __global__ void __launch_bounds__(256) k_deltap(SimParams p, SolverAux a, int ha
     f3 xi;
     const f3 dp = deltap_slot<false>(p, have_field, xl, bdata, max_nbr, nbr_cnt, nbr_list, t, xi);
     if (dp_out) dp_out[t] = f4(dp, 0.0f);
+    f3 xn;
     if constexpr (kBatch) {  // the scene's own domain (looked up after the loop: no registers held across it)
       SimParams ps = p;
       scene_domain(ps, scene_of<kBatch>(a.tab, t));
-      xs_out[t] = f4(clamp_rand(ps, xi + dp), 0.0f);
+      xn = clamp_rand(ps, xi + dp);
     } else {
-      xs_out[t] = f4(clamp_rand(p, xi + dp), 0.0f);
+      xn = clamp_rand(p, xi + dp);
     }
+    xs_out[t] = f4(xn, 0.0f);
+    if (a.band.list) band_mark<kBatch>(p, a.band, a.tab, t, xn);
   }
 }
 
@@ -879,7 +921,8 @@ void fill_set(PassSet* ps) {
   ps->nbr_build = k_nbr_build<B, P>;
   ps->nbr_build2 = k_nbr_build2<B, P>;
   ps->nbr_build_warp = k_nbr_build_warp<B, P>;
-  ps->boundary = k_boundary<B, P>;
+  ps->band = k_band<B, P>;
+  ps->boundary_band = k_boundary_band<B>;
   ps->lambda = k_lambda<0, B, P>;
   ps->lambda_feat = B ? nullptr : k_lambda<1, false, P>;
   ps->features = B ? nullptr : k_features<P>;

@@ -59,6 +59,7 @@ struct pbf_handle {
   std::vector<float> host_particles;  // SPH.particlePositionArray
 
   DBuf<float4> pos[2], xs[2], xl, vel, acc, bdata, omega, normal, dp, out_pos, out_tmp;
+  DBuf<float4> visc, coh;  // fast mode: XSPH's viscosity and cohesion sums from the vorticity pass
   DBuf<uint32_t> ids[2], key, rank, perm_raw, id_raw, perm, tmp_a, tmp_b;
   DBuf<uint32_t> cell_count, cell_start, big_list, big_count;
   DBuf<uint32_t> nbr_count, nbr_max, nbr_list;
@@ -557,18 +558,34 @@ int substep(pbf_handle* h, cudaEvent_t* ev) {
                                       dim3(256), args, 0, st));
   }
   if (a != 0) CU(h, cudaMemcpyAsync(h->xs[0].p, h->xs[1].p, (size_t)n * sizeof(float4), cudaMemcpyDeviceToDevice, st));
-  {
-    KScope ks(h, K_VORTICITY);
-    ps.vorticity<<<grid_of(h, n), h->blk, 0, st>>>(p, h->pos[cc].p, h->vel.p, ms, h->nbr_count.p, h->nbr_list.p, h->omega.p,
-                                                          h->normal.p);
+  if (ps.xsph_split) {  // fast mode: XSPH's sum split over the two passes
+    {
+      KScope ks(h, K_VORTICITY);
+      ps.vorticity_split<<<grid_of(h, n), h->blk, 0, st>>>(p, h->pos[cc].p, h->vel.p, ms, h->nbr_count.p,
+                                                            h->nbr_list.p, h->omega.p, h->normal.p, h->visc.p,
+                                                            h->coh.p);
+    }
+    CU(h, cudaGetLastError());
+    {
+      KScope ks(h, K_XSPH);
+      ps.xsph_split<<<grid_of(h, n), h->blk, 0, st>>>(p, h->pos[cc].p, h->omega.p, h->normal.p, h->visc.p, h->coh.p,
+                                                       ms, h->nbr_count.p, h->nbr_list.p, h->acc.p);
+    }
+    CU(h, cudaGetLastError());
+  } else {
+    {
+      KScope ks(h, K_VORTICITY);
+      ps.vorticity<<<grid_of(h, n), h->blk, 0, st>>>(p, h->pos[cc].p, h->vel.p, ms, h->nbr_count.p, h->nbr_list.p,
+                                                      h->omega.p, h->normal.p);
+    }
+    CU(h, cudaGetLastError());
+    {
+      KScope ks(h, K_XSPH);
+      ps.xsph<<<grid_of(h, n), h->blk, 0, st>>>(p, h->pos[cc].p, h->vel.p, h->omega.p, h->normal.p, ms,
+                                                 h->nbr_count.p, h->nbr_list.p, h->acc.p);
+    }
+    CU(h, cudaGetLastError());
   }
-  CU(h, cudaGetLastError());
-  {
-    KScope ks(h, K_XSPH);
-    ps.xsph<<<grid_of(h, n), h->blk, 0, st>>>(p, h->pos[cc].p, h->vel.p, h->omega.p, h->normal.p,
-                                                     ms, h->nbr_count.p, h->nbr_list.p, h->acc.p);
-  }
-  CU(h, cudaGetLastError());
   if (ev) CU(h, cudaEventRecord(ev[4], st));
   return PBF_OK;
 }
@@ -624,6 +641,7 @@ int upload_particles(pbf_handle* h, const float* xyzw, uint32_t n) {
 void release_all(pbf_handle* h) {
   invalidate_graph(h);
   DBuf<float4>* f4s[] = {&h->pos[0], &h->pos[1], &h->xs[0], &h->xs[1], &h->xl, &h->vel, &h->acc, &h->bdata,
+                         &h->visc,   &h->coh,
                          &h->omega,  &h->normal, &h->dp,    &h->out_pos, &h->out_tmp};
   for (auto* b : f4s) b->release();
   DBuf<uint32_t>* u32s[] = {&h->ids[0],   &h->ids[1],      &h->key,      &h->rank,      &h->perm_raw,
@@ -909,6 +927,10 @@ int pbf_create(const pbf_config* cfg, pbf_handle** out) {
   A(h->bdata.alloc(cap));
   A(h->omega.alloc(cap));
   A(h->normal.alloc(cap));
+  if (cfg->fp_mode != PBF_FP_EXACT) {
+    A(h->visc.alloc(cap));
+    A(h->coh.alloc(cap));
+  }
   A(h->out_pos.alloc(cap));
   A(h->out_tmp.alloc(cap));
   A(h->key.alloc(cap));

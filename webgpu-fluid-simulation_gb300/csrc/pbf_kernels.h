@@ -38,6 +38,11 @@ struct PassSet {
                     float4*);
   void (*xsph)(SimParams, const float4*, const float4*, const float4*, const float4*, uint32_t, const uint32_t*,
                const uint32_t*, float4*);
+  // fast mode: XSPH's neighbour sum split over the vorticity and XSPH passes (null in exact mode)
+  void (*vorticity_split)(SimParams, const float4*, const float4*, uint32_t, const uint32_t*, const uint32_t*,
+                          float4*, float4*, float4*, float4*);
+  void (*xsph_split)(SimParams, const float4*, const float4*, const float4*, const float4*, const float4*, uint32_t,
+                     const uint32_t*, const uint32_t*, float4*);
 };
 
 struct PassTable {

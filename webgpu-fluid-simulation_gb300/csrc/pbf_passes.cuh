@@ -914,6 +914,81 @@ __global__ void __launch_bounds__(256, 4) k_xsph(SimParams p, const float4* __re
   }
 }
 
+// Fast mode splits XSPH's neighbour sum over the two post-solve passes: the
+// vorticity pass, which already gathers x_j, rho_j and v_j, also sums the
+// viscosity term u = sum W (v_j - v_i) / rho_j and the cohesion part of the
+// surface tension c = sum K_ij m C(x_ij); the XSPH pass then gathers only
+// (x_j, rho_j) and (n_j, |omega_j|) for eta and the curvature part.  The
+// result is the reference's formula with the tension sum split in two (a
+// different rounding order), so exact mode keeps the single-pass form.
+template <bool kLoop>
+__global__ void __launch_bounds__(256, 4) k_vorticity_split(SimParams p, const float4* __restrict__ pos,
+                                                            const float4* __restrict__ vel, uint32_t max_nbr,
+                                                            const uint32_t* __restrict__ nbr_cnt,
+                                                            const uint32_t* __restrict__ nbr_list,
+                                                            float4* __restrict__ omega, float4* __restrict__ normal,
+                                                            float4* __restrict__ visc, float4* __restrict__ coh_sum) {
+  PBF_SLOTS(t, p.n) {
+    const float4 pi = pos[t];
+    f3 xi = xyz(pi);
+    const float ri = pi.w;
+    f3 vi = xyz(vel[t]);
+    uint32_t b, e;
+    list_slice(max_nbr, nbr_cnt, t, b, e);
+    f3 om = mk(0.f, 0.f, 0.f), nm = mk(0.f, 0.f, 0.f), vu = mk(0.f, 0.f, 0.f), cs = mk(0.f, 0.f, 0.f);
+    for_each_neighbor(nbr_list, b, e, pos, [&](uint32_t j, float4 pj) {
+      Pair q = make_pair_of(xi - xyz(pj));
+      f3 vd = xyz(__ldg(vel + j)) - vi;
+      const float inv_rj = __frcp_rn(pj.w);
+      const float volume = p.m * inv_rj;
+      f3 gw = spiky_p(p, q);
+      om = om + volume * cross3(vd, gw);
+      nm = nm + volume * gw;
+      vu = vu + (poly6_p(p, q) * inv_rj) * vd;
+      const float kij = p.two_rho0 * __frcp_rn(ri + pj.w);
+      cs = cs + kij * (p.m * cohesion_p(p, q));
+    });
+    const float wl = len3(om);
+    omega[t] = f4(om, wl);
+    normal[t] = f4(p.h * nm, wl);
+    visc[t] = f4(vu, 0.0f);
+    coh_sum[t] = f4(cs, 0.0f);
+  }
+}
+
+template <bool kLoop>
+__global__ void __launch_bounds__(256) k_xsph_split(SimParams p, const float4* __restrict__ pos,
+                                                    const float4* __restrict__ omega,
+                                                    const float4* __restrict__ normal,
+                                                    const float4* __restrict__ visc,
+                                                    const float4* __restrict__ coh_sum, uint32_t max_nbr,
+                                                    const uint32_t* __restrict__ nbr_cnt,
+                                                    const uint32_t* __restrict__ nbr_list, float4* __restrict__ acc) {
+  PBF_SLOTS(t, p.n) {
+    const float4 pi = pos[t];
+    f3 xi = xyz(pi);
+    const float ri = pi.w;
+    f3 wi = xyz(omega[t]);
+    f3 ni = xyz(normal[t]);
+    uint32_t b, e;
+    list_slice(max_nbr, nbr_cnt, t, b, e);
+    f3 eta = mk(0.f, 0.f, 0.f), cv = mk(0.f, 0.f, 0.f);
+    for_each_neighbor(nbr_list, b, e, pos, [&](uint32_t j, float4 pj) {
+      Pair q = make_pair_of(xi - xyz(pj));
+      const float4 nj = __ldg(normal + j);  // (normal_j, |omega_j|)
+      eta = eta + (nj.w * __frcp_rn(pj.w)) * spiky_p(p, q);
+      const float kij = p.two_rho0 * __frcp_rn(ri + pj.w);
+      cv = cv + kij * (ni - xyz(nj));
+    });
+    const f3 ten = mk(0.f, 0.f, 0.f) - (xyz(coh_sum[t]) + cv);
+    float el = len3(eta);
+    f3 en = (el > 0.0f) ? divs(eta, el) : mk(0.f, 0.f, 0.f);
+    float sx = p.xsph * p.inv_dt * p.m;
+    f3 av = (sx * xyz(visc[t]) + p.vorticity * cross3(en, wi)) + p.tension * ten;
+    acc[t] = f4(av, 0.0f);
+  }
+}
+
 // Launch table for this precision variant: [batch][persistent] pass sets.
 template <bool B, bool P>
 void fill_set(PassSet* ps) {
@@ -930,6 +1005,13 @@ void fill_set(PassSet* ps) {
   ps->density_velocity = k_density_velocity<P>;
   ps->vorticity = k_vorticity<P>;
   ps->xsph = k_xsph<P>;
+  if constexpr (kFast) {
+    ps->vorticity_split = k_vorticity_split<P>;
+    ps->xsph_split = k_xsph_split<P>;
+  } else {
+    ps->vorticity_split = nullptr;
+    ps->xsph_split = nullptr;
+  }
 }
 
 void fill_pass_table(PassTable* tbl) {

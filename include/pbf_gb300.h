@@ -134,6 +134,7 @@ typedef struct pbf_metrics {
 #define PBF_DEVERR_NEIGHBOR_OVERFLOW 0x1u
 #define PBF_DEVERR_SCAN_TIMEOUT 0x2u
 #define PBF_DEVERR_CELL_OVERFLOW 0x4u
+#define PBF_DEVERR_MMA_TIMEOUT 0x8u  /* a tensor-core completion wait gave up (network pass) */
 
 typedef struct pbf_handle pbf_handle;
 
@@ -323,6 +324,13 @@ int pbf_mlp_init(pbf_mlp* m, uint64_t seed);
 int pbf_mlp_fit_normalization(pbf_mlp* m, const float* feat, const float* target, uint32_t rows);
 /* Host arrays: feat rows x 8 (raw features), out rows (lambda_hat). */
 int pbf_mlp_forward(const pbf_mlp* m, const float* feat, uint32_t rows, float* out);
+/* The same with a choice of inference kernel: PBF_MLP_KERNEL_MMA_SYNC
+ * (mma.sync.m16n8k16, one warp per 16-row tile) or PBF_MLP_KERNEL_TCGEN05
+ * (tcgen05.mma, 128-row tiles, accumulators in tensor memory).  Both use the
+ * same bf16 rounding points; PBF_ETIMEOUT if a tensor-core wait gave up. */
+#define PBF_MLP_KERNEL_MMA_SYNC 0u
+#define PBF_MLP_KERNEL_TCGEN05 1u
+int pbf_mlp_forward_ex(const pbf_mlp* model, const float* feat, uint32_t rows, float* out, uint32_t kernel);
 /* Gradient of mean((y - target/lam_scale)^2) w.r.t. params (PBF_MLP_PARAMS floats), one GPU pass. */
 int pbf_mlp_gradient(const pbf_mlp* m, const float* feat, const float* target, uint32_t rows, float* grad,
                      float* loss);
@@ -345,6 +353,9 @@ int pbf_trace_error(pbf_handle* h, float* max_mean, float* avg_mean);
  * model = NULL switches the learned start off.  A negative bound makes every
  * substep fall back (the result is then the plain solve's). */
 int pbf_set_learned(pbf_handle* h, const pbf_mlp* model, uint32_t iterations, float fallback_bound);
+/* Inference kernel of the learned start's network pass (PBF_MLP_KERNEL_*;
+ * default PBF_MLP_KERNEL_TCGEN05). */
+int pbf_set_mlp_kernel(pbf_handle* h, uint32_t kernel);
 
 /* ---- allocation-free exclusive scan.  No counterpart in the reference: an
  * addition for callers that cannot allocate device memory when they scan —

@@ -46,6 +46,43 @@ def test_mlp_forward_matches_fp64_reference():
     assert np.abs(got - exact).max() <= 3e-2 * scl        # against full FP64 (bf16 quantisation)
 
 
+@pytest.mark.parametrize("rows", [1, 127, 128, 129, 5000])
+def test_mlp_forward_tcgen05_matches_mma_sync_and_fp64(rows):
+    """The tensor-core (tcgen05.mma, TMEM) inference kernel against the
+    mma.sync kernel and the FP64 reference with the same bf16 rounding
+    points; ragged last tiles included."""
+    m, feat, _ = random_model(11, rows=max(rows, 2))
+    feat = feat[:rows]
+    tc = mlp_forward(m, feat, kernel=L.MLP_KERNEL_TCGEN05)
+    ms = mlp_forward(m, feat, kernel=L.MLP_KERNEL_MMA_SYNC)
+    mean, istd, scale = norm_of(m)
+    ref = mlp_ref.forward(mlp_params(m), mean, istd, scale, feat, emulate=True)["lam"]
+    scl = max(np.abs(ref).max(), 1e-30)
+    assert np.abs(tc - ref).max() <= 2e-3 * scl
+    assert np.abs(tc - ms).max() <= 2e-3 * scl
+
+
+def test_learned_step_tcgen05_network_matches_mma_sync():
+    """The learned substep with the tcgen05 network pass stays within bf16
+    rounding of the mma.sync pass after a few substeps."""
+    sc = scenes.reference_scene("boundary_small")
+    pts = scenes.jitter(sc.particles, 0.001, seed=14)
+    f = sc.field
+    m, _, _ = random_model(15)
+    out = []
+    for kernel in (L.MLP_KERNEL_MMA_SYNC, L.MLP_KERNEL_TCGEN05):
+        s = PBF(sc.config)
+        s.set_particles(pts)
+        s.set_boundary_field(f["res"], f["origin"], f["extent"], f["sdf"], f["vol"])
+        s.set_mlp_kernel(kernel)
+        s.set_learned(m, iterations=1, fallback_bound=1e9)
+        s.step(3)
+        out.append(s.positions()[:, :3])
+        s.close()
+    span = np.abs(out[0]).max()
+    assert np.abs(out[0] - out[1]).max() <= 1e-4 * span
+
+
 def test_mlp_gradient_matches_fp64_reference():
     m, feat, target = random_model(2, rows=777)
     g, loss = mlp_gradient(m, feat, target)

@@ -23,6 +23,7 @@ UNITS = [
     ("pbf_volume.cu", ["-fmad=false"]),
     ("pbf_scan_static.cu", []),
     ("pbf_learned.cu", []),
+    ("pbf_mlp_tc.cu", []),
 ]
 
 

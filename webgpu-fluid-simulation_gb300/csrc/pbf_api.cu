@@ -81,6 +81,7 @@ struct pbf_handle {
   uint32_t last_nbr_total = 0;
   // learned start and trace capture
   bool learned = false;
+  uint32_t mlp_kernel = PBF_MLP_KERNEL_TCGEN05;  // network pass of the learned start
   uint32_t learned_iters = 2;
   float fallback_bound = 0.01f;
   pbf_mlp model;
@@ -311,6 +312,7 @@ int check_device_errors(pbf_handle* h) {
                   need, old, h->nbr_slice);
     }
     if (e & PBF_DEVERR_SCAN_TIMEOUT) return fail(h, PBF_ETIMEOUT, "scan look-back wait gave up");
+    if (e & PBF_DEVERR_MMA_TIMEOUT) return fail(h, PBF_ETIMEOUT, "tensor-core completion wait gave up");
     return fail(h, PBF_ECUDA, "device error word 0x%x", e);
   }
   return PBF_OK;
@@ -479,8 +481,12 @@ int substep(pbf_handle* h, cudaEvent_t* ev) {
     CU(h, cudaGetLastError());
     {
       KScope ks(h, K_MLP);
-      CU(h, launch_mlp_infer(h->mlp_params.p, h->model, (const float*)h->feat.p, n, nullptr, h->lam_sum.p, st,
-                             h->xs[0].p, h->xl.p));
+      if (h->mlp_kernel == PBF_MLP_KERNEL_TCGEN05)
+        CU(h, launch_mlp_infer_tc(h->mlp_params.p, h->model, (const float*)h->feat.p, n, nullptr, h->lam_sum.p, st,
+                                  h->xs[0].p, h->xl.p, h->err_word.p));
+      else
+        CU(h, launch_mlp_infer(h->mlp_params.p, h->model, (const float*)h->feat.p, n, nullptr, h->lam_sum.p, st,
+                               h->xs[0].p, h->xl.p));
     }
     {
       KScope ks(h, K_DELTAP);
@@ -1446,6 +1452,15 @@ int pbf_trace_error(pbf_handle* h, float* max_mean, float* avg_mean) {
   CU(h, cudaStreamSynchronize(h->stream));
   *max_mean = r[0];
   *avg_mean = r[2] > 0 ? r[1] / r[2] : 0.0f;
+  return PBF_OK;
+}
+
+int pbf_set_mlp_kernel(pbf_handle* h, uint32_t kernel) {
+  if (!h) return PBF_EINVAL;
+  if (kernel != PBF_MLP_KERNEL_MMA_SYNC && kernel != PBF_MLP_KERNEL_TCGEN05)
+    return fail(h, PBF_EINVAL, "unknown network kernel %u", kernel);
+  if (kernel != h->mlp_kernel) invalidate_graph(h);
+  h->mlp_kernel = kernel;
   return PBF_OK;
 }
 

@@ -135,6 +135,12 @@ namespace pbf {
 cudaError_t launch_mlp_infer(const float* d_params, const pbf_mlp& model, const float* d_feat, uint32_t rows,
                              float* d_lambda, float* d_lam_sum, cudaStream_t st, const float4* d_xs = nullptr,
                              float4* d_xl = nullptr);
+// The same on the 5th-generation tensor cores (tcgen05.mma, TMEM
+// accumulators; pbf_mlp_tc.cu); d_err receives PBF_DEVERR_MMA_TIMEOUT when a
+// bounded completion wait gives up.
+cudaError_t launch_mlp_infer_tc(const float* d_params, const pbf_mlp& model, const float* d_feat, uint32_t rows,
+                                float* d_lambda, float* d_lam_sum, cudaStream_t st, const float4* d_xs,
+                                float4* d_xl, uint32_t* d_err);
 cudaError_t launch_mlp_grad(const float* d_params, const pbf_mlp& model, const float* d_feat, const float* d_target,
                             uint32_t rows, float* d_grad, float* d_loss, cudaStream_t st);
 cudaError_t launch_gather_f32(uint32_t n, const uint32_t* perm, const float* src, float* dst, cudaStream_t st);

@@ -508,21 +508,36 @@ int pbf_mlp_fit_normalization(pbf_mlp* m, const float* feat, const float* target
   return PBF_OK;
 }
 
-int pbf_mlp_forward(const pbf_mlp* m, const float* feat, uint32_t rows, float* out) {
+int pbf_mlp_forward_ex(const pbf_mlp* m, const float* feat, uint32_t rows, float* out, uint32_t kernel) {
   if (!m || (!feat && rows) || (!out && rows)) return PBF_EINVAL;
+  if (kernel != PBF_MLP_KERNEL_MMA_SYNC && kernel != PBF_MLP_KERNEL_TCGEN05) return PBF_EINVAL;
   if (rows == 0) return PBF_OK;
   float *dP = nullptr, *dF = nullptr, *dO = nullptr;
+  uint32_t* dE = nullptr;
+  uint32_t herr = 0;
   cudaError_t e = cudaMalloc(&dP, sizeof(m->params));
   if (e == cudaSuccess) e = cudaMalloc(&dF, (size_t)rows * 8 * sizeof(float));
   if (e == cudaSuccess) e = cudaMalloc(&dO, (size_t)rows * sizeof(float));
+  if (e == cudaSuccess) e = cudaMalloc(&dE, sizeof(uint32_t));
+  if (e == cudaSuccess) e = cudaMemset(dE, 0, sizeof(uint32_t));
   if (e == cudaSuccess) e = cudaMemcpy(dP, m->params, sizeof(m->params), cudaMemcpyHostToDevice);
   if (e == cudaSuccess) e = cudaMemcpy(dF, feat, (size_t)rows * 8 * sizeof(float), cudaMemcpyHostToDevice);
-  if (e == cudaSuccess) e = launch_mlp_infer(dP, *m, dF, rows, dO, nullptr, 0);
+  if (e == cudaSuccess) {
+    e = kernel == PBF_MLP_KERNEL_TCGEN05 ? launch_mlp_infer_tc(dP, *m, dF, rows, dO, nullptr, 0, nullptr, nullptr, dE)
+                                         : launch_mlp_infer(dP, *m, dF, rows, dO, nullptr, 0);
+  }
   if (e == cudaSuccess) e = cudaMemcpy(out, dO, (size_t)rows * sizeof(float), cudaMemcpyDeviceToHost);
+  if (e == cudaSuccess) e = cudaMemcpy(&herr, dE, sizeof(uint32_t), cudaMemcpyDeviceToHost);
   cudaFree(dP);
   cudaFree(dF);
   cudaFree(dO);
-  return e == cudaSuccess ? PBF_OK : PBF_ECUDA;
+  cudaFree(dE);
+  if (e != cudaSuccess) return PBF_ECUDA;
+  return herr ? PBF_ETIMEOUT : PBF_OK;
+}
+
+int pbf_mlp_forward(const pbf_mlp* m, const float* feat, uint32_t rows, float* out) {
+  return pbf_mlp_forward_ex(m, feat, rows, out, PBF_MLP_KERNEL_MMA_SYNC);
 }
 
 int pbf_mlp_gradient(const pbf_mlp* m, const float* feat, const float* target, uint32_t rows, float* grad,

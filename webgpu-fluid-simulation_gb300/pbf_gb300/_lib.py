@@ -58,6 +58,7 @@ class KernelTime(ctypes.Structure):
 
 
 MLP_PARAMS = 4801
+MLP_KERNEL_MMA_SYNC, MLP_KERNEL_TCGEN05 = 0, 1
 
 
 class MLP(ctypes.Structure):
@@ -160,6 +161,8 @@ SIGNATURES = {
     "pbf_copy_trace": (ctypes.c_int, [_P, _FP, _FP, u32]),
     "pbf_trace_error": (ctypes.c_int, [_P, _FP, _FP]),
     "pbf_set_learned": (ctypes.c_int, [_P, ctypes.POINTER(MLP), u32, ctypes.c_float]),
+    "pbf_mlp_forward_ex": (ctypes.c_int, [ctypes.POINTER(MLP), _FP, u32, _FP, u32]),
+    "pbf_set_mlp_kernel": (ctypes.c_int, [_P, u32]),
     "pbf_set_launch": (ctypes.c_int, [_P, ctypes.POINTER(Launch)]),
     "pbf_get_launch": (ctypes.c_int, [_P, ctypes.POINTER(Launch)]),
     "pbf_autotune": (ctypes.c_int, [_P, u32, u32, ctypes.POINTER(TuneTrial), u32, _UP, ctypes.POINTER(Launch)]),

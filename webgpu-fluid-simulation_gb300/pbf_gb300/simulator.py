@@ -204,6 +204,10 @@ class PBF:
         self._check(self._lib.pbf_trace_error(self._h, ctypes.byref(a), ctypes.byref(b)), "trace_error")
         return a.value, b.value
 
+    def set_mlp_kernel(self, kernel):
+        """Inference kernel of the learned start's network pass (L.MLP_KERNEL_*)."""
+        self._check(self._lib.pbf_set_mlp_kernel(self._h, int(kernel)), "set_mlp_kernel")
+
     def set_learned(self, model, iterations=2, fallback_bound=0.01):
         m = None if model is None else ctypes.byref(model)
         self._check(self._lib.pbf_set_learned(self._h, m, int(iterations), float(fallback_bound)), "set_learned")
@@ -443,10 +447,10 @@ def mlp_fit_normalization(m, feat, target):
         raise L.PBFError(rc, "mlp_fit_normalization")
 
 
-def mlp_forward(m, feat):
+def mlp_forward(m, feat, kernel=L.MLP_KERNEL_MMA_SYNC):
     f = np.ascontiguousarray(feat, np.float32)
     out = np.zeros(f.shape[0], np.float32)
-    rc = L.load().pbf_mlp_forward(ctypes.byref(m), _fp(f), f.shape[0], _fp(out))
+    rc = L.load().pbf_mlp_forward_ex(ctypes.byref(m), _fp(f), f.shape[0], _fp(out), int(kernel))
     if rc:
         raise L.PBFError(rc, "mlp_forward")
     return out

@@ -123,7 +123,7 @@ enum PassId {
   K_EXPORT, K_FEATURES, K_MLP, K_FALLBACK, K_NUM
 };
 const char* kPassNames[K_NUM] = {"predict",   "sort", "gather", "nbr_build", "boundary",     "lambda", "deltap_apply",
-                                 "density_velocity", "vorticity", "xsph", "export", "features", "mlp",
+                                 "density_velocity", "vorticity", "xsph", "export", "nbr_build_feat", "mlp",
                                  "fallback_guarded"};
 
 // Brackets one launch (or one group of launches) with events when timing is on.
@@ -356,27 +356,10 @@ int substep(pbf_handle* h, cudaEvent_t* ev) {
   if (need_feat) CU(h, launch_gather_f32(n, h->perm.p, h->lam_sum.p, h->lam_prev.p, st));
   h->cur = nx;
   const int cc = nx;
-  // NeighborCount + NeighborList in one pass (fixed per-particle slices: no scan)
   const FieldParams f = h->fp;
   const uint32_t ms = h->nbr_slice;
   const float sub_index = (float)(h->substep_counter % h->cfg.substeps);
-  {
-    KScope ks(h, K_NBR_BUILD);
-    if (h->build == PBF_BUILD_PAIR)
-      ps.nbr_build2<<<grid_of(h, (n + 1) / 2), h->blk, 0, st>>>(p, g, h->tab, h->xs[0].p, h->cell_start.p, ms,
-                                                                  h->nbr_list.p, h->nbr_count.p, h->nbr_max.p,
-                                                                  h->err_word.p);
-    else if (h->build == PBF_BUILD_WARP)
-      ps.nbr_build_warp<<<grid_of(h, n), h->blk, 0, st>>>(p, g, h->tab, h->xs[0].p, h->cell_start.p, ms,
-                                                           h->nbr_list.p, h->nbr_count.p, h->nbr_max.p,
-                                                           h->err_word.p);
-    else
-      ps.nbr_build<<<grid_of(h, n), h->blk, 0, st>>>(p, g, h->tab, h->xs[0].p, h->cell_start.p, ms, h->nbr_list.p,
-                                                      h->nbr_count.p, h->nbr_max.p, h->err_word.p);
-  }
-  CU(h, cudaGetLastError());
-  if (ev) CU(h, cudaEventRecord(ev[2], st));
-  // constraint loop.  Boundary sampling works on a band list (BandArgs): the
+  // Boundary sampling works on a band list (BandArgs): the
   // band pass builds it at x*_0, each delta-p pass marks the band of the next
   // iteration at the positions it writes, and the sampling kernel interpolates
   // the volume map for the listed slots only.
@@ -405,11 +388,43 @@ int substep(pbf_handle* h, cudaEvent_t* ev) {
                                                  h->band_count.p + (1 - band));
     return cudaGetLastError();
   };
+  // NeighborCount + NeighborList in one pass (fixed per-particle slices: no
+  // scan).  The learned start samples the boundary at x*_0 first and sums its
+  // features in the same traversal.
+  if (h->learned) {
+    CU(h, cudaMemcpyAsync(h->xs_save.p, h->xs[0].p, (size_t)n * sizeof(float4), cudaMemcpyDeviceToDevice, st));
+    if (f.loaded) CU(h, sample_boundary(0, h->bsdf.p));
+    SolverAux al{};
+    al.pos = h->pos[cc].p;
+    al.lam_prev = h->lam_prev.p;
+    al.bsdf = f.loaded ? h->bsdf.p : nullptr;
+    al.substep_index = sub_index;
+    al.feat = h->feat.p;
+    KScope ks(h, K_FEATURES);
+    ps.nbr_build_feat<<<grid_of(h, n), h->blk, 0, st>>>(p, g, h->xs[0].p, h->cell_start.p, ms, h->nbr_list.p,
+                                                         h->nbr_count.p, h->nbr_max.p, h->err_word.p, f.loaded,
+                                                         h->bdata.p, al);
+  } else {
+    KScope ks(h, K_NBR_BUILD);
+    if (h->build == PBF_BUILD_PAIR)
+      ps.nbr_build2<<<grid_of(h, (n + 1) / 2), h->blk, 0, st>>>(p, g, h->tab, h->xs[0].p, h->cell_start.p, ms,
+                                                                  h->nbr_list.p, h->nbr_count.p, h->nbr_max.p,
+                                                                  h->err_word.p);
+    else if (h->build == PBF_BUILD_WARP)
+      ps.nbr_build_warp<<<grid_of(h, n), h->blk, 0, st>>>(p, g, h->tab, h->xs[0].p, h->cell_start.p, ms,
+                                                           h->nbr_list.p, h->nbr_count.p, h->nbr_max.p,
+                                                           h->err_word.p);
+    else
+      ps.nbr_build<<<grid_of(h, n), h->blk, 0, st>>>(p, g, h->tab, h->xs[0].p, h->cell_start.p, ms, h->nbr_list.p,
+                                                      h->nbr_count.p, h->nbr_max.p, h->err_word.p);
+  }
+  CU(h, cudaGetLastError());
+  if (ev) CU(h, cudaEventRecord(ev[2], st));
+  // constraint loop
   // `iters` plain iterations starting from xs[a]; returns the buffer holding
   // the result.  The first iteration's lambda pass records the features
-  // (feat_first) and/or starts lam_sum; stats go with the last one.
-  // mark_last: the last delta-p also marks the band for a boundary sampling
-  // that follows.
+  // (feat_first) and/or starts lam_sum; stats go with the last one.  Each
+  // delta-p but the last marks the band of the next iteration.
   auto iterate = [&](int a, uint32_t iters, bool feat_first, bool lam_sum_on, bool first_starts_sum,
                      SolveStats* stats, int* rc) -> int {
     for (uint32_t it = 0; it < iters; ++it) {
@@ -462,23 +477,9 @@ int substep(pbf_handle* h, cudaEvent_t* ev) {
   };
   int a = 0, rc = PBF_OK;
   if (h->learned) {
-    // learned start: boundary and features at x*_0 -> network -> (x*_0,
-    // lambda_hat) -> one projection -> learned_iters plain iterations ->
-    // device-side fallback test
-    CU(h, cudaMemcpyAsync(h->xs_save.p, h->xs[0].p, (size_t)n * sizeof(float4), cudaMemcpyDeviceToDevice, st));
-    if (f.loaded) CU(h, sample_boundary(0, h->bsdf.p));
-    SolverAux al{};
-    al.pos = h->pos[cc].p;
-    al.lam_prev = h->lam_prev.p;
-    al.bsdf = f.loaded ? h->bsdf.p : nullptr;
-    al.substep_index = sub_index;
-    al.feat = h->feat.p;
-    {
-      KScope ks(h, K_FEATURES);
-      ps.features<<<grid_of(h, n), h->blk, 0, st>>>(p, f.loaded, h->bdata.p, h->xs[0].p, ms, h->nbr_count.p,
-                                                     h->nbr_list.p, al);
-    }
-    CU(h, cudaGetLastError());
+    // learned start: (boundary and features at x*_0 from the neighbour
+    // build) -> network -> (x*_0, lambda_hat) -> one projection ->
+    // learned_iters plain iterations -> device-side fallback test
     {
       KScope ks(h, K_MLP);
       if (h->mlp_kernel == PBF_MLP_KERNEL_TCGEN05)

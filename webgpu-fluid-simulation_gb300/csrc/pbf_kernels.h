@@ -28,8 +28,8 @@ struct PassSet {
                  SolverAux);
   void (*lambda_feat)(SimParams, int, const float4*, const float4*, uint32_t, const uint32_t*, const uint32_t*,
                       float4*, SolverAux);     // null in batch sets
-  void (*features)(SimParams, int, const float4*, const float4*, uint32_t, const uint32_t*, const uint32_t*,
-                   SolverAux);  // null in batch sets
+  void (*nbr_build_feat)(SimParams, GridParams, const float4*, const uint32_t*, uint32_t, uint32_t*, uint32_t*,
+                         uint32_t*, uint32_t*, int, const float4*, SolverAux);  // null in batch sets
   void (*deltap)(SimParams, SolverAux, int, const float4*, const float4*, uint32_t, const uint32_t*, const uint32_t*,
                  float4*, float4*);
   void (*density_velocity)(SimParams, SolverAux, const float4*, uint32_t, const uint32_t*, const uint32_t*, float4*,

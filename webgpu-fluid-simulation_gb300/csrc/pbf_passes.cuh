@@ -151,6 +151,15 @@ __global__ void __launch_bounds__(256) k_nbr_count(SimParams p, GridParams g, co
   if (t <= p.n) nbr_count[t] = cnt;
 }
 
+// Velocity divergence feature of the learned start, -div(v') dt, by the
+// continuity equation: (rho_prev - rho*) / rho* with rho* the fluid density
+// at x* (V sum W) and rho_prev the particle's density after the previous
+// substep (x.w / rho0); 0 before the first density pass.
+__device__ __forceinline__ float divergence_feature(const SimParams& p, float4 x_prev, float dens_fluid) {
+  const float prev = x_prev.w / p.rho0;
+  return (prev > 0.0f && dens_fluid > 0.0f) ? (prev - dens_fluid) / dens_fluid : 0.0f;
+}
+
 // NeighborCount + NeighborList of the step in one traversal.  The list is
 // interleaved by warp with a fixed slice of max_nbr entries per particle:
 // neighbour q of slot t is at (t / 32) * 32 * max_nbr + 32 q + t % 32, so the
@@ -196,6 +205,68 @@ __global__ void __launch_bounds__(256) k_nbr_build(SimParams p, GridParams g0, S
           atomicOr(err, 0x1u);
         }
       }
+    }
+  }
+}
+
+// The learned start's neighbour build: the same traversal, which also sums
+// the fluid density at x*_0 over the neighbours it finds (poly6 from the
+// squared distance the test already has: a few FMAs per hit) and writes the
+// start's feature rows (a.feat, the layout the lambda pass records for
+// training).  Needs the boundary sampling at x*_0 first (bdata, a.bsdf).
+template <bool kLoop>
+__global__ void __launch_bounds__(256) k_nbr_build_feat(SimParams p, GridParams g, const float4* __restrict__ xs,
+                                                        const uint32_t* __restrict__ cell_start, uint32_t max_nbr,
+                                                        uint32_t* __restrict__ nbr_list,
+                                                        uint32_t* __restrict__ nbr_count, uint32_t* max_seen,
+                                                        uint32_t* err, int have_field,
+                                                        const float4* __restrict__ bdata, SolverAux a) {
+  PBF_TILES(p.n) {
+    const uint32_t t = tile0 + threadIdx.x;
+    if (t < p.n) {
+      const f3 xi = xyz(xs[t]);
+      int cx = cell_axis(xi.x, g.origin[0], g.inv_cell[0], g.dim[0]);
+      int cy = cell_axis(xi.y, g.origin[1], g.inv_cell[1], g.dim[1]);
+      int cz = cell_axis(xi.z, g.origin[2], g.inv_cell[2], g.dim[2]);
+      uint32_t* out = nbr_list + (size_t)(t >> 5) * 32u * max_nbr + (t & 31u);
+      uint32_t q = 0;
+      float w = 0.0f;  // sum of (h^2 - r^2)^3 over the neighbours
+      for (int dx = -g.reach; dx <= g.reach; ++dx)
+        for (int dy = -g.reach; dy <= g.reach; ++dy) {
+          Run r = run_of(g, cell_start, cx, cy, cz, dx, dy);
+          for (uint32_t u = r.b; u < r.e; ++u) {
+            f3 d = xyz(__ldg(xs + u)) - xi;
+            const float r2 = dot3(d, d);
+            if (r2 <= p.h2) {
+              if (q < max_nbr) out[32u * q] = u;
+              ++q;
+              const float c = p.h2 - r2;
+              w = w + c * c * c;
+            }
+          }
+        }
+      nbr_count[t] = q;
+      const unsigned m = __activemask();
+      if (__any_sync(m, q > max_nbr)) {
+        unsigned wmax = __reduce_max_sync(m, q);
+        if ((threadIdx.x & 31u) == (unsigned)(__ffs(m) - 1)) {
+          atomicMax(max_seen, wmax);
+          atomicOr(err, 0x1u);
+        }
+      }
+      const float dens_fluid = p.V * (p.poly6 * w);
+      float dens = dens_fluid, vb = 0.0f;
+      if (have_field) {
+        float4 bd = bdata[t];
+        vb = bd.w;
+        if (bd.w != 0.0f) dens = dens + bd.w * poly6_p(p, make_pair_of(xi - xyz(bd)));
+      }
+      const float4 xo = a.pos[t];
+      const f3 vi = p.inv_dt * (xi - xyz(xo));
+      float sd = a.bsdf ? fminf(a.bsdf[t], 2.0f * p.h) : 2.0f * p.h;
+      a.feat[2 * t] = make_float4(dens - 1.0f, a.lam_prev ? a.lam_prev[t] : 0.0f, (float)min(q, max_nbr),
+                                  len3(vi) * p.dt / p.h);
+      a.feat[2 * t + 1] = make_float4(divergence_feature(p, xo, dens_fluid), sd / p.h, vb / p.V, a.substep_index);
     }
   }
 }
@@ -565,14 +636,6 @@ __global__ void __launch_bounds__(256, 2) k_boundary_band(SimParams p, FieldPara
 //            error, previous multiplier, neighbour count, |v'| dt/h, -div(v') dt
 //            by continuity, boundary SDF/h, boundary volume/V, substep index;
 //            v' = (x* - x)/dt) for trace capture.
-// Velocity divergence feature of the learned start, -div(v') dt, by the
-// continuity equation: (rho_prev - rho*) / rho* with rho* the fluid density
-// at x* (V sum W) and rho_prev the particle's density after the previous
-// substep (x.w / rho0); 0 before the first density pass.
-__device__ __forceinline__ float divergence_feature(const SimParams& p, float4 x_prev, float dens_fluid) {
-  const float prev = x_prev.w / p.rho0;
-  return (prev > 0.0f && dens_fluid > 0.0f) ? (prev - dens_fluid) / dens_fluid : 0.0f;
-}
 
 template <int kMode, bool kC>
 __device__ __forceinline__ void lambda_slot(const SimParams& p, int have_field, const float4* bdata, const float4* xs,
@@ -631,41 +694,6 @@ __global__ void __launch_bounds__(256) k_lambda(SimParams p, int have_field, con
   PBF_SLOTS(t, p.n) {
     if (!iter_active(scene_of<kBatch>(a.tab, t), a.iter)) continue;
     lambda_slot<kMode, false>(p, have_field, bdata, xs, max_nbr, nbr_cnt, nbr_list, xl, a, t);
-  }
-}
-
-// The learned start's features at x*_0, over the neighbour list: two float4
-// per particle (a.feat) with the layout and values the lambda pass records
-// for training (density error, previous multiplier, neighbour count,
-// |v'| dt/h, -div(v') dt by continuity, boundary SDF/h, boundary volume/V,
-// substep index; v' = (x* - x)/dt).  Needs the boundary pass at x*_0 (bdata,
-// a.bsdf).  The network then runs over the rows as a separate dense pass.
-template <bool kLoop>
-__global__ void __launch_bounds__(256) k_features(SimParams p, int have_field, const float4* __restrict__ bdata,
-                                                  const float4* __restrict__ xs, uint32_t max_nbr,
-                                                  const uint32_t* __restrict__ nbr_cnt,
-                                                  const uint32_t* __restrict__ nbr_list, SolverAux a) {
-  PBF_SLOTS(t, p.n) {
-    const f3 xi = xyz(xs[t]);
-    uint32_t b, e;
-    list_slice(max_nbr, nbr_cnt, t, b, e);
-    float dens = 0.0f;
-    for_each_neighbor(nbr_list, b, e, xs, [&](uint32_t, float4 xj) {
-      dens = dens + poly6_p(p, make_pair_of(xi - xyz(xj)));
-    });
-    dens = dens * p.V;
-    const float dens_fluid = dens;
-    float vb = 0.0f;
-    if (have_field) {
-      float4 bd = bdata[t];
-      vb = bd.w;
-      if (bd.w != 0.0f) dens = dens + bd.w * poly6_p(p, make_pair_of(xi - xyz(bd)));
-    }
-    const float4 xo = a.pos[t];
-    const f3 vi = p.inv_dt * (xi - xyz(xo));
-    float sd = a.bsdf ? fminf(a.bsdf[t], 2.0f * p.h) : 2.0f * p.h;
-    a.feat[2 * t] = make_float4(dens - 1.0f, a.lam_prev ? a.lam_prev[t] : 0.0f, (float)e, len3(vi) * p.dt / p.h);
-    a.feat[2 * t + 1] = make_float4(divergence_feature(p, xo, dens_fluid), sd / p.h, vb / p.V, a.substep_index);
   }
 }
 
@@ -1000,7 +1028,7 @@ void fill_set(PassSet* ps) {
   ps->boundary_band = k_boundary_band<B>;
   ps->lambda = k_lambda<0, B, P>;
   ps->lambda_feat = B ? nullptr : k_lambda<1, false, P>;
-  ps->features = B ? nullptr : k_features<P>;
+  ps->nbr_build_feat = B ? nullptr : k_nbr_build_feat<P>;
   ps->deltap = k_deltap<B, P>;
   ps->density_velocity = k_density_velocity<P>;
   ps->vorticity = k_vorticity<P>;

@@ -51,7 +51,9 @@ ALG_BYTES = {
     "sort": 32,               # key, rank, id -> perm_raw, id_raw; cell fix -> perm
     "gather": 76,             # perm -> pos, x*, id in the new order
     "nbr_build": 20,          # read x*, write count; + 4 B per list entry written (added per run)
-    "boundary": 32,           # read x*, write (x_b, V_b)
+    "nbr_build_feat": 92,     # the build + read x, bData, previous lambda, SDF; write 2 feature float4
+    "mlp": 68,                # read 8 features (32), x* (16); write (x*, lambda_hat) (16), lambda sum (4)
+    "boundary": 32,           # band pass / sampling: read x*, write (x_b, V_b)
     "lambda": 32,             # read x*, write (x*, lambda)
     "deltap_apply": 32,       # read (x*, lambda); write x*
     "density_velocity": 64,   # read x*, x; write v, (x, rho)
@@ -61,12 +63,13 @@ ALG_BYTES = {
 }
 
 
-# DRAM bytes (read + write) per launch from one `ncu --set full` capture of
-# the same workload (profiles/neighbor_passes_sphere_drop_1m_ncu.md); the
-# neighbour list (~185 MB) is the difference to the algorithmic bytes.
+# DRAM bytes (read + write) per launch from `ncu --set full` captures of the
+# same workload (profiles/neighbor_passes_sphere_drop_1m_ncu.md,
+# profiles/learned_passes_sphere_drop_1m_ncu.md); the neighbour list
+# (~170 MB) is most of the difference to the algorithmic bytes.
 NCU_TRAFFIC_BYTES = {
-    "lambda": 214.0e6, "deltap_apply": 214.1e6, "xsph": 250.5e6, "nbr_build": 286.8e6, "vorticity": 225.5e6,
-    "boundary": 48.9e6, "density_velocity": 222.5e6,
+    "lambda": 214.0e6, "deltap_apply": 224.6e6, "xsph": 266.6e6, "nbr_build": 286.8e6, "vorticity": 247.8e6,
+    "boundary": 30.3e6, "density_velocity": 222.5e6, "nbr_build_feat": 372.9e6, "mlp": 51.0e6,
 }
 
 
@@ -388,7 +391,7 @@ def gpu_arm(args, dist):
         dom = max(kt.items(), key=lambda kv: kv[1][1])
         name, (launches, tot_ms) = dom
         per_launch_s = tot_ms / launches / 1000.0
-        bytes_launch = (ALG_BYTES.get(name, 0) + (4.0 * nbr_pp if name == "nbr_build" else 0.0)) * n
+        bytes_launch = (ALG_BYTES.get(name, 0) + (4.0 * nbr_pp if name.startswith("nbr_build") else 0.0)) * n
         achieved = bytes_launch / per_launch_s / 1e9
         total_ms = sum(v[1] for v in kt.values())
         roof = {"bound": "hbm", "kernel": name, "achieved": achieved, "peak": peak, "unit": "GB/s",
@@ -400,12 +403,15 @@ def gpu_arm(args, dist):
                                "share": round(v[1] / total_ms, 4) if total_ms else None} for k, v in kt.items()}}
     if chosen["learned_iters"] is None:
         # per substep: predict, scan + scatter + cell fix + big cells, gather,
-        # neighbour build, 3 per iteration, density/velocity, vorticity, XSPH
-        per_sub = 10 + 3 * iters
+        # neighbour build, band pass, 3 per iteration (band sampling, lambda,
+        # delta-p), density/velocity, vorticity, XSPH
+        per_sub = 11 + 3 * iters
     else:
-        # + lam_prev gather, boundary at x*_0, features, network, first
-        # projection, fallback decision, fallback kernel
-        per_sub = 10 + 7 + 3 * chosen["learned_iters"]
+        # predict, 4 sort, gather, lam_prev gather, band pass + sampling at
+        # x*_0, build with features, network, first projection, 3 per
+        # iteration, density/velocity, fallback decision, fallback kernel,
+        # vorticity, XSPH
+        per_sub = 17 + 3 * chosen["learned_iters"]
     launches_per_frame = sub * per_sub + 1  # + export
     m = plain["metrics"]
     line = {
@@ -682,7 +688,7 @@ def batch_arm(args, dist):
         "tuner_trials": trials,
         "e2e": {"value": total * sub * args.steps / e2e_s, "unit": UNIT,
                 "h2d_bytes_per_step": ctypes.sizeof(L.Options), "d2h_bytes_per_step": int(host.nbytes)},
-        "gpu_launches": (sub * (10 + 3 * iters_max) + 1) * args.steps,
+        "gpu_launches": (sub * (11 + 3 * iters_max) + 1) * args.steps,
         "roofline": roof, "clocks": clk,
         "scene_metrics": {"scenes": len(merged), "nonfinite": sum(m["nonfinite"] for m in merged.values()),
                           "penetrations": sum(m["penetrations"] for m in merged.values()),

@@ -157,6 +157,47 @@ int pbf_get_options(const pbf_handle* h, pbf_options* opt);
  * (PBFConfig.setParticlePosition, PBFConfig.ts:48-62). */
 int pbf_voxelize_cube(pbf_handle* h, const float mn[3], const float mx[3], uint32_t* added);
 int pbf_voxelize_sphere(pbf_handle* h, const float center[3], float radius, uint32_t* added);
+/* SPH.voxelizeMesh (SPH.ts:151-187) on the GPU: lattice points at spacing
+ * 2r over the mesh's world bounding box (the local vertex box's corners
+ * through the world matrix, Box3.expandByObject) that a +z ray in the mesh's
+ * local space shows to be inside (its nearest hit, over both face
+ * orientations, is a face pointing along the ray).  vertices: float3 in local
+ * space; indices: 3 per triangle; world: 4x4 column-major doubles, affine
+ * (three.js Matrix4.elements of mesh.matrixWorld).  Appends to the host
+ * particle array like pbf_voxelize_cube. */
+int pbf_voxelize_mesh(pbf_handle* h, const float* vertices, uint32_t vertex_count, const uint32_t* indices,
+                      uint32_t triangle_count, const double world[16], uint32_t* added);
+/* The same without a handle: up to `capacity` points (x, y, z, 0) into
+ * out_xyzw, their number in *count (PBF_ECAPACITY if it exceeds capacity;
+ * out_xyzw may be NULL with capacity 0 to count only). */
+int pbf_voxelize_mesh_points(const float* vertices, uint32_t vertex_count, const uint32_t* indices,
+                             uint32_t triangle_count, const double world[16], double particle_radius, float* out_xyzw,
+                             uint32_t capacity, uint32_t* count);
+/* Scene seeding on the device.  No single counterpart in the reference: the
+ * result equals pbf_reset's particle array cleared, the items voxelised in
+ * order (PBF_SEED_CUBE = voxelizeCube(a, b); PBF_SEED_SPHERE =
+ * voxelizeSphere(a, b[0]); PBF_SEED_MESH = voxelizeMesh of the mesh fields),
+ * pbf_jitter_particles(jitter_amplitude, jitter_seed) when the amplitude is
+ * positive, then pbf_set_particle_position — bit for bit — but the lattices,
+ * the compaction and the jitter run on the GPU and the points are written
+ * straight into the particle buffers (no host array, no upload; the host
+ * particle array is left empty).  *total gets the number of particles the
+ * items make; above max_particles nothing is seeded and PBF_ECAPACITY is
+ * returned.  Lattices are limited to 4096 points per axis and 2^30 points
+ * per item. */
+enum { PBF_SEED_CUBE = 0, PBF_SEED_SPHERE = 1, PBF_SEED_MESH = 2 };
+typedef struct pbf_seed_item {
+  uint32_t kind;            /* PBF_SEED_* */
+  float a[3];               /* cube: minimum corner; sphere: centre */
+  float b[3];               /* cube: maximum corner; sphere: b[0] = radius */
+  const float* vertices;    /* mesh: float3 per vertex, local space */
+  uint32_t vertex_count;
+  const uint32_t* indices;  /* mesh: 3 per triangle */
+  uint32_t triangle_count;
+  double world[16];         /* mesh: column-major affine world matrix */
+} pbf_seed_item;
+int pbf_seed_device(pbf_handle* h, const pbf_seed_item* items, uint32_t count, float jitter_amplitude,
+                    uint64_t jitter_seed, uint32_t* total);
 /* Seeded uniform jitter in [-amplitude, amplitude] on the host array (splitmix64). */
 int pbf_jitter_particles(pbf_handle* h, float amplitude, uint64_t seed);
 int pbf_host_particle_count(const pbf_handle* h, uint32_t* count);

@@ -56,6 +56,8 @@ def load():
                                                       ctypes.c_float, ctypes.c_uint32, ctypes.c_uint32, _FP, _FP]),
         "oracle_volume_from_sdf": (ctypes.c_int, [_UP, _FP, _FP, ctypes.c_float, ctypes.c_uint32, ctypes.c_uint32,
                                                   _FP, _FP]),
+        "oracle_voxelize_mesh": (ctypes.c_int, [_FP, ctypes.c_uint32, _UP, ctypes.c_uint32, _DP, ctypes.c_double,
+                                                _FP, ctypes.c_uint32, _UP]),
         "oracle_threads": (ctypes.c_int, []),
         "oracle_set_threads": (None, [ctypes.c_int]),
     }
@@ -226,4 +228,26 @@ def volume_from_sdf(res, origin, extent, h, sdf, quadrature=16, flags=1):
     s = np.ascontiguousarray(sdf, dtype=np.float32)
     out = np.zeros_like(s)
     load().oracle_volume_from_sdf(_up(r), _fp(o), _fp(e), float(h), int(quadrature), int(flags), _fp(s), _fp(out))
+    return out
+
+
+def voxelize_mesh(vertices, triangles, particle_radius, world=None):
+    """SPH.voxelizeMesh restated (brute force, double precision): the kept
+    lattice points as (n, 4) float32 in lattice order.  world: 4x4 row-major
+    float64 (identity by default)."""
+    lib = load()
+    v = np.ascontiguousarray(vertices, np.float32)
+    t = np.ascontiguousarray(triangles, np.uint32)
+    w = np.eye(4) if world is None else np.asarray(world, np.float64)
+    wc = np.ascontiguousarray(w.T, np.float64)
+    c = ctypes.c_uint32()
+    rc = lib.oracle_voxelize_mesh(_fp(v), v.shape[0], _up(t), t.shape[0], _dp(wc), float(particle_radius), None, 0,
+                                  ctypes.byref(c))
+    if rc not in (0, 2):
+        raise RuntimeError("oracle_voxelize_mesh failed (%d)" % rc)
+    out = np.zeros((c.value, 4), np.float32)
+    rc = lib.oracle_voxelize_mesh(_fp(v), v.shape[0], _up(t), t.shape[0], _dp(wc), float(particle_radius), _fp(out),
+                                  c.value, ctypes.byref(c))
+    if rc:
+        raise RuntimeError("oracle_voxelize_mesh failed (%d)" % rc)
     return out

@@ -1066,6 +1066,143 @@ int oracle_volume_from_sdf(const uint32_t* res, const float* origin, const float
   return gen_impl(nullptr, 0, res, origin, extent, support_radius, quadrature, flags | 2u, sdf, nullptr, vol_out);
 }
 
+// SPH.voxelizeMesh (src/simulator/SPH.ts:151-187): lattice at spacing 2r over
+// the mesh's world bounding box from its minimum corner (floor(extent / 2r)
+// points per axis, x slowest), a +z ray from each point in the mesh's local
+// space (origin through the inverse world matrix), the nearest hit over all
+// triangles of either orientation, and the point kept when the hit face's
+// normal points along the ray.  Brute force over every triangle in double
+// precision (the reference computes in JavaScript doubles); the inverse is
+// the cofactor expansion.  Returns the kept points (x, y, z, 0) in lattice
+// order.
+static bool vox_invert4(const double* m, double* inv) {
+  double r[16];
+  r[0] = m[5] * m[10] * m[15] - m[5] * m[11] * m[14] - m[9] * m[6] * m[15] + m[9] * m[7] * m[14] + m[13] * m[6] * m[11] -
+         m[13] * m[7] * m[10];
+  r[4] = -m[4] * m[10] * m[15] + m[4] * m[11] * m[14] + m[8] * m[6] * m[15] - m[8] * m[7] * m[14] -
+         m[12] * m[6] * m[11] + m[12] * m[7] * m[10];
+  r[8] = m[4] * m[9] * m[15] - m[4] * m[11] * m[13] - m[8] * m[5] * m[15] + m[8] * m[7] * m[13] + m[12] * m[5] * m[11] -
+         m[12] * m[7] * m[9];
+  r[12] = -m[4] * m[9] * m[14] + m[4] * m[10] * m[13] + m[8] * m[5] * m[14] - m[8] * m[6] * m[13] -
+          m[12] * m[5] * m[10] + m[12] * m[6] * m[9];
+  r[1] = -m[1] * m[10] * m[15] + m[1] * m[11] * m[14] + m[9] * m[2] * m[15] - m[9] * m[3] * m[14] -
+         m[13] * m[2] * m[11] + m[13] * m[3] * m[10];
+  r[5] = m[0] * m[10] * m[15] - m[0] * m[11] * m[14] - m[8] * m[2] * m[15] + m[8] * m[3] * m[14] + m[12] * m[2] * m[11] -
+         m[12] * m[3] * m[10];
+  r[9] = -m[0] * m[9] * m[15] + m[0] * m[11] * m[13] + m[8] * m[1] * m[15] - m[8] * m[3] * m[13] -
+         m[12] * m[1] * m[11] + m[12] * m[3] * m[9];
+  r[13] = m[0] * m[9] * m[14] - m[0] * m[10] * m[13] - m[8] * m[1] * m[14] + m[8] * m[2] * m[13] +
+          m[12] * m[1] * m[10] - m[12] * m[2] * m[9];
+  r[2] = m[1] * m[6] * m[15] - m[1] * m[7] * m[14] - m[5] * m[2] * m[15] + m[5] * m[3] * m[14] + m[13] * m[2] * m[7] -
+         m[13] * m[3] * m[6];
+  r[6] = -m[0] * m[6] * m[15] + m[0] * m[7] * m[14] + m[4] * m[2] * m[15] - m[4] * m[3] * m[14] - m[12] * m[2] * m[7] +
+         m[12] * m[3] * m[6];
+  r[10] = m[0] * m[5] * m[15] - m[0] * m[7] * m[13] - m[4] * m[1] * m[15] + m[4] * m[3] * m[13] + m[12] * m[1] * m[7] -
+          m[12] * m[3] * m[5];
+  r[14] = -m[0] * m[5] * m[14] + m[0] * m[6] * m[13] + m[4] * m[1] * m[14] - m[4] * m[2] * m[13] -
+          m[12] * m[1] * m[6] + m[12] * m[2] * m[5];
+  r[3] = -m[1] * m[6] * m[11] + m[1] * m[7] * m[10] + m[5] * m[2] * m[11] - m[5] * m[3] * m[10] - m[9] * m[2] * m[7] +
+         m[9] * m[3] * m[6];
+  r[7] = m[0] * m[6] * m[11] - m[0] * m[7] * m[10] - m[4] * m[2] * m[11] + m[4] * m[3] * m[10] + m[8] * m[2] * m[7] -
+         m[8] * m[3] * m[6];
+  r[11] = -m[0] * m[5] * m[11] + m[0] * m[7] * m[9] + m[4] * m[1] * m[11] - m[4] * m[3] * m[9] - m[8] * m[1] * m[7] +
+          m[8] * m[3] * m[5];
+  r[15] = m[0] * m[5] * m[10] - m[0] * m[6] * m[9] - m[4] * m[1] * m[10] + m[4] * m[2] * m[9] + m[8] * m[1] * m[6] -
+          m[8] * m[2] * m[5];
+  const double det = m[0] * r[0] + m[1] * r[4] + m[2] * r[8] + m[3] * r[12];
+  if (!(std::fabs(det) > 0.0) || !std::isfinite(det)) return false;
+  for (int q = 0; q < 16; ++q) inv[q] = r[q] / det;
+  return true;
+}
+
+int oracle_voxelize_mesh(const float* vertices, uint32_t nv, const uint32_t* idx, uint32_t nt, const double* world,
+                         double particle_radius, float* out, uint32_t capacity, uint32_t* count) {
+  *count = 0;
+  double W[16], M[16];
+  for (int q = 0; q < 16; ++q) W[q] = world[q];
+  if (!vox_invert4(W, M)) return 1;
+  // Box3.expandByObject: the local vertex box's eight corners through the
+  // world matrix (Box3.applyMatrix4; w = 1 for an affine matrix)
+  double llo[3] = {1e300, 1e300, 1e300}, lhi[3] = {-1e300, -1e300, -1e300};
+  for (uint32_t q = 0; q < nv; ++q)
+    for (int a = 0; a < 3; ++a) {
+      llo[a] = std::min(llo[a], (double)vertices[3 * (size_t)q + a]);
+      lhi[a] = std::max(lhi[a], (double)vertices[3 * (size_t)q + a]);
+    }
+  double lo[3] = {1e300, 1e300, 1e300}, hi[3] = {-1e300, -1e300, -1e300};
+  for (int corner = 0; corner < 8; ++corner) {
+    const double x = (corner & 4) ? lhi[0] : llo[0], y = (corner & 2) ? lhi[1] : llo[1],
+                 z = (corner & 1) ? lhi[2] : llo[2];
+    const double w[3] = {W[0] * x + W[4] * y + W[8] * z + W[12], W[1] * x + W[5] * y + W[9] * z + W[13],
+                         W[2] * x + W[6] * y + W[10] * z + W[14]};
+    for (int a = 0; a < 3; ++a) {
+      lo[a] = std::min(lo[a], w[a]);
+      hi[a] = std::max(hi[a], w[a]);
+    }
+  }
+  const double diam = 2.0 * particle_radius;
+  uint64_t dim[3];
+  for (int a = 0; a < 3; ++a) dim[a] = (uint64_t)std::floor((hi[a] - lo[a]) / diam);
+  std::vector<uint8_t> in(dim[0] * dim[1] * dim[2], 0);
+#pragma omp parallel for schedule(dynamic, 64)
+  for (int64_t id = 0; id < (int64_t)in.size(); ++id) {
+    const uint64_t k = (uint64_t)id % dim[2], j = ((uint64_t)id / dim[2]) % dim[1], i = (uint64_t)id / (dim[2] * dim[1]);
+    const double px = (double)i * diam + lo[0], py = (double)j * diam + lo[1], pz = (double)k * diam + lo[2];
+    const double o[3] = {M[0] * px + M[4] * py + M[8] * pz + M[12], M[1] * px + M[5] * py + M[9] * pz + M[13],
+                         M[2] * px + M[6] * py + M[10] * pz + M[14]};
+    double best = 1e300;
+    bool hit = false, along = false;
+    for (uint32_t f = 0; f < nt; ++f) {
+      const float* A = vertices + 3 * (size_t)idx[3 * (size_t)f];
+      const float* B = vertices + 3 * (size_t)idx[3 * (size_t)f + 1];
+      const float* C = vertices + 3 * (size_t)idx[3 * (size_t)f + 2];
+      const double e1[3] = {(double)B[0] - A[0], (double)B[1] - A[1], (double)B[2] - A[2]};
+      const double e2[3] = {(double)C[0] - A[0], (double)C[1] - A[1], (double)C[2] - A[2]};
+      const double nx = e1[1] * e2[2] - e1[2] * e2[1], ny = e1[2] * e2[0] - e1[0] * e2[2],
+                   nz = e1[0] * e2[1] - e1[1] * e2[0];
+      // ray direction (0, 0, 1): direction . normal = nz
+      double ddn = nz, sg;
+      if (ddn > 0.0) {
+        sg = 1.0;
+      } else if (ddn < 0.0) {
+        sg = -1.0;
+        ddn = -ddn;
+      } else {
+        continue;
+      }
+      const double q[3] = {o[0] - A[0], o[1] - A[1], o[2] - A[2]};
+      const double u = sg * (q[0] * e2[1] - q[1] * e2[0]);   // (q x e2).z
+      if (u < 0.0) continue;
+      const double v = sg * (e1[0] * q[1] - e1[1] * q[0]);   // (e1 x q).z
+      if (v < 0.0) continue;
+      if (u + v > ddn) continue;
+      const double qn = -sg * (q[0] * nx + q[1] * ny + q[2] * nz);
+      if (qn < 0.0) continue;
+      const double t = qn / ddn;
+      if (!hit || t < best) {
+        best = t;
+        hit = true;
+        along = sg > 0.0;
+      }
+    }
+    in[id] = (hit && along) ? 1 : 0;
+  }
+  uint32_t c = 0;
+  for (uint64_t id = 0; id < in.size(); ++id) {
+    if (!in[id]) continue;
+    if (c < capacity && out) {
+      const uint64_t k = id % dim[2], j = (id / dim[2]) % dim[1], i = id / (dim[2] * dim[1]);
+      out[4 * (size_t)c] = (float)((double)i * diam + lo[0]);
+      out[4 * (size_t)c + 1] = (float)((double)j * diam + lo[1]);
+      out[4 * (size_t)c + 2] = (float)((double)k * diam + lo[2]);
+      out[4 * (size_t)c + 3] = 0.0f;
+    }
+    ++c;
+  }
+  *count = c;
+  return c > capacity ? 2 : 0;
+}
+
 int oracle_threads(void) {
 #ifdef _OPENMP
   return omp_get_max_threads();

@@ -1,5 +1,6 @@
 """Regenerates the committed fixtures of this folder.
 
+0. mesh_torus.npz: the reference's triangle mesh public/model/torus.obj.
 1. cdm_*.npz: the reference's boundary assets public/model/torus.cdm and
    public/model/domain_boundary.cdm (20^3 cubic volume maps over the unit
    cube), parsed exactly as BoundaryModel.setData does
@@ -37,6 +38,17 @@ def make_cdm():
         print(name, res, sdf.size)
 
 
+def make_meshes():
+    """mesh_torus.npz: the reference's public/model/torus.obj (400 vertices,
+    800 triangles) as float32 vertices and uint32 triangles."""
+    sys.path.insert(0, os.path.join(REPO, "webgpu-fluid-simulation_gb300"))
+    from pbf_gb300 import scenes
+    with open(os.path.join(REFERENCE_ROOT, "public", "model", "torus.obj")) as f:
+        v, t = scenes.parse_obj(f.read())
+    np.savez_compressed(os.path.join(HERE, "mesh_torus.npz"), vertices=v, triangles=t)
+    print("torus mesh", v.shape, t.shape)
+
+
 def make_oracle():
     sys.path.insert(0, REPO)
     sys.path.insert(0, os.path.join(REPO, "webgpu-fluid-simulation_gb300"))
@@ -61,5 +73,6 @@ def make_oracle():
 
 if __name__ == "__main__":
     if "--oracle-only" not in sys.argv:
+        make_meshes()
         make_cdm()
     make_oracle()

@@ -38,6 +38,7 @@ def test_struct_sizes_match_header_layout():
     assert ctypes.sizeof(L.Options) == 20
     assert ctypes.sizeof(L.Config) % 8 == 0
     assert ctypes.sizeof(L.Shape) == 28
+    assert ctypes.sizeof(L.SeedItem) == 192   # 28 B of kinds/corners, 3 pointers + counts, double[16]
     assert ctypes.sizeof(L.Grid) == 36
 
 

@@ -24,6 +24,7 @@ UNITS = [
     ("pbf_scan_static.cu", []),
     ("pbf_learned.cu", []),
     ("pbf_mlp_tc.cu", []),
+    ("pbf_seed.cu", ["-fmad=false", "-Xcompiler", "-ffp-contract=off"]),
 ]
 
 

@@ -611,9 +611,9 @@ int frame(pbf_handle* h) {
   return export_positions(h);
 }
 
-int upload_particles(pbf_handle* h, const float* xyzw, uint32_t n) {
-  if (n > h->cfg.max_particles)
-    return fail(h, PBF_ECAPACITY, "To Many Particles! (%u > max_particles %u)", n, h->cfg.max_particles);
+// The state after an upload of n particles whose positions (w = 0) and ids
+// (0 .. n-1) are already in pos[0] / ids[0]: zero motion, exported positions.
+int finish_upload(pbf_handle* h, uint32_t n) {
   invalidate_graph(h);
   h->n = n;
   h->cur = 0;
@@ -621,19 +621,8 @@ int upload_particles(pbf_handle* h, const float* xyzw, uint32_t n) {
   uint32_t bits = 1;
   while (bits < 32 && (1ull << bits) < (uint64_t)n) ++bits;
   h->id_bits = bits;
-  std::vector<float> tmp((size_t)n * 4);
-  std::vector<uint32_t> iota(n);
-  for (uint32_t i = 0; i < n; ++i) {
-    tmp[4 * (size_t)i] = xyzw[4 * (size_t)i];
-    tmp[4 * (size_t)i + 1] = xyzw[4 * (size_t)i + 1];
-    tmp[4 * (size_t)i + 2] = xyzw[4 * (size_t)i + 2];
-    tmp[4 * (size_t)i + 3] = 0.0f;
-    iota[i] = i;
-  }
   cudaStream_t st = h->stream;
   if (n) {
-    CU(h, cudaMemcpyAsync(h->pos[0].p, tmp.data(), (size_t)n * sizeof(float4), cudaMemcpyHostToDevice, st));
-    CU(h, cudaMemcpyAsync(h->ids[0].p, iota.data(), (size_t)n * sizeof(uint32_t), cudaMemcpyHostToDevice, st));
     CU(h, cudaMemsetAsync(h->vel.p, 0, (size_t)n * sizeof(float4), st));
     CU(h, cudaMemsetAsync(h->acc.p, 0, (size_t)n * sizeof(float4), st));
     CU(h, cudaMemsetAsync(h->xl.p, 0, (size_t)n * sizeof(float4), st));
@@ -643,6 +632,27 @@ int upload_particles(pbf_handle* h, const float* xyzw, uint32_t n) {
   if (rc) return rc;
   CU(h, cudaStreamSynchronize(st));
   return PBF_OK;
+}
+
+int upload_particles(pbf_handle* h, const float* xyzw, uint32_t n) {
+  if (n > h->cfg.max_particles)
+    return fail(h, PBF_ECAPACITY, "To Many Particles! (%u > max_particles %u)", n, h->cfg.max_particles);
+  std::vector<float> tmp((size_t)n * 4);
+  std::vector<uint32_t> iota(n);
+  for (uint32_t i = 0; i < n; ++i) {
+    tmp[4 * (size_t)i] = xyzw[4 * (size_t)i];
+    tmp[4 * (size_t)i + 1] = xyzw[4 * (size_t)i + 1];
+    tmp[4 * (size_t)i + 2] = xyzw[4 * (size_t)i + 2];
+    tmp[4 * (size_t)i + 3] = 0.0f;
+    iota[i] = i;
+  }
+  if (n) {
+    invalidate_graph(h);
+    CU(h, cudaMemcpyAsync(h->pos[0].p, tmp.data(), (size_t)n * sizeof(float4), cudaMemcpyHostToDevice, h->stream));
+    CU(h, cudaMemcpyAsync(h->ids[0].p, iota.data(), (size_t)n * sizeof(uint32_t), cudaMemcpyHostToDevice,
+                          h->stream));
+  }
+  return finish_upload(h, n);
 }
 
 void release_all(pbf_handle* h) {
@@ -1080,6 +1090,43 @@ int pbf_voxelize_sphere(pbf_handle* h, const float c[3], float radius, uint32_t*
       }
   if (added) *added = count;
   return PBF_OK;
+}
+
+int pbf_voxelize_mesh(pbf_handle* h, const float* vertices, uint32_t vertex_count, const uint32_t* indices,
+                      uint32_t triangle_count, const double world[16], uint32_t* added) {
+  if (!h) return PBF_EINVAL;
+  std::vector<float> pts;
+  uint32_t count = 0;
+  int rc = voxelize_mesh_host(vertices, vertex_count, indices, triangle_count, world,
+                              (double)h->cfg.particle_radius, true, &pts, &count);
+  if (rc) return fail(h, rc, "voxelizeMesh failed");
+  h->host_particles.insert(h->host_particles.end(), pts.begin(), pts.end());
+  if (added) *added = count;
+  return PBF_OK;
+}
+
+int pbf_seed_device(pbf_handle* h, const pbf_seed_item* items, uint32_t count, float jitter_amplitude,
+                    uint64_t jitter_seed, uint32_t* total) {
+  if (!h || (!items && count)) return PBF_EINVAL;
+  if (h->batch) return not_for_batch(h, "pbf_seed_device");
+  uint32_t made = 0;
+  invalidate_graph(h);
+  // the items are seeded into pos[1] / ids[1] first, so a failure leaves the
+  // current particles as they were
+  int rc = seed_device(items, count, (double)h->cfg.particle_radius, jitter_amplitude, jitter_seed, h->pos[1].p,
+                       h->ids[1].p, h->cfg.max_particles, &made, h->stream);
+  if (total) *total = made;
+  if (rc == PBF_ECAPACITY)
+    return fail(h, PBF_ECAPACITY, "To Many Particles! (%u > max_particles %u)", made, h->cfg.max_particles);
+  if (rc) return fail(h, rc, "pbf_seed_device failed");
+  if (made) {
+    CU(h, cudaMemcpyAsync(h->pos[0].p, h->pos[1].p, (size_t)made * sizeof(float4), cudaMemcpyDeviceToDevice,
+                          h->stream));
+    CU(h, cudaMemcpyAsync(h->ids[0].p, h->ids[1].p, (size_t)made * sizeof(uint32_t), cudaMemcpyDeviceToDevice,
+                          h->stream));
+  }
+  h->host_particles.clear();
+  return finish_upload(h, made);
 }
 
 int pbf_jitter_particles(pbf_handle* h, float amplitude, uint64_t seed) {

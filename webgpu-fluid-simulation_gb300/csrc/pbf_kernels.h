@@ -4,6 +4,8 @@
 #pragma once
 #include <cstddef>
 #include <cstdint>
+#include <vector>
+
 #include <cuda_runtime.h>
 
 #include "pbf_params.h"
@@ -151,4 +153,18 @@ cudaError_t launch_stats_record(SolveStats* stats, float* rec, cudaStream_t st);
 cudaError_t launch_trace_append(uint32_t n, const uint32_t* ids, const float4* feat, const float* lam_sum,
                                 uint32_t stride, uint32_t salt, float* tf, float* tt, uint32_t* count, uint32_t cap,
                                 cudaStream_t st);
+// ---- scene seeding (pbf_seed.cu) -------------------------------------------------
+// Writes the points of `items` (cube / sphere / mesh lattices, in order) to
+// out[0 .. *total) as (x, y, z, 0), applies the host jitter's splitmix64
+// draws when jitter > 0 and sets ids[i] = i.  *total gets the number of
+// points the items make even on PBF_ECAPACITY (nothing beyond capacity is
+// written).  Synchronises `st` before returning.
+int seed_device(const pbf_seed_item* items, uint32_t count, double radius, float jitter, uint64_t seed, float4* out,
+                uint32_t* ids, uint32_t capacity, uint32_t* total, cudaStream_t st);
+// SPH.voxelizeMesh on the device with the kept points copied to *pts (when
+// emit) and their number in *kept.
+int voxelize_mesh_host(const float* vertices, uint32_t vertex_count, const uint32_t* indices, uint32_t triangle_count,
+                       const double* world, double particle_radius, bool emit, std::vector<float>* pts,
+                       uint32_t* kept);
+
 }  // namespace pbf

@@ -5,7 +5,7 @@ reference presets and the benchmark workloads.  All compute runs in
 libpbf_gb300.so (CUDA, sm_103a).
 """
 from . import _lib
-from .simulator import PBF, PBFBatch, NeighborSearch, exclusive_scan
+from .simulator import PBF, PBFBatch, NeighborSearch, exclusive_scan, voxelize_mesh_points
 from .simulator import mlp_init, mlp_params, mlp_fit_normalization, mlp_forward, mlp_gradient, mlp_train
 from . import scenes
 

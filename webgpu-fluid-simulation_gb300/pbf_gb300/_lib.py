@@ -99,9 +99,19 @@ class SceneInfo(ctypes.Structure):
     _fields_ = [("first_id", u32), ("particles", u32), ("iterations", u32), ("grid_dim", u32 * 3), ("cells", u32)]
 
 
+SEED_CUBE, SEED_SPHERE, SEED_MESH = 0, 1, 2
+
+
+class SeedItem(ctypes.Structure):
+    _fields_ = [("kind", u32), ("a", f32 * 3), ("b", f32 * 3), ("vertices", ctypes.POINTER(f32)),
+                ("vertex_count", u32), ("indices", ctypes.POINTER(u32)), ("triangle_count", u32),
+                ("world", ctypes.c_double * 16)]
+
+
 # Every symbol the header declares, with (restype, argtypes).
 _P = ctypes.c_void_p
 _FP = ctypes.POINTER(ctypes.c_float)
+_DP = ctypes.POINTER(ctypes.c_double)
 _UP = ctypes.POINTER(ctypes.c_uint32)
 SIGNATURES = {
     "pbf_abi_version": (ctypes.c_int, []),
@@ -115,6 +125,9 @@ SIGNATURES = {
     "pbf_voxelize_cube": (ctypes.c_int, [_P, _FP, _FP, _UP]),
     "pbf_voxelize_sphere": (ctypes.c_int, [_P, _FP, ctypes.c_float, _UP]),
     "pbf_jitter_particles": (ctypes.c_int, [_P, ctypes.c_float, ctypes.c_uint64]),
+    "pbf_voxelize_mesh": (ctypes.c_int, [_P, _FP, u32, _UP, u32, _DP, _UP]),
+    "pbf_voxelize_mesh_points": (ctypes.c_int, [_FP, u32, _UP, u32, _DP, ctypes.c_double, _FP, u32, _UP]),
+    "pbf_seed_device": (ctypes.c_int, [_P, ctypes.POINTER(SeedItem), u32, f32, ctypes.c_uint64, _UP]),
     "pbf_host_particle_count": (ctypes.c_int, [_P, _UP]),
     "pbf_copy_host_particles": (ctypes.c_int, [_P, _FP, u32]),
     "pbf_set_particle_position": (ctypes.c_int, [_P]),

@@ -91,6 +91,73 @@ def jitter(pts, amplitude, seed):
     return out
 
 
+# ---- triangle meshes (SPH.voxelizeMesh inputs) ----------------------------------------
+def parse_obj(text):
+    """Vertices (V, 3) float32 and triangles (T, 3) uint32 of a Wavefront OBJ
+    text (v and f records; polygons fanned into triangles, 1-based indices)."""
+    verts, tris = [], []
+    for line in text.splitlines():
+        t = line.split()
+        if not t:
+            continue
+        if t[0] == "v":
+            verts.append([float(t[1]), float(t[2]), float(t[3])])
+        elif t[0] == "f":
+            idx = [int(f.split("/")[0]) for f in t[1:]]
+            idx = [i - 1 if i > 0 else len(verts) + i for i in idx]
+            for q in range(1, len(idx) - 1):
+                tris.append([idx[0], idx[q], idx[q + 1]])
+    return np.array(verts, np.float32), np.array(tris, np.uint32)
+
+
+def uv_sphere(radius, center=(0.0, 0.0, 0.0), stacks=24, slices=48):
+    """Closed UV sphere with outward-facing triangles (counter-clockwise seen
+    from outside)."""
+    v = [[0.0, radius, 0.0]]
+    for i in range(1, stacks):
+        th = np.pi * i / stacks
+        for j in range(slices):
+            ph = 2.0 * np.pi * j / slices
+            v.append([radius * np.sin(th) * np.cos(ph), radius * np.cos(th), radius * np.sin(th) * np.sin(ph)])
+    v.append([0.0, -radius, 0.0])
+    v = np.array(v, np.float64) + np.array(center, np.float64)
+    t = []
+    ring = lambda i, j: 1 + (i - 1) * slices + (j % slices)
+    for j in range(slices):
+        t.append([0, ring(1, j + 1), ring(1, j)])
+    for i in range(1, stacks - 1):
+        for j in range(slices):
+            a, b, c, d = ring(i, j), ring(i, j + 1), ring(i + 1, j), ring(i + 1, j + 1)
+            t.append([a, b, d])
+            t.append([a, d, c])
+    last = len(v) - 1
+    for j in range(slices):
+        t.append([last, ring(stacks - 1, j), ring(stacks - 1, j + 1)])
+    return v.astype(np.float32), np.array(t, np.uint32)
+
+
+def trs_matrix(translate=(0.0, 0.0, 0.0), rotate_deg=(0.0, 0.0, 0.0), scale=1.0):
+    """4x4 row-major world matrix T * Rz * Ry * Rx * S (three.js Object3D
+    order for the default XYZ Euler rotation)."""
+    rx, ry, rz = np.radians(rotate_deg)
+    cx, sx, cy, sy, cz, sz = np.cos(rx), np.sin(rx), np.cos(ry), np.sin(ry), np.cos(rz), np.sin(rz)
+    Rx = np.array([[1, 0, 0], [0, cx, -sx], [0, sx, cx]])
+    Ry = np.array([[cy, 0, sy], [0, 1, 0], [-sy, 0, cy]])
+    Rz = np.array([[cz, -sz, 0], [sz, cz, 0], [0, 0, 1]])
+    m = np.eye(4)
+    m[:3, :3] = Rz @ Ry @ Rx * float(scale)
+    m[:3, 3] = translate
+    return m
+
+
+def load_mesh_npz(name, folder=None):
+    """A mesh fixture of tests/golden (vertices, triangles)."""
+    folder = folder or os.path.join(os.path.dirname(os.path.dirname(os.path.dirname(os.path.abspath(__file__)))),
+                                    "tests", "golden")
+    d = np.load(os.path.join(folder, "mesh_%s.npz" % name))
+    return d["vertices"], d["triangles"]
+
+
 # ---- configs ---------------------------------------------------------------------------
 def base_config(**kw):
     c = L.Config()

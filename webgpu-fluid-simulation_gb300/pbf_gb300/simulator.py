@@ -108,6 +108,58 @@ class PBF:
                     "voxelizeSphere")
         return c.value
 
+    def voxelizeMesh(self, vertices, triangles, world=None):
+        """SPH.voxelizeMesh (SPH.ts:151-187) for a triangle mesh given as
+        local-space vertices (V, 3), triangles (T, 3) and a 4x4 world matrix
+        (row-major numpy array, float64 like three.js matrices; identity by
+        default)."""
+        v = np.ascontiguousarray(vertices, np.float32)
+        t = np.ascontiguousarray(triangles, np.uint32)
+        w = np.eye(4) if world is None else np.asarray(world, np.float64)
+        wc = np.ascontiguousarray(w.T, np.float64)  # column-major, as three.js Matrix4.elements
+        c = ctypes.c_uint32()
+        self._check(self._lib.pbf_voxelize_mesh(self._h, v.ctypes.data_as(ctypes.POINTER(ctypes.c_float)), v.shape[0],
+                                                t.ctypes.data_as(ctypes.POINTER(ctypes.c_uint32)), t.shape[0],
+                                                wc.ctypes.data_as(ctypes.POINTER(ctypes.c_double)), ctypes.byref(c)),
+                    "voxelizeMesh")
+        return c.value
+
+    def seed_device(self, items, jitter=0.0, seed=0):
+        """Scene seeding on the GPU (pbf_seed_device): the same particles as
+        reset + voxelizeCube / voxelizeSphere / voxelizeMesh over `items` in
+        order + jitter(jitter, seed) + setParticlePosition, written straight
+        into the device buffers.  items: ("cube", mn, mx), ("sphere", centre,
+        radius) or ("mesh", vertices, triangles, world-or-None)."""
+        arr = (L.SeedItem * max(len(items), 1))()
+        keep = []
+        for q, it in enumerate(items):
+            d = arr[q]
+            if it[0] == "cube":
+                d.kind = L.SEED_CUBE
+                d.a[:] = [float(x) for x in it[1]]
+                d.b[:] = [float(x) for x in it[2]]
+            elif it[0] == "sphere":
+                d.kind = L.SEED_SPHERE
+                d.a[:] = [float(x) for x in it[1]]
+                d.b[:] = [float(it[2]), 0.0, 0.0]
+            elif it[0] == "mesh":
+                d.kind = L.SEED_MESH
+                v = np.ascontiguousarray(it[1], np.float32)
+                t = np.ascontiguousarray(it[2], np.uint32)
+                w = np.eye(4) if len(it) < 4 or it[3] is None else np.asarray(it[3], np.float64)
+                keep += [v, t]
+                d.vertices = v.ctypes.data_as(ctypes.POINTER(ctypes.c_float))
+                d.vertex_count = v.shape[0]
+                d.indices = t.ctypes.data_as(ctypes.POINTER(ctypes.c_uint32))
+                d.triangle_count = t.shape[0]
+                d.world[:] = [float(x) for x in w.T.ravel()]   # column-major
+            else:
+                raise ValueError("unknown seeding item %r" % (it[0],))
+        total = ctypes.c_uint32()
+        self._check(self._lib.pbf_seed_device(self._h, arr, len(items), float(jitter), int(seed), ctypes.byref(total)),
+                    "seed_device")
+        return total.value
+
     def jitter(self, amplitude, seed):
         self._check(self._lib.pbf_jitter_particles(self._h, float(amplitude), int(seed)), "jitter")
 
@@ -476,3 +528,27 @@ def mlp_train(m, feat, target, epochs=20, batch=8192, lr=2e-3, seed=0):
     if rc:
         raise L.PBFError(rc, "mlp_train")
     return loss.value
+
+
+def voxelize_mesh_points(vertices, triangles, particle_radius, world=None):
+    """Stand-alone mesh voxelisation on the GPU (pbf_voxelize_mesh_points):
+    the kept lattice points as (n, 4) float32.  world: 4x4 row-major float64
+    (identity by default)."""
+    lib = L.load()
+    v = np.ascontiguousarray(vertices, np.float32)
+    t = np.ascontiguousarray(triangles, np.uint32)
+    w = np.eye(4) if world is None else np.asarray(world, np.float64)
+    wc = np.ascontiguousarray(w.T, np.float64)
+    fp, up, dp = ctypes.POINTER(ctypes.c_float), ctypes.POINTER(ctypes.c_uint32), ctypes.POINTER(ctypes.c_double)
+    c = ctypes.c_uint32()
+    rc = lib.pbf_voxelize_mesh_points(v.ctypes.data_as(fp), v.shape[0], t.ctypes.data_as(up), t.shape[0],
+                                      wc.ctypes.data_as(dp), float(particle_radius), None, 0, ctypes.byref(c))
+    if rc not in (L.PBF_OK, L.PBF_ECAPACITY):
+        raise L.PBFError(rc, "voxelize_mesh_points")
+    out = np.zeros((c.value, 4), np.float32)
+    rc = lib.pbf_voxelize_mesh_points(v.ctypes.data_as(fp), v.shape[0], t.ctypes.data_as(up), t.shape[0],
+                                      wc.ctypes.data_as(dp), float(particle_radius),
+                                      out.ctypes.data_as(fp), c.value, ctypes.byref(c))
+    if rc:
+        raise L.PBFError(rc, "voxelize_mesh_points")
+    return out

@@ -492,6 +492,60 @@ uint32_t pbf_scene_count(const pbf_handle* h); /* 1 for a single-scene handle */
 int pbf_get_scene_info(const pbf_handle* h, uint32_t scene, pbf_scene_info* out);
 int pbf_get_scene_metrics(pbf_handle* h, uint32_t scene, pbf_metrics* out);
 
+/* ---- screen-space fluid buffers: FilteredParticleFluid
+ * (src/renderer/filteredParticleFluid/fluid.ts:150-185) without the WebGPU
+ * render pipelines.  ParicleRasterizer.execute (paricleRasterizer.ts:170-204)
+ * splats every particle of `position` twice: a camera-facing sprite of side
+ * particle_radius into the depth map (W x H, eye-space depth of the nearest
+ * sphere surface, 0 where empty; depthPassShader.ts), tested against and
+ * written to the scene depth (reverse-Z, 'greater'), and a sprite of side
+ * 2 * particle_radius into the volume map ((W/2) x (H/2), sum of
+ * exp(-2 |uv|^2); volumePassShader.ts).  TextureFilter.execute
+ * (textureFilter.ts:129-160, filterPassShader.ts) then applies the
+ * separable narrow-range filter to the depth map when filter_size >= 2.
+ * Everything runs as CUDA kernels on device buffers; the results are
+ * deterministic (ties go to the lower particle index, the volume sum is
+ * exact in 64-bit fixed point before one rounding to float). */
+typedef struct pbf_render_options {  /* RenderingOptions (src/common/shader.ts:40-47) */
+  uint32_t mode;          /* shading mode (kept for the screen-space shading pass) */
+  uint32_t filter_size;   /* 0..32; < 2 disables the filter */
+  float particle_radius;  /* rendering radius (0.02) */
+  float opacity;
+  float tint_color[3];    /* 0..1 */
+} pbf_render_options;
+typedef struct pbf_camera {  /* Camera uniform (src/common/shader.ts:2-10), column-major float32 */
+  float position[3];
+  float view[16];           /* matrixWorldInverse: affine */
+  float view_inverse[16];   /* matrixWorld */
+  float projection[16];     /* perspective (reverse-Z) or orthographic: no x/y shear */
+  float params[4];
+} pbf_camera;
+typedef struct pbf_renderer pbf_renderer;
+enum { PBF_RENDER_DEPTH = 0, PBF_RENDER_VOLUME = 1 };
+int pbf_renderer_create(uint32_t width, uint32_t height, pbf_renderer** out);
+int pbf_renderer_destroy(pbf_renderer* r);
+/* FilteredParticleFluid.setConfig (fluid.ts:114-133). */
+int pbf_renderer_set_config(pbf_renderer* r, const pbf_render_options* options);
+/* The camera uniform (GlobalResource.update, globalResource.ts:165-181). */
+int pbf_renderer_set_camera(pbf_renderer* r, const pbf_camera* camera);
+/* Rasterize + filter for n particles at d_positions (device float4, xyz
+ * used).  d_scene_depth: NULL (a cleared depth buffer, all 0) or a device
+ * float [W*H] reverse-Z depth buffer, read and updated in place. */
+int pbf_render(pbf_renderer* r, const float* d_positions, uint32_t n, float* d_scene_depth, void* stream);
+/* TextureFilter.execute (textureFilter.ts:129-160) on any device r32float
+ * image of width x height, in place, with options->filter_size and
+ * options->particle_radius (threshold 5 r, high bound r). */
+int pbf_texture_filter(const pbf_render_options* options, float* d_texture, uint32_t width, uint32_t height,
+                       void* stream);
+/* The same for a simulator's current particles (pbf_position_device, its stream). */
+int pbf_render_simulation(pbf_renderer* r, pbf_handle* h, float* d_scene_depth);
+const float* pbf_renderer_map_device(const pbf_renderer* r, uint32_t which); /* PBF_RENDER_* */
+int pbf_renderer_map_size(const pbf_renderer* r, uint32_t which, uint32_t* width, uint32_t* height);
+int pbf_renderer_copy_map(const pbf_renderer* r, uint32_t which, float* host, size_t bytes);
+/* Device times of the last pbf_render: rasterization and filter
+ * (FilteredParticleFluid.renderTimestamp, fluid.ts:150-175, timestamps 6-7). */
+int pbf_renderer_timings(const pbf_renderer* r, float ms[2]);
+
 #ifdef __cplusplus
 }
 #endif

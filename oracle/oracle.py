@@ -58,6 +58,11 @@ def load():
                                                   _FP, _FP]),
         "oracle_voxelize_mesh": (ctypes.c_int, [_FP, ctypes.c_uint32, _UP, ctypes.c_uint32, _DP, ctypes.c_double,
                                                 _FP, ctypes.c_uint32, _UP]),
+        "oracle_render": (ctypes.c_int, [_FP, ctypes.c_uint32, ctypes.c_uint32, ctypes.c_uint32, _FP, _FP,
+                                         ctypes.c_float, ctypes.c_uint32, _FP, _FP, _FP]),
+        "oracle_splat_exp": (ctypes.c_float, [ctypes.c_float]),
+        "oracle_narrow_range_filter": (ctypes.c_int, [_FP, ctypes.c_uint32, ctypes.c_uint32, ctypes.c_uint32,
+                                                      ctypes.c_float]),
         "oracle_threads": (ctypes.c_int, []),
         "oracle_set_threads": (None, [ctypes.c_int]),
     }
@@ -250,4 +255,35 @@ def voxelize_mesh(vertices, triangles, particle_radius, world=None):
                                   c.value, ctypes.byref(c))
     if rc:
         raise RuntimeError("oracle_voxelize_mesh failed (%d)" % rc)
+    return out
+
+
+def render(positions, width, height, view, projection, radius, filter_size, scene_depth=None):
+    """FilteredParticleFluid's rasterisation + narrow-range filter restated on
+    the CPU: (depth map (H, W), volume map (H/2, W/2), updated scene depth or
+    None).  view / projection: 4x4 row-major float32 arrays."""
+    lib = load()
+    p = np.ascontiguousarray(positions, np.float32).reshape(-1, 4)
+    v = np.ascontiguousarray(np.asarray(view, np.float32).T)
+    pr = np.ascontiguousarray(np.asarray(projection, np.float32).T)
+    depth = np.zeros((height, width), np.float32)
+    volume = np.zeros((height // 2, width // 2), np.float32)
+    scene = None if scene_depth is None else np.ascontiguousarray(scene_depth, np.float32).copy()
+    rc = lib.oracle_render(_fp(p), p.shape[0], width, height, _fp(v), _fp(pr), float(radius), int(filter_size),
+                           None if scene is None else _fp(scene), _fp(depth), _fp(volume))
+    if rc:
+        raise RuntimeError("oracle_render failed (%d)" % rc)
+    return depth, volume, scene
+
+
+def splat_exp(x):
+    return float(load().oracle_splat_exp(float(x)))
+
+
+def narrow_range_filter(img, filter_size, radius):
+    """TextureFilter.execute restated: the filtered copy of a float32 image."""
+    out = np.ascontiguousarray(img, np.float32).copy()
+    rc = load().oracle_narrow_range_filter(_fp(out), out.shape[1], out.shape[0], int(filter_size), float(radius))
+    if rc:
+        raise RuntimeError("oracle_narrow_range_filter failed (%d)" % rc)
     return out

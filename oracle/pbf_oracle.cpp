@@ -1203,6 +1203,177 @@ int oracle_voxelize_mesh(const float* vertices, uint32_t nv, const uint32_t* idx
   return c > capacity ? 2 : 0;
 }
 
+// ---- screen-space fluid buffers (src/renderer/filteredParticleFluid) ----
+// ParicleRasterizer.execute (paricleRasterizer.ts:170-204) with the sprite
+// shaders depthPassShader.ts / volumePassShader.ts, then TextureFilter
+// (textureFilter.ts:129-160, filterPassShader.ts), restated particle by
+// particle and pixel by pixel.  Sprite geometry: the camera-space centre c =
+// view * (p, 1) plus (+-hs, +-hs, 0, 0) (hs = R/2 for depth, R for volume)
+// through the projection; the rectangle's framebuffer edges are
+// 0.5 (ndc.x + 1) W and 0.5 (1 - ndc.y) H; pixels whose centres lie in it
+// (left/top edges in) are covered; uv is the centre's position across it.
+// Depth: ties of equal depth keep the lower particle index; the volume sum
+// is exact (integer sum of the terms scaled by 2^40).  Filter texel reads
+// clamp to the image edge.  Returns 0, or 1 for a clipped-out camera setup.
+static inline void rnd_mat_vec(const float* m, float x, float y, float z, float w, float o[4]) {
+  for (int r = 0; r < 4; ++r) o[r] = ((m[r] * x + m[4 + r] * y) + m[8 + r] * z) + m[12 + r] * w;
+}
+
+struct RndSprite {
+  float fx0, fx1, fyt, fyb, cz, cw;
+  int i0, i1, j0, j1;
+};
+
+static inline int rnd_edge(float f, int size) {
+  float e = std::min(std::max(f - 0.5f, -1.0f), (float)size);
+  int i = (int)std::ceil(e);
+  return std::min(std::max(i, 0), size);
+}
+
+static bool rnd_sprite(const float* P, const float c[4], float hs, int W, int H, RndSprite& s) {
+  float bl[4], tr[4];
+  rnd_mat_vec(P, c[0] + (-hs), c[1] + (-hs), c[2], c[3], bl);
+  rnd_mat_vec(P, c[0] + hs, c[1] + hs, c[2], c[3], tr);
+  if (!(bl[3] > 0.0f) || !(bl[2] >= 0.0f) || !(bl[2] <= bl[3])) return false;
+  s.fx0 = 0.5f * (bl[0] / bl[3] + 1.0f) * (float)W;
+  s.fx1 = 0.5f * (tr[0] / tr[3] + 1.0f) * (float)W;
+  s.fyb = 0.5f * (-(bl[1] / bl[3]) + 1.0f) * (float)H;
+  s.fyt = 0.5f * (-(tr[1] / tr[3]) + 1.0f) * (float)H;
+  if (!(s.fx1 != s.fx0) || !(s.fyb != s.fyt)) return false;
+  s.i0 = rnd_edge(std::min(s.fx0, s.fx1), W);
+  s.i1 = rnd_edge(std::max(s.fx0, s.fx1), W);
+  s.j0 = rnd_edge(std::min(s.fyt, s.fyb), H);
+  s.j1 = rnd_edge(std::max(s.fyt, s.fyb), H);
+  s.cz = c[2];
+  s.cw = c[3];
+  return s.i0 < s.i1 && s.j0 < s.j1;
+}
+
+static inline float rnd_r2(const RndSprite& s, int i, int j) {
+  const float u = (((float)i + 0.5f) - s.fx0) / (s.fx1 - s.fx0);
+  const float v = (s.fyb - ((float)j + 0.5f)) / (s.fyb - s.fyt);
+  const float nx = u * 2.0f - 1.0f, ny = v * 2.0f - 1.0f;
+  return nx * nx + ny * ny;
+}
+
+// exp(x), x in [-2, 0]: x = k ln2 + r (Cody-Waite, ln 2 = hi + lo with a
+// 16-bit hi), Taylor series of exp(r) to degree 8 (Horner), times 2^k.
+static inline float rnd_exp(float x) {
+  const float k = std::floor(x * 1.44269502f + 0.5f);
+  const float r = (x - k * 0.693145751953125f) - k * 1.42860677e-6f;
+  const float c[9] = {1.0f, 1.0f, 0.5f, 1.66666667e-1f, 4.16666667e-2f, 8.33333333e-3f, 1.38888889e-3f,
+                      1.98412698e-4f, 2.48015873e-5f};
+  float p = c[8];
+  for (int q = 7; q >= 0; --q) p = p * r + c[q];
+  return p * std::ldexp(1.0f, (int)k);
+}
+
+static void rnd_filter_line(const float* line, int len, int stride, int half, const float* g, float threshold,
+                            float mu, int pos, bool& write, float& out) {
+  // texel `pos` of a line: centre at pos - (16 - half), taps +-i, reads clamped
+  auto at = [&](int q) { return line[(size_t)std::min(std::max(q, 0), len - 1) * stride]; };
+  const int c = pos - (16 - half);
+  const float center = at(c);
+  write = center > 0.0f;
+  if (!write) return;
+  float vs = center, ws = 1.0f, lo = center - threshold, hi = center + threshold;
+  const float bh = center + mu;
+  for (int i = 1; i <= half; ++i) {
+    float a = at(c - i), b = at(c + i);
+    if (a < lo || b < lo) continue;
+    a = a > hi ? bh : a;
+    b = b > hi ? bh : b;
+    lo = std::min(lo, std::min(a, b) - threshold);
+    hi = std::max(hi, std::max(a, b) + threshold);
+    ws += g[i] * 2.0f;
+    vs += (a + b) * g[i];
+  }
+  out = vs / ws;
+}
+
+float oracle_splat_exp(float x) { return rnd_exp(x); }
+
+// TextureFilter.execute on one r32float image in place (x pass into a
+// cleared temporary, y pass back where the temporary's centre is positive).
+int oracle_narrow_range_filter(float* img, uint32_t width, uint32_t height, uint32_t filter_size, float R) {
+  if (filter_size > 32) return 1;
+  if (filter_size < 2) return 0;
+  const int W = (int)width, H = (int)height, half = (int)(filter_size >> 1);
+  const float sigma = (float)half * 0.5f, k = 0.5f / (sigma * sigma);
+  float g[17] = {};
+  for (int i = 0; i <= half; ++i) g[i] = (float)std::exp((double)(-(float)(i * i) * k));
+  std::vector<float> temp((size_t)W * H, 0.0f);
+  for (int y = 0; y < H; ++y)
+    for (int x = 0; x < W; ++x) {
+      bool wr;
+      float v = 0.0f;
+      rnd_filter_line(img + (size_t)y * W, W, 1, half, g, R * 5.0f, R, x, wr, v);
+      temp[(size_t)y * W + x] = wr ? v : 0.0f;
+    }
+  for (int x = 0; x < W; ++x)
+    for (int y = 0; y < H; ++y) {
+      bool wr;
+      float v = 0.0f;
+      rnd_filter_line(temp.data() + x, H, W, half, g, R * 5.0f, R, y, wr, v);
+      if (wr) img[(size_t)y * W + x] = v;
+    }
+  return 0;
+}
+
+int oracle_render(const float* pos, uint32_t n, uint32_t width, uint32_t height, const float* view, const float* proj,
+                  float R, uint32_t filter_size, float* scene, float* depth_out, float* volume_out) {
+  const int W = (int)width, H = (int)height, W2 = W / 2, H2 = H / 2;
+  std::vector<uint64_t> keys((size_t)W * H);
+  std::vector<float> eye((size_t)W * H, 0.0f);
+  std::vector<uint64_t> acc((size_t)W2 * H2, 0);
+  auto bits = [](float f) {
+    uint32_t b;
+    std::memcpy(&b, &f, 4);
+    return b;
+  };
+  auto clamp01 = [](float d) { return d > 0.0f ? std::min(d, 1.0f) : 0.0f; };
+  for (size_t p = 0; p < keys.size(); ++p)
+    keys[p] = ((uint64_t)bits(clamp01(scene ? scene[p] : 0.0f)) << 32) | 0xffffffffull;
+  for (uint32_t q = 0; q < n; ++q) {
+    float c[4];
+    rnd_mat_vec(view, pos[4 * (size_t)q], pos[4 * (size_t)q + 1], pos[4 * (size_t)q + 2], 1.0f, c);
+    RndSprite s;
+    if (rnd_sprite(proj, c, 0.5f * R, W, H, s))
+      for (int j = s.j0; j < s.j1; ++j)
+        for (int i = s.i0; i < s.i1; ++i) {
+          const float r2 = rnd_r2(s, i, j);
+          if (r2 > 1.0f) continue;
+          const float z = s.cz + std::sqrt(1.0f - r2) * R;
+          const float w = s.cw + 0.0f * R;
+          const float d = clamp01((proj[10] * z + proj[14] * w) / (proj[11] * z + proj[15] * w));
+          const uint64_t key = ((uint64_t)bits(d) << 32) | (0xffffffffull - q);
+          const size_t p = (size_t)j * W + i;
+          if (key > keys[p]) {
+            keys[p] = key;
+            eye[p] = -z / w;
+          }
+        }
+    if (rnd_sprite(proj, c, R, W2, H2, s))
+      for (int j = s.j0; j < s.j1; ++j)
+        for (int i = s.i0; i < s.i1; ++i) {
+          const float r2 = rnd_r2(s, i, j);
+          if (r2 > 1.0f) continue;
+          acc[(size_t)j * W2 + i] += (uint64_t)((double)rnd_exp(-r2 * 2.0f) * 1099511627776.0);
+        }
+  }
+  for (size_t p = 0; p < keys.size(); ++p) {
+    const uint32_t init = bits(clamp01(scene ? scene[p] : 0.0f));
+    const bool hit = (uint32_t)(keys[p] >> 32) != init;
+    depth_out[p] = hit ? eye[p] : 0.0f;
+    if (hit && scene) {
+      const uint32_t b = (uint32_t)(keys[p] >> 32);
+      std::memcpy(&scene[p], &b, 4);
+    }
+  }
+  for (size_t p = 0; p < acc.size(); ++p) volume_out[p] = (float)((double)acc[p] * (1.0 / 1099511627776.0));
+  return oracle_narrow_range_filter(depth_out, width, height, filter_size, R) ? 1 : 0;
+}
+
 int oracle_threads(void) {
 #ifdef _OPENMP
   return omp_get_max_threads();

@@ -25,6 +25,7 @@ UNITS = [
     ("pbf_learned.cu", []),
     ("pbf_mlp_tc.cu", []),
     ("pbf_seed.cu", ["-fmad=false", "-Xcompiler", "-ffp-contract=off"]),
+    ("pbf_render.cu", ["-fmad=false", "-Xcompiler", "-ffp-contract=off"]),
 ]
 
 

@@ -108,6 +108,19 @@ class SeedItem(ctypes.Structure):
                 ("world", ctypes.c_double * 16)]
 
 
+RENDER_DEPTH, RENDER_VOLUME = 0, 1
+
+
+class RenderOptions(ctypes.Structure):
+    _fields_ = [("mode", u32), ("filter_size", u32), ("particle_radius", f32), ("opacity", f32),
+                ("tint_color", f32 * 3)]
+
+
+class Camera(ctypes.Structure):
+    _fields_ = [("position", f32 * 3), ("view", f32 * 16), ("view_inverse", f32 * 16), ("projection", f32 * 16),
+                ("params", f32 * 4)]
+
+
 # Every symbol the header declares, with (restype, argtypes).
 _P = ctypes.c_void_p
 _FP = ctypes.POINTER(ctypes.c_float)
@@ -128,6 +141,17 @@ SIGNATURES = {
     "pbf_voxelize_mesh": (ctypes.c_int, [_P, _FP, u32, _UP, u32, _DP, _UP]),
     "pbf_voxelize_mesh_points": (ctypes.c_int, [_FP, u32, _UP, u32, _DP, ctypes.c_double, _FP, u32, _UP]),
     "pbf_seed_device": (ctypes.c_int, [_P, ctypes.POINTER(SeedItem), u32, f32, ctypes.c_uint64, _UP]),
+    "pbf_renderer_create": (ctypes.c_int, [u32, u32, ctypes.POINTER(_P)]),
+    "pbf_renderer_destroy": (ctypes.c_int, [_P]),
+    "pbf_renderer_set_config": (ctypes.c_int, [_P, ctypes.POINTER(RenderOptions)]),
+    "pbf_renderer_set_camera": (ctypes.c_int, [_P, ctypes.POINTER(Camera)]),
+    "pbf_render": (ctypes.c_int, [_P, _P, u32, _P, _P]),
+    "pbf_render_simulation": (ctypes.c_int, [_P, _P, _P]),
+    "pbf_texture_filter": (ctypes.c_int, [ctypes.POINTER(RenderOptions), _P, u32, u32, _P]),
+    "pbf_renderer_map_device": (_P, [_P, u32]),
+    "pbf_renderer_map_size": (ctypes.c_int, [_P, u32, _UP, _UP]),
+    "pbf_renderer_copy_map": (ctypes.c_int, [_P, u32, _FP, ctypes.c_size_t]),
+    "pbf_renderer_timings": (ctypes.c_int, [_P, _FP]),
     "pbf_host_particle_count": (ctypes.c_int, [_P, _UP]),
     "pbf_copy_host_particles": (ctypes.c_int, [_P, _FP, u32]),
     "pbf_set_particle_position": (ctypes.c_int, [_P]),

@@ -1220,7 +1220,7 @@ static inline void rnd_mat_vec(const float* m, float x, float y, float z, float 
 }
 
 struct RndSprite {
-  float fx0, fx1, fyt, fyb, cz, cw;
+  float sx, ox, sy, oy, cz, cw;
   int i0, i1, j0, j1;
 };
 
@@ -1230,41 +1230,48 @@ static inline int rnd_edge(float f, int size) {
   return std::min(std::max(i, 0), size);
 }
 
+// n.xy = 2 uv - 1 at pixel (i, j): nx = i sx + ox with sx = 2 / (x1 - x0),
+// ox = (0.5 - x0) sx - 1; ny = j sy + oy with sy = -2 / (yb - yt),
+// oy = (yb - 0.5) (2 / (yb - yt)) - 1 (uv measured from the bottom edge).
 static bool rnd_sprite(const float* P, const float c[4], float hs, int W, int H, RndSprite& s) {
   float bl[4], tr[4];
   rnd_mat_vec(P, c[0] + (-hs), c[1] + (-hs), c[2], c[3], bl);
   rnd_mat_vec(P, c[0] + hs, c[1] + hs, c[2], c[3], tr);
   if (!(bl[3] > 0.0f) || !(bl[2] >= 0.0f) || !(bl[2] <= bl[3])) return false;
-  s.fx0 = 0.5f * (bl[0] / bl[3] + 1.0f) * (float)W;
-  s.fx1 = 0.5f * (tr[0] / tr[3] + 1.0f) * (float)W;
-  s.fyb = 0.5f * (-(bl[1] / bl[3]) + 1.0f) * (float)H;
-  s.fyt = 0.5f * (-(tr[1] / tr[3]) + 1.0f) * (float)H;
-  if (!(s.fx1 != s.fx0) || !(s.fyb != s.fyt)) return false;
-  s.i0 = rnd_edge(std::min(s.fx0, s.fx1), W);
-  s.i1 = rnd_edge(std::max(s.fx0, s.fx1), W);
-  s.j0 = rnd_edge(std::min(s.fyt, s.fyb), H);
-  s.j1 = rnd_edge(std::max(s.fyt, s.fyb), H);
+  const float fx0 = 0.5f * (bl[0] / bl[3] + 1.0f) * (float)W;
+  const float fx1 = 0.5f * (tr[0] / tr[3] + 1.0f) * (float)W;
+  const float fyb = 0.5f * (-(bl[1] / bl[3]) + 1.0f) * (float)H;
+  const float fyt = 0.5f * (-(tr[1] / tr[3]) + 1.0f) * (float)H;
+  if (!(fx1 != fx0) || !(fyb != fyt)) return false;
+  s.i0 = rnd_edge(std::min(fx0, fx1), W);
+  s.i1 = rnd_edge(std::max(fx0, fx1), W);
+  s.j0 = rnd_edge(std::min(fyt, fyb), H);
+  s.j1 = rnd_edge(std::max(fyt, fyb), H);
+  const float ax = 2.0f / (fx1 - fx0), ay = 2.0f / (fyb - fyt);
+  s.sx = ax;
+  s.ox = std::fmaf(0.5f - fx0, ax, -1.0f);
+  s.sy = -ay;
+  s.oy = std::fmaf(fyb - 0.5f, ay, -1.0f);
   s.cz = c[2];
   s.cw = c[3];
   return s.i0 < s.i1 && s.j0 < s.j1;
 }
 
 static inline float rnd_r2(const RndSprite& s, int i, int j) {
-  const float u = (((float)i + 0.5f) - s.fx0) / (s.fx1 - s.fx0);
-  const float v = (s.fyb - ((float)j + 0.5f)) / (s.fyb - s.fyt);
-  const float nx = u * 2.0f - 1.0f, ny = v * 2.0f - 1.0f;
-  return nx * nx + ny * ny;
+  const float nx = std::fmaf((float)i, s.sx, s.ox), ny = std::fmaf((float)j, s.sy, s.oy);
+  return std::fmaf(nx, nx, ny * ny);
 }
 
 // exp(x), x in [-2, 0]: x = k ln2 + r (Cody-Waite, ln 2 = hi + lo with a
-// 16-bit hi), Taylor series of exp(r) to degree 8 (Horner), times 2^k.
+// 16-bit hi), Taylor series of exp(r) to degree 8 (Horner with fused
+// multiply-adds), times 2^k.
 static inline float rnd_exp(float x) {
-  const float k = std::floor(x * 1.44269502f + 0.5f);
-  const float r = (x - k * 0.693145751953125f) - k * 1.42860677e-6f;
+  const float k = std::floor(std::fmaf(x, 1.44269502f, 0.5f));
+  const float r = std::fmaf(-k, 1.42860677e-6f, std::fmaf(-k, 0.693145751953125f, x));
   const float c[9] = {1.0f, 1.0f, 0.5f, 1.66666667e-1f, 4.16666667e-2f, 8.33333333e-3f, 1.38888889e-3f,
                       1.98412698e-4f, 2.48015873e-5f};
   float p = c[8];
-  for (int q = 7; q >= 0; --q) p = p * r + c[q];
+  for (int q = 7; q >= 0; --q) p = std::fmaf(p, r, c[q]);
   return p * std::ldexp(1.0f, (int)k);
 }
 
@@ -1343,9 +1350,9 @@ int oracle_render(const float* pos, uint32_t n, uint32_t width, uint32_t height,
         for (int i = s.i0; i < s.i1; ++i) {
           const float r2 = rnd_r2(s, i, j);
           if (r2 > 1.0f) continue;
-          const float z = s.cz + std::sqrt(1.0f - r2) * R;
-          const float w = s.cw + 0.0f * R;
-          const float d = clamp01((proj[10] * z + proj[14] * w) / (proj[11] * z + proj[15] * w));
+          const float z = std::fmaf(std::sqrt(1.0f - r2), R, s.cz);
+          const float w = s.cw;
+          const float d = clamp01(std::fmaf(proj[10], z, proj[14] * w) / std::fmaf(proj[11], z, proj[15] * w));
           const uint64_t key = ((uint64_t)bits(d) << 32) | (0xffffffffull - q);
           const size_t p = (size_t)j * W + i;
           if (key > keys[p]) {

@@ -23,6 +23,12 @@
 // order.  The winner's eye depth -z / w goes to the depth map (0 elsewhere)
 // and its depth to the depth buffer.
 //
+// Fragment n.xy: uv is the pixel centre's position across the rectangle,
+// n = 2 uv - 1, evaluated as one fused multiply-add per axis from per-sprite
+// constants (sx = 2 / (x1 - x0), ox = (0.5 - x0) sx - 1; likewise in y from
+// the bottom edge).  A sprite's fragments are skipped where a bound of its
+// depths cannot beat the pixel's key, which changes nothing in the result.
+//
 // Volume pass: sprites of half-side R on the half-resolution target add
 // exp(-2 |n.xy|^2).  The sum is kept in 64-bit fixed point with 40
 // fraction bits, where every float term in [e^-2, 1] is exact, so the sum
@@ -40,7 +46,8 @@
 // temporary's centre is positive and leaves the other texels as they were.
 //
 // This unit is compiled with -fmad=false: every float operation rounds as
-// written, which the CPU restatement reproduces.
+// written, fused multiply-adds only where written (__fmaf_rn), which the CPU
+// restatement reproduces with fmaf.
 #include <algorithm>
 #include <cmath>
 #include <cstdint>
@@ -64,11 +71,14 @@ struct Cam {
   float p[16];  // projection, column-major
 };
 
+// A sprite on one target: its covered pixels and the affine maps from pixel
+// index to the fragment's n.xy = 2 uv - 1 (uv measured from the rectangle's
+// left and bottom edges at the pixel centre): nx = i sx + ox, ny = j sy + oy.
 struct Sprite {
-  float fx0, fx1;  // framebuffer x of the left / right edge
-  float fyt, fyb;  // framebuffer y of the top / bottom edge
   int i0, i1, j0, j1;  // covered pixels [i0, i1) x [j0, j1)
-  float cz, cw;    // camera-space z and w of the centre
+  float sx, ox, sy, oy;
+  float cz, cw;        // camera-space z and w of the centre
+  uint32_t dmax;       // bits of an upper bound of the fragment depths (depth sprites)
 };
 
 __device__ inline void mat_vec(const float* m, float x, float y, float z, float w, float o[4]) {
@@ -82,23 +92,28 @@ __device__ inline int pixel_edge(float f, int size) {
   return min(max((int)ceilf(e), 0), size);
 }
 
-// The sprite of half-side hs around the particle on a W x H target; false
-// when it is clipped away.
+// The sprite of half-side hs around the camera-space centre c on a W x H
+// target; false when it is clipped away or covers no pixel centre.
 __device__ inline bool make_sprite(const Cam& C, const float c[4], float hs, int W, int H, Sprite& s) {
   float bl[4], tr[4];
   mat_vec(C.p, c[0] + (-hs), c[1] + (-hs), c[2], c[3], bl);
   mat_vec(C.p, c[0] + hs, c[1] + hs, c[2], c[3], tr);
   if (!(bl[3] > 0.0f) || !(bl[2] >= 0.0f) || !(bl[2] <= bl[3])) return false;
   const float fw = (float)W, fh = (float)H;
-  s.fx0 = 0.5f * (bl[0] / bl[3] + 1.0f) * fw;
-  s.fx1 = 0.5f * (tr[0] / tr[3] + 1.0f) * fw;
-  s.fyb = 0.5f * (-(bl[1] / bl[3]) + 1.0f) * fh;
-  s.fyt = 0.5f * (-(tr[1] / tr[3]) + 1.0f) * fh;
-  if (!(s.fx1 != s.fx0) || !(s.fyb != s.fyt)) return false;
-  s.i0 = pixel_edge(fminf(s.fx0, s.fx1), W);
-  s.i1 = pixel_edge(fmaxf(s.fx0, s.fx1), W);
-  s.j0 = pixel_edge(fminf(s.fyt, s.fyb), H);
-  s.j1 = pixel_edge(fmaxf(s.fyt, s.fyb), H);
+  const float fx0 = 0.5f * (bl[0] / bl[3] + 1.0f) * fw;
+  const float fx1 = 0.5f * (tr[0] / tr[3] + 1.0f) * fw;
+  const float fyb = 0.5f * (-(bl[1] / bl[3]) + 1.0f) * fh;
+  const float fyt = 0.5f * (-(tr[1] / tr[3]) + 1.0f) * fh;
+  if (!(fx1 != fx0) || !(fyb != fyt)) return false;
+  s.i0 = pixel_edge(fminf(fx0, fx1), W);
+  s.i1 = pixel_edge(fmaxf(fx0, fx1), W);
+  s.j0 = pixel_edge(fminf(fyt, fyb), H);
+  s.j1 = pixel_edge(fmaxf(fyt, fyb), H);
+  const float ax = 2.0f / (fx1 - fx0), ay = 2.0f / (fyb - fyt);
+  s.sx = ax;
+  s.ox = __fmaf_rn(0.5f - fx0, ax, -1.0f);
+  s.sy = -ay;
+  s.oy = __fmaf_rn(fyb - 0.5f, ay, -1.0f);
   s.cz = c[2];
   s.cw = c[3];
   return s.i0 < s.i1 && s.j0 < s.j1;
@@ -106,42 +121,64 @@ __device__ inline bool make_sprite(const Cam& C, const float c[4], float hs, int
 
 // |n.xy|^2 of the sprite's fragment at pixel (i, j).
 __device__ inline float sprite_r2(const Sprite& s, int i, int j) {
-  const float uvx = (((float)i + 0.5f) - s.fx0) / (s.fx1 - s.fx0);
-  const float uvy = (s.fyb - ((float)j + 0.5f)) / (s.fyb - s.fyt);
-  const float nx = uvx * 2.0f - 1.0f, ny = uvy * 2.0f - 1.0f;
-  return nx * nx + ny * ny;
+  const float nx = __fmaf_rn((float)i, s.sx, s.ox), ny = __fmaf_rn((float)j, s.sy, s.oy);
+  return __fmaf_rn(nx, nx, ny * ny);
+}
+
+// [0, 1] depth of camera-space z (w = the centre's w).
+__device__ inline float depth_of(const Cam& C, float z, float w) {
+  const float d = __fmaf_rn(C.p[10], z, C.p[14] * w) / __fmaf_rn(C.p[11], z, C.p[15] * w);
+  return d > 0.0f ? fminf(d, 1.0f) : 0.0f;
 }
 
 // Depth-pass fragment: camera z of the sphere point and its [0, 1] depth.
 __device__ inline float sprite_depth(const Cam& C, const Sprite& s, float r2, float R, float& z) {
-  const float nz = sqrtf(1.0f - r2);
-  z = s.cz + nz * R;
-  const float w = s.cw + 0.0f * R;
-  const float d = (C.p[10] * z + C.p[14] * w) / (C.p[11] * z + C.p[15] * w);
-  return d > 0.0f ? fminf(d, 1.0f) : 0.0f;
+  z = __fmaf_rn(sqrtf(1.0f - r2), R, s.cz);
+  return depth_of(C, z, s.cw);
+}
+
+// An upper bound of the depths of a depth sprite's fragments.  Their z lie
+// in [c.z, zt = c.z + R] (sqrt(1 - r2) is in [0, 1] and the rounded fma is
+// monotone in it).  With a positive denominator on that interval, a
+// numerator that does not fall and a denominator that does not rise as z
+// grows (p10 >= 0 >= p11: the reverse-Z perspective) make every rounded
+// non-negative depth at most the depth at zt, and negative depths clamp to
+// 0; the mirror case bounds them by the depth at c.z.  Otherwise there is no
+// bound (all ones).
+__device__ inline uint32_t depth_bound(const Cam& C, float cz, float cw, float R) {
+  const float zt = __fmaf_rn(1.0f, R, cz);
+  const float d0 = __fmaf_rn(C.p[11], cz, C.p[15] * cw), d1 = __fmaf_rn(C.p[11], zt, C.p[15] * cw);
+  if (!(d0 > 0.0f && d1 > 0.0f)) return 0xffffffffu;
+  if (C.p[10] >= 0.0f && C.p[11] <= 0.0f) return __float_as_uint(depth_of(C, zt, cw));
+  if (C.p[10] <= 0.0f && C.p[11] >= 0.0f) return __float_as_uint(depth_of(C, cz, cw));
+  return 0xffffffffu;
+}
+
+// v * 2^40 as an integer, exactly, for a float v in [2^-3, 2): its 24-bit
+// significand shifted by (biased exponent - 110).
+__device__ inline unsigned long long fix40(float v) {
+  const uint32_t b = __float_as_uint(v);
+  const uint32_t e = (b >> 23) & 0xffu;
+  return (unsigned long long)((b & 0x7fffffu) | 0x800000u) << (e - 110u);
 }
 
 // exp(x) for x in [-2, 0]: Cody-Waite reduction x = k ln2 + r with ln 2 in
 // two parts (the high part has 16 significant bits, so k * hi is exact for
-// |k| <= 3), then exp(r) by its Taylor series to degree 8 in Horner form
-// (|r| <= 0.35: truncation below 3e-10), scaled by 2^k.
-__host__ __device__ inline float splat_exp(float x) {
-  const float k = floorf(x * 1.44269502f + 0.5f);
-  const float r = (x - k * 0.693145751953125f) - k * 1.42860677e-6f;
-  float p = 2.48015873e-5f;           // 1/8!
-  p = p * r + 1.98412698e-4f;         // 1/7!
-  p = p * r + 1.38888889e-3f;         // 1/6!
-  p = p * r + 8.33333333e-3f;         // 1/5!
-  p = p * r + 4.16666667e-2f;         // 1/4!
-  p = p * r + 1.66666667e-1f;         // 1/3!
-  p = p * r + 0.5f;
-  p = p * r + 1.0f;
-  p = p * r + 1.0f;
-  const int e = (int)k + 127;         // 2^k as a float (k in [-3, 0])
-  uint32_t bits = (uint32_t)e << 23;
-  float scale;
-  memcpy(&scale, &bits, 4);
-  return p * scale;
+// |k| <= 3), then exp(r) by its Taylor series to degree 8 in Horner form with
+// fused multiply-adds (|r| <= 0.35: truncation below 3e-10), scaled by 2^k.
+__device__ inline float splat_exp(float x) {
+  const float k = floorf(__fmaf_rn(x, 1.44269502f, 0.5f));
+  const float r = __fmaf_rn(-k, 1.42860677e-6f, __fmaf_rn(-k, 0.693145751953125f, x));
+  float p = 2.48015873e-5f;              // 1/8!
+  p = __fmaf_rn(p, r, 1.98412698e-4f);   // 1/7!
+  p = __fmaf_rn(p, r, 1.38888889e-3f);   // 1/6!
+  p = __fmaf_rn(p, r, 8.33333333e-3f);   // 1/5!
+  p = __fmaf_rn(p, r, 4.16666667e-2f);   // 1/4!
+  p = __fmaf_rn(p, r, 1.66666667e-1f);   // 1/3!
+  p = __fmaf_rn(p, r, 0.5f);
+  p = __fmaf_rn(p, r, 1.0f);
+  p = __fmaf_rn(p, r, 1.0f);
+  return p * __uint_as_float((uint32_t)((int)k + 127) << 23);   // 2^k (k in [-3, 0])
 }
 
 __device__ inline uint32_t depth_bits(float d) { return __float_as_uint(d); }
@@ -157,41 +194,87 @@ __global__ void k_init(const float* scene, unsigned long long* keys, unsigned lo
   if (x < W2 && y < H2) acc[(size_t)y * W2 + x] = 0ull;
 }
 
-// One warp per particle: the depth sprite on the full target, then the
-// volume sprite on the half-resolution target.
+// Sprites are set up one per lane (32 particles per warp) in shared memory;
+// the warp then walks them one by one with its lanes spread over each
+// sprite's pixels: for sprites up to 32 pixels wide, floor(32 / width) rows
+// per step (lane -> row lane / width by a 16-bit reciprocal, exact for lane
+// and width up to 32), else 32 columns per step.
+struct SpriteSlot {
+  Sprite s[2];   // depth, volume
+  uint32_t ok;   // bit 0: depth sprite visible, bit 1: volume sprite visible
+};
+
+// ceil(2^16 / w) for w = 1 .. 32
+__constant__ uint32_t c_recip16[33] = {0,    65536, 32768, 21846, 16384, 13108, 10923, 9363, 8192, 7282, 6554,
+                                       5958, 5462,  5042,  4682,  4370,  4096,  3856,  3641, 3450, 3277, 3121,
+                                       2979, 2850,  2731,  2622,  2521,  2428,  2341,  2260, 2185, 2115, 2048};
+
+template <typename Frag>
+__device__ inline void walk_sprite(const Sprite& s, uint32_t lane, Frag frag) {
+  const int w = s.i1 - s.i0;
+  if (w <= 32) {
+    const uint32_t m = c_recip16[w];
+    const int rows = (int)((32u * m) >> 16);
+    const int lr = (int)((lane * m) >> 16), lc = (int)lane - lr * w;
+    if (lr >= rows) return;
+    for (int j = s.j0 + lr; j < s.j1; j += rows) frag(s.i0 + lc, j);
+  } else {
+    for (int j = s.j0; j < s.j1; ++j)
+      for (int i = s.i0 + (int)lane; i < s.i1; i += 32) frag(i, j);
+  }
+}
+
 __global__ void __launch_bounds__(256) k_splat(Cam C, const float4* __restrict__ pos, uint32_t n, float R, int W, int H,
                                                int W2, int H2, unsigned long long* keys, unsigned long long* acc) {
-  const uint32_t lane = threadIdx.x & 31;
+  __shared__ SpriteSlot slots[8][32];
+  const uint32_t lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
+  const uint32_t warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
   const uint32_t warps = (gridDim.x * blockDim.x) >> 5;
-  for (uint32_t q = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; q < n; q += warps) {
-    const float4 x = pos[q];
-    float c[4];
-    mat_vec(C.v, x.x, x.y, x.z, 1.0f, c);
-    Sprite s;
-    if (make_sprite(C, c, 0.5f * R, W, H, s)) {
-      const int w = s.i1 - s.i0, cnt = w * (s.j1 - s.j0);
-      const unsigned long long low = 0xffffffffull - q;
-      for (int t = lane; t < cnt; t += 32) {
-        const int i = s.i0 + t % w, j = s.j0 + t / w;
-        const float r2 = sprite_r2(s, i, j);
-        if (r2 > 1.0f) continue;
-        float z;
-        const float d = sprite_depth(C, s, r2, R, z);
-        const unsigned long long key = ((unsigned long long)depth_bits(d) << 32) | low;
-        unsigned long long* k = keys + (size_t)j * W + i;
-        if (key > *(volatile unsigned long long*)k) atomicMax(k, key);
+  for (uint32_t base = warp * 32; base < n; base += warps * 32) {
+    const uint32_t q = base + lane;
+    SpriteSlot& mine = slots[wib][lane];
+    mine.ok = 0;
+    if (q < n) {
+      const float4 x = pos[q];
+      float c[4];
+      mat_vec(C.v, x.x, x.y, x.z, 1.0f, c);
+      if (make_sprite(C, c, 0.5f * R, W, H, mine.s[0])) {
+        mine.ok |= 1u;
+        mine.s[0].dmax = depth_bound(C, c[2], c[3], R);
+      }
+      if (make_sprite(C, c, R, W2, H2, mine.s[1])) mine.ok |= 2u;
+    }
+    __syncwarp();
+    const uint32_t cnt = min(32u, n - base);
+    for (uint32_t k = 0; k < cnt; ++k) {
+      const SpriteSlot& sl = slots[wib][k];
+      const uint32_t ok = sl.ok;
+      if (ok & 1u) {
+        const Sprite s = sl.s[0];
+        const unsigned long long low = 0xffffffffull - (base + k);
+        const unsigned long long bound = ((unsigned long long)s.dmax << 32) | low;
+        walk_sprite(s, lane, [&](int i, int j) {
+          unsigned long long* kp = keys + (size_t)j * W + i;
+          // no fragment of this sprite can beat the pixel's current key
+          if (bound <= *(volatile unsigned long long*)kp) return;
+          const float r2 = sprite_r2(s, i, j);
+          if (r2 > 1.0f) return;
+          float z;
+          const float d = sprite_depth(C, s, r2, R, z);
+          const unsigned long long key = ((unsigned long long)__float_as_uint(d) << 32) | low;
+          if (key > *(volatile unsigned long long*)kp) atomicMax(kp, key);
+        });
+      }
+      if (ok & 2u) {
+        const Sprite s = sl.s[1];
+        walk_sprite(s, lane, [&](int i, int j) {
+          const float r2 = sprite_r2(s, i, j);
+          if (r2 > 1.0f) return;
+          atomicAdd(acc + (size_t)j * W2 + i, fix40(splat_exp(-r2 * 2.0f)));
+        });
       }
     }
-    if (make_sprite(C, c, R, W2, H2, s)) {
-      const int w = s.i1 - s.i0, cnt = w * (s.j1 - s.j0);
-      for (int t = lane; t < cnt; t += 32) {
-        const int i = s.i0 + t % w, j = s.j0 + t / w;
-        const float r2 = sprite_r2(s, i, j);
-        if (r2 > 1.0f) continue;
-        const float v = splat_exp(-r2 * 2.0f);
-        atomicAdd(acc + (size_t)j * W2 + i, (unsigned long long)((double)v * kFix));
-      }
-    }
+    __syncwarp();
   }
 }
 
@@ -216,7 +299,7 @@ __global__ void k_resolve(Cam C, const float4* __restrict__ pos, float R, int W,
     make_sprite(C, c, 0.5f * R, W, H, s);
     float z;
     sprite_depth(C, s, sprite_r2(s, x, y), R, z);
-    out = -z / (s.cw + 0.0f * R);
+    out = -z / s.cw;
     if (scene) scene[p] = __uint_as_float((uint32_t)(key >> 32));
   }
   depth[p] = out;
@@ -426,7 +509,7 @@ int pbf_render(pbf_renderer* r, const float* d_positions, uint32_t n, float* d_s
     int sms = 0, dev = 0;
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-    const unsigned blocks = (unsigned)std::min<uint64_t>(((uint64_t)n * 32 + 255) / 256, (uint64_t)sms * 8 * 32);
+    const unsigned blocks = (unsigned)std::min<uint64_t>(((uint64_t)n + 255) / 256, (uint64_t)sms * 8);
     k_splat<<<blocks, 256, 0, st>>>(C, pos, n, R, r->W, r->H, r->W2, r->H2, r->keys, r->acc);
   }
   k_resolve<<<rows, 256, 0, st>>>(C, pos, R, r->W, r->H, r->W2, r->H2, r->keys, r->acc, r->depth, d_scene_depth,

@@ -498,25 +498,41 @@ __device__ __forceinline__ float4 ldo(const float4* p) {  // the slot's own reco
 }
 
 // Visit the cnt neighbours of a slot in list order (interleaved layout:
-// entry q at base + 32 q).  Indices and the neighbour's float4 are loaded
-// four at a time so the gathers overlap; fn(j, xj) keeps the sequential
-// accumulation order of the reference loop.
+// entry q at base + 32 q).  Neighbours go in batches of four: the batch's
+// records are gathered, the next batch's indices are requested, then the
+// batch is consumed, so the list read (from DRAM) of one batch overlaps the
+// gathers and arithmetic of the previous one.  List entries are streamed
+// (evict-first): each pass reads the list once, and the records it gathers
+// stay cached.  fn(j, xj) keeps the sequential accumulation order of the
+// reference loop.
 template <bool kC = false, class Fn>
 __device__ __forceinline__ void for_each_neighbor(const uint32_t* __restrict__ list, uint32_t base, uint32_t cnt,
                                                   const float4* xs, Fn&& fn) {
   const uint32_t* l = list + base;
+  const uint32_t full = cnt & ~3u;
   uint32_t q = 0;
-  for (; q + 4 <= cnt; q += 4) {
-    uint32_t j0 = __ldg(l + 32 * q), j1 = __ldg(l + 32 * q + 32), j2 = __ldg(l + 32 * q + 64),
-             j3 = __ldg(l + 32 * q + 96);
-    float4 x0 = ldr<kC>(xs + j0), x1 = ldr<kC>(xs + j1), x2 = ldr<kC>(xs + j2), x3 = ldr<kC>(xs + j3);
-    fn(j0, x0);
-    fn(j1, x1);
-    fn(j2, x2);
-    fn(j3, x3);
+  if (full) {
+    uint32_t j0 = __ldcs(l), j1 = __ldcs(l + 32), j2 = __ldcs(l + 64), j3 = __ldcs(l + 96);
+    while (true) {
+      const float4 x0 = ldr<kC>(xs + j0), x1 = ldr<kC>(xs + j1), x2 = ldr<kC>(xs + j2), x3 = ldr<kC>(xs + j3);
+      const uint32_t c0 = j0, c1 = j1, c2 = j2, c3 = j3;
+      q += 4;
+      const bool more = q < full;
+      if (more) {
+        j0 = __ldcs(l + 32 * q);
+        j1 = __ldcs(l + 32 * q + 32);
+        j2 = __ldcs(l + 32 * q + 64);
+        j3 = __ldcs(l + 32 * q + 96);
+      }
+      fn(c0, x0);
+      fn(c1, x1);
+      fn(c2, x2);
+      fn(c3, x3);
+      if (!more) break;
+    }
   }
   for (; q < cnt; ++q) {
-    uint32_t j = __ldg(l + 32 * q);
+    uint32_t j = __ldcs(l + 32 * q);
     fn(j, ldr<kC>(xs + j));
   }
 }

@@ -217,18 +217,26 @@ class ClockSampler:
 
 
 # ---- workload ------------------------------------------------------------------------------
-def build_workload(name, field_backend="gpu"):
+BENCH_SEED, TRAIN_SEED = 1, 2
+
+
+def build_workload(name, field_backend="gpu", seed=BENCH_SEED, field=None):
+    """The workload's scene; `seed` picks the lattice jitter, `field` reuses
+    an already generated volume map of the same geometry."""
     from pbf_gb300 import scenes
     if name == "sphere_drop_1m":
-        spec = scenes.sphere_drop_spec()
+        spec = scenes.sphere_drop_spec(seed=seed)
         desc = ("sphere_drop_1m: 1,048,576 particles (128x64x128 lattice, r=0.0125, h=0.05, jitter 0.1r) "
-                "dropped on a R=0.4 sphere in a 3.3x2.6x3.3 box, 128^3 cubic volume map, 2 substeps x 1/120 s, "
+                "dropped on a R=0.4 sphere in a 3.3x2.6x3.3 box, 128^3 cubic volume map, 2 substeps x 1/300 s, "
                 "4 iterations, XSPH 0.01, vorticity 5e-4, surface tension 0.1")
     else:
-        spec = scenes.dam_break_16k_spec()
+        spec = scenes.dam_break_16k_spec(seed=seed - 1)
         desc = ("dam_break_16k: 16,384 particles (32x16x32 lattice, r=0.025, h=0.1) in a 3.2x1.0x1.6 box, "
                 "64^3 volume map, 2 substeps x 1/120 s, 4 iterations")
-    sc = scenes.build_scene(spec, quadrature=12, backend=field_backend, name=name)
+    if field is not None:
+        sc = scenes.Scene(name, spec[0], spec[1], field)
+    else:
+        sc = scenes.build_scene(spec, quadrature=12, backend=field_backend, name=name)
     return sc, desc
 
 
@@ -340,26 +348,38 @@ def gpu_arm(args, dist):
     sub = cfg.substeps
     iters = cfg.options.iterations
     # input state: the scene after `settle` frames (past the impact), resident on
-    # the device; the last third of the settling run is traced for training
-    trace_from = (2 * args.settle) // 3
-    sim.step(trace_from)
-    if not args.no_learned:
-        sim.set_trace(2_000_000, stride=max(1, n // 20000), salt=12345)
-    sim.step(args.settle - trace_from)
+    # the device
+    sim.step(args.settle)
     sim.synchronize()
     model = None
     train_info = None
+    trace_lo, trace_hi = (2 * args.settle) // 3, args.settle + max(args.warmup, 3) + args.steps
     if not args.no_learned:
+        # Training traces come from a second instance of the scene (the same
+        # geometry, another jitter seed) solved by the plain method over frames
+        # trace_lo .. trace_hi, the phase of the run the timed window covers;
+        # the benchmarked instance itself is never traced.
         from pbf_gb300 import mlp_init, mlp_fit_normalization, mlp_train
-        feat, tgt = sim.trace()
-        plain_err_max, plain_err_avg = sim.trace_error()
-        sim.set_trace(0)
+        tsc, _ = build_workload(args.workload, seed=TRAIN_SEED, field=sc.field)
+        tr = PBF(tsc.config)
+        tr.set_particles(tsc.particles)
+        tr.set_boundary_field(f["res"], f["origin"], f["extent"], f["sdf"], f["vol"])
+        tr.step(trace_lo)
+        rows_per_substep = 2_000_000 // max(1, (trace_hi - trace_lo) * sub)
+        tr.set_trace(2_000_000, stride=max(1, n // max(rows_per_substep, 1)), salt=12345)
+        tr.step(trace_hi - trace_lo)
+        tr.synchronize()
+        feat, tgt = tr.trace()
+        plain_err_max, plain_err_avg = tr.trace_error()
+        tr.close()
         model = mlp_init(7)
         mlp_fit_normalization(model, feat, tgt)
         t0 = time.perf_counter()
         loss = mlp_train(model, feat, tgt, epochs=10, batch=8192, lr=3e-3, seed=7)
         train_info = {"rows": int(len(tgt)), "epochs": 10, "batch": 8192, "final_mse_normalised": loss,
-                      "seconds": time.perf_counter() - t0, "traced_frames": args.settle - trace_from,
+                      "seconds": time.perf_counter() - t0,
+                      "traced": "frames %d-%d of a second instance of the scene (jitter seed %d; the benchmarked "
+                                "instance uses seed %d)" % (trace_lo, trace_hi, TRAIN_SEED, BENCH_SEED),
                       "plain_mean_compression_while_tracing": {"max": plain_err_max, "avg": plain_err_avg}}
     global _LAUNCH
     tune = None

@@ -276,7 +276,7 @@ def generate_field(shapes, res, origin, extent, h, quadrature=12, flags=0, backe
                 extent=np.array(extent, np.float32), sdf=sdf, vol=vol)
 
 
-def dam_break_16k_spec():
+def dam_break_16k_spec(seed=0):
     r = 0.025
     cfg = base_config(particle_radius=r, kernel_radius=4 * r, time_step=np.float32(1.0 / 120.0), substeps=2,
                       domain_min=(0.0, 0.0, 0.0), domain_max=(3.2, 1.0, 1.6), max_particles=16384,
@@ -287,14 +287,14 @@ def dam_break_16k_spec():
     mx = (r + 32.5 * d, r + 16.5 * d, r + 32.5 * d)  # half a spacing of slack against float rounding
     pts = lattice_cube(r, mn, mx)
     assert pts.shape[0] == 32 * 16 * 32
-    pts = jitter(pts, 0.1 * r, seed=0)
+    pts = jitter(pts, 0.1 * r, seed=seed)
     shapes = [(L.SHAPE_BOX_CONTAINER, (1.6, 0.5, 0.8), (1.6, 0.5, 0.8))]
     field_args = dict(shapes=shapes, res=(64, 64, 64), origin=(0.0, 0.0, 0.0), extent=(3.2, 1.0, 1.6),
                       h=4 * r)
     return cfg, pts, field_args
 
 
-def sphere_drop_spec(nx=128, ny=64, nz=128, field_res=(128, 128, 128)):
+def sphere_drop_spec(nx=128, ny=64, nz=128, field_res=(128, 128, 128), seed=1):
     r = 0.0125
     box = (3.3, 2.6, 3.3)
     # The workload states no time step: use the reference's TIME_STEP (SPH.ts:27),
@@ -316,7 +316,7 @@ def sphere_drop_spec(nx=128, ny=64, nz=128, field_res=(128, 128, 128)):
     mx = (x0 + (nx + 0.5) * d, y0 + (ny + 0.5) * d, z0 + (nz + 0.5) * d)  # slack against float rounding
     pts = lattice_cube(r, mn, mx)
     assert pts.shape[0] == nx * ny * nz
-    pts = jitter(pts, 0.1 * r, seed=1)
+    pts = jitter(pts, 0.1 * r, seed=seed)
     shapes = [(L.SHAPE_BOX_CONTAINER, (box[0] / 2, box[1] / 2, box[2] / 2), (box[0] / 2, box[1] / 2, box[2] / 2)),
               (L.SHAPE_SPHERE, sphere_c, (0.4, 0.0, 0.0))]
     field_args = dict(shapes=shapes, res=field_res, origin=(0.0, 0.0, 0.0), extent=box, h=4 * r)

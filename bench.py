@@ -8,7 +8,8 @@ confinement and Akinci surface tension on; 2 substeps of 1/120 s per step,
 4 solver iterations.  A "step" is one frame (2 substeps).
 
   value  — device throughput, state resident in HBM, CUDA events on the
-           library's stream, max over ranks (N replicas for --gpus N).
+           library's stream, each frame replayed as a CUDA graph (--no-graph:
+           eager launches), max over ranks (N replicas for --gpus N).
   e2e    — the same metric through the public C ABI as a host program uses
            it: per step pbf_set_options (the 20-byte SimulationOptions from
            host memory) + pbf_step + pbf_copy_field(POSITION) into a host
@@ -84,7 +85,8 @@ def parse_args():
                     help="batch64: 64 independent scenes in one batch handle (its own JSON line; the scenes are "
                          "split over the ranks)")
     ap.add_argument("--no-cpu-baseline", action="store_true")
-    ap.add_argument("--graph", action="store_true", help="replay the frame as a CUDA graph")
+    ap.add_argument("--no-graph", dest="graph", action="store_false",
+                    help="launch the passes eagerly instead of replaying each frame as a CUDA graph")
     ap.add_argument("--settle", type=int, default=150,
                     help="frames advanced from the initial lattice to build the input state (untimed set-up)")
     ap.add_argument("--no-learned", action="store_true", help="skip the learned warm-start measurement")
@@ -499,13 +501,21 @@ def _errors_from(sc, snap, frames, model=None, iterations=None, learned_iters=2,
 
 
 def _timed_path(args, sc, snap, dist, model=None, learned_iters=None, bound=1e9, clocks=False):
-    """W warm-up and K timed frames (CUDA events on the library's stream, per-pass
-    events on) of the plain solve or, with a model, the learned start."""
+    """W warm-up and K timed frames (CUDA events on the library's stream;
+    each frame replayed as a CUDA graph unless --no-graph) of the plain solve
+    or, with a model, the learned start.  The pass shares come from a second
+    handle started from the same state, stepped eagerly with per-pass events
+    over the same frames (not part of the timed value)."""
     import torch
     n, sub = sc.n, sc.config.substeps
-    sim = _handle_from(sc, snap)
-    if model is not None:
-        sim.set_learned(model, iterations=learned_iters, fallback_bound=bound)
+
+    def start():
+        h = _handle_from(sc, snap)
+        if model is not None:
+            h.set_learned(model, iterations=learned_iters, fallback_bound=bound)
+        return h
+
+    sim = start()
     if args.graph:
         sim.enable_graph(True)
     for _ in range(max(args.warmup, 3)):
@@ -514,8 +524,6 @@ def _timed_path(args, sc, snap, dist, model=None, learned_iters=None, bound=1e9,
     fb0 = sim.metrics()["fallback_steps"]
     stream = torch.cuda.ExternalStream(sim.stream)
     ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-    sim.set_kernel_timing(not args.graph)
-    sim.kernel_timing()
     sampler = ClockSampler(dist.local) if clocks else None
     if sampler:
         sampler.start()
@@ -530,12 +538,21 @@ def _timed_path(args, sc, snap, dist, model=None, learned_iters=None, bound=1e9,
     dist.barrier()
     clk = sampler.stop() if sampler else None
     ms = dist.max(ev0.elapsed_time(ev1))
-    kt = sim.kernel_timing() if not args.graph else {}
-    sim.set_kernel_timing(False)
     m = sim.metrics()
+    fallbacks = int(m["fallback_steps"] - fb0)
+    sim.close()
+    sim = start()
+    for _ in range(max(args.warmup, 3)):
+        sim.step(1)
+    sim.set_kernel_timing(True)
+    sim.kernel_timing()
+    for _ in range(args.steps):
+        sim.step(1)
+    sim.synchronize()
+    kt = sim.kernel_timing()
     sim.close()
     return {"value": dist.world * n * sub * args.steps / (ms / 1000.0), "ms_per_step": ms / args.steps,
-            "fallback_substeps": int(m["fallback_steps"] - fb0), "timed_substeps": sub * args.steps,
+            "fallback_substeps": fallbacks, "timed_substeps": sub * args.steps,
             "passes": kt, "metrics": m, "clocks": clk}
 
 
@@ -549,6 +566,8 @@ def _e2e_path(args, sc, snap, dist, model, learned_iters, bound):
     sim = _handle_from(sc, snap)
     if model is not None:
         sim.set_learned(model, iterations=learned_iters, fallback_bound=bound)
+    if args.graph:
+        sim.enable_graph(True)  # pbf_set_options with unchanged options keeps the graph
     for _ in range(max(args.warmup, 3)):
         sim.step(1)
     host_t = torch.empty((n, 4), dtype=torch.float32, pin_memory=True)

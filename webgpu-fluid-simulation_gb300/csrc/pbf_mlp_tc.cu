@@ -3,20 +3,31 @@
 // tensor cores: tcgen05.mma with both operands in shared memory and the
 // accumulators in tensor memory (TMEM), read back with tcgen05.ld.
 //
-// A CTA of 256 threads (two warpgroups) owns TMEM lanes 0..127 and walks
-// 128-row tiles (persistent grid).  Thread t serves row t % 128; warp w reads
-// lanes 32 (w % 4) .. + 31, and warpgroup g takes accumulator columns
-// 32 g .. 32 g + 31 of each layer, so both warpgroups share every epilogue:
-//   1. each thread normalises its row's 8 features into bf16 (K padded to 16)
-//      and stores them in the A tile (shared memory);
-//   2. one thread issues D1 = X W1 (M=128, N=64, K=16) into TMEM columns
-//      0..63 and commits to an mbarrier;
-//   3. every thread loads its row of D1 (tcgen05.ld), adds b1, applies SiLU,
-//      rounds to bf16 and stores the row of H1 into the second A tile;
-//   4. one thread issues D2 = H1 W2 (four K=16 steps) into columns 64..127;
-//   5. every thread loads its row of D2, adds b2, applies SiLU, rounds to
-//      bf16 and forms y = w3 . h2 + b3; lambda_hat = y * lam_scale.
-// The rounding points are those of the mma.sync kernels (pbf_learned.cu).
+// A CTA of 256 threads holds the weights once and runs two independent tile
+// pipelines, one per warpgroup: warpgroup g walks its own 128-row tiles
+// (persistent grid), thread t of the warpgroup serving row t.  Each pipeline
+// has its own operand tiles, its own mbarrier, a named barrier of 128
+// threads, and TMEM columns 64 g .. 64 g + 63 (layer 2 reuses layer 1's
+// columns once they have been read), so an SM keeps eight tiles in flight:
+//   1. each thread normalises its row's 8 features into bf16 and stores them
+//      in columns 0..7 of the pipeline's X tile (K = 16); columns 8 and 9
+//      hold the constant 1, the rest 0;
+//   2. the warpgroup's first thread issues D = X W1' (M=128, N=64, K=16),
+//      where rows 8 and 9 of W1' carry b1 split into two bf16 parts (hi and
+//      the remainder lo), so D = X W1 + b1 to about 2^-16 relative; it
+//      commits to the pipeline's mbarrier;
+//   3. every thread loads its row of D (tcgen05.ld), applies SiLU, rounds to
+//      bf16 and stores the row of H1 into the pipeline's H tile;
+//   4. D = H1 W2 (four K=16 steps) + X B2 (one step; B2's only non-zero rows
+//      8 and 9 carry b2 hi/lo against X's constant columns), into the same
+//      columns;
+//   5. every thread loads its row of D, applies SiLU, rounds to bf16 and
+//      stores H2 over H1;
+//   6. D = H2 W3' + X B3 (M=128, N=16): columns 0 and 1 of W3' hold w3 hi and
+//      lo, B3 carries b3 hi/lo, so y = D[0] + D[1]; lambda_hat = y lam_scale.
+// The rounding points of the activations are those of the mma.sync kernels
+// (pbf_learned.cu); the biases and the last layer are summed by the tensor
+// cores in FP32.
 //
 // Operand layout: the canonical K-major layout without swizzling: 8-row x
 // 16-byte core matrices stored contiguously (128 B), core matrices adjacent
@@ -37,20 +48,21 @@ namespace {
 using namespace mlp;
 
 constexpr int kTcRows = 128;        // rows per tile (UMMA M)
-constexpr int kTcThreads = 256;     // two threads per row (one per warpgroup)
-constexpr uint32_t kTmemCols = 128; // D1: columns 0..63, D2: 64..127
+constexpr int kTcThreads = 256;     // two pipelines of one warpgroup each
+constexpr uint32_t kTmemCols = 128; // pipeline g: columns 64 g .. 64 g + 63
 constexpr uint32_t kWaitPolls = 1u << 24;
 
 struct TcSmem {
-  alignas(128) uint8_t a1[kTcRows * 16 * 2];  // X: 128 x 16 bf16
-  alignas(128) uint8_t a2[kTcRows * 64 * 2];  // H1: 128 x 64 bf16
-  alignas(128) uint8_t b1[64 * 16 * 2];       // W1^T: 64 x 16 bf16 (N x K)
-  alignas(128) uint8_t b2[64 * 64 * 2];       // W2^T: 64 x 64 bf16
-  float bias1[64], bias2[64], w3[64];
-  float ypart[kTcRows];  // warpgroup 1's half of w3 . h2 per row
-  alignas(8) uint64_t mbar;
+  alignas(128) uint8_t a1[2][kTcRows * 16 * 2];  // X per pipeline: 128 x 16 bf16
+  alignas(128) uint8_t a2[2][kTcRows * 64 * 2];  // H1, then H2, per pipeline: 128 x 64 bf16
+  alignas(128) uint8_t b1[64 * 16 * 2];          // W1'^T: 64 x 16 bf16 (N x K), b1 in K rows 8, 9
+  alignas(128) uint8_t b2[64 * 64 * 2];          // W2^T: 64 x 64 bf16
+  alignas(128) uint8_t b2b[64 * 16 * 2];         // b2 in K rows 8, 9 (against X's ones): 64 x 16
+  alignas(128) uint8_t b3[16 * 64 * 2];          // W3'^T: 16 x 64, w3 hi / lo in N rows 0, 1
+  alignas(128) uint8_t b3b[16 * 16 * 2];         // b3 hi / lo in N row 0, K rows 8, 9
+  alignas(8) uint64_t mbar[2];
   uint32_t tmem;
-  uint32_t failed;
+  uint32_t failed[2];  // per pipeline: a completion wait gave up
 };
 
 // Byte offset of element (row, k) in a K-major canonical tile with kk K elements.
@@ -69,13 +81,17 @@ __device__ __forceinline__ uint64_t smem_desc(uint32_t addr, uint32_t lbo, uint3
 
 // Instruction descriptor of kind::f16: D f32 (bits 4-5 = 1), A and B bf16
 // (bits 7-9, 10-12 = 1), both K-major, N >> 3 at bits 17-22, M >> 4 at 24-28.
-constexpr uint32_t kIdesc = (1u << 4) | (1u << 7) | (1u << 10) | ((64u >> 3) << 17) | ((128u >> 4) << 24);
+constexpr uint32_t idesc_of(uint32_t n) {
+  return (1u << 4) | (1u << 7) | (1u << 10) | ((n >> 3) << 17) | ((128u >> 4) << 24);
+}
+constexpr uint32_t kIdesc64 = idesc_of(64), kIdesc16 = idesc_of(16);
 
-__device__ __forceinline__ void mma_f16(uint32_t d_tmem, uint64_t adesc, uint64_t bdesc, uint32_t accumulate) {
+__device__ __forceinline__ void mma_f16(uint32_t d_tmem, uint64_t adesc, uint64_t bdesc, uint32_t idesc,
+                                        uint32_t accumulate) {
   asm volatile(
       "{\n\t.reg .pred p;\n\tsetp.ne.b32 p, %4, 0;\n\t"
       "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n\t}\n" ::"r"(d_tmem),
-      "l"(adesc), "l"(bdesc), "r"(kIdesc), "r"(accumulate));
+      "l"(adesc), "l"(bdesc), "r"(idesc), "r"(accumulate));
 }
 
 __device__ __forceinline__ void mma_commit(uint32_t mbar) {
@@ -117,37 +133,80 @@ __device__ __forceinline__ void tmem_ld32(uint32_t taddr, float (&v)[32]) {
   for (int i = 0; i < 32; ++i) v[i] = __uint_as_float(r[i]);
 }
 
+// Two consecutive TMEM columns of this thread's lane.
+__device__ __forceinline__ void tmem_ld2(uint32_t taddr, float& a, float& b) {
+  uint32_t r0, r1;
+  asm volatile("tcgen05.ld.sync.aligned.32x32b.x2.b32 {%0, %1}, [%2];" : "=r"(r0), "=r"(r1) : "r"(taddr));
+  asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+  a = __uint_as_float(r0);
+  b = __uint_as_float(r1);
+}
+
+// SiLU(z) = z sigmoid(z) = h + h tanh(h) with h = z / 2 (one tanh.approx).
+__device__ __forceinline__ float silu_h(float z) {
+  const float h = 0.5f * z;
+  return fmaf(h, tanh_fast(h), h);
+}
+
+// Splits of a float into two bf16 parts: hi = bf16(x), lo = bf16(x - hi).
+__device__ __forceinline__ __nv_bfloat16 bf_hi(float x) { return __float2bfloat16_rn(x); }
+__device__ __forceinline__ __nv_bfloat16 bf_lo(float x) {
+  return __float2bfloat16_rn(x - __bfloat162float(__float2bfloat16_rn(x)));
+}
+
 __device__ __forceinline__ void st_shared_v4(uint32_t addr, uint32_t a, uint32_t b, uint32_t c, uint32_t d) {
   asm volatile("st.shared.v4.b32 [%0], {%1, %2, %3, %4};" ::"r"(addr), "r"(a), "r"(b), "r"(c), "r"(d) : "memory");
 }
 
-__global__ void __launch_bounds__(kTcThreads) k_mlp_infer_tc(const float* __restrict__ P, Norm nm,
+// Barrier of one pipeline's 128 threads (named barriers 1 and 2).
+__device__ __forceinline__ void pipe_sync(uint32_t wg) {
+  asm volatile("bar.sync %0, 128;" ::"r"(1u + wg) : "memory");
+}
+
+__global__ void __launch_bounds__(kTcThreads, 4) k_mlp_infer_tc(const float* __restrict__ P, Norm nm,
                                                             const float* __restrict__ feat, uint32_t rows,
                                                             float* __restrict__ lambda, float* __restrict__ lam_sum,
                                                             const float4* __restrict__ xs, float4* __restrict__ xl,
                                                             uint32_t* err) {
   __shared__ TcSmem sm;
   const uint32_t tid = threadIdx.x, warp = tid >> 5, row = tid & 127u, wg = tid >> 7;
-  // weights into the canonical layouts, K padding of X set to zero once
+  // weights into the canonical layouts; X's constant columns (8, 9: one) set once
+  const __nv_bfloat16 z16 = __float2bfloat16_rn(0.0f);
   for (uint32_t q = tid; q < 64u * 16u; q += kTcThreads) {
     const uint32_t n = q / 16u, k = q % 16u;
-    const float w = (k < (uint32_t)kIn) ? P[OFF_W1 + k * kH + n] : 0.0f;
-    *reinterpret_cast<__nv_bfloat16*>(sm.b1 + canon(n, k, 16)) = __float2bfloat16_rn(w);
+    __nv_bfloat16 w = z16, wb = z16;
+    if (k < (uint32_t)kIn) {
+      w = __float2bfloat16_rn(P[OFF_W1 + k * kH + n]);
+    } else if (k == 8) {
+      w = bf_hi(P[OFF_B1 + n]);
+      wb = bf_hi(P[OFF_B2 + n]);
+    } else if (k == 9) {
+      w = bf_lo(P[OFF_B1 + n]);
+      wb = bf_lo(P[OFF_B2 + n]);
+    }
+    *reinterpret_cast<__nv_bfloat16*>(sm.b1 + canon(n, k, 16)) = w;
+    *reinterpret_cast<__nv_bfloat16*>(sm.b2b + canon(n, k, 16)) = wb;
   }
   for (uint32_t q = tid; q < 64u * 64u; q += kTcThreads) {
     const uint32_t k = q / 64u, n = q % 64u;  // W2[k][n]
     *reinterpret_cast<__nv_bfloat16*>(sm.b2 + canon(n, k, 64)) = __float2bfloat16_rn(P[OFF_W2 + q]);
   }
-  for (uint32_t q = tid; q < 64u; q += kTcThreads) {
-    sm.bias1[q] = P[OFF_B1 + q];
-    sm.bias2[q] = P[OFF_B2 + q];
-    sm.w3[q] = P[OFF_W3 + q];
+  for (uint32_t q = tid; q < 16u * 64u; q += kTcThreads) {
+    const uint32_t n = q / 64u, k = q % 64u;
+    const float w = P[OFF_W3 + k];
+    *reinterpret_cast<__nv_bfloat16*>(sm.b3 + canon(n, k, 64)) = n == 0 ? bf_hi(w) : n == 1 ? bf_lo(w) : z16;
   }
-  if (wg == 0) st_shared_v4(smem_u32(sm.a1 + canon(row, 8, 16)), 0u, 0u, 0u, 0u);
-  const uint32_t mbar = smem_u32(&sm.mbar);
-  if (tid == 0) {
+  for (uint32_t q = tid; q < 16u * 16u; q += kTcThreads) {
+    const uint32_t n = q / 16u, k = q % 16u;
+    const float b = P[OFF_B3];
+    *reinterpret_cast<__nv_bfloat16*>(sm.b3b + canon(n, k, 16)) =
+        (n == 0 && k == 8) ? bf_hi(b) : (n == 0 && k == 9) ? bf_lo(b) : z16;
+  }
+  st_shared_v4(smem_u32(sm.a1[wg] + canon(row, 8, 16)), pack_bf16(1.0f, 1.0f), 0u, 0u, 0u);
+  const uint32_t mbar = smem_u32(&sm.mbar[wg]);
+  if (row == 0) {
     asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(mbar) : "memory");
-    sm.failed = 0u;
+    sm.failed[wg] = 0u;
   }
   if (warp == 0) {
     asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(&sm.tmem)),
@@ -159,29 +218,31 @@ __global__ void __launch_bounds__(kTcThreads) k_mlp_infer_tc(const float* __rest
   fence_before_sync();
   __syncthreads();
   fence_after_sync();
-  const uint32_t tmem = sm.tmem;
-  const uint32_t lane_base = (32u * (warp & 3u)) << 16;
-  const float b3 = P[OFF_B3];
-  const uint64_t a1d = smem_desc(smem_u32(sm.a1), 128, 256);
+  const uint32_t dcol = sm.tmem + 64u * wg;                // this pipeline's accumulator
+  const uint32_t lane_base = (32u * (warp & 3u)) << 16;    // this warp's TMEM lanes
+  const uint64_t a1d = smem_desc(smem_u32(sm.a1[wg]), 128, 256);
   const uint64_t b1d = smem_desc(smem_u32(sm.b1), 128, 256);
+  const uint64_t b2bd = smem_desc(smem_u32(sm.b2b), 128, 256);
+  const uint64_t b3bd = smem_desc(smem_u32(sm.b3b), 128, 256);
+  const uint32_t a2 = smem_u32(sm.a2[wg]), b2 = smem_u32(sm.b2), b3 = smem_u32(sm.b3);
   uint32_t phase = 0;
   const uint32_t tiles = (rows + kTcRows - 1) / kTcRows;
-  // the next tile's feature row, loaded one tile ahead (warpgroup 0)
+  const uint32_t first = 2u * blockIdx.x + wg, step = 2u * gridDim.x;
+  // the next tile's feature row, loaded one tile ahead
   float4 nf0 = make_float4(0.f, 0.f, 0.f, 0.f), nf1 = nf0;
   auto fetch = [&](uint32_t tile) {
     const uint32_t rr = tile * kTcRows + row;
-    if (wg == 0 && tile < tiles && rr < rows) {
+    if (tile < tiles && rr < rows) {
       nf0 = reinterpret_cast<const float4*>(feat)[2 * (size_t)rr];
       nf1 = reinterpret_cast<const float4*>(feat)[2 * (size_t)rr + 1];
     }
   };
-  fetch(blockIdx.x);
-  for (uint32_t tile = blockIdx.x; tile < tiles; tile += gridDim.x) {
-    if (sm.failed) break;  // uniform: read after the previous tile's barriers
+  fetch(first);
+  for (uint32_t tile = first; tile < tiles; tile += step) {
     const uint32_t r = tile * kTcRows + row;
     const bool valid = r < rows;
     // 1. X row: normalised features in bf16
-    if (wg == 0) {
+    {
       float x[8];
       if (valid) {
         const float f[8] = {nf0.x, nf0.y, nf0.z, nf0.w, nf1.x, nf1.y, nf1.z, nf1.w};
@@ -191,70 +252,77 @@ __global__ void __launch_bounds__(kTcThreads) k_mlp_infer_tc(const float* __rest
 #pragma unroll
         for (int k = 0; k < 8; ++k) x[k] = 0.0f;
       }
-      st_shared_v4(smem_u32(sm.a1 + canon(row, 0, 16)), pack_bf16(x[0], x[1]), pack_bf16(x[2], x[3]),
+      st_shared_v4(smem_u32(sm.a1[wg] + canon(row, 0, 16)), pack_bf16(x[0], x[1]), pack_bf16(x[2], x[3]),
                    pack_bf16(x[4], x[5]), pack_bf16(x[6], x[7]));
     }
-    fetch(tile + gridDim.x);  // in flight while this tile is computed
+    fetch(tile + step);  // in flight while this tile is computed
     fence_async_smem();
     fence_before_sync();
-    __syncthreads();
+    pipe_sync(wg);
     fence_after_sync();
-    // 2. D1 = X W1
-    if (tid == 0 && !sm.failed) {
-      mma_f16(tmem, a1d, b1d, 0u);
+    // a failure flagged before this barrier is seen by every thread of the
+    // pipeline, so they leave together
+    if (*(volatile uint32_t*)&sm.failed[wg]) break;
+    // 2. D = X W1 + b1
+    if (row == 0) {
+      mma_f16(dcol, a1d, b1d, kIdesc64, 0u);
       mma_commit(mbar);
     }
-    if (!mbar_wait(mbar, phase)) atomicOr(&sm.failed, 1u);
+    bool ok = mbar_wait(mbar, phase);
     phase ^= 1u;
     fence_after_sync();
-    // 3. H1 row = bf16(SiLU(D1 + b1)), this warpgroup's 32 columns
-    {
-      float v[32];
-      tmem_ld32(tmem + lane_base + 32u * wg, v);
+    // 3. and 5.: this row of D -> bf16(SiLU(D)) into the H tile, 32 columns at a time
+    auto act = [&]() {
 #pragma unroll
-      for (int kb = 0; kb < 4; ++kb) {
-        uint32_t w[4];
+      for (int half = 0; half < 2; ++half) {
+        float v[32];
+        tmem_ld32(dcol + lane_base + 32u * half, v);
 #pragma unroll
-        for (int e = 0; e < 4; ++e) {
-          const int j = 8 * kb + 2 * e, c = 32 * (int)wg + j;
-          w[e] = pack_bf16(silu_f(v[j] + sm.bias1[c]), silu_f(v[j + 1] + sm.bias1[c + 1]));
+        for (int kb = 0; kb < 4; ++kb) {
+          const int j = 8 * kb;
+          st_shared_v4(a2 + canon(row, 32 * half + 8 * kb, 64), pack_bf16(silu_h(v[j]), silu_h(v[j + 1])),
+                       pack_bf16(silu_h(v[j + 2]), silu_h(v[j + 3])), pack_bf16(silu_h(v[j + 4]), silu_h(v[j + 5])),
+                       pack_bf16(silu_h(v[j + 6]), silu_h(v[j + 7])));
         }
-        st_shared_v4(smem_u32(sm.a2 + canon(row, 32 * wg + 8 * kb, 64)), w[0], w[1], w[2], w[3]);
       }
-    }
-    fence_async_smem();
-    fence_before_sync();
-    __syncthreads();
-    fence_after_sync();
-    // 4. D2 = H1 W2 (four K = 16 steps)
-    if (tid == 0 && !sm.failed) {
+      fence_async_smem();
+      fence_before_sync();
+      pipe_sync(wg);
+      fence_after_sync();
+    };
+    act();
+    // 4. D = H1 W2 + b2 (four K = 16 steps and the bias step), over layer 1's columns
+    if (row == 0) {
 #pragma unroll
-      for (uint32_t ks = 0; ks < 4; ++ks) {
-        mma_f16(tmem + 64u, smem_desc(smem_u32(sm.a2) + 256u * ks, 128, 1024),
-                smem_desc(smem_u32(sm.b2) + 256u * ks, 128, 1024), ks > 0 ? 1u : 0u);
-      }
+      for (uint32_t ks = 0; ks < 4; ++ks)
+        mma_f16(dcol, smem_desc(a2 + 256u * ks, 128, 1024), smem_desc(b2 + 256u * ks, 128, 1024), kIdesc64,
+                ks > 0 ? 1u : 0u);
+      mma_f16(dcol, a1d, b2bd, kIdesc64, 1u);
       mma_commit(mbar);
     }
-    if (!mbar_wait(mbar, phase)) atomicOr(&sm.failed, 1u);
+    ok = mbar_wait(mbar, phase) && ok;
     phase ^= 1u;
     fence_after_sync();
-    // 5. y = w3 . bf16(SiLU(D2 + b2)) + b3: each warpgroup its 32 columns,
-    //    warpgroup 1 hands its half to warpgroup 0
-    float y = wg == 0 ? b3 : 0.0f;
-    {
-      float v[32];
-      tmem_ld32(tmem + lane_base + 64u + 32u * wg, v);
+    act();
+    // 6. y = H2 w3 + b3 (N = 16; columns 0 and 1 hold the hi and lo parts)
+    if (row == 0) {
 #pragma unroll
-      for (int j = 0; j < 32; ++j) {
-        const int c = 32 * (int)wg + j;
-        y = fmaf(bf16_round(silu_f(v[j] + sm.bias2[c])), sm.w3[c], y);
-      }
+      for (uint32_t ks = 0; ks < 4; ++ks)
+        mma_f16(dcol, smem_desc(a2 + 256u * ks, 128, 1024), smem_desc(b3 + 256u * ks, 128, 1024), kIdesc16,
+                ks > 0 ? 1u : 0u);
+      mma_f16(dcol, a1d, b3bd, kIdesc16, 1u);
+      mma_commit(mbar);
     }
-    if (wg == 1) sm.ypart[row] = y;
+    ok = mbar_wait(mbar, phase) && ok;
+    phase ^= 1u;
+    fence_after_sync();
+    if (!ok) atomicOr(&sm.failed[wg], 1u);
+    float y0, y1;
+    tmem_ld2(dcol + lane_base, y0, y1);
+    const float y = y0 + y1;
+    // the next tile's layer 1 overwrites these columns only after this barrier
     fence_before_sync();
-    __syncthreads();
-    if (wg == 0 && valid) {
-      y += sm.ypart[row];
+    if (valid) {
       const float l = y * nm.lam_scale;
       if (xl) {
         const float4 x = xs[r];
@@ -269,16 +337,17 @@ __global__ void __launch_bounds__(kTcThreads) k_mlp_infer_tc(const float* __rest
   __syncthreads();
   fence_after_sync();
   if (warp == 0) {
-    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(kTmemCols) : "memory");
+    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(sm.tmem), "r"(kTmemCols) : "memory");
   }
-  if (tid == 0 && sm.failed && err) atomicOr(err, PBF_DEVERR_MMA_TIMEOUT);
+  if (tid == 0 && (sm.failed[0] | sm.failed[1]) && err) atomicOr(err, PBF_DEVERR_MMA_TIMEOUT);
 }
 
 }  // namespace
 
-// Dynamic shared memory requested on top of the static tile buffers so that
-// at most four CTAs share an SM (4 x 128 TMEM columns = the SM's 512).
-constexpr int kTcPadSmem = 24 * 1024;
+// No dynamic shared memory: the static tile buffers (about 55 KB per CTA) and
+// the 64-register cap of __launch_bounds__(256, 4) each keep an SM at four
+// CTAs, whose 4 x 128 TMEM columns are the SM's 512.
+constexpr int kTcPadSmem = 0;
 
 cudaError_t launch_mlp_infer_tc(const float* d_params, const pbf_mlp& model, const float* d_feat, uint32_t rows,
                                 float* d_lambda, float* d_lam_sum, cudaStream_t st, const float4* d_xs, float4* d_xl,
@@ -297,7 +366,7 @@ cudaError_t launch_mlp_infer_tc(const float* d_params, const pbf_mlp& model, con
       e = cudaFuncSetAttribute(k_mlp_infer_tc, cudaFuncAttributePreferredSharedMemoryCarveout,
                                (int)cudaSharedmemCarveoutMaxShared);
     // four CTAs per SM: the TMEM limit (4 x 128 of 512 columns), which the
-    // padded shared memory also enforces
+    // shared memory and the register cap also enforce
     per_sm = 4;
     if (e != cudaSuccess) {
       sms = 0;
@@ -311,7 +380,8 @@ cudaError_t launch_mlp_infer_tc(const float* d_params, const pbf_mlp& model, con
   }
   nm.lam_scale = model.lam_scale;
   const uint32_t tiles = (rows + kTcRows - 1) / kTcRows;
-  const uint32_t grid = std::min<uint32_t>(tiles, (uint32_t)sms * (uint32_t)per_sm);  // one resident wave
+  // one resident wave, two tile pipelines per CTA
+  const uint32_t grid = std::min<uint32_t>((tiles + 1) / 2, (uint32_t)sms * (uint32_t)per_sm);
   k_mlp_infer_tc<<<grid, kTcThreads, kTcPadSmem, st>>>(d_params, nm, d_feat, rows, d_lambda, d_lam_sum, d_xs, d_xl,
                                                        d_err);
   return cudaGetLastError();

@@ -228,13 +228,15 @@ __global__ void __launch_bounds__(kTcThreads, 4) k_mlp_infer_tc(const float* __r
   uint32_t phase = 0;
   const uint32_t tiles = (rows + kTcRows - 1) / kTcRows;
   const uint32_t first = 2u * blockIdx.x + wg, step = 2u * gridDim.x;
-  // the next tile's feature row, loaded one tile ahead
-  float4 nf0 = make_float4(0.f, 0.f, 0.f, 0.f), nf1 = nf0;
+  // the next tile's feature row (and x* when the output is packed), loaded
+  // one tile ahead
+  float4 nf0 = make_float4(0.f, 0.f, 0.f, 0.f), nf1 = nf0, nx = nf0;
   auto fetch = [&](uint32_t tile) {
     const uint32_t rr = tile * kTcRows + row;
     if (tile < tiles && rr < rows) {
       nf0 = reinterpret_cast<const float4*>(feat)[2 * (size_t)rr];
       nf1 = reinterpret_cast<const float4*>(feat)[2 * (size_t)rr + 1];
+      if (xl) nx = xs[rr];
     }
   };
   fetch(first);
@@ -255,6 +257,7 @@ __global__ void __launch_bounds__(kTcThreads, 4) k_mlp_infer_tc(const float* __r
       st_shared_v4(smem_u32(sm.a1[wg] + canon(row, 0, 16)), pack_bf16(x[0], x[1]), pack_bf16(x[2], x[3]),
                    pack_bf16(x[4], x[5]), pack_bf16(x[6], x[7]));
     }
+    const float4 xr = nx;
     fetch(tile + step);  // in flight while this tile is computed
     fence_async_smem();
     fence_before_sync();
@@ -325,8 +328,7 @@ __global__ void __launch_bounds__(kTcThreads, 4) k_mlp_infer_tc(const float* __r
     if (valid) {
       const float l = y * nm.lam_scale;
       if (xl) {
-        const float4 x = xs[r];
-        xl[r] = make_float4(x.x, x.y, x.z, l);
+        xl[r] = make_float4(xr.x, xr.y, xr.z, l);
       } else {
         lambda[r] = l;
       }

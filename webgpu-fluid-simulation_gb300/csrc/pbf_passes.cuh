@@ -983,13 +983,13 @@ __global__ void __launch_bounds__(256, 4) k_vorticity_split(SimParams p, const f
     for_each_neighbor(nbr_list, b, e, pos, [&](uint32_t j, float4 pj) {
       Pair q = make_pair_of(xi - xyz(pj));
       f3 vd = xyz(__ldg(vel + j)) - vi;
-      const float inv_rj = __frcp_rn(pj.w);
+      const float inv_rj = frcp_fast(pj.w);
       const float volume = p.m * inv_rj;
       f3 gw = spiky_p(p, q);
       om = om + volume * cross3(vd, gw);
       nm = nm + volume * gw;
       vu = vu + (poly6_p(p, q) * inv_rj) * vd;
-      const float kij = p.two_rho0 * __frcp_rn(ri + pj.w);
+      const float kij = p.two_rho0 * frcp_fast(ri + pj.w);
       cs = cs + kij * (p.m * cohesion_p(p, q));
     });
     const float wl = len3(om);
@@ -1020,8 +1020,8 @@ __global__ void __launch_bounds__(256) k_xsph_split(SimParams p, const float4* _
     for_each_neighbor(nbr_list, b, e, pos, [&](uint32_t j, float4 pj) {
       Pair q = make_pair_of(xi - xyz(pj));
       const float4 nj = __ldg(normal + j);  // (normal_j, |omega_j|)
-      eta = eta + (nj.w * __frcp_rn(pj.w)) * spiky_p(p, q);
-      const float kij = p.two_rho0 * __frcp_rn(ri + pj.w);
+      eta = eta + (nj.w * frcp_fast(pj.w)) * spiky_p(p, q);
+      const float kij = p.two_rho0 * frcp_fast(ri + pj.w);
       cv = cv + kij * (ni - xyz(nj));
     });
     const f3 ten = mk(0.f, 0.f, 0.f) - (xyz(coh_sum[t]) + cv);

@@ -1212,8 +1212,9 @@ int oracle_voxelize_mesh(const float* vertices, uint32_t nv, const uint32_t* idx
 // through the projection; the rectangle's framebuffer edges are
 // 0.5 (ndc.x + 1) W and 0.5 (1 - ndc.y) H; pixels whose centres lie in it
 // (left/top edges in) are covered; uv is the centre's position across it.
-// Depth: ties of equal depth keep the lower particle index; the volume sum
-// is exact (integer sum of the terms scaled by 2^40).  Filter texel reads
+// Depth: ties of equal depth keep the lower particle index; the volume term
+// is exp(-2 nx^2) exp(-2 ny^2) and its sum is exact (integer sum of the terms
+// scaled by 2^40).  Filter texel reads
 // clamp to the image edge.  Returns 0, or 1 for a clipped-out camera setup.
 static inline void rnd_mat_vec(const float* m, float x, float y, float z, float w, float o[4]) {
   for (int r = 0; r < 4; ++r) o[r] = ((m[r] * x + m[4 + r] * y) + m[8 + r] * z) + m[12 + r] * w;
@@ -1365,7 +1366,9 @@ int oracle_render(const float* pos, uint32_t n, uint32_t width, uint32_t height,
         for (int i = s.i0; i < s.i1; ++i) {
           const float r2 = rnd_r2(s, i, j);
           if (r2 > 1.0f) continue;
-          acc[(size_t)j * W2 + i] += (uint64_t)((double)rnd_exp(-r2 * 2.0f) * 1099511627776.0);
+          const float nx = std::fmaf((float)i, s.sx, s.ox), ny = std::fmaf((float)j, s.sy, s.oy);
+          const float v = rnd_exp((nx * nx) * -2.0f) * rnd_exp((ny * ny) * -2.0f);
+          acc[(size_t)j * W2 + i] += (uint64_t)((double)v * 1099511627776.0);
         }
   }
   for (size_t p = 0; p < keys.size(); ++p) {

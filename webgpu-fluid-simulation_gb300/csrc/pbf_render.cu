@@ -30,11 +30,12 @@
 // depths cannot beat the pixel's key, which changes nothing in the result.
 //
 // Volume pass: sprites of half-side R on the half-resolution target add
-// exp(-2 |n.xy|^2).  The sum is kept in 64-bit fixed point with 40
-// fraction bits, where every float term in [e^-2, 1] is exact, so the sum
-// is exact and order-free; it is rounded to float once.  The exponential is
-// this file's own (splat_exp), so the CPU restatement can produce the same
-// bits.
+// exp(-2 |n.xy|^2), evaluated as the product exp(-2 nx^2) exp(-2 ny^2) of
+// per-column and per-row factors.  The sum is kept in 64-bit fixed point
+// with 40 fraction bits, where every float term in [2^-3, 2) is exact, so
+// the sum is exact and order-free; it is rounded to float once.  The
+// exponential is this file's own (splat_exp), so the CPU restatement can
+// produce the same bits.
 //
 // The filter is the reference's narrow-range filter, separable, x then y,
 // with its sample window of 32 + 32 texels per 32-texel block: the centre it
@@ -198,7 +199,9 @@ __global__ void k_init(const float* scene, unsigned long long* keys, unsigned lo
 // the warp then walks them one by one with its lanes spread over each
 // sprite's pixels: for sprites up to 32 pixels wide, floor(32 / width) rows
 // per step (lane -> row lane / width by a 16-bit reciprocal, exact for lane
-// and width up to 32), else 32 columns per step.
+// and width up to 32), else 32 columns per step.  Every lane takes part in
+// every step (frag receives whether its pixel is inside the sprite), so the
+// fragment code may use warp-wide votes and shuffles.
 struct SpriteSlot {
   Sprite s[2];   // depth, volume
   uint32_t ok;   // bit 0: depth sprite visible, bit 1: volume sprite visible
@@ -216,20 +219,50 @@ __device__ inline void walk_sprite(const Sprite& s, uint32_t lane, Frag frag) {
     const uint32_t m = c_recip16[w];
     const int rows = (int)((32u * m) >> 16);
     const int lr = (int)((lane * m) >> 16), lc = (int)lane - lr * w;
-    if (lr >= rows) return;
-    for (int j = s.j0 + lr; j < s.j1; j += rows) frag(s.i0 + lc, j);
+    for (int jb = s.j0; jb < s.j1; jb += rows) {
+      const int j = jb + lr;
+      frag(s.i0 + lc, j, lr < rows && j < s.j1);
+    }
   } else {
     for (int j = s.j0; j < s.j1; ++j)
-      for (int i = s.i0 + (int)lane; i < s.i1; i += 32) frag(i, j);
+      for (int ib = s.i0; ib < s.i1; ib += 32) frag(ib + (int)lane, j, ib + (int)lane < s.i1);
   }
+}
+
+// exp(-2 n^2) of a fragment coordinate n: the volume term exp(-2 |n|^2) is
+// the product of the x and y factors.
+__device__ inline float gauss_axis(float n) { return splat_exp((n * n) * -2.0f); }
+
+constexpr int kQueue = 64;  // per-warp queue of depth fragments that pass the bound test
+
+// Depth fragments that may win are queued (pixel, sprite) per warp and
+// evaluated 32 at a time with all lanes busy: the full fragment (square root,
+// division, key, atomicMax) runs only for them.
+__device__ inline void depth_fragments(const Cam& C, const SpriteSlot* slots, const uint32_t* qij, const uint8_t* qk,
+                                       uint32_t count, uint32_t lane, uint32_t base, float R, int W,
+                                       unsigned long long* keys) {
+  if (lane >= count) return;
+  const uint32_t e = qij[lane], k = qk[lane];
+  const int i = (int)(e & 0xffffu), j = (int)(e >> 16);
+  const Sprite& s = slots[k].s[0];
+  const float r2 = sprite_r2(s, i, j);
+  if (r2 > 1.0f) return;
+  float z;
+  const float d = sprite_depth(C, s, r2, R, z);
+  const unsigned long long key = ((unsigned long long)__float_as_uint(d) << 32) | (0xffffffffull - (base + k));
+  unsigned long long* kp = keys + (size_t)j * W + i;
+  if (key > *(volatile unsigned long long*)kp) atomicMax(kp, key);
 }
 
 __global__ void __launch_bounds__(256) k_splat(Cam C, const float4* __restrict__ pos, uint32_t n, float R, int W, int H,
                                                int W2, int H2, unsigned long long* keys, unsigned long long* acc) {
   __shared__ SpriteSlot slots[8][32];
+  __shared__ uint32_t qij[8][kQueue];
+  __shared__ uint8_t qk[8][kQueue];
   const uint32_t lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
   const uint32_t warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
   const uint32_t warps = (gridDim.x * blockDim.x) >> 5;
+  const uint32_t lt = (1u << lane) - 1u;
   for (uint32_t base = warp * 32; base < n; base += warps * 32) {
     const uint32_t q = base + lane;
     SpriteSlot& mine = slots[wib][lane];
@@ -246,34 +279,60 @@ __global__ void __launch_bounds__(256) k_splat(Cam C, const float4* __restrict__
     }
     __syncwarp();
     const uint32_t cnt = min(32u, n - base);
+    uint32_t qn = 0;  // queued depth fragments (warp-uniform)
     for (uint32_t k = 0; k < cnt; ++k) {
       const SpriteSlot& sl = slots[wib][k];
       const uint32_t ok = sl.ok;
       if (ok & 1u) {
         const Sprite s = sl.s[0];
-        const unsigned long long low = 0xffffffffull - (base + k);
-        const unsigned long long bound = ((unsigned long long)s.dmax << 32) | low;
-        walk_sprite(s, lane, [&](int i, int j) {
-          unsigned long long* kp = keys + (size_t)j * W + i;
-          // no fragment of this sprite can beat the pixel's current key
-          if (bound <= *(volatile unsigned long long*)kp) return;
-          const float r2 = sprite_r2(s, i, j);
-          if (r2 > 1.0f) return;
-          float z;
-          const float d = sprite_depth(C, s, r2, R, z);
-          const unsigned long long key = ((unsigned long long)__float_as_uint(d) << 32) | low;
-          if (key > *(volatile unsigned long long*)kp) atomicMax(kp, key);
+        const unsigned long long bound = ((unsigned long long)s.dmax << 32) | (0xffffffffull - (base + k));
+        walk_sprite(s, lane, [&](int i, int j, bool in) {
+          // only fragments whose sprite bound beats the pixel's current key can win
+          const bool pass = in && bound > *(volatile unsigned long long*)(keys + (size_t)j * W + i);
+          const unsigned m = __ballot_sync(0xffffffffu, pass);
+          if (pass) {
+            const uint32_t at = qn + __popc(m & lt);
+            qij[wib][at] = ((uint32_t)j << 16) | (uint32_t)i;
+            qk[wib][at] = (uint8_t)k;
+          }
+          qn += __popc(m);
+          if (qn >= 32) {
+            __syncwarp();
+            depth_fragments(C, slots[wib], qij[wib], qk[wib], 32, lane, base, R, W, keys);
+            __syncwarp();
+            qn -= 32;
+            if (lane < qn) {
+              qij[wib][lane] = qij[wib][32 + lane];
+              qk[wib][lane] = qk[wib][32 + lane];
+            }
+            __syncwarp();
+          }
         });
       }
       if (ok & 2u) {
         const Sprite s = sl.s[1];
-        walk_sprite(s, lane, [&](int i, int j) {
+        // per-lane axis factors: this lane's column (narrow sprites) and row j0 + lane
+        const int w = s.i1 - s.i0, h = s.j1 - s.j0;
+        float ex = 0.0f, ey = 0.0f;
+        if (w <= 32) {
+          const uint32_t m = c_recip16[w];
+          const int lc = (int)lane - (int)((lane * m) >> 16) * w;
+          ex = gauss_axis(__fmaf_rn((float)(s.i0 + lc), s.sx, s.ox));
+        }
+        if (h <= 32) ey = gauss_axis(__fmaf_rn((float)(s.j0 + (int)lane), s.sy, s.oy));
+        walk_sprite(s, lane, [&](int i, int j, bool in) {
+          float fy = __shfl_sync(0xffffffffu, ey, (j - s.j0) & 31);
+          if (!in) return;
           const float r2 = sprite_r2(s, i, j);
           if (r2 > 1.0f) return;
-          atomicAdd(acc + (size_t)j * W2 + i, fix40(splat_exp(-r2 * 2.0f)));
+          if (h > 32) fy = gauss_axis(__fmaf_rn((float)j, s.sy, s.oy));
+          const float fx = w <= 32 ? ex : gauss_axis(__fmaf_rn((float)i, s.sx, s.ox));
+          atomicAdd(acc + (size_t)j * W2 + i, fix40(fx * fy));
         });
       }
     }
+    __syncwarp();
+    depth_fragments(C, slots[wib], qij[wib], qk[wib], qn, lane, base, R, W, keys);
     __syncwarp();
   }
 }

@@ -354,3 +354,45 @@ def test_dam_break_runs_stably():
     x = sim.positions()[:, :3]
     assert (x >= 0).all() and (x <= np.array([3.2, 1.0, 1.6], np.float32)).all()
     sim.close()
+
+
+def test_field_error_report():
+    """Per-field error of one substep against the FP64 replica, for the exact
+    and fast modes beside the FP32 restatement's own (the floor any f32
+    evaluation of the reference formulas sits on); printed as a table
+    (pytest -s) and bounded loosely here (the tight bars are the tests above)."""
+    rows = []
+    for name in SCENES:
+        sc = scenes.reference_scene(name)
+        pts = scenes.jitter(sc.particles, 0.001, seed=9)
+        o64 = O.Oracle(sc.config, 64)
+        o64.set_particles(pts)
+        if sc.field is not None:
+            f = sc.field
+            o64.set_field(f["res"], f["origin"], f["extent"], f["sdf"], f["vol"])
+        o64.substep(1)
+        d = {n: o64.field(f) for f, n in FIELDS}
+        got = {}
+        for mode, label in ((L.FP_EXACT, "exact"), (L.FP_FAST, "fast")):
+            sim, o32 = make_pair(sc, mode, pts, 32)
+            sim.run()
+            got[label] = fields_of(sim)
+            sim.close()
+        o32.substep(1)
+        a = oracle_fields(o32)
+        fields = {"rho": lambda x: x["position"][:, 3], "lambda": lambda x: x["lambda"],
+                  "delta_p": lambda x: x["delta_p"][:, :3], "velocity": lambda x: x["velocity"][:, :3]}
+        for fname, get in fields.items():
+            ref = get(d).astype(np.float64)
+            scale = max(np.abs(ref).max(), 1e-30)
+            rel = lambda x: (np.abs(get(x).astype(np.float64) - ref).max() / scale,
+                             float(np.sqrt(np.mean(np.square(get(x).astype(np.float64) - ref)))) / scale)
+            r32, rex, rfa = rel(a), rel(got["exact"]), rel(got["fast"])
+            rows.append((name, fname, r32, rex, rfa))
+            assert rex == r32                       # exact mode is the FP32 restatement, bit for bit
+            assert rfa[1] <= 3 * r32[1] + 1e-6      # fast mode near the f32 floor
+    print("\n| scene | field | FP32 restatement max / rms | exact mode max / rms | fast mode max / rms |")
+    print("|---|---|---|---|---|")
+    for name, fname, r32, rex, rfa in rows:
+        print("| %s | %s | %.2e / %.2e | %.2e / %.2e | %.2e / %.2e |" % (name, fname, r32[0], r32[1], rex[0], rex[1],
+                                                                     rfa[0], rfa[1]))

@@ -39,3 +39,11 @@ def test_render_reference_arm_line():
     assert d["impl"] == "reference" and d["metric"] == bench.RENDER_METRIC
     assert d["unit"] == "ms" and d["higher_is_better"] is False and d["value"] > 0
     assert d["cpu_baseline"]["kind"] == "port"
+
+
+def test_voxelize_reference_arm_line():
+    import bench
+    d = _run("--impl", "reference", "--workload", "voxelize_mesh", "--steps", "1", "--warmup", "0")
+    assert d["impl"] == "reference" and d["metric"] == bench.VOXEL_METRIC
+    assert d["unit"] == "ms" and d["higher_is_better"] is False and d["value"] > 0
+    assert d["config"]["points"] > 10000

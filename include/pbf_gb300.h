@@ -418,10 +418,12 @@ int pbf_exclusive_scan_u32_noalloc(const uint32_t* d_in, uint32_t* d_out, size_t
  * passes use a fixed workgroup size of 256).  The step's passes are
  * grid-stride loops over tiles of `block` slots: ctas_per_sm = 0 launches one
  * tile per CTA; k > 0 launches at most k CTAs per SM that loop over the
- * tiles.  cell_ratio is the hash-grid cell edge over the kernel radius: 1 is
- * the reference's grid (27-cell search, neighbour order and results as the
- * reference); 0.5 uses h/2 cells and a 125-cell search (the same neighbour
- * sets, summed in a different order, so results differ in rounding). */
+ * tiles.  cell_ratio is the hash-grid cell height (z) over the kernel
+ * radius: 1 is the reference's grid (h cells, 27-cell search, neighbour order
+ * and results as the reference); 0.5 keeps h in x and y and halves the cells
+ * in z, searched as 3 x 3 columns of 5 half cells (2.5 h instead of 3 h of
+ * candidates per column; the same neighbour sets, summed in a different
+ * order, so results differ in rounding). */
 typedef struct pbf_launch {
   uint32_t block;        /* threads per CTA: 128 or 256 (default 256) */
   uint32_t ctas_per_sm;  /* 0 (default) or 1..16 */

@@ -171,9 +171,11 @@ int fail(pbf_handle* h, int code, const char* fmt, ...) {
 
 // Hash grid over [dmin, dmax].  Cell ratio 1 keeps the reference's grid: the
 // given dims, else ceil(extent / h) cells per axis, searched over 27 cells.
-// Other ratios (and every batched scene: floor_dims) use floor(extent /
-// (ratio h)) cells, so no cell is smaller than ratio h and a search of
-// +-ceil(1/ratio) cells covers the kernel radius.
+// Other ratios (and every batched scene: floor_dims) use floor(extent / h)
+// cells in x and y and floor(extent / (ratio h)) in z, so no cell is smaller
+// than h across and ratio h high; a search of +-1 cells in x and y and
+// +-ceil(1/ratio) in z covers the kernel radius.  Keys are z-fastest, so the
+// finer z only lengthens the 9 runs (5 half cells, 2.5 h, instead of 3 h).
 GridParams make_grid(const float dmin[3], const float dmax[3], float hk, float ratio, const uint32_t fixed_dim[3],
                      bool floor_dims) {
   GridParams g{};
@@ -186,7 +188,8 @@ GridParams make_grid(const float dmin[3], const float dmax[3], float hk, float r
       if (ref) {
         d = (int)std::ceil(ext / (double)hk);
       } else {
-        d = (int)std::floor(ext / ((double)ratio * (double)hk));
+        // x and y cells of at least h; z cells of at least ratio h
+        d = (int)std::floor(ext / ((a == 2 ? (double)ratio : 1.0) * (double)hk));
         if (d < 1) d = 1;
       }
     }
@@ -197,7 +200,8 @@ GridParams make_grid(const float dmin[3], const float dmax[3], float hk, float r
   }
   g.cells = cells > 0xfffffffeull ? 0u : (uint32_t)cells;
   g.key_base = 0;
-  g.reach = ratio == 1.0f ? 1 : (int)std::ceil(1.0 / (double)ratio - 1e-9);
+  g.reach = 1;
+  g.reach_z = ratio == 1.0f ? 1 : (int)std::ceil(1.0 / (double)ratio - 1e-9);
   return g;
 }
 
@@ -1972,6 +1976,7 @@ int pbf_ns_create(const pbf_grid* grid, uint32_t max_particles, void* stream, pb
   s->g.cells = (uint32_t)cells;
   s->g.key_base = 0;
   s->g.reach = 1;
+  s->g.reach_z = 1;
   s->max_n = max_particles;
   cudaError_t e = cudaSuccess;
   if (stream) {

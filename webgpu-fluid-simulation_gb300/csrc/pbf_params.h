@@ -12,7 +12,8 @@ struct GridParams {
   int dim[3];
   uint32_t cells;     // dim[0] * dim[1] * dim[2]
   uint32_t key_base;  // first key of this grid in a shared key space (batched scenes; 0 otherwise)
-  int reach;          // neighbourhood half-width in cells (1: the 27-cell search; 2 when cells are h/2)
+  int reach;          // neighbourhood half-width in cells along x and y
+  int reach_z;        // ... along z (1: the 27-cell search; 2 when z cells are h/2)
 };
 
 struct FieldParams {

@@ -111,9 +111,9 @@ __global__ void __launch_bounds__(256) k_predict(SimParams p0, GridParams g0, Sc
   }
 }
 
-// Range of slots covering cells (cx+dx, cy+dy, cz-R .. cz+R), R = g.reach:
-// the (2R+1)^3-cell neighbourhood is (2R+1)^2 runs of consecutive keys
-// because keys are z-fastest (R = 1: the reference's 27 cells as 9 runs).
+// Range of slots covering cells (cx+dx, cy+dy, cz-Z .. cz+Z), Z = g.reach_z:
+// the neighbourhood is (2 g.reach + 1)^2 runs of consecutive keys because
+// keys are z-fastest (reach 1, Z = 1: the reference's 27 cells as 9 runs).
 struct Run {
   uint32_t b, e;
 };
@@ -121,7 +121,7 @@ __device__ __forceinline__ Run run_of(const GridParams& g, const uint32_t* __res
                                       int cz, int dx, int dy) {
   int x = cx + dx, y = cy + dy;
   if (x < 0 || y < 0 || x >= g.dim[0] || y >= g.dim[1]) return Run{0, 0};
-  int zlo = max(cz - g.reach, 0), zhi = min(cz + g.reach, g.dim[2] - 1);
+  int zlo = max(cz - g.reach_z, 0), zhi = min(cz + g.reach_z, g.dim[2] - 1);
   uint32_t k0 = cell_key(x, y, zlo, g), k1 = cell_key(x, y, zhi, g) + 1u;
   return Run{__ldg(cell_start + k0), __ldg(cell_start + k1)};
 }
@@ -417,6 +417,7 @@ __global__ void __launch_bounds__(256) k_nbr_build_warp(SimParams p, GridParams 
         gl.dim[2] = __shfl_sync(kFull, g.dim[2], leader);
         gl.key_base = __shfl_sync(kFull, g.key_base, leader);
         gl.reach = __shfl_sync(kFull, g.reach, leader);
+        gl.reach_z = __shfl_sync(kFull, g.reach_z, leader);
       }
       for (int dx = -gl.reach; dx <= gl.reach; ++dx)
         for (int dy = -gl.reach; dy <= gl.reach; ++dy) {

@@ -331,6 +331,13 @@ const char* pbf_ns_last_error(const pbf_ns* ns);
  * single-pass decoupled look-back over any length (no 512-multiple or
  * 262144 limit).  Scratch is owned by the call's context. */
 int pbf_exclusive_scan_u32(const uint32_t* d_in, uint32_t* d_out, size_t n, void* stream);
+/* Self-test of the bounded device waits (no counterpart in the reference):
+ * runs a scan tile whose look-back waits on a predecessor that never
+ * publishes; the wait gives up after its poll limit and the kernel
+ * completes.  Returns PBF_ETIMEOUT when the give-up was reported as it
+ * should be (the expected result), another status otherwise.  Takes a few
+ * hundred milliseconds. */
+int pbf_selftest_bounded_wait(void);
 
 /* ---- learned lambda warm start.  No counterpart in the reference (its solve
  * is a fixed number of plain iterations, PBF.ts:417-431): an MLP

@@ -396,3 +396,21 @@ def test_field_error_report():
     for name, fname, r32, rex, rfa in rows:
         print("| %s | %s | %.2e / %.2e | %.2e / %.2e | %.2e / %.2e |" % (name, fname, r32[0], r32[1], rex[0], rex[1],
                                                                      rfa[0], rfa[1]))
+
+
+def test_bounded_wait_gives_up_and_reports():
+    """A scan tile whose predecessor never publishes: the look-back wait runs
+    out, flags PBF_DEVERR_SCAN_TIMEOUT and the kernel completes; the context
+    stays usable (a normal scan afterwards is exact)."""
+    import time
+    t0 = time.perf_counter()
+    assert L.load().pbf_selftest_bounded_wait() == L.PBF_ETIMEOUT
+    assert time.perf_counter() - t0 < 30.0
+    import torch
+    from pbf_gb300.simulator import exclusive_scan
+    x = (np.arange(100000, dtype=np.int64) % 7).astype(np.int32)
+    d_in = torch.from_numpy(x).cuda()
+    d_out = torch.empty_like(d_in)
+    exclusive_scan(d_in.data_ptr(), d_out.data_ptr(), x.size)
+    torch.cuda.synchronize()
+    assert np.array_equal(d_out.cpu().numpy(), np.concatenate([[0], np.cumsum(x)[:-1]]).astype(np.int32))

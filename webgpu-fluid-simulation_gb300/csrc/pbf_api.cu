@@ -2126,6 +2126,18 @@ int pbf_ns_sync(pbf_ns* s) {
   return PBF_OK;
 }
 
+int pbf_selftest_bounded_wait(void) {
+  uint32_t* err = nullptr;
+  if (cudaMalloc(&err, sizeof(uint32_t)) != cudaSuccess) return PBF_ECUDA;
+  uint32_t e = 0;
+  cudaError_t ce = cudaMemset(err, 0, sizeof(uint32_t));
+  if (ce == cudaSuccess) ce = launch_scan_timeout_selftest(err, 0);
+  if (ce == cudaSuccess) ce = cudaMemcpy(&e, err, sizeof(uint32_t), cudaMemcpyDeviceToHost);
+  cudaFree(err);
+  if (ce != cudaSuccess) return PBF_ECUDA;
+  return (e & PBF_DEVERR_SCAN_TIMEOUT) ? PBF_ETIMEOUT : PBF_EINVAL;
+}
+
 int pbf_exclusive_scan_u32(const uint32_t* d_in, uint32_t* d_out, size_t n, void* stream) {
   if ((!d_in || !d_out) && n) return PBF_EINVAL;
   if (n == 0) return PBF_OK;

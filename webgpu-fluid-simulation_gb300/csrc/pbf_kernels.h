@@ -74,6 +74,9 @@ size_t scan_scratch_bytes(size_t n);
 // bounded look-back wait gives up.
 cudaError_t launch_exclusive_scan(const uint32_t* in, uint32_t* out, size_t n, void* scratch, uint32_t* err,
                                   cudaStream_t st);
+// Self-test of the scan's bounded look-back wait (a predecessor status that
+// nothing writes): *err receives PBF_DEVERR_SCAN_TIMEOUT.
+cudaError_t launch_scan_timeout_selftest(uint32_t* err, cudaStream_t st);
 
 // Counting-sort pipeline shared by the step and the stand-alone search.
 struct SortBuffers {

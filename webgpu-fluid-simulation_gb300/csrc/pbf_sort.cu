@@ -450,6 +450,38 @@ cudaError_t launch_exclusive_scan(const uint32_t* in, uint32_t* out, size_t n, v
   return cudaGetLastError();
 }
 
+// Self-test of the look-back's bounded wait: one CTA of a two-tile scan,
+// started as tile 1 (the tile counter is preset), so tile 0's status word,
+// which nothing writes, is what it waits for.  The wait gives up after
+// kSpinLimit polls, flags PBF_DEVERR_SCAN_TIMEOUT in *err and the kernel
+// completes.  Every access stays inside the two tiles' buffers.
+cudaError_t launch_scan_timeout_selftest(uint32_t* err, cudaStream_t st) {
+  const size_t n = 2 * (size_t)kScanTile;
+  uint32_t *in = nullptr, *out = nullptr;
+  void* scratch = nullptr;
+  cudaError_t e = cudaMallocAsync(&in, n * sizeof(uint32_t), st);
+  if (e == cudaSuccess) e = cudaMallocAsync(&out, n * sizeof(uint32_t), st);
+  if (e == cudaSuccess) e = cudaMallocAsync(&scratch, scan_scratch_bytes(n), st);
+  if (e == cudaSuccess) e = cudaMemsetAsync(in, 0, n * sizeof(uint32_t), st);
+  if (e == cudaSuccess) e = cudaMemsetAsync(scratch, 0, scan_scratch_bytes(n), st);
+  const uint32_t one = 1u;
+  uint32_t* counter = reinterpret_cast<uint32_t*>(scratch);
+  if (e == cudaSuccess) e = cudaMemcpyAsync(counter, &one, sizeof(one), cudaMemcpyHostToDevice, st);
+  unsigned long long* status = reinterpret_cast<unsigned long long*>(reinterpret_cast<char*>(scratch) + 256);
+  if (e == cudaSuccess) {
+    k_scan<<<1, kScanThreads, 0, st>>>(in, out, n, status, counter, err);
+    e = cudaGetLastError();
+  }
+  // the host value copied above must outlive the copy
+  cudaError_t e2 = cudaStreamSynchronize(st);
+  if (e == cudaSuccess) e = e2;
+  cudaFreeAsync(in, st);
+  cudaFreeAsync(out, st);
+  cudaFreeAsync(scratch, st);
+  e2 = cudaStreamSynchronize(st);
+  return e == cudaSuccess ? e2 : e;
+}
+
 cudaError_t launch_insert(GridParams g, const float4* pos, uint32_t n, uint32_t* key, uint32_t* rank,
                           uint32_t* cell_count, cudaStream_t st) {
   if (n == 0) return cudaSuccess;

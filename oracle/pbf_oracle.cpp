@@ -2,7 +2,7 @@
 //
 // TEST INFRASTRUCTURE ONLY.  Nothing in the product library links or calls
 // this file; only tests/, __graft_entry__.smoke() and bench.py's CPU baseline
-// load it, as the checker.
+// load it, to check the GPU results or to time the method on the host.
 //
 // It restates, pass by pass, the WGSL of WebGPU-Fluid-Simulation in the
 // order PBF.run encodes them (src/simulator/PBF/PBF.ts:398-448), on the

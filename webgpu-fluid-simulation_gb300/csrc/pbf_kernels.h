@@ -149,7 +149,6 @@ cudaError_t launch_mlp_infer_tc(const float* d_params, const pbf_mlp& model, con
 cudaError_t launch_mlp_grad(const float* d_params, const pbf_mlp& model, const float* d_feat, const float* d_target,
                             uint32_t rows, float* d_grad, float* d_loss, cudaStream_t st);
 cudaError_t launch_gather_f32(uint32_t n, const uint32_t* perm, const float* src, float* dst, cudaStream_t st);
-cudaError_t launch_copy_guarded(uint32_t n, const int* guard, const float4* src, float4* dst, cudaStream_t st);
 cudaError_t launch_fallback_decide(SolveStats* stats, float bound, int* flag, uint32_t* fallbacks, float* last_mean,
                                    cudaStream_t st);
 cudaError_t launch_stats_record(SolveStats* stats, float* rec, cudaStream_t st);

@@ -340,12 +340,6 @@ __global__ void k_gather_f32(uint32_t n, const uint32_t* __restrict__ perm, cons
   if (t < n) dst[t] = src[perm[t]];
 }
 
-__global__ void k_copy_guarded(uint32_t n, const int* __restrict__ guard, const float4* __restrict__ src,
-                               float4* __restrict__ dst) {
-  if (guard && *guard == 0) return;
-  for (uint32_t t = blockIdx.x * blockDim.x + threadIdx.x; t < n; t += gridDim.x * blockDim.x) dst[t] = src[t];
-}
-
 // Fallback decision from the last learned iteration's statistics; resets
 // them for the next substep.
 __global__ void k_fallback_decide(SolveStats* stats, float bound, int* flag, uint32_t* fallbacks, float* last_mean) {
@@ -401,12 +395,6 @@ __global__ void k_trace_append(uint32_t n, const uint32_t* __restrict__ ids, con
 cudaError_t launch_gather_f32(uint32_t n, const uint32_t* perm, const float* src, float* dst, cudaStream_t st) {
   if (n == 0) return cudaSuccess;
   k_gather_f32<<<(n + 255) / 256, 256, 0, st>>>(n, perm, src, dst);
-  return cudaGetLastError();
-}
-cudaError_t launch_copy_guarded(uint32_t n, const int* guard, const float4* src, float4* dst, cudaStream_t st) {
-  if (n == 0) return cudaSuccess;
-  // one wave of CTAs (grid-stride): an unset guard costs one short wave
-  k_copy_guarded<<<std::min((n + 255) / 256, 1216u), 256, 0, st>>>(n, guard, src, dst);
   return cudaGetLastError();
 }
 cudaError_t launch_fallback_decide(SolveStats* stats, float bound, int* flag, uint32_t* fallbacks, float* last_mean,

@@ -3,7 +3,7 @@
 // Some callers cannot allocate device memory at the moment they need a
 // prefix sum: a host framework that owns every device byte through its own
 // pool and forbids other allocators, a real-time frame loop that must not
-// enter the driver's allocator, or code that runs while a stream is being
+// enter the CUDA allocator, or code that runs while a stream is being
 // captured.  pbf_exclusive_scan_u32_noalloc serves them: the caller passes
 // the input and output arrays and the scan's look-back scratch lives in the
 // fixed file-scope device array below, which every GPU that loads this

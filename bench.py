@@ -12,8 +12,9 @@ confinement and Akinci surface tension on; 2 substeps of 1/120 s per step,
            eager launches), max over ranks (N replicas for --gpus N).
   e2e    — the same metric through the public C ABI as a host program uses
            it: per step pbf_set_options (the 20-byte SimulationOptions from
-           host memory) + pbf_step + pbf_copy_field(POSITION) into a host
-           array (N * 16 bytes), wall clock.
+           host memory) + pbf_step + pbf_copy_positions_async into a pinned
+           host array (N * 16 bytes, queued behind the frame), then one
+           pbf_synchronize; wall clock.
   roofline — the pass with the largest share of device time, its
            algorithmic bytes per launch over its average launch duration.
   cpu_baseline — the CPU restatement (oracle/) on a bounded sample.
@@ -581,7 +582,8 @@ def _e2e_path(args, sc, snap, dist, model, learned_iters, bound):
     for _ in range(args.steps):
         lib.pbf_set_options(sim._h, ctypes.byref(opts))
         sim.step(1)
-        lib.pbf_copy_field(sim._h, L.FIELD_POSITION, host.ctypes.data_as(ctypes.c_void_p), host.nbytes)
+        lib.pbf_copy_positions_async(sim._h, host.ctypes.data_as(ctypes.POINTER(ctypes.c_float)), host.nbytes)
+    sim.synchronize()  # every frame's positions are in host memory
     e2e_s = dist.max(time.perf_counter() - t0)
     sim.close()
     return {"value": dist.world * n * sub * args.steps / e2e_s, "unit": UNIT,
@@ -694,7 +696,8 @@ def batch_arm(args, dist):
     for _ in range(args.steps):
         lib.pbf_set_options(b._h, ctypes.byref(opts))
         b.step(1)
-        lib.pbf_copy_field(b._h, L.FIELD_POSITION, host.ctypes.data_as(ctypes.c_void_p), host.nbytes)
+        lib.pbf_copy_positions_async(b._h, host.ctypes.data_as(ctypes.POINTER(ctypes.c_float)), host.nbytes)
+    b.synchronize()
     e2e_s = dist.max(time.perf_counter() - t0)
     per_scene = {mine[s]: b.scene_metrics(s) for s in range(len(mine))}
     merged = gather_scene_results(per_scene, dist.pg)

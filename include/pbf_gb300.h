@@ -293,6 +293,13 @@ uint32_t pbf_particle_count(const pbf_handle* h);
 const float* pbf_position_device(pbf_handle* h);
 const float* pbf_velocity_device(pbf_handle* h);
 int pbf_copy_field(pbf_handle* h, int field, void* host, size_t bytes);
+/* The positions of the last frame (x, y, z, density by particle id, the
+ * buffer pbf_position_device exposes) copied to host memory asynchronously:
+ * a device-side copy after the frame, then the host copy on a second stream,
+ * so the host read overlaps the next frames and the call returns at once.
+ * host: n float4 (16 n bytes), ideally pinned; it is complete after
+ * pbf_synchronize, and must stay valid until then. */
+int pbf_copy_positions_async(pbf_handle* h, float* host, size_t bytes);
 int pbf_get_metrics(pbf_handle* h, pbf_metrics* out);
 /* Keep per-iteration debug fields (PBF_FIELD_DELTA_P); off by default. */
 int pbf_set_capture(pbf_handle* h, int enable);

@@ -414,3 +414,24 @@ def test_bounded_wait_gives_up_and_reports():
     exclusive_scan(d_in.data_ptr(), d_out.data_ptr(), x.size)
     torch.cuda.synchronize()
     assert np.array_equal(d_out.cpu().numpy(), np.concatenate([[0], np.cumsum(x)[:-1]]).astype(np.int32))
+
+
+def test_async_position_copy_matches_copy_field():
+    import ctypes
+    import torch
+    sc = scenes.reference_scene("cube_small")
+    sim = PBF(sc.config)
+    try:
+        sim.set_particles(sc.particles)
+        sim.enable_graph(True)
+        host = torch.empty((sc.n, 4), dtype=torch.float32, pin_memory=True)
+        for _ in range(3):
+            sim.step(1)
+            assert L.load().pbf_copy_positions_async(sim._h, ctypes.cast(host.data_ptr(), ctypes.POINTER(
+                ctypes.c_float)), host.numel() * 4) == L.PBF_OK
+        sim.synchronize()
+        assert np.array_equal(host.numpy(), sim.positions())
+        assert L.load().pbf_copy_positions_async(sim._h, ctypes.cast(host.data_ptr(), ctypes.POINTER(
+            ctypes.c_float)), 16) == L.PBF_EINVAL
+    finally:
+        sim.close()

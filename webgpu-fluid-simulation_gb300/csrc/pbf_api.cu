@@ -51,6 +51,10 @@ struct pbf_handle {
   PassTable passes;
   cudaStream_t stream = nullptr;
   bool own_stream = false;
+  // asynchronous position reads: their stream, events and the staging copy
+  cudaStream_t copy_stream = nullptr;
+  cudaEvent_t ev_frame = nullptr, ev_staged = nullptr;
+  DBuf<float4> staging;
   std::string err;
   uint32_t n = 0;
   bool paused = false;
@@ -1003,6 +1007,13 @@ int pbf_create(const pbf_config* cfg, pbf_handle** out) {
 int pbf_destroy(pbf_handle* h) {
   if (!h) return PBF_EINVAL;
   cudaStreamSynchronize(h->stream);
+  if (h->copy_stream) {
+    cudaStreamSynchronize(h->copy_stream);
+    cudaStreamDestroy(h->copy_stream);
+    cudaEventDestroy(h->ev_frame);
+    cudaEventDestroy(h->ev_staged);
+  }
+  h->staging.release();
   release_all(h);
   for (int i = 0; i < 5; ++i)
     if (h->ev[i]) cudaEventDestroy(h->ev[i]);
@@ -1393,6 +1404,7 @@ int pbf_run_timestamp(pbf_handle* h, float ms[4]) {
 int pbf_synchronize(pbf_handle* h) {
   if (!h) return PBF_EINVAL;
   CU(h, cudaStreamSynchronize(h->stream));
+  if (h->copy_stream) CU(h, cudaStreamSynchronize(h->copy_stream));
   return check_device_errors(h);
 }
 
@@ -1559,6 +1571,36 @@ const float* pbf_velocity_device(pbf_handle* h) {
   return (const float*)h->out_tmp.p;
 }
 void* pbf_stream(pbf_handle* h) { return h ? (void*)h->stream : nullptr; }
+
+// The frame's by-id positions are copied device to device into a staging
+// buffer on a second stream, then from there to the host on that stream, so
+// the host read overlaps the next frames.  The handle's stream waits only
+// for the device-to-device copy (a few microseconds) before its next work,
+// so the next frame's export cannot overwrite positions still being staged;
+// the staging buffer itself is reused in order on the copy stream.
+int pbf_copy_positions_async(pbf_handle* h, float* host, size_t bytes) {
+  if (!h || (!host && bytes)) return PBF_EINVAL;
+  if (bytes != (size_t)h->n * sizeof(float4))
+    return fail(h, PBF_EINVAL, "positions need %zu bytes, got %zu", (size_t)h->n * sizeof(float4), bytes);
+  if (bytes == 0) return PBF_OK;
+  if (!h->copy_stream) {
+    CU(h, cudaStreamCreateWithFlags(&h->copy_stream, cudaStreamNonBlocking));
+    CU(h, cudaEventCreateWithFlags(&h->ev_frame, cudaEventDisableTiming));
+    CU(h, cudaEventCreateWithFlags(&h->ev_staged, cudaEventDisableTiming));
+  }
+  if (h->staging.n < h->n) {
+    CU(h, cudaStreamSynchronize(h->copy_stream));
+    h->staging.release();
+    CU(h, h->staging.alloc(std::max<size_t>(h->cfg.max_particles, h->n)));
+  }
+  CU(h, cudaEventRecord(h->ev_frame, h->stream));
+  CU(h, cudaStreamWaitEvent(h->copy_stream, h->ev_frame, 0));
+  CU(h, cudaMemcpyAsync(h->staging.p, h->out_pos.p, bytes, cudaMemcpyDeviceToDevice, h->copy_stream));
+  CU(h, cudaEventRecord(h->ev_staged, h->copy_stream));
+  CU(h, cudaMemcpyAsync(host, h->staging.p, bytes, cudaMemcpyDeviceToHost, h->copy_stream));
+  CU(h, cudaStreamWaitEvent(h->stream, h->ev_staged, 0));
+  return PBF_OK;
+}
 
 int pbf_copy_field(pbf_handle* h, int field, void* host, size_t bytes) {
   if (!h || (!host && bytes)) return PBF_EINVAL;

@@ -142,6 +142,7 @@ SIGNATURES = {
     "pbf_voxelize_mesh_points": (ctypes.c_int, [_FP, u32, _UP, u32, _DP, ctypes.c_double, _FP, u32, _UP]),
     "pbf_seed_device": (ctypes.c_int, [_P, ctypes.POINTER(SeedItem), u32, f32, ctypes.c_uint64, _UP]),
     "pbf_selftest_bounded_wait": (ctypes.c_int, []),
+    "pbf_copy_positions_async": (ctypes.c_int, [_P, _FP, ctypes.c_size_t]),
     "pbf_renderer_create": (ctypes.c_int, [u32, u32, ctypes.POINTER(_P)]),
     "pbf_renderer_destroy": (ctypes.c_int, [_P]),
     "pbf_renderer_set_config": (ctypes.c_int, [_P, ctypes.POINTER(RenderOptions)]),

@@ -134,3 +134,20 @@ def test_empty_and_errors():
             r.set_camera(bad)
     finally:
         r.close()
+
+
+@pytest.mark.parametrize("R", [0.2, 0.6])
+def test_large_sprites_match_oracle(R):
+    """Sprites wider and taller than 32 pixels (the column-stepped walk, the
+    per-fragment row factor) and particles close to the camera."""
+    W, H = 400, 300
+    rng = np.random.default_rng(21)
+    p = np.zeros((1500, 4), np.float32)
+    p[:, :3] = rng.uniform(-0.6, 0.6, (1500, 3))
+    p[:40, :3] = np.array([1.6, 1.6, 0.0]) + rng.uniform(-0.1, 0.1, (40, 3))   # near the eye at (2, 2, 0)
+    cam = Rd.reference_camera(W, H)
+    got = _render_gpu(p, W, H, 32, R=R, cam=cam)
+    want = O.render(p, W, H, cam["view"], cam["projection"], R, 32)
+    assert np.count_nonzero(want[0]) > 5000
+    _same(got[0], want[0])
+    _same(got[1], want[1])

@@ -82,10 +82,14 @@ def parse_args():
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--workload", default="sphere_drop_1m",
-                    choices=["sphere_drop_1m", "dam_break_16k", "batch64", "render_1m_1080p", "voxelize_mesh"],
+                    choices=["sphere_drop_1m", "dam_break_16k", "batch64", "render_1m_1080p", "voxelize_mesh",
+                             "neighbor_search_16m"],
                     help="batch64: 64 independent scenes in one batch handle (its own JSON line; the scenes are "
                          "split over the ranks)")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--ns-log2", type=int, default=24,
+                    help="neighbor_search_16m: log2 of the points per input (24 = the workload; smaller for "
+                         "profiling captures)")
     ap.add_argument("--no-graph", dest="graph", action="store_false",
                     help="launch the passes eagerly instead of replaying each frame as a CUDA graph")
     ap.add_argument("--settle", type=int, default=150,
@@ -935,12 +939,189 @@ def voxel_arm(args, dist):
         print(json.dumps(line), flush=True)
 
 
+# ---- stand-alone neighbour search: NeighborSearch.execute ----------------------------------------
+NS_METRIC = "particles/s, stand-alone neighbour search (cell keys, counts, offsets, stable order, ranks)"
+NS_N = 1 << 24
+NS_DESC = ("neighbor_search_16m: 2^24 float4 points in the unit cube on a 128^3-cell grid (2,097,152 cells), "
+           "two inputs per step: uniform, and 64 Gaussian clumps (sigma = 2 cells, seed 13)")
+# Algorithmic bytes of each phase of pbf_ns_run: (per particle, per cell).
+NS_ALG = {
+    "keys": (20, 0),           # read x (16); write the cell key (4)
+    "sort_passes": (56, 0),    # 3 radix passes: count digits (read key 4) + move (key, id) records (read 8, write 8);
+                               # the first pass reads no ids: 3 * 20 - 4
+    "cell_offsets": (4, 12),   # read the sorted keys; clear counts, scan counts into offsets
+    "outputs": (20, 16),       # ranks: read sorted key + order, write rank; copy order; copy counts + offsets
+}
+
+
+def _ns_inputs(n):
+    from pbf_gb300 import scenes
+    from oracle import oracle as O
+    out = []
+    for dist_name in ("uniform", "clumps"):
+        cfg, pts = scenes.neighbor_case(n, dist_name, seed=13, dim=128)
+        dims, cells = O.grid_dims(cfg)
+        inv = [float(np.float32(float(dims[a]) / (cfg.domain_max[a] - cfg.domain_min[a]))) for a in range(3)]
+        out.append((dist_name, cfg, pts, list(cfg.domain_min), inv, list(dims), cells))
+    return out
+
+
+def _ns_cpu(inputs, sample, min_seconds):
+    """The CPU restatement's search (serial) on the first `sample` points of
+    each input, repeated until min_seconds; returns (particles/s, seconds)."""
+    from oracle import oracle as O
+    done, t0 = 0, time.perf_counter()
+    while True:
+        for _, cfg, pts, *_ in inputs:
+            O.neighbor_search(cfg, pts[:sample])
+            done += sample
+        dt = time.perf_counter() - t0
+        if dt >= min_seconds:
+            return done / dt, dt
+
+
+def ns_arm(args, dist):
+    """pbf_ns_run over 2^24 points, uniform and clumped, per step.  value:
+    device time (CUDA events on the search's stream), inputs resident in HBM
+    (256 MB each, larger than L2); e2e: positions from pinned host memory,
+    the search, keys/order/ranks/counts/offsets back, wall clock."""
+    n = 1 << args.ns_log2 if args.ns_log2 != 24 else NS_N
+    if args.impl == "reference":
+        if dist.rank != 0:
+            return
+        sample = 1 << 20
+        inputs = _ns_inputs(sample)
+        rate, dt = _ns_cpu(inputs, sample, min_seconds=10.0)
+        line = {"impl": "reference", "metric": NS_METRIC, "value": rate, "unit": "particles/s", "n_gpus": args.gpus,
+                "steps": args.steps, "warmup": 0, "ms_per_step": 2 * n / rate * 1000.0, "higher_is_better": True,
+                "scaling": "weak", "vs_baseline": None, "dtype": "u32", "data": "synthetic",
+                "config": {"workload": NS_DESC},
+                "cpu_baseline": {"value": rate, "unit": "particles/s", "cores": 1, "kind": "port",
+                                 "sample": "2^20 points of each input (same grid), %.1f s" % dt},
+                "e2e": {"value": rate, "unit": "particles/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+                "note": "the reference searches with WGSL compute shaders (no runtime here); its method runs as the "
+                        "project's CPU restatement (serial counting sort)"}
+        print(json.dumps(line), flush=True)
+        return
+    import torch
+    from pbf_gb300.simulator import NeighborSearch
+    torch.cuda.set_device(dist.local if dist.world > 1 else 0)
+    inputs = _ns_inputs(n)
+    stream = torch.cuda.Stream()
+    cells = inputs[0][6]
+    searches, dev = [], []
+    for name, cfg, pts, origin, inv, dims, _ in inputs:
+        searches.append(NeighborSearch(origin, inv, dims, n, stream=stream.cuda_stream))
+        dev.append(torch.from_numpy(pts).cuda())
+    keys = torch.empty(n, dtype=torch.int32, device="cuda")
+    order = torch.empty(n, dtype=torch.int32, device="cuda")
+    rank = torch.empty(n, dtype=torch.int32, device="cuda")
+    cc = torch.empty(cells, dtype=torch.int32, device="cuda")
+    co = torch.empty(cells + 1, dtype=torch.int32, device="cuda")
+    torch.cuda.synchronize()
+
+    def run(i):
+        searches[i].run(dev[i].data_ptr(), n, keys.data_ptr(), cc.data_ptr(), co.data_ptr(), order.data_ptr(),
+                        rank.data_ptr())
+
+    for _ in range(max(args.warmup, 3)):
+        run(0)
+        run(1)
+    stream.synchronize()
+    clocks = ClockSampler(dist.local)
+    clocks.start()
+    dist.barrier()
+    torch.cuda.synchronize()
+    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    ev0.record(stream)
+    for _ in range(args.steps):
+        run(0)
+        run(1)
+    ev1.record(stream)
+    ev1.synchronize()
+    torch.cuda.synchronize()
+    dist.barrier()
+    clk = clocks.stop()
+    ms_step = dist.max(ev0.elapsed_time(ev1) / args.steps)
+    value = dist.world * 2 * n / (ms_step / 1000.0)
+    for s in searches:
+        s.sync()
+    # phases of one search per input, over a few runs
+    phases = {k: [] for k in NS_ALG}
+    per_input = {}
+    for i, s in enumerate(searches):
+        s.set_timing(True)
+        acc = []
+        for _ in range(max(3, min(args.steps, 10))):
+            run(i)
+            ph = s.timings()
+            acc.append(ph)
+            for k, v in zip(NS_ALG, ph):
+                phases[k].append(v)
+        s.set_timing(False)
+        per_input[inputs[i][0]] = {k: statistics.mean(a[j] for a in acc) for j, k in enumerate(NS_ALG)}
+    mean_phase = {k: statistics.mean(v) for k, v in phases.items()}
+    top = max(mean_phase, key=mean_phase.get)
+    alg = NS_ALG[top][0] * n + NS_ALG[top][1] * cells
+    peak, peak_kind = peaks()
+    achieved = alg / (mean_phase[top] / 1000.0) / 1e9
+    # end to end through the public API: pinned positions in, the search, every output back
+    host_in = [torch.from_numpy(inp[2]).pin_memory() for inp in inputs]
+    outs = [torch.empty(n, dtype=torch.int32).pin_memory() for _ in range(3)]
+    out_c = [torch.empty(cells, dtype=torch.int32).pin_memory(), torch.empty(cells + 1, dtype=torch.int32).pin_memory()]
+    dist.barrier()
+    t0 = time.perf_counter()
+    with torch.cuda.stream(stream):
+        for _ in range(args.steps):
+            for i in range(2):
+                dev[i].copy_(host_in[i], non_blocking=True)
+                run(i)
+                for o, d in zip(outs, (keys, order, rank)):
+                    o.copy_(d, non_blocking=True)
+                out_c[0].copy_(cc, non_blocking=True)
+                out_c[1].copy_(co, non_blocking=True)
+        stream.synchronize()
+    e2e_s = dist.max(time.perf_counter() - t0)
+    e2e = dist.world * 2 * n * args.steps / e2e_s
+    # the last clumped search's outputs against properties of a correct search
+    o_np = outs[1].numpy().view(np.uint32)
+    k_np = outs[0].numpy().view(np.uint32)
+    assert np.all(np.diff(k_np[o_np].astype(np.int64)) >= 0)
+    for s in searches:
+        s.close()
+    cpu = None
+    if dist.rank == 0 and not args.no_cpu_baseline:
+        sample = 1 << 20
+        rate, dt = _ns_cpu(_ns_inputs(sample), sample, min_seconds=10.0)
+        cpu = {"value": rate, "unit": "particles/s", "cores": 1, "kind": "port",
+               "sample": "2^20 points of each input on the same grid (serial restatement), %.1f s" % dt}
+    line = {"metric": NS_METRIC, "value": value, "unit": "particles/s", "n_gpus": dist.world, "steps": args.steps,
+            "warmup": max(args.warmup, 3), "ms_per_step": ms_step, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "u32", "data": "synthetic",
+            "config": {"workload": NS_DESC, "points_per_input": n, "parallelism": "replicas",
+                       "l2": "inputs of 256 MB each, larger than the 129 MB L2", "phase_ms": per_input},
+            "e2e": {"value": e2e, "unit": "particles/s", "h2d_bytes_per_step": int(2 * 16 * n),
+                    "d2h_bytes_per_step": int(2 * (12 * n + 4 * cells + 4 * (cells + 1)))},
+            "gpu_launches": 12 * args.steps,
+            "roofline": {"bound": "hbm", "kernel": top, "achieved": achieved, "peak": peak, "unit": "GB/s",
+                         "frac": achieved / peak, "peak_kind": peak_kind, "traffic": None,
+                         "alg_bytes_per_launch": alg, "avg_launch_ms": mean_phase[top],
+                         "phases_ms": mean_phase,
+                         "note": "a phase of pbf_ns_run timed by its own CUDA events; sort_passes is 3 x (digit "
+                                 "count, scan of the digit x tile matrix, record move), 9 launches"},
+            "clocks": clk, "cpu_baseline": cpu}
+    if dist.rank == 0:
+        print(json.dumps(line), flush=True)
+
+
 def main():
     args = parse_args()
     dist = Dist(args.gpus)
     try:
         if args.workload == "voxelize_mesh":
             voxel_arm(args, dist)
+        elif args.workload == "neighbor_search_16m":
+            ns_arm(args, dist)
         elif args.workload == "render_1m_1080p":
             render_arm(args, dist)
         elif args.impl == "reference":

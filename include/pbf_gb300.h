@@ -333,6 +333,15 @@ int pbf_ns_lists(pbf_ns* ns, const float* d_pos4, uint32_t n, float radius,
                  uint32_t* total);
 int pbf_ns_sync(pbf_ns* ns);
 const char* pbf_ns_last_error(const pbf_ns* ns);
+/* Per-phase device times of pbf_ns_run (no counterpart in the reference):
+ * when enabled, each run records CUDA events on the context's stream and
+ * pbf_ns_timings returns the last run's phases in milliseconds after
+ * synchronising: [0] cell keys (ParticleInsert), [1] the stable radix-sort
+ * passes (CountingSort), [2] cell counts and offsets from
+ * the sorted keys (cellParticleCount + ExclusiveScan), [3] outputs (ranks,
+ * copies of counts, offsets and order).  PBF_ESTATE before a timed run. */
+int pbf_ns_set_timing(pbf_ns* ns, int enable);
+int pbf_ns_timings(pbf_ns* ns, float ms[4]);
 
 /* ---- exclusive scan (ExclusiveScan.execute, exclusiveScan.ts:134-166):
  * single-pass decoupled look-back over any length (no 512-multiple or

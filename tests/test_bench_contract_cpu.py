@@ -47,3 +47,11 @@ def test_voxelize_reference_arm_line():
     assert d["impl"] == "reference" and d["metric"] == bench.VOXEL_METRIC
     assert d["unit"] == "ms" and d["higher_is_better"] is False and d["value"] > 0
     assert d["config"]["points"] > 10000
+
+
+def test_neighbor_search_reference_arm_line():
+    import bench
+    d = _run("--impl", "reference", "--workload", "neighbor_search_16m", "--steps", "1", "--warmup", "0")
+    assert d["impl"] == "reference" and d["metric"] == bench.NS_METRIC
+    assert d["unit"] == "particles/s" and d["higher_is_better"] is True and d["value"] > 0
+    assert d["cpu_baseline"]["kind"] == "port" and d["cpu_baseline"]["cores"] == 1

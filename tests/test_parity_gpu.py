@@ -115,6 +115,32 @@ def test_neighbor_search_16m_properties(dist):
     assert np.array_equal(order[pos], np.arange(n))
 
 
+def test_neighbor_search_phase_timings():
+    """pbf_ns_set_timing / pbf_ns_timings: four non-negative phases of the
+    last run, none before a timed run, and the results unchanged."""
+    cfg, pts = scenes.neighbor_case(1 << 20, "clumps", seed=3, dim=128)
+    dims, cells = O.grid_dims(cfg)
+    inv = [float(np.float32(float(dims[a]) / (cfg.domain_max[a] - cfg.domain_min[a]))) for a in range(3)]
+    n = pts.shape[0]
+    ns = NeighborSearch(list(cfg.domain_min), inv, list(dims), n)
+    try:
+        d_pos = dev(pts)
+        order = torch.empty(n, dtype=torch.int32, device="cuda")
+        ns.set_timing(True)
+        with pytest.raises(Exception):
+            ns.timings()                                   # no timed run yet
+        ns.run(d_pos.data_ptr(), n, 0, 0, 0, order.data_ptr(), 0)
+        ms = ns.timings()
+        assert len(ms) == 4 and all(m >= 0.0 for m in ms) and sum(ms) > 0.0
+        ns.set_timing(False)
+        ns.run(d_pos.data_ptr(), n, 0, 0, 0, order.data_ptr(), 0)
+        ns.sync()
+        ref = O.neighbor_search(cfg, pts)
+        assert np.array_equal(order.cpu().numpy().view(np.uint32), ref["order"])
+    finally:
+        ns.close()
+
+
 def test_neighbor_search_full_cells():
     """Cells past the warp paths (33..1024 by counting, >1024 by block radix)."""
     rng = np.random.default_rng(5)

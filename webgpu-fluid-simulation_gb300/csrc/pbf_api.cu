@@ -1980,6 +1980,10 @@ struct pbf_ns {
   DBuf<uint32_t> key, rank, cell_count, cell_start, perm_raw, id_raw, perm, tmp_a, tmp_b, big_list, big_count, err_word;
   DBuf<uint32_t> nbr_count;
   void* scan_scratch = nullptr;
+  void* radix_scratch = nullptr;  // histograms and look-back words of the radix passes
+  // pbf_ns_set_timing: events at the phase boundaries of pbf_ns_run
+  bool timing = false, timed = false;
+  cudaEvent_t ev[5] = {};
 };
 
 namespace {
@@ -2047,6 +2051,7 @@ int pbf_ns_create(const pbf_grid* grid, uint32_t max_particles, void* stream, pb
   A(s->nbr_count.alloc(n + 1));
   size_t sb = scan_scratch_bytes(cells + 1), sb2 = scan_scratch_bytes(n + 1);
   A(cudaMalloc(&s->scan_scratch, sb > sb2 ? sb : sb2));
+  A(cudaMalloc(&s->radix_scratch, radix_scratch_bytes(n)));
   if (e == cudaSuccess) {
     A(cudaMemsetAsync(s->err_word.p, 0, 4, s->stream));
     A(cudaStreamSynchronize(s->stream));
@@ -2066,6 +2071,9 @@ int pbf_ns_destroy(pbf_ns* s) {
                             &s->tmp_a, &s->tmp_b, &s->big_list,   &s->big_count,  &s->err_word, &s->nbr_count};
   for (auto* b : bufs) b->release();
   if (s->scan_scratch) cudaFree(s->scan_scratch);
+  if (s->radix_scratch) cudaFree(s->radix_scratch);
+  for (cudaEvent_t& e : s->ev)
+    if (e) cudaEventDestroy(e);
   if (s->own_stream && s->stream) cudaStreamDestroy(s->stream);
   delete s;
   return PBF_OK;
@@ -2079,21 +2087,51 @@ int pbf_ns_run(pbf_ns* s, const float* d_pos4, uint32_t n, uint32_t* d_keys, uin
   if (n > s->max_n) return nsfail(s, PBF_ECAPACITY, "too many particles for this search context");
   cudaStream_t st = s->stream;
   const GridParams g = s->g;
-  NSCU(s, cudaMemsetAsync(s->cell_count.p, 0, ((size_t)g.cells + 1) * 4, st));
-  NSCU(s, launch_insert(g, (const float4*)d_pos4, n, s->key.p, s->rank.p, s->cell_count.p, st));
-  uint32_t bits = 1;
-  while (bits < 32 && (1ull << bits) < (uint64_t)n) ++bits;
-  SortBuffers sb{s->key.p,   s->rank.p,  s->cell_count.p, s->cell_start.p, s->perm_raw.p, s->id_raw.p,
-                 s->perm.p,  s->tmp_a.p, s->tmp_b.p,      s->big_list.p,   s->big_count.p, s->scan_scratch,
-                 s->err_word.p};
-  NSCU(s, launch_sort_by_cell(g, n, nullptr, sb, bits, st));
-  if (d_keys && n) NSCU(s, cudaMemcpyAsync(d_keys, s->key.p, (size_t)n * 4, cudaMemcpyDeviceToDevice, st));
+  const bool tm = s->timing;
+  s->timed = false;
+  if (tm) NSCU(s, cudaEventRecord(s->ev[0], st));
+  // The points come in particle-id order, so a stable radix sort of the ids
+  // by cell key is the counting sort with each cell in id order.  Keys go
+  // straight to the caller's array when it wants them.
+  uint32_t* key = d_keys ? d_keys : s->key.p;
+  uint32_t* const tk[2] = {s->tmp_a.p, s->perm_raw.p};
+  uint32_t* const tv[2] = {s->tmp_b.p, s->id_raw.p};
+  NSCU(s, launch_radix_sort_idorder(g, (const float4*)d_pos4, n, key, s->rank.p, s->perm.p, tk, tv, s->radix_scratch,
+                                    s->err_word.p, st, tm ? s->ev[1] : nullptr));
+  if (tm) NSCU(s, cudaEventRecord(s->ev[2], st));
+  // counts and offsets from the sorted keys (s->rank holds them); the order
+  // and offsets stay in the context for pbf_ns_lists
+  NSCU(s, launch_cells_from_sorted(n, s->rank.p, g.cells, s->cell_count.p, s->cell_start.p, s->scan_scratch,
+                                   s->err_word.p, st));
+  if (tm) NSCU(s, cudaEventRecord(s->ev[3], st));
+  if (d_rank) NSCU(s, launch_rank_sorted(n, s->rank.p, s->perm.p, s->cell_start.p, d_rank, st));
   if (d_cell_count)
     NSCU(s, cudaMemcpyAsync(d_cell_count, s->cell_count.p, (size_t)g.cells * 4, cudaMemcpyDeviceToDevice, st));
   if (d_cell_offset)
     NSCU(s, cudaMemcpyAsync(d_cell_offset, s->cell_start.p, ((size_t)g.cells + 1) * 4, cudaMemcpyDeviceToDevice, st));
   if (d_order && n) NSCU(s, cudaMemcpyAsync(d_order, s->perm.p, (size_t)n * 4, cudaMemcpyDeviceToDevice, st));
-  if (d_rank && n) NSCU(s, launch_rank_from_order(n, s->perm.p, s->key.p, s->cell_start.p, d_rank, st));
+  if (tm) {
+    NSCU(s, cudaEventRecord(s->ev[4], st));
+    s->timed = true;
+  }
+  return PBF_OK;
+}
+
+int pbf_ns_set_timing(pbf_ns* s, int enable) {
+  if (!s) return PBF_EINVAL;
+  if (enable)
+    for (cudaEvent_t& e : s->ev)
+      if (!e) NSCU(s, cudaEventCreate(&e));
+  s->timing = enable != 0;
+  s->timed = false;
+  return PBF_OK;
+}
+
+int pbf_ns_timings(pbf_ns* s, float ms[4]) {
+  if (!s || !ms) return PBF_EINVAL;
+  if (!s->timed) return nsfail(s, PBF_ESTATE, "no timed pbf_ns_run since timing was enabled");
+  NSCU(s, cudaEventSynchronize(s->ev[4]));
+  for (int i = 0; i < 4; ++i) NSCU(s, cudaEventElapsedTime(&ms[i], s->ev[i], s->ev[i + 1]));
   return PBF_OK;
 }
 

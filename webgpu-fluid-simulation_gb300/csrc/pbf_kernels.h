@@ -98,13 +98,31 @@ struct SortBuffers {
 cudaError_t launch_insert(GridParams g, const float4* pos, uint32_t n, uint32_t* key, uint32_t* rank,
                           uint32_t* cell_count, cudaStream_t st);
 // scatter + stable within-cell order + (optionally) gather of the particle state.
+// Stable LSD radix sort of points in particle-id order by cell key (the
+// stand-alone search): keys[n] (by id) receive the cell keys, skeys[n] the
+// sorted keys and order[n] the ids in sorted order, stable by id.  tmp_k /
+// tmp_v: two pairs of n-entry scratch arrays; scratch: radix_scratch_bytes(n)
+// bytes.  after_keys (optional) is recorded after the keys.
+struct RadixPlan {
+  int passes, width;
+  size_t tiles;
+};
+RadixPlan radix_plan(uint32_t cells, size_t n);
+size_t radix_scratch_bytes(size_t n);
+cudaError_t launch_radix_sort_idorder(GridParams g, const float4* pos, uint32_t n, uint32_t* keys, uint32_t* skeys,
+                                      uint32_t* order, uint32_t* const tmp_k[2], uint32_t* const tmp_v[2],
+                                      void* scratch, uint32_t* err, cudaStream_t st, cudaEvent_t after_keys);
+// Cell counts (cells + 1 entries, the last 0) and exclusive offsets from sorted keys.
+cudaError_t launch_cells_from_sorted(uint32_t n, const uint32_t* skeys, uint32_t cells, uint32_t* cell_count,
+                                     uint32_t* cell_start, void* scan_scratch, uint32_t* err, cudaStream_t st);
+// rank_out[order[q]] = q - cell_start[skeys[q]].
+cudaError_t launch_rank_sorted(uint32_t n, const uint32_t* skeys, const uint32_t* order, const uint32_t* cell_start,
+                               uint32_t* rank_out, cudaStream_t st);
 cudaError_t launch_sort_by_cell(GridParams g, uint32_t n, const uint32_t* ids, SortBuffers& b, uint32_t id_bits,
                                 cudaStream_t st);
 cudaError_t launch_gather_state(uint32_t n, const uint32_t* perm, const float4* pos_in, const float4* xs_in,
                                 const uint32_t* id_in, float4* pos_out, float4* xs_out, uint32_t* id_out,
                                 cudaStream_t st);
-cudaError_t launch_rank_from_order(uint32_t n, const uint32_t* perm, const uint32_t* key, const uint32_t* cell_start,
-                                   uint32_t* rank_out, cudaStream_t st);
 cudaError_t launch_scatter_by_id(uint32_t n, const uint32_t* id, const float4* src, float4* dst, cudaStream_t st);
 // dst[id[t]] = src[t].w (a scalar kept in the w lane of a packed float4 array)
 cudaError_t launch_scatter_w_by_id(uint32_t n, const uint32_t* id, const float4* src, float* dst, cudaStream_t st);

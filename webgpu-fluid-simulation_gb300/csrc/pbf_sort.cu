@@ -301,6 +301,229 @@ __global__ void __launch_bounds__(kRadixThreads) k_bigcell(const uint32_t* __res
   }
 }
 
+// ---- stable LSD radix sort by cell key of points in particle-id order ---------------
+// The stand-alone search receives its points in id order, so a stable sort
+// of the ids by cell key yields the order with every cell's particles in id
+// order: no within-cell pass, and skewed cell occupancy costs nothing extra.
+// Each pass over a digit is reduce-then-scan: every tile of 4096 records
+// counts its digits (written digit-major, count[d * tiles + tile]); one
+// exclusive scan of that matrix gives each (digit, tile) run its global
+// place; then every tile ranks its records by digit in shared memory (stable
+// in input order) and writes each digit's run there.  Reads and writes are
+// coalesced, and no tile waits on another.
+constexpr int kOsThreads = 256;
+constexpr int kOsItems = 16;
+constexpr int kOsTile = kOsThreads * kOsItems;  // 4096 records per tile
+constexpr int kOsWarps = kOsThreads / 32;
+constexpr int kOsMaxRadix = 256;
+
+// Lanes of the warp holding the same digit (valid lanes only): one ballot per
+// digit bit.
+template <int kWidth>
+__device__ __forceinline__ unsigned digit_peers(uint32_t d, bool valid) {
+  unsigned peers = __ballot_sync(kFull, valid);
+#pragma unroll
+  for (int b = 0; b < kWidth; ++b) {
+    const unsigned m = __ballot_sync(kFull, (d >> b) & 1u);
+    peers &= ((d >> b) & 1u) ? m : ~m;
+  }
+  return peers;
+}
+
+// Cell key of every point (ParticleInsert).
+__global__ void __launch_bounds__(256) k_cell_keys(GridParams g, const float4* __restrict__ pos, uint32_t n,
+                                                   uint32_t* __restrict__ key) {
+  for (uint32_t s = blockIdx.x * blockDim.x + threadIdx.x; s < n; s += gridDim.x * blockDim.x) {
+    const float4 x = __ldg(pos + s);
+    const int cx = cell_axis(x.x, g.origin[0], g.inv_cell[0], g.dim[0]);
+    const int cy = cell_axis(x.y, g.origin[1], g.inv_cell[1], g.dim[1]);
+    const int cz = cell_axis(x.z, g.origin[2], g.inv_cell[2], g.dim[2]);
+    key[s] = cell_key(cx, cy, cz, g);
+  }
+}
+
+// Digit counts of one tile, digit-major (per-warp counters in shared memory,
+// summed at the end).
+template <int kWidth>
+__global__ void __launch_bounds__(kOsThreads) k_tile_digits(uint32_t n, const uint32_t* __restrict__ kin,
+                                                            uint32_t* __restrict__ count, uint32_t tiles, int shift) {
+  constexpr uint32_t kRadix = 1u << kWidth, kMask = kRadix - 1u;
+  __shared__ uint32_t s_cnt[kOsWarps][kRadix];
+  const uint32_t tid = threadIdx.x, warp = tid >> 5;
+  for (uint32_t d = tid; d < kOsWarps * kRadix; d += kOsThreads) (&s_cnt[0][0])[d] = 0u;
+  const uint32_t t0 = blockIdx.x * (uint32_t)kOsTile;
+  uint32_t d[kOsItems];
+#pragma unroll
+  for (int i = 0; i < kOsItems; ++i) {
+    const uint32_t idx = t0 + (uint32_t)i * kOsThreads + tid;
+    d[i] = idx < n ? (__ldg(kin + idx) >> shift) & kMask : kRadix;
+  }
+  __syncthreads();
+#pragma unroll
+  for (int i = 0; i < kOsItems; ++i)
+    if (d[i] < kRadix) atomicAdd(&s_cnt[warp][d[i]], 1u);
+  __syncthreads();
+  for (uint32_t dd = tid; dd < kRadix; dd += kOsThreads) {
+    uint32_t c = 0;
+#pragma unroll
+    for (int w = 0; w < kOsWarps; ++w) c += s_cnt[w][dd];
+    count[(size_t)dd * tiles + blockIdx.x] = c;
+  }
+}
+
+// One pass over the digit (key >> shift) & (2^kWidth - 1): place[d * tiles +
+// tile] is where the tile's run of digit d starts.  vin == nullptr: the values
+// are the input positions (particle ids).
+template <int kWidth>
+__global__ void __launch_bounds__(kOsThreads, 3) k_radix_pass(uint32_t n, const uint32_t* __restrict__ kin,
+                                                              const uint32_t* __restrict__ vin,
+                                                              uint32_t* __restrict__ kout, uint32_t* __restrict__ vout,
+                                                              const uint32_t* __restrict__ place, uint32_t tiles,
+                                                              int shift) {
+  constexpr uint32_t kRadix = 1u << kWidth, kMask = kRadix - 1u;
+  __shared__ uint32_t s_key[kOsTile];
+  __shared__ uint32_t s_val[kOsTile];
+  __shared__ uint32_t s_wcnt[kOsWarps][kRadix];  // per-warp digit counts, then offsets over warps
+  __shared__ uint32_t s_loc[kRadix];             // digit counts of the tile, then their exclusive scan
+  __shared__ uint32_t s_glob[kRadix];            // global place of the tile's first record of each digit
+  const uint32_t tid = threadIdx.x, lane = tid & 31u, warp = tid >> 5;
+  const uint32_t tile = blockIdx.x;
+  for (uint32_t i = tid; i < kOsWarps * kRadix; i += kOsThreads) (&s_wcnt[0][0])[i] = 0u;
+  for (uint32_t d = tid; d < kRadix; d += kOsThreads) s_glob[d] = __ldg(place + (size_t)d * tiles + tile);
+  const uint32_t t0 = tile * (uint32_t)kOsTile;
+  // warp w holds records t0 + 512 w .. + 511; round i is records 32 i .. 32 i + 31 of it
+  const uint32_t w0 = t0 + warp * (32u * kOsItems) + lane;
+  uint32_t k[kOsItems], v[kOsItems], r[kOsItems];
+#pragma unroll
+  for (int i = 0; i < kOsItems; ++i) {
+    const uint32_t idx = w0 + 32u * i;
+    const bool valid = idx < n;
+    k[i] = valid ? __ldg(kin + idx) : 0xffffffffu;
+    v[i] = valid ? (vin ? __ldg(vin + idx) : idx) : 0u;
+  }
+  __syncthreads();
+  // stable ranks within the warp, round by round in input order: the lowest
+  // lane of each digit group adds the group to the warp's counter and passes
+  // the old count on (shared-memory atomics keep the rounds in order)
+  uint32_t* wc = s_wcnt[warp];
+  const unsigned lt = (1u << lane) - 1u;
+#pragma unroll
+  for (int i = 0; i < kOsItems; ++i) {
+    const bool valid = w0 + 32u * i < n;
+    const uint32_t d = (k[i] >> shift) & kMask;
+    const unsigned peers = digit_peers<kWidth>(d, valid);
+    const int leader = __ffs(peers) - 1;
+    uint32_t before = 0u;
+    if (valid && (int)lane == leader) before = atomicAdd(wc + d, (uint32_t)__popc(peers));
+    before = __shfl_sync(kFull, before, leader & 31);
+    r[i] = before + (uint32_t)__popc(peers & lt);
+  }
+  __syncthreads();
+  // per digit: offsets over the warps and the tile's count
+  if (tid < kRadix) {
+    uint32_t cnt = 0;
+#pragma unroll
+    for (int w = 0; w < kOsWarps; ++w) {
+      const uint32_t c = s_wcnt[w][tid];
+      s_wcnt[w][tid] = cnt;
+      cnt += c;
+    }
+    s_loc[tid] = cnt;
+  }
+  __syncthreads();
+  // exclusive scan of the tile's digit counts (warp 0)
+  if (warp == 0) {
+    constexpr uint32_t kPer = (kRadix + 31u) / 32u;
+    uint32_t loc[kPer];
+    uint32_t sum = 0;
+#pragma unroll
+    for (uint32_t j = 0; j < kPer; ++j) {
+      const uint32_t d = lane * kPer + j;
+      loc[j] = d < kRadix ? s_loc[d] : 0u;
+      sum += loc[j];
+    }
+    uint32_t x = sum;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      const uint32_t y = __shfl_up_sync(kFull, x, o);
+      if ((int)lane >= o) x += y;
+    }
+    uint32_t run = x - sum;
+#pragma unroll
+    for (uint32_t j = 0; j < kPer; ++j) {
+      const uint32_t d = lane * kPer + j;
+      if (d < kRadix) s_loc[d] = run;
+      run += loc[j];
+    }
+  }
+  __syncthreads();
+  // records to their tile-sorted place in shared memory
+#pragma unroll
+  for (int i = 0; i < kOsItems; ++i) {
+    if (w0 + 32u * i < n) {
+      const uint32_t d = (k[i] >> shift) & kMask;
+      const uint32_t lp = s_loc[d] + s_wcnt[warp][d] + r[i];
+      s_key[lp] = k[i];
+      s_val[lp] = v[i];
+    }
+  }
+  __syncthreads();
+  // each digit's run to its global place: consecutive j, consecutive addresses
+  const uint32_t in_tile = (n - t0) < (uint32_t)kOsTile ? (n - t0) : (uint32_t)kOsTile;
+#pragma unroll 4
+  for (uint32_t j = tid; j < in_tile; j += kOsThreads) {
+    const uint32_t kk = s_key[j];
+    const uint32_t d = (kk >> shift) & kMask;
+    const uint32_t p = s_glob[d] + (j - s_loc[d]);
+    if (p < n) {
+      kout[p] = kk;
+      vout[p] = s_val[j];
+    }
+  }
+}
+
+// Cell counts from the sorted keys: each run of equal keys within a warp is
+// found from its neighbour's key (one shuffle and one ballot) and added once.
+__global__ void __launch_bounds__(256) k_count_sorted(uint32_t n, const uint32_t* __restrict__ skey,
+                                                      uint32_t* cell_count) {
+  const uint32_t q = blockIdx.x * blockDim.x + threadIdx.x;
+  const uint32_t lane = threadIdx.x & 31u;
+  const bool valid = q < n;
+  const uint32_t k = valid ? __ldg(skey + q) : 0xffffffffu;
+  const uint32_t up = __shfl_up_sync(kFull, k, 1);
+  const bool start = valid && (lane == 0u || up != k);
+  const unsigned starts = __ballot_sync(kFull, start);
+  const unsigned valid_mask = __ballot_sync(kFull, valid);
+  if (start) {
+    const unsigned later = starts & ~((2u << lane) - 1u);  // run starts after this lane
+    const uint32_t end = later ? (uint32_t)(__ffs(later) - 1) : (uint32_t)(32 - __clz(valid_mask));
+    atomicAdd(cell_count + k, end - lane);
+  }
+}
+
+// particleSortIndex: the place of each particle within its cell, by particle
+// id.  Four sorted positions a thread (vector loads keep more reads in flight
+// ahead of the scattered stores).
+__global__ void __launch_bounds__(256) k_rank_sorted(uint32_t n, const uint32_t* __restrict__ skey,
+                                                     const uint32_t* __restrict__ order,
+                                                     const uint32_t* __restrict__ cell_start,
+                                                     uint32_t* __restrict__ rank_out) {
+  const uint32_t q0 = 4u * (blockIdx.x * blockDim.x + threadIdx.x);
+  if (q0 >= n) return;
+  if (q0 + 4u <= n) {
+    const uint4 k = __ldg(reinterpret_cast<const uint4*>(skey + q0));
+    const uint4 o = __ldg(reinterpret_cast<const uint4*>(order + q0));
+    const uint32_t s0 = __ldg(cell_start + k.x), s1 = __ldg(cell_start + k.y), s2 = __ldg(cell_start + k.z),
+                   s3 = __ldg(cell_start + k.w);
+    rank_out[o.x] = q0 - s0;
+    rank_out[o.y] = q0 + 1u - s1;
+    rank_out[o.z] = q0 + 2u - s2;
+    rank_out[o.w] = q0 + 3u - s3;
+  } else {
+    for (uint32_t q = q0; q < n; ++q) rank_out[order[q]] = q - __ldg(cell_start + skey[q]);
+  }
+}
+
 // ---- gather of the particle state into the new order -------------------------------
 __global__ void __launch_bounds__(256) k_gather(uint32_t n, const uint32_t* __restrict__ perm,
                                                 const float4* __restrict__ pos_in, const float4* __restrict__ xs_in,
@@ -312,14 +535,6 @@ __global__ void __launch_bounds__(256) k_gather(uint32_t n, const uint32_t* __re
   pos_out[t] = __ldg(pos_in + o);
   xs_out[t] = __ldg(xs_in + o);
   id_out[t] = id_in ? __ldg(id_in + o) : o;  // no id array: the input order is the id order
-}
-
-__global__ void k_rank_from_order(uint32_t n, const uint32_t* __restrict__ perm, const uint32_t* __restrict__ key,
-                                  const uint32_t* __restrict__ cell_start, uint32_t* __restrict__ rank_out) {
-  uint32_t t = blockIdx.x * blockDim.x + threadIdx.x;
-  if (t >= n) return;
-  uint32_t s = perm[t];
-  rank_out[s] = t - cell_start[key[s]];
 }
 
 __global__ void k_scatter_f4(uint32_t n, const uint32_t* __restrict__ id, const float4* __restrict__ src,
@@ -432,6 +647,97 @@ inline unsigned blocks_for(size_t n, int threads) { return (unsigned)((n + threa
 
 }  // namespace
 
+RadixPlan radix_plan(uint32_t cells, size_t n) {
+  RadixPlan r;
+  uint32_t bits = 1;
+  while (bits < 32 && (1ull << bits) < (uint64_t)cells) ++bits;
+  r.passes = (int)((bits + 7) / 8);
+  r.width = (int)((bits + (uint32_t)r.passes - 1) / (uint32_t)r.passes);
+  r.tiles = (n + kOsTile - 1) / kOsTile;
+  return r;
+}
+
+namespace {
+size_t round256(size_t b) { return (b + 255) / 256 * 256; }
+}  // namespace
+
+// Scratch: the digit-major count matrix, its scan and the scan's own scratch.
+size_t radix_scratch_bytes(size_t n) {
+  size_t tiles = (n + kOsTile - 1) / kOsTile;
+  if (tiles == 0) tiles = 1;
+  const size_t m = tiles * kOsMaxRadix;
+  return 2 * round256(m * sizeof(uint32_t)) + scan_scratch_bytes(m);
+}
+
+cudaError_t launch_radix_sort_idorder(GridParams g, const float4* pos, uint32_t n, uint32_t* keys, uint32_t* skeys,
+                                      uint32_t* order, uint32_t* const tmp_k[2], uint32_t* const tmp_v[2],
+                                      void* scratch, uint32_t* err, cudaStream_t st, cudaEvent_t after_keys) {
+  cudaError_t e = cudaSuccess;
+  if (n == 0) return after_keys ? cudaEventRecord(after_keys, st) : cudaSuccess;
+  const RadixPlan plan = radix_plan(g.cells, n);
+  const uint32_t radix = 1u << plan.width;
+  const size_t m = plan.tiles * radix;
+  char* sc = reinterpret_cast<char*>(scratch);
+  uint32_t* count = reinterpret_cast<uint32_t*>(sc);
+  uint32_t* place = reinterpret_cast<uint32_t*>(sc + round256(plan.tiles * kOsMaxRadix * sizeof(uint32_t)));
+  void* scan_scr = sc + 2 * round256(plan.tiles * kOsMaxRadix * sizeof(uint32_t));
+  unsigned blocks = (unsigned)((n + 255) / 256);
+  if (blocks > 152u * 8u) blocks = 152u * 8u;
+  k_cell_keys<<<blocks, 256, 0, st>>>(g, pos, n, keys);
+  if ((e = cudaGetLastError()) != cudaSuccess) return e;
+  if (after_keys && (e = cudaEventRecord(after_keys, st)) != cudaSuccess) return e;
+  for (int p = 0; p < plan.passes; ++p) {
+    const bool last = p == plan.passes - 1;
+    const uint32_t* kin = p == 0 ? keys : tmp_k[(p - 1) & 1];
+    const uint32_t* vin = p == 0 ? nullptr : tmp_v[(p - 1) & 1];
+    uint32_t* kout = last ? skeys : tmp_k[p & 1];
+    uint32_t* vout = last ? order : tmp_v[p & 1];
+    const int shift = p * plan.width;
+    const unsigned grid = (unsigned)plan.tiles;
+    const uint32_t tl = (uint32_t)plan.tiles;
+    switch (plan.width) {
+#define PBF_RADIX_WIDTH(W)                                                              \
+  case W:                                                                               \
+    k_tile_digits<W><<<grid, kOsThreads, 0, st>>>(n, kin, count, tl, shift);            \
+    if ((e = cudaGetLastError()) != cudaSuccess) return e;                              \
+    if ((e = launch_exclusive_scan(count, place, m, scan_scr, err, st)) != cudaSuccess) \
+      return e;                                                                         \
+    k_radix_pass<W><<<grid, kOsThreads, 0, st>>>(n, kin, vin, kout, vout, place, tl, shift); \
+    break;
+      PBF_RADIX_WIDTH(1)
+      PBF_RADIX_WIDTH(2)
+      PBF_RADIX_WIDTH(3)
+      PBF_RADIX_WIDTH(4)
+      PBF_RADIX_WIDTH(5)
+      PBF_RADIX_WIDTH(6)
+      PBF_RADIX_WIDTH(7)
+      PBF_RADIX_WIDTH(8)
+#undef PBF_RADIX_WIDTH
+      default:
+        return cudaErrorInvalidValue;
+    }
+    if ((e = cudaGetLastError()) != cudaSuccess) return e;
+  }
+  return cudaSuccess;
+}
+
+cudaError_t launch_cells_from_sorted(uint32_t n, const uint32_t* skeys, uint32_t cells, uint32_t* cell_count,
+                                     uint32_t* cell_start, void* scan_scratch, uint32_t* err, cudaStream_t st) {
+  cudaError_t e = cudaMemsetAsync(cell_count, 0, ((size_t)cells + 1) * sizeof(uint32_t), st);
+  if (e != cudaSuccess) return e;
+  if (n) k_count_sorted<<<(unsigned)((n + 255) / 256), 256, 0, st>>>(n, skeys, cell_count);
+  if ((e = cudaGetLastError()) != cudaSuccess) return e;
+  return launch_exclusive_scan(cell_count, cell_start, (size_t)cells + 1, scan_scratch, err, st);
+}
+
+cudaError_t launch_rank_sorted(uint32_t n, const uint32_t* skeys, const uint32_t* order, const uint32_t* cell_start,
+                               uint32_t* rank_out, cudaStream_t st) {
+  if (n == 0) return cudaSuccess;
+  const uint32_t threads = (n + 3u) / 4u;
+  k_rank_sorted<<<(threads + 255u) / 256u, 256, 0, st>>>(n, skeys, order, cell_start, rank_out);
+  return cudaGetLastError();
+}
+
 size_t scan_scratch_bytes(size_t n) {
   size_t tiles = (n + kScanTile - 1) / kScanTile;
   if (tiles == 0) tiles = 1;
@@ -511,13 +817,6 @@ cudaError_t launch_gather_state(uint32_t n, const uint32_t* perm, const float4* 
                                 cudaStream_t st) {
   if (n == 0) return cudaSuccess;
   k_gather<<<blocks_for(n, 256), 256, 0, st>>>(n, perm, pos_in, xs_in, id_in, pos_out, xs_out, id_out);
-  return cudaGetLastError();
-}
-
-cudaError_t launch_rank_from_order(uint32_t n, const uint32_t* perm, const uint32_t* key, const uint32_t* cell_start,
-                                   uint32_t* rank_out, cudaStream_t st) {
-  if (n == 0) return cudaSuccess;
-  k_rank_from_order<<<blocks_for(n, 256), 256, 0, st>>>(n, perm, key, cell_start, rank_out);
   return cudaGetLastError();
 }
 

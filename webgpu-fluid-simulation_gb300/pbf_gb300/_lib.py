@@ -184,6 +184,8 @@ SIGNATURES = {
     "pbf_ns_run": (ctypes.c_int, [_P, _P, u32, _P, _P, _P, _P, _P]),
     "pbf_ns_lists": (ctypes.c_int, [_P, _P, u32, ctypes.c_float, _P, _P, u32, _UP]),
     "pbf_ns_sync": (ctypes.c_int, [_P]),
+    "pbf_ns_set_timing": (ctypes.c_int, [_P, ctypes.c_int]),
+    "pbf_ns_timings": (ctypes.c_int, [_P, _P]),
     "pbf_ns_last_error": (ctypes.c_char_p, [_P]),
     "pbf_exclusive_scan_u32": (ctypes.c_int, [_P, _P, ctypes.c_size_t, _P]),
     "pbf_generate_volume_map": (ctypes.c_int, [ctypes.POINTER(Shape), u32, _UP, _FP, _FP, ctypes.c_float, u32, u32,

@@ -456,6 +456,16 @@ class NeighborSearch:
     def sync(self):
         self._check(self._lib.pbf_ns_sync(self._h), "pbf_ns_sync")
 
+    def set_timing(self, enable=True):
+        self._check(self._lib.pbf_ns_set_timing(self._h, 1 if enable else 0), "pbf_ns_set_timing")
+
+    def timings(self):
+        """The last timed run's phases in ms: [cell keys + counts, scan of the
+        counts, counting-sort reorder, outputs]."""
+        ms = (ctypes.c_float * 4)()
+        self._check(self._lib.pbf_ns_timings(self._h, ms), "pbf_ns_timings")
+        return [float(x) for x in ms]
+
     def close(self):
         if getattr(self, "_h", None):
             self._lib.pbf_ns_destroy(self._h)

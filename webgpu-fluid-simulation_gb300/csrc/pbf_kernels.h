@@ -95,9 +95,6 @@ struct SortBuffers {
   uint32_t* err;
 };
 
-cudaError_t launch_insert(GridParams g, const float4* pos, uint32_t n, uint32_t* key, uint32_t* rank,
-                          uint32_t* cell_count, cudaStream_t st);
-// scatter + stable within-cell order + (optionally) gather of the particle state.
 // Stable LSD radix sort of points in particle-id order by cell key (the
 // stand-alone search): keys[n] (by id) receive the cell keys, skeys[n] the
 // sorted keys and order[n] the ids in sorted order, stable by id.  tmp_k /
@@ -118,6 +115,7 @@ cudaError_t launch_cells_from_sorted(uint32_t n, const uint32_t* skeys, uint32_t
 // rank_out[order[q]] = q - cell_start[skeys[q]].
 cudaError_t launch_rank_sorted(uint32_t n, const uint32_t* skeys, const uint32_t* order, const uint32_t* cell_start,
                                uint32_t* rank_out, cudaStream_t st);
+// scatter + stable within-cell order + (optionally) gather of the particle state.
 cudaError_t launch_sort_by_cell(GridParams g, uint32_t n, const uint32_t* ids, SortBuffers& b, uint32_t id_bits,
                                 cudaStream_t st);
 cudaError_t launch_gather_state(uint32_t n, const uint32_t* perm, const float4* pos_in, const float4* xs_in,
@@ -128,13 +126,11 @@ cudaError_t launch_scatter_by_id(uint32_t n, const uint32_t* id, const float4* s
 cudaError_t launch_scatter_w_by_id(uint32_t n, const uint32_t* id, const float4* src, float* dst, cudaStream_t st);
 cudaError_t launch_scatter_by_id_u32(uint32_t n, const uint32_t* id, const uint32_t* src, uint32_t* dst,
                                      cudaStream_t st);
-cudaError_t launch_scatter_by_id_f32(uint32_t n, const uint32_t* id, const float* src, float* dst, cudaStream_t st);
 cudaError_t launch_list_to_ids(uint32_t total, const uint32_t* list, const uint32_t* id, uint32_t* out,
                                cudaStream_t st);
 // dst[id_off[ids[t]] + q] = src[slot_off[t] + q] for each slot t's run.
 cudaError_t launch_copy_runs(uint32_t n, const uint32_t* slot_off, const uint32_t* id_off, const uint32_t* ids,
                              const uint32_t* src, uint32_t* dst, cudaStream_t st);
-cudaError_t launch_nbr_count_sub(uint32_t n, const uint32_t* off, uint32_t* cnt, cudaStream_t st);
 
 // Metrics (max / mean density error, kinetic energy, non-finite and penetration counts).
 struct MetricsAccum {

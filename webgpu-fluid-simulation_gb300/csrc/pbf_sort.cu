@@ -1,7 +1,8 @@
 // pbf_sort.cu — integer pipeline of the neighbour search: single-pass
 // decoupled look-back exclusive scan, counting-sort scatter, stable
-// within-cell order by particle id, state gather, id-order export and the
-// per-step metrics reduction.
+// within-cell order by particle id, the stable LSD radix sort of the
+// stand-alone search, state gather, id-order export and the per-step
+// metrics reduction.
 //
 // Reference counterparts (relative to the reference root):
 //   ExclusiveScan.execute + scanShader.ts  src/simulator/neighbor/exclusiveScan.ts:134-166,
@@ -156,29 +157,6 @@ __global__ void __launch_bounds__(kScanThreads) k_scan(const uint32_t* __restric
     size_t gi = base + li;
     if (gi < n) out[gi] = s_items[li + (li >> 5)];
   }
-}
-
-// ---- insert (ParticleInsert on given positions; the step fuses this into predict) ----
-__global__ void __launch_bounds__(256) k_insert(GridParams g, const float4* __restrict__ pos, uint32_t n,
-                                                uint32_t* __restrict__ key, uint32_t* __restrict__ rank,
-                                                uint32_t* cell_count) {
-  uint32_t s = blockIdx.x * blockDim.x + threadIdx.x;
-  uint32_t k = 0xffffffffu;
-  if (s < n) {
-    float4 x = __ldg(pos + s);
-    int cx = cell_axis(x.x, g.origin[0], g.inv_cell[0], g.dim[0]);
-    int cy = cell_axis(x.y, g.origin[1], g.inv_cell[1], g.dim[1]);
-    int cz = cell_axis(x.z, g.origin[2], g.inv_cell[2], g.dim[2]);
-    k = cell_key(cx, cy, cz, g);
-    key[s] = k;
-  }
-  const uint32_t lane = threadIdx.x & 31u;
-  uint32_t peers = __match_any_sync(kFull, k);
-  uint32_t leader = __ffs(peers) - 1;
-  uint32_t b = 0;
-  if (lane == leader && k != 0xffffffffu) b = atomicAdd(cell_count + k, (uint32_t)__popc(peers));
-  b = __shfl_sync(kFull, b, leader);
-  if (s < n) rank[s] = b + (uint32_t)__popc(peers & ((1u << lane) - 1u));
 }
 
 // ---- counting-sort scatter (CountingSort, neighborShader.ts:49-60) -----------------
@@ -555,12 +533,6 @@ __global__ void k_scatter_u32(uint32_t n, const uint32_t* __restrict__ id, const
   if (t >= n) return;
   dst[id[t]] = src[t];
 }
-__global__ void k_scatter_f32(uint32_t n, const uint32_t* __restrict__ id, const float* __restrict__ src,
-                              float* __restrict__ dst) {
-  uint32_t t = blockIdx.x * blockDim.x + threadIdx.x;
-  if (t >= n) return;
-  dst[id[t]] = src[t];
-}
 __global__ void k_list_to_ids(uint32_t total, const uint32_t* __restrict__ list, const uint32_t* __restrict__ id,
                               uint32_t* __restrict__ out) {
   uint32_t q = blockIdx.x * blockDim.x + threadIdx.x;
@@ -574,12 +546,6 @@ __global__ void k_copy_runs(uint32_t n, const uint32_t* __restrict__ slot_off, c
   uint32_t b = slot_off[t], e = slot_off[t + 1], o = id_off[ids[t]];
   for (uint32_t q = b; q < e; ++q) dst[o + (q - b)] = src[q];
 }
-__global__ void k_count_from_offsets(uint32_t n, const uint32_t* __restrict__ off, uint32_t* __restrict__ cnt) {
-  uint32_t t = blockIdx.x * blockDim.x + threadIdx.x;
-  if (t >= n) return;
-  cnt[t] = off[t + 1] - off[t];
-}
-
 // ---- metrics --------------------------------------------------------------------------
 __device__ __forceinline__ void atomic_max_pos_float(float* addr, float v) {
   // v >= 0: the int ordering of non-negative floats matches their value ordering
@@ -788,13 +754,6 @@ cudaError_t launch_scan_timeout_selftest(uint32_t* err, cudaStream_t st) {
   return e == cudaSuccess ? e2 : e;
 }
 
-cudaError_t launch_insert(GridParams g, const float4* pos, uint32_t n, uint32_t* key, uint32_t* rank,
-                          uint32_t* cell_count, cudaStream_t st) {
-  if (n == 0) return cudaSuccess;
-  k_insert<<<blocks_for(n, 256), 256, 0, st>>>(g, pos, n, key, rank, cell_count);
-  return cudaGetLastError();
-}
-
 cudaError_t launch_sort_by_cell(GridParams g, uint32_t n, const uint32_t* ids, SortBuffers& b, uint32_t id_bits,
                                 cudaStream_t st) {
   cudaError_t e = launch_exclusive_scan(b.cell_count, b.cell_start, (size_t)g.cells + 1, b.scan_scratch, b.err, st);
@@ -836,11 +795,6 @@ cudaError_t launch_scatter_by_id_u32(uint32_t n, const uint32_t* id, const uint3
   k_scatter_u32<<<blocks_for(n, 256), 256, 0, st>>>(n, id, src, dst);
   return cudaGetLastError();
 }
-cudaError_t launch_scatter_by_id_f32(uint32_t n, const uint32_t* id, const float* src, float* dst, cudaStream_t st) {
-  if (n == 0) return cudaSuccess;
-  k_scatter_f32<<<blocks_for(n, 256), 256, 0, st>>>(n, id, src, dst);
-  return cudaGetLastError();
-}
 cudaError_t launch_list_to_ids(uint32_t total, const uint32_t* list, const uint32_t* id, uint32_t* out,
                                cudaStream_t st) {
   if (total == 0) return cudaSuccess;
@@ -853,12 +807,6 @@ cudaError_t launch_copy_runs(uint32_t n, const uint32_t* slot_off, const uint32_
   k_copy_runs<<<blocks_for(n, 256), 256, 0, st>>>(n, slot_off, id_off, ids, src, dst);
   return cudaGetLastError();
 }
-cudaError_t launch_nbr_count_sub(uint32_t n, const uint32_t* off, uint32_t* cnt, cudaStream_t st) {
-  if (n == 0) return cudaSuccess;
-  k_count_from_offsets<<<blocks_for(n, 256), 256, 0, st>>>(n, off, cnt);
-  return cudaGetLastError();
-}
-
 cudaError_t launch_metrics(SimParams p, FieldParams f, const float* sdf, const float4* pos, const float4* vel,
                            const uint32_t* nbr_count, uint32_t n, float* accum_f, double* accum_d, uint32_t* accum_u,
                            cudaStream_t st) {

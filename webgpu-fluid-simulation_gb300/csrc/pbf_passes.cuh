@@ -538,6 +538,44 @@ __device__ __forceinline__ void for_each_neighbor(const uint32_t* __restrict__ l
   }
 }
 
+// The same walk gathering two records per neighbour (its x_j and a second
+// per-particle float4): both loads of a batch are issued before the batch is
+// consumed.  fn(j, xj, yj).  The XSPH pass uses it for (n_j, |omega_j|)
+// (0.134 -> 0.131 ms at 2^20); in the vorticity pass, which is held to 64
+// registers, the extra live records made it slower (0.130 -> 0.137 ms).
+template <class Fn>
+__device__ __forceinline__ void for_each_neighbor2(const uint32_t* __restrict__ list, uint32_t base, uint32_t cnt,
+                                                   const float4* xs, const float4* ys, Fn&& fn) {
+  const uint32_t* l = list + base;
+  const uint32_t full = cnt & ~3u;
+  uint32_t q = 0;
+  if (full) {
+    uint32_t j0 = __ldcs(l), j1 = __ldcs(l + 32), j2 = __ldcs(l + 64), j3 = __ldcs(l + 96);
+    while (true) {
+      const float4 x0 = __ldg(xs + j0), x1 = __ldg(xs + j1), x2 = __ldg(xs + j2), x3 = __ldg(xs + j3);
+      const float4 y0 = __ldg(ys + j0), y1 = __ldg(ys + j1), y2 = __ldg(ys + j2), y3 = __ldg(ys + j3);
+      const uint32_t c0 = j0, c1 = j1, c2 = j2, c3 = j3;
+      q += 4;
+      const bool more = q < full;
+      if (more) {
+        j0 = __ldcs(l + 32 * q);
+        j1 = __ldcs(l + 32 * q + 32);
+        j2 = __ldcs(l + 32 * q + 64);
+        j3 = __ldcs(l + 32 * q + 96);
+      }
+      fn(c0, x0, y0);
+      fn(c1, x1, y1);
+      fn(c2, x2, y2);
+      fn(c3, x3, y3);
+      if (!more) break;
+    }
+  }
+  for (; q < cnt; ++q) {
+    const uint32_t j = __ldcs(l + 32 * q);
+    fn(j, __ldg(xs + j), __ldg(ys + j));
+  }
+}
+
 // Whether the boundary sample of a particle can be non-zero: per field cell,
 // 0 when all 32 volume nodes are zero (the interpolated volume is then zero)
 // or the SDF provably stays >= h over the cell; then bData = 0 exactly.
@@ -1018,9 +1056,8 @@ __global__ void __launch_bounds__(256) k_xsph_split(SimParams p, const float4* _
     uint32_t b, e;
     list_slice(max_nbr, nbr_cnt, t, b, e);
     f3 eta = mk(0.f, 0.f, 0.f), cv = mk(0.f, 0.f, 0.f);
-    for_each_neighbor(nbr_list, b, e, pos, [&](uint32_t j, float4 pj) {
+    for_each_neighbor2(nbr_list, b, e, pos, normal, [&](uint32_t, float4 pj, float4 nj) {  // nj: (normal_j, |omega_j|)
       Pair q = make_pair_of(xi - xyz(pj));
-      const float4 nj = __ldg(normal + j);  // (normal_j, |omega_j|)
       eta = eta + (nj.w * frcp_fast(pj.w)) * spiky_p(p, q);
       const float kij = p.two_rho0 * frcp_fast(ri + pj.w);
       cv = cv + kij * (ni - xyz(nj));

@@ -409,7 +409,7 @@ def gpu_arm(args, dist):
             chosen = best
     bound = learned["bound_mean_compression"] if learned else None
     e2e = _e2e_path(args, sc, snap, dist, model if chosen["learned_iters"] is not None else None,
-                    chosen["learned_iters"], bound)
+                    chosen["learned_iters"], bound, adaptive=chosen.get("adaptive", False))
     kt = chosen["passes"]
     # roofline of the dominant pass of the chosen path
     roof = None
@@ -491,11 +491,13 @@ def _handle_from(sc, snap, iterations=None):
     return sim
 
 
-def _errors_from(sc, snap, frames, model=None, iterations=None, learned_iters=2, bound=1e9):
+def _errors_from(sc, snap, frames, model=None, iterations=None, learned_iters=2, bound=1e9, adaptive=False):
     """Per-step mean compression (the metrics' density error) from a snapshot."""
     h = _handle_from(sc, snap, iterations=iterations)
     if model is not None:
         h.set_learned(model, iterations=learned_iters, fallback_bound=bound)
+        if adaptive:
+            h.set_adaptive_iterations(True)
     e = []
     for _ in range(frames):
         h.step(1)
@@ -505,7 +507,7 @@ def _errors_from(sc, snap, frames, model=None, iterations=None, learned_iters=2,
     return np.array(e), fb
 
 
-def _timed_path(args, sc, snap, dist, model=None, learned_iters=None, bound=1e9, clocks=False):
+def _timed_path(args, sc, snap, dist, model=None, learned_iters=None, bound=1e9, clocks=False, adaptive=False):
     """W warm-up and K timed frames (CUDA events on the library's stream;
     each frame replayed as a CUDA graph unless --no-graph) of the plain solve
     or, with a model, the learned start.  The pass shares come from a second
@@ -518,6 +520,8 @@ def _timed_path(args, sc, snap, dist, model=None, learned_iters=None, bound=1e9,
         h = _handle_from(sc, snap)
         if model is not None:
             h.set_learned(model, iterations=learned_iters, fallback_bound=bound)
+            if adaptive:
+                h.set_adaptive_iterations(True)
         return h
 
     sim = start()
@@ -545,6 +549,7 @@ def _timed_path(args, sc, snap, dist, model=None, learned_iters=None, bound=1e9,
     ms = dist.max(ev0.elapsed_time(ev1))
     m = sim.metrics()
     fallbacks = int(m["fallback_steps"] - fb0)
+    counts = sim.adaptive_counts() if (model is not None and adaptive) else None
     sim.close()
     sim = start()
     for _ in range(max(args.warmup, 3)):
@@ -558,10 +563,10 @@ def _timed_path(args, sc, snap, dist, model=None, learned_iters=None, bound=1e9,
     sim.close()
     return {"value": dist.world * n * sub * args.steps / (ms / 1000.0), "ms_per_step": ms / args.steps,
             "fallback_substeps": fallbacks, "timed_substeps": sub * args.steps,
-            "passes": kt, "metrics": m, "clocks": clk}
+            "adaptive_tests_updates": counts, "passes": kt, "metrics": m, "clocks": clk}
 
 
-def _e2e_path(args, sc, snap, dist, model, learned_iters, bound):
+def _e2e_path(args, sc, snap, dist, model, learned_iters, bound, adaptive=False):
     """The same frames end to end through the C ABI with host buffers: per
     frame the options struct from the host, pbf_step, and the positions copied
     to pinned host memory."""
@@ -571,6 +576,8 @@ def _e2e_path(args, sc, snap, dist, model, learned_iters, bound):
     sim = _handle_from(sc, snap)
     if model is not None:
         sim.set_learned(model, iterations=learned_iters, fallback_bound=bound)
+        if adaptive:
+            sim.set_adaptive_iterations(True)
     if args.graph:
         sim.enable_graph(True)  # pbf_set_options with unchanged options keeps the graph
     for _ in range(max(args.warmup, 3)):
@@ -598,9 +605,10 @@ def learned_arm(args, sc, snap, model, train_info, dist, plain):
     """Learned start against the plain solve at equal max density error: from
     the same input state, the plain solve's largest per-step mean compression
     over the window is the learned start's fallback bound; the learned start
-    with 2, 1 and 0 plain iterations then runs the same window (timed), each
-    falling back to the plain solve on the device in any substep that exceeds
-    it.  `_best` is the fastest learned variant whose largest per-step error
+    with 2, 1 and 0 plain iterations, and with up to 2 and 1 adaptive
+    iterations (each position update run only while the error at its start
+    exceeds the bound), then runs the same window (timed), each falling back
+    to the plain solve on the device in any substep that exceeds it.  `_best` is the fastest learned variant whose largest per-step error
     over the window is at most the plain solve's."""
     frames = max(args.warmup, 3) + args.steps
     e_plain, _ = _errors_from(sc, snap, frames)
@@ -614,20 +622,28 @@ def learned_arm(args, sc, snap, model, train_info, dist, plain):
                            "input state" if args.bound is None else "--bound",
            "density_error_same_window": {"plain": w(e_plain), "plain2": w(e_plain2)}}
     best = None
-    for li in (2, 1, 0):
-        r = _timed_path(args, sc, snap, dist, model=model, learned_iters=li, bound=bound, clocks=True)
-        e_l, _ = _errors_from(sc, snap, frames, model=model, learned_iters=li, bound=bound)
+    # (iterations, adaptive): "a" variants run each iteration's position
+    # update only while the density error at its start exceeds the bound
+    for li, ad in ((2, False), (1, False), (0, False), (2, True), (1, True)):
+        key = "learned%d%s" % (li, "a" if ad else "")
+        r = _timed_path(args, sc, snap, dist, model=model, learned_iters=li, bound=bound, clocks=True, adaptive=ad)
+        e_l, _ = _errors_from(sc, snap, frames, model=model, learned_iters=li, bound=bound, adaptive=ad)
         err = w(e_l)
         ok = err["max_step"] <= w(e_plain)["max_step"]
-        out["learned%d" % li] = {"value": r["value"], "ms_per_step": r["ms_per_step"],
-                                 "speedup_vs_plain": r["value"] / plain["value"],
-                                 "fallback_substeps": r["fallback_substeps"], "timed_substeps": r["timed_substeps"],
-                                 "density_error_same_window": err, "meets_plain_error": ok,
-                                 "passes_ms": {k: round(v[1], 4) for k, v in r["passes"].items()}}
+        out[key] = {"value": r["value"], "ms_per_step": r["ms_per_step"],
+                    "speedup_vs_plain": r["value"] / plain["value"],
+                    "fallback_substeps": r["fallback_substeps"], "timed_substeps": r["timed_substeps"],
+                    "density_error_same_window": err, "meets_plain_error": ok,
+                    "passes_ms": {k: round(v[1], 4) for k, v in r["passes"].items()}}
+        if ad:
+            tests, runs = r["adaptive_tests_updates"]
+            out[key]["adaptive"] = {"tests": tests, "position_updates_run": runs}
         if ok and (best is None or r["value"] > best["value"]):
-            best = {"name": "learned%d" % li, "learned_iters": li,
-                    "label": "learned start + %d iteration(s), fallback to the plain solve above the plain solve's "
-                             "own max per-step mean compression" % li,
+            best = {"name": key, "learned_iters": li, "adaptive": ad,
+                    "label": "learned start + %s%d iteration(s)%s, fallback to the plain solve above the plain "
+                             "solve's own max per-step mean compression"
+                             % ("up to " if ad else "", li, " (each run only while the error exceeds the bound)"
+                                if ad else ""),
                     "value": r["value"], "ms_per_step": r["ms_per_step"], "passes": r["passes"],
                     "clocks": r["clocks"]}
     e_n2, _ = _errors_from(sc, snap, frames, model=model, learned_iters=2)

@@ -420,6 +420,17 @@ int pbf_set_learned(pbf_handle* h, const pbf_mlp* model, uint32_t iterations, fl
 /* Inference kernel of the learned start's network pass (PBF_MLP_KERNEL_*;
  * default PBF_MLP_KERNEL_TCGEN05). */
 int pbf_set_mlp_kernel(pbf_handle* h, uint32_t kernel);
+/* Adaptive iterations of the learned start (no counterpart in the reference):
+ * when enabled, each of the `iterations` plain iterations after the learned
+ * projection first measures the density error at its starting positions in
+ * its lambda pass (the mean compression AttributeUpdate reports, fluid
+ * only), and runs its position update only if that error exceeds the
+ * fallback bound; otherwise the positions pass through unchanged.  The
+ * substep's final error test and fallback are unchanged.  Off by default.
+ * pbf_adaptive_counts: tests made and position updates run since the last
+ * pbf_set_adaptive_iterations (device counters, so graph replays count). */
+int pbf_set_adaptive_iterations(pbf_handle* h, int enable);
+int pbf_adaptive_counts(pbf_handle* h, uint32_t* tests, uint32_t* updates_run);
 
 /* ---- allocation-free exclusive scan.  No counterpart in the reference: an
  * addition for callers that cannot allocate device memory when they scan —

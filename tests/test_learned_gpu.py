@@ -224,3 +224,69 @@ def test_learned_graph_replay_matches_eager(bound):
         s.close()
     assert np.array_equal(out[0][0], out[1][0]) and np.array_equal(out[0][1], out[1][1])
     assert out[0][2] == out[1][2] == (4 * sc.config.substeps if bound < 0 else 0)
+
+
+def _learned_sim(sc, pts, model, iterations, bound, adaptive, graph=False, vel=None):
+    f = sc.field
+    s = PBF(sc.config)
+    s.set_particles(pts)
+    if vel is not None:
+        s.set_velocities(vel)
+    s.set_boundary_field(f["res"], f["origin"], f["extent"], f["sdf"], f["vol"])
+    s.set_learned(model, iterations=iterations, fallback_bound=bound)
+    if adaptive:
+        s.set_adaptive_iterations(True)
+    s.enable_graph(graph)
+    return s
+
+
+def test_adaptive_iterations_skip_to_the_projection():
+    """With a bound no error reaches, every adaptive test skips its position
+    update: one substep ends exactly where the learned start with no plain
+    iteration ends (exact mode), and the counters show the tests and no
+    updates."""
+    sc = scenes.reference_scene("boundary_small", fp_mode=L.FP_EXACT)
+    pts = scenes.jitter(sc.particles, 0.001, seed=14)
+    m, _, _ = random_model(11)
+    a = _learned_sim(sc, pts, m, 2, 1e9, adaptive=True)
+    b = _learned_sim(sc, pts, m, 0, 1e9, adaptive=False)
+    a.run()
+    b.run()
+    assert np.array_equal(a.positions(), b.positions())
+    assert np.array_equal(a.velocities(), b.velocities())
+    assert a.adaptive_counts() == (2, 0)
+    a.close()
+    b.close()
+
+
+def test_adaptive_iterations_run_while_needed():
+    """With a bound below the error after the projection, the first update
+    runs and the test is repeated per iteration; the results are the same
+    eagerly and from a CUDA graph, and at the end the final error test of
+    each substep either passes or falls back."""
+    sc = scenes.reference_scene("boundary_small", fp_mode=L.FP_EXACT)
+    settle = PBF(sc.config)  # a compressed state: the block after falling onto the floor
+    f = sc.field
+    settle.set_particles(scenes.jitter(sc.particles, 0.001, seed=15))
+    settle.set_boundary_field(f["res"], f["origin"], f["extent"], f["sdf"], f["vol"])
+    settle.step(60)
+    pts, vel = settle.positions(), settle.velocities()
+    settle.close()
+    m, _, _ = random_model(13)
+    probe = _learned_sim(sc, pts, m, 0, 1e9, adaptive=False, vel=vel)
+    probe.run()
+    e0 = probe.metrics()["mean_compression"]  # the error after the projection alone
+    probe.close()
+    assert e0 > 0.0
+    bound = 0.5 * e0
+    out = []
+    for graph in (False, True):
+        s = _learned_sim(sc, pts, m, 2, bound, adaptive=True, graph=graph, vel=vel)
+        s.step(3)
+        tests, runs = s.adaptive_counts()
+        out.append((s.positions(), s.velocities(), tests, runs, s.metrics()["fallback_steps"]))
+        s.close()
+    assert np.array_equal(out[0][0], out[1][0]) and np.array_equal(out[0][1], out[1][1])
+    assert out[0][2:] == out[1][2:]
+    tests, runs = out[0][2], out[0][3]
+    assert tests == 2 * 3 * sc.config.substeps and 1 <= runs <= tests

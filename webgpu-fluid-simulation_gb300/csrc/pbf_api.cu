@@ -88,6 +88,12 @@ struct pbf_handle {
   uint32_t mlp_kernel = PBF_MLP_KERNEL_TCGEN05;  // network pass of the learned start
   uint32_t learned_iters = 2;
   float fallback_bound = 0.01f;
+  // adaptive iterations (pbf_set_adaptive_iterations): each of the learned
+  // start's iterations runs its position update only while the density error
+  // at its start exceeds the fallback bound.  stats[1], fb_flag[1] and
+  // fb_mean[1] hold the test's statistics, flag and last mean; fb_count[1..2]
+  // count the tests and the updates run (on the device: graph replays count).
+  bool adaptive = false;
   pbf_mlp model;
   DBuf<float> mlp_params, lam_sum, lam_prev, bsdf, fb_mean;
   DBuf<float4> feat, xs_save, pos_save;
@@ -434,7 +440,7 @@ int substep(pbf_handle* h, cudaEvent_t* ev) {
   // (feat_first) and/or starts lam_sum; stats go with the last one.  Each
   // delta-p but the last marks the band of the next iteration.
   auto iterate = [&](int a, uint32_t iters, bool feat_first, bool lam_sum_on, bool first_starts_sum,
-                     SolveStats* stats, int* rc) -> int {
+                     SolveStats* stats, int* rc, bool adaptive = false) -> int {
     for (uint32_t it = 0; it < iters; ++it) {
       if (f.loaded && sample_boundary(a, (need_feat && feat_first && it == 0) ? h->bsdf.p : nullptr) !=
                           cudaSuccess) {
@@ -449,6 +455,7 @@ int substep(pbf_handle* h, cudaEvent_t* ev) {
         al.lam_first = (first_starts_sum && it == 0) ? 1 : 0;
       }
       if (stats && it + 1 == iters) al.stats = stats;
+      if (adaptive) al.stats = h->stats.p + 1;  // the density error at this iteration's start
       const bool fe = feat_first && it == 0;
       if (fe) {
         al.feat = h->feat.p;
@@ -468,6 +475,15 @@ int substep(pbf_handle* h, cudaEvent_t* ev) {
       ad.tab = h->tab;
       ad.iter = (int)it;
       ad.xs_in = h->xs[a].p;
+      if (adaptive) {
+        // flag [1] = error above the bound: the position update runs (and is counted)
+        if (launch_iterate_decide(h->stats.p + 1, h->fallback_bound, h->fb_flag.p + 1, h->fb_count.p + 1,
+                                  h->fb_mean.p + 1, st) != cudaSuccess) {
+          *rc = PBF_ECUDA;
+          return a;
+        }
+        ad.need = h->fb_flag.p + 1;
+      }
       if (f.loaded && it + 1 < iters) {  // the next iteration's band, at the positions written now
         ad.band = band_args(1 - band, nullptr);
         band = 1 - band;
@@ -508,7 +524,7 @@ int substep(pbf_handle* h, cudaEvent_t* ev) {
                                                    h->nbr_list.p, h->xs[1].p, nullptr);
     }
     CU(h, cudaGetLastError());
-    a = iterate(1, h->learned_iters, false, true, false, nullptr, &rc);
+    a = iterate(1, h->learned_iters, false, true, false, nullptr, &rc, h->adaptive);
     if (rc) return fail(h, rc, "learned solve launch failed");
   } else {
     a = iterate(0, h->cfg.options.iterations, need_feat, need_feat, true, nullptr, &rc);
@@ -1545,14 +1561,17 @@ int pbf_set_learned(pbf_handle* h, const pbf_mlp* model, uint32_t iterations, fl
     CU(h, h->mlp_params.alloc(PBF_MLP_PARAMS));
     CU(h, h->xs_save.alloc(cap));
     CU(h, h->pos_save.alloc(cap));
-    if (!h->stats.p) CU(h, h->stats.alloc(1));
-    CU(h, h->fb_flag.alloc(1));
-    CU(h, h->fb_count.alloc(1));
-    CU(h, h->fb_mean.alloc(1));
-    CU(h, cudaMemsetAsync(h->stats.p, 0, sizeof(SolveStats), h->stream));
-    CU(h, cudaMemsetAsync(h->fb_flag.p, 0, sizeof(int), h->stream));
-    CU(h, cudaMemsetAsync(h->fb_count.p, 0, sizeof(uint32_t), h->stream));
-    CU(h, cudaMemsetAsync(h->fb_mean.p, 0, sizeof(float), h->stream));
+    if (h->stats.n < 2) {
+      h->stats.release();
+      CU(h, h->stats.alloc(2));
+    }
+    CU(h, h->fb_flag.alloc(2));
+    CU(h, h->fb_count.alloc(3));
+    CU(h, h->fb_mean.alloc(2));
+    CU(h, cudaMemsetAsync(h->stats.p, 0, 2 * sizeof(SolveStats), h->stream));
+    CU(h, cudaMemsetAsync(h->fb_flag.p, 0, 2 * sizeof(int), h->stream));
+    CU(h, cudaMemsetAsync(h->fb_count.p, 0, 3 * sizeof(uint32_t), h->stream));
+    CU(h, cudaMemsetAsync(h->fb_mean.p, 0, 2 * sizeof(float), h->stream));
   }
   h->model = *model;
   CU(h, cudaMemcpyAsync(h->mlp_params.p, model->params, sizeof(model->params), cudaMemcpyHostToDevice, h->stream));
@@ -1560,6 +1579,32 @@ int pbf_set_learned(pbf_handle* h, const pbf_mlp* model, uint32_t iterations, fl
   h->learned_iters = iterations;
   h->fallback_bound = fallback_bound;
   h->learned = true;
+  return PBF_OK;
+}
+
+int pbf_set_adaptive_iterations(pbf_handle* h, int enable) {
+  if (!h) return PBF_EINVAL;
+  if (h->batch) return not_for_batch(h, "pbf_set_adaptive_iterations");
+  if ((enable != 0) != h->adaptive) invalidate_graph(h);
+  h->adaptive = enable != 0;
+  if (h->fb_count.p) {  // restart the test counters
+    CU(h, cudaMemsetAsync(h->fb_count.p + 1, 0, 2 * sizeof(uint32_t), h->stream));
+    CU(h, cudaStreamSynchronize(h->stream));
+  }
+  return PBF_OK;
+}
+
+int pbf_adaptive_counts(pbf_handle* h, uint32_t* tests, uint32_t* updates_run) {
+  if (!h || !tests || !updates_run) return PBF_EINVAL;
+  *tests = 0;
+  *updates_run = 0;
+  if (h->fb_count.p) {
+    uint32_t c[3];
+    CU(h, cudaStreamSynchronize(h->stream));
+    CU(h, cudaMemcpy(c, h->fb_count.p, sizeof(c), cudaMemcpyDeviceToHost));
+    *tests = c[1];
+    *updates_run = c[2];
+  }
   return PBF_OK;
 }
 

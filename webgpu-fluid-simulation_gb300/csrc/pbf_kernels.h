@@ -165,6 +165,9 @@ cudaError_t launch_mlp_grad(const float* d_params, const pbf_mlp& model, const f
 cudaError_t launch_gather_f32(uint32_t n, const uint32_t* perm, const float* src, float* dst, cudaStream_t st);
 cudaError_t launch_fallback_decide(SolveStats* stats, float bound, int* flag, uint32_t* fallbacks, float* last_mean,
                                    cudaStream_t st);
+// The adaptive iteration's test (counts[0] tests, counts[1] position updates run).
+cudaError_t launch_iterate_decide(SolveStats* stats, float bound, int* flag, uint32_t* counts, float* last_mean,
+                                  cudaStream_t st);
 cudaError_t launch_stats_record(SolveStats* stats, float* rec, cudaStream_t st);
 cudaError_t launch_trace_append(uint32_t n, const uint32_t* ids, const float4* feat, const float* lam_sum,
                                 uint32_t stride, uint32_t salt, float* tf, float* tt, uint32_t* count, uint32_t cap,

@@ -354,6 +354,22 @@ __global__ void k_fallback_decide(SolveStats* stats, float bound, int* flag, uin
   stats->sum_fx = 0ull;
 }
 
+// The adaptive iteration's test: the position update runs (*flag = 1) when
+// the mean compression at the iteration's start exceeds the bound; counts[0]
+// counts the tests, counts[1] the updates run.  Resets the statistics.
+__global__ void k_iterate_decide(SolveStats* stats, float bound, int* flag, uint32_t* counts, float* last_mean) {
+  unsigned cnt = stats->count;
+  double mean = cnt ? (double)stats->sum_fx / 1048576.0 / (double)cnt : 0.0;
+  int f = mean > (double)bound ? 1 : 0;
+  *flag = f;
+  counts[0] += 1u;
+  counts[1] += (uint32_t)f;
+  *last_mean = (float)mean;
+  stats->max_bits = 0u;
+  stats->count = 0u;
+  stats->sum_fx = 0ull;
+}
+
 // Records a plain solve's in-solve mean compression (trace capture): running
 // max and sum over substeps, then resets the statistics.
 __global__ void k_stats_record(SolveStats* stats, float* rec) {
@@ -400,6 +416,11 @@ cudaError_t launch_gather_f32(uint32_t n, const uint32_t* perm, const float* src
 cudaError_t launch_fallback_decide(SolveStats* stats, float bound, int* flag, uint32_t* fallbacks, float* last_mean,
                                    cudaStream_t st) {
   k_fallback_decide<<<1, 1, 0, st>>>(stats, bound, flag, fallbacks, last_mean);
+  return cudaGetLastError();
+}
+cudaError_t launch_iterate_decide(SolveStats* stats, float bound, int* flag, uint32_t* counts, float* last_mean,
+                                  cudaStream_t st) {
+  k_iterate_decide<<<1, 1, 0, st>>>(stats, bound, flag, counts, last_mean);
   return cudaGetLastError();
 }
 cudaError_t launch_stats_record(SolveStats* stats, float* rec, cudaStream_t st) {

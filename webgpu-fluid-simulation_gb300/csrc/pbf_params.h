@@ -108,6 +108,7 @@ struct SolverAux {
   int iter;                  // solver iteration of this launch (scenes with fewer iterations skip it)
   const float4* xs_in;       // delta-p pass: x* of a scene that skips the iteration is copied through
   BandArgs band;             // delta-p pass: the band of the next iteration's boundary sampling
+  const int* need;           // delta-p pass: *need == 0 skips the iteration (x* copied through from xs_in)
 };
 
 // The learned start's fallback: the plain solve of one substep from the saved

@@ -684,6 +684,41 @@ __global__ void __launch_bounds__(256, 2) k_boundary_band(SimParams p, FieldPara
   }
 }
 
+// Per-step density error statistics (compression max(0, V sum W - 1), fluid
+// only): each thread's running max / fixed-point sum / count, reduced over
+// the CTA in shared memory, one set of atomics per CTA.  Every thread of the
+// CTA calls it.
+__device__ __forceinline__ void compression_add(unsigned& cmax, unsigned& csum, unsigned& ccnt, float vsum_times_v) {
+  const float c = fmaxf(0.0f, vsum_times_v - 1.0f);
+  cmax = max(cmax, __float_as_uint(c));  // non-negative floats order as their bits
+  csum += (unsigned)(fminf(c, 1.0f) * 1048576.0f);
+  ++ccnt;
+}
+__device__ __forceinline__ void compression_flush(SolveStats* stats, unsigned cmax, unsigned csum, unsigned ccnt) {
+  __shared__ unsigned s_max, s_cnt;
+  __shared__ unsigned long long s_sum;
+  if (threadIdx.x == 0) {
+    s_max = 0u;
+    s_cnt = 0u;
+    s_sum = 0ull;
+  }
+  __syncthreads();
+  cmax = __reduce_max_sync(0xffffffffu, cmax);
+  csum = __reduce_add_sync(0xffffffffu, csum);
+  ccnt = __reduce_add_sync(0xffffffffu, ccnt);
+  if ((threadIdx.x & 31u) == 0) {
+    atomicMax(&s_max, cmax);
+    atomicAdd(&s_cnt, ccnt);
+    atomicAdd(&s_sum, (unsigned long long)csum);
+  }
+  __syncthreads();
+  if (threadIdx.x == 0 && s_cnt) {
+    atomicMax(&stats->max_bits, s_max);
+    atomicAdd(&stats->count, s_cnt);
+    atomicAdd(&stats->sum_fx, s_sum);
+  }
+}
+
 // LambdaCalculation (pressureConstrain.ts:31-85).  Writes xl[t] = (x*, lambda):
 // the next pass gathers a neighbour's position and multiplier in one load.
 //   kMode 0: the reference pass.
@@ -693,7 +728,7 @@ __global__ void __launch_bounds__(256, 2) k_boundary_band(SimParams p, FieldPara
 //            v' = (x* - x)/dt) for trace capture.
 
 template <int kMode, bool kC>
-__device__ __forceinline__ void lambda_slot(const SimParams& p, int have_field, const float4* bdata, const float4* xs,
+__device__ __forceinline__ float lambda_slot(const SimParams& p, int have_field, const float4* bdata, const float4* xs,
                                             uint32_t max_nbr, const uint32_t* __restrict__ nbr_cnt,
                                             const uint32_t* __restrict__ nbr_list, float4* xl, const SolverAux& a,
                                             uint32_t t) {
@@ -710,6 +745,7 @@ __device__ __forceinline__ void lambda_slot(const SimParams& p, int have_field, 
     sum2 = sum2 + dot3(gk, gk);
     dens = dens + poly6_p(p, q);
   });
+  const float vsum = dens;
   dens = dens * p.V;
   const float dens_fluid = dens;
   grad = p.V * grad;
@@ -737,6 +773,7 @@ __device__ __forceinline__ void lambda_slot(const SimParams& p, int have_field, 
     a.feat[2 * t] = make_float4(dens - 1.0f, a.lam_prev ? a.lam_prev[t] : 0.0f, (float)e, len3(vi) * p.dt / p.h);
     a.feat[2 * t + 1] = make_float4(divergence_feature(p, xo, dens_fluid), sd / p.h, vb / p.V, a.substep_index);
   }
+  return vsum;
 }
 
 template <int kMode, bool kBatch, bool kLoop>
@@ -746,10 +783,15 @@ __global__ void __launch_bounds__(256) k_lambda(SimParams p, int have_field, con
                                                 const uint32_t* __restrict__ nbr_list,
                                                 float4* __restrict__ xl, SolverAux a) {
   if (a.guard && *a.guard == 0) return;
+  // with a.stats: the density error at these positions (the adaptive
+  // iteration's test; the same quantity AttributeUpdate reports)
+  unsigned cmax = 0u, csum = 0u, ccnt = 0u;
   PBF_SLOTS(t, p.n) {
     if (!iter_active(scene_of<kBatch>(a.tab, t), a.iter)) continue;
-    lambda_slot<kMode, false>(p, have_field, bdata, xs, max_nbr, nbr_cnt, nbr_list, xl, a, t);
+    const float vsum = lambda_slot<kMode, false>(p, have_field, bdata, xs, max_nbr, nbr_cnt, nbr_list, xl, a, t);
+    if (a.stats) compression_add(cmax, csum, ccnt, vsum * p.V);
   }
+  if (a.stats) compression_flush(a.stats, cmax, csum, ccnt);
 }
 
 // ConstrainSolve + ConstrainApply: x*_new = clamp(x* + 0.5 * dp) into the other
@@ -790,8 +832,9 @@ __global__ void __launch_bounds__(256) k_deltap(SimParams p, SolverAux a, int ha
                                                 const uint32_t* __restrict__ nbr_list,
                                                 float4* __restrict__ xs_out, float4* __restrict__ dp_out) {
   if (a.guard && *a.guard == 0) return;
+  const bool skip = a.need && *a.need == 0;  // the adaptive test found this iteration unneeded
   PBF_SLOTS(t, p.n) {
-    if (!iter_active(scene_of<kBatch>(a.tab, t), a.iter)) {
+    if (skip || !iter_active(scene_of<kBatch>(a.tab, t), a.iter)) {
       xs_out[t] = a.xs_in[t];
       continue;
     }
@@ -847,37 +890,9 @@ __global__ void __launch_bounds__(256) k_density_velocity(SimParams p, SolverAux
   unsigned cmax = 0u, csum = 0u, ccnt = 0u;
   PBF_SLOTS(t, p.n) {
     const float vsum = density_slot<false>(p, xs, max_nbr, nbr_cnt, nbr_list, pos, vel, t);
-    if (a.stats) {
-      float c = fmaxf(0.0f, vsum * p.V - 1.0f);
-      cmax = max(cmax, __float_as_uint(c));  // non-negative floats order as their bits
-      csum += (unsigned)(fminf(c, 1.0f) * 1048576.0f);
-      ++ccnt;
-    }
+    if (a.stats) compression_add(cmax, csum, ccnt, vsum * p.V);
   }
-  if (a.stats) {
-    __shared__ unsigned s_max, s_cnt;
-    __shared__ unsigned long long s_sum;
-    if (threadIdx.x == 0) {
-      s_max = 0u;
-      s_cnt = 0u;
-      s_sum = 0ull;
-    }
-    __syncthreads();
-    cmax = __reduce_max_sync(0xffffffffu, cmax);
-    csum = __reduce_add_sync(0xffffffffu, csum);
-    ccnt = __reduce_add_sync(0xffffffffu, ccnt);
-    if ((threadIdx.x & 31u) == 0) {
-      atomicMax(&s_max, cmax);
-      atomicAdd(&s_cnt, ccnt);
-      atomicAdd(&s_sum, (unsigned long long)csum);
-    }
-    __syncthreads();
-    if (threadIdx.x == 0 && s_cnt) {
-      atomicMax(&a.stats->max_bits, s_max);
-      atomicAdd(&a.stats->count, s_cnt);
-      atomicAdd(&a.stats->sum_fx, s_sum);
-    }
-  }
+  if (a.stats) compression_flush(a.stats, cmax, csum, ccnt);
 }
 
 // The learned start's fallback: when *guard is set, restores x and x*_0 and

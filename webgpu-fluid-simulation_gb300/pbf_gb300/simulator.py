@@ -264,6 +264,17 @@ class PBF:
         m = None if model is None else ctypes.byref(model)
         self._check(self._lib.pbf_set_learned(self._h, m, int(iterations), float(fallback_bound)), "set_learned")
 
+    def set_adaptive_iterations(self, enable=True):
+        """Run each learned-start iteration's position update only while the
+        density error at its start exceeds the fallback bound."""
+        self._check(self._lib.pbf_set_adaptive_iterations(self._h, 1 if enable else 0), "set_adaptive_iterations")
+
+    def adaptive_counts(self):
+        """(tests made, position updates run) since set_adaptive_iterations."""
+        t, r = ctypes.c_uint32(), ctypes.c_uint32()
+        self._check(self._lib.pbf_adaptive_counts(self._h, ctypes.byref(t), ctypes.byref(r)), "adaptive_counts")
+        return t.value, r.value
+
     def update(self):
         return None
 

@@ -409,7 +409,8 @@ def gpu_arm(args, dist):
             chosen = best
     bound = learned["bound_mean_compression"] if learned else None
     e2e = _e2e_path(args, sc, snap, dist, model if chosen["learned_iters"] is not None else None,
-                    chosen["learned_iters"], bound, adaptive=chosen.get("adaptive", False))
+                    chosen["learned_iters"], bound, adaptive=chosen.get("adaptive", False),
+                    lagged=chosen.get("lagged", 0.0))
     kt = chosen["passes"]
     # roofline of the dominant pass of the chosen path
     roof = None
@@ -491,13 +492,16 @@ def _handle_from(sc, snap, iterations=None):
     return sim
 
 
-def _errors_from(sc, snap, frames, model=None, iterations=None, learned_iters=2, bound=1e9, adaptive=False):
+def _errors_from(sc, snap, frames, model=None, iterations=None, learned_iters=2, bound=1e9, adaptive=False,
+                 lagged=0.0):
     """Per-step mean compression (the metrics' density error) from a snapshot."""
     h = _handle_from(sc, snap, iterations=iterations)
     if model is not None:
         h.set_learned(model, iterations=learned_iters, fallback_bound=bound)
         if adaptive:
             h.set_adaptive_iterations(True)
+        if lagged > 0.0:
+            h.set_lagged_iterations(lagged)
     e = []
     for _ in range(frames):
         h.step(1)
@@ -507,7 +511,8 @@ def _errors_from(sc, snap, frames, model=None, iterations=None, learned_iters=2,
     return np.array(e), fb
 
 
-def _timed_path(args, sc, snap, dist, model=None, learned_iters=None, bound=1e9, clocks=False, adaptive=False):
+def _timed_path(args, sc, snap, dist, model=None, learned_iters=None, bound=1e9, clocks=False, adaptive=False,
+                lagged=0.0):
     """W warm-up and K timed frames (CUDA events on the library's stream;
     each frame replayed as a CUDA graph unless --no-graph) of the plain solve
     or, with a model, the learned start.  The pass shares come from a second
@@ -522,6 +527,8 @@ def _timed_path(args, sc, snap, dist, model=None, learned_iters=None, bound=1e9,
             h.set_learned(model, iterations=learned_iters, fallback_bound=bound)
             if adaptive:
                 h.set_adaptive_iterations(True)
+            if lagged > 0.0:
+                h.set_lagged_iterations(lagged)
         return h
 
     sim = start()
@@ -549,7 +556,7 @@ def _timed_path(args, sc, snap, dist, model=None, learned_iters=None, bound=1e9,
     ms = dist.max(ev0.elapsed_time(ev1))
     m = sim.metrics()
     fallbacks = int(m["fallback_steps"] - fb0)
-    counts = sim.adaptive_counts() if (model is not None and adaptive) else None
+    counts = sim.adaptive_counts() if (model is not None and (adaptive or lagged > 0.0)) else None
     sim.close()
     sim = start()
     for _ in range(max(args.warmup, 3)):
@@ -566,7 +573,7 @@ def _timed_path(args, sc, snap, dist, model=None, learned_iters=None, bound=1e9,
             "adaptive_tests_updates": counts, "passes": kt, "metrics": m, "clocks": clk}
 
 
-def _e2e_path(args, sc, snap, dist, model, learned_iters, bound, adaptive=False):
+def _e2e_path(args, sc, snap, dist, model, learned_iters, bound, adaptive=False, lagged=0.0):
     """The same frames end to end through the C ABI with host buffers: per
     frame the options struct from the host, pbf_step, and the positions copied
     to pinned host memory."""
@@ -578,6 +585,8 @@ def _e2e_path(args, sc, snap, dist, model, learned_iters, bound, adaptive=False)
         sim.set_learned(model, iterations=learned_iters, fallback_bound=bound)
         if adaptive:
             sim.set_adaptive_iterations(True)
+        if lagged > 0.0:
+            sim.set_lagged_iterations(lagged)
     if args.graph:
         sim.enable_graph(True)  # pbf_set_options with unchanged options keeps the graph
     for _ in range(max(args.warmup, 3)):
@@ -624,10 +633,15 @@ def learned_arm(args, sc, snap, model, train_info, dist, plain):
     best = None
     # (iterations, adaptive): "a" variants run each iteration's position
     # update only while the density error at its start exceeds the bound
-    for li, ad in ((2, False), (1, False), (0, False), (2, True), (1, True)):
-        key = "learned%d%s" % (li, "a" if ad else "")
-        r = _timed_path(args, sc, snap, dist, model=model, learned_iters=li, bound=bound, clocks=True, adaptive=ad)
-        e_l, _ = _errors_from(sc, snap, frames, model=model, learned_iters=li, bound=bound, adaptive=ad)
+    # "l" variants: a substep iterates only when the previous substep's final
+    # error exceeded the given fraction of the bound
+    for li, ad, lag in ((2, False, 0.0), (1, False, 0.0), (0, False, 0.0), (2, True, 0.0), (1, True, 0.0),
+                        (1, False, 0.3)):
+        key = "learned%d%s" % (li, "a" if ad else ("l%02d" % round(100 * lag) if lag > 0.0 else ""))
+        r = _timed_path(args, sc, snap, dist, model=model, learned_iters=li, bound=bound, clocks=True, adaptive=ad,
+                        lagged=lag)
+        e_l, _ = _errors_from(sc, snap, frames, model=model, learned_iters=li, bound=bound, adaptive=ad,
+                              lagged=lag)
         err = w(e_l)
         ok = err["max_step"] <= w(e_plain)["max_step"]
         out[key] = {"value": r["value"], "ms_per_step": r["ms_per_step"],
@@ -638,12 +652,17 @@ def learned_arm(args, sc, snap, model, train_info, dist, plain):
         if ad:
             tests, runs = r["adaptive_tests_updates"]
             out[key]["adaptive"] = {"tests": tests, "position_updates_run": runs}
+        if lag > 0.0:
+            tests, runs = r["adaptive_tests_updates"]
+            out[key]["lagged"] = {"fraction_of_bound": lag, "substeps": tests, "substeps_iterated": runs}
         if ok and (best is None or r["value"] > best["value"]):
-            best = {"name": key, "learned_iters": li, "adaptive": ad,
+            best = {"name": key, "learned_iters": li, "adaptive": ad, "lagged": lag,
                     "label": "learned start + %s%d iteration(s)%s, fallback to the plain solve above the plain "
                              "solve's own max per-step mean compression"
-                             % ("up to " if ad else "", li, " (each run only while the error exceeds the bound)"
-                                if ad else ""),
+                             % ("up to " if (ad or lag > 0.0) else "", li,
+                                " (each run only while the error exceeds the bound)" if ad else
+                                (" (run when the previous substep's error exceeded %.2f of the bound)" % lag
+                                 if lag > 0.0 else "")),
                     "value": r["value"], "ms_per_step": r["ms_per_step"], "passes": r["passes"],
                     "clocks": r["clocks"]}
     e_n2, _ = _errors_from(sc, snap, frames, model=model, learned_iters=2)

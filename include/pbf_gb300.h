@@ -430,6 +430,16 @@ int pbf_set_mlp_kernel(pbf_handle* h, uint32_t kernel);
  * pbf_adaptive_counts: tests made and position updates run since the last
  * pbf_set_adaptive_iterations (device counters, so graph replays count). */
 int pbf_set_adaptive_iterations(pbf_handle* h, int enable);
+/* Lagged iteration control of the learned start (no counterpart in the
+ * reference): with fraction > 0, a substep runs its plain iterations
+ * (boundary sampling, lambda, delta-p) only when the previous substep's final
+ * mean compression exceeded fraction x the fallback bound; otherwise it keeps
+ * the learned projection alone.  The decision uses the error AttributeUpdate
+ * already measured (no extra neighbour pass); the final error test and
+ * fallback are unchanged.  fraction <= 0 turns it off (default); it takes
+ * precedence over pbf_set_adaptive_iterations.  pbf_adaptive_counts then
+ * reports decisions made and substeps that iterated. */
+int pbf_set_lagged_iterations(pbf_handle* h, float fraction);
 int pbf_adaptive_counts(pbf_handle* h, uint32_t* tests, uint32_t* updates_run);
 
 /* ---- allocation-free exclusive scan.  No counterpart in the reference: an

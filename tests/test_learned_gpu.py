@@ -290,3 +290,42 @@ def test_adaptive_iterations_run_while_needed():
     assert out[0][2:] == out[1][2:]
     tests, runs = out[0][2], out[0][3]
     assert tests == 2 * 3 * sc.config.substeps and 1 <= runs <= tests
+
+
+def test_lagged_iterations_never_and_always():
+    """Lagged iteration control: with a threshold no error reaches, every
+    substep keeps the projection alone (bit for bit the learned start with no
+    iteration, over several substeps); with a tiny threshold every substep
+    after the first iterates, identically eager and from a CUDA graph."""
+    sc = scenes.reference_scene("boundary_small", fp_mode=L.FP_EXACT)
+    pts = scenes.jitter(sc.particles, 0.001, seed=16)
+    m, _, _ = random_model(17)
+    a = _learned_sim(sc, pts, m, 1, 1e9, adaptive=False)
+    a.set_lagged_iterations(1.0)  # threshold 1e9: never iterates
+    b = _learned_sim(sc, pts, m, 0, 1e9, adaptive=False)
+    for _ in range(4):
+        a.run()
+        b.run()
+    assert np.array_equal(a.positions(), b.positions())
+    assert np.array_equal(a.velocities(), b.velocities())
+    assert a.adaptive_counts() == (4, 0)
+    a.close()
+    b.close()
+    settle = PBF(sc.config)  # a compressed state: the block after falling onto the floor
+    f = sc.field
+    settle.set_particles(pts)
+    settle.set_boundary_field(f["res"], f["origin"], f["extent"], f["sdf"], f["vol"])
+    settle.step(60)
+    x, v = settle.positions(), settle.velocities()
+    settle.close()
+    out = []
+    for graph in (False, True):
+        s = _learned_sim(sc, x, m, 1, 1e9, adaptive=False, graph=graph, vel=v)
+        s.set_lagged_iterations(1e-15)  # threshold 1e-15 x 1e9 = 1e-6: iterates once any compression was seen
+        s.step(3)
+        out.append((s.positions(), s.velocities(), s.adaptive_counts()))
+        s.close()
+    assert np.array_equal(out[0][0], out[1][0]) and np.array_equal(out[0][1], out[1][1])
+    n_sub = 3 * sc.config.substeps
+    # the first substep has no previous error (it keeps the projection); the others iterate
+    assert out[0][2] == out[1][2] == (n_sub, n_sub - 1)

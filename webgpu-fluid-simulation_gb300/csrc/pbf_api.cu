@@ -94,6 +94,11 @@ struct pbf_handle {
   // fb_mean[1] hold the test's statistics, flag and last mean; fb_count[1..2]
   // count the tests and the updates run (on the device: graph replays count).
   bool adaptive = false;
+  // lagged iteration control (pbf_set_lagged_iterations): a substep's
+  // iterations run only when the previous substep's final mean compression
+  // (fb_mean[0]) exceeded lagged_fraction x the bound; 0 = off.  Uses the same
+  // flag and counters as the adaptive test.
+  float lagged_fraction = 0.0f;
   pbf_mlp model;
   DBuf<float> mlp_params, lam_sum, lam_prev, bsdf, fb_mean;
   DBuf<float4> feat, xs_save, pos_save;
@@ -390,8 +395,9 @@ int substep(pbf_handle* h, cudaEvent_t* ev) {
     B.count = h->band_count.p + list;
     return B;
   };
-  // Boundary sampling at x*_a (bsdf: also the SDF feature).
-  auto sample_boundary = [&](int a, float* bsdf) -> cudaError_t {
+  // Boundary sampling at x*_a (bsdf: also the SDF feature); guard: the
+  // lagged iteration control's flag (the sampling is skipped with it).
+  auto sample_boundary = [&](int a, float* bsdf, const int* guard = nullptr) -> cudaError_t {
     KScope ks(h, K_BOUNDARY);
     if (band < 0) {
       ps.band<<<grid_of(h, n), h->blk, 0, st>>>(p, h->tab, h->xs[a].p, band_args(0, bsdf));
@@ -399,7 +405,7 @@ int substep(pbf_handle* h, cudaEvent_t* ev) {
     }
     ps.boundary_band<<<band_grid, 256, 0, st>>>(p, f, h->sdf.p, h->vol.p, h->tab, h->xs[a].p, h->bdata.p, bsdf,
                                                  h->band_list[band].p, h->band_count.p + band,
-                                                 h->band_count.p + (1 - band));
+                                                 h->band_count.p + (1 - band), guard);
     return cudaGetLastError();
   };
   // NeighborCount + NeighborList in one pass (fixed per-particle slices: no
@@ -440,9 +446,19 @@ int substep(pbf_handle* h, cudaEvent_t* ev) {
   // (feat_first) and/or starts lam_sum; stats go with the last one.  Each
   // delta-p but the last marks the band of the next iteration.
   auto iterate = [&](int a, uint32_t iters, bool feat_first, bool lam_sum_on, bool first_starts_sum,
-                     SolveStats* stats, int* rc, bool adaptive = false) -> int {
+                     SolveStats* stats, int* rc, bool adaptive = false, bool lagged = false) -> int {
+    const int* lag = nullptr;  // lagged control: every pass of the iterations is guarded by this flag
+    if (lagged && iters > 0) {
+      if (launch_lagged_decide(h->fb_mean.p, h->lagged_fraction * h->fallback_bound, h->fb_flag.p + 1,
+                               h->fb_count.p + 1, st) != cudaSuccess) {
+        *rc = PBF_ECUDA;
+        return a;
+      }
+      lag = h->fb_flag.p + 1;
+      adaptive = false;
+    }
     for (uint32_t it = 0; it < iters; ++it) {
-      if (f.loaded && sample_boundary(a, (need_feat && feat_first && it == 0) ? h->bsdf.p : nullptr) !=
+      if (f.loaded && sample_boundary(a, (need_feat && feat_first && it == 0) ? h->bsdf.p : nullptr, lag) !=
                           cudaSuccess) {
         *rc = PBF_ECUDA;
         return a;
@@ -450,6 +466,7 @@ int substep(pbf_handle* h, cudaEvent_t* ev) {
       SolverAux al{};
       al.tab = h->tab;
       al.iter = (int)it;
+      al.guard = lag;
       if (lam_sum_on) {
         al.lam_sum = h->lam_sum.p;
         al.lam_first = (first_starts_sum && it == 0) ? 1 : 0;
@@ -475,6 +492,7 @@ int substep(pbf_handle* h, cudaEvent_t* ev) {
       ad.tab = h->tab;
       ad.iter = (int)it;
       ad.xs_in = h->xs[a].p;
+      ad.need = lag;
       if (adaptive) {
         // flag [1] = error above the bound: the position update runs (and is counted)
         if (launch_iterate_decide(h->stats.p + 1, h->fallback_bound, h->fb_flag.p + 1, h->fb_count.p + 1,
@@ -524,7 +542,7 @@ int substep(pbf_handle* h, cudaEvent_t* ev) {
                                                    h->nbr_list.p, h->xs[1].p, nullptr);
     }
     CU(h, cudaGetLastError());
-    a = iterate(1, h->learned_iters, false, true, false, nullptr, &rc, h->adaptive);
+    a = iterate(1, h->learned_iters, false, true, false, nullptr, &rc, h->adaptive, h->lagged_fraction > 0.0f);
     if (rc) return fail(h, rc, "learned solve launch failed");
   } else {
     a = iterate(0, h->cfg.options.iterations, need_feat, need_feat, true, nullptr, &rc);
@@ -1588,6 +1606,20 @@ int pbf_set_adaptive_iterations(pbf_handle* h, int enable) {
   if ((enable != 0) != h->adaptive) invalidate_graph(h);
   h->adaptive = enable != 0;
   if (h->fb_count.p) {  // restart the test counters
+    CU(h, cudaMemsetAsync(h->fb_count.p + 1, 0, 2 * sizeof(uint32_t), h->stream));
+    CU(h, cudaStreamSynchronize(h->stream));
+  }
+  return PBF_OK;
+}
+
+int pbf_set_lagged_iterations(pbf_handle* h, float fraction) {
+  if (!h) return PBF_EINVAL;
+  if (h->batch) return not_for_batch(h, "pbf_set_lagged_iterations");
+  if (!std::isfinite(fraction)) return fail(h, PBF_EINVAL, "the lagged fraction must be finite");
+  const float fr = fraction > 0.0f ? fraction : 0.0f;
+  if (fr != h->lagged_fraction) invalidate_graph(h);
+  h->lagged_fraction = fr;
+  if (h->fb_count.p) {  // restart the decision counters
     CU(h, cudaMemsetAsync(h->fb_count.p + 1, 0, 2 * sizeof(uint32_t), h->stream));
     CU(h, cudaStreamSynchronize(h->stream));
   }

@@ -25,7 +25,7 @@ struct PassSet {
                          uint32_t*, uint32_t*, uint32_t*);  // warp-cooperative per cell
   void (*band)(SimParams, SceneTab, const float4*, BandArgs);
   void (*boundary_band)(SimParams, FieldParams, const float*, const float*, SceneTab, const float4*, float4*, float*,
-                        const uint32_t*, const uint32_t*, uint32_t*);
+                        const uint32_t*, const uint32_t*, uint32_t*, const int*);
   void (*lambda)(SimParams, int, const float4*, const float4*, uint32_t, const uint32_t*, const uint32_t*, float4*,
                  SolverAux);
   void (*lambda_feat)(SimParams, int, const float4*, const float4*, uint32_t, const uint32_t*, const uint32_t*,
@@ -165,6 +165,9 @@ cudaError_t launch_mlp_grad(const float* d_params, const pbf_mlp& model, const f
 cudaError_t launch_gather_f32(uint32_t n, const uint32_t* perm, const float* src, float* dst, cudaStream_t st);
 cudaError_t launch_fallback_decide(SolveStats* stats, float bound, int* flag, uint32_t* fallbacks, float* last_mean,
                                    cudaStream_t st);
+// Lagged iteration control (counts[0] decisions, counts[1] substeps that iterated).
+cudaError_t launch_lagged_decide(const float* last_mean, float threshold, int* flag, uint32_t* counts,
+                                 cudaStream_t st);
 // The adaptive iteration's test (counts[0] tests, counts[1] position updates run).
 cudaError_t launch_iterate_decide(SolveStats* stats, float bound, int* flag, uint32_t* counts, float* last_mean,
                                   cudaStream_t st);

@@ -370,6 +370,16 @@ __global__ void k_iterate_decide(SolveStats* stats, float bound, int* flag, uint
   stats->sum_fx = 0ull;
 }
 
+// Lagged iteration control: this substep's iterations run (*flag = 1) when
+// the previous substep's final mean compression exceeded the threshold;
+// counts[0] counts the decisions, counts[1] the substeps that iterated.
+__global__ void k_lagged_decide(const float* last_mean, float threshold, int* flag, uint32_t* counts) {
+  const int f = *last_mean > threshold ? 1 : 0;
+  *flag = f;
+  counts[0] += 1u;
+  counts[1] += (uint32_t)f;
+}
+
 // Records a plain solve's in-solve mean compression (trace capture): running
 // max and sum over substeps, then resets the statistics.
 __global__ void k_stats_record(SolveStats* stats, float* rec) {
@@ -421,6 +431,11 @@ cudaError_t launch_fallback_decide(SolveStats* stats, float bound, int* flag, ui
 cudaError_t launch_iterate_decide(SolveStats* stats, float bound, int* flag, uint32_t* counts, float* last_mean,
                                   cudaStream_t st) {
   k_iterate_decide<<<1, 1, 0, st>>>(stats, bound, flag, counts, last_mean);
+  return cudaGetLastError();
+}
+cudaError_t launch_lagged_decide(const float* last_mean, float threshold, int* flag, uint32_t* counts,
+                                 cudaStream_t st) {
+  k_lagged_decide<<<1, 1, 0, st>>>(last_mean, threshold, flag, counts);
   return cudaGetLastError();
 }
 cudaError_t launch_stats_record(SolveStats* stats, float* rec, cudaStream_t st) {

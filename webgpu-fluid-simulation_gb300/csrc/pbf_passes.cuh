@@ -669,8 +669,10 @@ __global__ void __launch_bounds__(256, 2) k_boundary_band(SimParams p, FieldPara
                                                           const float* __restrict__ vol0, SceneTab tab,
                                                           const float4* __restrict__ xs, float4* __restrict__ bdata,
                                                           float* __restrict__ bsdf, const uint32_t* __restrict__ list,
-                                                          const uint32_t* count, uint32_t* other_count) {
+                                                          const uint32_t* count, uint32_t* other_count,
+                                                          const int* guard) {
   if (other_count && blockIdx.x == 0 && threadIdx.x == 0) *other_count = 0u;
+  if (guard && *guard == 0) return;  // the iteration is skipped (lagged iteration control)
   const uint32_t nb = *count;
   for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < nb; i += gridDim.x * blockDim.x) {
     const uint32_t t = list[i];

@@ -205,6 +205,7 @@ SIGNATURES = {
     "pbf_mlp_forward_ex": (ctypes.c_int, [ctypes.POINTER(MLP), _FP, u32, _FP, u32]),
     "pbf_set_mlp_kernel": (ctypes.c_int, [_P, u32]),
     "pbf_set_adaptive_iterations": (ctypes.c_int, [_P, ctypes.c_int]),
+    "pbf_set_lagged_iterations": (ctypes.c_int, [_P, ctypes.c_float]),
     "pbf_adaptive_counts": (ctypes.c_int, [_P, _UP, _UP]),
     "pbf_set_launch": (ctypes.c_int, [_P, ctypes.POINTER(Launch)]),
     "pbf_get_launch": (ctypes.c_int, [_P, ctypes.POINTER(Launch)]),

@@ -269,6 +269,11 @@ class PBF:
         density error at its start exceeds the fallback bound."""
         self._check(self._lib.pbf_set_adaptive_iterations(self._h, 1 if enable else 0), "set_adaptive_iterations")
 
+    def set_lagged_iterations(self, fraction):
+        """Run a substep's iterations only when the previous substep's final
+        mean compression exceeded fraction x the fallback bound (0: off)."""
+        self._check(self._lib.pbf_set_lagged_iterations(self._h, float(fraction)), "set_lagged_iterations")
+
     def adaptive_counts(self):
         """(tests made, position updates run) since set_adaptive_iterations."""
         t, r = ctypes.c_uint32(), ctypes.c_uint32()

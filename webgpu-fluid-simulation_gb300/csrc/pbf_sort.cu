@@ -283,15 +283,15 @@ __global__ void __launch_bounds__(kRadixThreads) k_bigcell(const uint32_t* __res
 // The stand-alone search receives its points in id order, so a stable sort
 // of the ids by cell key yields the order with every cell's particles in id
 // order: no within-cell pass, and skewed cell occupancy costs nothing extra.
-// Each pass over a digit is reduce-then-scan: every tile of 4096 records
+// Each pass over a digit is reduce-then-scan: every tile of 3072 records
 // counts its digits (written digit-major, count[d * tiles + tile]); one
 // exclusive scan of that matrix gives each (digit, tile) run its global
 // place; then every tile ranks its records by digit in shared memory (stable
 // in input order) and writes each digit's run there.  Reads and writes are
 // coalesced, and no tile waits on another.
 constexpr int kOsThreads = 256;
-constexpr int kOsItems = 16;
-constexpr int kOsTile = kOsThreads * kOsItems;  // 4096 records per tile
+constexpr int kOsItems = 12;
+constexpr int kOsTile = kOsThreads * kOsItems;  // 3072 records per tile
 constexpr int kOsWarps = kOsThreads / 32;
 constexpr int kOsMaxRadix = 256;
 
@@ -353,7 +353,7 @@ __global__ void __launch_bounds__(kOsThreads) k_tile_digits(uint32_t n, const ui
 // tile] is where the tile's run of digit d starts.  vin == nullptr: the values
 // are the input positions (particle ids).
 template <int kWidth>
-__global__ void __launch_bounds__(kOsThreads, 3) k_radix_pass(uint32_t n, const uint32_t* __restrict__ kin,
+__global__ void __launch_bounds__(kOsThreads, 4) k_radix_pass(uint32_t n, const uint32_t* __restrict__ kin,
                                                               const uint32_t* __restrict__ vin,
                                                               uint32_t* __restrict__ kout, uint32_t* __restrict__ vout,
                                                               const uint32_t* __restrict__ place, uint32_t tiles,

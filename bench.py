@@ -983,8 +983,8 @@ NS_DESC = ("neighbor_search_16m: 2^24 float4 points in the unit cube on a 128^3-
 NS_ALG = {
     "keys": (20, 0),           # read x (16); write the cell key (4)
     "sort_passes": (56, 0),    # 3 radix passes: count digits (read key 4) + move (key, id) records (read 8, write 8);
-                               # the first pass reads no ids: 3 * 20 - 4
-    "cell_offsets": (4, 12),   # read the sorted keys; clear counts, scan counts into offsets
+                               # the first pass reads no ids: 3 * 20 - 4; the last also counts the cells
+    "cell_offsets": (0, 8),    # scan the counts (made by the last sort pass) into offsets
     "outputs": (20, 16),       # ranks: read sorted key + order, write rank; copy order; copy counts + offsets
 }
 

@@ -337,9 +337,9 @@ const char* pbf_ns_last_error(const pbf_ns* ns);
  * when enabled, each run records CUDA events on the context's stream and
  * pbf_ns_timings returns the last run's phases in milliseconds after
  * synchronising: [0] cell keys (ParticleInsert), [1] the stable radix-sort
- * passes (CountingSort), [2] cell counts and offsets from
- * the sorted keys (cellParticleCount + ExclusiveScan), [3] outputs (ranks,
- * copies of counts, offsets and order).  PBF_ESTATE before a timed run. */
+ * passes (CountingSort; the last one also counts the cells), [2] cell
+ * offsets (ExclusiveScan of the counts), [3] outputs (ranks, copies of
+ * counts, offsets and order).  PBF_ESTATE before a timed run. */
 int pbf_ns_set_timing(pbf_ns* ns, int enable);
 int pbf_ns_timings(pbf_ns* ns, float ms[4]);
 

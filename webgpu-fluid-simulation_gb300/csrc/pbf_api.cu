@@ -2167,6 +2167,7 @@ int pbf_ns_run(pbf_ns* s, const float* d_pos4, uint32_t n, uint32_t* d_keys, uin
   const bool tm = s->timing;
   s->timed = false;
   if (tm) NSCU(s, cudaEventRecord(s->ev[0], st));
+  NSCU(s, cudaMemsetAsync(s->cell_count.p, 0, ((size_t)g.cells + 1) * 4, st));
   // The points come in particle-id order, so a stable radix sort of the ids
   // by cell key is the counting sort with each cell in id order.  Keys go
   // straight to the caller's array when it wants them.
@@ -2174,12 +2175,11 @@ int pbf_ns_run(pbf_ns* s, const float* d_pos4, uint32_t n, uint32_t* d_keys, uin
   uint32_t* const tk[2] = {s->tmp_a.p, s->perm_raw.p};
   uint32_t* const tv[2] = {s->tmp_b.p, s->id_raw.p};
   NSCU(s, launch_radix_sort_idorder(g, (const float4*)d_pos4, n, key, s->rank.p, s->perm.p, tk, tv, s->radix_scratch,
-                                    s->err_word.p, st, tm ? s->ev[1] : nullptr));
+                                    s->err_word.p, st, tm ? s->ev[1] : nullptr, s->cell_count.p));
   if (tm) NSCU(s, cudaEventRecord(s->ev[2], st));
-  // counts and offsets from the sorted keys (s->rank holds them); the order
-  // and offsets stay in the context for pbf_ns_lists
-  NSCU(s, launch_cells_from_sorted(n, s->rank.p, g.cells, s->cell_count.p, s->cell_start.p, s->scan_scratch,
-                                   s->err_word.p, st));
+  // offsets from the counts the last pass made (s->rank holds the sorted
+  // keys); the order and offsets stay in the context for pbf_ns_lists
+  NSCU(s, launch_cell_offsets(g.cells, s->cell_count.p, s->cell_start.p, s->scan_scratch, s->err_word.p, st));
   if (tm) NSCU(s, cudaEventRecord(s->ev[3], st));
   if (d_rank) NSCU(s, launch_rank_sorted(n, s->rank.p, s->perm.p, s->cell_start.p, d_rank, st));
   if (d_cell_count)

@@ -99,7 +99,9 @@ struct SortBuffers {
 // stand-alone search): keys[n] (by id) receive the cell keys, skeys[n] the
 // sorted keys and order[n] the ids in sorted order, stable by id.  tmp_k /
 // tmp_v: two pairs of n-entry scratch arrays; scratch: radix_scratch_bytes(n)
-// bytes.  after_keys (optional) is recorded after the keys.
+// bytes.  after_keys (optional) is recorded after the keys.  cell_count
+// (cells + 1 entries, zeroed by the caller) receives the cell counts from the
+// last pass.
 struct RadixPlan {
   int passes, width;
   size_t tiles;
@@ -108,10 +110,11 @@ RadixPlan radix_plan(uint32_t cells, size_t n);
 size_t radix_scratch_bytes(size_t n);
 cudaError_t launch_radix_sort_idorder(GridParams g, const float4* pos, uint32_t n, uint32_t* keys, uint32_t* skeys,
                                       uint32_t* order, uint32_t* const tmp_k[2], uint32_t* const tmp_v[2],
-                                      void* scratch, uint32_t* err, cudaStream_t st, cudaEvent_t after_keys);
-// Cell counts (cells + 1 entries, the last 0) and exclusive offsets from sorted keys.
-cudaError_t launch_cells_from_sorted(uint32_t n, const uint32_t* skeys, uint32_t cells, uint32_t* cell_count,
-                                     uint32_t* cell_start, void* scan_scratch, uint32_t* err, cudaStream_t st);
+                                      void* scratch, uint32_t* err, cudaStream_t st, cudaEvent_t after_keys,
+                                      uint32_t* cell_count);
+// Exclusive offsets (cells + 1 entries) of the cell counts.
+cudaError_t launch_cell_offsets(uint32_t cells, const uint32_t* cell_count, uint32_t* cell_start, void* scan_scratch,
+                                uint32_t* err, cudaStream_t st);
 // rank_out[order[q]] = q - cell_start[skeys[q]].
 cudaError_t launch_rank_sorted(uint32_t n, const uint32_t* skeys, const uint32_t* order, const uint32_t* cell_start,
                                uint32_t* rank_out, cudaStream_t st);

@@ -351,13 +351,15 @@ __global__ void __launch_bounds__(kOsThreads) k_tile_digits(uint32_t n, const ui
 
 // One pass over the digit (key >> shift) & (2^kWidth - 1): place[d * tiles +
 // tile] is where the tile's run of digit d starts.  vin == nullptr: the values
-// are the input positions (particle ids).
+// are the input positions (particle ids).  cell_count (the last pass only):
+// the written keys are in final order, so each run of equal keys a warp
+// writes is added to its cell's count once.
 template <int kWidth>
 __global__ void __launch_bounds__(kOsThreads, 4) k_radix_pass(uint32_t n, const uint32_t* __restrict__ kin,
                                                               const uint32_t* __restrict__ vin,
                                                               uint32_t* __restrict__ kout, uint32_t* __restrict__ vout,
                                                               const uint32_t* __restrict__ place, uint32_t tiles,
-                                                              int shift) {
+                                                              int shift, uint32_t* cell_count) {
   constexpr uint32_t kRadix = 1u << kWidth, kMask = kRadix - 1u;
   __shared__ uint32_t s_key[kOsTile];
   __shared__ uint32_t s_val[kOsTile];
@@ -449,33 +451,29 @@ __global__ void __launch_bounds__(kOsThreads, 4) k_radix_pass(uint32_t n, const 
   // each digit's run to its global place: consecutive j, consecutive addresses
   const uint32_t in_tile = (n - t0) < (uint32_t)kOsTile ? (n - t0) : (uint32_t)kOsTile;
 #pragma unroll 4
-  for (uint32_t j = tid; j < in_tile; j += kOsThreads) {
-    const uint32_t kk = s_key[j];
-    const uint32_t d = (kk >> shift) & kMask;
-    const uint32_t p = s_glob[d] + (j - s_loc[d]);
-    if (p < n) {
-      kout[p] = kk;
-      vout[p] = s_val[j];
+  for (uint32_t j0 = 0; j0 < in_tile; j0 += kOsThreads) {
+    const uint32_t j = j0 + tid;
+    const bool valid = j < in_tile;
+    const uint32_t kk = valid ? s_key[j] : 0xffffffffu;
+    if (valid) {
+      const uint32_t d = (kk >> shift) & kMask;
+      const uint32_t p = s_glob[d] + (j - s_loc[d]);
+      if (p < n) {
+        kout[p] = kk;
+        vout[p] = s_val[j];
+      }
     }
-  }
-}
-
-// Cell counts from the sorted keys: each run of equal keys within a warp is
-// found from its neighbour's key (one shuffle and one ballot) and added once.
-__global__ void __launch_bounds__(256) k_count_sorted(uint32_t n, const uint32_t* __restrict__ skey,
-                                                      uint32_t* cell_count) {
-  const uint32_t q = blockIdx.x * blockDim.x + threadIdx.x;
-  const uint32_t lane = threadIdx.x & 31u;
-  const bool valid = q < n;
-  const uint32_t k = valid ? __ldg(skey + q) : 0xffffffffu;
-  const uint32_t up = __shfl_up_sync(kFull, k, 1);
-  const bool start = valid && (lane == 0u || up != k);
-  const unsigned starts = __ballot_sync(kFull, start);
-  const unsigned valid_mask = __ballot_sync(kFull, valid);
-  if (start) {
-    const unsigned later = starts & ~((2u << lane) - 1u);  // run starts after this lane
-    const uint32_t end = later ? (uint32_t)(__ffs(later) - 1) : (uint32_t)(32 - __clz(valid_mask));
-    atomicAdd(cell_count + k, end - lane);
+    if (cell_count) {  // a warp's 32 consecutive records: one add per run of equal keys
+      const uint32_t up = __shfl_up_sync(kFull, kk, 1);
+      const bool start = valid && (lane == 0u || up != kk);
+      const unsigned starts = __ballot_sync(kFull, start);
+      const unsigned valid_mask = __ballot_sync(kFull, valid);
+      if (start) {
+        const unsigned later = starts & ~((2u << lane) - 1u);
+        const uint32_t end = later ? (uint32_t)(__ffs(later) - 1) : (uint32_t)(32 - __clz(valid_mask));
+        atomicAdd(cell_count + kk, end - lane);
+      }
+    }
   }
 }
 
@@ -637,7 +635,8 @@ size_t radix_scratch_bytes(size_t n) {
 
 cudaError_t launch_radix_sort_idorder(GridParams g, const float4* pos, uint32_t n, uint32_t* keys, uint32_t* skeys,
                                       uint32_t* order, uint32_t* const tmp_k[2], uint32_t* const tmp_v[2],
-                                      void* scratch, uint32_t* err, cudaStream_t st, cudaEvent_t after_keys) {
+                                      void* scratch, uint32_t* err, cudaStream_t st, cudaEvent_t after_keys,
+                                      uint32_t* cell_count) {
   cudaError_t e = cudaSuccess;
   if (n == 0) return after_keys ? cudaEventRecord(after_keys, st) : cudaSuccess;
   const RadixPlan plan = radix_plan(g.cells, n);
@@ -668,7 +667,7 @@ cudaError_t launch_radix_sort_idorder(GridParams g, const float4* pos, uint32_t 
     if ((e = cudaGetLastError()) != cudaSuccess) return e;                              \
     if ((e = launch_exclusive_scan(count, place, m, scan_scr, err, st)) != cudaSuccess) \
       return e;                                                                         \
-    k_radix_pass<W><<<grid, kOsThreads, 0, st>>>(n, kin, vin, kout, vout, place, tl, shift); \
+    k_radix_pass<W><<<grid, kOsThreads, 0, st>>>(n, kin, vin, kout, vout, place, tl, shift, last ? cell_count : nullptr); \
     break;
       PBF_RADIX_WIDTH(1)
       PBF_RADIX_WIDTH(2)
@@ -687,12 +686,8 @@ cudaError_t launch_radix_sort_idorder(GridParams g, const float4* pos, uint32_t 
   return cudaSuccess;
 }
 
-cudaError_t launch_cells_from_sorted(uint32_t n, const uint32_t* skeys, uint32_t cells, uint32_t* cell_count,
-                                     uint32_t* cell_start, void* scan_scratch, uint32_t* err, cudaStream_t st) {
-  cudaError_t e = cudaMemsetAsync(cell_count, 0, ((size_t)cells + 1) * sizeof(uint32_t), st);
-  if (e != cudaSuccess) return e;
-  if (n) k_count_sorted<<<(unsigned)((n + 255) / 256), 256, 0, st>>>(n, skeys, cell_count);
-  if ((e = cudaGetLastError()) != cudaSuccess) return e;
+cudaError_t launch_cell_offsets(uint32_t cells, const uint32_t* cell_count, uint32_t* cell_start, void* scan_scratch,
+                                uint32_t* err, cudaStream_t st) {
   return launch_exclusive_scan(cell_count, cell_start, (size_t)cells + 1, scan_scratch, err, st);
 }
 

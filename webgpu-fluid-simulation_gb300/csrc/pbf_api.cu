@@ -483,7 +483,7 @@ int substep(pbf_handle* h, cudaEvent_t* ev) {
       }
       {
         KScope ks(h, K_LAMBDA);
-        auto kl = fe ? ps.lambda_feat : ps.lambda;
+        auto kl = fe ? ps.lambda_feat : (al.stats && adaptive ? ps.lambda_stats : ps.lambda);
         kl<<<grid_of(h, n), h->blk, 0, st>>>(p, f.loaded, h->bdata.p, h->xs[a].p, ms, h->nbr_count.p,
                                              h->nbr_list.p, h->xl.p, al);
       }

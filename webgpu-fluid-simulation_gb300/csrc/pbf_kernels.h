@@ -29,6 +29,8 @@ struct PassSet {
   void (*lambda)(SimParams, int, const float4*, const float4*, uint32_t, const uint32_t*, const uint32_t*, float4*,
                  SolverAux);
   void (*lambda_feat)(SimParams, int, const float4*, const float4*, uint32_t, const uint32_t*, const uint32_t*,
+                      float4*, SolverAux);
+  void (*lambda_stats)(SimParams, int, const float4*, const float4*, uint32_t, const uint32_t*, const uint32_t*,
                       float4*, SolverAux);     // null in batch sets
   void (*nbr_build_feat)(SimParams, GridParams, const float4*, const uint32_t*, uint32_t, uint32_t*, uint32_t*,
                          uint32_t*, uint32_t*, int, const float4*, SolverAux);  // null in batch sets

@@ -724,6 +724,7 @@ __device__ __forceinline__ void compression_flush(SolveStats* stats, unsigned cm
 // LambdaCalculation (pressureConstrain.ts:31-85).  Writes xl[t] = (x*, lambda):
 // the next pass gathers a neighbour's position and multiplier in one load.
 //   kMode 0: the reference pass.
+//   kMode 2: the reference pass + the density error statistics (a.stats).
 //   kMode 1: also writes the learned start's 8 features at x*_0 (density
 //            error, previous multiplier, neighbour count, |v'| dt/h, -div(v') dt
 //            by continuity, boundary SDF/h, boundary volume/V, substep index;
@@ -785,15 +786,17 @@ __global__ void __launch_bounds__(256) k_lambda(SimParams p, int have_field, con
                                                 const uint32_t* __restrict__ nbr_list,
                                                 float4* __restrict__ xl, SolverAux a) {
   if (a.guard && *a.guard == 0) return;
-  // with a.stats: the density error at these positions (the adaptive
-  // iteration's test; the same quantity AttributeUpdate reports)
+  // kMode 2: also the density error at these positions into a.stats (the
+  // adaptive iteration's test; the same quantity AttributeUpdate reports)
+  constexpr bool kStats = kMode == 2;
   unsigned cmax = 0u, csum = 0u, ccnt = 0u;
   PBF_SLOTS(t, p.n) {
     if (!iter_active(scene_of<kBatch>(a.tab, t), a.iter)) continue;
-    const float vsum = lambda_slot<kMode, false>(p, have_field, bdata, xs, max_nbr, nbr_cnt, nbr_list, xl, a, t);
-    if (a.stats) compression_add(cmax, csum, ccnt, vsum * p.V);
+    const float vsum =
+        lambda_slot<kStats ? 0 : kMode, false>(p, have_field, bdata, xs, max_nbr, nbr_cnt, nbr_list, xl, a, t);
+    if constexpr (kStats) compression_add(cmax, csum, ccnt, vsum * p.V);
   }
-  if (a.stats) compression_flush(a.stats, cmax, csum, ccnt);
+  if constexpr (kStats) compression_flush(a.stats, cmax, csum, ccnt);
 }
 
 // ConstrainSolve + ConstrainApply: x*_new = clamp(x* + 0.5 * dp) into the other
@@ -1099,6 +1102,7 @@ void fill_set(PassSet* ps) {
   ps->boundary_band = k_boundary_band<B>;
   ps->lambda = k_lambda<0, B, P>;
   ps->lambda_feat = B ? nullptr : k_lambda<1, false, P>;
+  ps->lambda_stats = B ? nullptr : k_lambda<2, false, P>;
   ps->nbr_build_feat = B ? nullptr : k_nbr_build_feat<P>;
   ps->deltap = k_deltap<B, P>;
   ps->density_velocity = k_density_velocity<P>;

@@ -160,6 +160,26 @@ def test_neighbor_search_full_cells():
         assert np.array_equal(got[k], ref[k]), k
 
 
+@pytest.mark.parametrize("dims,n", [((5, 7, 3), 20000),        # 105 cells: one 7-bit pass
+                                    ((64, 64, 64), 150001),    # 2^18 cells: three 6-bit passes
+                                    ((200, 150, 90), 150003),  # 2.7 M cells: three 8-bit passes
+                                    ((40, 40, 40), 4095),      # 64,000 cells: two 8-bit passes, one tile
+                                    ((40, 40, 40), 0)])        # no points
+def test_neighbor_search_grid_shapes(dims, n):
+    """The radix plan follows the cell count (1-3 passes of 6-8-bit digits);
+    every plan gives the oracle's keys, counts, offsets, order and ranks."""
+    rng = np.random.default_rng(sum(dims) + n)
+    pts = np.zeros((n, 4), np.float32)
+    pts[:, :3] = rng.random((n, 3), dtype=np.float32)
+    pts[: n // 3, :3] = (0.4 + 0.05 * rng.random((n // 3, 3))).astype(np.float32)  # a crowded corner
+    pts = pts[rng.permutation(n)]
+    cfg = scenes.base_config(kernel_radius=1.0 / max(dims), grid_dim=dims, max_particles=max(n, 1))
+    ref = O.neighbor_search(cfg, pts)
+    got = run_ns(cfg, pts)
+    for k in ("keys", "cell_count", "cell_offset", "order", "rank"):
+        assert np.array_equal(got[k], ref[k]), k
+
+
 def test_neighbor_lists_bitexact():
     sc = scenes.reference_scene("cube_drop")
     pts = scenes.jitter(sc.particles, 0.002, seed=3)

@@ -1137,7 +1137,8 @@ def ns_arm(args, dist):
                        "l2": "inputs of 256 MB each, larger than the 129 MB L2", "phase_ms": per_input},
             "e2e": {"value": e2e, "unit": "particles/s", "h2d_bytes_per_step": int(2 * 16 * n),
                     "d2h_bytes_per_step": int(2 * (12 * n + 4 * cells + 4 * (cells + 1)))},
-            "gpu_launches": 12 * args.steps,
+            # per search: keys, 3 x (digit counts, matrix scan, record move), offsets scan, ranks
+            "gpu_launches": 2 * 12 * args.steps,
             "roofline": {"bound": "hbm", "kernel": top, "achieved": achieved, "peak": peak, "unit": "GB/s",
                          "frac": achieved / peak, "peak_kind": peak_kind, "traffic": None,
                          "alg_bytes_per_launch": alg, "avg_launch_ms": mean_phase[top],

@@ -441,6 +441,10 @@ def gpu_arm(args, dist):
         # iteration, density/velocity, fallback decision, fallback kernel,
         # vorticity, XSPH
         per_sub = 17 + 3 * chosen["learned_iters"]
+        if chosen.get("adaptive"):
+            per_sub += chosen["learned_iters"]  # the test's decision after each lambda pass
+        elif chosen.get("lagged", 0.0) > 0.0:
+            per_sub += 1  # the lagged decision before the iterations
     launches_per_frame = sub * per_sub + 1  # + export
     m = plain["metrics"]
     line = {
@@ -449,8 +453,9 @@ def gpu_arm(args, dist):
         "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
         "config": {"workload": desc, "path": chosen["label"],
                    "selection": "fastest of the plain %d-iteration solve and the learned start (+2/+1/+0 "
-                                "iterations, device-side fallback to the plain solve) whose largest per-step "
-                                "mean compression over the timed window is at most the plain solve's" % iters,
+                                "iterations; up to 2 or 1 measured adaptive iterations; 1 iteration under lagged "
+                                "control; device-side fallback to the plain solve) whose largest per-step mean "
+                                "compression over the timed window is at most the plain solve's" % iters,
                    "launch": _LAUNCH if _LAUNCH else "default (256 threads, one tile per CTA, cell = h)",
                    "input_state": "frame %d of the run (after the impact); %d warm-up frames" % (args.settle,
                                                                                              max(args.warmup, 3)),

@@ -207,6 +207,11 @@ int pbf_set_particle_position(pbf_handle* h);
 int pbf_set_particles(pbf_handle* h, const float* xyzw, uint32_t n);
 /* Optional: overwrite velocities (float4 per particle, by id). */
 int pbf_set_velocities(pbf_handle* h, const float* xyzw, uint32_t n);
+/* Optional: overwrite the accelerations (SPH.acceleration, float4 per
+ * particle, by id): the XSPH / vorticity / tension force the next substep's
+ * TimeIntegration applies (timeIntegration.ts:25-28).  With
+ * pbf_set_particles and pbf_set_velocities it restores a saved state. */
+int pbf_set_accelerations(pbf_handle* h, const float* xyzw, uint32_t n);
 
 /* ---- boundary: PBF.setBoundaryData -> BoundaryModel.setData (PBF.ts:91-94, volumeMap.ts:23-39).
  * `text` is the .cdm file: "nx ny nz\n<len>\n<sdf floats>\n<len>\n<volume floats>".
@@ -301,6 +306,20 @@ int pbf_copy_field(pbf_handle* h, int field, void* host, size_t bytes);
  * pbf_synchronize, and must stay valid until then. */
 int pbf_copy_positions_async(pbf_handle* h, float* host, size_t bytes);
 int pbf_get_metrics(pbf_handle* h, pbf_metrics* out);
+/* The neighbour search of the last substep (NeighborSearch's buffers,
+ * src/simulator/neighbor/neighborSearch.ts:25-29): the cell key of each
+ * particle's predicted position (by id, ParticleInsert), cellParticleCount
+ * (per cell), cellOffset (per cell + 1: the exclusive scan and the total) and
+ * particleSortIndexCopy (the order, slot -> particle id, stable by id within
+ * a cell).  `count` must be the array's length (n, n, cells, cells + 1).
+ * Valid right after a substep, before the next one; single-scene handles. */
+typedef enum pbf_search_array {
+  PBF_SEARCH_CELL_KEY = 0,
+  PBF_SEARCH_CELL_COUNT = 1,
+  PBF_SEARCH_CELL_OFFSET = 2,
+  PBF_SEARCH_ORDER = 3
+} pbf_search_array;
+int pbf_copy_search_state(pbf_handle* h, int which, uint32_t* host, size_t count);
 /* Keep per-iteration debug fields (PBF_FIELD_DELTA_P); off by default. */
 int pbf_set_capture(pbf_handle* h, int enable);
 void* pbf_stream(pbf_handle* h);
@@ -445,16 +464,18 @@ int pbf_adaptive_counts(pbf_handle* h, uint32_t* tests, uint32_t* updates_run);
 /* ---- allocation-free exclusive scan.  No counterpart in the reference: an
  * addition for callers that cannot allocate device memory when they scan —
  * hosts whose own pool owns all device memory, real-time loops that must not
- * enter the allocator, code running during stream capture.  Same result as
- * pbf_exclusive_scan_u32, but the look-back scratch is a fixed static device
- * array of about 256 KB that every GPU loading this library keeps until
- * exit, and the call allocates nothing (no cudaMalloc / cudaMallocAsync /
- * cudaFree).  Sizes above PBF_SCAN_NOALLOC_MAX elements return
- * PBF_ECAPACITY without launching anything.  The first call on a device
- * looks up the array's device address; make that first call before any
- * stream capture on that device.  All calls on a device share the array:
- * calls that overlap on the GPU (e.g. on unordered streams) race and give
- * wrong results; serialise them.  Synchronises `stream` before returning. */
+ * enter the allocator.  Same result as pbf_exclusive_scan_u32, but the
+ * look-back scratch is a fixed static device array of about 256 KB that
+ * every GPU loading this library keeps until exit, and the call allocates
+ * nothing (no cudaMalloc / cudaMallocAsync / cudaFree).  Sizes above
+ * PBF_SCAN_NOALLOC_MAX elements return PBF_ECAPACITY without launching
+ * anything.  The call is synchronous: it reads the device error word back to
+ * the host and synchronises `stream` before returning (so it cannot be
+ * recorded into a CUDA graph).  The first call on a device looks up the
+ * array's device address and caches it for the process; the library must
+ * not be used on a device after cudaDeviceReset there.  All calls on a
+ * device share the array: calls that overlap on the GPU (e.g. on unordered
+ * streams) race and give wrong results; serialise them. */
 #define PBF_SCAN_NOALLOC_MAX (1u << 26)
 int pbf_exclusive_scan_u32_noalloc(const uint32_t* d_in, uint32_t* d_out, size_t n, void* stream);
 

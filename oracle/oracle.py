@@ -38,6 +38,8 @@ def load():
         "oracle_set_options": (None, [_P, ctypes.POINTER(L.Options)]),
         "oracle_set_particles": (None, [_P, _FP, ctypes.c_uint32]),
         "oracle_set_velocities": (None, [_P, _FP, ctypes.c_uint32]),
+        "oracle_set_accelerations": (None, [_P, _FP, ctypes.c_uint32]),
+        "oracle_search_state": (ctypes.c_long, [_P, ctypes.c_int, _UP, ctypes.c_size_t]),
         "oracle_set_field": (ctypes.c_int, [_P, _UP, _FP, _FP, _FP, _FP, ctypes.c_size_t]),
         "oracle_substep": (None, [_P, ctypes.c_uint32]),
         "oracle_get_field": (ctypes.c_int, [_P, ctypes.c_int, _DP]),
@@ -117,6 +119,25 @@ class Oracle:
     def set_velocities(self, xyzw):
         a = np.ascontiguousarray(xyzw, dtype=np.float32)
         self._lib.oracle_set_velocities(self._h, _fp(a), a.shape[0])
+
+    def set_accelerations(self, xyzw):
+        a = np.ascontiguousarray(xyzw, dtype=np.float32)
+        self._lib.oracle_set_accelerations(self._h, _fp(a), a.shape[0])
+
+    def set_state(self, positions, velocities, accelerations):
+        """A saved simulation state (by particle id): x, v and a."""
+        self.set_particles(positions)
+        self.set_velocities(velocities)
+        self.set_accelerations(accelerations)
+
+    def search_state(self, which):
+        """The last substep's neighbour search: 'keys' (per particle),
+        'cell_count', 'cell_offset' or 'order'."""
+        k = {"keys": 0, "cell_count": 1, "cell_offset": 2, "order": 3}[which]
+        m = self._lib.oracle_search_state(self._h, k, None, 0)
+        out = np.zeros(max(m, 0), np.uint32)
+        self._lib.oracle_search_state(self._h, k, _up(out), out.size)
+        return out
 
     def set_field(self, res, origin, extent, sdf, vol):
         r = np.asarray(res, dtype=np.uint32)

@@ -719,6 +719,35 @@ void oracle_set_velocities(oracle_handle* h, const float* xyzw, uint32_t n) {
   }
 }
 
+void oracle_set_accelerations(oracle_handle* h, const float* xyzw, uint32_t n) {
+  for (uint32_t i = 0; i < n; ++i) {
+    if (h->precision == 64)
+      h->d.a[i] = v3<double>(xyzw[4 * i], xyzw[4 * i + 1], xyzw[4 * i + 2]);
+    else
+      h->f.a[i] = v3<float>(xyzw[4 * i], xyzw[4 * i + 1], xyzw[4 * i + 2]);
+  }
+}
+
+// The last substep's neighbour search: 0 cell key per particle, 1 cell count,
+// 2 cell offset (cells + 1), 3 sorted order.  Returns the array's length
+// (copied when out is non-null and count matches), -1 for an unknown array.
+long oracle_search_state(oracle_handle* h, int which, uint32_t* out, size_t count) {
+  const std::vector<uint32_t>* v = nullptr;
+  auto pick = [&](auto& sim) {
+    switch (which) {
+      case 0: v = &sim.key; break;
+      case 1: v = &sim.cell_count; break;
+      case 2: v = &sim.cell_offset; break;
+      case 3: v = &sim.sorted; break;
+      default: break;
+    }
+  };
+  if (h->precision == 64) pick(h->d); else pick(h->f);
+  if (!v) return -1;
+  if (out && count == v->size()) std::copy(v->begin(), v->end(), out);
+  return (long)v->size();
+}
+
 int oracle_set_field(oracle_handle* h, const uint32_t* res, const float* origin, const float* extent,
                      const float* sdf, const float* vol, size_t nodes) {
   Field& f = (h->precision == 64) ? h->d.field : h->f.field;

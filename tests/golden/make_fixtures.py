@@ -5,7 +5,8 @@
    public/model/domain_boundary.cdm (20^3 cubic volume maps over the unit
    cube), parsed exactly as BoundaryModel.setData does
    (src/simulator/boundary/volumeMap.ts:23-39) and stored as float32 arrays.
-   Run from a checkout that has the reference at REFERENCE_ROOT.
+   Needs the environment variable REFERENCE_ROOT set to a checkout of the
+   reference (the script refuses to guess a path).
 2. oracle_*.npz: outputs of the CPU restatement (oracle/) on small seeded
    inputs, kept as regression vectors for the restatement itself.
 """
@@ -16,7 +17,13 @@ import numpy as np
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 REPO = os.path.dirname(os.path.dirname(HERE))
-REFERENCE_ROOT = os.environ.get("REFERENCE_ROOT", "/root/reference")
+REFERENCE_ROOT = os.environ.get("REFERENCE_ROOT")
+
+
+def _reference_root():
+    if not REFERENCE_ROOT:
+        raise SystemExit("set REFERENCE_ROOT to the reference checkout (or pass --oracle-only)")
+    return REFERENCE_ROOT
 
 
 def parse_cdm_text(text):
@@ -30,7 +37,7 @@ def parse_cdm_text(text):
 
 def make_cdm():
     for name in ("torus", "domain_boundary"):
-        path = os.path.join(REFERENCE_ROOT, "public", "model", name + ".cdm")
+        path = os.path.join(_reference_root(), "public", "model", name + ".cdm")
         with open(path) as f:
             res, sdf, vol, n1, n2 = parse_cdm_text(f.read())
         assert int(n1) == sdf.size and int(n2) == vol.size
@@ -43,7 +50,7 @@ def make_meshes():
     800 triangles) as float32 vertices and uint32 triangles."""
     sys.path.insert(0, os.path.join(REPO, "webgpu-fluid-simulation_gb300"))
     from pbf_gb300 import scenes
-    with open(os.path.join(REFERENCE_ROOT, "public", "model", "torus.obj")) as f:
+    with open(os.path.join(_reference_root(), "public", "model", "torus.obj")) as f:
         v, t = scenes.parse_obj(f.read())
     np.savez_compressed(os.path.join(HERE, "mesh_torus.npz"), vertices=v, triangles=t)
     print("torus mesh", v.shape, t.shape)

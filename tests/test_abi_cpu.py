@@ -61,6 +61,9 @@ def test_field_length_matches_reference_formula():
     nx, ny, nz = 3, 4, 5
     assert lib.pbf_field_length(r) == ((nx + 1) * (ny + 1) * (nz + 1) + 2 * nx * (ny + 1) * (nz + 1) +
                                        (nx + 1) * 2 * ny * (nz + 1) + (nx + 1) * (ny + 1) * 2 * nz)
+    from pbf_gb300 import scenes  # the host-side count the CPU-only paths use
+    for res in ((20, 20, 20), (3, 4, 5), (128, 128, 128)):
+        assert scenes.field_length(res) == lib.pbf_field_length((ctypes.c_uint32 * 3)(*res))
 
 
 def test_host_argument_validation_without_gpu():

@@ -33,6 +33,23 @@ def test_reference_arm_line():
     assert "workload" in d["config"]
 
 
+def test_reference_arm_maps_only_the_restatement():
+    """The reference arm runs the method through the CPU restatement alone:
+    the CUDA library of the product is never mapped into its process."""
+    code = ("import sys, bench\n"
+            "sys.argv = ['bench.py', '--impl', 'reference', '--workload', 'dam_break_16k', '--steps', '1', "
+            "'--warmup', '0', '--settle', '2']\n"
+            "bench.main()\n"
+            "maps = open('/proc/self/maps').read()\n"
+            "assert 'libpbf_oracle' in maps\n"
+            "assert 'libpbf_gb300' not in maps, 'product library mapped'\n")
+    out = subprocess.run([sys.executable, "-c", code], capture_output=True, text=True, timeout=600, cwd=REPO)
+    assert out.returncode == 0, out.stderr[-2000:]
+    line = json.loads([l for l in out.stdout.splitlines() if l.startswith("{")][0])
+    assert line["config"]["sample"] == "all 16384 particles"
+    assert "frame 2" in line["config"]["input_state"]
+
+
 def test_render_reference_arm_line():
     import bench
     d = _run("--impl", "reference", "--workload", "render_1m_1080p", "--steps", "1", "--warmup", "0")

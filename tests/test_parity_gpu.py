@@ -86,15 +86,20 @@ def test_neighbor_search_bitexact(dist, n):
 
 
 @pytest.mark.parametrize("dist", ["uniform", "clumps"])
-def test_neighbor_search_16m_properties(dist):
-    """2^24 particles (the largest neighbour-search size): checked through
-    size-independent properties instead of the oracle — keys from the cell
-    formula, counts = histogram of keys, offsets = exclusive scan of counts,
-    order a permutation sorted by key and, within a cell, by particle id,
-    ranks placing every particle at its sorted position."""
+def test_neighbor_search_16m_bitexact_and_properties(dist):
+    """2^24 particles (the largest neighbour-search size): bit-exact against
+    the oracle (keys, counts, offsets, order, ranks), and the size-independent
+    properties checked on their own — keys from the cell formula, counts =
+    histogram of keys, offsets = exclusive scan of counts, order a permutation
+    sorted by key and, within a cell, by particle id, ranks placing every
+    particle at its sorted position."""
     n = 1 << 24
     cfg, pts = scenes.neighbor_case(n, dist, seed=13, dim=128)
     got = run_ns(cfg, pts)
+    ref = O.neighbor_search(cfg, pts)
+    for k in ("keys", "cell_count", "cell_offset", "order", "rank"):
+        assert np.array_equal(got[k], ref[k]), k
+    del ref
     dims = np.array([128, 128, 128])
     inv = np.float32(128.0)  # unit cube, 128 cells per axis
     c = np.floor(pts[:, :3] * inv).astype(np.int64)

@@ -1,0 +1,271 @@
+"""GPU parity at the benchmarked workloads, against the CPU restatement.
+
+1. The 2^20-particle sphere-drop scene (the bench's workload) after 150
+   frames of the production path (fast mode, the autotuner's launch shape and
+   cell height), used as a snapshot (x, v, a by particle id):
+   - production mode, one substep from the snapshot against the FP32
+     restatement and the FP64 replica, per field (rho, lambda, delta-p, v,
+     x, a, omega, n), with the neighbour counts bit-exact;
+   - exact mode (-fmad=false, the reference's grid) from the same snapshot:
+     every field and the neighbour search of the substep (cell keys, counts,
+     offsets, order) bit-identical to the FP32 restatement.
+2. The 16,384-particle dam break (the reference's CPU-runnable case):
+   - the first substep's cell keys, cell counts, cell scan and order
+     bit-exact against the restatement;
+   - 200 frames of the production path against 200 frames of the FP32
+     restatement, compared every 20 frames on aggregate statistics (the
+     trajectories are chaotic, so particle-wise comparison ends after a few
+     frames), within these bands, fixed before the comparison was run:
+       nonfinite particles: 0 on both;
+       boundary penetrations (SDF < 0): at most 0.1 % of the particles on both;
+       kinetic energy: |GPU - CPU| <= 10 % of the run's peak CPU value;
+       mean compression: |GPU - CPU| <= 25 % of the run's peak CPU value + 1e-3;
+       max compression: |GPU - CPU| <= 50 % of the run's peak CPU value + 1e-2.
+
+Tolerances of the per-field comparison (fast mode): rho and x within 1e-5 of
+scale of both references; for the fields that are differences of nearly
+equal f32 values in the reference formulas (lambda, delta-p, v, omega, a)
+the GPU's RMS error against FP64 stays within 3x the FP32 restatement's own
+RMS error and its maximum within 25x the restatement's maximum, each plus
+1e-6 of scale; n within 1e-4 of scale of FP64.
+"""
+import numpy as np
+import pytest
+
+from oracle import oracle as O
+from pbf_gb300 import PBF, scenes
+from pbf_gb300 import _lib as L
+
+torch = pytest.importorskip("torch")
+pytestmark = pytest.mark.gpu
+
+FIELDS = [(L.FIELD_POSITION, "position"), (L.FIELD_VELOCITY, "velocity"), (L.FIELD_ACCELERATION, "acceleration"),
+          (L.FIELD_LAMBDA, "lambda"), (L.FIELD_BOUNDARY, "boundary"), (L.FIELD_OMEGA, "omega"),
+          (L.FIELD_NORMAL, "normal"), (L.FIELD_DELTA_P, "delta_p"), (L.FIELD_NEIGHBOR_COUNT, "nbr_count")]
+SEARCH = ("keys", "cell_count", "cell_offset", "order")
+
+
+def _set_field(obj, field):
+    args = (field["res"], field["origin"], field["extent"], field["sdf"], field["vol"])
+    if isinstance(obj, O.Oracle):
+        obj.set_field(*args)
+    else:
+        obj.set_boundary_field(*args)
+
+
+def _gpu_fields(sim):
+    return {name: sim.copy_field(f) for f, name in FIELDS}
+
+
+def _oracle_fields(orc, precision=32):
+    out = {}
+    for f, name in FIELDS:
+        v = orc.field(f)
+        if f == L.FIELD_NEIGHBOR_COUNT:
+            out[name] = v.astype(np.uint32)
+        else:
+            out[name] = v.astype(np.float32) if precision == 32 else v
+    return out
+
+
+def _tuned(sim):
+    """The bench's launch shape: the autotuner's choice over the shapes and
+    both cell heights, timed on the current state (which it restores)."""
+    best, _ = sim.autotune(substeps=4, cell_ratio=True)
+    return best
+
+
+# ---- 1. the sphere-drop snapshot ------------------------------------------------------------
+@pytest.fixture(scope="module")
+def sphere_drop():
+    sc = scenes.build_scene(scenes.sphere_drop_spec(seed=1), quadrature=12, name="sphere_drop_1m")
+    cfg = scenes.copy_config(sc.config)
+    cfg.fp_mode = L.FP_FAST
+    sim = PBF(cfg)
+    try:
+        sim.set_particles(sc.particles)
+        _set_field(sim, sc.field)
+        _tuned(sim)
+        sim.enable_graph(True)
+        sim.step(150)
+        sim.synchronize()
+        snap = dict(x=sim.positions(), v=sim.velocities(), a=sim.copy_field(L.FIELD_ACCELERATION))
+    finally:
+        sim.close()
+    assert np.isfinite(snap["x"]).all() and np.isfinite(snap["v"]).all()
+    return sc, snap
+
+
+def _oracle_from(sc, snap, precision):
+    o = O.Oracle(sc.config, precision)
+    o.set_state(snap["x"], snap["v"], snap["a"])
+    _set_field(o, sc.field)
+    return o
+
+
+def test_sphere_drop_snapshot_production_mode_per_field(sphere_drop):
+    sc, snap = sphere_drop
+    cfg = scenes.copy_config(sc.config)
+    cfg.fp_mode = L.FP_FAST
+    sim = PBF(cfg)
+    try:
+        sim.set_state(snap["x"], snap["v"], snap["a"])
+        _set_field(sim, sc.field)
+        best = _tuned(sim)
+        sim.set_capture(True)
+        sim.run()
+        g = _gpu_fields(sim)
+    finally:
+        sim.close()
+    o32 = _oracle_from(sc, snap, 32)
+    o32.substep(1)
+    a = _oracle_fields(o32)
+    o32.close()
+    o64 = _oracle_from(sc, snap, 64)
+    o64.substep(1)
+    d = _oracle_fields(o64, 64)
+    o64.close()
+    # the same neighbour sets, whatever the grid's cell height
+    assert np.array_equal(g["nbr_count"], a["nbr_count"])
+    assert (a["boundary"][:, 3] > 0).sum() > 1000  # the volume map (sphere and floor) was exercised
+    rms = lambda x: float(np.sqrt(np.mean(np.square(x))))
+    rows = []
+    fields = {"rho": lambda x: x["position"][:, 3], "lambda": lambda x: x["lambda"],
+              "delta_p": lambda x: x["delta_p"][:, :3], "velocity": lambda x: x["velocity"][:, :3],
+              "position": lambda x: x["position"][:, :3], "acceleration": lambda x: x["acceleration"][:, :3],
+              "omega": lambda x: x["omega"][:, :3], "normal": lambda x: x["normal"][:, :3]}
+    for name, get in fields.items():
+        ref = get(d).astype(np.float64)
+        scale = max(np.abs(ref).max(), 1e-30)
+        eg = get(g).astype(np.float64) - ref
+        er = get(a).astype(np.float64) - ref
+        rows.append((name, np.abs(er).max() / scale, rms(er) / scale, np.abs(eg).max() / scale, rms(eg) / scale))
+    print("\nsphere_drop_1m snapshot (frame 150), one substep, launch %s" % (best,))
+    print("| field | FP32 restatement max / rms | GPU production mode max / rms |")
+    print("|---|---|---|")
+    for name, m32, r32, mg, rg in rows:
+        print("| %s | %.2e / %.2e | %.2e / %.2e |" % (name, m32, r32, mg, rg))
+    err = {r[0]: r for r in rows}
+    for k in ("lambda", "delta_p", "velocity", "omega", "acceleration"):
+        _, m32, r32, mg, rg = err[k]
+        assert rg <= 3 * r32 + 1e-6, (k, rg, r32)
+        assert mg <= 25 * m32 + 1e-6, (k, mg, m32)
+    rho_g, rho_a, rho_d = g["position"][:, 3], a["position"][:, 3], d["position"][:, 3]
+    assert np.abs(rho_g - rho_a).max() <= 1e-5 * rho_a.max()
+    assert np.abs(rho_g - rho_d).max() <= 1e-5 * rho_d.max()
+    assert np.abs(g["position"][:, :3] - a["position"][:, :3]).max() <= 1e-5
+    assert err["normal"][3] <= 1e-4
+
+
+def test_sphere_drop_snapshot_exact_mode_bitexact(sphere_drop):
+    sc, snap = sphere_drop
+    cfg = scenes.copy_config(sc.config)
+    cfg.fp_mode = L.FP_EXACT
+    sim = PBF(cfg)
+    try:
+        sim.set_state(snap["x"], snap["v"], snap["a"])
+        _set_field(sim, sc.field)
+        sim.set_capture(True)
+        sim.run()
+        dims, cells = O.grid_dims(cfg)
+        got_search = {k: sim.search_state(k, cells) for k in SEARCH}
+        g = _gpu_fields(sim)
+    finally:
+        sim.close()
+    o = _oracle_from(sc, snap, 32)
+    o.substep(1)
+    a = _oracle_fields(o)
+    ref_search = {k: o.search_state(k) for k in SEARCH}
+    o.close()
+    for k in SEARCH:
+        assert np.array_equal(got_search[k], ref_search[k]), k
+    for k in g:
+        assert np.array_equal(g[k], a[k]), (k, float(np.abs(g[k].astype(np.float64) - a[k]).max()))
+
+
+# ---- 2. the dam break ---------------------------------------------------------------------------
+@pytest.fixture(scope="module")
+def dam_break():
+    cfg, pts, fa = scenes.dam_break_16k_spec(seed=0)
+    field = scenes.generate_field(fa["shapes"], fa["res"], fa["origin"], fa["extent"], fa["h"], quadrature=12)
+    return cfg, pts, field
+
+
+def test_dam_break_first_substep_search_bitexact(dam_break):
+    cfg0, pts, field = dam_break
+    cfg = scenes.copy_config(cfg0)
+    cfg.fp_mode = L.FP_EXACT
+    sim = PBF(cfg)
+    try:
+        sim.set_particles(pts)
+        _set_field(sim, field)
+        sim.run()
+        dims, cells = O.grid_dims(cfg)
+        got = {k: sim.search_state(k, cells) for k in SEARCH}
+        x_gpu = sim.positions()
+    finally:
+        sim.close()
+    o = O.Oracle(cfg, 32)
+    o.set_particles(pts)
+    _set_field(o, field)
+    o.substep(1)
+    ref = {k: o.search_state(k) for k in SEARCH}
+    assert np.array_equal(x_gpu, o.field(L.FIELD_POSITION).astype(np.float32))
+    o.close()
+    for k in SEARCH:
+        assert np.array_equal(got[k], ref[k]), k
+    assert int(got["cell_offset"][-1]) == pts.shape[0]
+    assert np.array_equal(np.diff(got["cell_offset"].astype(np.int64)), got["cell_count"].astype(np.int64))
+
+
+def _oracle_stats(orc, field, rho0, m):
+    x = orc.field(L.FIELD_POSITION)
+    v = orc.field(L.FIELD_VELOCITY)[:, :3]
+    comp = np.maximum(0.0, x[:, 3] / rho0 - 1.0)
+    sdf = O.interpolate(field["res"], field["origin"], field["extent"], field["sdf"], field["vol"],
+                        x[:, :3].astype(np.float32).astype(np.float64))[:, 0]
+    return dict(ke=0.5 * m * float(np.sum(v * v)), mean_comp=float(comp.mean()), max_comp=float(comp.max()),
+                pen=int((sdf < 0).sum()), nonfinite=int((~np.isfinite(x[:, :3]).all(1) | ~np.isfinite(v).all(1)).sum()))
+
+
+def test_dam_break_trajectory_statistics(dam_break):
+    cfg0, pts, field = dam_break
+    n = pts.shape[0]
+    cfg = scenes.copy_config(cfg0)
+    cfg.fp_mode = L.FP_FAST
+    sim = PBF(cfg)
+    o = O.Oracle(scenes.copy_config(cfg0), 32)
+    gpu, cpu = [], []
+    try:
+        sim.set_particles(pts)
+        _set_field(sim, field)
+        _tuned(sim)
+        sim.enable_graph(True)
+        o.set_particles(pts)
+        _set_field(o, field)
+        r, rho0 = float(cfg0.particle_radius), float(cfg0.rest_density)
+        mass = 0.9 * (2 * r) ** 3 * rho0  # SPH.ts:49-50
+        for _ in range(10):
+            sim.step(20)
+            o.substep(20 * cfg0.substeps)
+            m = sim.metrics()
+            gpu.append(dict(ke=m["kinetic_energy"], mean_comp=m["mean_compression"], max_comp=m["max_compression"],
+                            pen=m["penetrations"], nonfinite=m["nonfinite"]))
+            cpu.append(_oracle_stats(o, field, rho0, mass))
+    finally:
+        sim.close()
+        o.close()
+    print("\ndam_break_16k, every 20 frames: (GPU production mode | FP32 restatement)")
+    print("| frame | KE | mean compression | max compression | penetrations |")
+    print("|---|---|---|---|---|")
+    for i, (g, c) in enumerate(zip(gpu, cpu)):
+        print("| %d | %.4g / %.4g | %.4f / %.4f | %.4f / %.4f | %d / %d |" % (
+            20 * (i + 1), g["ke"], c["ke"], g["mean_comp"], c["mean_comp"], g["max_comp"], c["max_comp"], g["pen"],
+            c["pen"]))
+    peak = {k: max(c[k] for c in cpu) for k in ("ke", "mean_comp", "max_comp")}
+    for g, c in zip(gpu, cpu):
+        assert g["nonfinite"] == 0 and c["nonfinite"] == 0
+        assert g["pen"] <= n // 1000 and c["pen"] <= n // 1000
+        assert abs(g["ke"] - c["ke"]) <= 0.10 * peak["ke"], (g["ke"], c["ke"])
+        assert abs(g["mean_comp"] - c["mean_comp"]) <= 0.25 * peak["mean_comp"] + 1e-3
+        assert abs(g["max_comp"] - c["max_comp"]) <= 0.50 * peak["max_comp"] + 1e-2

@@ -1227,21 +1227,30 @@ int pbf_set_particles(pbf_handle* h, const float* xyzw, uint32_t n) {
   return upload_particles(h, xyzw, n);
 }
 
-int pbf_set_velocities(pbf_handle* h, const float* xyzw, uint32_t n) {
+// Overwrites a per-particle float4 state array (slot order on the device)
+// from a by-id host array: the host reorders through the current ids
+// (slot -> id); w is cleared.
+static int upload_by_id(pbf_handle* h, float4* dst, const float* xyzw, uint32_t n, const char* what) {
   if (!h || !xyzw) return PBF_EINVAL;
-  if (n != h->n) return fail(h, PBF_EINVAL, "velocity count %u != particle count %u", n, h->n);
-  // velocities are stored in slot order: scatter through the current ids
-  // (slot -> id); upload by id into out_tmp then gather with a host-side inverse
+  if (n != h->n) return fail(h, PBF_EINVAL, "%s count %u != particle count %u", what, n, h->n);
   std::vector<uint32_t> ids(n);
   CU(h, cudaMemcpyAsync(ids.data(), h->ids[h->cur].p, (size_t)n * 4, cudaMemcpyDeviceToHost, h->stream));
   CU(h, cudaStreamSynchronize(h->stream));
   std::vector<float> v((size_t)n * 4);
   for (uint32_t t = 0; t < n; ++t)
     for (int a = 0; a < 4; ++a) v[4 * (size_t)t + a] = (a == 3) ? 0.0f : xyzw[4 * (size_t)ids[t] + a];
-  CU(h, cudaMemcpyAsync(h->vel.p, v.data(), (size_t)n * sizeof(float4), cudaMemcpyHostToDevice, h->stream));
+  CU(h, cudaMemcpyAsync(dst, v.data(), (size_t)n * sizeof(float4), cudaMemcpyHostToDevice, h->stream));
   CU(h, cudaStreamSynchronize(h->stream));
   invalidate_graph(h);
   return PBF_OK;
+}
+
+int pbf_set_velocities(pbf_handle* h, const float* xyzw, uint32_t n) {
+  return h ? upload_by_id(h, h->vel.p, xyzw, n, "velocity") : PBF_EINVAL;
+}
+
+int pbf_set_accelerations(pbf_handle* h, const float* xyzw, uint32_t n) {
+  return h ? upload_by_id(h, h->acc.p, xyzw, n, "acceleration") : PBF_EINVAL;
 }
 
 size_t pbf_field_length(const uint32_t res[3]) {
@@ -1381,7 +1390,10 @@ int pbf_enable_graph(pbf_handle* h, int enable) {
 int pbf_step(pbf_handle* h, uint32_t frames) {
   if (!h) return PBF_EINVAL;
   if (h->paused || h->n == 0) return PBF_OK;
-  if (!h->graph_enabled || h->ktiming) {
+  // Trace capture samples a different particle subset every substep (its salt
+  // and the substep counter are host values a graph would freeze), so it
+  // runs eagerly, as per-kernel timing does.
+  if (!h->graph_enabled || h->ktiming || h->trace_cap > 0) {
     for (uint32_t f = 0; f < frames; ++f) {
       int rc = frame(h);
       if (rc) return rc;
@@ -1720,6 +1732,39 @@ int pbf_copy_field(pbf_handle* h, int field, void* host, size_t bytes) {
     }
   }
   CU(h, cudaStreamSynchronize(st));
+  return check_device_errors(h);
+}
+
+int pbf_copy_search_state(pbf_handle* h, int which, uint32_t* host, size_t count) {
+  if (!h || (!host && count)) return PBF_EINVAL;
+  if (h->batch) return not_for_batch(h, "pbf_copy_search_state");
+  const uint32_t n = h->n;
+  cudaStream_t st = h->stream;
+  size_t need = 0;
+  switch (which) {
+    case PBF_SEARCH_CELL_KEY:
+    case PBF_SEARCH_ORDER: need = n; break;
+    case PBF_SEARCH_CELL_COUNT: need = h->gp.cells; break;
+    case PBF_SEARCH_CELL_OFFSET: need = (size_t)h->gp.cells + 1; break;
+    default: return fail(h, PBF_EINVAL, "unknown search array %d", which);
+  }
+  if (count != need) return fail(h, PBF_EINVAL, "search array %d has %zu entries, got %zu", which, need, count);
+  if (need == 0) return PBF_OK;
+  if (which == PBF_SEARCH_CELL_KEY) {
+    // keys were computed in the slot order before the sort: slot s of the
+    // previous order held particle ids[1 - cur][s]
+    std::vector<uint32_t> key(n), old_ids(n);
+    CU(h, cudaMemcpyAsync(key.data(), h->key.p, (size_t)n * 4, cudaMemcpyDeviceToHost, st));
+    CU(h, cudaMemcpyAsync(old_ids.data(), h->ids[1 - h->cur].p, (size_t)n * 4, cudaMemcpyDeviceToHost, st));
+    CU(h, cudaStreamSynchronize(st));
+    for (uint32_t s = 0; s < n; ++s) host[old_ids[s]] = key[s];
+  } else {
+    const uint32_t* src = which == PBF_SEARCH_ORDER        ? h->ids[h->cur].p
+                          : which == PBF_SEARCH_CELL_COUNT ? h->cell_count.p
+                                                           : h->cell_start.p;
+    CU(h, cudaMemcpyAsync(host, src, need * 4, cudaMemcpyDeviceToHost, st));
+    CU(h, cudaStreamSynchronize(st));
+  }
   return check_device_errors(h);
 }
 
@@ -2304,12 +2349,15 @@ int pbf_exclusive_scan_u32(const uint32_t* d_in, uint32_t* d_out, size_t n, void
   size_t bytes = scan_scratch_bytes(n);
   if (cudaMallocAsync(&scratch, bytes + 16, st) != cudaSuccess) return PBF_ECUDA;
   err = (uint32_t*)((char*)scratch + bytes);
-  if (cudaMemsetAsync(err, 0, 4, st) != cudaSuccess) return PBF_ECUDA;
-  if (launch_exclusive_scan(d_in, d_out, n, scratch, err, st) != cudaSuccess) return PBF_ECUDA;
   uint32_t e = 0;
-  if (cudaMemcpyAsync(&e, err, 4, cudaMemcpyDeviceToHost, st) != cudaSuccess) return PBF_ECUDA;
-  if (cudaFreeAsync(scratch, st) != cudaSuccess) return PBF_ECUDA;
-  if (cudaStreamSynchronize(st) != cudaSuccess) return PBF_ECUDA;
+  // every path after the allocation releases the scratch
+  cudaError_t ce = cudaMemsetAsync(err, 0, 4, st);
+  if (ce == cudaSuccess) ce = launch_exclusive_scan(d_in, d_out, n, scratch, err, st);
+  if (ce == cudaSuccess) ce = cudaMemcpyAsync(&e, err, 4, cudaMemcpyDeviceToHost, st);
+  const cudaError_t fe = cudaFreeAsync(scratch, st);
+  if (ce == cudaSuccess) ce = fe;
+  if (ce == cudaSuccess) ce = cudaStreamSynchronize(st);
+  if (ce != cudaSuccess) return PBF_ECUDA;
   return e ? PBF_ETIMEOUT : PBF_OK;
 }
 

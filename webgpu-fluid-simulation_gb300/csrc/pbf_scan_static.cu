@@ -2,12 +2,18 @@
 //
 // Some callers cannot allocate device memory at the moment they need a
 // prefix sum: a host framework that owns every device byte through its own
-// pool and forbids other allocators, a real-time frame loop that must not
-// enter the CUDA allocator, or code that runs while a stream is being
-// captured.  pbf_exclusive_scan_u32_noalloc serves them: the caller passes
-// the input and output arrays and the scan's look-back scratch lives in the
-// fixed file-scope device array below, which every GPU that loads this
-// library holds until the process exits.
+// pool and forbids other allocators, or a real-time frame loop that must not
+// enter the CUDA allocator.  pbf_exclusive_scan_u32_noalloc serves them: the
+// caller passes the input and output arrays and the scan's look-back scratch
+// lives in the fixed file-scope device array below, which every GPU that
+// loads this library holds until the process exits.
+//
+// The call is synchronous: after the scan it copies the device error word
+// back to the host and synchronises the caller's stream, so it cannot be
+// recorded into a CUDA graph.  The array's device address is looked up once
+// per device (first call, that device current) and cached for the life of
+// the process; do not keep using the library on a device after
+// cudaDeviceReset there.
 //
 // The array is shared by all calls on a device and keeps the last call's
 // contents; each call clears the parts that must start at zero (tile

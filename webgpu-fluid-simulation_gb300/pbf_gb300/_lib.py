@@ -18,6 +18,7 @@ INTERP_CUBIC, INTERP_TRILINEAR = 0, 1
 (FIELD_POSITION, FIELD_VELOCITY, FIELD_ACCELERATION, FIELD_PREDICTED, FIELD_LAMBDA, FIELD_BOUNDARY,
  FIELD_OMEGA, FIELD_NORMAL, FIELD_DELTA_P, FIELD_NEIGHBOR_COUNT) = range(10)
 SCAN_NOALLOC_MAX = 1 << 26
+SEARCH_ARRAYS = {"keys": 0, "cell_count": 1, "cell_offset": 2, "order": 3}  # pbf_search_array
 SCALAR_FIELDS = {FIELD_LAMBDA: "f4", FIELD_NEIGHBOR_COUNT: "u4"}
 
 u32, f32 = ctypes.c_uint32, ctypes.c_float
@@ -159,6 +160,8 @@ SIGNATURES = {
     "pbf_set_particle_position": (ctypes.c_int, [_P]),
     "pbf_set_particles": (ctypes.c_int, [_P, _FP, u32]),
     "pbf_set_velocities": (ctypes.c_int, [_P, _FP, u32]),
+    "pbf_set_accelerations": (ctypes.c_int, [_P, _FP, u32]),
+    "pbf_copy_search_state": (ctypes.c_int, [_P, ctypes.c_int, _UP, ctypes.c_size_t]),
     "pbf_set_boundary_data": (ctypes.c_int, [_P, ctypes.c_char_p, ctypes.c_size_t]),
     "pbf_set_boundary_field": (ctypes.c_int, [_P, _UP, _FP, _FP, _FP, _FP, ctypes.c_size_t]),
     "pbf_clear_boundary": (ctypes.c_int, [_P]),

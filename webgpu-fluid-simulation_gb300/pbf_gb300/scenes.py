@@ -249,8 +249,20 @@ def reference_scene(name, **kw):
     return Scene(name, cfg, pts, field, frames=1)
 
 
+def field_length(res):
+    """Floats per field of a volume map of res = (nx, ny, nz) cells
+    (BoundaryModel.FIELD_LENGTH, src/simulator/boundary/volumeMap.ts:7-11):
+    the corner nodes, then two nodes on every x-, y- and z-edge."""
+    nx, ny, nz = (int(v) for v in res)
+    return ((nx + 1) * (ny + 1) * (nz + 1) + 2 * nx * (ny + 1) * (nz + 1) + (nx + 1) * 2 * ny * (nz + 1)
+            + (nx + 1) * (ny + 1) * 2 * nz)
+
+
 def generate_field(shapes, res, origin, extent, h, quadrature=12, flags=0, backend="gpu"):
-    """Volume map for analytic shapes: list of (kind, center, size)."""
+    """Volume map for analytic shapes: list of (kind, center, size).
+    backend "gpu" runs pbf_generate_volume_map; otherwise a callable with the
+    same arguments (the CPU restatement's generator) is used and the CUDA
+    library is not loaded."""
     arr = (L.Shape * len(shapes))()
     for i, (kind, c, s) in enumerate(shapes):
         arr[i].kind = kind
@@ -259,12 +271,12 @@ def generate_field(shapes, res, origin, extent, h, quadrature=12, flags=0, backe
     r = (ctypes.c_uint32 * 3)(*[int(x) for x in res])
     o = (ctypes.c_float * 3)(*[float(x) for x in origin])
     e = (ctypes.c_float * 3)(*[float(x) for x in extent])
-    lib = L.load()
-    n = lib.pbf_field_length(r)
+    n = field_length(res)
     sdf = np.zeros(n, np.float32)
     vol = np.zeros(n, np.float32)
     fp = ctypes.POINTER(ctypes.c_float)
     if backend == "gpu":
+        lib = L.load()
         rc = lib.pbf_generate_volume_map(arr, len(shapes), r, o, e, float(h), int(quadrature), int(flags),
                                          sdf.ctypes.data_as(fp), vol.ctypes.data_as(fp))
     else:

@@ -186,6 +186,31 @@ class PBF:
         self._check(self._lib.pbf_set_velocities(
             self._h, a.ctypes.data_as(ctypes.POINTER(ctypes.c_float)), a.shape[0]), "set_velocities")
 
+    def set_accelerations(self, xyzw):
+        a = np.ascontiguousarray(xyzw, dtype=np.float32)
+        self._check(self._lib.pbf_set_accelerations(
+            self._h, a.ctypes.data_as(ctypes.POINTER(ctypes.c_float)), a.shape[0]), "set_accelerations")
+
+    def set_state(self, positions, velocities, accelerations):
+        """Restores a saved state (by particle id): x, v and a."""
+        self.set_particles(positions)
+        self.set_velocities(velocities)
+        self.set_accelerations(accelerations)
+
+    def search_state(self, which, cells=None):
+        """The last substep's neighbour search: 'keys' (per particle),
+        'cell_count' / 'cell_offset' (per cell; `cells` = the grid's cell
+        count) or 'order' (slot -> particle id)."""
+        n = self.particleCount
+        size = {"keys": n, "order": n, "cell_count": cells, "cell_offset": None if cells is None else cells + 1}[which]
+        if size is None:
+            raise ValueError("search_state(%r) needs the grid's cell count" % which)
+        out = np.zeros(size, np.uint32)
+        self._check(self._lib.pbf_copy_search_state(self._h, L.SEARCH_ARRAYS[which],
+                                                    out.ctypes.data_as(ctypes.POINTER(ctypes.c_uint32)), size),
+                    "search_state")
+        return out
+
     # ---- boundary -----------------------------------------------------------
     def setBoundaryData(self, text):
         b = text.encode() if isinstance(text, str) else bytes(text)

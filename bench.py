@@ -511,7 +511,7 @@ _LAUNCH = None  # the autotuner's launch shape, applied to every handle of the r
 # plain solve's; the other variants are reported beside it, never selected.
 HEADLINE = {"name": "learned1", "learned_iters": 1}
 CMP_FRAMES = 100  # frames per arm in the learned-vs-plain comparison
-LEARNED_VARIANTS = (("learned2", 2, 0.0), ("learned1", 1, 0.0), ("learned1l30", 1, 0.3))
+LEARNED_VARIANTS = (("learned2", 2, 0.0), ("learned1", 1, 0.0))
 
 
 def _handle_from(sc, snap, iterations=None):

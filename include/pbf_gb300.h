@@ -135,6 +135,8 @@ typedef struct pbf_metrics {
 #define PBF_DEVERR_SCAN_TIMEOUT 0x2u
 #define PBF_DEVERR_CELL_OVERFLOW 0x4u
 #define PBF_DEVERR_MMA_TIMEOUT 0x8u  /* a tensor-core completion wait gave up (network pass) */
+#define PBF_DEVERR_STAGE_TIMEOUT 0x10u /* a cell-block pass's shared-memory staging wait gave up (the tile
+                                          then read global memory; results are still complete) */
 
 typedef struct pbf_handle pbf_handle;
 
@@ -496,12 +498,31 @@ typedef struct pbf_launch {
   uint32_t build;        /* neighbour-build variant: PBF_BUILD_THREAD (default, one slot
                             per thread), PBF_BUILD_PAIR (two slots of one cell per thread,
                             sharing candidate loads), PBF_BUILD_WARP (warp-cooperative
-                            per cell: coalesced candidate chunks, ballot-collected hits) */
+                            per cell: coalesced candidate chunks, ballot-collected hits);
+                            or one of the cell-block modes, which replace the neighbour
+                            lists: each neighbour pass runs one CTA per 128 sorted slots,
+                            stages the tile's 27-cell halo (the 3 x 3 neighbouring
+                            columns' slot runs) into shared memory with bulk copies and
+                            walks it in the reference's neighbour order.
+                            PBF_BUILD_CELLBLOCK_MASK keeps 9 membership masks per particle
+                            (one 32-bit mask per neighbour column, written by a cell-block
+                            search); PBF_BUILD_CELLBLOCK_FREE keeps no neighbour structure
+                            and tests every candidate at the search positions in every
+                            pass.  Both give the list's neighbour sets and order (exact
+                            mode stays bit-identical to the reference method); single-scene
+                            handles with ctas_per_sm = 0 only. */
 } pbf_launch;
 #define PBF_BUILD_THREAD 0u
 #define PBF_BUILD_PAIR 1u
 #define PBF_BUILD_WARP 2u
+#define PBF_BUILD_CELLBLOCK_MASK 3u
+#define PBF_BUILD_CELLBLOCK_FREE 4u
 int pbf_set_launch(pbf_handle* h, const pbf_launch* launch);
+/* Shared-memory plan of the cell-block passes (no counterpart in the
+ * reference): the records per staged field a CTA holds (a multiple of 16 in
+ * [16, 4096]; default 2048).  A tile whose halo needs more (or spans more
+ * than 8 cell columns) walks global memory instead, with the same results. */
+int pbf_set_cellblock_capacity(pbf_handle* h, uint32_t records);
 int pbf_get_launch(const pbf_handle* h, pbf_launch* launch);
 
 typedef struct pbf_tune_trial {

@@ -68,6 +68,13 @@ struct pbf_handle {
   DBuf<uint32_t> cell_count, cell_start, big_list, big_count;
   DBuf<uint32_t> nbr_count, nbr_max, nbr_list;
   DBuf<uint32_t> band_list[2], band_count;  // boundary band lists (ping-pong) and their lengths
+  // cell-block passes (PBF_BUILD_CELLBLOCK_*): cell key and x*_0 per sorted
+  // slot, the 9 window masks per slot and their overflow bits
+  DBuf<uint32_t> skey, cb_mask;
+  DBuf<uint16_t> cb_ovf;
+  DBuf<float4> xs0;
+  uint32_t cb_cap = 2048;   // staged records per field and CTA
+  unsigned cb_fb_grid = 0;  // CTAs of the cell-block fallback kernel
   DBuf<float> sdf, vol;
   DBuf<uint8_t> bflag;  // per field cell: 1 when the boundary sample can be non-zero
   DBuf<uint32_t> err_word;
@@ -294,6 +301,33 @@ inline unsigned grid_of(const pbf_handle* h, uint32_t n) {
   return g ? g : 1u;
 }
 
+// Cell-block passes in use (PBF_BUILD_CELLBLOCK_*): single scene, one tile per CTA.
+inline bool cb_active(const pbf_handle* h) {
+  return (h->build == PBF_BUILD_CELLBLOCK_MASK || h->build == PBF_BUILD_CELLBLOCK_FREE) && !h->batch &&
+         h->grid_cap == 0;
+}
+constexpr int kMemMaskHost = 0;  // CbSet index of the mask variant (1: the list-free variant)
+inline int cb_memb(const pbf_handle* h) { return h->build == PBF_BUILD_CELLBLOCK_FREE ? 1 : kMemMaskHost; }
+inline unsigned cb_grid(uint32_t n) { return (n + 127u) / 128u; }
+// Dynamic shared memory of a cell-block pass staging kP fields (+ x*_0 when
+// membership is tested).
+inline size_t cb_smem(const pbf_handle* h, int kP) {
+  return (size_t)(kP + cb_memb(h)) * h->cb_cap * sizeof(float4);
+}
+CbArgs cb_args(const pbf_handle* h) {
+  CbArgs A{};
+  A.g = h->gp;
+  A.cell_start = h->cell_start.p;
+  A.skey = h->skey.p;
+  A.xs0 = h->xs0.p;
+  A.mask = h->cb_mask.p;
+  A.ovf = h->cb_ovf.p;
+  A.err = h->err_word.p;
+  A.cap = h->cb_cap;
+  A.n = h->n;
+  return A;
+}
+
 void invalidate_graph(pbf_handle* h) {
   if (h->graph_exec) cudaGraphExecDestroy(h->graph_exec);
   h->graph_exec = nullptr;
@@ -348,6 +382,12 @@ int substep(pbf_handle* h, cudaEvent_t* ev) {
   const GridParams g = h->gp;
   const int c = h->cur, nx = 1 - c;
   const PassSet& ps = h->passes.set[h->batch ? 1 : 0][h->grid_cap ? 1 : 0];
+  // cell-block passes: one CTA per 128 sorted slots, the halo staged in
+  // shared memory (pbf_cellblock.cuh)
+  const bool cb = cb_active(h);
+  const CbSet& cs = h->passes.cb[cb_memb(h)];
+  CbArgs A = cb ? cb_args(h) : CbArgs{};
+  const unsigned cbg = cb_grid(n);
   if (ev) CU(h, cudaEventRecord(ev[0], st));
   // neighborSearch.clearBuffer + TimeIntegration (+ ParticleInsert counts)
   CU(h, cudaMemsetAsync(h->cell_count.p, 0, ((size_t)g.cells + 1) * sizeof(uint32_t), st));
@@ -368,8 +408,12 @@ int substep(pbf_handle* h, cudaEvent_t* ev) {
   }
   {
     KScope ks(h, K_GATHER);
-    CU(h, launch_gather_state(n, h->perm.p, h->pos[c].p, h->xs[1].p, h->ids[c].p, h->pos[nx].p, h->xs[0].p,
-                              h->ids[nx].p, st));
+    if (cb)
+      CU(h, launch_gather_state_cb(n, h->perm.p, h->pos[c].p, h->xs[1].p, h->ids[c].p, h->key.p, h->pos[nx].p,
+                                   h->xs[0].p, h->ids[nx].p, h->skey.p, h->xs0.p, st));
+    else
+      CU(h, launch_gather_state(n, h->perm.p, h->pos[c].p, h->xs[1].p, h->ids[c].p, h->pos[nx].p, h->xs[0].p,
+                                h->ids[nx].p, st));
   }
   const bool need_feat = h->learned || h->trace_cap > 0;
   if (need_feat) CU(h, launch_gather_f32(n, h->perm.p, h->lam_sum.p, h->lam_prev.p, st));
@@ -421,9 +465,21 @@ int substep(pbf_handle* h, cudaEvent_t* ev) {
     al.substep_index = sub_index;
     al.feat = h->feat.p;
     KScope ks(h, K_FEATURES);
-    ps.nbr_build_feat<<<grid_of(h, n), h->blk, 0, st>>>(p, g, h->xs[0].p, h->cell_start.p, ms, h->nbr_list.p,
-                                                         h->nbr_count.p, h->nbr_max.p, h->err_word.p, f.loaded,
-                                                         h->bdata.p, al);
+    if (cb)
+      h->passes.cb_build_feat<<<cbg, 128, (size_t)h->cb_cap * sizeof(float4), st>>>(
+          p, A, h->cb_mask.p, h->cb_ovf.p, h->nbr_count.p, f.loaded, h->bdata.p, al);
+    else
+      ps.nbr_build_feat<<<grid_of(h, n), h->blk, 0, st>>>(p, g, h->xs[0].p, h->cell_start.p, ms, h->nbr_list.p,
+                                                           h->nbr_count.p, h->nbr_max.p, h->err_word.p, f.loaded,
+                                                           h->bdata.p, al);
+  } else if (cb) {
+    // the mask variant's search; the list-free variant has none (the
+    // density pass counts the neighbours)
+    if (cb_memb(h) == kMemMaskHost) {
+      KScope ks(h, K_NBR_BUILD);
+      h->passes.cb_build<<<cbg, 128, (size_t)h->cb_cap * sizeof(float4), st>>>(
+          p, A, h->cb_mask.p, h->cb_ovf.p, h->nbr_count.p, 0, nullptr, SolverAux{});
+    }
   } else {
     KScope ks(h, K_NBR_BUILD);
     if (h->build == PBF_BUILD_PAIR)
@@ -483,9 +539,14 @@ int substep(pbf_handle* h, cudaEvent_t* ev) {
       }
       {
         KScope ks(h, K_LAMBDA);
-        auto kl = fe ? ps.lambda_feat : (al.stats && adaptive ? ps.lambda_stats : ps.lambda);
-        kl<<<grid_of(h, n), h->blk, 0, st>>>(p, f.loaded, h->bdata.p, h->xs[a].p, ms, h->nbr_count.p,
-                                             h->nbr_list.p, h->xl.p, al);
+        if (cb) {
+          auto kl = fe ? cs.lambda_feat : (al.stats && adaptive ? cs.lambda_stats : cs.lambda);
+          kl<<<cbg, 128, cb_smem(h, 1), st>>>(p, A, f.loaded, h->bdata.p, h->xs[a].p, h->xl.p, al);
+        } else {
+          auto kl = fe ? ps.lambda_feat : (al.stats && adaptive ? ps.lambda_stats : ps.lambda);
+          kl<<<grid_of(h, n), h->blk, 0, st>>>(p, f.loaded, h->bdata.p, h->xs[a].p, ms, h->nbr_count.p,
+                                               h->nbr_list.p, h->xl.p, al);
+        }
       }
       if (cudaGetLastError() != cudaSuccess) { *rc = PBF_ECUDA; return a; }
       SolverAux ad{};
@@ -508,8 +569,12 @@ int substep(pbf_handle* h, cudaEvent_t* ev) {
       }
       {
         KScope ks(h, K_DELTAP);
-        ps.deltap<<<grid_of(h, n), h->blk, 0, st>>>(p, ad, f.loaded, h->xl.p, h->bdata.p, ms, h->nbr_count.p,
-                                                     h->nbr_list.p, h->xs[1 - a].p, h->capture ? h->dp.p : nullptr);
+        if (cb)
+          cs.deltap<<<cbg, 128, cb_smem(h, 1), st>>>(p, A, ad, f.loaded, h->xl.p, h->bdata.p, h->xs[1 - a].p,
+                                                     h->capture ? h->dp.p : nullptr);
+        else
+          ps.deltap<<<grid_of(h, n), h->blk, 0, st>>>(p, ad, f.loaded, h->xl.p, h->bdata.p, ms, h->nbr_count.p,
+                                                       h->nbr_list.p, h->xs[1 - a].p, h->capture ? h->dp.p : nullptr);
       }
       if (cudaGetLastError() != cudaSuccess) { *rc = PBF_ECUDA; return a; }
       a = 1 - a;
@@ -538,8 +603,11 @@ int substep(pbf_handle* h, cudaEvent_t* ev) {
         ad.band = band_args(1 - band, nullptr);
         band = 1 - band;
       }
-      ps.deltap<<<grid_of(h, n), h->blk, 0, st>>>(p, ad, f.loaded, h->xl.p, h->bdata.p, ms, h->nbr_count.p,
-                                                   h->nbr_list.p, h->xs[1].p, nullptr);
+      if (cb)
+        cs.deltap<<<cbg, 128, cb_smem(h, 1), st>>>(p, A, ad, f.loaded, h->xl.p, h->bdata.p, h->xs[1].p, nullptr);
+      else
+        ps.deltap<<<grid_of(h, n), h->blk, 0, st>>>(p, ad, f.loaded, h->xl.p, h->bdata.p, ms, h->nbr_count.p,
+                                                     h->nbr_list.p, h->xs[1].p, nullptr);
     }
     CU(h, cudaGetLastError());
     a = iterate(1, h->learned_iters, false, true, false, nullptr, &rc, h->adaptive, h->lagged_fraction > 0.0f);
@@ -565,8 +633,12 @@ int substep(pbf_handle* h, cudaEvent_t* ev) {
     KScope ks(h, K_DENSITY);
     SolverAux ad{};
     if (h->learned || rec) ad.stats = h->stats.p;
-    ps.density_velocity<<<grid_of(h, n), h->blk, 0, st>>>(p, ad, h->xs[a].p, ms, h->nbr_count.p,
-                                                                 h->nbr_list.p, h->pos[cc].p, h->vel.p);
+    if (cb)
+      cs.density_velocity<<<cbg, 128, cb_smem(h, 1), st>>>(p, A, ad, h->xs[a].p, h->pos[cc].p, h->vel.p,
+                                                            cb_memb(h) == kMemMaskHost ? nullptr : h->nbr_count.p);
+    else
+      ps.density_velocity<<<grid_of(h, n), h->blk, 0, st>>>(p, ad, h->xs[a].p, ms, h->nbr_count.p,
+                                                             h->nbr_list.p, h->pos[cc].p, h->vel.p);
   }
   CU(h, cudaGetLastError());
   if (rec) CU(h, launch_stats_record(h->stats.p, h->trace_err.p, st));
@@ -596,18 +668,54 @@ int substep(pbf_handle* h, cudaEvent_t* ev) {
     fa.max_nbr = ms;
     fa.iters = (int)h->cfg.options.iterations;
     fa.final_buf = a;
-    if (h->fb_grid == 0) {
-      int per_sm = 0;
-      CU(h, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, h->passes.fallback, 256, 0));
-      if (per_sm < 1) return fail(h, PBF_ECUDA, "fallback kernel does not fit on an SM");
-      h->fb_grid = (unsigned)per_sm * (unsigned)h->sms;
+    if (cb) {
+      if (h->cb_fb_grid == 0) {
+        int per_sm = 0;
+        CU(h, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, cs.fallback, 256, 0));
+        if (per_sm < 1) return fail(h, PBF_ECUDA, "fallback kernel does not fit on an SM");
+        h->cb_fb_grid = (unsigned)per_sm * (unsigned)h->sms;
+      }
+      void* args[] = {&fa, &A};
+      CU(h, cudaLaunchCooperativeKernel((const void*)cs.fallback, dim3(std::min(h->cb_fb_grid, nblocks(n, 256))),
+                                        dim3(256), args, 0, st));
+    } else {
+      if (h->fb_grid == 0) {
+        int per_sm = 0;
+        CU(h, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, h->passes.fallback, 256, 0));
+        if (per_sm < 1) return fail(h, PBF_ECUDA, "fallback kernel does not fit on an SM");
+        h->fb_grid = (unsigned)per_sm * (unsigned)h->sms;
+      }
+      void* args[] = {&fa};
+      CU(h, cudaLaunchCooperativeKernel((const void*)h->passes.fallback, dim3(std::min(h->fb_grid, nblocks(n, 256))),
+                                        dim3(256), args, 0, st));
     }
-    void* args[] = {&fa};
-    CU(h, cudaLaunchCooperativeKernel((const void*)h->passes.fallback, dim3(std::min(h->fb_grid, nblocks(n, 256))),
-                                      dim3(256), args, 0, st));
   }
   if (a != 0) CU(h, cudaMemcpyAsync(h->xs[0].p, h->xs[1].p, (size_t)n * sizeof(float4), cudaMemcpyDeviceToDevice, st));
-  if (ps.xsph_split) {  // fast mode: XSPH's sum split over the two passes
+  if (cb && cs.xsph_split) {  // fast mode: XSPH's sum split over the two passes
+    {
+      KScope ks(h, K_VORTICITY);
+      cs.vorticity_split<<<cbg, 128, cb_smem(h, 2), st>>>(p, A, h->pos[cc].p, h->vel.p, h->omega.p, h->normal.p,
+                                                          h->visc.p, h->coh.p);
+    }
+    CU(h, cudaGetLastError());
+    {
+      KScope ks(h, K_XSPH);
+      cs.xsph_split<<<cbg, 128, cb_smem(h, 2), st>>>(p, A, h->pos[cc].p, h->omega.p, h->normal.p, h->visc.p,
+                                                     h->coh.p, h->acc.p);
+    }
+    CU(h, cudaGetLastError());
+  } else if (cb) {
+    {
+      KScope ks(h, K_VORTICITY);
+      cs.vorticity<<<cbg, 128, cb_smem(h, 2), st>>>(p, A, h->pos[cc].p, h->vel.p, h->omega.p, h->normal.p);
+    }
+    CU(h, cudaGetLastError());
+    {
+      KScope ks(h, K_XSPH);
+      cs.xsph<<<cbg, 128, cb_smem(h, 3), st>>>(p, A, h->pos[cc].p, h->vel.p, h->omega.p, h->normal.p, h->acc.p);
+    }
+    CU(h, cudaGetLastError());
+  } else if (ps.xsph_split) {  // fast mode: XSPH's sum split over the two passes
     {
       KScope ks(h, K_VORTICITY);
       ps.vorticity_split<<<grid_of(h, n), h->blk, 0, st>>>(p, h->pos[cc].p, h->vel.p, ms, h->nbr_count.p,
@@ -701,13 +809,14 @@ void release_all(pbf_handle* h) {
   invalidate_graph(h);
   DBuf<float4>* f4s[] = {&h->pos[0], &h->pos[1], &h->xs[0], &h->xs[1], &h->xl, &h->vel, &h->acc, &h->bdata,
                          &h->visc,   &h->coh,
-                         &h->omega,  &h->normal, &h->dp,    &h->out_pos, &h->out_tmp};
+                         &h->omega,  &h->normal, &h->dp,    &h->out_pos, &h->out_tmp, &h->xs0};
   for (auto* b : f4s) b->release();
   DBuf<uint32_t>* u32s[] = {&h->ids[0],   &h->ids[1],      &h->key,      &h->rank,      &h->perm_raw,
                             &h->id_raw,   &h->perm,        &h->tmp_a,    &h->tmp_b,     &h->cell_count,
                             &h->cell_start, &h->big_list,  &h->big_count, &h->nbr_count, &h->nbr_max,
-                            &h->nbr_list, &h->err_word,    &h->m_u};
+                            &h->nbr_list, &h->err_word,    &h->m_u,      &h->skey,      &h->cb_mask};
   for (auto* b : u32s) b->release();
+  h->cb_ovf.release();
   h->sdf.release();
   h->vol.release();
   h->bflag.release();
@@ -843,13 +952,47 @@ int apply_cell_ratio(pbf_handle* h, float ratio) {
   return PBF_OK;
 }
 
+// Buffers of the cell-block passes (allocated on first use) and the
+// kernels' shared-memory limits: up to four staged fields of cb_cap records.
+int ensure_cb(pbf_handle* h) {
+  const size_t cap = std::max<size_t>(h->cfg.max_particles, 1);
+  if (!h->skey.p) {
+    CU(h, h->skey.alloc(cap));
+    CU(h, h->xs0.alloc(cap));
+    CU(h, h->cb_mask.alloc(9 * cap));
+    CU(h, h->cb_ovf.alloc(cap));
+    CU(h, cudaMemsetAsync(h->cb_ovf.p, 0, cap * sizeof(uint16_t), h->stream));
+  }
+  const int bytes = (int)(4 * (size_t)h->cb_cap * sizeof(float4));
+  auto attr = [&](const void* k) -> cudaError_t {
+    return k ? cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes) : cudaSuccess;
+  };
+  const PassTable& T = h->passes;
+  CU(h, attr((const void*)T.cb_build));
+  CU(h, attr((const void*)T.cb_build_feat));
+  for (const CbSet& c : T.cb) {
+    for (const void* k : {(const void*)c.lambda, (const void*)c.lambda_feat, (const void*)c.lambda_stats,
+                          (const void*)c.deltap, (const void*)c.density_velocity, (const void*)c.vorticity,
+                          (const void*)c.xsph, (const void*)c.vorticity_split, (const void*)c.xsph_split})
+      CU(h, attr(k));
+  }
+  return PBF_OK;
+}
+
 int apply_launch(pbf_handle* h, const pbf_launch& l) {
   if (l.block != 128 && l.block != 256) return fail(h, PBF_EINVAL, "block must be 128 or 256");
   if (l.ctas_per_sm > 16) return fail(h, PBF_EINVAL, "ctas_per_sm must be 0..16");
   if (l.cell_ratio != 1.0f && l.cell_ratio != 0.5f) return fail(h, PBF_EINVAL, "cell_ratio must be 1 or 0.5");
-  if (l.build > PBF_BUILD_WARP) return fail(h, PBF_EINVAL, "unknown neighbour-build variant %u", l.build);
+  if (l.build > PBF_BUILD_CELLBLOCK_FREE) return fail(h, PBF_EINVAL, "unknown neighbour-build variant %u", l.build);
+  const bool cb = l.build == PBF_BUILD_CELLBLOCK_MASK || l.build == PBF_BUILD_CELLBLOCK_FREE;
+  if (cb && (h->batch || l.ctas_per_sm != 0))
+    return fail(h, PBF_EINVAL, "the cell-block passes need a single-scene handle and ctas_per_sm = 0");
   int rc = apply_cell_ratio(h, l.cell_ratio);
   if (rc) return rc;
+  if (cb) {
+    rc = ensure_cb(h);
+    if (rc) return rc;
+  }
   if ((int)l.block != h->blk || l.ctas_per_sm != h->per_sm || l.build != h->build) invalidate_graph(h);
   h->build = l.build;
   h->blk = (int)l.block;
@@ -1813,6 +1956,15 @@ int pbf_set_launch(pbf_handle* h, const pbf_launch* l) {
   return apply_launch(h, *l);
 }
 
+int pbf_set_cellblock_capacity(pbf_handle* h, uint32_t records) {
+  if (!h) return PBF_EINVAL;
+  if (records < 16 || records % 16 || records > 4096)
+    return fail(h, PBF_EINVAL, "cell-block capacity must be a multiple of 16 in [16, 4096]");
+  if (records != h->cb_cap) invalidate_graph(h);
+  h->cb_cap = records;
+  return cb_active(h) ? ensure_cb(h) : PBF_OK;
+}
+
 int pbf_get_launch(const pbf_handle* h, pbf_launch* l) {
   if (!h || !l) return PBF_EINVAL;
   l->block = (uint32_t)h->blk;
@@ -1883,11 +2035,18 @@ int pbf_autotune(pbf_handle* h, uint32_t substeps, uint32_t flags, pbf_tune_tria
   // one tile per CTA or a persistent grid holding all of an SM's 2048
   // threads; the three neighbour-build variants
   const uint32_t blocks[2] = {128, 256};
-  for (int r = 0; r < ((flags & PBF_TUNE_CELL_RATIO) ? 2 : 1); ++r)
+  for (int r = 0; r < ((flags & PBF_TUNE_CELL_RATIO) ? 2 : 1); ++r) {
     for (uint32_t b : blocks)
       for (uint32_t k : {0u, 2048u / b})
         for (uint32_t bv : {PBF_BUILD_THREAD, PBF_BUILD_PAIR, PBF_BUILD_WARP})
           cand.push_back(pbf_launch{b, k, ratios[r], bv});
+    // the cell-block passes (single scenes): their own 128-slot tiles; the
+    // other passes take either block size
+    if (!h->batch)
+      for (uint32_t b : blocks)
+        for (uint32_t bv : {PBF_BUILD_CELLBLOCK_MASK, PBF_BUILD_CELLBLOCK_FREE})
+          cand.push_back(pbf_launch{b, 0u, ratios[r], bv});
+  }
   const pbf_launch orig{(uint32_t)h->blk, h->per_sm, h->cell_ratio, h->build};
   const bool kt = h->ktiming;
   h->ktiming = false;

@@ -49,6 +49,21 @@ struct PassSet {
                      const uint32_t*, const uint32_t*, float4*);
 };
 
+// The cell-block passes of one membership variant (pbf_cellblock.cuh).
+struct CbSet {
+  void (*lambda)(SimParams, CbArgs, int, const float4*, const float4*, float4*, SolverAux);
+  void (*lambda_feat)(SimParams, CbArgs, int, const float4*, const float4*, float4*, SolverAux);
+  void (*lambda_stats)(SimParams, CbArgs, int, const float4*, const float4*, float4*, SolverAux);
+  void (*deltap)(SimParams, CbArgs, SolverAux, int, const float4*, const float4*, float4*, float4*);
+  void (*density_velocity)(SimParams, CbArgs, SolverAux, const float4*, float4*, float4*, uint32_t*);
+  void (*vorticity)(SimParams, CbArgs, const float4*, const float4*, float4*, float4*);
+  void (*xsph)(SimParams, CbArgs, const float4*, const float4*, const float4*, const float4*, float4*);
+  void (*vorticity_split)(SimParams, CbArgs, const float4*, const float4*, float4*, float4*, float4*, float4*);
+  void (*xsph_split)(SimParams, CbArgs, const float4*, const float4*, const float4*, const float4*, const float4*,
+                     float4*);
+  void (*fallback)(FallbackArgs, CbArgs);  // cooperative launch only
+};
+
 struct PassTable {
   // the stand-alone neighbour search (reference list layout)
   void (*nbr_count)(SimParams, GridParams, const float4*, const uint32_t*, uint32_t*);
@@ -56,6 +71,11 @@ struct PassTable {
                    uint32_t*);
   PassSet set[2][2];  // [batch][persistent]
   void (*fallback)(FallbackArgs);  // cooperative launch only
+  // cell-block passes: the search (masks; with the learned start's features)
+  // and the passes per membership variant [mask, test]
+  void (*cb_build)(SimParams, CbArgs, uint32_t*, uint16_t*, uint32_t*, int, const float4*, SolverAux);
+  void (*cb_build_feat)(SimParams, CbArgs, uint32_t*, uint16_t*, uint32_t*, int, const float4*, SolverAux);
+  CbSet cb[2];
 };
 
 namespace exact {
@@ -126,6 +146,12 @@ cudaError_t launch_sort_by_cell(GridParams g, uint32_t n, const uint32_t* ids, S
 cudaError_t launch_gather_state(uint32_t n, const uint32_t* perm, const float4* pos_in, const float4* xs_in,
                                 const uint32_t* id_in, float4* pos_out, float4* xs_out, uint32_t* id_out,
                                 cudaStream_t st);
+// The same gather that also writes, for the cell-block passes, the cell key
+// of each sorted slot (skey_out[t] = key_in[perm[t]]) and a second copy of
+// the predicted positions x*_0 (xs0_out) that the solve leaves untouched.
+cudaError_t launch_gather_state_cb(uint32_t n, const uint32_t* perm, const float4* pos_in, const float4* xs_in,
+                                   const uint32_t* id_in, const uint32_t* key_in, float4* pos_out, float4* xs_out,
+                                   uint32_t* id_out, uint32_t* skey_out, float4* xs0_out, cudaStream_t st);
 cudaError_t launch_scatter_by_id(uint32_t n, const uint32_t* id, const float4* src, float4* dst, cudaStream_t st);
 // dst[id[t]] = src[t].w (a scalar kept in the w lane of a packed float4 array)
 cudaError_t launch_scatter_w_by_id(uint32_t n, const uint32_t* id, const float4* src, float* dst, cudaStream_t st);

@@ -111,6 +111,21 @@ struct SolverAux {
   const int* need;           // delta-p pass: *need == 0 skips the iteration (x* copied through from xs_in)
 };
 
+// Inputs of the cell-block neighbour passes (pbf_cellblock.cuh): the grid and
+// its cell offsets, the search-time cell key and position of every slot, and
+// the membership masks of the mask variant.
+struct CbArgs {
+  GridParams g;
+  const uint32_t* cell_start;  // [cells + 1]
+  const uint32_t* skey;        // [n] cell key of each slot at x*_0
+  const float4* xs0;           // [n] x*_0 of each slot (the search positions)
+  const uint32_t* mask;        // [9][n] window membership masks (mask variant)
+  const uint16_t* ovf;         // [n] bit q: window q has more than 32 candidates (mask variant)
+  uint32_t* err;               // device error word
+  uint32_t cap;                // staged records per field (shared-memory plan)
+  uint32_t n;
+};
+
 // The learned start's fallback: the plain solve of one substep from the saved
 // predicted positions, run as one cooperative kernel when the device flag is
 // set (a no-op launch otherwise).

@@ -111,6 +111,15 @@ __global__ void __launch_bounds__(256) k_predict(SimParams p0, GridParams g0, Sc
   }
 }
 
+// |d|^2 with the reference's rounding (x*x + y*y, then + z*z, each product
+// and sum rounded once; no contraction in either compile mode) and the
+// neighbour test |d|^2 <= h^2 on it: every neighbour search of the library
+// and the CPU restatement then agree on the neighbour sets bit for bit.
+__device__ __forceinline__ float dist2_rn(f3 d) {
+  return __fadd_rn(__fadd_rn(__fmul_rn(d.x, d.x), __fmul_rn(d.y, d.y)), __fmul_rn(d.z, d.z));
+}
+__device__ __forceinline__ bool within_h(const SimParams& p, f3 d) { return dist2_rn(d) <= p.h2; }
+
 // Range of slots covering cells (cx+dx, cy+dy, cz-Z .. cz+Z), Z = g.reach_z:
 // the neighbourhood is (2 g.reach + 1)^2 runs of consecutive keys because
 // keys are z-fastest (reach 1, Z = 1: the reference's 27 cells as 9 runs).
@@ -144,7 +153,7 @@ __global__ void __launch_bounds__(256) k_nbr_count(SimParams p, GridParams g, co
         Run r = run_of(g, cell_start, cx, cy, cz, dx, dy);
         for (uint32_t u = r.b; u < r.e; ++u) {
           f3 d = xyz(__ldg(xs + u)) - xi;
-          if (dot3(d, d) <= p.h2) ++cnt;
+          if (within_h(p, d)) ++cnt;
         }
       }
   }
@@ -190,7 +199,7 @@ __global__ void __launch_bounds__(256) k_nbr_build(SimParams p, GridParams g0, S
           Run r = run_of(g, cell_start, cx, cy, cz, dx, dy);
           for (uint32_t u = r.b; u < r.e; ++u) {
             f3 d = xyz(__ldg(xs + u)) - xi;
-            if (dot3(d, d) <= p.h2) {
+            if (within_h(p, d)) {
               if (q < max_nbr) out[32u * q] = u;
               ++q;
             }
@@ -236,7 +245,7 @@ __global__ void __launch_bounds__(256) k_nbr_build_feat(SimParams p, GridParams 
           Run r = run_of(g, cell_start, cx, cy, cz, dx, dy);
           for (uint32_t u = r.b; u < r.e; ++u) {
             f3 d = xyz(__ldg(xs + u)) - xi;
-            const float r2 = dot3(d, d);
+            const float r2 = dist2_rn(d);
             if (r2 <= p.h2) {
               if (q < max_nbr) out[32u * q] = u;
               ++q;
@@ -318,11 +327,11 @@ __global__ void __launch_bounds__(256) k_nbr_build2(SimParams p, GridParams g0, 
             for (uint32_t u = r.b; u < r.e; ++u) {
               const f3 xj = xyz(__ldg(xs + u));
               const f3 da = xj - xa, db = xj - xb;
-              if (dot3(da, da) <= p.h2) {
+              if (within_h(p, da)) {
                 if (qa < max_nbr) outa[32u * qa] = u;
                 ++qa;
               }
-              if (dot3(db, db) <= p.h2) {
+              if (within_h(p, db)) {
                 if (qb < max_nbr) outb[32u * qb] = u;
                 ++qb;
               }
@@ -334,7 +343,7 @@ __global__ void __launch_bounds__(256) k_nbr_build2(SimParams p, GridParams g0, 
             Run r = run_of(ga, cell_start, ax, ay, az, dx, dy);
             for (uint32_t u = r.b; u < r.e; ++u) {
               const f3 d = xyz(__ldg(xs + u)) - xa;
-              if (dot3(d, d) <= p.h2) {
+              if (within_h(p, d)) {
                 if (qa < max_nbr) outa[32u * qa] = u;
                 ++qa;
               }
@@ -346,7 +355,7 @@ __global__ void __launch_bounds__(256) k_nbr_build2(SimParams p, GridParams g0, 
               Run r = run_of(gb, cell_start, bx, by, bz, dx, dy);
               for (uint32_t u = r.b; u < r.e; ++u) {
                 const f3 d = xyz(__ldg(xs + u)) - xb;
-                if (dot3(d, d) <= p.h2) {
+                if (within_h(p, d)) {
                   if (qb < max_nbr) outb[32u * qb] = u;
                   ++qb;
                 }
@@ -434,7 +443,7 @@ __global__ void __launch_bounds__(256) k_nbr_build_warp(SimParams p, GridParams 
               const f3 xp = mk(__shfl_sync(kFull, xi.x, pl), __shfl_sync(kFull, xi.y, pl),
                                __shfl_sync(kFull, xi.z, pl));
               const f3 d = c - xp;
-              const unsigned hits = __ballot_sync(kFull, in && dot3(d, d) <= p.h2);
+              const unsigned hits = __ballot_sync(kFull, in && within_h(p, d));
               if ((int)lane == pl) mine = hits;
             }
             while (mine) {
@@ -475,7 +484,7 @@ __global__ void __launch_bounds__(256) k_nbr_list(SimParams p, GridParams g, con
       Run r = run_of(g, cell_start, cx, cy, cz, dx, dy);
       for (uint32_t u = r.b; u < r.e; ++u) {
         f3 d = xyz(__ldg(xs + u)) - xi;
-        if (dot3(d, d) <= p.h2) {
+        if (within_h(p, d)) {
           if (o < capacity) nbr_list[o] = u;
           ++o;
         }
@@ -721,6 +730,146 @@ __device__ __forceinline__ void compression_flush(SolveStats* stats, unsigned cm
   }
 }
 
+// ---- per-neighbour sums of the passes --------------------------------------------
+// One struct per pass holds the slot's own values and running sums; add()
+// takes one neighbour's records.  The list walks and the cell-block walks
+// (pbf_cellblock.cuh) call the same add(), so both evaluate the same
+// arithmetic in the same (reference) order.
+
+// LambdaCalculation's sums (pressureConstrain.ts:49-61): grad, sum |grad|^2, sum W.
+struct LamSum {
+  f3 xi, grad;
+  float sum2, dens;
+  __device__ __forceinline__ void init(f3 x) {
+    xi = x;
+    grad = mk(0.f, 0.f, 0.f);
+    sum2 = 0.0f;
+    dens = 0.0f;
+  }
+  __device__ __forceinline__ void add(const SimParams& p, float4 xj) {
+    Pair q = make_pair_of(xi - xyz(xj));
+    f3 gk = spiky_p(p, q);
+    grad = grad + gk;
+    sum2 = sum2 + dot3(gk, gk);
+    dens = dens + poly6_p(p, q);
+  }
+};
+// ConstrainSolve's sum (pressureConstrain.ts:127-141) over packed (x*_j, lambda_j).
+struct DpSum {
+  f3 xi, pu;
+  float li;
+  __device__ __forceinline__ void init(float4 xli) {
+    xi = xyz(xli);
+    li = xli.w;
+    pu = mk(0.f, 0.f, 0.f);
+  }
+  __device__ __forceinline__ void add(const SimParams& p, float4 xj) {
+    Pair q = make_pair_of(xi - xyz(xj));
+    pu = pu + (li + xj.w) * spiky_p(p, q);
+  }
+};
+// AttributeUpdate's density sum (attributeUpdate.ts:40-49).
+struct DensSum {
+  f3 xi;
+  float dens;
+  __device__ __forceinline__ void init(f3 x) {
+    xi = x;
+    dens = 0.0f;
+  }
+  __device__ __forceinline__ void add(const SimParams& p, float4 xj) {
+    Pair q = make_pair_of(xi - xyz(xj));
+    dens = dens + poly6_p(p, q);
+  }
+};
+// VorticityConfinement's sums (vorticityConfinement.ts:46-61): omega and the Akinci normal.
+struct VortSum {
+  f3 xi, vi, om, nm;
+  __device__ __forceinline__ void init(f3 x, f3 v) {
+    xi = x;
+    vi = v;
+    om = mk(0.f, 0.f, 0.f);
+    nm = mk(0.f, 0.f, 0.f);
+  }
+  __device__ __forceinline__ void add(const SimParams& p, float4 pj, float4 vj) {
+    Pair q = make_pair_of(xi - xyz(pj));
+    f3 vd = xyz(vj) - vi;
+    float volume = fdiv(p.m, pj.w);
+    f3 gw = spiky_p(p, q);
+    om = om + volume * cross3(vd, gw);
+    nm = nm + volume * gw;
+  }
+};
+// XSPH + vorticity force + Akinci tension sums (XSPH.ts:57-81), single pass.
+struct XsphSum {
+  f3 xi, vi, ni, vu, eta, ten;
+  float ri;
+  __device__ __forceinline__ void init(float4 pi, f3 v, f3 n) {
+    xi = xyz(pi);
+    ri = pi.w;
+    vi = v;
+    ni = n;
+    vu = mk(0.f, 0.f, 0.f);
+    eta = mk(0.f, 0.f, 0.f);
+    ten = mk(0.f, 0.f, 0.f);
+  }
+  __device__ __forceinline__ void add(const SimParams& p, float4 pj, float4 vj, float4 nj) {
+    float rj = pj.w;
+    Pair q = make_pair_of(xi - xyz(pj));
+    f3 vd = xyz(vj) - vi;
+    float kij = fdiv(p.two_rho0, ri + rj);
+    vu = vu + fdiv3(poly6_p(p, q) * vd, rj);
+    eta = eta + fdiv3(nj.w * spiky_p(p, q), rj);  // nj: (normal_j, |omega_j|)
+    f3 coh = p.m * cohesion_p(p, q);
+    f3 curv = ni - xyz(nj);
+    ten = ten - kij * (coh + curv);
+  }
+};
+// Fast mode's split: the vorticity pass also sums XSPH's viscosity term and
+// the cohesion part of the tension (see k_vorticity_split).
+struct VortSplitSum {
+  f3 xi, vi, om, nm, vu, cs;
+  float ri;
+  __device__ __forceinline__ void init(float4 pi, f3 v) {
+    xi = xyz(pi);
+    ri = pi.w;
+    vi = v;
+    om = mk(0.f, 0.f, 0.f);
+    nm = mk(0.f, 0.f, 0.f);
+    vu = mk(0.f, 0.f, 0.f);
+    cs = mk(0.f, 0.f, 0.f);
+  }
+  __device__ __forceinline__ void add(const SimParams& p, float4 pj, float4 vj) {
+    Pair q = make_pair_of(xi - xyz(pj));
+    f3 vd = xyz(vj) - vi;
+    const float inv_rj = frcp_fast(pj.w);
+    const float volume = p.m * inv_rj;
+    f3 gw = spiky_p(p, q);
+    om = om + volume * cross3(vd, gw);
+    nm = nm + volume * gw;
+    vu = vu + (poly6_p(p, q) * inv_rj) * vd;
+    const float kij = p.two_rho0 * frcp_fast(ri + pj.w);
+    cs = cs + kij * (p.m * cohesion_p(p, q));
+  }
+};
+// ... and the XSPH pass the vorticity-force eta and the curvature part.
+struct XsphSplitSum {
+  f3 xi, ni, eta, cv;
+  float ri;
+  __device__ __forceinline__ void init(float4 pi, f3 n) {
+    xi = xyz(pi);
+    ri = pi.w;
+    ni = n;
+    eta = mk(0.f, 0.f, 0.f);
+    cv = mk(0.f, 0.f, 0.f);
+  }
+  __device__ __forceinline__ void add(const SimParams& p, float4 pj, float4 nj) {  // nj: (normal_j, |omega_j|)
+    Pair q = make_pair_of(xi - xyz(pj));
+    eta = eta + (nj.w * frcp_fast(pj.w)) * spiky_p(p, q);
+    const float kij = p.two_rho0 * frcp_fast(ri + pj.w);
+    cv = cv + kij * (ni - xyz(nj));
+  }
+};
+
 // LambdaCalculation (pressureConstrain.ts:31-85).  Writes xl[t] = (x*, lambda):
 // the next pass gathers a neighbour's position and multiplier in one load.
 //   kMode 0: the reference pass.
@@ -730,24 +879,16 @@ __device__ __forceinline__ void compression_flush(SolveStats* stats, unsigned cm
 //            by continuity, boundary SDF/h, boundary volume/V, substep index;
 //            v' = (x* - x)/dt) for trace capture.
 
+// The rest of LambdaCalculation after the neighbour sums: the boundary
+// pseudo-particle, the constraint and the multiplier; writes xl[t] and the
+// optional multiplier sum / features (nbr: the neighbour count); returns sum W.
 template <int kMode, bool kC>
-__device__ __forceinline__ float lambda_slot(const SimParams& p, int have_field, const float4* bdata, const float4* xs,
-                                            uint32_t max_nbr, const uint32_t* __restrict__ nbr_cnt,
-                                            const uint32_t* __restrict__ nbr_list, float4* xl, const SolverAux& a,
-                                            uint32_t t) {
+__device__ __forceinline__ float lambda_finish(const SimParams& p, int have_field, const float4* bdata, float4* xl,
+                                               const SolverAux& a, uint32_t t, const LamSum& acc, uint32_t nbr) {
   constexpr bool kFeat = kMode >= 1;
-  f3 xi = xyz(ldo<kC>(xs + t));
-  uint32_t b, e;
-  list_slice(max_nbr, nbr_cnt, t, b, e);
-  f3 grad = mk(0.f, 0.f, 0.f);
-  float sum2 = 0.0f, dens = 0.0f;
-  for_each_neighbor<kC>(nbr_list, b, e, xs, [&](uint32_t, float4 xj) {
-    Pair q = make_pair_of(xi - xyz(xj));
-    f3 gk = spiky_p(p, q);
-    grad = grad + gk;
-    sum2 = sum2 + dot3(gk, gk);
-    dens = dens + poly6_p(p, q);
-  });
+  const f3 xi = acc.xi;
+  f3 grad = acc.grad;
+  float sum2 = acc.sum2, dens = acc.dens;
   const float vsum = dens;
   dens = dens * p.V;
   const float dens_fluid = dens;
@@ -773,10 +914,23 @@ __device__ __forceinline__ float lambda_slot(const SimParams& p, int have_field,
     const float4 xo = a.pos[t];
     const f3 vi = p.inv_dt * (xi - xyz(xo));
     float sd = a.bsdf ? fminf(a.bsdf[t], 2.0f * p.h) : 2.0f * p.h;
-    a.feat[2 * t] = make_float4(dens - 1.0f, a.lam_prev ? a.lam_prev[t] : 0.0f, (float)e, len3(vi) * p.dt / p.h);
+    a.feat[2 * t] = make_float4(dens - 1.0f, a.lam_prev ? a.lam_prev[t] : 0.0f, (float)nbr, len3(vi) * p.dt / p.h);
     a.feat[2 * t + 1] = make_float4(divergence_feature(p, xo, dens_fluid), sd / p.h, vb / p.V, a.substep_index);
   }
   return vsum;
+}
+
+template <int kMode, bool kC>
+__device__ __forceinline__ float lambda_slot(const SimParams& p, int have_field, const float4* bdata, const float4* xs,
+                                            uint32_t max_nbr, const uint32_t* __restrict__ nbr_cnt,
+                                            const uint32_t* __restrict__ nbr_list, float4* xl, const SolverAux& a,
+                                            uint32_t t) {
+  uint32_t b, e;
+  list_slice(max_nbr, nbr_cnt, t, b, e);
+  LamSum acc;
+  acc.init(xyz(ldo<kC>(xs + t)));
+  for_each_neighbor<kC>(nbr_list, b, e, xs, [&](uint32_t, float4 xj) { acc.add(p, xj); });
+  return lambda_finish<kMode, kC>(p, have_field, bdata, xl, a, t, acc, e);
 }
 
 template <int kMode, bool kBatch, bool kLoop>
@@ -805,21 +959,14 @@ __global__ void __launch_bounds__(256) k_lambda(SimParams p, int have_field, con
 // every scene ends in the same buffer.
 // Position correction of slot t from the packed (x*, lambda) records; xi
 // receives the slot's own x*.
+// The rest of ConstrainSolve after the neighbour sum: the boundary term and
+// the 0.5 factor (pressureConstrain.ts:142-158).
 template <bool kC>
-__device__ __forceinline__ f3 deltap_slot(const SimParams& p, int have_field, const float4* xl, const float4* bdata,
-                                          uint32_t max_nbr, const uint32_t* __restrict__ nbr_cnt,
-                                          const uint32_t* __restrict__ nbr_list, uint32_t t, f3& xi) {
-  const float4 xli = ldo<kC>(xl + t);
-  xi = xyz(xli);
-  float li = xli.w;
-  uint32_t b, e;
-  list_slice(max_nbr, nbr_cnt, t, b, e);
-  f3 pu = mk(0.f, 0.f, 0.f);
-  for_each_neighbor<kC>(nbr_list, b, e, xl, [&](uint32_t, float4 xj) {
-    Pair q = make_pair_of(xi - xyz(xj));
-    pu = pu + (li + xj.w) * spiky_p(p, q);
-  });
-  pu = p.V * pu;
+__device__ __forceinline__ f3 deltap_finish(const SimParams& p, int have_field, const float4* bdata, uint32_t t,
+                                            const DpSum& acc) {
+  const f3 xi = acc.xi;
+  const float li = acc.li;
+  f3 pu = p.V * acc.pu;
   if (have_field) {
     float4 bd = ldo<kC>(bdata + t);
     if (bd.w != 0.0f) {
@@ -828,6 +975,19 @@ __device__ __forceinline__ f3 deltap_slot(const SimParams& p, int have_field, co
     }
   }
   return 0.5f * pu;
+}
+
+template <bool kC>
+__device__ __forceinline__ f3 deltap_slot(const SimParams& p, int have_field, const float4* xl, const float4* bdata,
+                                          uint32_t max_nbr, const uint32_t* __restrict__ nbr_cnt,
+                                          const uint32_t* __restrict__ nbr_list, uint32_t t, f3& xi) {
+  uint32_t b, e;
+  list_slice(max_nbr, nbr_cnt, t, b, e);
+  DpSum acc;
+  acc.init(ldo<kC>(xl + t));
+  for_each_neighbor<kC>(nbr_list, b, e, xl, [&](uint32_t, float4 xj) { acc.add(p, xj); });
+  xi = acc.xi;
+  return deltap_finish<kC>(p, have_field, bdata, t, acc);
 }
 
 template <bool kBatch, bool kLoop>
@@ -859,26 +1019,31 @@ __global__ void __launch_bounds__(256) k_deltap(SimParams p, SolverAux a, int ha
   }
 }
 
+// The rest of AttributeUpdate: rho = m sum W, v = (x* - x) / dt, x <- (x*, rho).
+template <bool kC>
+__device__ __forceinline__ float density_finish(const SimParams& p, float4* pos, float4* vel, uint32_t t,
+                                                const DensSum& acc) {
+  const f3 xi = acc.xi;
+  const float vsum = acc.dens;
+  const float dens = acc.dens * p.m;
+  f3 xo = xyz(ldo<kC>(pos + t));
+  vel[t] = f4(p.inv_dt * (xi - xo), 0.0f);
+  pos[t] = f4(xi, dens);
+  return vsum;
+}
+
 // AttributeUpdate of slot t; returns sum W (fluid only).
 template <bool kC>
 __device__ __forceinline__ float density_slot(const SimParams& p, const float4* xs, uint32_t max_nbr,
                                               const uint32_t* __restrict__ nbr_cnt,
                                               const uint32_t* __restrict__ nbr_list, float4* pos, float4* vel,
                                               uint32_t t) {
-  f3 xi = xyz(ldo<kC>(xs + t));
   uint32_t b, e;
   list_slice(max_nbr, nbr_cnt, t, b, e);
-  float dens = 0.0f;
-  for_each_neighbor<kC>(nbr_list, b, e, xs, [&](uint32_t, float4 xj) {
-    Pair q = make_pair_of(xi - xyz(xj));
-    dens = dens + poly6_p(p, q);
-  });
-  const float vsum = dens;
-  dens = dens * p.m;
-  f3 xo = xyz(ldo<kC>(pos + t));
-  vel[t] = f4(p.inv_dt * (xi - xo), 0.0f);
-  pos[t] = f4(xi, dens);
-  return vsum;
+  DensSum acc;
+  acc.init(xyz(ldo<kC>(xs + t)));
+  for_each_neighbor<kC>(nbr_list, b, e, xs, [&](uint32_t, float4 xj) { acc.add(p, xj); });
+  return density_finish<kC>(p, pos, vel, t, acc);
 }
 
 // AttributeUpdate: rho = m * sum W (fluid only), v = (x* - x) / dt, x <- (x*, rho).
@@ -950,6 +1115,41 @@ __global__ void __launch_bounds__(256) k_fallback_solve(FallbackArgs A) {
     density_slot<true>(A.p, fin, A.max_nbr, A.nbr_cnt, A.nbr_list, A.pos, A.vel, t);
 }
 
+// Writes (omega, |omega|) and (h n, |omega|): the normal's w repeats |omega|
+// so XSPH gathers one float4 per neighbour fewer.
+__device__ __forceinline__ void vorticity_finish(const SimParams& p, float4* omega, float4* normal, uint32_t t,
+                                                 const VortSum& acc) {
+  const float wl = len3(acc.om);
+  omega[t] = f4(acc.om, wl);
+  normal[t] = f4(p.h * acc.nm, wl);
+}
+// XSPH's output a from its sums (XSPH.ts:82-89).
+__device__ __forceinline__ void xsph_finish(const SimParams& p, float4* acc_out, uint32_t t, const XsphSum& s,
+                                            f3 wi) {
+  float el = len3(s.eta);
+  f3 en = (el > 0.0f) ? divs(s.eta, el) : mk(0.f, 0.f, 0.f);
+  float sx = p.xsph * p.inv_dt * p.m;
+  f3 av = (sx * s.vu + p.vorticity * cross3(en, wi)) + p.tension * s.ten;
+  acc_out[t] = f4(av, 0.0f);
+}
+__device__ __forceinline__ void vorticity_split_finish(const SimParams& p, float4* omega, float4* normal, float4* visc,
+                                                       float4* coh_sum, uint32_t t, const VortSplitSum& s) {
+  const float wl = len3(s.om);
+  omega[t] = f4(s.om, wl);
+  normal[t] = f4(p.h * s.nm, wl);
+  visc[t] = f4(s.vu, 0.0f);
+  coh_sum[t] = f4(s.cs, 0.0f);
+}
+__device__ __forceinline__ void xsph_split_finish(const SimParams& p, float4* acc_out, uint32_t t,
+                                                  const XsphSplitSum& s, f3 wi, float4 visc_t, float4 coh_t) {
+  const f3 ten = mk(0.f, 0.f, 0.f) - (xyz(coh_t) + s.cv);
+  float el = len3(s.eta);
+  f3 en = (el > 0.0f) ? divs(s.eta, el) : mk(0.f, 0.f, 0.f);
+  float sx = p.xsph * p.inv_dt * p.m;
+  f3 av = (sx * xyz(visc_t) + p.vorticity * cross3(en, wi)) + p.tension * ten;
+  acc_out[t] = f4(av, 0.0f);
+}
+
 // VorticityConfinement: omega_i and the Akinci normal n_i.
 template <bool kLoop>
 __global__ void __launch_bounds__(256) k_vorticity(SimParams p, const float4* __restrict__ pos,
@@ -959,22 +1159,12 @@ __global__ void __launch_bounds__(256) k_vorticity(SimParams p, const float4* __
                                                    const uint32_t* __restrict__ nbr_list,
                                                    float4* __restrict__ omega, float4* __restrict__ normal) {
   PBF_SLOTS(t, p.n) {
-    f3 xi = xyz(pos[t]);
-    f3 vi = xyz(vel[t]);
     uint32_t b, e;
     list_slice(max_nbr, nbr_cnt, t, b, e);
-    f3 om = mk(0.f, 0.f, 0.f), nm = mk(0.f, 0.f, 0.f);
-    for_each_neighbor(nbr_list, b, e, pos, [&](uint32_t j, float4 pj) {
-      Pair q = make_pair_of(xi - xyz(pj));
-      f3 vd = xyz(__ldg(vel + j)) - vi;
-      float volume = fdiv(p.m, pj.w);
-      f3 gw = spiky_p(p, q);
-      om = om + volume * cross3(vd, gw);
-      nm = nm + volume * gw;
-    });
-    const float wl = len3(om);
-    omega[t] = f4(om, wl);
-    normal[t] = f4(p.h * nm, wl);  // w: |omega| again, so XSPH gathers one float4 per neighbour fewer
+    VortSum acc;
+    acc.init(xyz(pos[t]), xyz(vel[t]));
+    for_each_neighbor(nbr_list, b, e, pos, [&](uint32_t j, float4 pj) { acc.add(p, pj, __ldg(vel + j)); });
+    vorticity_finish(p, omega, normal, t, acc);
   }
 }
 
@@ -988,32 +1178,13 @@ __global__ void __launch_bounds__(256, 4) k_xsph(SimParams p, const float4* __re
                                                  const uint32_t* __restrict__ nbr_list,
                                                  float4* __restrict__ acc) {
   PBF_SLOTS(t, p.n) {
-    float4 pi = pos[t];
-    f3 xi = xyz(pi);
-    float ri = pi.w;
-    f3 vi = xyz(vel[t]);
-    f3 wi = xyz(omega[t]);
-    f3 ni = xyz(normal[t]);
     uint32_t b, e;
     list_slice(max_nbr, nbr_cnt, t, b, e);
-    f3 vu = mk(0.f, 0.f, 0.f), eta = mk(0.f, 0.f, 0.f), ten = mk(0.f, 0.f, 0.f);
-    for_each_neighbor(nbr_list, b, e, pos, [&](uint32_t j, float4 pj) {
-      float rj = pj.w;
-      Pair q = make_pair_of(xi - xyz(pj));
-      f3 vd = xyz(__ldg(vel + j)) - vi;
-      float kij = fdiv(p.two_rho0, ri + rj);
-      vu = vu + fdiv3(poly6_p(p, q) * vd, rj);
-      const float4 nj = __ldg(normal + j);  // (normal_j, |omega_j|)
-      eta = eta + fdiv3(nj.w * spiky_p(p, q), rj);
-      f3 coh = p.m * cohesion_p(p, q);
-      f3 curv = ni - xyz(nj);
-      ten = ten - kij * (coh + curv);
-    });
-    float el = len3(eta);
-    f3 en = (el > 0.0f) ? divs(eta, el) : mk(0.f, 0.f, 0.f);
-    float sx = p.xsph * p.inv_dt * p.m;
-    f3 av = (sx * vu + p.vorticity * cross3(en, wi)) + p.tension * ten;
-    acc[t] = f4(av, 0.0f);
+    XsphSum s;
+    s.init(pos[t], xyz(vel[t]), xyz(normal[t]));
+    for_each_neighbor(nbr_list, b, e, pos,
+                      [&](uint32_t j, float4 pj) { s.add(p, pj, __ldg(vel + j), __ldg(normal + j)); });
+    xsph_finish(p, acc, t, s, xyz(omega[t]));
   }
 }
 
@@ -1032,30 +1203,12 @@ __global__ void __launch_bounds__(256, 4) k_vorticity_split(SimParams p, const f
                                                             float4* __restrict__ omega, float4* __restrict__ normal,
                                                             float4* __restrict__ visc, float4* __restrict__ coh_sum) {
   PBF_SLOTS(t, p.n) {
-    const float4 pi = pos[t];
-    f3 xi = xyz(pi);
-    const float ri = pi.w;
-    f3 vi = xyz(vel[t]);
     uint32_t b, e;
     list_slice(max_nbr, nbr_cnt, t, b, e);
-    f3 om = mk(0.f, 0.f, 0.f), nm = mk(0.f, 0.f, 0.f), vu = mk(0.f, 0.f, 0.f), cs = mk(0.f, 0.f, 0.f);
-    for_each_neighbor(nbr_list, b, e, pos, [&](uint32_t j, float4 pj) {
-      Pair q = make_pair_of(xi - xyz(pj));
-      f3 vd = xyz(__ldg(vel + j)) - vi;
-      const float inv_rj = frcp_fast(pj.w);
-      const float volume = p.m * inv_rj;
-      f3 gw = spiky_p(p, q);
-      om = om + volume * cross3(vd, gw);
-      nm = nm + volume * gw;
-      vu = vu + (poly6_p(p, q) * inv_rj) * vd;
-      const float kij = p.two_rho0 * frcp_fast(ri + pj.w);
-      cs = cs + kij * (p.m * cohesion_p(p, q));
-    });
-    const float wl = len3(om);
-    omega[t] = f4(om, wl);
-    normal[t] = f4(p.h * nm, wl);
-    visc[t] = f4(vu, 0.0f);
-    coh_sum[t] = f4(cs, 0.0f);
+    VortSplitSum s;
+    s.init(pos[t], xyz(vel[t]));
+    for_each_neighbor(nbr_list, b, e, pos, [&](uint32_t j, float4 pj) { s.add(p, pj, __ldg(vel + j)); });
+    vorticity_split_finish(p, omega, normal, visc, coh_sum, t, s);
   }
 }
 
@@ -1068,28 +1221,16 @@ __global__ void __launch_bounds__(256) k_xsph_split(SimParams p, const float4* _
                                                     const uint32_t* __restrict__ nbr_cnt,
                                                     const uint32_t* __restrict__ nbr_list, float4* __restrict__ acc) {
   PBF_SLOTS(t, p.n) {
-    const float4 pi = pos[t];
-    f3 xi = xyz(pi);
-    const float ri = pi.w;
-    f3 wi = xyz(omega[t]);
-    f3 ni = xyz(normal[t]);
     uint32_t b, e;
     list_slice(max_nbr, nbr_cnt, t, b, e);
-    f3 eta = mk(0.f, 0.f, 0.f), cv = mk(0.f, 0.f, 0.f);
-    for_each_neighbor2(nbr_list, b, e, pos, normal, [&](uint32_t, float4 pj, float4 nj) {  // nj: (normal_j, |omega_j|)
-      Pair q = make_pair_of(xi - xyz(pj));
-      eta = eta + (nj.w * frcp_fast(pj.w)) * spiky_p(p, q);
-      const float kij = p.two_rho0 * frcp_fast(ri + pj.w);
-      cv = cv + kij * (ni - xyz(nj));
-    });
-    const f3 ten = mk(0.f, 0.f, 0.f) - (xyz(coh_sum[t]) + cv);
-    float el = len3(eta);
-    f3 en = (el > 0.0f) ? divs(eta, el) : mk(0.f, 0.f, 0.f);
-    float sx = p.xsph * p.inv_dt * p.m;
-    f3 av = (sx * xyz(visc[t]) + p.vorticity * cross3(en, wi)) + p.tension * ten;
-    acc[t] = f4(av, 0.0f);
+    XsphSplitSum s;
+    s.init(pos[t], xyz(normal[t]));
+    for_each_neighbor2(nbr_list, b, e, pos, normal, [&](uint32_t, float4 pj, float4 nj) { s.add(p, pj, nj); });
+    xsph_split_finish(p, acc, t, s, xyz(omega[t]), visc[t], coh_sum[t]);
   }
 }
+
+#include "pbf_cellblock.cuh"
 
 // Launch table for this precision variant: [batch][persistent] pass sets.
 template <bool B, bool P>
@@ -1125,6 +1266,10 @@ void fill_pass_table(PassTable* tbl) {
   fill_set<false, true>(&tbl->set[0][1]);
   fill_set<true, false>(&tbl->set[1][0]);
   fill_set<true, true>(&tbl->set[1][1]);
+  tbl->cb_build = k_cb_build<false>;
+  tbl->cb_build_feat = k_cb_build<true>;
+  fill_cb_set<kMemMask>(&tbl->cb[kMemMask]);
+  fill_cb_set<kMemTest>(&tbl->cb[kMemTest]);
 }
 
 }  // namespace PBF_NS

@@ -513,6 +513,24 @@ __global__ void __launch_bounds__(256) k_gather(uint32_t n, const uint32_t* __re
   id_out[t] = id_in ? __ldg(id_in + o) : o;  // no id array: the input order is the id order
 }
 
+__global__ void __launch_bounds__(256) k_gather_cb(uint32_t n, const uint32_t* __restrict__ perm,
+                                                   const float4* __restrict__ pos_in,
+                                                   const float4* __restrict__ xs_in,
+                                                   const uint32_t* __restrict__ id_in,
+                                                   const uint32_t* __restrict__ key_in, float4* __restrict__ pos_out,
+                                                   float4* __restrict__ xs_out, uint32_t* __restrict__ id_out,
+                                                   uint32_t* __restrict__ skey_out, float4* __restrict__ xs0_out) {
+  uint32_t t = blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= n) return;
+  uint32_t o = perm[t];
+  pos_out[t] = __ldg(pos_in + o);
+  const float4 x = __ldg(xs_in + o);
+  xs_out[t] = x;
+  xs0_out[t] = x;
+  skey_out[t] = __ldg(key_in + o);
+  id_out[t] = id_in ? __ldg(id_in + o) : o;
+}
+
 __global__ void k_scatter_f4(uint32_t n, const uint32_t* __restrict__ id, const float4* __restrict__ src,
                              float4* __restrict__ dst) {
   uint32_t t = blockIdx.x * blockDim.x + threadIdx.x;
@@ -771,6 +789,15 @@ cudaError_t launch_gather_state(uint32_t n, const uint32_t* perm, const float4* 
                                 cudaStream_t st) {
   if (n == 0) return cudaSuccess;
   k_gather<<<blocks_for(n, 256), 256, 0, st>>>(n, perm, pos_in, xs_in, id_in, pos_out, xs_out, id_out);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_gather_state_cb(uint32_t n, const uint32_t* perm, const float4* pos_in, const float4* xs_in,
+                                   const uint32_t* id_in, const uint32_t* key_in, float4* pos_out, float4* xs_out,
+                                   uint32_t* id_out, uint32_t* skey_out, float4* xs0_out, cudaStream_t st) {
+  if (n == 0) return cudaSuccess;
+  k_gather_cb<<<blocks_for(n, 256), 256, 0, st>>>(n, perm, pos_in, xs_in, id_in, key_in, pos_out, xs_out, id_out,
+                                                  skey_out, xs0_out);
   return cudaGetLastError();
 }
 

@@ -79,7 +79,8 @@ class Grid(ctypes.Structure):
 class Launch(ctypes.Structure):
     _fields_ = [("block", u32), ("ctas_per_sm", u32), ("cell_ratio", f32), ("build", u32)]
 
-BUILD_THREAD, BUILD_PAIR, BUILD_WARP = 0, 1, 2
+BUILD_THREAD, BUILD_PAIR, BUILD_WARP, BUILD_CELLBLOCK_MASK, BUILD_CELLBLOCK_FREE = 0, 1, 2, 3, 4
+DEVERR_STAGE_TIMEOUT = 0x10
 
 
 class TuneTrial(ctypes.Structure):
@@ -211,6 +212,7 @@ SIGNATURES = {
     "pbf_set_lagged_iterations": (ctypes.c_int, [_P, ctypes.c_float]),
     "pbf_adaptive_counts": (ctypes.c_int, [_P, _UP, _UP]),
     "pbf_set_launch": (ctypes.c_int, [_P, ctypes.POINTER(Launch)]),
+    "pbf_set_cellblock_capacity": (ctypes.c_int, [_P, u32]),
     "pbf_get_launch": (ctypes.c_int, [_P, ctypes.POINTER(Launch)]),
     "pbf_autotune": (ctypes.c_int, [_P, u32, u32, ctypes.POINTER(TuneTrial), u32, _UP, ctypes.POINTER(Launch)]),
     "pbf_batch_create": (ctypes.c_int, [ctypes.POINTER(Config), ctypes.POINTER(Scene), u32, ctypes.POINTER(_P)]),

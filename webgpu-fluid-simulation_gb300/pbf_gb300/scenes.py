@@ -316,9 +316,10 @@ def sphere_drop_spec(nx=128, ny=64, nz=128, field_res=(128, 128, 128), seed=1):
     cfg = base_config(particle_radius=r, kernel_radius=4 * r, time_step=np.float32(1.0 / 300.0), substeps=2,
                       domain_min=(0.0, 0.0, 0.0), domain_max=box, max_particles=nx * ny * nz,
                       options=dict(iterations=4, xsph=0.01, vorticity=5e-4, surface_tension=0.1, gravity=9.8))
-    # per-particle list slice with headroom for the impact; the passes only
-    # touch the entries up to each warp's largest neighbour count
-    cfg.max_neighbors = 96
+    # per-particle list slice with headroom for the impact (a few particles
+    # reach ~100 neighbours in long runs of the learned start); the passes
+    # only touch the entries up to each warp's largest neighbour count
+    cfg.max_neighbors = 128
     sphere_c = (box[0] / 2, 0.4, box[2] / 2)
     d = 2 * r
     x0 = (box[0] - nx * d) / 2 + r

@@ -375,6 +375,10 @@ class PBF:
         lc = L.Launch(int(block), int(ctas_per_sm), float(cell_ratio), int(build))
         self._check(self._lib.pbf_set_launch(self._h, ctypes.byref(lc)), "set_launch")
 
+    def set_cellblock_capacity(self, records):
+        """Records per staged field of the cell-block passes' shared-memory plan."""
+        self._check(self._lib.pbf_set_cellblock_capacity(self._h, int(records)), "set_cellblock_capacity")
+
     def launch(self):
         lc = L.Launch()
         self._check(self._lib.pbf_get_launch(self._h, ctypes.byref(lc)), "get_launch")
@@ -384,16 +388,16 @@ class PBF:
     def autotune(self, substeps=4, cell_ratio=False):
         """Times every candidate launch shape on the current state (restored
         afterwards) and keeps the fastest; returns (best, trials)."""
-        trials = (L.TuneTrial * 32)()
+        trials = (L.TuneTrial * 64)()
         cnt = ctypes.c_uint32()
         best = L.Launch()
         flags = L.TUNE_CELL_RATIO if cell_ratio else 0
-        self._check(self._lib.pbf_autotune(self._h, int(substeps), flags, trials, 32, ctypes.byref(cnt),
+        self._check(self._lib.pbf_autotune(self._h, int(substeps), flags, trials, 64, ctypes.byref(cnt),
                                            ctypes.byref(best)), "autotune")
         as_dict = lambda lc: {"block": lc.block, "ctas_per_sm": lc.ctas_per_sm, "cell_ratio": lc.cell_ratio,
                               "build": lc.build}
         return as_dict(best), [dict(as_dict(t.launch), ms_per_substep=t.ms_per_substep)
-                               for t in trials[:min(cnt.value, 32)]]
+                               for t in trials[:min(cnt.value, 64)]]
 
     # ---- scenes (a batch handle holds many; a single handle holds one) ---------
     def scene_count(self):

@@ -520,7 +520,7 @@ typedef struct pbf_launch {
 int pbf_set_launch(pbf_handle* h, const pbf_launch* launch);
 /* Shared-memory plan of the cell-block passes (no counterpart in the
  * reference): the records per staged field a CTA holds (a multiple of 16 in
- * [16, 4096]; default 2048).  A tile whose halo needs more (or spans more
+ * [16, 3072]; default 2048).  A tile whose halo needs more (or spans more
  * than 8 cell columns) walks global memory instead, with the same results. */
 int pbf_set_cellblock_capacity(pbf_handle* h, uint32_t records);
 int pbf_get_launch(const pbf_handle* h, pbf_launch* launch);

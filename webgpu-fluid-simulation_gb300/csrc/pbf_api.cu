@@ -514,8 +514,8 @@ int substep(pbf_handle* h, cudaEvent_t* ev) {
       adaptive = false;
     }
     for (uint32_t it = 0; it < iters; ++it) {
-      if (f.loaded && sample_boundary(a, (need_feat && feat_first && it == 0) ? h->bsdf.p : nullptr, lag) !=
-                          cudaSuccess) {
+      float* bsdf_it = (need_feat && feat_first && it == 0) ? h->bsdf.p : nullptr;
+      if (f.loaded && sample_boundary(a, bsdf_it, lag) != cudaSuccess) {
         *rc = PBF_ECUDA;
         return a;
       }
@@ -1958,8 +1958,8 @@ int pbf_set_launch(pbf_handle* h, const pbf_launch* l) {
 
 int pbf_set_cellblock_capacity(pbf_handle* h, uint32_t records) {
   if (!h) return PBF_EINVAL;
-  if (records < 16 || records % 16 || records > 4096)
-    return fail(h, PBF_EINVAL, "cell-block capacity must be a multiple of 16 in [16, 4096]");
+  if (records < 16 || records % 16 || records > 3072)
+    return fail(h, PBF_EINVAL, "cell-block capacity must be a multiple of 16 in [16, 3072]");
   if (records != h->cb_cap) invalidate_graph(h);
   h->cb_cap = records;
   return cb_active(h) ? ensure_cb(h) : PBF_OK;

@@ -208,15 +208,18 @@ __device__ __forceinline__ float4 cb_ldg(const float4* p) {
   return __ldg(p);
 }
 
-// Visits slot me.t's neighbours in the reference order and calls
-// fn(const float4 (&r)[kP]) with the kP pass fields of each (kOff = 1 when
-// field 0 is the staged x*_0 of the membership test).  Returns the neighbour
-// count.
+// The pass fields of one neighbour.
 template <int kP>
 struct CbRec {
   float4 v[kP];
 };
 
+// Visits slot me.t's neighbours in the reference order and calls
+// fn(const CbRec<kP>&) with the kP pass fields of each (field 0 of the
+// staged records is x*_0 when membership is tested).  Returns the neighbour
+// count.  The next window's bounds (and mask) are loaded while the current
+// one is walked; inside a window the neighbours go in batches of four —
+// four record loads in flight, then four add()s — as the list walk does.
 template <bool kStaged, int kMemb, int kP, bool kC, class Fn>
 __device__ __forceinline__ uint32_t cb_walk(const SimParams& p, const CbArgs& A, const CbShared* S, const float4* rec,
                                             const float4* const* src, const CbSlot& me, Fn&& fn) {
@@ -226,51 +229,91 @@ __device__ __forceinline__ uint32_t cb_walk(const SimParams& p, const CbArgs& A,
   if constexpr (kMemb == kMemMask) ovf = __ldg(A.ovf + me.t);
   f3 x0i = mk(0.f, 0.f, 0.f);
   if (kMemb == kMemTest || ovf) x0i = xyz(cb_ldg<kC>(A.xs0 + me.t));
-  uint32_t cnt = 0;
-  int q = 0;
-  for (int dx = -1; dx <= 1; ++dx)
-    for (int dy = -1; dy <= 1; ++dy, ++q) {
-      const Run r = run_of(g, A.cell_start, me.cx, me.cy, me.cz, dx, dy);
-      if (r.b == r.e) continue;
-      int base = 0;  // shared-memory record index of slot j: j + base
-      if constexpr (kStaged) {
-        const int ri = me.seg * 9 + q;
-        base = (int)S->run_off[ri] - (int)S->run_slot0[ri];
-      }
-      auto visit = [&](uint32_t j) {
-        CbRec<kP> r;
+  auto window = [&](int q, Run& r, uint32_t& m) {
+    r = run_of(g, A.cell_start, me.cx, me.cy, me.cz, q / 3 - 1, q % 3 - 1);
+    m = 0u;
+    if constexpr (kMemb == kMemMask) m = (r.b != r.e) ? __ldg(A.mask + (size_t)q * A.n + me.t) : 0u;
+  };
+  auto load = [&](uint32_t j, int base) {
+    CbRec<kP> r;
 #pragma unroll
-        for (int f = 0; f < kP; ++f) {
-          if constexpr (kStaged)
-            r.v[f] = rec[(size_t)(f + kOff) * A.cap + (uint32_t)((int)j + base)];
-          else
-            r.v[f] = cb_ldg<kC>(src[f + kOff] + j);
-        }
-        fn(r);
-        ++cnt;
-      };
-      if constexpr (kMemb == kMemMask) {
-        uint32_t m = __ldg(A.mask + (size_t)q * A.n + me.t);
-        while (m) {
-          const uint32_t bit = (uint32_t)__ffs(m) - 1u;
+    for (int f = 0; f < kP; ++f) {
+      if constexpr (kStaged)
+        r.v[f] = rec[(size_t)(f + kOff) * A.cap + (uint32_t)((int)j + base)];
+      else
+        r.v[f] = cb_ldg<kC>(src[f + kOff] + j);
+    }
+    return r;
+  };
+  auto x0_of = [&](uint32_t j, int base) -> f3 {
+    if constexpr (kStaged && kMemb == kMemTest) return xyz(rec[(uint32_t)((int)j + base)]);
+    return xyz(cb_ldg<kC>(A.xs0 + j));
+  };
+  uint32_t cnt = 0;
+  Run r;
+  uint32_t m;
+  window(0, r, m);
+#pragma unroll 1
+  for (int q = 0; q < 9; ++q) {
+    Run rn{0u, 0u};
+    uint32_t mn = 0u;
+    if (q < 8) window(q + 1, rn, mn);
+    int base = 0;  // shared-memory record index of slot j: j + base
+    if constexpr (kStaged) {
+      const int ri = me.seg * 9 + q;
+      base = (int)S->run_off[ri] - (int)S->run_slot0[ri];
+    }
+    if constexpr (kMemb == kMemMask) {
+      while (m) {
+        uint32_t j[4];
+        bool v[4];
+#pragma unroll
+        for (int k = 0; k < 4; ++k) {
+          v[k] = m != 0u;
+          j[k] = r.b + (v[k] ? (uint32_t)__ffs(m) - 1u : 0u);
           m &= m - 1u;
-          visit(r.b + bit);
         }
-        if ((ovf >> q) & 1u) {
-          for (uint32_t j = r.b + 32u; j < r.e; ++j)
-            if (within_h(p, xyz(cb_ldg<kC>(A.xs0 + j)) - x0i)) visit(j);
+        CbRec<kP> rr[4];
+#pragma unroll
+        for (int k = 0; k < 4; ++k)
+          if (v[k]) rr[k] = load(j[k], base);
+#pragma unroll
+        for (int k = 0; k < 4; ++k)
+          if (v[k]) {
+            fn(rr[k]);
+            ++cnt;
+          }
+      }
+      if ((ovf >> q) & 1u) {  // candidates past the mask: tested at x*_0
+        for (uint32_t j = r.b + 32u; j < r.e; ++j)
+          if (within_h(p, xyz(cb_ldg<kC>(A.xs0 + j)) - x0i)) {
+            fn(load(j, base));
+            ++cnt;
+          }
+      }
+    } else {
+      for (uint32_t j0 = r.b; j0 < r.e; j0 += 4u) {
+        bool v[4];
+#pragma unroll
+        for (int k = 0; k < 4; ++k) {
+          const uint32_t j = j0 + (uint32_t)k;
+          v[k] = j < r.e && within_h(p, x0_of(j < r.e ? j : j0, base) - x0i);
         }
-      } else {
-        for (uint32_t j = r.b; j < r.e; ++j) {
-          float4 x0j;
-          if constexpr (kStaged)
-            x0j = rec[(uint32_t)((int)j + base)];
-          else
-            x0j = cb_ldg<kC>(A.xs0 + j);
-          if (within_h(p, xyz(x0j) - x0i)) visit(j);
-        }
+        CbRec<kP> rr[4];
+#pragma unroll
+        for (int k = 0; k < 4; ++k)
+          if (v[k]) rr[k] = load(j0 + (uint32_t)k, base);
+#pragma unroll
+        for (int k = 0; k < 4; ++k)
+          if (v[k]) {
+            fn(rr[k]);
+            ++cnt;
+          }
       }
     }
+    r = rn;
+    m = mn;
+  }
   return cnt;
 }
 
@@ -369,7 +412,7 @@ __global__ void __launch_bounds__(cbk::kT) k_cb_build(SimParams p, CbArgs A, uin
 }
 
 template <int kMemb, int kMode>
-__global__ void __launch_bounds__(cbk::kT) k_cb_lambda(SimParams p, CbArgs A, int have_field,
+__global__ void __launch_bounds__(cbk::kT, 8) k_cb_lambda(SimParams p, CbArgs A, int have_field,
                                                        const float4* __restrict__ bdata,
                                                        const float4* __restrict__ xs, float4* __restrict__ xl,
                                                        SolverAux a) {
@@ -392,7 +435,7 @@ __global__ void __launch_bounds__(cbk::kT) k_cb_lambda(SimParams p, CbArgs A, in
 }
 
 template <int kMemb>
-__global__ void __launch_bounds__(cbk::kT) k_cb_deltap(SimParams p, CbArgs A, SolverAux a, int have_field,
+__global__ void __launch_bounds__(cbk::kT, 8) k_cb_deltap(SimParams p, CbArgs A, SolverAux a, int have_field,
                                                        const float4* __restrict__ xl,
                                                        const float4* __restrict__ bdata, float4* __restrict__ xs_out,
                                                        float4* __restrict__ dp_out) {
@@ -418,7 +461,7 @@ __global__ void __launch_bounds__(cbk::kT) k_cb_deltap(SimParams p, CbArgs A, So
 }
 
 template <int kMemb>
-__global__ void __launch_bounds__(cbk::kT) k_cb_density(SimParams p, CbArgs A, SolverAux a,
+__global__ void __launch_bounds__(cbk::kT, 8) k_cb_density(SimParams p, CbArgs A, SolverAux a,
                                                         const float4* __restrict__ xs, float4* __restrict__ pos,
                                                         float4* __restrict__ vel, uint32_t* __restrict__ nbr_count) {
   __shared__ CbShared S;
@@ -440,7 +483,7 @@ __global__ void __launch_bounds__(cbk::kT) k_cb_density(SimParams p, CbArgs A, S
 }
 
 template <int kMemb>
-__global__ void __launch_bounds__(cbk::kT) k_cb_vorticity(SimParams p, CbArgs A, const float4* __restrict__ pos,
+__global__ void __launch_bounds__(cbk::kT, 6) k_cb_vorticity(SimParams p, CbArgs A, const float4* __restrict__ pos,
                                                           const float4* __restrict__ vel, float4* __restrict__ omega,
                                                           float4* __restrict__ normal) {
   __shared__ CbShared S;
@@ -455,7 +498,7 @@ __global__ void __launch_bounds__(cbk::kT) k_cb_vorticity(SimParams p, CbArgs A,
 }
 
 template <int kMemb>
-__global__ void __launch_bounds__(cbk::kT) k_cb_xsph(SimParams p, CbArgs A, const float4* __restrict__ pos,
+__global__ void __launch_bounds__(cbk::kT, 6) k_cb_xsph(SimParams p, CbArgs A, const float4* __restrict__ pos,
                                                      const float4* __restrict__ vel,
                                                      const float4* __restrict__ omega,
                                                      const float4* __restrict__ normal, float4* __restrict__ acc_out) {
@@ -472,7 +515,7 @@ __global__ void __launch_bounds__(cbk::kT) k_cb_xsph(SimParams p, CbArgs A, cons
 }
 
 template <int kMemb>
-__global__ void __launch_bounds__(cbk::kT) k_cb_vorticity_split(SimParams p, CbArgs A,
+__global__ void __launch_bounds__(cbk::kT, 6) k_cb_vorticity_split(SimParams p, CbArgs A,
                                                                 const float4* __restrict__ pos,
                                                                 const float4* __restrict__ vel,
                                                                 float4* __restrict__ omega,
@@ -491,7 +534,7 @@ __global__ void __launch_bounds__(cbk::kT) k_cb_vorticity_split(SimParams p, CbA
 }
 
 template <int kMemb>
-__global__ void __launch_bounds__(cbk::kT) k_cb_xsph_split(SimParams p, CbArgs A, const float4* __restrict__ pos,
+__global__ void __launch_bounds__(cbk::kT, 6) k_cb_xsph_split(SimParams p, CbArgs A, const float4* __restrict__ pos,
                                                            const float4* __restrict__ omega,
                                                            const float4* __restrict__ normal,
                                                            const float4* __restrict__ visc,

@@ -337,9 +337,10 @@ __device__ __forceinline__ float boundary_distance(const FieldParams& f, const f
 }
 
 // BoundaryVolume pass for one particle (src/simulator/PBF/shader/boundaryVolume.ts:31-55):
-// returns (x_b, V_b) or zero when the particle is outside the band 0 < d < h.
+// returns (x_b, V_b) or zero when the particle is outside the band 0 < d < h;
+// dist_out (optional) receives the interpolated SDF (boundary_distance's value).
 __device__ __forceinline__ float4 boundary_sample(const SimParams& p, const FieldParams& f, const float* __restrict__ sdf,
-                                                  const float* __restrict__ vol, f3 x) {
+                                                  const float* __restrict__ vol, f3 x, float* dist_out = nullptr) {
   CellLoc L = field_locate(f, x);
   uint32_t idx[32];
   cell_nodes(f, L.i, L.j, L.k, false, idx);
@@ -359,6 +360,7 @@ __device__ __forceinline__ float4 boundary_sample(const SimParams& p, const Fiel
       g = g + mk(sx * wy * wz * v, wx * sy * wz * v, wx * wy * sz * v);
     }
     grad = mk(0.5f * f.gscale[0] * g.x, 0.5f * f.gscale[1] * g.y, 0.5f * f.gscale[2] * g.z);
+    if (dist_out) *dist_out = dist;
     float4 out = make_float4(0.f, 0.f, 0.f, 0.f);
     if (dist > 0.0f && dist < p.h && len3(grad) > 1e-9f) {
       volume = 0.0f;
@@ -385,6 +387,7 @@ __device__ __forceinline__ float4 boundary_sample(const SimParams& p, const Fiel
   dist = sum32(N, val);
   f3 g = sum32v(dN, val);
   grad = mk(f.gscale[0] * g.x, f.gscale[1] * g.y, f.gscale[2] * g.z);
+  if (dist_out) *dist_out = dist;
   float4 out = make_float4(0.f, 0.f, 0.f, 0.f);
   if (dist > 0.0f && dist < p.h && len3(grad) > 1e-9f) {
     if (f.quirk) cell_nodes(f, L.i, L.j, L.k, true, idx);

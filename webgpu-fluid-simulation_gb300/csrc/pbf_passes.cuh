@@ -628,12 +628,7 @@ __device__ __forceinline__ void boundary_slot(const SimParams& p, const FieldPar
     const float* sdf = sdf0 + f.node_off;
     const float* vol = vol0 + f.node_off;
     const uint8_t* bflag = bflag0 ? bflag0 + f.flag_off : nullptr;
-    if (boundary_possible(f, bflag, xi)) {
-      if (bsdf) {
-        dist = boundary_distance(f, sdf, xi);
-      }
-      bd = boundary_sample(p, f, sdf, vol, xi);
-    }
+    if (boundary_possible(f, bflag, xi)) bd = boundary_sample(p, f, sdf, vol, xi, bsdf ? &dist : nullptr);
   }
   bdata[t] = bd;
   if (bsdf) bsdf[t] = dist;
@@ -690,8 +685,9 @@ __global__ void __launch_bounds__(256, 2) k_boundary_band(SimParams p, FieldPara
     const float* sdf = sdf0 + f.node_off;
     const float* vol = vol0 + f.node_off;
     const f3 xi = xyz(xs[t]);
-    if (bsdf) bsdf[t] = boundary_distance(f, sdf, xi);
-    bdata[t] = boundary_sample(p, f, sdf, vol, xi);
+    float dist;
+    bdata[t] = boundary_sample(p, f, sdf, vol, xi, &dist);
+    if (bsdf) bsdf[t] = dist;
   }
 }
 

@@ -98,6 +98,13 @@ def parse_args():
     ap.add_argument("--no-learned", action="store_true", help="skip the learned warm-start measurement")
     ap.add_argument("--no-tune", action="store_true",
                     help="keep the default launch shape instead of the autotuner's choice")
+    ap.add_argument("--neighbors", default=None, choices=["lists", "cellblock-mask", "cellblock-free"],
+                    help="force the neighbour representation (default: the autotuner's choice; lists, or the "
+                         "cell-block passes with per-window masks or list-free)")
+    ap.add_argument("--profile-substeps", type=int, default=0,
+                    help="profiling run: build the input state (--settle frames), run this many eager substeps "
+                         "with the launch shape of --neighbors (128-thread CTAs, cell height h/2), print one line "
+                         "and exit (for ncu captures of single launches)")
     ap.add_argument("--bound", type=float, default=None,
                     help="learned start: fall back to the plain solve when the in-solve mean compression exceeds "
                          "this (default: the largest per-substep value the plain 4-iteration solve showed while "
@@ -380,6 +387,22 @@ def gpu_arm(args, dist):
     # the device
     sim.step(args.settle)
     sim.synchronize()
+    if args.profile_substeps > 0:
+        snap = (sim.positions(), sim.velocities(), sim.copy_field(L.FIELD_ACCELERATION))
+        sim.close()
+        h = PBF(cfg)
+        h.set_state(*snap)
+        h.set_boundary_field(f["res"], f["origin"], f["extent"], f["sdf"], f["vol"])
+        h.set_launch(block=128, ctas_per_sm=0, cell_ratio=0.5, build=NEIGHBOR_BUILDS[args.neighbors or "lists"])
+        for _ in range(args.profile_substeps):
+            h.run()
+        h.synchronize()
+        m = h.metrics()
+        h.close()
+        if dist.rank == 0:
+            print(json.dumps({"profile_substeps": args.profile_substeps, "neighbors": args.neighbors or "lists",
+                              "settle": args.settle, "error_flags": m["error_flags"], "nonfinite": m["nonfinite"]}))
+        return
     model = None
     train_info = None
     trace_lo, trace_hi = (2 * args.settle) // 3, args.settle + max(args.warmup, 3) + args.steps
@@ -416,6 +439,9 @@ def gpu_arm(args, dist):
         best, trials = sim.autotune(substeps=4, cell_ratio=True)
         _LAUNCH = best
         tune = {"launch": best, "trials": trials}
+    if args.neighbors is not None:
+        _LAUNCH = dict(_LAUNCH or {"block": 128, "ctas_per_sm": 0, "cell_ratio": 0.5}, ctas_per_sm=0,
+                       build=NEIGHBOR_BUILDS[args.neighbors])
     snap = (sim.positions(), sim.velocities(), sim.copy_field(L.FIELD_ACCELERATION))
     sim.close()
     # every measured path starts from the same snapshot (fresh handles)
@@ -503,6 +529,7 @@ def gpu_arm(args, dist):
 
 
 _LAUNCH = None  # the autotuner's launch shape, applied to every handle of the run
+NEIGHBOR_BUILDS = {"lists": 0, "cellblock-mask": 3, "cellblock-free": 4}  # pbf_launch.build
 
 # The headline path, declared before anything is timed: the learned start
 # with one plain iteration after its projection (device-side fallback to the

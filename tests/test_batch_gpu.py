@@ -144,7 +144,9 @@ def test_autotune_restores_state_and_keeps_results():
         s.step(2)
     before = b.positions().copy(), b.velocities().copy()
     best, trials = b.autotune(substeps=2)
-    assert len(trials) == 12 and best["block"] in (128, 256) and best["cell_ratio"] == 1.0
+    # 12 list-build shapes and 4 cell-block ones (a single scene)
+    assert len(trials) == 16 and best["block"] in (128, 256) and best["cell_ratio"] == 1.0
+    assert sorted(t["build"] for t in trials if t["build"] >= L.BUILD_CELLBLOCK_MASK) == [3, 3, 4, 4]
     assert all(t["ms_per_substep"] > 0 for t in trials)
     assert b.launch() == best
     assert np.array_equal(b.positions(), before[0]) and np.array_equal(b.velocities(), before[1])

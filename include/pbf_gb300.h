@@ -398,11 +398,19 @@ typedef struct pbf_mlp {
   float feat_inv_std[8];
   float lam_scale;          /* target scale: the network predicts lambda / lam_scale */
 } pbf_mlp;
+/* Gradient kernels of the training (no counterpart in the reference):
+ * PBF_MLP_TRAIN_TCGEN05 (the default) runs forward and backward on tcgen05.mma
+ * with the accumulators in tensor memory, the weight and bias gradients
+ * accumulated there over each CTA's 128-row tiles; PBF_MLP_TRAIN_MMA_SYNC is
+ * the warp-level mma.sync.m16n8k16 kernel.  Both use the same bf16 rounding
+ * points. */
+#define PBF_MLP_TRAIN_TCGEN05 0u
+#define PBF_MLP_TRAIN_MMA_SYNC 1u
 typedef struct pbf_train_config {
   uint32_t epochs;
   uint32_t batch;
   float learning_rate;      /* Adam, cosine-decayed over the epochs */
-  uint32_t reserved;
+  uint32_t kernel;          /* PBF_MLP_TRAIN_*: the gradient kernel (0: tcgen05) */
   uint64_t seed;
 } pbf_train_config;
 int pbf_mlp_init(pbf_mlp* m, uint64_t seed);
@@ -419,6 +427,10 @@ int pbf_mlp_forward_ex(const pbf_mlp* model, const float* feat, uint32_t rows, f
 /* Gradient of mean((y - target/lam_scale)^2) w.r.t. params (PBF_MLP_PARAMS floats), one GPU pass. */
 int pbf_mlp_gradient(const pbf_mlp* m, const float* feat, const float* target, uint32_t rows, float* grad,
                      float* loss);
+/* The same with a choice of gradient kernel (PBF_MLP_TRAIN_*); PBF_ETIMEOUT if
+ * a tensor-core completion wait gave up. */
+int pbf_mlp_gradient_ex(const pbf_mlp* m, const float* feat, const float* target, uint32_t rows, float* grad,
+                        float* loss, uint32_t kernel);
 int pbf_mlp_train(pbf_mlp* m, const float* feat, const float* target, uint32_t rows,
                   const pbf_train_config* cfg, float* final_loss);
 /* Trace capture during plain substeps: every `stride`-th particle (hashed

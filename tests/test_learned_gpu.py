@@ -83,9 +83,15 @@ def test_learned_step_tcgen05_network_matches_mma_sync():
     assert np.abs(out[0] - out[1]).max() <= 1e-4 * span
 
 
-def test_mlp_gradient_matches_fp64_reference():
-    m, feat, target = random_model(2, rows=777)
-    g, loss = mlp_gradient(m, feat, target)
+@pytest.mark.parametrize("kernel", [L.MLP_TRAIN_TCGEN05, L.MLP_TRAIN_MMA_SYNC])
+@pytest.mark.parametrize("rows", [777, 20000])
+def test_mlp_gradient_matches_fp64_reference(kernel, rows):
+    """Both gradient kernels (tcgen05 with TMEM accumulators across a CTA's
+    tiles, and mma.sync) against the FP64 reference with the same bf16
+    rounding points; 20,000 rows make each tcgen05 CTA accumulate several
+    128-row tiles."""
+    m, feat, target = random_model(2, rows=rows)
+    g, loss = mlp_gradient(m, feat, target, kernel=kernel)
     mean, istd, scale = norm_of(m)
     ge, le = mlp_ref.gradient(mlp_params(m), mean, istd, scale, feat, target, emulate=True)
     gx, _ = mlp_ref.gradient(mlp_params(m), mean, istd, scale, feat, target, emulate=False)
@@ -100,16 +106,32 @@ def test_mlp_gradient_matches_fp64_reference():
         assert cos >= 0.99, (a, b, cos)
 
 
-def test_training_reduces_loss():
+@pytest.mark.parametrize("kernel", [L.MLP_TRAIN_TCGEN05, L.MLP_TRAIN_MMA_SYNC])
+def test_training_reduces_loss(kernel):
     rng = np.random.default_rng(3)
     feat = rng.normal(size=(50000, 8)).astype(np.float32)
     target = (np.tanh(feat[:, 0]) - 0.5 * feat[:, 1] * feat[:, 2] + 0.1 * feat[:, 3]).astype(np.float32) * 1e-5
     m = mlp_init(3)
     mlp_fit_normalization(m, feat, target)
-    _, l0 = mlp_gradient(m, feat, target)
-    loss = mlp_train(m, feat, target, epochs=30, batch=2048, lr=3e-3, seed=3)
-    _, l1 = mlp_gradient(m, feat, target)
+    _, l0 = mlp_gradient(m, feat, target, kernel=kernel)
+    loss = mlp_train(m, feat, target, epochs=30, batch=2048, lr=3e-3, seed=3, kernel=kernel)
+    _, l1 = mlp_gradient(m, feat, target, kernel=kernel)
     assert l1 < 0.05 * l0 and loss < 0.05 * l0, (l0, l1, loss)
+
+
+def test_gradient_kernels_agree():
+    """The tcgen05 and mma.sync gradient kernels on the same rows: every
+    parameter block within 2 % (relative L2) of each other, equal losses
+    within 1e-3."""
+    m, feat, target = random_model(5, rows=5000)
+    g_tc, l_tc = mlp_gradient(m, feat, target, kernel=L.MLP_TRAIN_TCGEN05)
+    g_ms, l_ms = mlp_gradient(m, feat, target, kernel=L.MLP_TRAIN_MMA_SYNC)
+    assert abs(l_tc - l_ms) <= 1e-3 * max(l_ms, 1e-12)
+    blocks = [(mlp_ref.OFF_W1, mlp_ref.OFF_B1), (mlp_ref.OFF_B1, mlp_ref.OFF_W2), (mlp_ref.OFF_W2, mlp_ref.OFF_B2),
+              (mlp_ref.OFF_B2, mlp_ref.OFF_W3), (mlp_ref.OFF_W3, mlp_ref.OFF_B3), (mlp_ref.OFF_B3, 4801)]
+    for a, b in blocks:
+        err = np.linalg.norm(g_tc[a:b] - g_ms[a:b]) / max(np.linalg.norm(g_ms[a:b]), 1e-30)
+        assert err <= 2e-2, (a, b, err)
 
 
 def test_trace_target_is_sum_of_iteration_multipliers():

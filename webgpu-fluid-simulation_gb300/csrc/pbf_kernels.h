@@ -191,6 +191,12 @@ cudaError_t launch_mlp_infer(const float* d_params, const pbf_mlp& model, const 
 cudaError_t launch_mlp_infer_tc(const float* d_params, const pbf_mlp& model, const float* d_feat, uint32_t rows,
                                 float* d_lambda, float* d_lam_sum, cudaStream_t st, const float4* d_xs,
                                 float4* d_xl, uint32_t* d_err);
+// Forward + backward on tcgen05.mma (pbf_mlp_tc.cu): the gradient accumulates
+// into d_grad (atomically), the summed squared error into d_loss; d_err
+// receives PBF_DEVERR_MMA_TIMEOUT when a bounded completion wait gives up.
+cudaError_t launch_mlp_grad_tc(const float* d_params, const pbf_mlp& model, const float* d_feat,
+                               const float* d_target, uint32_t rows, float* d_grad, float* d_loss, uint32_t* d_err,
+                               cudaStream_t st);
 cudaError_t launch_mlp_grad(const float* d_params, const pbf_mlp& model, const float* d_feat, const float* d_target,
                             uint32_t rows, float* d_grad, float* d_loss, cudaStream_t st);
 cudaError_t launch_gather_f32(uint32_t n, const uint32_t* perm, const float* src, float* dst, cudaStream_t st);

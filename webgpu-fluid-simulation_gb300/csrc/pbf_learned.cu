@@ -566,26 +566,39 @@ int pbf_mlp_forward(const pbf_mlp* m, const float* feat, uint32_t rows, float* o
 
 int pbf_mlp_gradient(const pbf_mlp* m, const float* feat, const float* target, uint32_t rows, float* grad,
                      float* loss) {
+  return pbf_mlp_gradient_ex(m, feat, target, rows, grad, loss, PBF_MLP_TRAIN_TCGEN05);
+}
+
+int pbf_mlp_gradient_ex(const pbf_mlp* m, const float* feat, const float* target, uint32_t rows, float* grad,
+                        float* loss, uint32_t kernel) {
   if (!m || !feat || !target || !grad || rows == 0) return PBF_EINVAL;
+  if (kernel != PBF_MLP_TRAIN_TCGEN05 && kernel != PBF_MLP_TRAIN_MMA_SYNC) return PBF_EINVAL;
   float *dP = nullptr, *dF = nullptr, *dT = nullptr, *dG = nullptr;
   cudaError_t e = cudaMalloc(&dP, sizeof(m->params));
   if (e == cudaSuccess) e = cudaMalloc(&dF, (size_t)rows * 8 * sizeof(float));
   if (e == cudaSuccess) e = cudaMalloc(&dT, (size_t)rows * sizeof(float));
-  if (e == cudaSuccess) e = cudaMalloc(&dG, (PBF_MLP_PARAMS + 1) * sizeof(float));
+  // gradient, loss, then the device error word
+  if (e == cudaSuccess) e = cudaMalloc(&dG, (PBF_MLP_PARAMS + 2) * sizeof(float));
   if (e == cudaSuccess) e = cudaMemcpy(dP, m->params, sizeof(m->params), cudaMemcpyHostToDevice);
   if (e == cudaSuccess) e = cudaMemcpy(dF, feat, (size_t)rows * 8 * sizeof(float), cudaMemcpyHostToDevice);
   if (e == cudaSuccess) e = cudaMemcpy(dT, target, (size_t)rows * sizeof(float), cudaMemcpyHostToDevice);
-  if (e == cudaSuccess) e = cudaMemset(dG, 0, (PBF_MLP_PARAMS + 1) * sizeof(float));
-  if (e == cudaSuccess) e = launch_mlp_grad(dP, *m, dF, dT, rows, dG, dG + PBF_MLP_PARAMS, 0);
+  if (e == cudaSuccess) e = cudaMemset(dG, 0, (PBF_MLP_PARAMS + 2) * sizeof(float));
+  uint32_t* dErr = reinterpret_cast<uint32_t*>(dG + PBF_MLP_PARAMS + 1);
+  if (e == cudaSuccess)
+    e = kernel == PBF_MLP_TRAIN_TCGEN05 ? launch_mlp_grad_tc(dP, *m, dF, dT, rows, dG, dG + PBF_MLP_PARAMS, dErr, 0)
+                                        : launch_mlp_grad(dP, *m, dF, dT, rows, dG, dG + PBF_MLP_PARAMS, 0);
   float l = 0.0f;
+  uint32_t herr = 0;
   if (e == cudaSuccess) e = cudaMemcpy(grad, dG, PBF_MLP_PARAMS * sizeof(float), cudaMemcpyDeviceToHost);
   if (e == cudaSuccess) e = cudaMemcpy(&l, dG + PBF_MLP_PARAMS, sizeof(float), cudaMemcpyDeviceToHost);
+  if (e == cudaSuccess) e = cudaMemcpy(&herr, dErr, sizeof(uint32_t), cudaMemcpyDeviceToHost);
   if (loss) *loss = l / (float)rows;
   cudaFree(dP);
   cudaFree(dF);
   cudaFree(dT);
   cudaFree(dG);
-  return e == cudaSuccess ? PBF_OK : PBF_ECUDA;
+  if (e != cudaSuccess) return PBF_ECUDA;
+  return herr ? PBF_ETIMEOUT : PBF_OK;
 }
 
 // Mini-batch Adam on rows (feat, target) held on the host; shuffled once by
@@ -593,6 +606,7 @@ int pbf_mlp_gradient(const pbf_mlp* m, const float* feat, const float* target, u
 int pbf_mlp_train(pbf_mlp* m, const float* feat, const float* target, uint32_t rows, const pbf_train_config* tc,
                   float* final_loss) {
   if (!m || !feat || !target || !tc || rows == 0 || tc->batch == 0) return PBF_EINVAL;
+  if (tc->kernel != PBF_MLP_TRAIN_TCGEN05 && tc->kernel != PBF_MLP_TRAIN_MMA_SYNC) return PBF_EINVAL;
   std::vector<uint32_t> perm(rows);
   for (uint32_t i = 0; i < rows; ++i) perm[i] = i;
   uint64_t s = tc->seed ^ 0x5eedull;
@@ -609,7 +623,10 @@ int pbf_mlp_train(pbf_mlp* m, const float* feat, const float* target, uint32_t r
   cudaError_t e = cudaMalloc(&dP, sizeof(m->params));
   if (e == cudaSuccess) e = cudaMalloc(&dF, f.size() * sizeof(float));
   if (e == cudaSuccess) e = cudaMalloc(&dT, tg.size() * sizeof(float));
-  if (e == cudaSuccess) e = cudaMalloc(&dG, (PBF_MLP_PARAMS + 1) * sizeof(float));
+  // gradient, loss, then the device error word
+  if (e == cudaSuccess) e = cudaMalloc(&dG, (PBF_MLP_PARAMS + 2) * sizeof(float));
+  if (e == cudaSuccess) e = cudaMemset(dG, 0, (PBF_MLP_PARAMS + 2) * sizeof(float));
+  uint32_t* dErr = reinterpret_cast<uint32_t*>(dG + PBF_MLP_PARAMS + 1);
   if (e == cudaSuccess) e = cudaMalloc(&dM, PBF_MLP_PARAMS * sizeof(float));
   if (e == cudaSuccess) e = cudaMalloc(&dV, PBF_MLP_PARAMS * sizeof(float));
   if (e == cudaSuccess) e = cudaMemcpy(dP, m->params, sizeof(m->params), cudaMemcpyHostToDevice);
@@ -628,7 +645,10 @@ int pbf_mlp_train(pbf_mlp* m, const float* feat, const float* target, uint32_t r
     for (uint32_t b = 0; b < per_epoch && e == cudaSuccess; ++b) {
       e = cudaMemsetAsync(dG, 0, (PBF_MLP_PARAMS + 1) * sizeof(float), 0);
       if (e == cudaSuccess)
-        e = launch_mlp_grad(dP, *m, dF + 8 * (size_t)b * batch, dT + (size_t)b * batch, batch, dG, dLoss, 0);
+        e = tc->kernel == PBF_MLP_TRAIN_TCGEN05
+                ? launch_mlp_grad_tc(dP, *m, dF + 8 * (size_t)b * batch, dT + (size_t)b * batch, batch, dG, dLoss,
+                                     dErr, 0)
+                : launch_mlp_grad(dP, *m, dF + 8 * (size_t)b * batch, dT + (size_t)b * batch, batch, dG, dLoss, 0);
       ++step;
       float lr = tc->learning_rate;
       if (tc->epochs > 1) lr *= (float)(0.5 * (1.0 + std::cos(3.14159265358979 * ep / tc->epochs)));
@@ -641,7 +661,9 @@ int pbf_mlp_train(pbf_mlp* m, const float* feat, const float* target, uint32_t r
     }
     epoch_loss = acc;
   }
+  uint32_t herr = 0;
   if (e == cudaSuccess) e = cudaMemcpy(m->params, dP, sizeof(m->params), cudaMemcpyDeviceToHost);
+  if (e == cudaSuccess) e = cudaMemcpy(&herr, dErr, sizeof(uint32_t), cudaMemcpyDeviceToHost);
   cudaFree(dP);
   cudaFree(dF);
   cudaFree(dT);
@@ -649,7 +671,8 @@ int pbf_mlp_train(pbf_mlp* m, const float* feat, const float* target, uint32_t r
   cudaFree(dM);
   cudaFree(dV);
   if (final_loss) *final_loss = (float)epoch_loss;
-  return e == cudaSuccess ? PBF_OK : PBF_ECUDA;
+  if (e != cudaSuccess) return PBF_ECUDA;
+  return herr ? PBF_ETIMEOUT : PBF_OK;
 }
 
 }  // extern "C"

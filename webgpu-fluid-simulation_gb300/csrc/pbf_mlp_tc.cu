@@ -344,6 +344,311 @@ __global__ void __launch_bounds__(kTcThreads, 4) k_mlp_infer_tc(const float* __r
   if (tid == 0 && (sm.failed[0] | sm.failed[1]) && err) atomicOr(err, PBF_DEVERR_MMA_TIMEOUT);
 }
 
+
+// ---- training: forward + backward on the tensor cores --------------------------------
+//
+// One CTA of 128 threads (one warpgroup), thread t serving row t of each
+// 128-row tile, TMEM holding every accumulator (512 columns: one CTA per SM):
+//   columns   0- 63  z1 = X W1 + b1            (kept for the backward pass)
+//   columns  64-127  z2 = H1 W2 + b2           (kept for the backward pass)
+//   columns 128-143  y  = H2 w3 + b3           (hi / lo columns 0, 1)
+//   columns 160-223  dH1 = dZ2 W2^T
+//   columns 256-319  [dW2; db2]  accumulated over the CTA's tiles
+//   columns 320-383  [dW1; db1]  accumulated over the CTA's tiles
+//   columns 384-399  [dw3; db3]  accumulated over the CTA's tiles
+// The weight and bias gradients are products over the tile's rows: their A
+// operands are the transposed activations H1^T, X^T, H2^T (M = 128: the
+// hidden / input units, then one row of ones that turns the same product
+// into the bias gradient, then zeros) and their B operands dZ2^T, dZ1^T and
+// dy (N x K = rows), each written by its row's thread into column t of a
+// K-major tile.  dy is split into bf16 hi / lo rows, so dw3 and db3 keep
+// about 2^-16 relative accuracy; the other products take their operands in
+// bf16 at the rounding points of the mma.sync kernel (X, W, H1, H2, dZ2,
+// dZ1).  All operands are K-major, no swizzle, as in k_mlp_infer_tc.
+constexpr uint32_t kGrTmemCols = 512;
+constexpr uint32_t kColZ1 = 0, kColZ2 = 64, kColY = 128, kColDH1 = 160, kColG1 = 256, kColG2 = 320, kColG3 = 384;
+
+struct GrSmem {
+  alignas(128) uint8_t x1[128 * 16 * 2];    // X rows (K = 16: 8 features, ones at 8, 9)
+  alignas(128) uint8_t hA[128 * 64 * 2];    // H1 rows, then H2 rows, then dZ2 rows
+  alignas(128) uint8_t tH1[128 * 128 * 2];  // A of [dW2; db2]: H1^T, ones (row 64), zeros
+  alignas(128) uint8_t tX[128 * 128 * 2];   // A of [dW1; db1]: X^T, ones (row 8), zeros
+  alignas(128) uint8_t tH2[128 * 128 * 2];  // A of [dw3; db3]: H2^T, ones (row 64), zeros
+  alignas(128) uint8_t tDZ2[64 * 128 * 2];  // B: dZ2^T (N = 64 x K = rows)
+  alignas(128) uint8_t tDZ1[64 * 128 * 2];  // B: dZ1^T
+  alignas(128) uint8_t tDY[16 * 128 * 2];   // B: dy hi (N row 0), lo (row 1), zeros
+  alignas(128) uint8_t b1[64 * 16 * 2];     // W1'^T with b1 hi / lo in K rows 8, 9
+  alignas(128) uint8_t b2[64 * 64 * 2];     // W2^T (N = out, K = in)
+  alignas(128) uint8_t b2b[64 * 16 * 2];    // b2 hi / lo in K rows 8, 9
+  alignas(128) uint8_t b3[16 * 64 * 2];     // w3 hi / lo in N rows 0, 1
+  alignas(128) uint8_t b3b[16 * 16 * 2];    // b3 hi / lo in N row 0, K rows 8, 9
+  alignas(128) uint8_t b2t[64 * 64 * 2];    // W2 (N = in, K = out): B of dH1 = dZ2 W2^T
+  alignas(8) uint64_t mbar;
+  uint32_t tmem;
+  uint32_t failed;
+};
+
+__device__ __forceinline__ void st_bf16(uint8_t* tile, uint32_t off, float v) {
+  *reinterpret_cast<__nv_bfloat16*>(tile + off) = __float2bfloat16_rn(v);
+}
+
+// All threads' shared-memory writes visible to the tensor cores, then thread
+// 0 issues `issue()` and commits; everyone waits for the MMAs (bounded).
+template <class F>
+__device__ __forceinline__ bool gr_mma_step(GrSmem& sm, uint32_t mbar, uint32_t& phase, F&& issue) {
+  fence_async_smem();
+  fence_before_sync();
+  __syncthreads();
+  fence_after_sync();
+  if (threadIdx.x == 0) {
+    issue();
+    mma_commit(mbar);
+  }
+  const bool ok = mbar_wait(mbar, phase);
+  phase ^= 1u;
+  fence_after_sync();
+  return ok;
+}
+
+__global__ void __launch_bounds__(128, 1) k_mlp_grad_tc(const float* __restrict__ P, Norm nm,
+                                                      const float* __restrict__ feat,
+                                                      const float* __restrict__ target, uint32_t rows,
+                                                      float inv_batch, float* __restrict__ G,
+                                                      float* __restrict__ loss, uint32_t* err) {
+  extern __shared__ __align__(128) uint8_t gr_raw[];
+  GrSmem& sm = *reinterpret_cast<GrSmem*>(gr_raw);
+  const uint32_t tid = threadIdx.x, warp = tid >> 5, row = tid;
+  const __nv_bfloat16 z16 = __float2bfloat16_rn(0.0f);
+  // weights (as in k_mlp_infer_tc) and the transposed W2
+  for (uint32_t q = tid; q < 64u * 16u; q += 128u) {
+    const uint32_t n = q / 16u, k = q % 16u;
+    __nv_bfloat16 w = z16, wb = z16;
+    if (k < (uint32_t)kIn) {
+      w = __float2bfloat16_rn(P[OFF_W1 + k * kH + n]);
+    } else if (k == 8) {
+      w = bf_hi(P[OFF_B1 + n]);
+      wb = bf_hi(P[OFF_B2 + n]);
+    } else if (k == 9) {
+      w = bf_lo(P[OFF_B1 + n]);
+      wb = bf_lo(P[OFF_B2 + n]);
+    }
+    *reinterpret_cast<__nv_bfloat16*>(sm.b1 + canon(n, k, 16)) = w;
+    *reinterpret_cast<__nv_bfloat16*>(sm.b2b + canon(n, k, 16)) = wb;
+  }
+  for (uint32_t q = tid; q < 64u * 64u; q += 128u) {
+    const uint32_t i = q / 64u, j = q % 64u;  // W2[i][j]: in i, out j
+    const __nv_bfloat16 w = __float2bfloat16_rn(P[OFF_W2 + q]);
+    *reinterpret_cast<__nv_bfloat16*>(sm.b2 + canon(j, i, 64)) = w;
+    *reinterpret_cast<__nv_bfloat16*>(sm.b2t + canon(i, j, 64)) = w;
+  }
+  for (uint32_t q = tid; q < 16u * 64u; q += 128u) {
+    const uint32_t n = q / 64u, k = q % 64u;
+    const float w = P[OFF_W3 + k];
+    *reinterpret_cast<__nv_bfloat16*>(sm.b3 + canon(n, k, 64)) = n == 0 ? bf_hi(w) : n == 1 ? bf_lo(w) : z16;
+  }
+  for (uint32_t q = tid; q < 16u * 16u; q += 128u) {
+    const uint32_t n = q / 16u, k = q % 16u;
+    const float b = P[OFF_B3];
+    *reinterpret_cast<__nv_bfloat16*>(sm.b3b + canon(n, k, 16)) =
+        (n == 0 && k == 8) ? bf_hi(b) : (n == 0 && k == 9) ? bf_lo(b) : z16;
+  }
+  // constant parts of the gradient operands: the ones rows and the zeros
+  // (the data rows are rewritten for every tile)
+  for (uint32_t q = tid; q < 128u * 128u; q += 128u) {
+    const uint32_t m = q / 128u, k = q % 128u;
+    const uint32_t off = canon(m, k, 128);
+    *reinterpret_cast<__nv_bfloat16*>(sm.tH1 + off) = __float2bfloat16_rn(m == 64u ? 1.0f : 0.0f);
+    *reinterpret_cast<__nv_bfloat16*>(sm.tH2 + off) = __float2bfloat16_rn(m == 64u ? 1.0f : 0.0f);
+    *reinterpret_cast<__nv_bfloat16*>(sm.tX + off) = __float2bfloat16_rn(m == 8u ? 1.0f : 0.0f);
+  }
+  for (uint32_t q = tid; q < 16u * 128u; q += 128u) *reinterpret_cast<__nv_bfloat16*>(sm.tDY + 2u * q) = z16;
+  st_shared_v4(smem_u32(sm.x1 + canon(row, 8, 16)), pack_bf16(1.0f, 1.0f), 0u, 0u, 0u);
+  const uint32_t mbar = smem_u32(&sm.mbar);
+  if (tid == 0) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(mbar) : "memory");
+    sm.failed = 0u;
+  }
+  if (warp == 0) {
+    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(&sm.tmem)),
+                 "r"(kGrTmemCols)
+                 : "memory");
+    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+  }
+  fence_async_smem();
+  fence_before_sync();
+  __syncthreads();
+  fence_after_sync();
+  const uint32_t tm = sm.tmem;
+  const uint32_t lane_base = (32u * warp) << 16;
+  const uint64_t x1d = smem_desc(smem_u32(sm.x1), 128, 256);
+  const uint64_t b1d = smem_desc(smem_u32(sm.b1), 128, 256);
+  const uint64_t b2bd = smem_desc(smem_u32(sm.b2b), 128, 256);
+  const uint64_t b3bd = smem_desc(smem_u32(sm.b3b), 128, 256);
+  const uint32_t hA = smem_u32(sm.hA), b2 = smem_u32(sm.b2), b3 = smem_u32(sm.b3), b2t = smem_u32(sm.b2t);
+  const uint32_t tH1 = smem_u32(sm.tH1), tX = smem_u32(sm.tX), tH2 = smem_u32(sm.tH2);
+  const uint32_t tDZ2 = smem_u32(sm.tDZ2), tDZ1 = smem_u32(sm.tDZ1), tDY = smem_u32(sm.tDY);
+  uint32_t phase = 0;
+  bool ok = true;
+  float lsum = 0.0f;
+  uint32_t done_tiles = 0;
+  const uint32_t tiles = (rows + 127u) / 128u;
+  for (uint32_t tile = blockIdx.x; tile < tiles && ok; tile += gridDim.x, ++done_tiles) {
+    const uint32_t r = tile * 128u + row;
+    const bool valid = r < rows;
+    float x[8], t = 0.0f;
+#pragma unroll
+    for (int k = 0; k < 8; ++k) x[k] = valid ? (feat[8 * (size_t)r + k] - nm.mean[k]) * nm.inv_std[k] : 0.0f;
+    if (valid) t = target[r] / nm.lam_scale;
+    st_shared_v4(smem_u32(sm.x1 + canon(row, 0, 16)), pack_bf16(x[0], x[1]), pack_bf16(x[2], x[3]),
+                 pack_bf16(x[4], x[5]), pack_bf16(x[6], x[7]));
+#pragma unroll
+    for (int k = 0; k < 8; ++k) st_bf16(sm.tX, canon(k, row, 128), x[k]);
+    // z1 = X W1 + b1
+    ok = gr_mma_step(sm, mbar, phase, [&] { mma_f16(tm + kColZ1, x1d, b1d, kIdesc64, 0u); }) && ok;
+    // H1 rows (layer 2's A) and H1^T (dW2's A)
+#pragma unroll
+    for (int half = 0; half < 2; ++half) {
+      float v[32];
+      tmem_ld32(tm + lane_base + kColZ1 + 32u * half, v);
+#pragma unroll
+      for (int kb = 0; kb < 4; ++kb) {
+        const int j = 8 * kb;
+        float h[8];
+#pragma unroll
+        for (int e = 0; e < 8; ++e) h[e] = silu_h(v[j + e]);
+        st_shared_v4(hA + canon(row, 32 * half + j, 64), pack_bf16(h[0], h[1]), pack_bf16(h[2], h[3]),
+                     pack_bf16(h[4], h[5]), pack_bf16(h[6], h[7]));
+#pragma unroll
+        for (int e = 0; e < 8; ++e) st_bf16(sm.tH1, canon(32 * half + j + e, row, 128), h[e]);
+      }
+    }
+    // z2 = H1 W2 + b2
+    ok = gr_mma_step(sm, mbar, phase, [&] {
+      for (uint32_t ks = 0; ks < 4; ++ks)
+        mma_f16(tm + kColZ2, smem_desc(hA + 256u * ks, 128, 1024), smem_desc(b2 + 256u * ks, 128, 1024), kIdesc64,
+                ks > 0 ? 1u : 0u);
+      mma_f16(tm + kColZ2, x1d, b2bd, kIdesc64, 1u);
+    }) && ok;
+    // H2 rows (layer 3's A) and H2^T (dw3's A)
+#pragma unroll
+    for (int half = 0; half < 2; ++half) {
+      float v[32];
+      tmem_ld32(tm + lane_base + kColZ2 + 32u * half, v);
+#pragma unroll
+      for (int kb = 0; kb < 4; ++kb) {
+        const int j = 8 * kb;
+        float h[8];
+#pragma unroll
+        for (int e = 0; e < 8; ++e) h[e] = silu_h(v[j + e]);
+        st_shared_v4(hA + canon(row, 32 * half + j, 64), pack_bf16(h[0], h[1]), pack_bf16(h[2], h[3]),
+                     pack_bf16(h[4], h[5]), pack_bf16(h[6], h[7]));
+#pragma unroll
+        for (int e = 0; e < 8; ++e) st_bf16(sm.tH2, canon(32 * half + j + e, row, 128), h[e]);
+      }
+    }
+    // y = H2 w3 + b3
+    ok = gr_mma_step(sm, mbar, phase, [&] {
+      for (uint32_t ks = 0; ks < 4; ++ks)
+        mma_f16(tm + kColY, smem_desc(hA + 256u * ks, 128, 1024), smem_desc(b3 + 256u * ks, 128, 1024), kIdesc16,
+                ks > 0 ? 1u : 0u);
+      mma_f16(tm + kColY, x1d, b3bd, kIdesc16, 1u);
+    }) && ok;
+    float y0, y1;
+    tmem_ld2(tm + lane_base + kColY, y0, y1);
+    const float err_y = valid ? (y0 + y1) - t : 0.0f;
+    lsum += err_y * err_y;
+    const float dy = 2.0f * err_y * inv_batch;
+    st_bf16(sm.tDY, canon(0, row, 128), dy);
+    st_bf16(sm.tDY, canon(1, row, 128), dy - __bfloat162float(__float2bfloat16_rn(dy)));
+    // dZ2 = dy w3 silu'(z2): rows (dH1's A) and transposed (dW2's B)
+#pragma unroll
+    for (int half = 0; half < 2; ++half) {
+      float v[32];
+      tmem_ld32(tm + lane_base + kColZ2 + 32u * half, v);
+#pragma unroll
+      for (int kb = 0; kb < 4; ++kb) {
+        const int j = 8 * kb;
+        float d[8];
+#pragma unroll
+        for (int e = 0; e < 8; ++e) d[e] = dy * P[OFF_W3 + 32 * half + j + e] * dsilu_f(v[j + e]);
+        st_shared_v4(hA + canon(row, 32 * half + j, 64), pack_bf16(d[0], d[1]), pack_bf16(d[2], d[3]),
+                     pack_bf16(d[4], d[5]), pack_bf16(d[6], d[7]));
+#pragma unroll
+        for (int e = 0; e < 8; ++e) st_bf16(sm.tDZ2, canon(32 * half + j + e, row, 128), d[e]);
+      }
+    }
+    // dH1 = dZ2 W2^T
+    ok = gr_mma_step(sm, mbar, phase, [&] {
+      for (uint32_t ks = 0; ks < 4; ++ks)
+        mma_f16(tm + kColDH1, smem_desc(hA + 256u * ks, 128, 1024), smem_desc(b2t + 256u * ks, 128, 1024),
+                kIdesc64, ks > 0 ? 1u : 0u);
+    }) && ok;
+    // dZ1 = dH1 silu'(z1), transposed (dW1's B)
+#pragma unroll
+    for (int half = 0; half < 2; ++half) {
+      float g[32], z[32];
+      tmem_ld32(tm + lane_base + kColDH1 + 32u * half, g);
+      tmem_ld32(tm + lane_base + kColZ1 + 32u * half, z);
+#pragma unroll
+      for (int e = 0; e < 32; ++e) st_bf16(sm.tDZ1, canon(32 * half + e, row, 128), g[e] * dsilu_f(z[e]));
+    }
+    // the gradient products over the tile's rows, accumulated across tiles
+    const uint32_t acc0 = done_tiles > 0 ? 1u : 0u;
+    ok = gr_mma_step(sm, mbar, phase, [&] {
+      for (uint32_t ks = 0; ks < 8; ++ks) {
+        const uint32_t a = ks > 0 ? 1u : acc0;
+        mma_f16(tm + kColG1, smem_desc(tH1 + 256u * ks, 128, 2048), smem_desc(tDZ2 + 256u * ks, 128, 2048), kIdesc64,
+                a);
+        mma_f16(tm + kColG2, smem_desc(tX + 256u * ks, 128, 2048), smem_desc(tDZ1 + 256u * ks, 128, 2048), kIdesc64,
+                a);
+        mma_f16(tm + kColG3, smem_desc(tH2 + 256u * ks, 128, 2048), smem_desc(tDY + 256u * ks, 128, 2048), kIdesc16,
+                a);
+      }
+    }) && ok;
+    ok = !__syncthreads_or(!ok);
+  }
+  if (!ok) {
+    // a completion wait gave up: let the MMAs in flight finish (bounded)
+    // before TMEM is read or released
+    mbar_wait(mbar, phase);
+    if (tid == 0 && err) atomicOr(err, PBF_DEVERR_MMA_TIMEOUT);
+  } else if (done_tiles > 0) {
+    // row m of the accumulators: [dW2; db2], [dW1; db1], [dw3; db3]
+#pragma unroll
+    for (int half = 0; half < 2; ++half) {
+      float v[32];
+      tmem_ld32(tm + lane_base + kColG1 + 32u * half, v);
+      if (row < 64u) {
+#pragma unroll
+        for (int e = 0; e < 32; ++e) atomicAdd(G + OFF_W2 + row * kH + 32 * half + e, v[e]);
+      } else if (row == 64u) {
+#pragma unroll
+        for (int e = 0; e < 32; ++e) atomicAdd(G + OFF_B2 + 32 * half + e, v[e]);
+      }
+      tmem_ld32(tm + lane_base + kColG2 + 32u * half, v);
+      if (row < (uint32_t)kIn) {
+#pragma unroll
+        for (int e = 0; e < 32; ++e) atomicAdd(G + OFF_W1 + row * kH + 32 * half + e, v[e]);
+      } else if (row == (uint32_t)kIn) {
+#pragma unroll
+        for (int e = 0; e < 32; ++e) atomicAdd(G + OFF_B1 + 32 * half + e, v[e]);
+      }
+    }
+    float g0, g1;
+    tmem_ld2(tm + lane_base + kColG3, g0, g1);
+    if (row < 64u) atomicAdd(G + OFF_W3 + row, g0 + g1);
+    else if (row == 64u) atomicAdd(G + OFF_B3, g0 + g1);
+  }
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) lsum += __shfl_xor_sync(0xffffffffu, lsum, o);
+  if ((tid & 31u) == 0) atomicAdd(loss, lsum);
+  fence_before_sync();
+  __syncthreads();
+  fence_after_sync();
+  if (warp == 0) {
+    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tm), "r"(kGrTmemCols) : "memory");
+  }
+}
 }  // namespace
 
 // No dynamic shared memory: the static tile buffers (about 55 KB per CTA) and
@@ -386,6 +691,36 @@ cudaError_t launch_mlp_infer_tc(const float* d_params, const pbf_mlp& model, con
   const uint32_t grid = std::min<uint32_t>((tiles + 1) / 2, (uint32_t)sms * (uint32_t)per_sm);
   k_mlp_infer_tc<<<grid, kTcThreads, kTcPadSmem, st>>>(d_params, nm, d_feat, rows, d_lambda, d_lam_sum, d_xs, d_xl,
                                                        d_err);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_mlp_grad_tc(const float* d_params, const pbf_mlp& model, const float* d_feat,
+                               const float* d_target, uint32_t rows, float* d_grad, float* d_loss, uint32_t* d_err,
+                               cudaStream_t st) {
+  if (rows == 0) return cudaSuccess;
+  static int sms = 0;
+  if (sms == 0) {
+    int dev = 0;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e == cudaSuccess) e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    if (e == cudaSuccess)
+      e = cudaFuncSetAttribute(k_mlp_grad_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sizeof(GrSmem));
+    if (e != cudaSuccess) {
+      sms = 0;
+      return e;
+    }
+  }
+  Norm nm;
+  for (int k = 0; k < kIn; ++k) {
+    nm.mean[k] = model.feat_mean[k];
+    nm.inv_std[k] = model.feat_inv_std[k];
+  }
+  nm.lam_scale = model.lam_scale;
+  const uint32_t tiles = (rows + 127u) / 128u;
+  // one CTA per SM at most: each holds all 512 TMEM columns
+  const uint32_t grid = std::min<uint32_t>(tiles, (uint32_t)sms);
+  k_mlp_grad_tc<<<grid, 128, sizeof(GrSmem), st>>>(d_params, nm, d_feat, d_target, rows, 1.0f / (float)rows,
+                                                   d_grad, d_loss, d_err);
   return cudaGetLastError();
 }
 

@@ -60,6 +60,7 @@ class KernelTime(ctypes.Structure):
 
 MLP_PARAMS = 4801
 MLP_KERNEL_MMA_SYNC, MLP_KERNEL_TCGEN05 = 0, 1
+MLP_TRAIN_TCGEN05, MLP_TRAIN_MMA_SYNC = 0, 1  # pbf_train_config.kernel
 
 
 class MLP(ctypes.Structure):
@@ -68,7 +69,7 @@ class MLP(ctypes.Structure):
 
 
 class TrainConfig(ctypes.Structure):
-    _fields_ = [("epochs", u32), ("batch", u32), ("learning_rate", f32), ("reserved", u32),
+    _fields_ = [("epochs", u32), ("batch", u32), ("learning_rate", f32), ("kernel", u32),
                 ("seed", ctypes.c_uint64)]
 
 
@@ -200,6 +201,7 @@ SIGNATURES = {
     "pbf_mlp_fit_normalization": (ctypes.c_int, [ctypes.POINTER(MLP), _FP, _FP, u32]),
     "pbf_mlp_forward": (ctypes.c_int, [ctypes.POINTER(MLP), _FP, u32, _FP]),
     "pbf_mlp_gradient": (ctypes.c_int, [ctypes.POINTER(MLP), _FP, _FP, u32, _FP, _FP]),
+    "pbf_mlp_gradient_ex": (ctypes.c_int, [ctypes.POINTER(MLP), _FP, _FP, u32, _FP, _FP, u32]),
     "pbf_mlp_train": (ctypes.c_int, [ctypes.POINTER(MLP), _FP, _FP, u32, ctypes.POINTER(TrainConfig), _FP]),
     "pbf_set_trace": (ctypes.c_int, [_P, u32, u32, ctypes.c_uint64]),
     "pbf_trace_rows": (ctypes.c_int, [_P, _UP]),

@@ -563,21 +563,25 @@ def mlp_forward(m, feat, kernel=L.MLP_KERNEL_MMA_SYNC):
     return out
 
 
-def mlp_gradient(m, feat, target):
+def mlp_gradient(m, feat, target, kernel=None):
+    """Gradient and mean loss of the network on (feat, target); kernel:
+    L.MLP_TRAIN_TCGEN05 (default) or L.MLP_TRAIN_MMA_SYNC."""
     f = np.ascontiguousarray(feat, np.float32)
     t = np.ascontiguousarray(target, np.float32)
     g = np.zeros(L.MLP_PARAMS, np.float32)
     loss = ctypes.c_float()
-    rc = L.load().pbf_mlp_gradient(ctypes.byref(m), _fp(f), _fp(t), f.shape[0], _fp(g), ctypes.byref(loss))
+    k = L.MLP_TRAIN_TCGEN05 if kernel is None else int(kernel)
+    rc = L.load().pbf_mlp_gradient_ex(ctypes.byref(m), _fp(f), _fp(t), f.shape[0], _fp(g), ctypes.byref(loss), k)
     if rc:
         raise L.PBFError(rc, "mlp_gradient")
     return g, loss.value
 
 
-def mlp_train(m, feat, target, epochs=20, batch=8192, lr=2e-3, seed=0):
+def mlp_train(m, feat, target, epochs=20, batch=8192, lr=2e-3, seed=0, kernel=None):
     f = np.ascontiguousarray(feat, np.float32)
     t = np.ascontiguousarray(target, np.float32)
-    tc = L.TrainConfig(epochs=int(epochs), batch=int(batch), learning_rate=float(lr), reserved=0, seed=int(seed))
+    k = L.MLP_TRAIN_TCGEN05 if kernel is None else int(kernel)
+    tc = L.TrainConfig(epochs=int(epochs), batch=int(batch), learning_rate=float(lr), kernel=k, seed=int(seed))
     loss = ctypes.c_float()
     rc = L.load().pbf_mlp_train(ctypes.byref(m), _fp(f), _fp(t), f.shape[0], ctypes.byref(tc), ctypes.byref(loss))
     if rc:

@@ -243,6 +243,26 @@ def test_step_exact_mode_bitexact(name, substeps):
     sim.close()
 
 
+@pytest.mark.parametrize("substeps", [1, 4])
+def test_step_exact_mode_trilinear_bitexact(substeps):
+    """The trilinear boundary interpolation (PBF_INTERP_TRILINEAR: the 8
+    corner nodes of the field cell) in exact mode, against the restatement's
+    trilinear sampler on the torus map: every field bit-identical."""
+    sc = scenes.reference_scene("boundary_small")
+    sc.config = scenes.copy_config(sc.config)
+    sc.config.boundary_interp = L.INTERP_TRILINEAR
+    pts = scenes.jitter(sc.particles, 0.001, seed=30 + substeps)
+    sim, orc = make_pair(sc, L.FP_EXACT, pts)
+    for _ in range(substeps):
+        sim.run()
+    orc.substep(substeps)
+    a, b = fields_of(sim), oracle_fields(orc)
+    sim.close()
+    for k in a:
+        assert np.array_equal(a[k], b[k]), (k, np.abs(a[k].astype(np.float64) - b[k]).max())
+    assert (b["boundary"][:, 3] > 0).sum() > 50
+
+
 @pytest.mark.parametrize("name", SCENES)
 def test_step_fast_mode_tolerance(name):
     """Fast mode (FMA, reciprocal math) against the FP32 restatement and the

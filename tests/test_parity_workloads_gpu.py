@@ -186,6 +186,64 @@ def test_sphere_drop_snapshot_exact_mode_bitexact(sphere_drop):
         assert np.array_equal(g[k], a[k]), (k, float(np.abs(g[k].astype(np.float64) - a[k]).max()))
 
 
+def test_sphere_drop_snapshot_trilinear_deviation(sphere_drop):
+    """The trilinear boundary interpolation beside the cubic one, one
+    production-mode substep from the snapshot, both against the FP64 cubic
+    replica (the reference's sampler).  Printed per field.  The trilinear
+    mode is an approximation, not a parity mode: its boundary volumes differ
+    from the cubic ones by up to ~15 % of the map's largest volume (the
+    volume falls off cubically across a field cell).  The bars are sanity
+    bounds only: at least 95 % of the sampled particles shared, volume
+    differences within half the map's largest volume, positions within h/2
+    of the cubic mode's after the substep."""
+    sc, snap = sphere_drop
+    out = {}
+    for interp in (L.INTERP_CUBIC, L.INTERP_TRILINEAR):
+        cfg = scenes.copy_config(sc.config)
+        cfg.fp_mode = L.FP_FAST
+        cfg.boundary_interp = interp
+        sim = PBF(cfg)
+        try:
+            sim.set_state(snap["x"], snap["v"], snap["a"])
+            _set_field(sim, sc.field)
+            sim.set_launch(block=128, ctas_per_sm=0, cell_ratio=0.5)
+            sim.set_capture(True)
+            sim.run()
+            out[interp] = _gpu_fields(sim)
+        finally:
+            sim.close()
+    o64 = _oracle_from(sc, snap, 64)
+    o64.substep(1)
+    d = _oracle_fields(o64, 64)
+    o64.close()
+    cub, tri = out[L.INTERP_CUBIC], out[L.INTERP_TRILINEAR]
+    h = float(sc.config.kernel_radius)
+    vmax = float(np.max(sc.field["vol"]))
+    print("\nsphere_drop_1m snapshot, one substep: cubic and trilinear boundary sampling against FP64 cubic")
+    print("| field | cubic max / rms (of scale) | trilinear max / rms (of scale) |")
+    print("|---|---|---|")
+    for name, get in (("boundary x_b", lambda x: x["boundary"][:, :3]), ("boundary V_b", lambda x: x["boundary"][:, 3]),
+                      ("rho", lambda x: x["position"][:, 3]), ("position", lambda x: x["position"][:, :3]),
+                      ("velocity", lambda x: x["velocity"][:, :3])):
+        ref = get(d).astype(np.float64)
+        scale = max(np.abs(ref).max(), 1e-30)
+        row = []
+        for g in (cub, tri):
+            e = get(g).astype(np.float64) - ref
+            row.append((np.abs(e).max() / scale, float(np.sqrt(np.mean(np.square(e)))) / scale))
+        print("| %s | %.2e / %.2e | %.2e / %.2e |" % (name, row[0][0], row[0][1], row[1][0], row[1][1]))
+    in_c, in_t = cub["boundary"][:, 3] > 0, tri["boundary"][:, 3] > 0
+    print("particles with a boundary sample: cubic %d, trilinear %d, both %d" % (in_c.sum(), in_t.sum(), (in_c & in_t).sum()))
+    both = in_c & in_t
+    assert both.sum() >= 0.95 * max(in_c.sum(), in_t.sum())
+    dv = np.abs(cub["boundary"][both, 3].astype(np.float64) - tri["boundary"][both, 3])
+    print("boundary volume |trilinear - cubic|: max %.3e, mean %.3e (map maximum %.3e)" % (dv.max(), dv.mean(), vmax))
+    dx = np.abs(cub["position"][:, :3].astype(np.float64) - tri["position"][:, :3]).max()
+    print("position |trilinear - cubic| max: %.3e (h = %.4f)" % (dx, h))
+    assert dv.max() <= 0.5 * vmax
+    assert dx <= 0.5 * h
+
+
 # ---- 2. the dam break ---------------------------------------------------------------------------
 @pytest.fixture(scope="module")
 def dam_break():

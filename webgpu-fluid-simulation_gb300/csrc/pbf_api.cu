@@ -19,6 +19,7 @@
 #include <cuda_runtime.h>
 
 #include "../../include/pbf_gb300.h"
+#include "pbf_device.cuh"
 #include "pbf_kernels.h"
 
 using namespace pbf;
@@ -77,6 +78,8 @@ struct pbf_handle {
   unsigned cb_fb_grid = 0;  // CTAs of the cell-block fallback kernel
   DBuf<float> sdf, vol;
   DBuf<uint8_t> bflag;  // per field cell: 1 when the boundary sample can be non-zero
+  DBuf<uint32_t> bcell;  // per field cell: its packed node block, or kNoBlock (FieldBlocks)
+  DBuf<float4> bnodes;   // 16 float4 per flagged field cell
   DBuf<uint32_t> err_word;
   DBuf<float> m_f;
   DBuf<double> m_d;
@@ -447,7 +450,8 @@ int substep(pbf_handle* h, cudaEvent_t* ev) {
       ps.band<<<grid_of(h, n), h->blk, 0, st>>>(p, h->tab, h->xs[a].p, band_args(0, bsdf));
       band = 0;
     }
-    ps.boundary_band<<<band_grid, 256, 0, st>>>(p, f, h->sdf.p, h->vol.p, h->tab, h->xs[a].p, h->bdata.p, bsdf,
+    ps.boundary_band<<<band_grid, 256, 0, st>>>(p, f, h->sdf.p, h->vol.p, FieldBlocks{h->bcell.p, h->bnodes.p},
+                                                 h->tab, h->xs[a].p, h->bdata.p, bsdf,
                                                  h->band_list[band].p, h->band_count.p + band,
                                                  h->band_count.p + (1 - band), guard);
     return cudaGetLastError();
@@ -820,6 +824,8 @@ void release_all(pbf_handle* h) {
   h->sdf.release();
   h->vol.release();
   h->bflag.release();
+  h->bcell.release();
+  h->bnodes.release();
   h->scenes_dev.release();
   h->slot_scene.release();
   h->band_list[0].release();
@@ -889,6 +895,28 @@ void boundary_flags(const uint32_t res[3], const float* sdf, const float* vol, f
       }
 }
 
+
+// Packed node blocks (FieldBlocks) of one map's flagged cells, appended to
+// blocks; cell[] gets each cell's block index (counted from the blocks
+// already present) or kNoBlock.
+void pack_field_blocks(const uint32_t res[3], const float* sdf, const float* vol, const std::vector<uint8_t>& flag,
+                       std::vector<uint32_t>& cell, std::vector<float>& blocks) {
+  FieldParams f{};
+  for (int a = 0; a < 3; ++a) f.res[a] = (int)res[a];
+  const size_t nx = res[0], ny = res[1], nz = res[2];
+  cell.assign(nx * ny * nz, kNoBlock);
+  for (size_t k = 0; k < nz; ++k)
+    for (size_t j = 0; j < ny; ++j)
+      for (size_t i = 0; i < nx; ++i) {
+        const size_t c = (k * ny + j) * nx + i;
+        if (!flag[c]) continue;
+        uint32_t idx[32];
+        cell_nodes(f, (int)i, (int)j, (int)k, false, idx);
+        cell[c] = (uint32_t)(blocks.size() / 64);
+        for (int q = 0; q < 32; ++q) blocks.push_back(sdf[idx[q]]);
+        for (int q = 0; q < 32; ++q) blocks.push_back(vol[idx[q]]);
+      }
+}
 
 // (Re)allocates the cell arrays for h->gp.cells cells.
 cudaError_t alloc_cells(pbf_handle* h) {
@@ -1412,6 +1440,7 @@ int pbf_set_boundary_field(pbf_handle* h, const uint32_t res[3], const float ori
   }
   size_t len = pbf_field_length(res);
   if (nodes != len) return fail(h, PBF_EFORMAT, "Invalid Boundary Model File! (%zu values, expected %zu)", nodes, len);
+  if (len > 0xffffffffull) return fail(h, PBF_ECAPACITY, "field of %zu nodes (32-bit node indices)", len);
   invalidate_graph(h);
   h->sdf.release();
   h->vol.release();
@@ -1423,9 +1452,20 @@ int pbf_set_boundary_field(pbf_handle* h, const uint32_t res[3], const float ori
   {
     std::vector<uint8_t> flag;
     boundary_flags(res, sdf, volume, h->cfg.kernel_radius, flag);
+    std::vector<uint32_t> cell;
+    std::vector<float> blocks;
+    pack_field_blocks(res, sdf, volume, flag, cell, blocks);
     h->bflag.release();
+    h->bcell.release();
+    h->bnodes.release();
     CU(h, h->bflag.alloc(flag.size()));
+    CU(h, h->bcell.alloc(cell.size()));
+    CU(h, h->bnodes.alloc(blocks.size() / 4));
     CU(h, cudaMemcpyAsync(h->bflag.p, flag.data(), flag.size(), cudaMemcpyHostToDevice, h->stream));
+    CU(h, cudaMemcpyAsync(h->bcell.p, cell.data(), cell.size() * sizeof(uint32_t), cudaMemcpyHostToDevice, h->stream));
+    if (!blocks.empty())
+      CU(h, cudaMemcpyAsync(h->bnodes.p, blocks.data(), blocks.size() * sizeof(float), cudaMemcpyHostToDevice,
+                            h->stream));
     CU(h, cudaStreamSynchronize(h->stream));
   }
   CU(h, cudaStreamSynchronize(h->stream));
@@ -2171,8 +2211,9 @@ int pbf_batch_create(const pbf_config* shared, const pbf_scene* scenes, uint32_t
   h->gp.cells = (uint32_t)cells;
   if (alloc_cells(h) != cudaSuccess) return bail(PBF_ECUDA, "cells");
   if (any_field) {
-    std::vector<float> sdf(nodes), vol(nodes);
+    std::vector<float> sdf(nodes), vol(nodes), blocks;
     std::vector<uint8_t> flag(flags), f1;
+    std::vector<uint32_t> cell(flags, kNoBlock), c1;
     for (uint32_t s = 0; s < count; ++s) {
       const pbf_scene& sc = scenes[s];
       const SceneDesc& sd = h->scenes[s];
@@ -2182,12 +2223,20 @@ int pbf_batch_create(const pbf_config* shared, const pbf_scene* scenes, uint32_t
       std::memcpy(vol.data() + sd.field.node_off, sc.volume, len * sizeof(float));
       boundary_flags(sc.field_res, sc.sdf, sc.volume, c.kernel_radius, f1);
       std::memcpy(flag.data() + sd.field.flag_off, f1.data(), f1.size());
+      pack_field_blocks(sc.field_res, sc.sdf, sc.volume, f1, c1, blocks);
+      std::memcpy(cell.data() + sd.field.flag_off, c1.data(), c1.size() * sizeof(uint32_t));
     }
-    if (h->sdf.alloc(nodes) != cudaSuccess || h->vol.alloc(nodes) != cudaSuccess || h->bflag.alloc(flags) != cudaSuccess)
+    if (blocks.size() / 64 >= (size_t)kNoBlock) return bail(PBF_ECAPACITY, "fields");
+    if (h->sdf.alloc(nodes) != cudaSuccess || h->vol.alloc(nodes) != cudaSuccess ||
+        h->bflag.alloc(flags) != cudaSuccess || h->bcell.alloc(flags) != cudaSuccess ||
+        h->bnodes.alloc(blocks.size() / 4) != cudaSuccess)
       return bail(PBF_ECUDA, "fields");
     if (cudaMemcpy(h->sdf.p, sdf.data(), nodes * sizeof(float), cudaMemcpyHostToDevice) != cudaSuccess ||
         cudaMemcpy(h->vol.p, vol.data(), nodes * sizeof(float), cudaMemcpyHostToDevice) != cudaSuccess ||
-        cudaMemcpy(h->bflag.p, flag.data(), flags, cudaMemcpyHostToDevice) != cudaSuccess)
+        cudaMemcpy(h->bflag.p, flag.data(), flags, cudaMemcpyHostToDevice) != cudaSuccess ||
+        cudaMemcpy(h->bcell.p, cell.data(), flags * sizeof(uint32_t), cudaMemcpyHostToDevice) != cudaSuccess ||
+        (!blocks.empty() && cudaMemcpy(h->bnodes.p, blocks.data(), blocks.size() * sizeof(float),
+                                       cudaMemcpyHostToDevice) != cudaSuccess))
       return bail(PBF_ECUDA, "fields");
     h->fp = FieldParams{};
     h->fp.loaded = 1;

@@ -201,7 +201,8 @@ __device__ __forceinline__ CellLoc field_locate(const FieldParams& f, f3 x) {
   return CellLoc{c[0], c[1], c[2], mk(s[0], s[1], s[2])};
 }
 
-__device__ __forceinline__ void cell_nodes(const FieldParams& f, int i, int j, int k, bool quirk, uint32_t* idx) {
+__host__ __device__ __forceinline__ void cell_nodes(const FieldParams& f, int i, int j, int k, bool quirk,
+                                                    uint32_t* idx) {
   const uint32_t nx = f.res[0], ny = f.res[1], nz = f.res[2];
   const uint32_t nc = (nx + 1) * (ny + 1) * (nz + 1);
   const uint32_t nex = 2 * nx * (ny + 1) * (nz + 1);
@@ -232,6 +233,40 @@ __device__ __forceinline__ void cell_nodes(const FieldParams& f, int i, int j, i
     idx[27] = idx[26];
     idx[29] = idx[28];
     idx[31] = idx[30];
+  }
+}
+
+// The node quirk of cell_nodes applied to the 32 volume values of a packed
+// block (stored in the plain node order): the same values the quirked node
+// indices would read.
+__device__ __forceinline__ void volume_quirk_values(float* v) {
+  v[11] = v[10];
+  v[15] = v[14];
+  v[25] = v[24];
+  v[27] = v[26];
+  v[29] = v[28];
+  v[31] = v[30];
+}
+
+// Packed block of the field cell (i,j,k), or null when the map has no
+// blocks or the cell has none (its nodes are then gathered).
+__device__ __forceinline__ const float4* field_block(const FieldParams& f, const FieldBlocks& fb, int i, int j,
+                                                     int k) {
+  if (!fb.cell) return nullptr;
+  const uint32_t c = __ldg(fb.cell + f.flag_off + ((size_t)k * f.res[1] + j) * f.res[0] + i);
+  return c == kNoBlock ? nullptr : fb.nodes + (size_t)c * 16u;
+}
+
+// kN node values (a multiple of 4) from a packed block.
+template <int kN>
+__device__ __forceinline__ void block_values(const float4* blk, float* val) {
+#pragma unroll
+  for (int q = 0; q < kN / 4; ++q) {
+    const float4 v = __ldg(blk + q);
+    val[4 * q] = v.x;
+    val[4 * q + 1] = v.y;
+    val[4 * q + 2] = v.z;
+    val[4 * q + 3] = v.w;
   }
 }
 
@@ -336,18 +371,56 @@ __device__ __forceinline__ float boundary_distance(const FieldParams& f, const f
   return sum32(N, val);
 }
 
-// BoundaryVolume pass for one particle (src/simulator/PBF/shader/boundaryVolume.ts:31-55):
-// returns (x_b, V_b) or zero when the particle is outside the band 0 < d < h;
-// dist_out (optional) receives the interpolated SDF (boundary_distance's value).
-__device__ __forceinline__ float4 boundary_sample(const SimParams& p, const FieldParams& f, const float* __restrict__ sdf,
-                                                  const float* __restrict__ vol, f3 x, float* dist_out = nullptr) {
-  CellLoc L = field_locate(f, x);
-  uint32_t idx[32];
-  cell_nodes(f, L.i, L.j, L.k, false, idx);
+// Node values of one field cell for the boundary sample: gathered from the
+// node arrays by the cell's node indices, or read from its packed block.
+struct NodeGather {
+  const FieldParams& f;
+  const float* __restrict__ sdf;
+  const float* __restrict__ vol;
+  int i, j, k;
+  __device__ __forceinline__ void sdf_values(float* v, int n) const {
+    uint32_t idx[32];
+    cell_nodes(f, i, j, k, false, idx);
+#pragma unroll
+    for (int q = 0; q < n; ++q) v[q] = __ldg(sdf + idx[q]);
+  }
+  __device__ __forceinline__ void vol_values(float* v, int n) const {
+    uint32_t idx[32];
+    cell_nodes(f, i, j, k, f.quirk != 0, idx);  // the quirk touches edge nodes only (n == 8 reads corners)
+#pragma unroll
+    for (int q = 0; q < n; ++q) v[q] = __ldg(vol + idx[q]);
+  }
+};
+struct NodeBlock {
+  const float4* blk;
+  int quirk;
+  __device__ __forceinline__ void sdf_values(float* v, int n) const {
+    if (n == 8) block_values<8>(blk, v);
+    else block_values<32>(blk, v);
+  }
+  __device__ __forceinline__ void vol_values(float* v, int n) const {
+    if (n == 8) {
+      block_values<8>(blk + 8, v);
+    } else {
+      block_values<32>(blk + 8, v);
+      if (quirk) volume_quirk_values(v);
+    }
+  }
+};
+
+// BoundaryVolume pass for one particle (src/simulator/PBF/shader/boundaryVolume.ts:31-55)
+// from the cell located at x: returns (x_b, V_b) or zero when the particle is
+// outside the band 0 < d < h; dist_out (optional) receives the interpolated
+// SDF (boundary_distance's value).  Src supplies the node values.
+template <class Src>
+__device__ __forceinline__ float4 boundary_sample_from(const SimParams& p, const FieldParams& f, const CellLoc& L,
+                                                       const Src& src, f3 x, float* dist_out) {
   float dist, volume;
   f3 grad;
   if (f.trilinear) {
     float tx = (L.s.x + 1.0f) * 0.5f, ty = (L.s.y + 1.0f) * 0.5f, tz = (L.s.z + 1.0f) * 0.5f;
+    float c8[8];
+    src.sdf_values(c8, 8);
     dist = 0.0f;
     f3 g = mk(0.f, 0.f, 0.f);
 #pragma unroll
@@ -355,7 +428,7 @@ __device__ __forceinline__ float4 boundary_sample(const SimParams& p, const Fiel
       int a = q & 1, b = (q >> 1) & 1, e = (q >> 2) & 1;
       float wx = a ? tx : 1.0f - tx, wy = b ? ty : 1.0f - ty, wz = e ? tz : 1.0f - tz;
       float sx = a ? 1.0f : -1.0f, sy = b ? 1.0f : -1.0f, sz = e ? 1.0f : -1.0f;
-      float v = __ldg(sdf + idx[q]);
+      float v = c8[q];
       dist = dist + wx * wy * wz * v;
       g = g + mk(sx * wy * wz * v, wx * sy * wz * v, wx * wy * sz * v);
     }
@@ -363,12 +436,13 @@ __device__ __forceinline__ float4 boundary_sample(const SimParams& p, const Fiel
     if (dist_out) *dist_out = dist;
     float4 out = make_float4(0.f, 0.f, 0.f, 0.f);
     if (dist > 0.0f && dist < p.h && len3(grad) > 1e-9f) {
+      src.vol_values(c8, 8);
       volume = 0.0f;
 #pragma unroll
       for (int q = 0; q < 8; ++q) {
         int a = q & 1, b = (q >> 1) & 1, e = (q >> 2) & 1;
         float wx = a ? tx : 1.0f - tx, wy = b ? ty : 1.0f - ty, wz = e ? tz : 1.0f - tz;
-        volume = volume + wx * wy * wz * __ldg(vol + idx[q]);
+        volume = volume + wx * wy * wz * c8[q];
       }
       if (volume > 0.0f) {
         f3 n = divs(grad, len3(grad));
@@ -382,17 +456,14 @@ __device__ __forceinline__ float4 boundary_sample(const SimParams& p, const Fiel
   f3 dN[32];
   float val[32];
   shape32(L.s, N, dN);
-#pragma unroll
-  for (int q = 0; q < 32; ++q) val[q] = __ldg(sdf + idx[q]);
+  src.sdf_values(val, 32);
   dist = sum32(N, val);
   f3 g = sum32v(dN, val);
   grad = mk(f.gscale[0] * g.x, f.gscale[1] * g.y, f.gscale[2] * g.z);
   if (dist_out) *dist_out = dist;
   float4 out = make_float4(0.f, 0.f, 0.f, 0.f);
   if (dist > 0.0f && dist < p.h && len3(grad) > 1e-9f) {
-    if (f.quirk) cell_nodes(f, L.i, L.j, L.k, true, idx);
-#pragma unroll
-    for (int q = 0; q < 32; ++q) val[q] = __ldg(vol + idx[q]);
+    src.vol_values(val, 32);
     volume = sum32(N, val);
     if (volume > 0.0f) {
       f3 n = divs(grad, len3(grad));
@@ -401,6 +472,30 @@ __device__ __forceinline__ float4 boundary_sample(const SimParams& p, const Fiel
     }
   }
   return out;
+}
+
+// The boundary sample with the nodes gathered from the node arrays.
+__device__ __forceinline__ float4 boundary_sample(const SimParams& p, const FieldParams& f, const float* __restrict__ sdf,
+                                                  const float* __restrict__ vol, f3 x, float* dist_out = nullptr) {
+  const CellLoc L = field_locate(f, x);
+  return boundary_sample_from(p, f, L, NodeGather{f, sdf, vol, L.i, L.j, L.k}, x, dist_out);
+}
+static __device__ __noinline__ float4 boundary_sample_gather(const SimParams& p, const FieldParams& f,
+                                                             const float* __restrict__ sdf,
+                                                             const float* __restrict__ vol, f3 x, float* dist_out) {
+  return boundary_sample(p, f, sdf, vol, x, dist_out);
+}
+
+// The boundary sample from the cell's packed block (FieldBlocks): two
+// 128-byte lines per field instead of 32 scattered nodes.  A cell without a
+// block (not flagged; the band never lists one) takes the gather path.
+__device__ __forceinline__ float4 boundary_sample_packed(const SimParams& p, const FieldParams& f,
+                                                         const FieldBlocks& fb, const float* __restrict__ sdf,
+                                                         const float* __restrict__ vol, f3 x, float* dist_out) {
+  const CellLoc L = field_locate(f, x);
+  const float4* blk = field_block(f, fb, L.i, L.j, L.k);
+  if (!blk) return boundary_sample_gather(p, f, sdf, vol, x, dist_out);
+  return boundary_sample_from(p, f, L, NodeBlock{blk, f.quirk}, x, dist_out);
 }
 
 }  // namespace pbf

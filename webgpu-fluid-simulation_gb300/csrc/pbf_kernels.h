@@ -24,8 +24,8 @@ struct PassSet {
   void (*nbr_build_warp)(SimParams, GridParams, SceneTab, const float4*, const uint32_t*, uint32_t, uint32_t*,
                          uint32_t*, uint32_t*, uint32_t*);  // warp-cooperative per cell
   void (*band)(SimParams, SceneTab, const float4*, BandArgs);
-  void (*boundary_band)(SimParams, FieldParams, const float*, const float*, SceneTab, const float4*, float4*, float*,
-                        const uint32_t*, const uint32_t*, uint32_t*, const int*);
+  void (*boundary_band)(SimParams, FieldParams, const float*, const float*, FieldBlocks, SceneTab, const float4*,
+                        float4*, float*, const uint32_t*, const uint32_t*, uint32_t*, const int*);
   void (*lambda)(SimParams, int, const float4*, const float4*, uint32_t, const uint32_t*, const uint32_t*, float4*,
                  SolverAux);
   void (*lambda_feat)(SimParams, int, const float4*, const float4*, uint32_t, const uint32_t*, const uint32_t*,

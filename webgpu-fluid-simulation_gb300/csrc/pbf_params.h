@@ -76,6 +76,19 @@ struct BandArgs {
   uint32_t* count;
 };
 
+// Packed node blocks of a volume map: for each field cell whose boundary
+// sample can be non-zero (the band flag), its 32 SDF node values and then
+// its 32 volume node values, in the node order of the 32-node cell, 16
+// float4 (256 B) contiguous.  cell[] maps a field cell (the flag's index,
+// concatenated for batches) to its block, or to kNoBlock.  The volume
+// values are stored without the reference's node quirk; the sampler applies
+// it to the loaded values.
+struct FieldBlocks {
+  const uint32_t* cell;
+  const float4* nodes;
+};
+constexpr uint32_t kNoBlock = 0xffffffffu;
+
 // Per-slot scene lookup of a batch; scene == nullptr for a single scene
 // (every parameter then comes by value).
 struct SceneTab {

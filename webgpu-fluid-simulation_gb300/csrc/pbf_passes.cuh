@@ -668,9 +668,11 @@ __global__ void __launch_bounds__(256) k_band(SimParams p, SceneTab tab, const f
 // BoundaryVolume for the band's slots only: a grid of resident CTAs walks the
 // list (its length is known on the device only).  Also clears the count of
 // the other band list, which delta-p fills next.
+// Node values come from the packed blocks (FieldBlocks): every listed slot's
+// field cell is flagged, so it has one.
 template <bool kBatch>
 __global__ void __launch_bounds__(256, 2) k_boundary_band(SimParams p, FieldParams f0, const float* __restrict__ sdf0,
-                                                          const float* __restrict__ vol0, SceneTab tab,
+                                                          const float* __restrict__ vol0, FieldBlocks fb, SceneTab tab,
                                                           const float4* __restrict__ xs, float4* __restrict__ bdata,
                                                           float* __restrict__ bsdf, const uint32_t* __restrict__ list,
                                                           const uint32_t* count, uint32_t* other_count,
@@ -686,7 +688,7 @@ __global__ void __launch_bounds__(256, 2) k_boundary_band(SimParams p, FieldPara
     const float* vol = vol0 + f.node_off;
     const f3 xi = xyz(xs[t]);
     float dist;
-    bdata[t] = boundary_sample(p, f, sdf, vol, xi, &dist);
+    bdata[t] = boundary_sample_packed(p, f, fb, sdf, vol, xi, &dist);
     if (bsdf) bsdf[t] = dist;
   }
 }

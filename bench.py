@@ -428,8 +428,17 @@ def gpu_arm(args, dist):
         mlp_fit_normalization(model, feat, tgt)
         t0 = time.perf_counter()
         loss = mlp_train(model, feat, tgt, epochs=10, batch=8192, lr=3e-3, seed=7)
+        t_train = time.perf_counter() - t0
+        # the same training with the warp-level mma.sync gradient kernel, on a
+        # throwaway copy of the model (not used below): the two kernels' times
+        side = mlp_init(7)
+        mlp_fit_normalization(side, feat, tgt)
+        t0 = time.perf_counter()
+        loss_ms = mlp_train(side, feat, tgt, epochs=10, batch=8192, lr=3e-3, seed=7, kernel=L.MLP_TRAIN_MMA_SYNC)
+        t_ms = time.perf_counter() - t0
         train_info = {"rows": int(len(tgt)), "epochs": 10, "batch": 8192, "final_mse_normalised": loss,
-                      "seconds": time.perf_counter() - t0,
+                      "seconds": t_train, "gradient_kernel": "tcgen05",
+                      "mma_sync_gradient_kernel": {"seconds": t_ms, "final_mse_normalised": loss_ms},
                       "traced": "frames %d-%d of a second instance of the scene (jitter seed %d; the benchmarked "
                                 "instance uses seed %d)" % (trace_lo, trace_hi, TRAIN_SEED, BENCH_SEED),
                       "plain_mean_compression_while_tracing": {"max": plain_err_max, "avg": plain_err_avg}}

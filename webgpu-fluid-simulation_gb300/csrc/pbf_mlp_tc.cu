@@ -383,6 +383,7 @@ struct GrSmem {
   alignas(128) uint8_t b3[16 * 64 * 2];     // w3 hi / lo in N rows 0, 1
   alignas(128) uint8_t b3b[16 * 16 * 2];    // b3 hi / lo in N row 0, K rows 8, 9
   alignas(128) uint8_t b2t[64 * 64 * 2];    // W2 (N = in, K = out): B of dH1 = dZ2 W2^T
+  float w3[64];                             // w3 in FP32 (dZ2's factor)
   alignas(8) uint64_t mbar;
   uint32_t tmem;
   uint32_t failed;
@@ -454,14 +455,19 @@ __global__ void __launch_bounds__(128, 1) k_mlp_grad_tc(const float* __restrict_
   }
   // constant parts of the gradient operands: the ones rows and the zeros
   // (the data rows are rewritten for every tile)
-  for (uint32_t q = tid; q < 128u * 128u; q += 128u) {
-    const uint32_t m = q / 128u, k = q % 128u;
-    const uint32_t off = canon(m, k, 128);
-    *reinterpret_cast<__nv_bfloat16*>(sm.tH1 + off) = __float2bfloat16_rn(m == 64u ? 1.0f : 0.0f);
-    *reinterpret_cast<__nv_bfloat16*>(sm.tH2 + off) = __float2bfloat16_rn(m == 64u ? 1.0f : 0.0f);
-    *reinterpret_cast<__nv_bfloat16*>(sm.tX + off) = __float2bfloat16_rn(m == 8u ? 1.0f : 0.0f);
+  // 16 bytes at a time: the 16-byte unit at byte o of a canonical tile
+  // holds elements k..k+7 of row m = ((o / 2048) * 8 + (o / 16) % 8)
+  // (kk = 128: 16 core matrices of 128 B per 8-row group)
+  const uint32_t ones2 = pack_bf16(1.0f, 1.0f);
+  for (uint32_t o = 16u * tid; o < 128u * 128u * 2u; o += 16u * 128u) {
+    const uint32_t m = (o / 2048u) * 8u + (o / 16u) % 8u;
+    const uint32_t h = m == 64u ? ones2 : 0u, xv = m == 8u ? ones2 : 0u;
+    st_shared_v4(smem_u32(sm.tH1 + o), h, h, h, h);
+    st_shared_v4(smem_u32(sm.tH2 + o), h, h, h, h);
+    st_shared_v4(smem_u32(sm.tX + o), xv, xv, xv, xv);
   }
-  for (uint32_t q = tid; q < 16u * 128u; q += 128u) *reinterpret_cast<__nv_bfloat16*>(sm.tDY + 2u * q) = z16;
+  for (uint32_t o = 16u * tid; o < 16u * 128u * 2u; o += 16u * 128u) st_shared_v4(smem_u32(sm.tDY + o), 0u, 0u, 0u, 0u);
+  if (tid < 64u) sm.w3[tid] = P[OFF_W3 + tid];
   st_shared_v4(smem_u32(sm.x1 + canon(row, 8, 16)), pack_bf16(1.0f, 1.0f), 0u, 0u, 0u);
   const uint32_t mbar = smem_u32(&sm.mbar);
   if (tid == 0) {
@@ -570,7 +576,7 @@ __global__ void __launch_bounds__(128, 1) k_mlp_grad_tc(const float* __restrict_
         const int j = 8 * kb;
         float d[8];
 #pragma unroll
-        for (int e = 0; e < 8; ++e) d[e] = dy * P[OFF_W3 + 32 * half + j + e] * dsilu_f(v[j + e]);
+        for (int e = 0; e < 8; ++e) d[e] = dy * sm.w3[32 * half + j + e] * dsilu_f(v[j + e]);
         st_shared_v4(hA + canon(row, 32 * half + j, 64), pack_bf16(d[0], d[1]), pack_bf16(d[2], d[3]),
                      pack_bf16(d[4], d[5]), pack_bf16(d[6], d[7]));
 #pragma unroll

@@ -111,7 +111,7 @@ struct pbf_handle {
   float lagged_fraction = 0.0f;
   pbf_mlp model;
   DBuf<float> mlp_params, lam_sum, lam_prev, bsdf, fb_mean;
-  DBuf<float4> feat, xs_save, pos_save;
+  DBuf<float4> feat, xs_save;
   DBuf<SolveStats> stats;
   DBuf<int> fb_flag;
   DBuf<uint32_t> fb_count;
@@ -460,7 +460,6 @@ int substep(pbf_handle* h, cudaEvent_t* ev) {
   // scan).  The learned start samples the boundary at x*_0 first and sums its
   // features in the same traversal.
   if (h->learned) {
-    CU(h, cudaMemcpyAsync(h->xs_save.p, h->xs[0].p, (size_t)n * sizeof(float4), cudaMemcpyDeviceToDevice, st));
     if (f.loaded) CU(h, sample_boundary(0, h->bsdf.p));
     SolverAux al{};
     al.pos = h->pos[cc].p;
@@ -590,15 +589,17 @@ int substep(pbf_handle* h, cudaEvent_t* ev) {
   if (h->learned) {
     // learned start: (boundary and features at x*_0 from the neighbour
     // build) -> network -> (x*_0, lambda_hat) -> one projection ->
-    // learned_iters plain iterations -> device-side fallback test
+    // learned_iters plain iterations -> device-side fallback test.  The
+    // network writes (x*_0, lambda_hat) into xs_save, which the projection
+    // reads as its (x*, lambda) records and the fallback keeps as x*_0.
     {
       KScope ks(h, K_MLP);
       if (h->mlp_kernel == PBF_MLP_KERNEL_TCGEN05)
         CU(h, launch_mlp_infer_tc(h->mlp_params.p, h->model, (const float*)h->feat.p, n, nullptr, h->lam_sum.p, st,
-                                  h->xs[0].p, h->xl.p, h->err_word.p));
+                                  h->xs[0].p, h->xs_save.p, h->err_word.p));
       else
         CU(h, launch_mlp_infer(h->mlp_params.p, h->model, (const float*)h->feat.p, n, nullptr, h->lam_sum.p, st,
-                               h->xs[0].p, h->xl.p));
+                               h->xs[0].p, h->xs_save.p));
     }
     {
       KScope ks(h, K_DELTAP);
@@ -608,9 +609,10 @@ int substep(pbf_handle* h, cudaEvent_t* ev) {
         band = 1 - band;
       }
       if (cb)
-        cs.deltap<<<cbg, 128, cb_smem(h, 1), st>>>(p, A, ad, f.loaded, h->xl.p, h->bdata.p, h->xs[1].p, nullptr);
+        cs.deltap<<<cbg, 128, cb_smem(h, 1), st>>>(p, A, ad, f.loaded, h->xs_save.p, h->bdata.p, h->xs[1].p,
+                                                   nullptr);
       else
-        ps.deltap<<<grid_of(h, n), h->blk, 0, st>>>(p, ad, f.loaded, h->xl.p, h->bdata.p, ms, h->nbr_count.p,
+        ps.deltap<<<grid_of(h, n), h->blk, 0, st>>>(p, ad, f.loaded, h->xs_save.p, h->bdata.p, ms, h->nbr_count.p,
                                                      h->nbr_list.p, h->xs[1].p, nullptr);
     }
     CU(h, cudaGetLastError());
@@ -631,8 +633,6 @@ int substep(pbf_handle* h, cudaEvent_t* ev) {
   // AttributeUpdate.  Its density error (mean compression) is the learned
   // start's fallback test; while tracing it records the plain solve's error.
   const bool rec = !h->learned && h->trace_cap > 0 && h->stats.p && h->trace_err.p;
-  if (h->learned) CU(h, cudaMemcpyAsync(h->pos_save.p, h->pos[cc].p, (size_t)n * sizeof(float4),
-                                        cudaMemcpyDeviceToDevice, st));
   {
     KScope ks(h, K_DENSITY);
     SolverAux ad{};
@@ -658,7 +658,8 @@ int substep(pbf_handle* h, cudaEvent_t* ev) {
     fa.sdf = h->sdf.p;
     fa.vol = h->vol.p;
     fa.bflag = h->bflag.p;
-    fa.pos_save = h->pos_save.p;
+    fa.pos_old = h->pos[c].p;
+    fa.perm = h->perm.p;
     fa.xs_save = h->xs_save.p;
     fa.pos = h->pos[cc].p;
     fa.vel = h->vel.p;
@@ -838,7 +839,6 @@ void release_all(pbf_handle* h) {
   h->fb_mean.release();
   h->feat.release();
   h->xs_save.release();
-  h->pos_save.release();
   h->stats.release();
   h->fb_flag.release();
   h->fb_count.release();
@@ -1773,7 +1773,6 @@ int pbf_set_learned(pbf_handle* h, const pbf_mlp* model, uint32_t iterations, fl
   if (!h->mlp_params.p) {
     CU(h, h->mlp_params.alloc(PBF_MLP_PARAMS));
     CU(h, h->xs_save.alloc(cap));
-    CU(h, h->pos_save.alloc(cap));
     if (h->stats.n < 2) {
       h->stats.release();
       CU(h, h->stats.alloc(2));

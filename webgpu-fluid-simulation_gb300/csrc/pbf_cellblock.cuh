@@ -589,8 +589,9 @@ __global__ void __launch_bounds__(256) k_cb_fallback_solve(FallbackArgs F, CbArg
   const uint32_t n = p.n, stride = gridDim.x * blockDim.x, t0 = blockIdx.x * blockDim.x + threadIdx.x;
   constexpr bool kT0 = kMemb == kMemTest;  // field 0 of the walk is x*_0
   for (uint32_t t = t0; t < n; t += stride) {
-    F.pos[t] = __ldcg(F.pos_save + t);
-    F.xs0[t] = __ldcg(F.xs_save + t);
+    F.pos[t] = __ldcg(F.pos_old + __ldg(F.perm + t));
+    const float4 x0 = __ldcg(F.xs_save + t);
+    F.xs0[t] = make_float4(x0.x, x0.y, x0.z, 0.0f);
   }
   grid.sync();
   int b = 0;

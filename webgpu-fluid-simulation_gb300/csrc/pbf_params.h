@@ -149,8 +149,9 @@ struct FallbackArgs {
   const float* sdf;
   const float* vol;
   const uint8_t* bflag;
-  const float4* pos_save;   // x at the start of the substep
-  const float4* xs_save;    // x*_0
+  const float4* pos_old;    // the state before this substep's reorder: x at the start of the
+  const uint32_t* perm;     // substep is pos_old[perm[t]] (the reorder's own gather)
+  const float4* xs_save;    // (x*_0, lambda_hat) as the network pass wrote it
   float4* pos;
   float4* vel;
   float4* xs0;

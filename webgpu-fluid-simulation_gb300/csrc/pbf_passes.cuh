@@ -1076,8 +1076,9 @@ __global__ void __launch_bounds__(256) k_fallback_solve(FallbackArgs A) {
   cooperative_groups::grid_group grid = cooperative_groups::this_grid();
   const uint32_t n = A.p.n, stride = gridDim.x * blockDim.x, t0 = blockIdx.x * blockDim.x + threadIdx.x;
   for (uint32_t t = t0; t < n; t += stride) {
-    A.pos[t] = __ldcg(A.pos_save + t);
-    A.xs0[t] = __ldcg(A.xs_save + t);
+    A.pos[t] = __ldcg(A.pos_old + __ldg(A.perm + t));
+    const float4 x0 = __ldcg(A.xs_save + t);
+    A.xs0[t] = make_float4(x0.x, x0.y, x0.z, 0.0f);
   }
   grid.sync();
   int a = 0;

@@ -70,12 +70,21 @@ struct Pair {
   f3 d;
   float r2, rl, ir;
 };
+// 1 / sqrt(x) by the hardware approximation (rsqrt.approx.ftz.f32, one MUFU
+// instruction): the fast mode's pair distance.  A squared distance below the
+// normal range (|d| < 1e-19, only the pair of a particle with itself in
+// practice, where r^2 = 0) gives +inf; make_pair_of zeroes r^2 = 0 itself.
+__device__ __forceinline__ float frsqrt_fast(float x) {
+  float y;
+  asm("rsqrt.approx.ftz.f32 %0, %1;" : "=f"(y) : "f"(x));
+  return y;
+}
 __device__ __forceinline__ Pair make_pair_of(f3 d) {
   Pair q;
   q.d = d;
   q.r2 = dot3(d, d);
   if (kFast) {
-    q.ir = (q.r2 > 0.0f) ? rsqrtf(q.r2) : 0.0f;
+    q.ir = (q.r2 > 0.0f) ? frsqrt_fast(q.r2) : 0.0f;
     q.rl = q.r2 * q.ir;
   } else {
     q.rl = sqrtf(q.r2);

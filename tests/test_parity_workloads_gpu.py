@@ -160,6 +160,36 @@ def test_sphere_drop_snapshot_production_mode_per_field(sphere_drop):
     assert close.mean() >= 0.999
 
 
+@pytest.mark.parametrize("build", [L.BUILD_THREAD, L.BUILD_PAIR, L.BUILD_WARP, L.BUILD_CELLBLOCK_MASK,
+                                   L.BUILD_CELLBLOCK_FREE])
+def test_sphere_drop_snapshot_neighbor_counts_every_build(sphere_drop, build):
+    """Every neighbour build the autotuner can choose, at both cell heights,
+    finds the restatement's neighbour counts at the 2^20 snapshot (fast
+    mode, one substep)."""
+    sc, snap = sphere_drop
+    o32 = _oracle_from(sc, snap, 32)
+    o32.substep(1)
+    want = o32.field(L.FIELD_NEIGHBOR_COUNT).astype(np.uint32)
+    o32.close()
+    for ratio in (1.0, 0.5):
+        cfg = scenes.copy_config(sc.config)
+        cfg.fp_mode = L.FP_FAST
+        sim = PBF(cfg)
+        try:
+            sim.set_state(snap["x"], snap["v"], snap["a"])
+            _set_field(sim, sc.field)
+            sim.set_launch(block=128, ctas_per_sm=0, cell_ratio=ratio, build=build)
+            sim.set_capture(True)
+            sim.run()
+            got = sim.copy_field(L.FIELD_NEIGHBOR_COUNT)
+            flags = sim.metrics()["error_flags"]
+        finally:
+            sim.close()
+        assert flags == 0, (build, ratio, flags)
+        bad = np.flatnonzero(got != want)
+        assert bad.size == 0, (build, ratio, bad.size, bad[:5], got[bad[:5]], want[bad[:5]])
+
+
 def test_sphere_drop_snapshot_exact_mode_bitexact(sphere_drop):
     sc, snap = sphere_drop
     cfg = scenes.copy_config(sc.config)

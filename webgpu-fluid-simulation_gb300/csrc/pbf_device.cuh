@@ -92,6 +92,18 @@ __device__ __forceinline__ Pair make_pair_of(f3 d) {
   }
   return q;
 }
+// The same pair with the library's rsqrtf in fast mode (exact mode: as
+// make_pair_of): the XSPH pass runs faster with it (0.1265 against 0.1310 ms
+// at 2^20), the other passes with frsqrt_fast.
+__device__ __forceinline__ Pair make_pair_of_lib(f3 d) {
+  if (!kFast) return make_pair_of(d);
+  Pair q;
+  q.d = d;
+  q.r2 = dot3(d, d);
+  q.ir = (q.r2 > 0.0f) ? rsqrtf(q.r2) : 0.0f;
+  q.rl = q.r2 * q.ir;
+  return q;
+}
 __device__ __forceinline__ float poly6_p(const SimParams& p, const Pair& q) {
   if (kFast) {
     float t = p.h2 - q.r2;

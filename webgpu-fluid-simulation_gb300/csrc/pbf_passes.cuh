@@ -861,7 +861,7 @@ struct XsphSplitSum {
     cv = mk(0.f, 0.f, 0.f);
   }
   __device__ __forceinline__ void add(const SimParams& p, float4 pj, float4 nj) {  // nj: (normal_j, |omega_j|)
-    Pair q = make_pair_of(xi - xyz(pj));
+    Pair q = make_pair_of_lib(xi - xyz(pj));
     eta = eta + (nj.w * frcp_fast(pj.w)) * spiky_p(p, q);
     const float kij = p.two_rho0 * frcp_fast(ri + pj.w);
     cv = cv + kij * (ni - xyz(nj));

@@ -190,6 +190,37 @@ def test_sphere_drop_snapshot_neighbor_counts_every_build(sphere_drop, build):
         assert bad.size == 0, (build, ratio, bad.size, bad[:5], got[bad[:5]], want[bad[:5]])
 
 
+def test_sphere_drop_snapshot_predicted_positions_bitexact(sphere_drop):
+    """The neighbour search's positions in production (fast) mode: x*
+    predicted from the snapshot equals the restatement's bit for bit (one
+    substep with no solver iteration, so the predicted field is the search's
+    x*), and so do the neighbour counts."""
+    sc, snap = sphere_drop
+    cfg = scenes.copy_config(sc.config)
+    cfg.options.iterations = 0
+    cfg.fp_mode = L.FP_FAST
+    sim = PBF(cfg)
+    try:
+        sim.set_state(snap["x"], snap["v"], snap["a"])
+        _set_field(sim, sc.field)
+        sim.set_launch(block=128, ctas_per_sm=0, cell_ratio=0.5)
+        sim.set_capture(True)
+        sim.run()
+        xs = sim.copy_field(L.FIELD_PREDICTED)
+        cnt = sim.copy_field(L.FIELD_NEIGHBOR_COUNT)
+    finally:
+        sim.close()
+    o = O.Oracle(cfg, 32)
+    o.set_state(snap["x"], snap["v"], snap["a"])
+    _set_field(o, sc.field)
+    o.substep(1)
+    want = o.field(L.FIELD_PREDICTED).astype(np.float32)
+    want_cnt = o.field(L.FIELD_NEIGHBOR_COUNT).astype(np.uint32)
+    o.close()
+    assert np.array_equal(xs[:, :3], want[:, :3]), int((xs[:, :3] != want[:, :3]).any(axis=1).sum())
+    assert np.array_equal(cnt, want_cnt)
+
+
 def test_sphere_drop_snapshot_exact_mode_bitexact(sphere_drop):
     sc, snap = sphere_drop
     cfg = scenes.copy_config(sc.config)

@@ -179,9 +179,11 @@ __device__ __forceinline__ f3 clamp_rand(const SimParams& p, f3 q) {
     r1 = hash2(q.x, q.z);
     r2 = hash2(q.x, q.y);
   }
-  f3 rv = p.jitter * mk(r0, r1, r2);
-  f3 lo = mk(p.dmin[0] + rv.x, p.dmin[1] + rv.y, p.dmin[2] + rv.z);
-  f3 hi = mk(p.dmax[0] - rv.x, p.dmax[1] - rv.y, p.dmax[2] - rv.z);
+  // each product and sum rounded once in both precision modes (no
+  // contraction into FMAs): the clamp bounds of the reference
+  f3 rv = mk(__fmul_rn(p.jitter, r0), __fmul_rn(p.jitter, r1), __fmul_rn(p.jitter, r2));
+  f3 lo = mk(__fadd_rn(p.dmin[0], rv.x), __fadd_rn(p.dmin[1], rv.y), __fadd_rn(p.dmin[2], rv.z));
+  f3 hi = mk(__fsub_rn(p.dmax[0], rv.x), __fsub_rn(p.dmax[1], rv.y), __fsub_rn(p.dmax[2], rv.z));
   return mk(fmaxf(fminf(q.x, hi.x), lo.x), fmaxf(fminf(q.y, hi.y), lo.y), fmaxf(fminf(q.z, hi.z), lo.z));
 }
 

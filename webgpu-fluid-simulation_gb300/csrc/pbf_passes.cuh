@@ -78,7 +78,15 @@ __device__ __forceinline__ void scene_domain(SimParams& p, const SceneDesc* sd) 
   }
 }
 
+// y + a x with the product and the sum each rounded once (no contraction).
+__device__ __forceinline__ f3 axpy_rn(float a, f3 x, f3 y) {
+  return mk(__fadd_rn(y.x, __fmul_rn(a, x.x)), __fadd_rn(y.y, __fmul_rn(a, x.y)), __fadd_rn(y.z, __fmul_rn(a, x.z)));
+}
+
 // predict x* (TimeIntegration), its cell key and within-cell rank (ParticleInsert).
+// x* is computed with the reference's rounding in both precision modes, so
+// the neighbour search starts from the restatement's positions bit for bit
+// and fast mode finds the reference's neighbour sets too.
 template <bool kBatch, bool kLoop>
 __global__ void __launch_bounds__(256) k_predict(SimParams p0, GridParams g0, SceneTab tab,
                                                  const float4* __restrict__ pos, const float4* __restrict__ vel,
@@ -100,8 +108,8 @@ __global__ void __launch_bounds__(256) k_predict(SimParams p0, GridParams g0, Sc
       f3 v = xyz(vel[s]);
       f3 a = xyz(acc[s]);
       f3 gv = mk(0.0f + a.x, p.gy + a.y, 0.0f + a.z);
-      f3 vp = v + p.dt * gv;
-      f3 xp = clamp_rand(p, x + p.dt * vp);
+      f3 vp = axpy_rn(p.dt, gv, v);
+      f3 xp = clamp_rand(p, axpy_rn(p.dt, vp, x));
       xs_out[s] = f4(xp, 0.0f);
       key = key_of(g, xp);
       key_out[s] = key;

@@ -3,12 +3,16 @@
 // tensor cores: tcgen05.mma with both operands in shared memory and the
 // accumulators in tensor memory (TMEM), read back with tcgen05.ld.
 //
-// A CTA of 256 threads holds the weights once and runs two independent tile
-// pipelines, one per warpgroup: warpgroup g walks its own 128-row tiles
-// (persistent grid), thread t of the warpgroup serving row t.  Each pipeline
-// has its own operand tiles, its own mbarrier, a named barrier of 128
-// threads, and TMEM columns 64 g .. 64 g + 63 (layer 2 reuses layer 1's
-// columns once they have been read), so an SM keeps eight tiles in flight:
+// One CTA of 1024 threads per SM holds the weights once and runs eight
+// independent tile pipelines, one per warpgroup: warpgroup g walks its own
+// 128-row tiles (persistent grid), thread t of the warpgroup serving row t.
+// Each pipeline has its own operand tiles, its own mbarrier, a named barrier
+// of 128 threads, and TMEM columns 64 g .. 64 g + 63 (layer 2 reuses layer
+// 1's columns once they have been read), so an SM keeps eight tiles in
+// flight.  (Four CTAs of two pipelines each, the same resources per SM,
+// entered in waves about 10 us apart, each after the previous wave's weight
+// staging; one CTA per SM stages the weights once and starts every pipeline
+// together.)  Per tile:
 //   1. each thread normalises its row's 8 features into bf16 and stores them
 //      in columns 0..7 of the pipeline's X tile (K = 16); columns 8 and 9
 //      hold the constant 1, the rest 0;
@@ -47,22 +51,23 @@ namespace {
 
 using namespace mlp;
 
-constexpr int kTcRows = 128;        // rows per tile (UMMA M)
-constexpr int kTcThreads = 256;     // two pipelines of one warpgroup each
-constexpr uint32_t kTmemCols = 128; // pipeline g: columns 64 g .. 64 g + 63
+constexpr int kTcRows = 128;                     // rows per tile (UMMA M)
+constexpr int kTcPipes = 8;                      // tile pipelines (warpgroups) per CTA
+constexpr int kTcThreads = 128 * kTcPipes;       // one CTA per SM
+constexpr uint32_t kTmemCols = 64u * kTcPipes;   // pipeline g: columns 64 g .. 64 g + 63
 constexpr uint32_t kWaitPolls = 1u << 24;
 
 struct TcSmem {
-  alignas(128) uint8_t a1[2][kTcRows * 16 * 2];  // X per pipeline: 128 x 16 bf16
-  alignas(128) uint8_t a2[2][kTcRows * 64 * 2];  // H1, then H2, per pipeline: 128 x 64 bf16
+  alignas(128) uint8_t a1[kTcPipes][kTcRows * 16 * 2];  // X per pipeline: 128 x 16 bf16
+  alignas(128) uint8_t a2[kTcPipes][kTcRows * 64 * 2];  // H1, then H2, per pipeline: 128 x 64 bf16
   alignas(128) uint8_t b1[64 * 16 * 2];          // W1'^T: 64 x 16 bf16 (N x K), b1 in K rows 8, 9
   alignas(128) uint8_t b2[64 * 64 * 2];          // W2^T: 64 x 64 bf16
   alignas(128) uint8_t b2b[64 * 16 * 2];         // b2 in K rows 8, 9 (against X's ones): 64 x 16
   alignas(128) uint8_t b3[16 * 64 * 2];          // W3'^T: 16 x 64, w3 hi / lo in N rows 0, 1
   alignas(128) uint8_t b3b[16 * 16 * 2];         // b3 hi / lo in N row 0, K rows 8, 9
-  alignas(8) uint64_t mbar[2];
+  alignas(8) uint64_t mbar[kTcPipes];
   uint32_t tmem;
-  uint32_t failed[2];  // per pipeline: a completion wait gave up
+  uint32_t failed[kTcPipes];  // per pipeline: a completion wait gave up
 };
 
 // Byte offset of element (row, k) in a K-major canonical tile with kk K elements.
@@ -158,17 +163,18 @@ __device__ __forceinline__ void st_shared_v4(uint32_t addr, uint32_t a, uint32_t
   asm volatile("st.shared.v4.b32 [%0], {%1, %2, %3, %4};" ::"r"(addr), "r"(a), "r"(b), "r"(c), "r"(d) : "memory");
 }
 
-// Barrier of one pipeline's 128 threads (named barriers 1 and 2).
+// Barrier of one pipeline's 128 threads (named barriers 1 .. kTcPipes).
 __device__ __forceinline__ void pipe_sync(uint32_t wg) {
   asm volatile("bar.sync %0, 128;" ::"r"(1u + wg) : "memory");
 }
 
-__global__ void __launch_bounds__(kTcThreads, 4) k_mlp_infer_tc(const float* __restrict__ P, Norm nm,
+__global__ void __launch_bounds__(kTcThreads, 1) k_mlp_infer_tc(const float* __restrict__ P, Norm nm,
                                                             const float* __restrict__ feat, uint32_t rows,
                                                             float* __restrict__ lambda, float* __restrict__ lam_sum,
                                                             const float4* __restrict__ xs, float4* __restrict__ xl,
                                                             uint32_t* err) {
-  __shared__ TcSmem sm;
+  extern __shared__ __align__(128) uint8_t tc_raw[];
+  TcSmem& sm = *reinterpret_cast<TcSmem*>(tc_raw);
   const uint32_t tid = threadIdx.x, warp = tid >> 5, row = tid & 127u, wg = tid >> 7;
   // weights into the canonical layouts; X's constant columns (8, 9: one) set once
   const __nv_bfloat16 z16 = __float2bfloat16_rn(0.0f);
@@ -227,7 +233,7 @@ __global__ void __launch_bounds__(kTcThreads, 4) k_mlp_infer_tc(const float* __r
   const uint32_t a2 = smem_u32(sm.a2[wg]), b2 = smem_u32(sm.b2), b3 = smem_u32(sm.b3);
   uint32_t phase = 0;
   const uint32_t tiles = (rows + kTcRows - 1) / kTcRows;
-  const uint32_t first = 2u * blockIdx.x + wg, step = 2u * gridDim.x;
+  const uint32_t first = (uint32_t)kTcPipes * blockIdx.x + wg, step = (uint32_t)kTcPipes * gridDim.x;
   // the next tile's feature row (and x* when the output is packed), loaded
   // one tile ahead
   float4 nf0 = make_float4(0.f, 0.f, 0.f, 0.f), nf1 = nf0, nx = nf0;
@@ -341,7 +347,11 @@ __global__ void __launch_bounds__(kTcThreads, 4) k_mlp_infer_tc(const float* __r
   if (warp == 0) {
     asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(sm.tmem), "r"(kTmemCols) : "memory");
   }
-  if (tid == 0 && (sm.failed[0] | sm.failed[1]) && err) atomicOr(err, PBF_DEVERR_MMA_TIMEOUT);
+  if (tid == 0 && err) {
+    uint32_t f = 0;
+    for (int g = 0; g < kTcPipes; ++g) f |= sm.failed[g];
+    if (f) atomicOr(err, PBF_DEVERR_MMA_TIMEOUT);
+  }
 }
 
 
@@ -657,10 +667,9 @@ __global__ void __launch_bounds__(128, 1) k_mlp_grad_tc(const float* __restrict_
 }
 }  // namespace
 
-// No dynamic shared memory: the static tile buffers (about 55 KB per CTA) and
-// the 64-register cap of __launch_bounds__(256, 4) each keep an SM at four
-// CTAs, whose 4 x 128 TMEM columns are the SM's 512.
-constexpr int kTcPadSmem = 0;
+// The tile buffers of the eight pipelines and the weights (about 175 KB) in
+// dynamic shared memory; one CTA per SM holds all 512 TMEM columns.
+constexpr int kTcSmem = (int)sizeof(TcSmem);
 
 cudaError_t launch_mlp_infer_tc(const float* d_params, const pbf_mlp& model, const float* d_feat, uint32_t rows,
                                 float* d_lambda, float* d_lam_sum, cudaStream_t st, const float4* d_xs, float4* d_xl,
@@ -671,16 +680,14 @@ cudaError_t launch_mlp_infer_tc(const float* d_params, const pbf_mlp& model, con
     int dev = 0;
     cudaError_t e = cudaGetDevice(&dev);
     if (e == cudaSuccess) e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-    // static + dynamic shared memory above the 48 KB default needs the opt-in
+    // dynamic shared memory above the 48 KB default needs the opt-in
     if (e == cudaSuccess)
-      e = cudaFuncSetAttribute(k_mlp_infer_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, kTcPadSmem);
-    // the whole L1/shared array as shared memory, so four CTAs fit
+      e = cudaFuncSetAttribute(k_mlp_infer_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, kTcSmem);
     if (e == cudaSuccess)
       e = cudaFuncSetAttribute(k_mlp_infer_tc, cudaFuncAttributePreferredSharedMemoryCarveout,
                                (int)cudaSharedmemCarveoutMaxShared);
-    // four CTAs per SM: the TMEM limit (4 x 128 of 512 columns), which the
-    // shared memory and the register cap also enforce
-    per_sm = 4;
+    // one CTA per SM: it allocates all 512 TMEM columns
+    per_sm = 1;
     if (e != cudaSuccess) {
       sms = 0;
       return e;
@@ -693,10 +700,11 @@ cudaError_t launch_mlp_infer_tc(const float* d_params, const pbf_mlp& model, con
   }
   nm.lam_scale = model.lam_scale;
   const uint32_t tiles = (rows + kTcRows - 1) / kTcRows;
-  // one resident wave, two tile pipelines per CTA
-  const uint32_t grid = std::min<uint32_t>((tiles + 1) / 2, (uint32_t)sms * (uint32_t)per_sm);
-  k_mlp_infer_tc<<<grid, kTcThreads, kTcPadSmem, st>>>(d_params, nm, d_feat, rows, d_lambda, d_lam_sum, d_xs, d_xl,
-                                                       d_err);
+  // one resident wave, kTcPipes tile pipelines per CTA
+  const uint32_t grid =
+      std::min<uint32_t>((tiles + kTcPipes - 1) / kTcPipes, (uint32_t)sms * (uint32_t)per_sm);
+  k_mlp_infer_tc<<<grid, kTcThreads, kTcSmem, st>>>(d_params, nm, d_feat, rows, d_lambda, d_lam_sum, d_xs, d_xl,
+                                                    d_err);
   return cudaGetLastError();
 }
 

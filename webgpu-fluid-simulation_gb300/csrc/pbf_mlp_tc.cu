@@ -369,7 +369,8 @@ __global__ void __launch_bounds__(kTcThreads, 1) k_mlp_infer_tc(const float* __r
 // The weight and bias gradients are products over the tile's rows: their A
 // operands are the transposed activations H1^T, X^T, H2^T (M = 128: the
 // hidden / input units, then one row of ones that turns the same product
-// into the bias gradient, then zeros) and their B operands dZ2^T, dZ1^T and
+// into the bias gradient; the rows past it are never written, as the
+// accumulator rows they feed are never read) and their B operands dZ2^T, dZ1^T and
 // dy (N x K = rows), each written by its row's thread into column t of a
 // K-major tile.  dy is split into bf16 hi / lo rows, so dw3 and db3 keep
 // about 2^-16 relative accuracy; the other products take their operands in
@@ -381,12 +382,12 @@ constexpr uint32_t kColZ1 = 0, kColZ2 = 64, kColY = 128, kColDH1 = 160, kColG1 =
 struct GrSmem {
   alignas(128) uint8_t x1[128 * 16 * 2];    // X rows (K = 16: 8 features, ones at 8, 9)
   alignas(128) uint8_t hA[128 * 64 * 2];    // H1 rows, then H2 rows, then dZ2 rows
-  alignas(128) uint8_t tH1[128 * 128 * 2];  // A of [dW2; db2]: H1^T, ones (row 64), zeros
-  alignas(128) uint8_t tX[128 * 128 * 2];   // A of [dW1; db1]: X^T, ones (row 8), zeros
-  alignas(128) uint8_t tH2[128 * 128 * 2];  // A of [dw3; db3]: H2^T, ones (row 64), zeros
+  alignas(128) uint8_t tH1[128 * 128 * 2];  // A of [dW2; db2]: H1^T, ones (row 64); rows 65+ unused
+  alignas(128) uint8_t tX[128 * 128 * 2];   // A of [dW1; db1]: X^T, ones (row 8); rows 9+ unused
+  alignas(128) uint8_t tH2[128 * 128 * 2];  // A of [dw3; db3]: H2^T, ones (row 64); rows 65+ unused
   alignas(128) uint8_t tDZ2[64 * 128 * 2];  // B: dZ2^T (N = 64 x K = rows)
   alignas(128) uint8_t tDZ1[64 * 128 * 2];  // B: dZ1^T
-  alignas(128) uint8_t tDY[16 * 128 * 2];   // B: dy hi (N row 0), lo (row 1), zeros
+  alignas(128) uint8_t tDY[16 * 128 * 2];   // B: dy hi (N row 0), lo (row 1); rows 2+ unused
   alignas(128) uint8_t b1[64 * 16 * 2];     // W1'^T with b1 hi / lo in K rows 8, 9
   alignas(128) uint8_t b2[64 * 64 * 2];     // W2^T (N = out, K = in)
   alignas(128) uint8_t b2b[64 * 16 * 2];    // b2 hi / lo in K rows 8, 9
@@ -463,20 +464,18 @@ __global__ void __launch_bounds__(128, 1) k_mlp_grad_tc(const float* __restrict_
     *reinterpret_cast<__nv_bfloat16*>(sm.b3b + canon(n, k, 16)) =
         (n == 0 && k == 8) ? bf_hi(b) : (n == 0 && k == 9) ? bf_lo(b) : z16;
   }
-  // constant parts of the gradient operands: the ones rows and the zeros
-  // (the data rows are rewritten for every tile)
-  // 16 bytes at a time: the 16-byte unit at byte o of a canonical tile
-  // holds elements k..k+7 of row m = ((o / 2048) * 8 + (o / 16) % 8)
-  // (kk = 128: 16 core matrices of 128 B per 8-row group)
-  const uint32_t ones2 = pack_bf16(1.0f, 1.0f);
-  for (uint32_t o = 16u * tid; o < 128u * 128u * 2u; o += 16u * 128u) {
-    const uint32_t m = (o / 2048u) * 8u + (o / 16u) % 8u;
-    const uint32_t h = m == 64u ? ones2 : 0u, xv = m == 8u ? ones2 : 0u;
-    st_shared_v4(smem_u32(sm.tH1 + o), h, h, h, h);
-    st_shared_v4(smem_u32(sm.tH2 + o), h, h, h, h);
-    st_shared_v4(smem_u32(sm.tX + o), xv, xv, xv, xv);
+  // constant parts of the gradient operands: the ones rows (row 64 of H1^T
+  // and H2^T, row 8 of X^T) that turn the products into bias gradients.
+  // The data rows are rewritten for every tile.  The rows below them (and
+  // dy's rows 2..15) are not written: they only reach accumulator rows
+  // (columns of [dw3; db3]) that are never read.  Thread t writes the
+  // 16-byte unit of elements k = 8 (t % 16) .. + 7 of one ones row.
+  if (tid < 48u) {
+    const uint32_t ones2 = pack_bf16(1.0f, 1.0f);
+    uint8_t* tile = tid < 16u ? sm.tH1 : tid < 32u ? sm.tH2 : sm.tX;
+    const uint32_t m = tid < 32u ? 64u : 8u, k = 8u * (tid % 16u);
+    st_shared_v4(smem_u32(tile + canon(m, k, 128)), ones2, ones2, ones2, ones2);
   }
-  for (uint32_t o = 16u * tid; o < 16u * 128u * 2u; o += 16u * 128u) st_shared_v4(smem_u32(sm.tDY + o), 0u, 0u, 0u, 0u);
   if (tid < 64u) sm.w3[tid] = P[OFF_W3 + tid];
   st_shared_v4(smem_u32(sm.x1 + canon(row, 8, 16)), pack_bf16(1.0f, 1.0f), 0u, 0u, 0u);
   const uint32_t mbar = smem_u32(&sm.mbar);

@@ -46,11 +46,12 @@ def test_mlp_forward_matches_fp64_reference():
     assert np.abs(got - exact).max() <= 3e-2 * scl        # against full FP64 (bf16 quantisation)
 
 
-@pytest.mark.parametrize("rows", [1, 127, 128, 129, 5000])
+@pytest.mark.parametrize("rows", [1, 127, 128, 129, 5000, 300001])
 def test_mlp_forward_tcgen05_matches_mma_sync_and_fp64(rows):
     """The tensor-core (tcgen05.mma, TMEM) inference kernel against the
     mma.sync kernel and the FP64 reference with the same bf16 rounding
-    points; ragged last tiles included."""
+    points; ragged last tiles included, and (300,001 rows: 2,344 tiles over
+    152 x 8 pipelines) pipelines that walk several tiles."""
     m, feat, _ = random_model(11, rows=max(rows, 2))
     feat = feat[:rows]
     tc = mlp_forward(m, feat, kernel=L.MLP_KERNEL_TCGEN05)

@@ -54,6 +54,10 @@ struct pbf_handle {
   bool own_stream = false;
   // asynchronous position reads: their stream, events and the staging copy
   cudaStream_t copy_stream = nullptr;
+  // the learned start's boundary sampling at x*_0 beside the neighbour build
+  // (fast mode, tcgen05 network): its stream and the fork / join events
+  cudaStream_t side_stream = nullptr;
+  cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
   cudaEvent_t ev_frame = nullptr, ev_staged = nullptr;
   DBuf<float4> staging;
   std::string err;
@@ -444,13 +448,15 @@ int substep(pbf_handle* h, cudaEvent_t* ev) {
   };
   // Boundary sampling at x*_a (bsdf: also the SDF feature); guard: the
   // lagged iteration control's flag (the sampling is skipped with it).
-  auto sample_boundary = [&](int a, float* bsdf, const int* guard = nullptr) -> cudaError_t {
+  auto sample_boundary = [&](int a, float* bsdf, const int* guard = nullptr,
+                             cudaStream_t on = nullptr) -> cudaError_t {
     KScope ks(h, K_BOUNDARY);
+    cudaStream_t sst = on ? on : st;
     if (band < 0) {
-      ps.band<<<grid_of(h, n), h->blk, 0, st>>>(p, h->tab, h->xs[a].p, band_args(0, bsdf));
+      ps.band<<<grid_of(h, n), h->blk, 0, sst>>>(p, h->tab, h->xs[a].p, band_args(0, bsdf));
       band = 0;
     }
-    ps.boundary_band<<<band_grid, 256, 0, st>>>(p, f, h->sdf.p, h->vol.p, FieldBlocks{h->bcell.p, h->bnodes.p},
+    ps.boundary_band<<<band_grid, 256, 0, sst>>>(p, f, h->sdf.p, h->vol.p, FieldBlocks{h->bcell.p, h->bnodes.p},
                                                  h->tab, h->xs[a].p, h->bdata.p, bsdf,
                                                  h->band_list[band].p, h->band_count.p + band,
                                                  h->band_count.p + (1 - band), guard);
@@ -459,12 +465,25 @@ int substep(pbf_handle* h, cudaEvent_t* ev) {
   // NeighborCount + NeighborList in one pass (fixed per-particle slices: no
   // scan).  The learned start samples the boundary at x*_0 first and sums its
   // features in the same traversal.
+  // Fast mode with the tcgen05 network: the boundary sampling at x*_0 runs on
+  // the side stream beside the neighbour build, and the network pass adds
+  // the features' boundary terms (LateBoundary).
+  const bool late = h->learned && f.loaded && !cb && !h->ktiming && h->side_stream &&
+                    h->mlp_kernel == PBF_MLP_KERNEL_TCGEN05 && h->cfg.fp_mode == PBF_FP_FAST;
   if (h->learned) {
-    if (f.loaded) CU(h, sample_boundary(0, h->bsdf.p));
+    if (late) {
+      CU(h, cudaEventRecord(h->ev_fork, st));
+      CU(h, cudaStreamWaitEvent(h->side_stream, h->ev_fork, 0));
+      CU(h, sample_boundary(0, h->bsdf.p, nullptr, h->side_stream));
+      CU(h, cudaEventRecord(h->ev_join, h->side_stream));
+    } else if (f.loaded) {
+      CU(h, sample_boundary(0, h->bsdf.p));
+    }
     SolverAux al{};
     al.pos = h->pos[cc].p;
     al.lam_prev = h->lam_prev.p;
-    al.bsdf = f.loaded ? h->bsdf.p : nullptr;
+    al.bsdf = (f.loaded && !late) ? h->bsdf.p : nullptr;
+    al.late_boundary = late ? 1 : 0;
     al.substep_index = sub_index;
     al.feat = h->feat.p;
     KScope ks(h, K_FEATURES);
@@ -473,8 +492,8 @@ int substep(pbf_handle* h, cudaEvent_t* ev) {
           p, A, h->cb_mask.p, h->cb_ovf.p, h->nbr_count.p, f.loaded, h->bdata.p, al);
     else
       ps.nbr_build_feat<<<grid_of(h, n), h->blk, 0, st>>>(p, g, h->xs[0].p, h->cell_start.p, ms, h->nbr_list.p,
-                                                           h->nbr_count.p, h->nbr_max.p, h->err_word.p, f.loaded,
-                                                           h->bdata.p, al);
+                                                           h->nbr_count.p, h->nbr_max.p, h->err_word.p,
+                                                           (f.loaded && !late) ? 1 : 0, h->bdata.p, al);
   } else if (cb) {
     // the mask variant's search; the list-free variant has none (the
     // density pass counts the neighbours)
@@ -594,9 +613,14 @@ int substep(pbf_handle* h, cudaEvent_t* ev) {
     // reads as its (x*, lambda) records and the fallback keeps as x*_0.
     {
       KScope ks(h, K_MLP);
+      LateBoundary lb{};
+      if (late) {
+        CU(h, cudaStreamWaitEvent(st, h->ev_join, 0));  // the side stream's boundary sampling
+        lb = LateBoundary{h->bdata.p, h->bsdf.p, p.h, p.h2, p.poly6, p.V};
+      }
       if (h->mlp_kernel == PBF_MLP_KERNEL_TCGEN05)
         CU(h, launch_mlp_infer_tc(h->mlp_params.p, h->model, (const float*)h->feat.p, n, nullptr, h->lam_sum.p, st,
-                                  h->xs[0].p, h->xs_save.p, h->err_word.p));
+                                  h->xs[0].p, h->xs_save.p, h->err_word.p, lb));
       else
         CU(h, launch_mlp_infer(h->mlp_params.p, h->model, (const float*)h->feat.p, n, nullptr, h->lam_sum.p, st,
                                h->xs[0].p, h->xs_save.p));
@@ -1218,6 +1242,12 @@ int pbf_destroy(pbf_handle* h) {
     cudaEventDestroy(h->ev_frame);
     cudaEventDestroy(h->ev_staged);
   }
+  if (h->side_stream) {
+    cudaStreamSynchronize(h->side_stream);
+    cudaStreamDestroy(h->side_stream);
+    cudaEventDestroy(h->ev_fork);
+    cudaEventDestroy(h->ev_join);
+  }
   h->staging.release();
   release_all(h);
   for (int i = 0; i < 5; ++i)
@@ -1784,6 +1814,11 @@ int pbf_set_learned(pbf_handle* h, const pbf_mlp* model, uint32_t iterations, fl
     CU(h, cudaMemsetAsync(h->fb_flag.p, 0, 2 * sizeof(int), h->stream));
     CU(h, cudaMemsetAsync(h->fb_count.p, 0, 3 * sizeof(uint32_t), h->stream));
     CU(h, cudaMemsetAsync(h->fb_mean.p, 0, 2 * sizeof(float), h->stream));
+  }
+  if (!h->side_stream) {
+    CU(h, cudaStreamCreateWithFlags(&h->side_stream, cudaStreamNonBlocking));
+    CU(h, cudaEventCreateWithFlags(&h->ev_fork, cudaEventDisableTiming));
+    CU(h, cudaEventCreateWithFlags(&h->ev_join, cudaEventDisableTiming));
   }
   h->model = *model;
   CU(h, cudaMemcpyAsync(h->mlp_params.p, model->params, sizeof(model->params), cudaMemcpyHostToDevice, h->stream));

@@ -190,7 +190,7 @@ cudaError_t launch_mlp_infer(const float* d_params, const pbf_mlp& model, const 
 // bounded completion wait gives up.
 cudaError_t launch_mlp_infer_tc(const float* d_params, const pbf_mlp& model, const float* d_feat, uint32_t rows,
                                 float* d_lambda, float* d_lam_sum, cudaStream_t st, const float4* d_xs,
-                                float4* d_xl, uint32_t* d_err);
+                                float4* d_xl, uint32_t* d_err, LateBoundary lb = LateBoundary{});
 // Forward + backward on tcgen05.mma (pbf_mlp_tc.cu): the gradient accumulates
 // into d_grad (atomically), the summed squared error into d_loss; d_err
 // receives PBF_DEVERR_MMA_TIMEOUT when a bounded completion wait gives up.

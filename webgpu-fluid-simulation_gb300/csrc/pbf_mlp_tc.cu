@@ -172,7 +172,7 @@ __global__ void __launch_bounds__(kTcThreads, 1) k_mlp_infer_tc(const float* __r
                                                             const float* __restrict__ feat, uint32_t rows,
                                                             float* __restrict__ lambda, float* __restrict__ lam_sum,
                                                             const float4* __restrict__ xs, float4* __restrict__ xl,
-                                                            uint32_t* err) {
+                                                            uint32_t* err, LateBoundary lb) {
   extern __shared__ __align__(128) uint8_t tc_raw[];
   TcSmem& sm = *reinterpret_cast<TcSmem*>(tc_raw);
   const uint32_t tid = threadIdx.x, warp = tid >> 5, row = tid & 127u, wg = tid >> 7;
@@ -236,13 +236,18 @@ __global__ void __launch_bounds__(kTcThreads, 1) k_mlp_infer_tc(const float* __r
   const uint32_t first = (uint32_t)kTcPipes * blockIdx.x + wg, step = (uint32_t)kTcPipes * gridDim.x;
   // the next tile's feature row (and x* when the output is packed), loaded
   // one tile ahead
-  float4 nf0 = make_float4(0.f, 0.f, 0.f, 0.f), nf1 = nf0, nx = nf0;
+  float4 nf0 = make_float4(0.f, 0.f, 0.f, 0.f), nf1 = nf0, nx = nf0, nb = nf0;
+  float nsd = 0.0f;
   auto fetch = [&](uint32_t tile) {
     const uint32_t rr = tile * kTcRows + row;
     if (tile < tiles && rr < rows) {
       nf0 = reinterpret_cast<const float4*>(feat)[2 * (size_t)rr];
       nf1 = reinterpret_cast<const float4*>(feat)[2 * (size_t)rr + 1];
       if (xl) nx = xs[rr];
+      if (lb.bdata) {
+        nb = lb.bdata[rr];
+        nsd = lb.bsdf[rr];
+      }
     }
   };
   fetch(first);
@@ -253,7 +258,19 @@ __global__ void __launch_bounds__(kTcThreads, 1) k_mlp_infer_tc(const float* __r
     {
       float x[8];
       if (valid) {
-        const float f[8] = {nf0.x, nf0.y, nf0.z, nf0.w, nf1.x, nf1.y, nf1.z, nf1.w};
+        float f[8] = {nf0.x, nf0.y, nf0.z, nf0.w, nf1.x, nf1.y, nf1.z, nf1.w};
+        if (lb.bdata) {  // the boundary terms of features 0, 5 and 6 (LateBoundary)
+          float dens = f[0];
+          if (nb.w != 0.0f) {
+            const float dx = nx.x - nb.x, dy = nx.y - nb.y, dz = nx.z - nb.z;
+            const float r2 = dx * dx + dy * dy + dz * dz;
+            const float t = lb.h2 - r2;
+            dens = dens + nb.w * ((r2 <= lb.h2) ? lb.poly6 * (t * t * t) : 0.0f);
+          }
+          f[0] = dens - 1.0f;
+          f[5] = fminf(nsd, 2.0f * lb.h) / lb.h;
+          f[6] = nb.w / lb.V;
+        }
 #pragma unroll
         for (int k = 0; k < 8; ++k) x[k] = (f[k] - nm.mean[k]) * nm.inv_std[k];
       } else {
@@ -672,7 +689,7 @@ constexpr int kTcSmem = (int)sizeof(TcSmem);
 
 cudaError_t launch_mlp_infer_tc(const float* d_params, const pbf_mlp& model, const float* d_feat, uint32_t rows,
                                 float* d_lambda, float* d_lam_sum, cudaStream_t st, const float4* d_xs, float4* d_xl,
-                                uint32_t* d_err) {
+                                uint32_t* d_err, LateBoundary lb) {
   if (rows == 0) return cudaSuccess;
   static int sms = 0, per_sm = 0;
   if (sms == 0) {
@@ -703,7 +720,7 @@ cudaError_t launch_mlp_infer_tc(const float* d_params, const pbf_mlp& model, con
   const uint32_t grid =
       std::min<uint32_t>((tiles + kTcPipes - 1) / kTcPipes, (uint32_t)sms * (uint32_t)per_sm);
   k_mlp_infer_tc<<<grid, kTcThreads, kTcSmem, st>>>(d_params, nm, d_feat, rows, d_lambda, d_lam_sum, d_xs, d_xl,
-                                                    d_err);
+                                                    d_err, lb);
   return cudaGetLastError();
 }
 

@@ -96,6 +96,18 @@ struct SceneTab {
   const uint16_t* slot_scene;
 };
 
+// The boundary terms of the learned start's features, added by the network
+// pass instead of the neighbour build (so the boundary sampling at x*_0 can
+// run beside the build): the build writes the fluid density in feature 0
+// and the network pass adds V_b W(x*_0 - x_b), then writes feature 0 =
+// rho - 1, feature 5 = min(SDF, 2h) / h and feature 6 = V_b / V, with the
+// build's own arithmetic (fast mode).
+struct LateBoundary {
+  const float4* bdata;  // null: the features are complete
+  const float* bsdf;
+  float h, h2, poly6, V;
+};
+
 // Input normalisation of the learned start's network.
 struct MLPNorm {
   float mean[8];
@@ -114,6 +126,7 @@ struct SolverAux {
   const float4* pos;         // lambda pass (features): x before the predict step
   const float* lam_prev;     // lambda pass (features): previous substep's multiplier
   SolveStats* stats;         // lambda pass: compression statistics
+  int late_boundary;         // learned start's build: feature 0 = fluid density, 5 and 6 left to the network pass
   float substep_index;       // lambda pass (features)
   const float* mlp;          // lambda pass (network): flat FP32 parameters
   MLPNorm norm;              // lambda pass (network)

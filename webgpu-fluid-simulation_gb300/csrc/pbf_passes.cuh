@@ -230,7 +230,9 @@ __global__ void __launch_bounds__(256) k_nbr_build(SimParams p, GridParams g0, S
 // the fluid density at x*_0 over the neighbours it finds (poly6 from the
 // squared distance the test already has: a few FMAs per hit) and writes the
 // start's feature rows (a.feat, the layout the lambda pass records for
-// training).  Needs the boundary sampling at x*_0 first (bdata, a.bsdf).
+// training).  Needs the boundary sampling at x*_0 first (bdata, a.bsdf),
+// unless a.late_boundary leaves the boundary terms to the network pass
+// (have_field = 0, a.bsdf = null: the sampling may then run concurrently).
 template <bool kLoop>
 __global__ void __launch_bounds__(256) k_nbr_build_feat(SimParams p, GridParams g, const float4* __restrict__ xs,
                                                         const uint32_t* __restrict__ cell_start, uint32_t max_nbr,
@@ -281,9 +283,15 @@ __global__ void __launch_bounds__(256) k_nbr_build_feat(SimParams p, GridParams 
       const float4 xo = a.pos[t];
       const f3 vi = p.inv_dt * (xi - xyz(xo));
       float sd = a.bsdf ? fminf(a.bsdf[t], 2.0f * p.h) : 2.0f * p.h;
-      a.feat[2 * t] = make_float4(dens - 1.0f, a.lam_prev ? a.lam_prev[t] : 0.0f, (float)min(q, max_nbr),
+      float f0 = dens - 1.0f, f5 = sd / p.h, f6 = vb / p.V;
+      if (a.late_boundary) {  // the network pass adds the boundary terms (LateBoundary)
+        f0 = dens_fluid;
+        f5 = 0.0f;
+        f6 = 0.0f;
+      }
+      a.feat[2 * t] = make_float4(f0, a.lam_prev ? a.lam_prev[t] : 0.0f, (float)min(q, max_nbr),
                                   len3(vi) * p.dt / p.h);
-      a.feat[2 * t + 1] = make_float4(divergence_feature(p, xo, dens_fluid), sd / p.h, vb / p.V, a.substep_index);
+      a.feat[2 * t + 1] = make_float4(divergence_feature(p, xo, dens_fluid), f5, f6, a.substep_index);
     }
   }
 }

@@ -463,11 +463,10 @@ int substep(pbf_handle* h, cudaEvent_t* ev) {
     return cudaGetLastError();
   };
   // NeighborCount + NeighborList in one pass (fixed per-particle slices: no
-  // scan).  The learned start samples the boundary at x*_0 first and sums its
-  // features in the same traversal.
-  // Fast mode with the tcgen05 network: the boundary sampling at x*_0 runs on
-  // the side stream beside the neighbour build, and the network pass adds
-  // the features' boundary terms (LateBoundary).
+  // scan).  The learned start sums its features in the same traversal; their
+  // boundary terms need the boundary sampling at x*_0, which runs before the
+  // build, or (fast mode, tcgen05 network) on the side stream beside it, the
+  // network pass then adding those terms (LateBoundary).
   const bool late = h->learned && f.loaded && !cb && !h->ktiming && h->side_stream &&
                     h->mlp_kernel == PBF_MLP_KERNEL_TCGEN05 && h->cfg.fp_mode == PBF_FP_FAST;
   if (h->learned) {

@@ -469,6 +469,16 @@ int substep(pbf_handle* h, cudaEvent_t* ev) {
   // network pass then adding those terms (LateBoundary).
   const bool late = h->learned && f.loaded && !cb && !h->ktiming && h->side_stream &&
                     h->mlp_kernel == PBF_MLP_KERNEL_TCGEN05 && h->cfg.fp_mode == PBF_FP_FAST;
+  // The plain solve's first boundary sampling (at x*_0) likewise runs on the
+  // side stream beside the build; the first iteration waits for it.
+  const bool pre_sampled = !h->learned && f.loaded && !cb && !h->ktiming && !h->batch && h->side_stream &&
+                           h->cfg.options.iterations > 0;
+  if (pre_sampled) {
+    CU(h, cudaEventRecord(h->ev_fork, st));
+    CU(h, cudaStreamWaitEvent(h->side_stream, h->ev_fork, 0));
+    CU(h, sample_boundary(0, need_feat ? h->bsdf.p : nullptr, nullptr, h->side_stream));
+    CU(h, cudaEventRecord(h->ev_join, h->side_stream));
+  }
   if (h->learned) {
     if (late) {
       CU(h, cudaEventRecord(h->ev_fork, st));
@@ -536,7 +546,13 @@ int substep(pbf_handle* h, cudaEvent_t* ev) {
     }
     for (uint32_t it = 0; it < iters; ++it) {
       float* bsdf_it = (need_feat && feat_first && it == 0) ? h->bsdf.p : nullptr;
-      if (f.loaded && sample_boundary(a, bsdf_it, lag) != cudaSuccess) {
+      if (pre_sampled && it == 0 && !h->learned) {
+        // sampled on the side stream beside the build
+        if (cudaStreamWaitEvent(st, h->ev_join, 0) != cudaSuccess) {
+          *rc = PBF_ECUDA;
+          return a;
+        }
+      } else if (f.loaded && sample_boundary(a, bsdf_it, lag) != cudaSuccess) {
         *rc = PBF_ECUDA;
         return a;
       }
@@ -1213,6 +1229,9 @@ int pbf_create(const pbf_config* cfg, pbf_handle** out) {
   if (sb2 > sb) sb = sb2;
   A(cudaMalloc(&h->scan_scratch, sb));
   for (int i = 0; i < 5; ++i) A(cudaEventCreate(&h->ev[i]));
+  A(cudaStreamCreateWithFlags(&h->side_stream, cudaStreamNonBlocking));
+  A(cudaEventCreateWithFlags(&h->ev_fork, cudaEventDisableTiming));
+  A(cudaEventCreateWithFlags(&h->ev_join, cudaEventDisableTiming));
   if (e == cudaSuccess) {
     A(cudaMemsetAsync(h->nbr_max.p, 0, sizeof(uint32_t), h->stream));
     A(cudaMemsetAsync(h->err_word.p, 0, sizeof(uint32_t), h->stream));
@@ -1222,6 +1241,9 @@ int pbf_create(const pbf_config* cfg, pbf_handle** out) {
   }
   if (e != cudaSuccess) {
     release_all(h);
+    if (h->side_stream) cudaStreamDestroy(h->side_stream);
+    if (h->ev_fork) cudaEventDestroy(h->ev_fork);
+    if (h->ev_join) cudaEventDestroy(h->ev_join);
     if (h->own_stream && h->stream) cudaStreamDestroy(h->stream);
     for (int i = 0; i < 5; ++i)
       if (h->ev[i]) cudaEventDestroy(h->ev[i]);
@@ -1244,9 +1266,9 @@ int pbf_destroy(pbf_handle* h) {
   if (h->side_stream) {
     cudaStreamSynchronize(h->side_stream);
     cudaStreamDestroy(h->side_stream);
-    cudaEventDestroy(h->ev_fork);
-    cudaEventDestroy(h->ev_join);
   }
+  if (h->ev_fork) cudaEventDestroy(h->ev_fork);
+  if (h->ev_join) cudaEventDestroy(h->ev_join);
   h->staging.release();
   release_all(h);
   for (int i = 0; i < 5; ++i)

@@ -413,17 +413,20 @@ int substep(pbf_handle* h, cudaEvent_t* ev) {
     KScope ks(h, K_SORT);
     CU(h, launch_sort_by_cell(g, n, h->ids[c].p, sb, h->id_bits, st));
   }
+  // the learned start's and trace capture's features: the previous multiplier
+  // sum is gathered with the state
+  const bool need_feat = h->learned || h->trace_cap > 0;
   {
     KScope ks(h, K_GATHER);
     if (cb)
       CU(h, launch_gather_state_cb(n, h->perm.p, h->pos[c].p, h->xs[1].p, h->ids[c].p, h->key.p, h->pos[nx].p,
-                                   h->xs[0].p, h->ids[nx].p, h->skey.p, h->xs0.p, st));
+                                   h->xs[0].p, h->ids[nx].p, h->skey.p, h->xs0.p, st,
+                                   need_feat ? h->lam_sum.p : nullptr, need_feat ? h->lam_prev.p : nullptr));
     else
       CU(h, launch_gather_state(n, h->perm.p, h->pos[c].p, h->xs[1].p, h->ids[c].p, h->pos[nx].p, h->xs[0].p,
-                                h->ids[nx].p, st));
+                                h->ids[nx].p, st, need_feat ? h->lam_sum.p : nullptr,
+                                need_feat ? h->lam_prev.p : nullptr));
   }
-  const bool need_feat = h->learned || h->trace_cap > 0;
-  if (need_feat) CU(h, launch_gather_f32(n, h->perm.p, h->lam_sum.p, h->lam_prev.p, st));
   h->cur = nx;
   const int cc = nx;
   const FieldParams f = h->fp;

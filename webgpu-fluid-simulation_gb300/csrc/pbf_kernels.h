@@ -143,15 +143,18 @@ cudaError_t launch_rank_sorted(uint32_t n, const uint32_t* skeys, const uint32_t
 // scatter + stable within-cell order + (optionally) gather of the particle state.
 cudaError_t launch_sort_by_cell(GridParams g, uint32_t n, const uint32_t* ids, SortBuffers& b, uint32_t id_bits,
                                 cudaStream_t st);
+// f_in / f_out (optional): one scalar per particle gathered along (the
+// learned start's previous multiplier sum).
 cudaError_t launch_gather_state(uint32_t n, const uint32_t* perm, const float4* pos_in, const float4* xs_in,
                                 const uint32_t* id_in, float4* pos_out, float4* xs_out, uint32_t* id_out,
-                                cudaStream_t st);
+                                cudaStream_t st, const float* f_in = nullptr, float* f_out = nullptr);
 // The same gather that also writes, for the cell-block passes, the cell key
 // of each sorted slot (skey_out[t] = key_in[perm[t]]) and a second copy of
 // the predicted positions x*_0 (xs0_out) that the solve leaves untouched.
 cudaError_t launch_gather_state_cb(uint32_t n, const uint32_t* perm, const float4* pos_in, const float4* xs_in,
                                    const uint32_t* id_in, const uint32_t* key_in, float4* pos_out, float4* xs_out,
-                                   uint32_t* id_out, uint32_t* skey_out, float4* xs0_out, cudaStream_t st);
+                                   uint32_t* id_out, uint32_t* skey_out, float4* xs0_out, cudaStream_t st,
+                                   const float* f_in = nullptr, float* f_out = nullptr);
 cudaError_t launch_scatter_by_id(uint32_t n, const uint32_t* id, const float4* src, float4* dst, cudaStream_t st);
 // dst[id[t]] = src[t].w (a scalar kept in the w lane of a packed float4 array)
 cudaError_t launch_scatter_w_by_id(uint32_t n, const uint32_t* id, const float4* src, float* dst, cudaStream_t st);
@@ -199,7 +202,6 @@ cudaError_t launch_mlp_grad_tc(const float* d_params, const pbf_mlp& model, cons
                                cudaStream_t st);
 cudaError_t launch_mlp_grad(const float* d_params, const pbf_mlp& model, const float* d_feat, const float* d_target,
                             uint32_t rows, float* d_grad, float* d_loss, cudaStream_t st);
-cudaError_t launch_gather_f32(uint32_t n, const uint32_t* perm, const float* src, float* dst, cudaStream_t st);
 cudaError_t launch_fallback_decide(SolveStats* stats, float bound, int* flag, uint32_t* fallbacks, float* last_mean,
                                    cudaStream_t st);
 // Lagged iteration control (counts[0] decisions, counts[1] substeps that iterated).

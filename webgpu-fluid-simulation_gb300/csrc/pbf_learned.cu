@@ -334,12 +334,6 @@ cudaError_t ensure_grad_kernel() {
 
 }  // namespace
 
-__global__ void k_gather_f32(uint32_t n, const uint32_t* __restrict__ perm, const float* __restrict__ src,
-                             float* __restrict__ dst) {
-  uint32_t t = blockIdx.x * blockDim.x + threadIdx.x;
-  if (t < n) dst[t] = src[perm[t]];
-}
-
 // Fallback decision from the last learned iteration's statistics; resets
 // them for the next substep.
 __global__ void k_fallback_decide(SolveStats* stats, float bound, int* flag, uint32_t* fallbacks, float* last_mean) {
@@ -418,11 +412,6 @@ __global__ void k_trace_append(uint32_t n, const uint32_t* __restrict__ ids, con
 }
 
 // ---- launch helpers used by the step driver -------------------------------------------
-cudaError_t launch_gather_f32(uint32_t n, const uint32_t* perm, const float* src, float* dst, cudaStream_t st) {
-  if (n == 0) return cudaSuccess;
-  k_gather_f32<<<(n + 255) / 256, 256, 0, st>>>(n, perm, src, dst);
-  return cudaGetLastError();
-}
 cudaError_t launch_fallback_decide(SolveStats* stats, float bound, int* flag, uint32_t* fallbacks, float* last_mean,
                                    cudaStream_t st) {
   k_fallback_decide<<<1, 1, 0, st>>>(stats, bound, flag, fallbacks, last_mean);

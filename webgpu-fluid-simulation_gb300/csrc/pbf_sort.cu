@@ -504,13 +504,15 @@ __global__ void __launch_bounds__(256) k_rank_sorted(uint32_t n, const uint32_t*
 __global__ void __launch_bounds__(256) k_gather(uint32_t n, const uint32_t* __restrict__ perm,
                                                 const float4* __restrict__ pos_in, const float4* __restrict__ xs_in,
                                                 const uint32_t* __restrict__ id_in, float4* __restrict__ pos_out,
-                                                float4* __restrict__ xs_out, uint32_t* __restrict__ id_out) {
+                                                float4* __restrict__ xs_out, uint32_t* __restrict__ id_out,
+                                                const float* __restrict__ f_in, float* __restrict__ f_out) {
   uint32_t t = blockIdx.x * blockDim.x + threadIdx.x;
   if (t >= n) return;
   uint32_t o = perm[t];
   pos_out[t] = __ldg(pos_in + o);
   xs_out[t] = __ldg(xs_in + o);
   id_out[t] = id_in ? __ldg(id_in + o) : o;  // no id array: the input order is the id order
+  if (f_in) f_out[t] = __ldg(f_in + o);
 }
 
 __global__ void __launch_bounds__(256) k_gather_cb(uint32_t n, const uint32_t* __restrict__ perm,
@@ -519,7 +521,8 @@ __global__ void __launch_bounds__(256) k_gather_cb(uint32_t n, const uint32_t* _
                                                    const uint32_t* __restrict__ id_in,
                                                    const uint32_t* __restrict__ key_in, float4* __restrict__ pos_out,
                                                    float4* __restrict__ xs_out, uint32_t* __restrict__ id_out,
-                                                   uint32_t* __restrict__ skey_out, float4* __restrict__ xs0_out) {
+                                                   uint32_t* __restrict__ skey_out, float4* __restrict__ xs0_out,
+                                                   const float* __restrict__ f_in, float* __restrict__ f_out) {
   uint32_t t = blockIdx.x * blockDim.x + threadIdx.x;
   if (t >= n) return;
   uint32_t o = perm[t];
@@ -529,6 +532,7 @@ __global__ void __launch_bounds__(256) k_gather_cb(uint32_t n, const uint32_t* _
   xs0_out[t] = x;
   skey_out[t] = __ldg(key_in + o);
   id_out[t] = id_in ? __ldg(id_in + o) : o;
+  if (f_in) f_out[t] = __ldg(f_in + o);
 }
 
 __global__ void k_scatter_f4(uint32_t n, const uint32_t* __restrict__ id, const float4* __restrict__ src,
@@ -786,18 +790,19 @@ cudaError_t launch_sort_by_cell(GridParams g, uint32_t n, const uint32_t* ids, S
 
 cudaError_t launch_gather_state(uint32_t n, const uint32_t* perm, const float4* pos_in, const float4* xs_in,
                                 const uint32_t* id_in, float4* pos_out, float4* xs_out, uint32_t* id_out,
-                                cudaStream_t st) {
+                                cudaStream_t st, const float* f_in, float* f_out) {
   if (n == 0) return cudaSuccess;
-  k_gather<<<blocks_for(n, 256), 256, 0, st>>>(n, perm, pos_in, xs_in, id_in, pos_out, xs_out, id_out);
+  k_gather<<<blocks_for(n, 256), 256, 0, st>>>(n, perm, pos_in, xs_in, id_in, pos_out, xs_out, id_out, f_in, f_out);
   return cudaGetLastError();
 }
 
 cudaError_t launch_gather_state_cb(uint32_t n, const uint32_t* perm, const float4* pos_in, const float4* xs_in,
                                    const uint32_t* id_in, const uint32_t* key_in, float4* pos_out, float4* xs_out,
-                                   uint32_t* id_out, uint32_t* skey_out, float4* xs0_out, cudaStream_t st) {
+                                   uint32_t* id_out, uint32_t* skey_out, float4* xs0_out, cudaStream_t st,
+                                   const float* f_in, float* f_out) {
   if (n == 0) return cudaSuccess;
   k_gather_cb<<<blocks_for(n, 256), 256, 0, st>>>(n, perm, pos_in, xs_in, id_in, key_in, pos_out, xs_out, id_out,
-                                                  skey_out, xs0_out);
+                                                  skey_out, xs0_out, f_in, f_out);
   return cudaGetLastError();
 }
 
